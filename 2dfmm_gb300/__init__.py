@@ -1,0 +1,230 @@
+"""Host-side Python view of libtree2d_gb300.so (the GB300 vortex-blob treecode).
+
+The product is the shared library with the C ABI declared in
+include/tree2d.h; this module binds it with ctypes and mirrors the
+reference's interface:
+
+    make_tree(vor_b, cir_b, cor_b)     ver-c/src/quadtree.c:102-171
+    biot_tree(x, y) -> (u, v)          ver-c/src/fmm.c:69-118
+
+plus the library's extensions (parameters, modes, batch evaluation,
+device-resident solves, tree export, statistics).  There is no fallback:
+if the library is missing or has no GPU, calls raise.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libtree2d_gb300.so")
+
+OK = 0
+ERR_PARAM_FILE, ERR_BAD_PARAMS, ERR_BAD_INPUT, ERR_TOO_DEEP, ERR_CUDA, ERR_NO_TREE, ERR_NO_DEVICE, ERR_TIMEOUT, \
+    ERR_MODE = range(1, 10)
+MODE_PLAIN, MODE_MIXED, MODE_LEARNED = 0, 1, 2
+
+# Every symbol include/tree2d.h declares.
+EXPORTS = [
+    "make_tree", "biot_tree", "tree2d_last_error", "tree2d_error_string", "tree2d_set_params",
+    "tree2d_clear_params", "tree2d_get_params", "tree2d_set_mode", "tree2d_get_mode", "biot_tree_batch",
+    "tree2d_solve_device", "tree2d_get_stats", "tree2d_export_tree", "tree2d_direct_device", "tree2d_fp64_probe", "tree2d_version",
+]
+
+
+class Tree2DError(RuntimeError):
+    def __init__(self, code: int, where: str = ""):
+        self.code = code
+        super().__init__(f"{where}: tree2d error {code}: {error_string(code)}")
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [
+        ("n_blobs", ctypes.c_longlong), ("n_cells", ctypes.c_longlong), ("n_leaves", ctypes.c_longlong),
+        ("depth", ctypes.c_int), ("mode", ctypes.c_int), ("n_m2s", ctypes.c_longlong),
+        ("n_pairs", ctypes.c_longlong), ("n_m2l", ctypes.c_longlong), ("ms_build", ctypes.c_double),
+        ("ms_upward", ctypes.c_double), ("ms_eval", ctypes.c_double), ("ms_total", ctypes.c_double),
+        ("n_launches", ctypes.c_longlong),
+    ]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+_dp = ctypes.POINTER(ctypes.c_double)
+_ip = ctypes.POINTER(ctypes.c_int)
+_lib = None
+
+
+def build(verbose: bool = False) -> str:
+    """Compiles the CUDA sources for sm_103a (see build.py)."""
+    from importlib import import_module
+    return import_module(__name__ + ".build").build(verbose=verbose)
+
+
+def load(path: str | None = None):
+    """Loads the library (raises if it is missing: there is no CPU fallback)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = path or LIB_PATH
+    if not os.path.exists(path):
+        raise RuntimeError(f"{path} is missing: build it first (python -c 'import __graft_entry__ as g; g.build()')")
+    L = ctypes.CDLL(path)
+    L.make_tree.argtypes = [ctypes.c_int, _dp, _dp, _dp]
+    L.make_tree.restype = None
+    L.biot_tree.argtypes = [ctypes.c_double, ctypes.c_double, _dp, _dp]
+    L.biot_tree.restype = None
+    L.tree2d_last_error.restype = ctypes.c_int
+    L.tree2d_error_string.argtypes = [ctypes.c_int]
+    L.tree2d_error_string.restype = ctypes.c_char_p
+    L.tree2d_set_params.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double]
+    L.tree2d_set_params.restype = ctypes.c_int
+    L.tree2d_clear_params.restype = None
+    L.tree2d_get_params.argtypes = [_ip, _ip, _dp, _dp]
+    L.tree2d_set_mode.argtypes = [ctypes.c_int]
+    L.tree2d_set_mode.restype = ctypes.c_int
+    L.tree2d_get_mode.restype = ctypes.c_int
+    L.biot_tree_batch.argtypes = [ctypes.c_int, _dp, _dp]
+    L.biot_tree_batch.restype = ctypes.c_int
+    L.tree2d_solve_device.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                      ctypes.c_void_p, ctypes.c_void_p]
+    L.tree2d_solve_device.restype = ctypes.c_int
+    L.tree2d_get_stats.argtypes = [ctypes.POINTER(Stats)]
+    L.tree2d_get_stats.restype = ctypes.c_int
+    L.tree2d_export_tree.argtypes = [_ip, ctypes.c_longlong, _ip, _ip, _ip, _ip, _dp, _dp, _dp, _dp]
+    L.tree2d_export_tree.restype = ctypes.c_longlong
+    L.tree2d_direct_device.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
+                                       ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+    L.tree2d_direct_device.restype = ctypes.c_int
+    L.tree2d_fp64_probe.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, _dp]
+    L.tree2d_fp64_probe.restype = ctypes.c_int
+    L.tree2d_version.restype = ctypes.c_char_p
+    _lib = L
+    return L
+
+
+def _f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def _ptr(a):
+    return a.ctypes.data_as(_dp)
+
+
+def error_string(code: int) -> str:
+    return load().tree2d_error_string(code).decode()
+
+
+def last_error() -> int:
+    return load().tree2d_last_error()
+
+
+def _check(rc: int, where: str):
+    if rc != OK:
+        raise Tree2DError(rc, where)
+
+
+def set_params(nterms: int, num_p: int, theta: float, r_min: float = 0.01):
+    _check(load().tree2d_set_params(nterms, num_p, theta, r_min), "set_params")
+
+
+def clear_params():
+    load().tree2d_clear_params()
+
+
+def get_params():
+    a, b = ctypes.c_int(), ctypes.c_int()
+    c, d = ctypes.c_double(), ctypes.c_double()
+    load().tree2d_get_params(ctypes.byref(a), ctypes.byref(b), ctypes.byref(c), ctypes.byref(d))
+    return a.value, b.value, c.value, d.value
+
+
+def set_mode(mode: int):
+    _check(load().tree2d_set_mode(mode), "set_mode")
+
+
+def get_mode() -> int:
+    return load().tree2d_get_mode()
+
+
+def make_tree(vor_b, cir_b, cor_b, check: bool = True) -> int:
+    """make_tree(nvor_b, vor_b, cir_b, cor_b) of the reference; vor_b is
+    (n, 2) x,y per blob.  Returns the library status (the C call itself
+    returns void, like the reference)."""
+    xy = _f64(vor_b).reshape(-1, 2)
+    cir = _f64(cir_b)
+    cor = _f64(cor_b)
+    n = len(cir)
+    if xy.shape[0] != n or cor.shape[0] != n:
+        raise ValueError("vor_b, cir_b and cor_b must describe the same number of blobs")
+    L = load()
+    L.make_tree(n, _ptr(xy), _ptr(cir), _ptr(cor))
+    rc = L.tree2d_last_error()
+    if check:
+        _check(rc, "make_tree")
+    return rc
+
+
+def biot_tree(x: float, y: float):
+    """Velocity (u, v) at one point, as the reference's biot_tree."""
+    u, v = ctypes.c_double(), ctypes.c_double()
+    load().biot_tree(float(x), float(y), ctypes.byref(u), ctypes.byref(v))
+    return u.value, v.value
+
+
+def biot_tree_batch(xy, check: bool = True):
+    xy = _f64(xy).reshape(-1, 2)
+    uv = np.empty_like(xy)
+    rc = load().biot_tree_batch(len(xy), _ptr(xy), _ptr(uv))
+    if check:
+        _check(rc, "biot_tree_batch")
+    return uv
+
+
+def solve_device(d_xy: int, d_cir: int, d_cor: int, d_uv: int, n: int, stream: int = 0):
+    """Device-resident solve over raw device pointers (ints)."""
+    _check(load().tree2d_solve_device(n, d_xy, d_cir, d_cor, d_uv, stream or None), "solve_device")
+
+
+def direct_device(d_txy: int, ntgt: int, d_sxy: int, d_cir: int, d_cor: int, nsrc: int, d_uv: int, stream: int = 0):
+    _check(load().tree2d_direct_device(ntgt, d_txy, nsrc, d_sxy, d_cir, d_cor, d_uv, stream or None), "direct")
+
+
+def stats() -> dict:
+    s = Stats()
+    _check(load().tree2d_get_stats(ctypes.byref(s)), "stats")
+    return s.as_dict()
+
+
+def export_tree(n: int, nterms: int) -> dict:
+    """Permutation and non-empty cells below the root (pre-order) of the
+    last make_tree, in the oracle's dump format."""
+    L = load()
+    nc = L.tree2d_export_tree(None, 0, None, None, None, None, None, None, None, None)
+    if nc < 0:
+        raise Tree2DError(ERR_NO_TREE, "export_tree")
+    perm = np.empty(n, np.int32)
+    lev, beg, end, leaf = (np.empty(nc, np.int32) for _ in range(4))
+    cx, cy, reg = (np.empty(nc) for _ in range(3))
+    coef = np.empty((nc, max(nterms, 1), 2))
+    ip = lambda a: a.ctypes.data_as(_ip)  # noqa: E731
+    got = L.tree2d_export_tree(ip(perm), max(nc, 1), ip(lev), ip(beg), ip(end), ip(leaf), _ptr(cx), _ptr(cy),
+                               _ptr(reg), _ptr(coef))
+    if got != nc:
+        raise Tree2DError(ERR_CUDA, "export_tree")
+    return dict(perm=perm, level=lev, begin=beg, end=end, leaf=leaf, cx=cx, cy=cy, region=reg,
+                coef=(coef[..., 0] + 1j * coef[..., 1])[:, :nterms])
+
+
+def fp64_peak_tflops(blocks: int = 152 * 8, iters: int = 20000, stream: int = 0) -> float:
+    """Measured FP64 FMA throughput of this GPU (TFLOP/s, FMA = 2 flops)."""
+    ms = ctypes.c_double()
+    _check(load().tree2d_fp64_probe(blocks, iters, stream or None, ctypes.byref(ms)), "fp64_probe")
+    return blocks * 256.0 * iters * 16.0 / (ms.value * 1e-3) / 1e12
+
+
+def version() -> str:
+    return load().tree2d_version().decode()

@@ -1,0 +1,594 @@
+// C ABI of libtree2d_gb300.so: the reference's make_tree / biot_tree
+// (ver-c/src/quadtree.c:102-171, ver-c/src/fmm.c:69-118) plus extensions.
+//
+// State is library-global, as in the reference (quadtree.c:9-10 keeps
+// `qtree` and `vors` global): make_tree replaces the tree, biot_tree reads
+// it.  make_tree runs the whole pipeline on the GPU and evaluates the
+// velocity at every blob position, because the reference's callers ask for
+// exactly those points one call at a time (e_velo_mpi.f90:37-48): a GPU
+// launch per call would be latency bound.  biot_tree answers blob positions
+// from that table (matched bit for bit on x and y) and evaluates any other
+// point on the GPU with the same kernel.
+#include <atomic>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "dev_common.cuh"
+
+namespace t2d {
+
+Arena::~Arena() {
+  // Device memory is released at process exit; freeing here could run after
+  // the CUDA runtime has been torn down.
+}
+
+cudaError_t Arena::reserve(size_t bytes) {
+  if (bytes <= cap_) return cudaSuccess;
+  if (base_) cudaFree(base_);
+  base_ = nullptr;
+  cap_ = 0;
+  used_ = 0;
+  size_t want = bytes + bytes / 8 + 4096;
+  cudaError_t e = cudaMalloc(reinterpret_cast<void **>(&base_), want);
+  if (e == cudaSuccess) cap_ = want;
+  return e;
+}
+
+cudaError_t workspace_init(Workspace &ws) {
+  if (ws.init) return cudaSuccess;
+  cudaError_t e = cudaMalloc(reinterpret_cast<void **>(&ws.status), sizeof(DevStatus));
+  if (e != cudaSuccess) return e;
+  e = cudaMallocHost(reinterpret_cast<void **>(&ws.h_status), 4096);
+  if (e != cudaSuccess) return e;
+  for (auto &ev : ws.ev) {
+    e = cudaEventCreate(&ev);
+    if (e != cudaSuccess) return e;
+  }
+  ws.init = true;
+  return cudaSuccess;
+}
+
+std::atomic<long long> g_launches{0};
+
+static std::mutex g_msg_mu;
+static std::string g_cuda_msg;
+
+void note_cuda_error(cudaError_t e, const char *what) {
+  std::lock_guard<std::mutex> lk(g_msg_mu);
+  g_cuda_msg = std::string(cudaGetErrorString(e)) + " (" + what + ")";
+}
+
+namespace {
+
+struct Solver {
+  Workspace ws;
+  Tree tree;
+  Arena io;       // device copies of host inputs and outputs
+  Arena targets;  // evaluation-order targets
+};
+
+struct Lib {
+  std::mutex mu;
+  Params params;
+  bool have_params = false;
+  bool params_fixed = false;
+  int mode = TREE2D_MODE_PLAIN;
+  std::atomic<int> last_error{0};
+  cudaStream_t stream = nullptr;
+  bool stream_ready = false;
+  Solver main, dev;
+  // results of the last make_tree
+  std::atomic<bool> valid{false};
+  std::atomic<unsigned long long> generation{0};
+  std::vector<double> h_xy, h_uv;
+  int n = 0;
+  // position -> blob index, built on first need
+  std::mutex hash_mu;
+  std::atomic<bool> hash_ready{false};
+  std::vector<int> hash_slot;
+  size_t hash_mask = 0;
+  tree2d_stats_t stats{};
+  tree2d_stats_t dev_stats{};
+  bool last_was_dev = false;
+};
+
+Lib &lib() {
+  static Lib *l = new Lib();  // never destroyed (see Arena::~Arena)
+  return *l;
+}
+
+int fail(int code) {
+  lib().last_error.store(code);
+  return code;
+}
+
+int ensure_stream(Lib &L) {
+  if (L.stream_ready) return TREE2D_OK;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return TREE2D_ERR_NO_DEVICE;
+  T2D_CUDA_TRY(cudaStreamCreateWithFlags(&L.stream, cudaStreamNonBlocking));
+  L.stream_ready = true;
+  return TREE2D_OK;
+}
+
+// ../cal_cond/fmm_param.dat, read as quadtree.c:12-27 reads it.
+bool read_param_file(Params &p) {
+  FILE *f = std::fopen("../cal_cond/fmm_param.dat", "r");
+  if (!f) {
+    std::printf("Error: Could not read FMM parameters.");
+    std::fflush(stdout);
+    return false;
+  }
+  if (std::fscanf(f, "%i    nterms", &p.nterms) < 0) { /* as the reference: ignored */ }
+  if (std::fscanf(f, "%i   num_p", &p.num_p) < 0) { /* ignored */ }
+  if (std::fscanf(f, "%lf theta", &p.theta) < 0) { /* ignored */ }
+  if (std::fscanf(f, "%lf  r_min ! for Tree", &p.r_min) < 0) { /* ignored */ }
+  std::fclose(f);
+  return true;
+}
+
+int check_params(const Params &p) {
+  if (p.nterms < 0 || p.nterms > kMaxTerms) return TREE2D_ERR_BAD_PARAMS;
+  if (p.num_p < 2 || p.num_p > 65536) return TREE2D_ERR_BAD_PARAMS;
+  if (!std::isfinite(p.theta)) return TREE2D_ERR_BAD_PARAMS;
+  return TREE2D_OK;
+}
+
+// Parameters in force for the next solve: the fixed ones, else the file
+// (when the file cannot be read, the previous values stay in force, as the
+// reference's globals do).
+int resolve_params(Lib &L) {
+  if (!L.params_fixed) {
+    Params p = L.params;
+    if (read_param_file(p)) {
+      L.params = p;
+      L.have_params = true;
+    }
+  }
+  if (!L.have_params) return TREE2D_ERR_PARAM_FILE;
+  return check_params(L.params);
+}
+
+float elapsed(cudaEvent_t a, cudaEvent_t b) {
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, a, b);
+  return ms;
+}
+
+// Whole pipeline over n device-resident blobs; uv (interleaved, original
+// order) on the device.
+int solve(Lib &L, Solver &S, int n, const double *d_xy, const double *d_cir, const double *d_cor, double *d_uv,
+          cudaStream_t s, tree2d_stats_t &st) {
+  T2D_CUDA_TRY(workspace_init(S.ws));
+  std::memset(&st, 0, sizeof(st));
+  st.n_blobs = n;
+  st.mode = L.mode;
+  if (n == 0) {
+    S.tree = Tree();
+    return TREE2D_OK;
+  }
+  Workspace &ws = S.ws;
+  const long long launches0 = g_launches.load();
+  T2D_CUDA_TRY(cudaEventRecord(ws.ev[0], s));
+  int rc = build_tree(ws, n, d_xy, d_cir, d_cor, L.params, S.tree, s);
+  if (rc) return rc;
+  T2D_CUDA_TRY(cudaEventRecord(ws.ev[1], s));
+  rc = plain_upward(ws, S.tree, L.params, s);
+  if (rc) return rc;
+  T2D_CUDA_TRY(cudaEventRecord(ws.ev[2], s));
+  rc = plain_evaluate(ws, S.tree, L.params, n, S.tree.x, S.tree.y, S.tree.perm, d_uv, s);
+  if (rc) return rc;
+  T2D_CUDA_TRY(cudaEventRecord(ws.ev[3], s));
+  T2D_CUDA_TRY(cudaMemcpyAsync(ws.h_status, ws.status, sizeof(DevStatus), cudaMemcpyDeviceToHost, s));
+  T2D_CUDA_TRY(cudaStreamSynchronize(s));
+  if (ws.h_status->err) return ws.h_status->err;
+  st.n_cells = S.tree.ncell;
+  st.n_leaves = S.tree.nleaf;
+  st.depth = S.tree.depth;
+  st.n_m2s = (long long)ws.h_status->n_m2s;
+  st.n_pairs = (long long)ws.h_status->n_pairs;
+  st.n_m2l = (long long)ws.h_status->n_m2l;
+  st.ms_build = elapsed(ws.ev[0], ws.ev[1]);
+  st.ms_upward = elapsed(ws.ev[1], ws.ev[2]);
+  st.ms_eval = elapsed(ws.ev[2], ws.ev[3]);
+  st.ms_total = elapsed(ws.ev[0], ws.ev[3]);
+  st.n_launches = g_launches.load() - launches0;
+  return TREE2D_OK;
+}
+
+uint64_t mix64(uint64_t x) {
+  x += 0x9e3779b97f4a7c15ull;
+  x = (x ^ (x >> 30)) * 0xbf58476d1ce4e5b9ull;
+  x = (x ^ (x >> 27)) * 0x94d049bb133111ebull;
+  return x ^ (x >> 31);
+}
+
+uint64_t pos_hash(double x, double y) {
+  uint64_t a, b;
+  std::memcpy(&a, &x, 8);
+  std::memcpy(&b, &y, 8);
+  return mix64(a ^ mix64(b));
+}
+
+bool same_bits(double a, double b) { return std::memcmp(&a, &b, 8) == 0; }
+
+void ensure_hash(Lib &L) {
+  if (L.hash_ready.load(std::memory_order_acquire)) return;
+  std::lock_guard<std::mutex> lk(L.hash_mu);
+  if (L.hash_ready.load(std::memory_order_relaxed)) return;
+  size_t cap = 16;
+  while (cap < 2 * (size_t)L.n) cap <<= 1;
+  L.hash_slot.assign(cap, 0);
+  L.hash_mask = cap - 1;
+  for (int i = 0; i < L.n; i++) {
+    double x = L.h_xy[2 * (size_t)i], y = L.h_xy[2 * (size_t)i + 1];
+    size_t h = pos_hash(x, y) & L.hash_mask;
+    while (true) {
+      int s = L.hash_slot[h];
+      if (s == 0) {
+        L.hash_slot[h] = i + 1;
+        break;
+      }
+      if (same_bits(L.h_xy[2 * (size_t)(s - 1)], x) && same_bits(L.h_xy[2 * (size_t)(s - 1) + 1], y)) break;
+      h = (h + 1) & L.hash_mask;
+    }
+  }
+  L.hash_ready.store(true, std::memory_order_release);
+}
+
+// Index of a blob at exactly (x,y), or -1.
+long find_blob(Lib &L, double x, double y) {
+  thread_local unsigned long long gen = ~0ull;
+  thread_local long hint = -1;
+  unsigned long long g = L.generation.load(std::memory_order_acquire);
+  if (gen != g) {
+    gen = g;
+    hint = -1;
+  }
+  const long n = L.n;
+  for (long c : {hint + 1, hint}) {
+    if (c >= 0 && c < n && same_bits(L.h_xy[2 * c], x) && same_bits(L.h_xy[2 * c + 1], y)) {
+      hint = c;
+      return c;
+    }
+  }
+  ensure_hash(L);
+  size_t h = pos_hash(x, y) & L.hash_mask;
+  while (true) {
+    int s = L.hash_slot[h];
+    if (s == 0) return -1;
+    if (same_bits(L.h_xy[2 * (size_t)(s - 1)], x) && same_bits(L.h_xy[2 * (size_t)(s - 1) + 1], y)) {
+      hint = s - 1;
+      return s - 1;
+    }
+    h = (h + 1) & L.hash_mask;
+  }
+}
+
+// GPU evaluation of m arbitrary points (host xy) into host uv; L.mu held.
+int eval_points(Lib &L, int m, const double *xy, double *uv) {
+  Solver &S = L.main;
+  if (L.n == 0) {
+    for (int i = 0; i < 2 * m; i++) uv[i] = 0.0;
+    return TREE2D_OK;
+  }
+  cudaStream_t s = L.stream;
+  size_t need = Arena::bytes_for(2 * (size_t)m, 8) * 2 + Arena::bytes_for(m, 8) * 2 + Arena::bytes_for(m, 4) * 2;
+  T2D_CUDA_TRY(S.targets.reserve(need));
+  S.targets.reset();
+  double *d_xy = S.targets.take<double>(2 * (size_t)m);
+  double *d_uv = S.targets.take<double>(2 * (size_t)m);
+  double *tx = S.targets.take<double>(m);
+  double *ty = S.targets.take<double>(m);
+  int *order = S.targets.take<int>(m);
+  int *out = S.targets.take<int>(m);
+  T2D_CUDA_TRY(cudaMemcpyAsync(d_xy, xy, sizeof(double) * 2 * (size_t)m, cudaMemcpyHostToDevice, s));
+  int rc;
+  if (m > 1024) {
+    rc = sort_targets(S.ws, m, d_xy, S.tree.root, order, s);
+    if (rc) return rc;
+    rc = gather_targets(m, d_xy, order, tx, ty, out, s);
+  } else {
+    rc = gather_targets(m, d_xy, nullptr, tx, ty, out, s);
+  }
+  if (rc) return rc;
+  T2D_CUDA_TRY(cudaMemsetAsync(S.ws.status, 0, sizeof(DevStatus), s));
+  rc = plain_evaluate(S.ws, S.tree, L.params, m, tx, ty, out, d_uv, s);
+  if (rc) return rc;
+  T2D_CUDA_TRY(cudaMemcpyAsync(uv, d_uv, sizeof(double) * 2 * (size_t)m, cudaMemcpyDeviceToHost, s));
+  T2D_CUDA_TRY(cudaMemcpyAsync(S.ws.h_status, S.ws.status, sizeof(DevStatus), cudaMemcpyDeviceToHost, s));
+  T2D_CUDA_TRY(cudaStreamSynchronize(s));
+  return S.ws.h_status->err;
+}
+
+}  // namespace
+}  // namespace t2d
+
+using namespace t2d;
+
+extern "C" {
+
+void make_tree(int nvor_b, const double *vor_b, const double *cir_b, const double *cor_b) {
+  Lib &L = lib();
+  std::lock_guard<std::mutex> lk(L.mu);
+  L.valid.store(false);
+  L.hash_ready.store(false);
+  L.generation.fetch_add(1);
+  L.last_error.store(TREE2D_OK);
+  int rc = resolve_params(L);
+  if (rc) {
+    fail(rc);
+    return;
+  }
+  if (nvor_b < 0 || (nvor_b > 0 && (!vor_b || !cir_b || !cor_b))) {
+    fail(TREE2D_ERR_BAD_INPUT);
+    return;
+  }
+  rc = ensure_stream(L);
+  if (rc) {
+    fail(rc);
+    return;
+  }
+  const int n = nvor_b;
+  Solver &S = L.main;
+  double *d_xy = nullptr, *d_cir = nullptr, *d_cor = nullptr, *d_uv = nullptr;
+  if (n > 0) {
+    size_t need = Arena::bytes_for(2 * (size_t)n, 8) * 2 + Arena::bytes_for(n, 8) * 2;
+    cudaError_t e = S.io.reserve(need);
+    if (e != cudaSuccess) {
+      note_cuda_error(e, "make_tree input buffers");
+      fail(TREE2D_ERR_CUDA);
+      return;
+    }
+    S.io.reset();
+    d_xy = S.io.take<double>(2 * (size_t)n);
+    d_uv = S.io.take<double>(2 * (size_t)n);
+    d_cir = S.io.take<double>(n);
+    d_cor = S.io.take<double>(n);
+    cudaStream_t s = L.stream;
+    if (cudaMemcpyAsync(d_xy, vor_b, sizeof(double) * 2 * (size_t)n, cudaMemcpyHostToDevice, s) != cudaSuccess ||
+        cudaMemcpyAsync(d_cir, cir_b, sizeof(double) * (size_t)n, cudaMemcpyHostToDevice, s) != cudaSuccess ||
+        cudaMemcpyAsync(d_cor, cor_b, sizeof(double) * (size_t)n, cudaMemcpyHostToDevice, s) != cudaSuccess) {
+      note_cuda_error(cudaGetLastError(), "make_tree upload");
+      fail(TREE2D_ERR_CUDA);
+      return;
+    }
+  }
+  rc = solve(L, S, n, d_xy, d_cir, d_cor, d_uv, L.stream, L.stats);
+  L.last_was_dev = false;
+  if (rc) {
+    fail(rc);
+    return;
+  }
+  L.h_xy.assign(vor_b, vor_b + 2 * (size_t)n);
+  L.h_uv.resize(2 * (size_t)n);
+  if (n > 0) {
+    cudaError_t e = cudaMemcpy(L.h_uv.data(), d_uv, sizeof(double) * 2 * (size_t)n, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) {
+      note_cuda_error(e, "make_tree download");
+      fail(TREE2D_ERR_CUDA);
+      return;
+    }
+  }
+  L.n = n;
+  L.valid.store(true);
+}
+
+void biot_tree(double x, double y, double *u, double *v) {
+  Lib &L = lib();
+  if (!L.valid.load(std::memory_order_acquire)) {
+    *u = NAN;
+    *v = NAN;
+    L.last_error.store(TREE2D_ERR_NO_TREE);
+    return;
+  }
+  long k = find_blob(L, x, y);
+  if (k >= 0) {
+    *u = L.h_uv[2 * k];
+    *v = L.h_uv[2 * k + 1];
+    return;
+  }
+  std::lock_guard<std::mutex> lk(L.mu);
+  double xy[2] = {x, y}, uv[2];
+  int rc = eval_points(L, 1, xy, uv);
+  if (rc) {
+    fail(rc);
+    *u = NAN;
+    *v = NAN;
+    return;
+  }
+  *u = uv[0];
+  *v = uv[1];
+}
+
+int biot_tree_batch(int n, const double *xy, double *uv) {
+  Lib &L = lib();
+  if (n < 0 || (n > 0 && (!xy || !uv))) return fail(TREE2D_ERR_BAD_INPUT);
+  if (!L.valid.load(std::memory_order_acquire)) {
+    for (long i = 0; i < 2 * (long)n; i++) uv[i] = NAN;
+    return fail(TREE2D_ERR_NO_TREE);
+  }
+  std::vector<int> miss;
+  for (int i = 0; i < n; i++) {
+    long k = find_blob(L, xy[2 * (size_t)i], xy[2 * (size_t)i + 1]);
+    if (k >= 0) {
+      uv[2 * (size_t)i] = L.h_uv[2 * k];
+      uv[2 * (size_t)i + 1] = L.h_uv[2 * k + 1];
+    } else {
+      miss.push_back(i);
+    }
+  }
+  if (miss.empty()) return TREE2D_OK;
+  std::vector<double> mxy(2 * miss.size()), muv(2 * miss.size());
+  for (size_t j = 0; j < miss.size(); j++) {
+    mxy[2 * j] = xy[2 * (size_t)miss[j]];
+    mxy[2 * j + 1] = xy[2 * (size_t)miss[j] + 1];
+  }
+  std::lock_guard<std::mutex> lk(L.mu);
+  int rc = eval_points(L, (int)miss.size(), mxy.data(), muv.data());
+  for (size_t j = 0; j < miss.size(); j++) {
+    uv[2 * (size_t)miss[j]] = rc ? NAN : muv[2 * j];
+    uv[2 * (size_t)miss[j] + 1] = rc ? NAN : muv[2 * j + 1];
+  }
+  return rc ? fail(rc) : TREE2D_OK;
+}
+
+int tree2d_last_error(void) { return lib().last_error.load(); }
+
+const char *tree2d_error_string(int code) {
+  switch (code) {
+    case TREE2D_OK: return "ok";
+    case TREE2D_ERR_PARAM_FILE: return "could not read ../cal_cond/fmm_param.dat and no parameters were set";
+    case TREE2D_ERR_BAD_PARAMS: return "invalid parameters (need 0<=nterms<=32, 2<=num_p<=65536, finite theta)";
+    case TREE2D_ERR_BAD_INPUT: return "invalid input (negative count, null array, or non-finite value)";
+    case TREE2D_ERR_TOO_DEEP: return "tree deeper than 32 levels (>= num_p coincident blobs?)";
+    case TREE2D_ERR_CUDA: {
+      std::lock_guard<std::mutex> lk(g_msg_mu);
+      static thread_local std::string s;
+      s = "CUDA error: " + g_cuda_msg;
+      return s.c_str();
+    }
+    case TREE2D_ERR_NO_TREE: return "no valid tree (make_tree not called or failed)";
+    case TREE2D_ERR_NO_DEVICE: return "no CUDA device";
+    case TREE2D_ERR_TIMEOUT: return "a bounded device loop gave up (traversal stack overflow)";
+    case TREE2D_ERR_MODE: return "unknown or unavailable mode";
+    default: return "unknown error";
+  }
+}
+
+int tree2d_set_params(int nterms, int num_p, double theta, double r_min) {
+  Lib &L = lib();
+  std::lock_guard<std::mutex> lk(L.mu);
+  Params p;
+  p.nterms = nterms;
+  p.num_p = num_p;
+  p.theta = theta;
+  p.r_min = r_min;
+  int rc = check_params(p);
+  if (rc) return fail(rc);
+  L.params = p;
+  L.have_params = true;
+  L.params_fixed = true;
+  return TREE2D_OK;
+}
+
+void tree2d_clear_params(void) {
+  Lib &L = lib();
+  std::lock_guard<std::mutex> lk(L.mu);
+  L.params_fixed = false;
+}
+
+void tree2d_get_params(int *nterms, int *num_p, double *theta, double *r_min) {
+  Lib &L = lib();
+  std::lock_guard<std::mutex> lk(L.mu);
+  if (nterms) *nterms = L.params.nterms;
+  if (num_p) *num_p = L.params.num_p;
+  if (theta) *theta = L.params.theta;
+  if (r_min) *r_min = L.params.r_min;
+}
+
+int tree2d_set_mode(int mode) {
+  Lib &L = lib();
+  std::lock_guard<std::mutex> lk(L.mu);
+  if (mode != TREE2D_MODE_PLAIN) return fail(TREE2D_ERR_MODE);
+  L.mode = mode;
+  return TREE2D_OK;
+}
+
+int tree2d_get_mode(void) { return lib().mode; }
+
+int tree2d_solve_device(int n, const double *d_xy, const double *d_cir, const double *d_cor, double *d_uv,
+                        void *stream) {
+  Lib &L = lib();
+  std::lock_guard<std::mutex> lk(L.mu);
+  int rc = resolve_params(L);
+  if (rc) return fail(rc);
+  if (n < 0) return fail(TREE2D_ERR_BAD_INPUT);
+  rc = ensure_stream(L);
+  if (rc) return fail(rc);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  rc = solve(L, L.dev, n, d_xy, d_cir, d_cor, d_uv, s, L.dev_stats);
+  L.last_was_dev = true;
+  if (rc) return fail(rc);
+  return TREE2D_OK;
+}
+
+int tree2d_get_stats(tree2d_stats_t *out) {
+  Lib &L = lib();
+  std::lock_guard<std::mutex> lk(L.mu);
+  if (!out) return TREE2D_ERR_BAD_INPUT;
+  *out = L.last_was_dev ? L.dev_stats : L.stats;  // the most recent solve
+  return TREE2D_OK;
+}
+
+long long tree2d_export_tree(int *perm, long long cap, int *level, int *begin, int *end, int *leaf, double *cx,
+                             double *cy, double *region, double *coef) {
+  Lib &L = lib();
+  std::lock_guard<std::mutex> lk(L.mu);
+  if (!L.valid.load()) return -1;
+  const Tree &t = L.main.tree;
+  if (t.n == 0) return 0;
+  long long nc = t.ncell - 1;
+  if (cap <= 0) return nc;
+  if (cap < nc) return -1;
+  const int nt = t.nterms;
+  if (perm && cudaMemcpy(perm, t.perm, sizeof(int) * (size_t)t.n, cudaMemcpyDeviceToHost) != cudaSuccess) return -1;
+  std::vector<unsigned char> lf(nc);
+  if (level) cudaMemcpy(level, t.level + 1, sizeof(int) * nc, cudaMemcpyDeviceToHost);
+  if (begin) cudaMemcpy(begin, t.begin + 1, sizeof(int) * nc, cudaMemcpyDeviceToHost);
+  if (end) cudaMemcpy(end, t.end + 1, sizeof(int) * nc, cudaMemcpyDeviceToHost);
+  if (leaf) {
+    cudaMemcpy(lf.data(), t.leaf + 1, nc, cudaMemcpyDeviceToHost);
+    for (long long i = 0; i < nc; i++) leaf[i] = lf[i];
+  }
+  if (cx) cudaMemcpy(cx, t.cx + 1, sizeof(double) * nc, cudaMemcpyDeviceToHost);
+  if (cy) cudaMemcpy(cy, t.cy + 1, sizeof(double) * nc, cudaMemcpyDeviceToHost);
+  if (region) cudaMemcpy(region, t.region + 1, sizeof(double) * nc, cudaMemcpyDeviceToHost);
+  if (coef && nt > 0) cudaMemcpy(coef, t.coef + nt, sizeof(double2) * nc * nt, cudaMemcpyDeviceToHost);
+  if (cudaGetLastError() != cudaSuccess) return -1;
+  return nc;
+}
+
+int tree2d_direct_device(int ntgt, const double *d_txy, int nsrc, const double *d_sxy, const double *d_cir,
+                         const double *d_cor, double *d_uv, void *stream) {
+  cudaError_t e = direct_sum(ntgt, d_txy, nsrc, d_sxy, d_cir, d_cor, d_uv, static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) {
+    note_cuda_error(e, "direct_sum");
+    return fail(TREE2D_ERR_CUDA);
+  }
+  return TREE2D_OK;
+}
+
+int tree2d_fp64_probe(int blocks, int iters, void *stream, double *ms) {
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  double *buf = nullptr;
+  cudaEvent_t a, b;
+  if (cudaMalloc(reinterpret_cast<void **>(&buf), 64) != cudaSuccess) return fail(TREE2D_ERR_CUDA);
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  dfma_probe(buf, blocks, iters / 8 + 1, s);  // warm-up
+  cudaEventRecord(a, s);
+  cudaError_t e = dfma_probe(buf, blocks, iters, s);
+  cudaEventRecord(b, s);
+  cudaEventSynchronize(b);
+  float f = 0.f;
+  cudaEventElapsedTime(&f, a, b);
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  cudaFree(buf);
+  if (e != cudaSuccess) {
+    note_cuda_error(e, "dfma_probe");
+    return fail(TREE2D_ERR_CUDA);
+  }
+  if (ms) *ms = f;
+  return TREE2D_OK;
+}
+
+const char *tree2d_version(void) { return "tree2d-gb300 0.1 (sm_103a)"; }
+
+}  // extern "C"

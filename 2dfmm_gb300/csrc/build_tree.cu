@@ -1,0 +1,577 @@
+// Tree build on the device, bit-exact with the reference's recursive
+// bucketing (ver-c/src/quadtree.c:81-99 root box, :29-35 quadrant test,
+// :61-79 child centres, :173-251 split_cell).
+//
+//   1. k_bbox/k_root  root box: min/max reduction, side = max(dx,dy)+1e-4,
+//                     centre = midpoint (quadtree.c:81-99)
+//   2. k_keys         per blob, 32 levels of the reference's quadrant test
+//                     against FP64 centres formed exactly as the reference
+//                     forms them (c +- 0.25*R per level) -> 64-bit key of
+//                     base-4 digits, level 1 in the top bits
+//   3. radix sort     (key, blob index) pairs, stable
+//   4. k_cpl          cpl[i] = levels shared by keys i and i+1;
+//                     w[j]   = levels shared by keys j and j+num_p-1
+//   5. k_leaf_level   a level-l cell holds >= num_p blobs iff some window of
+//                     num_p consecutive keys inside it shares l levels, so the
+//                     deepest split level of blob i is the max of w over the
+//                     windows that contain i; its leaf sits one level below
+//                     (the root is always split, quadtree.c:183-196)
+//   6. cell counts    position i starts the cells of levels
+//                     (cpl[i-1], leaf_level[i]]; a scan numbers all cells in
+//                     depth-first pre-order (root = 0)
+//   7. k_emit_cells   level, begin, leaf flag, centre (same FP64 descent),
+//                     side; k_cell_end (binary search), k_children
+//   8. k_leaf_order   blobs inside a leaf in ascending original index, the
+//                     order the reference's stable bucketing leaves them in
+//   9. k_gather       blob arrays in tree order
+#include <cstdio>
+
+#include "dev_common.cuh"
+
+namespace t2d {
+namespace {
+
+constexpr int kBoxBlocks = 304;   // 2 x 152 SMs
+
+struct __align__(16) Box4 {
+  double x, y, z, w;  // xmax, xmin, ymax, ymin
+};
+constexpr int kScanThreads = 256;
+constexpr int kScanItems = 16;
+constexpr int kScanTile = kScanThreads * kScanItems;
+
+__device__ __forceinline__ double warp_max(double v) {
+  for (int o = 16; o; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+__device__ __forceinline__ double warp_min(double v) {
+  for (int o = 16; o; o >>= 1) v = fmin(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+
+__global__ void __launch_bounds__(256) k_bbox(const double *__restrict__ xy, const double *__restrict__ cir,
+                                              const double *__restrict__ cor, int n, Box4 *part,
+                                              DevStatus *st) {
+  double xmax = -INFINITY, xmin = INFINITY, ymax = -INFINITY, ymin = INFINITY;
+  bool bad = false;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+    double x = xy[2 * i], y = xy[2 * i + 1];
+    double c = cir[i], r = cor[i];
+    bad |= !(isfinite(x) && isfinite(y) && isfinite(c)) || isnan(r);
+    xmax = fmax(xmax, x);
+    xmin = fmin(xmin, x);
+    ymax = fmax(ymax, y);
+    ymin = fmin(ymin, y);
+  }
+  __shared__ Box4 s[8];
+  xmax = warp_max(xmax);
+  xmin = warp_min(xmin);
+  ymax = warp_max(ymax);
+  ymin = warp_min(ymin);
+  int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (lane == 0) s[w] = Box4{xmax, xmin, ymax, ymin};
+  if (__syncthreads_or(bad) && threadIdx.x == 0) set_err(st, TREE2D_ERR_BAD_INPUT);
+  if (threadIdx.x == 0) {
+    Box4 r = s[0];
+    for (int k = 1; k < (int)(blockDim.x >> 5); k++) {
+      r.x = fmax(r.x, s[k].x);
+      r.y = fmin(r.y, s[k].y);
+      r.z = fmax(r.z, s[k].z);
+      r.w = fmin(r.w, s[k].w);
+    }
+    part[blockIdx.x] = r;
+  }
+}
+
+__global__ void k_root(const Box4 *part, int nparts, RootBox *root) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  Box4 r = part[0];
+  for (int k = 1; k < nparts; k++) {
+    r.x = fmax(r.x, part[k].x);
+    r.y = fmin(r.y, part[k].y);
+    r.z = fmax(r.z, part[k].z);
+    r.w = fmin(r.w, part[k].w);
+  }
+  // quadtree.c:87-98
+  double rx = __dadd_rn(fabs(__dsub_rn(r.x, r.y)), 0.0001);
+  double ry = __dadd_rn(fabs(__dsub_rn(r.z, r.w)), 0.0001);
+  RootBox b;
+  b.region = rx > ry ? rx : ry;
+  b.cx = __dmul_rn(0.5, __dadd_rn(r.x, r.y));
+  b.cy = __dmul_rn(0.5, __dadd_rn(r.z, r.w));
+  b.xmax = r.x;
+  b.xmin = r.y;
+  b.ymax = r.z;
+  b.ymin = r.w;
+  *root = b;
+}
+
+// One level of the reference's descent: digit of (x,y) against the centre,
+// then the centre of that child (quadtree.c:29-35, :61-79, :236).
+__device__ __forceinline__ unsigned descend(double x, double y, double &cx, double &cy, double &R) {
+  unsigned q = (x >= cx ? 1u : 0u) | (y <= cy ? 2u : 0u);
+  double h = __dmul_rn(0.25, R);
+  cx = (q & 1u) ? __dadd_rn(cx, h) : __dsub_rn(cx, h);
+  cy = (q & 2u) ? __dsub_rn(cy, h) : __dadd_rn(cy, h);
+  R = __dmul_rn(0.5, R);
+  return q;
+}
+
+__global__ void __launch_bounds__(256) k_keys(const double *__restrict__ xy, int n, const RootBox *__restrict__ root,
+                                              uint64_t *__restrict__ keys, uint32_t *__restrict__ vals) {
+  long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double x = xy[2 * i], y = xy[2 * i + 1];
+  double cx = root->cx, cy = root->cy, R = root->region;
+  uint64_t key = 0;
+#pragma unroll 8
+  for (int l = 0; l < kKeyLevels; l++) key = (key << 2) | descend(x, y, cx, cy, R);
+  keys[i] = key;
+  vals[i] = (uint32_t)i;
+}
+
+__global__ void __launch_bounds__(256) k_cpl(const uint64_t *__restrict__ keys, int n, int num_p,
+                                             uint8_t *__restrict__ cpl, uint8_t *__restrict__ w) {
+  long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (i + 1 < n) cpl[i] = (uint8_t)common_levels(keys[i], keys[i + 1]);
+  if (i + num_p - 1 < n) w[i] = (uint8_t)common_levels(keys[i], keys[i + num_p - 1]);
+}
+
+// Sliding maximum of w over the num_p windows that contain position i.
+// Tile of kLLTile outputs; two shared buffers hold w[tile-H .. tile+kLLTile)
+// (H = num_p-1) and the log-step doubling ping-pongs between them:
+// after the step of width k, buf[t] = max(w[t .. t+k-1]).
+constexpr int kLLTile = 2048;
+__global__ void __launch_bounds__(256) k_leaf_level(const uint8_t *__restrict__ w, int n, int num_p,
+                                                    uint8_t *__restrict__ leaf_level, DevStatus *st) {
+  extern __shared__ uint8_t sbuf[];
+  const int H = num_p - 1;
+  const long tile0 = (long)blockIdx.x * kLLTile;
+  const int len = kLLTile + H;
+  uint8_t *cur = sbuf, *nxt = sbuf + len;
+  const long nw = (long)n - num_p + 1;  // number of windows
+  for (int t = threadIdx.x; t < len; t += blockDim.x) {
+    long j = tile0 - H + t;
+    cur[t] = (j >= 0 && j < nw) ? w[j] : 0;
+  }
+  __syncthreads();
+  const int W = num_p;
+  int K = 1;
+  while (K * 2 <= W) K *= 2;
+  for (int k = 1; k < K; k *= 2) {
+    for (int t = threadIdx.x; t < len; t += blockDim.x) {
+      uint8_t a = cur[t];
+      uint8_t b = (t + k < len) ? cur[t + k] : 0;
+      nxt[t] = a > b ? a : b;
+    }
+    __syncthreads();
+    uint8_t *tmp = cur;
+    cur = nxt;
+    nxt = tmp;
+  }
+  int local_max = 0;
+  for (int t = threadIdx.x; t < kLLTile; t += blockDim.x) {
+    long i = tile0 + t;
+    if (i >= n) break;
+    // window starts j in [i-H, i]  ->  buffer [t, t+H]
+    uint8_t a = cur[t];
+    uint8_t b = cur[t + W - K];
+    int s = a > b ? a : b;
+    if (s >= kKeyLevels) {
+      set_err(st, TREE2D_ERR_TOO_DEEP);
+      s = kKeyLevels - 1;
+    }
+    leaf_level[i] = (uint8_t)(s + 1);
+    local_max = max(local_max, s + 1);
+  }
+  for (int o = 16; o; o >>= 1) local_max = max(local_max, __shfl_xor_sync(0xffffffffu, local_max, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(&st->depth, local_max);
+}
+
+__device__ __forceinline__ void cell_counts(const uint8_t *cpl, const uint8_t *leaf_level, long i, int n,
+                                            unsigned &ncell, unsigned &isleaf) {
+  ncell = 0;
+  isleaf = 0;
+  if (i < n) {
+    int prev = i > 0 ? cpl[i - 1] : 0;
+    int lam = leaf_level[i];
+    if (lam > prev) {
+      ncell = (unsigned)(lam - prev);
+      isleaf = 1;
+    }
+  }
+}
+
+// pack: cells in the high 32 bits, leaves in the low 32 bits
+__global__ void __launch_bounds__(kScanThreads) k_cells_reduce(const uint8_t *cpl, const uint8_t *leaf_level, int n,
+                                                               unsigned long long *part) {
+  unsigned long long s = 0;
+  long base = (long)blockIdx.x * kScanTile;
+  for (int k = threadIdx.x; k < kScanTile; k += kScanThreads) {
+    unsigned c, l;
+    cell_counts(cpl, leaf_level, base + k, n, c, l);
+    s += ((unsigned long long)c << 32) | l;
+  }
+  for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  __shared__ unsigned long long ws[kScanThreads / 32];
+  if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned long long t = 0;
+    for (int k = 0; k < kScanThreads / 32; k++) t += ws[k];
+    part[blockIdx.x] = t;
+  }
+}
+
+// exclusive scan of the tile partials (one block); total -> *total
+__global__ void __launch_bounds__(1024) k_scan_part(unsigned long long *part, int len, unsigned long long *total) {
+  __shared__ unsigned long long s[1024];
+  const int t = threadIdx.x;
+  const int per = (len + 1023) / 1024;
+  const int b = t * per, e = min(len, b + per);
+  unsigned long long acc = 0;
+  for (int i = b; i < e; i++) acc += part[i];
+  s[t] = acc;
+  __syncthreads();
+  for (int off = 1; off < 1024; off <<= 1) {
+    unsigned long long v = t >= off ? s[t - off] : 0;
+    __syncthreads();
+    s[t] += v;
+    __syncthreads();
+  }
+  unsigned long long run = t == 0 ? 0 : s[t - 1];
+  for (int i = b; i < e; i++) {
+    unsigned long long c = part[i];
+    part[i] = run;
+    run += c;
+  }
+  if (t == 1023) *total = s[1023];
+}
+
+struct EmitArgs {
+  const uint64_t *keys;
+  const uint8_t *cpl;
+  const uint8_t *leaf_level;
+  const unsigned long long *part;
+  const RootBox *root;
+  int n;
+  unsigned *cellbase;  // per position: id of the first cell it starts
+  int *level, *begin;
+  unsigned char *leaf;
+  double *cx, *cy, *region;
+  int *leaf_cell;
+};
+
+__global__ void __launch_bounds__(kScanThreads) k_emit_cells(EmitArgs a) {
+  const long base = (long)blockIdx.x * kScanTile + (long)threadIdx.x * kScanItems;
+  unsigned c[kScanItems], l[kScanItems];
+  unsigned long long mine = 0;
+#pragma unroll
+  for (int k = 0; k < kScanItems; k++) {
+    cell_counts(a.cpl, a.leaf_level, base + k, a.n, c[k], l[k]);
+    mine += ((unsigned long long)c[k] << 32) | l[k];
+  }
+  // block exclusive scan of `mine`
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  unsigned long long incl = mine;
+  for (int o = 1; o < 32; o <<= 1) {
+    unsigned long long v = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += v;
+  }
+  __shared__ unsigned long long wsum[kScanThreads / 32];
+  if (lane == 31) wsum[warp] = incl;
+  __syncthreads();
+  unsigned long long woff = 0;
+  for (int k = 0; k < warp; k++) woff += wsum[k];
+  unsigned long long run = a.part[blockIdx.x] + woff + incl - mine;
+  const double R0 = a.root->region, cx0 = a.root->cx, cy0 = a.root->cy;
+#pragma unroll 1
+  for (int k = 0; k < kScanItems; k++) {
+    long i = base + k;
+    if (i >= a.n) break;
+    unsigned cell0 = 1u + (unsigned)(run >> 32);  // root is cell 0
+    unsigned leaf0 = (unsigned)(run & 0xffffffffu);
+    a.cellbase[i] = cell0;
+    if (c[k]) {
+      int prev = i > 0 ? a.cpl[i - 1] : 0;
+      int lam = a.leaf_level[i];
+      uint64_t key = a.keys[i];
+      double cx = cx0, cy = cy0, R = R0;
+      for (int lev = 1; lev <= lam; lev++) {
+        unsigned q = (unsigned)(key >> (64 - 2 * lev)) & 3u;
+        double h = __dmul_rn(0.25, R);
+        cx = (q & 1u) ? __dadd_rn(cx, h) : __dsub_rn(cx, h);
+        cy = (q & 2u) ? __dsub_rn(cy, h) : __dadd_rn(cy, h);
+        R = __dmul_rn(0.5, R);
+        if (lev > prev) {
+          unsigned id = cell0 + (unsigned)(lev - prev - 1);
+          a.level[id] = lev;
+          a.begin[id] = (int)i;
+          a.leaf[id] = (lev == lam) ? 1 : 0;
+          a.cx[id] = cx;
+          a.cy[id] = cy;
+          a.region[id] = R;
+          if (lev == lam) a.leaf_cell[leaf0] = (int)id;
+        }
+      }
+    }
+    run += ((unsigned long long)c[k] << 32) | l[k];
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    a.level[0] = 0;
+    a.begin[0] = 0;
+    a.leaf[0] = 0;
+    a.cx[0] = cx0;
+    a.cy[0] = cy0;
+    a.region[0] = R0;
+  }
+}
+
+__global__ void __launch_bounds__(256) k_cell_end(const uint64_t *__restrict__ keys, int n, int ncell,
+                                                  const int *__restrict__ level, const int *__restrict__ begin,
+                                                  int *__restrict__ end) {
+  int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= ncell) return;
+  if (c == 0) {
+    end[0] = n;
+    return;
+  }
+  int lev = level[c];
+  int b = begin[c];
+  uint64_t k = keys[b];
+  int s = 64 - 2 * lev;
+  uint64_t hi = (s == 0) ? k : (k | ((1ull << s) - 1));
+  // first position in (b, n) whose key > hi
+  int lo = b + 1, up = n;
+  while (lo < up) {
+    int mid = lo + ((up - lo) >> 1);
+    if (keys[mid] <= hi)
+      lo = mid + 1;
+    else
+      up = mid;
+  }
+  end[c] = lo;
+}
+
+__global__ void __launch_bounds__(256) k_children(const uint64_t *__restrict__ keys, const uint8_t *__restrict__ cpl,
+                                                  const unsigned *__restrict__ cellbase, int ncell,
+                                                  const int *__restrict__ level, const int *__restrict__ begin,
+                                                  const int *__restrict__ end, const unsigned char *__restrict__ leaf,
+                                                  int *__restrict__ child) {
+  int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= ncell) return;
+  int4 ch = make_int4(-1, -1, -1, -1);
+  if (!leaf[c] && end[c] > begin[c]) {
+    int lev = level[c] + 1;
+    int pos = begin[c], e = end[c];
+    int id = c + 1;
+    for (int k = 0; k < 4 && pos < e; k++) {
+      if (k > 0) {
+        int prev = cpl[pos - 1];
+        id = (int)cellbase[pos] + (lev - prev - 1);
+      }
+      unsigned q = (unsigned)(keys[pos] >> (64 - 2 * lev)) & 3u;
+      (&ch.x)[q] = id;
+      pos = end[id];
+    }
+  }
+  reinterpret_cast<int4 *>(child)[c] = ch;
+}
+
+// One warp per leaf: blobs of the leaf in ascending original index.
+__global__ void __launch_bounds__(256) k_leaf_order(const uint32_t *__restrict__ vals, int nleaf,
+                                                    const int *__restrict__ leaf_cell, const int *__restrict__ begin,
+                                                    const int *__restrict__ end, int *__restrict__ perm) {
+  int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  int lane = threadIdx.x & 31;
+  if (wid >= nleaf) return;
+  int c = leaf_cell[wid];
+  int b = begin[c], e = end[c];
+  for (int i = b + lane; i < e; i += 32) {
+    uint32_t v = vals[i];
+    int rank = 0;
+    for (int j = b; j < e; j++) rank += vals[j] < v;
+    perm[b + rank] = (int)v;
+  }
+}
+
+__global__ void __launch_bounds__(256) k_gather(const double *__restrict__ xy, const double *__restrict__ cir,
+                                                const double *__restrict__ cor, const int *__restrict__ perm, int n,
+                                                double *x, double *y, double *c, double *r) {
+  long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  int p = perm[i];
+  x[i] = xy[2 * (long)p];
+  y[i] = xy[2 * (long)p + 1];
+  c[i] = cir[p];
+  r[i] = cor[p];
+}
+
+}  // namespace
+
+int build_tree(Workspace &ws, int n, const double *d_xy, const double *d_cir, const double *d_cor, const Params &p,
+               Tree &t, cudaStream_t s) {
+  t.n = n;
+  t.nterms = p.nterms;
+  const int ntiles = (n + kScanTile - 1) / kScanTile;
+  // ---- blob-sized buffers
+  size_t need = 0;
+  need += Arena::bytes_for(n, 8) * 4;           // x y cir cor
+  need += Arena::bytes_for(n, 4);               // perm
+  need += Arena::bytes_for(n, 8);               // keys (sorted)
+  need += Arena::bytes_for(n, 4);               // cellbase
+  need += Arena::bytes_for(1, sizeof(RootBox));
+  T2D_CUDA_TRY(ws.blob_arena.reserve(need));
+  ws.blob_arena.reset();
+  t.x = ws.blob_arena.take<double>(n);
+  t.y = ws.blob_arena.take<double>(n);
+  t.cir = ws.blob_arena.take<double>(n);
+  t.cor = ws.blob_arena.take<double>(n);
+  t.perm = ws.blob_arena.take<int>(n);
+  t.keys = ws.blob_arena.take<uint64_t>(n);
+  unsigned *cellbase = ws.blob_arena.take<unsigned>(n);
+  t.root = ws.blob_arena.take<RootBox>(1);
+
+  // ---- scratch
+  size_t tneed = 0;
+  tneed += Arena::bytes_for(n, 8) + Arena::bytes_for(n, 4) * 2;  // keys_alt, vals, vals_alt
+  tneed += Arena::bytes_for(n, 1) * 3;                          // cpl, w, leaf_level
+  tneed += radix_sort_temp_bytes(n) + 256;
+  tneed += Arena::bytes_for(kBoxBlocks, sizeof(Box4));
+  tneed += Arena::bytes_for(ntiles + 1, 8) + 256;
+  T2D_CUDA_TRY(ws.tmp_arena.reserve(tneed));
+  ws.tmp_arena.reset();
+  uint64_t *keys_alt = ws.tmp_arena.take<uint64_t>(n);
+  uint32_t *vals = ws.tmp_arena.take<uint32_t>(n);
+  uint32_t *vals_alt = ws.tmp_arena.take<uint32_t>(n);
+  uint8_t *cpl = ws.tmp_arena.take<uint8_t>(n);
+  uint8_t *w = ws.tmp_arena.take<uint8_t>(n);
+  uint8_t *leaf_level = ws.tmp_arena.take<uint8_t>(n);
+  void *sort_tmp = ws.tmp_arena.take<char>(radix_sort_temp_bytes(n));
+  Box4 *bpart = ws.tmp_arena.take<Box4>(kBoxBlocks);
+  unsigned long long *part = ws.tmp_arena.take<unsigned long long>(ntiles + 1);
+  unsigned long long *total = ws.tmp_arena.take<unsigned long long>(1);
+
+  T2D_CUDA_TRY(cudaMemsetAsync(ws.status, 0, sizeof(DevStatus), s));
+
+  // 1. root box
+  k_bbox<<<kBoxBlocks, 256, 0, s>>>(d_xy, d_cir, d_cor, n, bpart, ws.status);
+  ::t2d::g_launches.fetch_add(1, std::memory_order_relaxed);
+  k_root<<<1, 32, 0, s>>>(bpart, kBoxBlocks, t.root);
+  ::t2d::g_launches.fetch_add(1, std::memory_order_relaxed);
+  // 2. keys
+  k_keys<<<(n + 255) / 256, 256, 0, s>>>(d_xy, n, t.root, t.keys, vals);
+  ::t2d::g_launches.fetch_add(1, std::memory_order_relaxed);
+  // 3. sort
+  T2D_CUDA_TRY(radix_sort_pairs(t.keys, vals, keys_alt, vals_alt, n, 64, sort_tmp, s));
+  // 4-5. leaf levels
+  k_cpl<<<(n + 255) / 256, 256, 0, s>>>(t.keys, n, p.num_p, cpl, w);
+  ::t2d::g_launches.fetch_add(1, std::memory_order_relaxed);
+  {
+    const int H = p.num_p - 1;
+    size_t smem = 2 * (size_t)(kLLTile + H);
+    if (smem > 48 * 1024) T2D_CUDA_TRY(cudaFuncSetAttribute(k_leaf_level, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    k_leaf_level<<<(n + kLLTile - 1) / kLLTile, 256, smem, s>>>(w, n, p.num_p, leaf_level, ws.status);
+    ::t2d::g_launches.fetch_add(1, std::memory_order_relaxed);
+  }
+  // 6. counts and scan
+  k_cells_reduce<<<ntiles, kScanThreads, 0, s>>>(cpl, leaf_level, n, part);
+  ::t2d::g_launches.fetch_add(1, std::memory_order_relaxed);
+  k_scan_part<<<1, 1024, 0, s>>>(part, ntiles, total);
+  ::t2d::g_launches.fetch_add(1, std::memory_order_relaxed);
+  T2D_CUDA_TRY(cudaGetLastError());
+  T2D_CUDA_TRY(cudaMemcpyAsync(ws.h_status, ws.status, sizeof(DevStatus), cudaMemcpyDeviceToHost, s));
+  unsigned long long *h_total = reinterpret_cast<unsigned long long *>(ws.h_status + 1);
+  T2D_CUDA_TRY(cudaMemcpyAsync(h_total, total, 8, cudaMemcpyDeviceToHost, s));
+  T2D_CUDA_TRY(cudaStreamSynchronize(s));
+  if (ws.h_status->err) return ws.h_status->err;
+  unsigned long long tot = *h_total;
+  long long ncell = 1 + (long long)(tot >> 32);
+  long long nleaf = (long long)(tot & 0xffffffffu);
+  if (ncell > (1ll << 31) - 1) return TREE2D_ERR_TOO_DEEP;
+  t.ncell = (int)ncell;
+  t.nleaf = (int)nleaf;
+  t.depth = ws.h_status->depth;
+  const int nt = p.nterms;
+
+  // ---- cell-sized buffers
+  size_t cneed = 0;
+  cneed += Arena::bytes_for(ncell, 4) * 3;       // level begin end
+  cneed += Arena::bytes_for(ncell * 4, 4);       // child
+  cneed += Arena::bytes_for(ncell, 1);           // leaf
+  cneed += Arena::bytes_for(ncell, 8) * 3;       // cx cy region
+  cneed += Arena::bytes_for(nleaf, 4);           // leaf_cell
+  cneed += Arena::bytes_for(ncell * nt, 16);     // coef
+  T2D_CUDA_TRY(ws.cell_arena.reserve(cneed));
+  ws.cell_arena.reset();
+  t.level = ws.cell_arena.take<int>(ncell);
+  t.begin = ws.cell_arena.take<int>(ncell);
+  t.end = ws.cell_arena.take<int>(ncell);
+  t.child = ws.cell_arena.take<int>(ncell * 4);
+  t.leaf = ws.cell_arena.take<unsigned char>(ncell);
+  t.cx = ws.cell_arena.take<double>(ncell);
+  t.cy = ws.cell_arena.take<double>(ncell);
+  t.region = ws.cell_arena.take<double>(ncell);
+  t.leaf_cell = ws.cell_arena.take<int>(nleaf > 0 ? nleaf : 1);
+  t.coef = ws.cell_arena.take<double2>(ncell * nt);
+
+  // 7. cells
+  EmitArgs ea{t.keys, cpl, leaf_level, part, t.root, n, cellbase, t.level, t.begin, t.leaf, t.cx, t.cy, t.region,
+              t.leaf_cell};
+  k_emit_cells<<<ntiles, kScanThreads, 0, s>>>(ea);
+  ::t2d::g_launches.fetch_add(1, std::memory_order_relaxed);
+  k_cell_end<<<(t.ncell + 255) / 256, 256, 0, s>>>(t.keys, n, t.ncell, t.level, t.begin, t.end);
+  ::t2d::g_launches.fetch_add(1, std::memory_order_relaxed);
+  k_children<<<(t.ncell + 255) / 256, 256, 0, s>>>(t.keys, cpl, cellbase, t.ncell, t.level, t.begin, t.end, t.leaf,
+                                                    t.child);
+  ::t2d::g_launches.fetch_add(1, std::memory_order_relaxed);
+  // 8. in-leaf order, 9. gather
+  if (t.nleaf > 0)
+    k_leaf_order<<<(int)(((long)t.nleaf * 32 + 255) / 256), 256, 0, s>>>(vals, t.nleaf, t.leaf_cell, t.begin, t.end,
+                                                                          t.perm);
+    ::t2d::g_launches.fetch_add(1, std::memory_order_relaxed);
+  k_gather<<<(n + 255) / 256, 256, 0, s>>>(d_xy, d_cir, d_cor, t.perm, n, t.x, t.y, t.cir, t.cor);
+  ::t2d::g_launches.fetch_add(1, std::memory_order_relaxed);
+  T2D_CUDA_TRY(cudaGetLastError());
+  return TREE2D_OK;
+}
+
+int sort_targets(Workspace &ws, int n, const double *d_xy, const RootBox *d_root, int *d_order, cudaStream_t s) {
+  if (n <= 0) return TREE2D_OK;
+  size_t need = Arena::bytes_for(n, 8) * 2 + Arena::bytes_for(n, 4) + radix_sort_temp_bytes(n) + 512;
+  T2D_CUDA_TRY(ws.tmp_arena.reserve(need));
+  ws.tmp_arena.reset();
+  uint64_t *k = ws.tmp_arena.take<uint64_t>(n);
+  uint64_t *k2 = ws.tmp_arena.take<uint64_t>(n);
+  uint32_t *v2 = ws.tmp_arena.take<uint32_t>(n);
+  void *tmp = ws.tmp_arena.take<char>(radix_sort_temp_bytes(n));
+  k_keys<<<(n + 255) / 256, 256, 0, s>>>(d_xy, n, d_root, k, reinterpret_cast<uint32_t *>(d_order));
+  ::t2d::g_launches.fetch_add(1, std::memory_order_relaxed);
+  T2D_CUDA_TRY(radix_sort_pairs(k, reinterpret_cast<uint32_t *>(d_order), k2, v2, n, 64, tmp, s));
+  return TREE2D_OK;
+}
+
+}  // namespace t2d
+
+namespace t2d {
+namespace {
+__global__ void k_gather_targets(const double *__restrict__ xy, const int *__restrict__ order, int n,
+                                 double *__restrict__ tx, double *__restrict__ ty, int *__restrict__ out_idx) {
+  long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  int o = order ? order[i] : (int)i;
+  tx[i] = xy[2 * (long)o];
+  ty[i] = xy[2 * (long)o + 1];
+  out_idx[i] = o;
+}
+}  // namespace
+
+int gather_targets(int n, const double *d_xy, const int *d_order, double *tx, double *ty, int *out_idx,
+                   cudaStream_t s) {
+  if (n <= 0) return TREE2D_OK;
+  k_gather_targets<<<(n + 255) / 256, 256, 0, s>>>(d_xy, d_order, n, tx, ty, out_idx);
+  ::t2d::g_launches.fetch_add(1, std::memory_order_relaxed);
+  T2D_CUDA_TRY(cudaGetLastError());
+  return TREE2D_OK;
+}
+}  // namespace t2d

@@ -1,0 +1,87 @@
+// FP64 direct O(N*M) sum of the regularised Biot-Savart kernel: the judge
+// of the approximate modes.  The pair kernel is direct_evaluate's
+// (ver-c/src/fmm.c:121-142, r > 1e-10) applied to every source.  Sources are
+// staged through shared memory in tiles; one thread per target.
+#include "dev_common.cuh"
+
+namespace t2d {
+namespace {
+
+constexpr int kThreads = 256;
+constexpr double kPi = 3.14159265358979323846;
+
+__global__ void __launch_bounds__(kThreads) k_direct(int ntgt, const double *__restrict__ txy, int nsrc,
+                                                     const double *__restrict__ sxy, const double *__restrict__ cir,
+                                                     const double *__restrict__ cor, double *__restrict__ uv) {
+  __shared__ double sx[kThreads], sy[kThreads], sg[kThreads], sr[kThreads];
+  const long i = blockIdx.x * (long)kThreads + threadIdx.x;
+  const bool valid = i < ntgt;
+  const double x = valid ? txy[2 * i] : 0.0, y = valid ? txy[2 * i + 1] : 0.0;
+  double ax = 0.0, ay = 0.0;
+  for (int base = 0; base < nsrc; base += kThreads) {
+    const int j = base + threadIdx.x;
+    if (j < nsrc) {
+      sx[threadIdx.x] = sxy[2 * (long)j];
+      sy[threadIdx.x] = sxy[2 * (long)j + 1];
+      sg[threadIdx.x] = cir[j];
+      sr[threadIdx.x] = 1.0 / cor[j];
+    }
+    __syncthreads();
+    const int cnt = min(kThreads, nsrc - base);
+    for (int k = 0; k < cnt; k++) {
+      const double rx = x - sx[k];
+      const double ry = y - sy[k];
+      const double r2 = rx * rx + ry * ry;
+      const double r = sqrt(r2);
+      if (r > 1.0e-10) {
+        const double xai = r * sr[k];
+        const double x2 = xai * xai;
+        const double e1 = x2 > 40.0 ? 1.0 : 1.0 - exp(-x2);
+        const double rv = sg[k] * e1 / r2;
+        ax -= rv * ry;
+        ay += rv * rx;
+      }
+    }
+    __syncthreads();
+  }
+  if (valid) {
+    uv[2 * i] = 0.5 * ax / kPi;
+    uv[2 * i + 1] = 0.5 * ay / kPi;
+  }
+}
+
+// FP64 pipe throughput probe: 8 independent FMA chains per thread.
+__global__ void __launch_bounds__(256) k_dfma_probe(double *out, int iters, double b, double c) {
+  double a0 = threadIdx.x * 1e-9, a1 = a0 + 1e-3, a2 = a0 + 2e-3, a3 = a0 + 3e-3;
+  double a4 = a0 + 4e-3, a5 = a0 + 5e-3, a6 = a0 + 6e-3, a7 = a0 + 7e-3;
+  for (int i = 0; i < iters; i++) {
+    a0 = fma(a0, b, c);
+    a1 = fma(a1, b, c);
+    a2 = fma(a2, b, c);
+    a3 = fma(a3, b, c);
+    a4 = fma(a4, b, c);
+    a5 = fma(a5, b, c);
+    a6 = fma(a6, b, c);
+    a7 = fma(a7, b, c);
+  }
+  double s = a0 + a1 + a2 + a3 + a4 + a5 + a6 + a7;
+  if (s == 12345.678) out[0] = s;  // never true in practice; keeps the chains live
+}
+
+}  // namespace
+
+cudaError_t dfma_probe(double *out, int blocks, int iters, cudaStream_t s) {
+  k_dfma_probe<<<blocks, 256, 0, s>>>(out, iters, 0.999999, 1e-7);
+  ::t2d::g_launches.fetch_add(1, std::memory_order_relaxed);
+  return cudaGetLastError();
+}
+
+cudaError_t direct_sum(int ntgt, const double *txy, int nsrc, const double *sxy, const double *cir,
+                       const double *cor, double *uv, cudaStream_t s) {
+  if (ntgt <= 0) return cudaSuccess;
+  k_direct<<<(ntgt + kThreads - 1) / kThreads, kThreads, 0, s>>>(ntgt, txy, nsrc, sxy, cir, cor, uv);
+  ::t2d::g_launches.fetch_add(1, std::memory_order_relaxed);
+  return cudaGetLastError();
+}
+
+}  // namespace t2d

@@ -1,0 +1,143 @@
+// Internal interfaces shared by the translation units of libtree2d_gb300.so.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <cstddef>
+#include <cstdint>
+#include <string>
+
+#include "../../include/tree2d.h"
+
+namespace t2d {
+
+// Key depth: 2 bits per level in a 64-bit key.  A cell holding >= num_p
+// blobs at this level cannot be split further (TREE2D_ERR_TOO_DEEP).
+constexpr int kKeyLevels = 32;
+// Largest number of stored coefficients (nterms) the kernels support.
+constexpr int kMaxTerms = 32;
+
+struct Params {
+  int nterms = 0;   // stored coefficients; M2S uses nterms-1 of them
+  int num_p = 0;    // a cell with >= num_p blobs is split
+  double theta = 0;
+  double r_min = 0; // read and kept, unused (as in the reference)
+};
+
+// Root box, written on the device (quadtree.c:81-99 semantics).
+struct RootBox {
+  double cx, cy, region;
+  double xmin, xmax, ymin, ymax;
+};
+
+// Device-side status and work counters.
+struct DevStatus {
+  int err;                 // TREE2D_ERR_* (first error wins via atomicCAS)
+  int depth;               // deepest leaf level
+  unsigned long long n_m2s;
+  unsigned long long n_pairs;
+  unsigned long long n_m2l;
+  unsigned long long n_fallback;  // targets whose traversal stack overflowed
+};
+
+// Bump allocator over one device allocation.  Buffers are 256-byte aligned.
+class Arena {
+ public:
+  ~Arena();
+  // Makes sure `bytes` are available from the start; keeps the contents
+  // only if no reallocation was needed.
+  cudaError_t reserve(size_t bytes);
+  void reset() { used_ = 0; }
+  template <class T>
+  T *take(size_t count) {
+    size_t bytes = (count * sizeof(T) + 255) & ~size_t(255);
+    if (used_ + bytes > cap_) return nullptr;
+    T *p = reinterpret_cast<T *>(base_ + used_);
+    used_ += bytes;
+    return p;
+  }
+  size_t used() const { return used_; }
+  static size_t bytes_for(size_t count, size_t elem) { return (count * elem + 255) & ~size_t(255); }
+
+ private:
+  char *base_ = nullptr;
+  size_t cap_ = 0, used_ = 0;
+};
+
+// A tree on the device.  Blobs are stored in tree order (leaves in
+// depth-first quadrant order, ascending original index inside a leaf);
+// cells in depth-first pre-order with the root at 0.
+struct Tree {
+  int n = 0, ncell = 0, nleaf = 0, depth = 0, nterms = 0;
+  double *x = nullptr, *y = nullptr, *cir = nullptr, *cor = nullptr;
+  int *perm = nullptr;        // tree position -> original blob index
+  int *level = nullptr, *begin = nullptr, *end = nullptr;
+  int *child = nullptr;       // 4 per cell, quadrant order, -1 = no blob there
+  unsigned char *leaf = nullptr;
+  double *cx = nullptr, *cy = nullptr, *region = nullptr;
+  int *leaf_cell = nullptr;   // leaf ordinal -> cell id
+  int *level_start = nullptr; // host-built cell lists per level (device copy)
+  int *by_level = nullptr;    // cell ids grouped by level
+  double2 *coef = nullptr;    // ncell * nterms, FP64 Laurent coefficients
+  RootBox *root = nullptr;    // device
+  uint64_t *keys = nullptr;   // sorted keys (tree order before in-leaf sort)
+  int h_level_start[kKeyLevels + 2] = {0};
+};
+
+// Per-solver working state (one per library instance).
+struct Workspace {
+  Arena blob_arena;   // N-sized buffers
+  Arena cell_arena;   // cell-sized buffers
+  Arena tmp_arena;    // scratch (sort buffers, scans)
+  DevStatus *status = nullptr;   // device
+  DevStatus *h_status = nullptr; // pinned host mirror
+  cudaEvent_t ev[6] = {};
+  bool init = false;
+};
+
+cudaError_t workspace_init(Workspace &ws);
+
+// --- tree build (build_tree.cu) --------------------------------------
+// Builds the tree over n blobs (xy interleaved, device).  Synchronises the
+// stream once to size the cell arrays.  Returns a TREE2D status.
+int build_tree(Workspace &ws, int n, const double *d_xy, const double *d_cir, const double *d_cor,
+               const Params &p, Tree &t, cudaStream_t s);
+
+// Keys of arbitrary points against an existing root box, then sorted:
+// order[i] = index of the i-th target in key order.
+int sort_targets(Workspace &ws, int n, const double *d_xy, const RootBox *d_root, int *d_order,
+                 cudaStream_t s);
+
+// Targets in evaluation order: tx/ty[i] = xy[order[i]], out_idx[i] = order[i]
+// (order == nullptr: identity).
+int gather_targets(int n, const double *d_xy, const int *d_order, double *tx, double *ty, int *out_idx,
+                   cudaStream_t s);
+
+// --- radix sort (sort.cu) --------------------------------------------
+// Stable LSD radix sort of (key, value) pairs on bits [0, end_bit).
+// Buffers *_alt are scratch of the same size.  The result ends in keys/vals.
+size_t radix_sort_temp_bytes(int n);
+cudaError_t radix_sort_pairs(uint64_t *keys, uint32_t *vals, uint64_t *keys_alt, uint32_t *vals_alt,
+                             int n, int end_bit, void *temp, cudaStream_t s);
+
+// --- plain FP64 path (plain.cu) ---------------------------------------
+int plain_upward(Workspace &ws, const Tree &t, const Params &p, cudaStream_t s);
+// Evaluates targets (tx,ty) in the given order, writing uv[2*out_idx[i]].
+int plain_evaluate(Workspace &ws, const Tree &t, const Params &p, int ntgt, const double *tx,
+                   const double *ty, const int *out_idx, double *uv, cudaStream_t s);
+
+// --- direct sum (direct.cu) -------------------------------------------
+cudaError_t direct_sum(int ntgt, const double *txy, int nsrc, const double *sxy, const double *cir,
+                       const double *cor, double *uv, cudaStream_t s);
+
+// FP64 pipe probe: blocks x 256 threads x iters x 8 FMAs (2 flops each).
+cudaError_t dfma_probe(double *out, int blocks, int iters, cudaStream_t s);
+
+// Kernels launched by this library (for the launch count in the stats).
+extern std::atomic<long long> g_launches;
+
+// error text of the last CUDA failure (for tree2d_error_string)
+void note_cuda_error(cudaError_t e, const char *what);
+
+}  // namespace t2d

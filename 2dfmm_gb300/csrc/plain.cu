@@ -1,0 +1,262 @@
+// Plain FP64 treecode on the device: the reference's numerics
+// (ver-c/src/fmm.c) with GPU-shaped control flow.
+//
+//  k_s2m       one warp per leaf, lane k owns coefficient k; blobs are
+//              summed in the leaf's order (ascending original index), the
+//              order fmm.c:24-29 sums them; powers by a warp product scan.
+//  k_m2m       one warp per internal cell of one level, deepest level first;
+//              children in quadrant order 3,2,1,0 (fmm.c:41-56); the
+//              level-1 -> root shift is skipped as in the reference.
+//  k_eval      one warp per 32 consecutive targets (tree order, so the warp's
+//              targets are neighbours).  The warp walks the UNION of its
+//              lanes' traversals with a shared LIFO of (cell, lane mask):
+//              restricted to one lane, the visit order is that lane's own
+//              LIFO order in fmm.c:90-112, so every lane accumulates M2S and
+//              direct terms in the reference's order.  The opening test uses
+//              round-to-nearest FP64 operations without contraction
+//              (r = sqrt(dx*dx + dy*dy); region > theta*r), so each lane
+//              takes exactly the reference's branch.  M2S (fmm.c:60-67) is
+//              evaluated by Horner in w = 1/(z - zc); P2P is fmm.c:121-142.
+#include "dev_common.cuh"
+
+namespace t2d {
+namespace {
+
+__constant__ double c_binom[kMaxTerms][kMaxTerms];
+
+constexpr double kPi = 3.14159265358979323846;
+
+__global__ void __launch_bounds__(256) k_s2m(Tree t, int nt) {
+  const int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (wid >= t.nleaf) return;
+  const int c = t.leaf_cell[wid];
+  const int b = t.begin[c], e = t.end[c];
+  const double cx = t.cx[c], cy = t.cy[c];
+  double2 acc = make_double2(0.0, 0.0);
+  for (int j = b; j < e; j++) {
+    double2 z = make_double2(t.x[j] - cx, t.y[j] - cy);
+    double2 pw = warp_powers(z, lane);
+    double g = t.cir[j];
+    acc.x += g * pw.x;
+    acc.y += g * pw.y;
+  }
+  if (lane < nt) t.coef[(size_t)c * nt + lane] = acc;
+}
+
+__global__ void __launch_bounds__(256) k_zero_internal(Tree t, int nt) {
+  long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (i >= (long)t.ncell * nt) return;
+  int c = (int)(i / nt);
+  if (!t.leaf[c]) t.coef[i] = make_double2(0.0, 0.0);
+}
+
+__global__ void __launch_bounds__(256) k_m2m(Tree t, int nt, int lev) {
+  const int p = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (p >= t.ncell) return;
+  if (t.level[p] != lev || t.leaf[p]) return;
+  const double px = t.cx[p], py = t.cy[p];
+  double2 acc = make_double2(0.0, 0.0);
+  const int4 ch = reinterpret_cast<const int4 *>(t.child)[p];
+  for (int q = 3; q >= 0; q--) {
+    const int c = (&ch.x)[q];
+    if (c < 0) continue;
+    // -(z_p - z_c), fmm.c:50
+    double2 dz = make_double2(t.cx[c] - px, t.cy[c] - py);
+    double2 pw = warp_powers(dz, lane);
+    double2 a = lane < nt ? t.coef[(size_t)c * nt + lane] : make_double2(0.0, 0.0);
+    double2 s = make_double2(0.0, 0.0);
+    for (int k = 0; k < nt; k++) {
+      double2 ak = shfl_d2(a, k);
+      double2 pk = shfl_d2(pw, (lane - k) & 31);
+      if (k <= lane) {
+        double bin = c_binom[lane & (kMaxTerms - 1)][k];
+        s = cadd(s, cmul(make_double2(ak.x * bin, ak.y * bin), pk));
+      }
+    }
+    acc = cadd(acc, s);
+  }
+  if (lane < nt) t.coef[(size_t)p * nt + lane] = acc;
+}
+
+constexpr int kEvalWarps = 4;
+constexpr int kStackCap = 160;
+
+struct EvalArgs {
+  Tree t;
+  int nt;
+  double theta;
+  int ntgt;
+  const double *tx, *ty;
+  const int *out_idx;
+  double *uv;
+  DevStatus *st;
+};
+
+__global__ void __launch_bounds__(kEvalWarps * 32) k_eval(EvalArgs a) {
+  __shared__ int s_cell[kEvalWarps][kStackCap];
+  __shared__ unsigned s_mask[kEvalWarps][kStackCap];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const long i = ((long)blockIdx.x * kEvalWarps + warp) * 32 + lane;
+  const bool valid = i < a.ntgt;
+  const unsigned vmask = __ballot_sync(0xffffffffu, valid);
+  if (vmask == 0) return;
+  const Tree &t = a.t;
+  const int nt = a.nt;
+  const double x = valid ? a.tx[i] : 0.0, y = valid ? a.ty[i] : 0.0;
+  const double theta = a.theta;
+  double2 phi = make_double2(0.0, 0.0);
+  double ud0 = 0.0, ud1 = 0.0;
+  unsigned long long n_m2s = 0, n_pairs = 0;
+  bool overflow = false;
+
+  int top = 0;
+  if (lane == 0) {
+    s_cell[warp][0] = 0;
+    s_mask[warp][0] = vmask;
+  }
+  __syncwarp();
+  while (top >= 0) {
+    const int c = s_cell[warp][top];
+    const unsigned m = s_mask[warp][top];
+    __syncwarp();
+    top--;
+    const bool act = (m >> lane) & 1u;
+    if (t.leaf[c]) {
+      // direct_evaluate, fmm.c:121-142
+      const int b = t.begin[c], e = t.end[c];
+      if (act) {
+        double ax = 0.0, ay = 0.0;
+        for (int j = b; j < e; j++) {
+          const double rx = __dsub_rn(x, t.x[j]);
+          const double ry = __dsub_rn(y, t.y[j]);
+          const double r = __dsqrt_rn(__dadd_rn(__dmul_rn(rx, rx), __dmul_rn(ry, ry)));
+          if (r > 1.0e-10) {
+            const double rv2 = 1.0 / __dmul_rn(r, r);
+            const double xai = r / t.cor[j];
+            const double x2 = __dmul_rn(xai, xai);
+            // 1 - exp(-x2) rounds to exactly 1.0 once exp(-x2) < 2^-54
+            // (x2 > 37.4); the shortcut keeps the result bit-identical.
+            const double e1 = x2 > 40.0 ? 1.0 : 1.0 - exp(-x2);
+            const double rv = t.cir[j] * e1;
+            ax -= rv * ry * rv2;
+            ay += rv * rx * rv2;
+          }
+        }
+        ud0 += 0.5 * ax / kPi;
+        ud1 += 0.5 * ay / kPi;
+        n_pairs += (unsigned long long)(e - b);
+      }
+    } else {
+      const int4 ch = reinterpret_cast<const int4 *>(t.child)[c];
+#pragma unroll 1
+      for (int q = 0; q < 4; q++) {
+        const int cc = (&ch.x)[q];
+        if (cc < 0) continue;
+        const double ccx = t.cx[cc], ccy = t.cy[cc], creg = t.region[cc];
+        bool desc = false;
+        double dx = 0.0, dy = 0.0;
+        if (act) {
+          dx = __dsub_rn(x, ccx);
+          dy = __dsub_rn(y, ccy);
+          const double r = __dsqrt_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)));
+          desc = creg > __dmul_rn(theta, r);
+        }
+        const unsigned dmask = __ballot_sync(0xffffffffu, desc);
+        if (act && !desc && nt >= 2) {
+          // M2S, fmm.c:60-67: sum_{k<nt-1} a_k w^{k+1}, w = 1/(z - zc)
+          const double d2 = dx * dx + dy * dy;
+          const double inv = 1.0 / d2;
+          const double2 w = make_double2(dx * inv, -dy * inv);
+          const double2 *cf = t.coef + (size_t)cc * nt;
+          double2 acc = cf[nt - 2];
+          for (int k = nt - 3; k >= 0; k--) acc = cadd(cmul(acc, w), cf[k]);
+          phi = cadd(phi, cmul(acc, w));
+        }
+        if (act && !desc) n_m2s++;
+        if (dmask) {
+          if (top + 1 >= kStackCap) {
+            overflow = true;
+            break;
+          }
+          top++;
+          if (lane == 0) {
+            s_cell[warp][top] = cc;
+            s_mask[warp][top] = dmask;
+          }
+        }
+        __syncwarp();
+      }
+      if (__any_sync(0xffffffffu, overflow)) break;
+    }
+  }
+  if (__any_sync(0xffffffffu, overflow)) {
+    if (lane == 0) set_err(a.st, TREE2D_ERR_TIMEOUT);
+  }
+  if (valid) {
+    // fmm.c:115-117
+    const double pre = (0.5 * -phi.y) / kPi;
+    const double pim = (0.5 * phi.x) / kPi;
+    const double u = -pre + ud0;
+    const double v = pim + ud1;
+    const long o = a.out_idx ? a.out_idx[i] : i;
+    a.uv[2 * o] = overflow ? NAN : u;
+    a.uv[2 * o + 1] = overflow ? NAN : v;
+  }
+  for (int o = 16; o; o >>= 1) {
+    n_m2s += __shfl_xor_sync(0xffffffffu, n_m2s, o);
+    n_pairs += __shfl_xor_sync(0xffffffffu, n_pairs, o);
+  }
+  if (lane == 0) {
+    atomicAdd(&a.st->n_m2s, n_m2s);
+    atomicAdd(&a.st->n_pairs, n_pairs);
+  }
+}
+
+bool g_binom_ready = false;
+
+cudaError_t upload_binom() {
+  if (g_binom_ready) return cudaSuccess;
+  static double h[kMaxTerms][kMaxTerms];
+  for (int n = 0; n < kMaxTerms; n++) {
+    h[n][0] = 1.0;
+    for (int k = 1; k < kMaxTerms; k++) h[n][k] = k > n ? 0.0 : h[n][k - 1] * (double)(n - k + 1) / (double)k;
+  }
+  // exact: every C(n,k), n < 32, is an integer below 2^53 and the running
+  // product above stays integral (C(n,k-1)*(n-k+1) is divisible by k).
+  cudaError_t e = cudaMemcpyToSymbol(c_binom, h, sizeof(h));
+  if (e == cudaSuccess) g_binom_ready = true;
+  return e;
+}
+
+}  // namespace
+
+int plain_upward(Workspace &ws, const Tree &t, const Params &p, cudaStream_t s) {
+  T2D_CUDA_TRY(upload_binom());
+  const int nt = p.nterms;
+  long tot = (long)t.ncell * nt;
+  if (tot == 0) return TREE2D_OK;
+  k_zero_internal<<<(int)((tot + 255) / 256), 256, 0, s>>>(t, nt);
+  ::t2d::g_launches.fetch_add(1, std::memory_order_relaxed);
+  if (t.nleaf > 0) k_s2m<<<(int)(((long)t.nleaf * 32 + 255) / 256), 256, 0, s>>>(t, nt);
+  ::t2d::g_launches.fetch_add(1, std::memory_order_relaxed);
+  const int blocks = (int)(((long)t.ncell * 32 + 255) / 256);
+  for (int lev = t.depth - 1; lev >= 1; lev--) k_m2m<<<blocks, 256, 0, s>>>(t, nt, lev);
+  ::t2d::g_launches.fetch_add(1, std::memory_order_relaxed);
+  T2D_CUDA_TRY(cudaGetLastError());
+  return TREE2D_OK;
+}
+
+int plain_evaluate(Workspace &ws, const Tree &t, const Params &p, int ntgt, const double *tx, const double *ty,
+                   const int *out_idx, double *uv, cudaStream_t s) {
+  if (ntgt <= 0) return TREE2D_OK;
+  EvalArgs a{t, p.nterms, p.theta, ntgt, tx, ty, out_idx, uv, ws.status};
+  const int warps = (ntgt + 31) / 32;
+  k_eval<<<(warps + kEvalWarps - 1) / kEvalWarps, kEvalWarps * 32, 0, s>>>(a);
+  ::t2d::g_launches.fetch_add(1, std::memory_order_relaxed);
+  T2D_CUDA_TRY(cudaGetLastError());
+  return TREE2D_OK;
+}
+
+}  // namespace t2d

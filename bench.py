@@ -1,0 +1,365 @@
+#!/usr/bin/env python3
+"""Benchmark: target evaluations per second of the vortex-blob treecode.
+
+Workload (default): 4,194,304 blobs -- two Gaussian patches (45% + 45%,
+std 0.05, centres (0.4,0.5)/(0.6,0.5), Gamma = |N(0,1)|) and a perturbed
+shear sheet (10%, y = 0.2 + 0.01 sin(8 pi x), Gamma = -1/N_sheet), stored
+FP32, sigma 0.001, p = 12 (nterms 13), theta 0.5, at most 64 blobs per leaf;
+every blob is a target.  Inputs are seeded synthetic data (there is no
+public dataset for this path).
+
+A step is one whole solve: tree build, upward pass and evaluation at all
+targets.  `value` times the device-resident call (inputs already in HBM,
+CUDA events on the launching stream, L2 flushed between steps); `e2e`
+times the reference-facing calls with host buffers (make_tree + one batch
+of biot_tree answers), copies included.  `cpu_baseline` times the CPU
+oracle (the reference's algorithm restated in C) on the host cores on a
+bounded sample.  `--impl reference` times that CPU implementation alone.
+
+Run:  python bench.py [--gpus N --steps K --warmup W] [--impl reference]
+"""
+from __future__ import annotations
+
+import argparse
+import importlib
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "target evals/s at 4M blobs (two patches + sheet), all blobs as targets"
+UNIT = "targets/s"
+MODES = {"plain": 0, "mixed": 1, "learned": 2}
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--mode", default="plain", choices=list(MODES))
+    ap.add_argument("--workload", default="two_patch_sheet", choices=["two_patch_sheet", "lamb_oseen", "uniform"])
+    ap.add_argument("--n", type=int, default=0, help="override the blob count (exploration only)")
+    ap.add_argument("--err-targets", type=int, default=4096)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-sample", type=int, default=0, help="targets per CPU step (0: auto)")
+    return ap.parse_args()
+
+
+def workload(args, rank=0):
+    W = importlib.import_module("2dfmm_gb300.workloads")
+    if args.workload == "two_patch_sheet":
+        kw = {"n": args.n} if args.n else {}
+        return W.two_patch_sheet(seed=3 + rank, **kw), "two_patch_sheet_4M" if not args.n else f"two_patch_sheet_{args.n}"
+    if args.workload == "lamb_oseen":
+        kw = {"n": args.n} if args.n else {}
+        return W.lamb_oseen(seed=2 + rank, **kw), "lamb_oseen_1M" if not args.n else f"lamb_oseen_{args.n}"
+    kw = {"n": args.n} if args.n else {}
+    return W.uniform(seed=1 + rank, **kw), "uniform_20k" if not args.n else f"uniform_{args.n}"
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+# --------------------------------------------------------------------------
+# clocks during the timed region
+
+class Clocks:
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.path = tempfile.mktemp(suffix=".csv")
+        self.proc = None
+        self.gpu = gpu_index
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        rows = []
+        try:
+            for line in open(self.path):
+                f = [x.strip() for x in line.split(",")]
+                if len(f) >= 9 and f[1].replace(".", "").isdigit():
+                    rows.append(f)
+        except OSError:
+            pass
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"], "samples": 0}
+        sm = [float(r[1]) for r in rows]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": float(rows[0][2]), "reasons": reasons,
+                "samples": len(rows), "power_w_max": max(float(r[3]) for r in rows if r[3] not in ("[N/A]", ""))}
+
+
+# --------------------------------------------------------------------------
+# CPU baseline: the oracle (the reference's algorithm, restated in C)
+
+def mem_available_gb():
+    try:
+        for line in open("/proc/meminfo"):
+            if line.startswith("MemAvailable:"):
+                return int(line.split()[1]) / 1e6
+    except OSError:
+        pass
+    return 0.0
+
+
+def cpu_reference(b, depth_hint, steps, warmup, sample, threads=0):
+    """Times the oracle on `b`: make_tree once (single-threaded, as the
+    reference), then `steps` batches of `sample` sampled targets over all
+    host threads.  Returns (targets/s projected to the whole job, detail)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O  # noqa: WPS433
+    W = importlib.import_module("2dfmm_gb300.workloads")
+    threads = threads or O.max_threads()
+    # the reference's dense complete tree: (4^(L+1)-1)/3 nodes of ~56 B, plus
+    # one num_nodes-int traversal stack per concurrent biot_tree call
+    nodes = (4 ** (depth_hint + 1) - 1) // 3
+    need_gb = nodes * 56 / 1e9 + 1.2 * b.n * 64 / 1e9
+    per_thread_gb = nodes * 4 / 1e9
+    avail = mem_available_gb()
+    if avail and need_gb + per_thread_gb > 0.7 * avail:
+        return None, {"unavailable": f"dense reference tree needs {need_gb:.1f} GB, {avail:.1f} GB available"}
+    if avail:
+        threads = max(1, min(threads, int((0.7 * avail - need_gb) / max(per_thread_gb, 1e-9))))
+    o = O.Oracle(b.nterms, b.num_p, b.theta)
+    t0 = time.perf_counter()
+    o.make_tree(b.xy, b.cir, b.cor, max_level_cap=30)
+    t_make = time.perf_counter() - t0
+    if not sample:
+        # aim for ~2 s per step
+        probe = W.sample_targets(b.n, threads, seed=99)
+        t0 = time.perf_counter()
+        o.biot(b.xy[probe], threads=threads)
+        per = (time.perf_counter() - t0) / threads
+        sample = int(max(threads, min(200_000, 2.0 * threads / max(per, 1e-9))))
+        sample -= sample % threads
+    times = []
+    for k in range(warmup + steps):
+        idx = W.sample_targets(b.n, sample, seed=100 + k)
+        t0 = time.perf_counter()
+        o.biot(b.xy[idx], threads=threads)
+        dt = time.perf_counter() - t0
+        if k >= warmup:
+            times.append(dt)
+    per_target = statistics.median(times) / sample
+    value = b.n / (t_make + b.n * per_target)
+    detail = {"make_tree_s": round(t_make, 3), "biot_tree_s_per_target_per_job": per_target,
+              "sample": f"make_tree over all {b.n} blobs (1 thread, as the reference), then {steps} batches of "
+                        f"{sample} sampled targets over {threads} threads; value = N / (t_make + N * t_target)",
+              "cores": threads, "levels": o.levels()}
+    return value, detail
+
+
+# --------------------------------------------------------------------------
+
+def roofline_traffic():
+    """DRAM bytes per launch of the evaluation kernel from the committed ncu
+    summary (profiles/), or None."""
+    path = os.path.join(ROOT, "profiles", "traffic.json")
+    try:
+        with open(path) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    b, wname = workload(args)
+    depth_hint = {"two_patch_sheet": 14, "lamb_oseen": 10, "uniform": 6}[args.workload]
+    value, det = cpu_reference(b, depth_hint, args.steps, args.warmup, args.cpu_sample)
+    line = {"metric": METRIC, "impl": "reference", "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "higher_is_better": True, "dtype": "f64", "data": "synthetic (seeded)",
+            "config": {"workload": wname, "n_blobs": b.n, "nterms": b.nterms, "num_p": b.num_p, "theta": b.theta}}
+    if value is None:
+        line.update({"value": None, "unavailable": det["unavailable"]})
+    else:
+        line.update({"value": value, "ms_per_step": 1e3 * b.n / value,
+                     "cpu_baseline": {"value": value, "unit": UNIT, "cores": det["cores"], "kind": "port",
+                                      "sample": det["sample"]},
+                     "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+                     "detail": det})
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import torch
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    P = importlib.import_module("2dfmm_gb300")
+    P.load()
+    b, wname = workload(args, rank)
+    P.set_params(b.nterms, b.num_p, b.theta)
+    P.set_mode(MODES[args.mode])
+    n = b.n
+    xy = torch.from_numpy(b.xy).to(dev).contiguous()
+    cir = torch.from_numpy(b.cir).to(dev)
+    cor = torch.from_numpy(b.cor).to(dev)
+    uv = torch.empty((n, 2), dtype=torch.float64, device=dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)  # > 129 MB L2
+    stream = torch.cuda.current_stream()
+    sp = stream.cuda_stream
+
+    def solve():
+        P.solve_device(xy.data_ptr(), cir.data_ptr(), cor.data_ptr(), uv.data_ptr(), n, sp)
+
+    for _ in range(args.warmup):
+        solve()
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    times, st_list = [], []
+    with Clocks(local) as clk:
+        for _ in range(args.steps):
+            flush.fill_(1)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            e0.record(stream)
+            solve()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            times.append(e0.elapsed_time(e1))
+            st_list.append(P.stats())
+    total_ms = float(sum(times))
+    if world > 1:
+        t = torch.tensor([total_ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = world * n * args.steps / (total_ms * 1e-3)
+    st = st_list[-1]
+    ms_eval = statistics.mean(s["ms_eval"] for s in st_list)
+
+    # roofline of the dominant kernel (the evaluation kernel)
+    p = b.nterms - 1
+    flops = st["n_m2s"] * (8 * p + 10) + st["n_pairs"] * 20
+    achieved = flops / (ms_eval * 1e-3) / 1e12
+    peak = P.fp64_peak_tflops(stream=sp)
+    tr = roofline_traffic().get(f"{args.mode}:{wname}")
+    roofline = {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+                "traffic": tr, "kernel": "k_eval (traversal + M2S + P2P, FP64)",
+                "peak_source": "measured on this GPU by the library's DFMA probe (tree2d_fp64_probe)",
+                "algorithmic_flops_per_launch": flops, "ms_per_launch": ms_eval}
+
+    # accuracy against the FP64 direct sum (outside the timed region)
+    W = importlib.import_module("2dfmm_gb300.workloads")
+    idx = W.sample_targets(n, args.err_targets, seed=7)
+    tidx = torch.from_numpy(idx).to(dev)
+    txy = xy[tidx].contiguous()
+    ref = torch.empty_like(txy)
+    P.direct_device(txy.data_ptr(), len(idx), xy.data_ptr(), cir.data_ptr(), cor.data_ptr(), n, ref.data_ptr(), sp)
+    torch.cuda.synchronize()
+    got = uv[tidx]
+    rel_l2 = float(torch.linalg.norm(got - ref) / torch.linalg.norm(ref))
+    max_rel = float(((got - ref).norm(dim=1) / ref.norm(dim=1).clamp_min(1e-300)).max())
+
+    # end to end through the reference-facing calls, host buffers
+    h_xy = torch.empty((n, 2), dtype=torch.float64, pin_memory=True)
+    h_cir = torch.empty(n, dtype=torch.float64, pin_memory=True)
+    h_cor = torch.empty(n, dtype=torch.float64, pin_memory=True)
+    h_xy.numpy()[:] = b.xy
+    h_cir.numpy()[:] = b.cir
+    h_cor.numpy()[:] = b.cor
+    e2e_times = []
+    e2e_steps = max(1, min(args.steps, 3))
+    for k in range(1 + e2e_steps):
+        t0 = time.perf_counter()
+        P.make_tree(h_xy.numpy(), h_cir.numpy(), h_cor.numpy())
+        out = P.biot_tree_batch(h_xy.numpy())
+        dt = time.perf_counter() - t0
+        if k >= 1:
+            e2e_times.append(dt)
+    e2e_t = statistics.mean(e2e_times)
+    if world > 1:
+        t = torch.tensor([e2e_t], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_t = float(t.item())
+    e2e_match = bool(np.array_equal(out, uv.cpu().numpy()))
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        v, det = cpu_reference(b, st["depth"], 1, 0, args.cpu_sample)
+        if v is None:
+            cpu = {"value": None, "unit": UNIT, "cores": 0, "kind": "port", "sample": det["unavailable"]}
+        else:
+            cpu = {"value": v, "unit": UNIT, "cores": det["cores"], "kind": "port", "sample": det["sample"],
+                   "make_tree_s": det["make_tree_s"]}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.mode == "plain" else "f32+bf16/tf32",
+            "data": "synthetic (seeded numpy PCG64), shapes and distributions of the configuration",
+            "config": {"workload": wname, "n_blobs": n, "targets": "all blobs", "nterms": b.nterms,
+                       "p": b.nterms - 1, "num_p": b.num_p, "theta": b.theta, "mode": args.mode,
+                       "parallelism": f"replicas x{world} (independent blob sets, no collective)",
+                       "l2": "flushed between steps (256 MiB write); inputs 134 MB > L2"},
+            "gpu_launches": int(sum(s["n_launches"] for s in st_list)),
+            "e2e": {"value": world * n / e2e_t, "unit": UNIT, "h2d_bytes_per_step": n * 32,
+                    "d2h_bytes_per_step": n * 16, "api": "make_tree + biot_tree_batch (host buffers)",
+                    "matches_device_path": e2e_match},
+            "roofline": roofline,
+            "accuracy": {"relL2_vs_fp64_direct": rel_l2, "max_rel_vs_fp64_direct": max_rel,
+                         "targets": len(idx)},
+            "stages_ms": {"build": statistics.mean(s["ms_build"] for s in st_list),
+                          "upward": statistics.mean(s["ms_upward"] for s in st_list), "eval": ms_eval},
+            "tree": {"cells": st["n_cells"], "leaves": st["n_leaves"], "depth": st["depth"],
+                     "m2s_per_target": st["n_m2s"] / n, "pairs_per_target": st["n_pairs"] / n},
+            "clocks": clk.summary(),
+        }
+        if cpu is not None:
+            line["cpu_baseline"] = cpu
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

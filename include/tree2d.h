@@ -1,0 +1,142 @@
+/*
+ * tree2d.h -- C ABI of the GB300 vortex-blob treecode (libtree2d_gb300.so).
+ *
+ * Drop-in replacement for the reference's two entry points and the Fortran
+ * bind(C) interface that calls them:
+ *
+ *   make_tree  <- ver-c/src/quadtree.c:102-171 (declared quadtree.h:38-41)
+ *   biot_tree  <- ver-c/src/fmm.c:69-118       (declared fmm.h:7)
+ *   Fortran    <- ver-c/src/m_tree_bindc.f90:1-17 (module m_tree_bindc)
+ *
+ * All other symbols are additive extensions; a caller written for the
+ * reference needs none of them.  All functions use plain C types; there are
+ * no CUDA or library types in any signature (streams are passed as void*).
+ *
+ * Threading: make_tree and the tree2d_* calls that change state must not
+ * run concurrently with any other call.  biot_tree and biot_tree_batch may
+ * be called from several threads at once after make_tree returned.
+ */
+#ifndef TREE2D_GB300_H
+#define TREE2D_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------ */
+/* Reference entry points                                              */
+
+/* Builds the tree over nvor_b vortex blobs and evaluates the velocity at
+ * every blob position.  vor_b holds x,y interleaved per blob (C
+ * double[nvor_b][2] == Fortran vor_b(2,nvor_b)); cir_b the circulations,
+ * cor_b the core radii.  Inputs are copied; the caller may reuse them at
+ * once.  Parameters come from ../cal_cond/fmm_param.dat relative to the
+ * working directory, as in the reference (quadtree.c:12-27), unless
+ * tree2d_set_params() fixed them.  Replaces quadtree.c:102 make_tree.
+ * Errors: none returned (the reference returns void); see
+ * tree2d_last_error().  After a failed call biot_tree returns NaN. */
+void make_tree(int nvor_b, const double *vor_b, const double *cir_b, const double *cor_b);
+
+/* Velocity (u,v) induced at (x,y) by the blobs of the last make_tree.
+ * Replaces fmm.c:69 biot_tree.  Positions equal (bit for bit) to a blob
+ * position are answered from the velocities make_tree computed; any other
+ * point is evaluated on the GPU by the same traversal.  Without a valid
+ * tree, u and v are set to NaN. */
+void biot_tree(double x, double y, double *u, double *v);
+
+/* ------------------------------------------------------------------ */
+/* Extensions                                                          */
+
+/* Status codes (tree2d_last_error). */
+#define TREE2D_OK 0
+#define TREE2D_ERR_PARAM_FILE 1    /* parameter file missing and no override      */
+#define TREE2D_ERR_BAD_PARAMS 2    /* nterms < 2, nterms > 32, num_p < 2, theta<=0 */
+#define TREE2D_ERR_BAD_INPUT 3     /* n < 0, or non-finite position/cir/cor        */
+#define TREE2D_ERR_TOO_DEEP 4      /* >= num_p blobs share one cell at level 32    */
+#define TREE2D_ERR_CUDA 5          /* CUDA runtime or kernel failure               */
+#define TREE2D_ERR_NO_TREE 6       /* evaluation requested before a valid tree     */
+#define TREE2D_ERR_NO_DEVICE 7     /* no CUDA device                               */
+#define TREE2D_ERR_TIMEOUT 8       /* a bounded device loop gave up                */
+#define TREE2D_ERR_MODE 9          /* unknown mode                                 */
+
+/* Evaluation modes (tree2d_set_mode). */
+#define TREE2D_MODE_PLAIN 0        /* FP64 treecode, reference semantics             */
+#define TREE2D_MODE_MIXED 1        /* scaled FP32 FMM, tensor-core M2L, FP64 final sum */
+#define TREE2D_MODE_LEARNED 2      /* MIXED with learned per-interaction order         */
+
+int tree2d_last_error(void);
+const char *tree2d_error_string(int code);
+
+/* Fixes the parameters (nterms = stored coefficients, num_p = leaf split
+ * threshold, theta = opening angle, r_min unused as in the reference) so
+ * that make_tree no longer reads the parameter file.  Returns a status. */
+int tree2d_set_params(int nterms, int num_p, double theta, double r_min);
+/* Returns make_tree to reading ../cal_cond/fmm_param.dat. */
+void tree2d_clear_params(void);
+/* Reads the parameters in force (after the last make_tree). */
+void tree2d_get_params(int *nterms, int *num_p, double *theta, double *r_min);
+
+int tree2d_set_mode(int mode);
+int tree2d_get_mode(void);
+
+/* Evaluates n targets (xy interleaved, host memory) into uv (interleaved,
+ * host memory) against the last make_tree.  Blob positions are answered
+ * from the precomputed velocities, the rest in one GPU launch.  Returns a
+ * status; on error uv is filled with NaN. */
+int biot_tree_batch(int n, const double *xy, double *uv);
+
+/* Device-resident solve: builds the tree over n blobs whose arrays are in
+ * device memory (xy interleaved f64, cir f64, cor f64) and writes the
+ * velocity at every blob position into d_uv (interleaved, original blob
+ * order), all on `stream` (a cudaStream_t, or NULL for the legacy default
+ * stream).  Uses the parameters and mode in force.  It does not change the
+ * state seen by biot_tree.  Returns a status. */
+int tree2d_solve_device(int n, const double *d_xy, const double *d_cir, const double *d_cor,
+                        double *d_uv, void *stream);
+
+/* Statistics of the last solve (make_tree or tree2d_solve_device). */
+typedef struct {
+  long long n_blobs;
+  long long n_cells;      /* non-empty cells, root included          */
+  long long n_leaves;
+  int depth;              /* deepest leaf level                      */
+  int mode;
+  long long n_m2s;        /* accepted (target, cell) pairs            */
+  long long n_pairs;      /* direct (target, source) pairs            */
+  long long n_m2l;        /* M2L (target cell, source cell) pairs     */
+  double ms_build;        /* device time of the tree build            */
+  double ms_upward;       /* S2M + M2M                                */
+  double ms_eval;         /* evaluation at the targets                */
+  double ms_total;
+  long long n_launches;   /* kernels launched by the solve            */
+} tree2d_stats_t;
+int tree2d_get_stats(tree2d_stats_t *out);
+
+/* Copies the tree of the last make_tree to host arrays, for inspection and
+ * parity tests.  perm[n_blobs] receives the original blob index of each
+ * position in tree order.  Cell arrays (cap entries each; pass cap=0 to
+ * query the count) describe the non-empty cells below the root in
+ * depth-first pre-order, quadrants 0..3: level, [begin,end) in tree order,
+ * leaf flag, centre and side length, and the nterms complex coefficients
+ * (re,im interleaved) after M2M.  Returns the number of cells, or -1. */
+long long tree2d_export_tree(int *perm, long long cap, int *level, int *begin, int *end, int *leaf,
+                             double *cx, double *cy, double *region, double *coef);
+
+/* FP64 direct O(N*M) sum of the regularised kernel (the judge of the
+ * approximate modes): targets and sources in device memory. */
+int tree2d_direct_device(int ntgt, const double *d_txy, int nsrc, const double *d_sxy,
+                         const double *d_cir, const double *d_cor, double *d_uv, void *stream);
+
+/* Measures the FP64 FMA pipe: runs blocks x 256 threads x iters x 8
+ * dependent-chain FMAs on `stream` and returns the elapsed device time in
+ * milliseconds through *ms (flops = blocks*256*iters*16).  A measurement
+ * helper for roofline reporting; no counterpart in the reference. */
+int tree2d_fp64_probe(int blocks, int iters, void *stream, double *ms);
+
+/* Library version string. */
+const char *tree2d_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

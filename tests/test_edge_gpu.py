@@ -1,0 +1,70 @@
+"""Edge cases on the GPU: empty and one-blob sets, invalid input, trees
+that cannot be built, parameter override versus file."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from conftest import load_golden
+
+
+@pytest.mark.gpu
+def test_empty_set(gpu_lib):
+    P = gpu_lib
+    P.set_params(11, 33, 0.5)
+    P.make_tree(np.zeros((0, 2)), np.zeros(0), np.zeros(0))
+    assert P.biot_tree(0.3, 0.4) == (0.0, 0.0)
+
+
+@pytest.mark.gpu
+def test_non_finite_input_is_rejected(gpu_lib):
+    P = gpu_lib
+    P.set_params(11, 33, 0.5)
+    xy = np.random.default_rng(0).random((100, 2))
+    xy[17, 0] = np.nan
+    rc = P.make_tree(xy, np.ones(100), np.ones(100), check=False)
+    assert rc == P.ERR_BAD_INPUT
+    u, v = P.biot_tree(0.5, 0.5)
+    assert np.isnan(u) and np.isnan(v)
+
+
+@pytest.mark.gpu
+def test_too_many_coincident_blobs(gpu_lib):
+    """num_p blobs at one point can never be separated: the reference grows
+    its max level forever; the library reports TREE2D_ERR_TOO_DEEP."""
+    P = gpu_lib
+    P.set_params(11, 33, 0.5)
+    xy = np.random.default_rng(1).random((200, 2))
+    xy[:40] = xy[0]
+    rc = P.make_tree(xy, np.ones(200), np.ones(200), check=False)
+    assert rc == P.ERR_TOO_DEEP
+    # a valid call afterwards works again
+    g = load_golden("u2k")
+    P.make_tree(g["xy"], g["cir"], g["cor"])
+    assert np.isfinite(P.biot_tree(0.5, 0.5)).all()
+
+
+@pytest.mark.gpu
+def test_tiny_sets_and_leaf_threshold(gpu_lib):
+    P = gpu_lib
+    for name in ("tiny1", "tiny2", "tiny32", "tiny33"):
+        g = load_golden(name)
+        P.set_params(int(g["nterms"]), int(g["num_p"]), float(g["theta"]))
+        P.make_tree(g["xy"], g["cir"], g["cor"])
+        uv = P.biot_tree_batch(g["txy"])
+        assert np.allclose(uv, g["uv"], rtol=1e-12, atol=1e-300), name
+
+
+@pytest.mark.gpu
+def test_param_file_drives_make_tree(gpu_lib, tmp_path, monkeypatch):
+    P = gpu_lib
+    g = load_golden("u2k")
+    (tmp_path / "cal_cond").mkdir()
+    (tmp_path / "run").mkdir()
+    (tmp_path / "cal_cond" / "fmm_param.dat").write_text(
+        f"{int(g['nterms'])}    nterms\n{int(g['num_p'])}   num_p\n{float(g['theta'])}d0 theta\n0.01  r_min ! for Tree\n")
+    monkeypatch.chdir(tmp_path / "run")
+    P.clear_params()
+    P.make_tree(g["xy"], g["cir"], g["cor"])
+    uv = P.biot_tree_batch(g["txy"])
+    assert np.abs(uv - g["uv"]).max() <= 1e-12 * np.abs(g["uv"]).max()
