@@ -29,6 +29,7 @@ Arena::~Arena() {
 
 cudaError_t Arena::reserve(size_t bytes) {
   if (bytes <= cap_) return cudaSuccess;
+  if (fixed_) return cudaErrorMemoryAllocation;
   if (base_) cudaFree(base_);
   base_ = nullptr;
   cap_ = 0;

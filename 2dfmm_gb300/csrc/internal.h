@@ -46,8 +46,16 @@ class Arena {
  public:
   ~Arena();
   // Makes sure `bytes` are available from the start; keeps the contents
-  // only if no reallocation was needed.
+  // only if no reallocation was needed.  An arena attached to caller-owned
+  // memory never allocates: it fails with cudaErrorMemoryAllocation instead.
   cudaError_t reserve(size_t bytes);
+  // Uses [base, base+cap) as the arena's memory (owned by the caller).
+  void attach(void *base, size_t cap) {
+    base_ = static_cast<char *>(base);
+    cap_ = cap;
+    used_ = 0;
+    fixed_ = true;
+  }
   void reset() { used_ = 0; }
   template <class T>
   T *take(size_t count) {
@@ -63,6 +71,7 @@ class Arena {
  private:
   char *base_ = nullptr;
   size_t cap_ = 0, used_ = 0;
+  bool fixed_ = false;
 };
 
 // A tree on the device.  Blobs are stored in tree order (leaves in

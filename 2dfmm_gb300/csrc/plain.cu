@@ -214,10 +214,15 @@ __global__ void __launch_bounds__(kEvalWarps * 32) k_eval(EvalArgs a) {
   }
 }
 
-bool g_binom_ready = false;
+// Binomial table, uploaded once per device (the table lives in each
+// device's copy of the module).
+bool g_binom_ready[64] = {};
 
 cudaError_t upload_binom() {
-  if (g_binom_ready) return cudaSuccess;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev >= 0 && dev < 64 && g_binom_ready[dev]) return cudaSuccess;
   static double h[kMaxTerms][kMaxTerms];
   for (int n = 0; n < kMaxTerms; n++) {
     h[n][0] = 1.0;
@@ -225,8 +230,8 @@ cudaError_t upload_binom() {
   }
   // exact: every C(n,k), n < 32, is an integer below 2^53 and the running
   // product above stays integral (C(n,k-1)*(n-k+1) is divisible by k).
-  cudaError_t e = cudaMemcpyToSymbol(c_binom, h, sizeof(h));
-  if (e == cudaSuccess) g_binom_ready = true;
+  e = cudaMemcpyToSymbol(c_binom, h, sizeof(h));
+  if (e == cudaSuccess && dev >= 0 && dev < 64) g_binom_ready[dev] = true;
   return e;
 }
 
