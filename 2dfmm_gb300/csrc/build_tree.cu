@@ -420,6 +420,7 @@ int build_tree(Workspace &ws, int n, const double *d_xy, const double *d_cir, co
   need += Arena::bytes_for(n, 4);               // perm
   need += Arena::bytes_for(n, 8);               // keys (sorted)
   need += Arena::bytes_for(n, 4);               // cellbase
+  need += Arena::bytes_for(n, 1) * 2;           // cpl, leaf_level
   need += Arena::bytes_for(1, sizeof(RootBox));
   T2D_CUDA_TRY(ws.blob_arena.reserve(need));
   ws.blob_arena.reset();
@@ -430,12 +431,17 @@ int build_tree(Workspace &ws, int n, const double *d_xy, const double *d_cir, co
   t.perm = ws.blob_arena.take<int>(n);
   t.keys = ws.blob_arena.take<uint64_t>(n);
   unsigned *cellbase = ws.blob_arena.take<unsigned>(n);
+  uint8_t *cpl = ws.blob_arena.take<uint8_t>(n);
+  uint8_t *leaf_level = ws.blob_arena.take<uint8_t>(n);
   t.root = ws.blob_arena.take<RootBox>(1);
+  t.cpl = cpl;
+  t.leaf_level = leaf_level;
+  t.cellbase = cellbase;
 
   // ---- scratch
   size_t tneed = 0;
   tneed += Arena::bytes_for(n, 8) + Arena::bytes_for(n, 4) * 2;  // keys_alt, vals, vals_alt
-  tneed += Arena::bytes_for(n, 1) * 3;                          // cpl, w, leaf_level
+  tneed += Arena::bytes_for(n, 1);                              // w
   tneed += radix_sort_temp_bytes(n) + 256;
   tneed += Arena::bytes_for(kBoxBlocks, sizeof(Box4));
   tneed += Arena::bytes_for(ntiles + 1, 8) + 256;
@@ -444,9 +450,7 @@ int build_tree(Workspace &ws, int n, const double *d_xy, const double *d_cir, co
   uint64_t *keys_alt = ws.tmp_arena.take<uint64_t>(n);
   uint32_t *vals = ws.tmp_arena.take<uint32_t>(n);
   uint32_t *vals_alt = ws.tmp_arena.take<uint32_t>(n);
-  uint8_t *cpl = ws.tmp_arena.take<uint8_t>(n);
   uint8_t *w = ws.tmp_arena.take<uint8_t>(n);
-  uint8_t *leaf_level = ws.tmp_arena.take<uint8_t>(n);
   void *sort_tmp = ws.tmp_arena.take<char>(radix_sort_temp_bytes(n));
   Box4 *bpart = ws.tmp_arena.take<Box4>(kBoxBlocks);
   unsigned long long *part = ws.tmp_arena.take<unsigned long long>(ntiles + 1);

@@ -56,6 +56,7 @@ class Arena {
     used_ = 0;
     fixed_ = true;
   }
+
   void reset() { used_ = 0; }
   template <class T>
   T *take(size_t count) {
@@ -91,7 +92,9 @@ struct Tree {
   double2 *coef = nullptr;    // ncell * nterms, FP64 Laurent coefficients
   RootBox *root = nullptr;    // device
   uint64_t *keys = nullptr;   // sorted keys (tree order before in-leaf sort)
-  int h_level_start[kKeyLevels + 2] = {0};
+  uint8_t *cpl = nullptr;     // per position: levels shared with the next key
+  uint8_t *leaf_level = nullptr;  // per position: level of its leaf
+  unsigned *cellbase = nullptr;   // per position: id of the first cell it starts
 };
 
 // Per-solver working state (one per library instance).
