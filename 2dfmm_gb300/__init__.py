@@ -23,14 +23,15 @@ LIB_PATH = os.path.join(HERE, "libtree2d_gb300.so")
 
 OK = 0
 ERR_PARAM_FILE, ERR_BAD_PARAMS, ERR_BAD_INPUT, ERR_TOO_DEEP, ERR_CUDA, ERR_NO_TREE, ERR_NO_DEVICE, ERR_TIMEOUT, \
-    ERR_MODE = range(1, 10)
+    ERR_MODE, ERR_TOO_LARGE = range(1, 11)
+STATIC_MAX_BLOBS = 65536
 MODE_PLAIN, MODE_MIXED, MODE_LEARNED = 0, 1, 2
 
 # Every symbol include/tree2d.h declares.
 EXPORTS = [
     "make_tree", "biot_tree", "tree2d_last_error", "tree2d_error_string", "tree2d_set_params",
     "tree2d_clear_params", "tree2d_get_params", "tree2d_set_mode", "tree2d_get_mode", "biot_tree_batch",
-    "tree2d_solve_device", "tree2d_get_stats", "tree2d_export_tree", "tree2d_direct_device", "tree2d_fp64_probe", "tree2d_version",
+    "tree2d_solve_device", "tree2d_solve_device_static", "tree2d_get_stats", "tree2d_export_tree", "tree2d_direct_device", "tree2d_fp64_probe", "tree2d_version",
 ]
 
 
@@ -92,6 +93,9 @@ def load(path: str | None = None):
     L.tree2d_solve_device.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                       ctypes.c_void_p, ctypes.c_void_p]
     L.tree2d_solve_device.restype = ctypes.c_int
+    L.tree2d_solve_device_static.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                             ctypes.c_void_p, ctypes.c_void_p]
+    L.tree2d_solve_device_static.restype = ctypes.c_int
     L.tree2d_get_stats.argtypes = [ctypes.POINTER(Stats)]
     L.tree2d_get_stats.restype = ctypes.c_int
     L.tree2d_export_tree.argtypes = [_ip, ctypes.c_longlong, _ip, _ip, _ip, _ip, _dp, _dp, _dp, _dp]
@@ -187,6 +191,12 @@ def biot_tree_batch(xy, check: bool = True):
 def solve_device(d_xy: int, d_cir: int, d_cor: int, d_uv: int, n: int, stream: int = 0):
     """Device-resident solve over raw device pointers (ints)."""
     _check(load().tree2d_solve_device(n, d_xy, d_cir, d_cor, d_uv, stream or None), "solve_device")
+
+
+def solve_device_static(d_xy: int, d_cir: int, d_cor: int, d_uv: int, n: int, stream: int = 0) -> int:
+    """The no-allocation variant of solve_device (scratch in a fixed device
+    array; n <= STATIC_MAX_BLOBS).  Returns the status."""
+    return load().tree2d_solve_device_static(n, d_xy, d_cir, d_cor, d_uv, stream or None)
 
 
 def direct_device(d_txy: int, ntgt: int, d_sxy: int, d_cir: int, d_cor: int, nsrc: int, d_uv: int, stream: int = 0):

@@ -29,7 +29,10 @@ Arena::~Arena() {
 
 cudaError_t Arena::reserve(size_t bytes) {
   if (bytes <= cap_) return cudaSuccess;
-  if (fixed_) return cudaErrorMemoryAllocation;
+  if (fixed_) {
+    overflowed_ = true;
+    return cudaErrorMemoryAllocation;
+  }
   if (base_) cudaFree(base_);
   base_ = nullptr;
   cap_ = 0;
@@ -308,6 +311,20 @@ int eval_points(Lib &L, int m, const double *xy, double *uv) {
 }
 
 }  // namespace
+
+// Parameters in force for a device solve (as tree2d_solve_device resolves
+// them), taken under the library lock.
+int params_for_device_solve(Params &out) {
+  Lib &L = lib();
+  std::lock_guard<std::mutex> lk(L.mu);
+  int rc = resolve_params(L);
+  if (rc) return fail(rc);
+  out = L.params;
+  return TREE2D_OK;
+}
+
+int record_error(int code) { return fail(code); }
+
 }  // namespace t2d
 
 using namespace t2d;
@@ -458,6 +475,8 @@ const char *tree2d_error_string(int code) {
     case TREE2D_ERR_NO_DEVICE: return "no CUDA device";
     case TREE2D_ERR_TIMEOUT: return "a bounded device loop gave up (traversal stack overflow)";
     case TREE2D_ERR_MODE: return "unknown or unavailable mode";
+    case TREE2D_ERR_TOO_LARGE:
+      return "input larger than the fixed scratch of tree2d_solve_device_static (65536 blobs, 32 MiB)";
     default: return "unknown error";
   }
 }

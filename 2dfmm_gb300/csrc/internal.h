@@ -56,7 +56,8 @@ class Arena {
     used_ = 0;
     fixed_ = true;
   }
-
+  // True once reserve() was refused on attached memory.
+  bool overflowed() const { return overflowed_; }
   void reset() { used_ = 0; }
   template <class T>
   T *take(size_t count) {
@@ -73,6 +74,7 @@ class Arena {
   char *base_ = nullptr;
   size_t cap_ = 0, used_ = 0;
   bool fixed_ = false;
+  bool overflowed_ = false;
 };
 
 // A tree on the device.  Blobs are stored in tree order (leaves in
@@ -145,6 +147,11 @@ cudaError_t direct_sum(int ntgt, const double *txy, int nsrc, const double *sxy,
 
 // FP64 pipe probe: blocks x 256 threads x iters x 8 FMAs (2 flops each).
 cudaError_t dfma_probe(double *out, int blocks, int iters, cudaStream_t s);
+
+// Parameters for a device solve, resolved under the library lock.
+int params_for_device_solve(Params &out);
+// Stores `code` as the library's last error and returns it.
+int record_error(int code);
 
 // Kernels launched by this library (for the launch count in the stats).
 extern std::atomic<long long> g_launches;

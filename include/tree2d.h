@@ -58,6 +58,7 @@ void biot_tree(double x, double y, double *u, double *v);
 #define TREE2D_ERR_NO_DEVICE 7     /* no CUDA device                               */
 #define TREE2D_ERR_TIMEOUT 8       /* a bounded device loop gave up                */
 #define TREE2D_ERR_MODE 9          /* unknown mode                                 */
+#define TREE2D_ERR_TOO_LARGE 10    /* beyond the fixed scratch of the static solve */
 
 /* Evaluation modes (tree2d_set_mode). */
 #define TREE2D_MODE_PLAIN 0        /* FP64 treecode, reference semantics             */
@@ -93,6 +94,22 @@ int biot_tree_batch(int n, const double *xy, double *uv);
  * state seen by biot_tree.  Returns a status. */
 int tree2d_solve_device(int n, const double *d_xy, const double *d_cir, const double *d_cor,
                         double *d_uv, void *stream);
+
+/* Same solve as tree2d_solve_device (plain mode), for callers that cannot
+ * allocate GPU memory: a host program whose device memory belongs to a pool
+ * it must not go around, or an embedding that fixes its memory footprint at
+ * start-up.  The call allocates nothing: all scratch lives in one 32 MiB
+ * file-scope device array per GPU, resident until the process exits.  The
+ * caller still passes inputs and outputs.  Limits: n <= 65536 blobs and as
+ * many cells as fit in the array; beyond that it returns
+ * TREE2D_ERR_TOO_LARGE.  Every call shares the array and it keeps the last
+ * call's contents (what the solve reads it clears first); calls that
+ * overlap on the GPU race, so do not run two at once on different streams.
+ * The first call on a device looks up the array's device address; make it
+ * before any stream capture.  It returns after its work on `stream` is done.
+ * No counterpart in the reference. */
+int tree2d_solve_device_static(int n, const double *d_xy, const double *d_cir, const double *d_cor,
+                               double *d_uv, void *stream);
 
 /* Statistics of the last solve (make_tree or tree2d_solve_device). */
 typedef struct {
