@@ -185,14 +185,18 @@ def cpu_reference(b, depth_hint, steps, warmup, sample, threads=0):
 # --------------------------------------------------------------------------
 
 def roofline_traffic():
-    """DRAM bytes per launch of the evaluation kernel from the committed ncu
-    summary (profiles/), or None."""
-    path = os.path.join(ROOT, "profiles", "traffic.json")
+    """DRAM bytes per launch of each mode's dominant kernel, from the
+    committed ncu summary (profiles/dram_traffic.txt)."""
+    out = {}
     try:
-        with open(path) as f:
-            return json.load(f)
-    except (OSError, ValueError):
-        return {}
+        with open(os.path.join(ROOT, "profiles", "dram_traffic.txt")) as f:
+            for line in f:
+                if line.strip() and not line.startswith("#"):
+                    parts = line.split()
+                    out[parts[0]] = int(parts[1])
+    except (OSError, ValueError, IndexError):
+        pass
+    return out
 
 
 def run_reference(args):
