@@ -30,7 +30,7 @@ MODE_PLAIN, MODE_MIXED, MODE_LEARNED = 0, 1, 2
 # Every symbol include/tree2d.h declares.
 EXPORTS = [
     "make_tree", "biot_tree", "tree2d_last_error", "tree2d_error_string", "tree2d_set_params",
-    "tree2d_clear_params", "tree2d_get_params", "tree2d_set_mode", "tree2d_get_mode", "biot_tree_batch",
+    "tree2d_clear_params", "tree2d_get_params", "tree2d_set_mode", "tree2d_get_mode", "tree2d_set_mixed_params", "biot_tree_batch",
     "tree2d_solve_device", "tree2d_solve_device_static", "tree2d_get_stats", "tree2d_export_tree", "tree2d_direct_device", "tree2d_fp64_probe", "tree2d_version",
 ]
 
@@ -88,6 +88,8 @@ def load(path: str | None = None):
     L.tree2d_set_mode.argtypes = [ctypes.c_int]
     L.tree2d_set_mode.restype = ctypes.c_int
     L.tree2d_get_mode.restype = ctypes.c_int
+    L.tree2d_set_mixed_params.argtypes = [ctypes.c_int, ctypes.c_double, ctypes.c_int]
+    L.tree2d_set_mixed_params.restype = ctypes.c_int
     L.biot_tree_batch.argtypes = [ctypes.c_int, _dp, _dp]
     L.biot_tree_batch.restype = ctypes.c_int
     L.tree2d_solve_device.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
@@ -148,6 +150,10 @@ def get_params():
 
 def set_mode(mode: int):
     _check(load().tree2d_set_mode(mode), "set_mode")
+
+
+def set_mixed_params(pterms: int = 16, cutoff_sigmas: float = 4.0, use_tensor_cores: bool = True):
+    _check(load().tree2d_set_mixed_params(pterms, cutoff_sigmas, int(use_tensor_cores)), "set_mixed_params")
 
 
 def get_mode() -> int:

@@ -19,6 +19,7 @@
 #include <vector>
 
 #include "dev_common.cuh"
+#include "mixed.h"
 
 namespace t2d {
 
@@ -72,6 +73,7 @@ namespace {
 struct Solver {
   Workspace ws;
   Tree tree;
+  bool plain_coef = false;  // FP64 coefficients present (plain upward ran)
   Arena io;       // device copies of host inputs and outputs
   Arena targets;  // evaluation-order targets
 };
@@ -82,6 +84,7 @@ struct Lib {
   bool have_params = false;
   bool params_fixed = false;
   int mode = TREE2D_MODE_PLAIN;
+  MixedParams mixed;
   std::atomic<int> last_error{0};
   cudaStream_t stream = nullptr;
   bool stream_ready = false;
@@ -182,11 +185,19 @@ int solve(Lib &L, Solver &S, int n, const double *d_xy, const double *d_cir, con
   int rc = build_tree(ws, n, d_xy, d_cir, d_cor, L.params, S.tree, s);
   if (rc) return rc;
   T2D_CUDA_TRY(cudaEventRecord(ws.ev[1], s));
-  rc = plain_upward(ws, S.tree, L.params, s);
-  if (rc) return rc;
-  T2D_CUDA_TRY(cudaEventRecord(ws.ev[2], s));
-  rc = plain_evaluate(ws, S.tree, L.params, n, S.tree.x, S.tree.y, S.tree.perm, d_uv, s);
-  if (rc) return rc;
+  S.plain_coef = false;
+  if (L.mode == TREE2D_MODE_PLAIN) {
+    rc = plain_upward(ws, S.tree, L.params, s);
+    if (rc) return rc;
+    S.plain_coef = true;
+    T2D_CUDA_TRY(cudaEventRecord(ws.ev[2], s));
+    rc = plain_evaluate(ws, S.tree, L.params, n, S.tree.x, S.tree.y, S.tree.perm, d_uv, s);
+    if (rc) return rc;
+  } else {
+    T2D_CUDA_TRY(cudaEventRecord(ws.ev[2], s));
+    rc = mixed_solve(ws, S.tree, L.mixed, d_uv, s, st);
+    if (rc) return rc;
+  }
   T2D_CUDA_TRY(cudaEventRecord(ws.ev[3], s));
   T2D_CUDA_TRY(cudaMemcpyAsync(ws.h_status, ws.status, sizeof(DevStatus), cudaMemcpyDeviceToHost, s));
   T2D_CUDA_TRY(cudaStreamSynchronize(s));
@@ -293,6 +304,13 @@ int eval_points(Lib &L, int m, const double *xy, double *uv) {
   int *out = S.targets.take<int>(m);
   T2D_CUDA_TRY(cudaMemcpyAsync(d_xy, xy, sizeof(double) * 2 * (size_t)m, cudaMemcpyHostToDevice, s));
   int rc;
+  if (!S.plain_coef) {
+    // Points off the blobs are answered by the plain FP64 treecode; after a
+    // mixed-mode make_tree its FP64 coefficients are formed on first need.
+    rc = plain_upward(S.ws, S.tree, L.params, s);
+    if (rc) return rc;
+    S.plain_coef = true;
+  }
   if (m > 1024) {
     rc = sort_targets(S.ws, m, d_xy, S.tree.root, order, s);
     if (rc) return rc;
@@ -515,12 +533,23 @@ void tree2d_get_params(int *nterms, int *num_p, double *theta, double *r_min) {
 int tree2d_set_mode(int mode) {
   Lib &L = lib();
   std::lock_guard<std::mutex> lk(L.mu);
-  if (mode != TREE2D_MODE_PLAIN) return fail(TREE2D_ERR_MODE);
+  if (mode != TREE2D_MODE_PLAIN && mode != TREE2D_MODE_MIXED) return fail(TREE2D_ERR_MODE);
   L.mode = mode;
   return TREE2D_OK;
 }
 
 int tree2d_get_mode(void) { return lib().mode; }
+
+int tree2d_set_mixed_params(int pterms, double cutoff_sigmas, int use_tensor_cores) {
+  Lib &L = lib();
+  std::lock_guard<std::mutex> lk(L.mu);
+  if (pterms < 2 || pterms > kMaxP || !(cutoff_sigmas >= 0.0) || !std::isfinite(cutoff_sigmas))
+    return fail(TREE2D_ERR_BAD_PARAMS);
+  L.mixed.pterms = pterms;
+  L.mixed.cutoff = cutoff_sigmas;
+  L.mixed.use_tensor_cores = use_tensor_cores ? 1 : 0;
+  return TREE2D_OK;
+}
 
 int tree2d_solve_device(int n, const double *d_xy, const double *d_cir, const double *d_cor, double *d_uv,
                         void *stream) {

@@ -25,6 +25,13 @@ struct Params {
   double r_min = 0; // read and kept, unused (as in the reference)
 };
 
+// Parameters of the mixed-precision form.
+struct MixedParams {
+  int pterms = 16;        // expansion length P (terms 0..P-1) of multipole and local
+  double cutoff = 4.0;    // regularisation correction radius, in units of max sigma
+  int use_tensor_cores = 1;
+};
+
 // Root box, written on the device (quadtree.c:81-99 semantics).
 struct RootBox {
   double cx, cy, region;
@@ -104,6 +111,10 @@ struct Workspace {
   Arena blob_arena;   // N-sized buffers
   Arena cell_arena;   // cell-sized buffers
   Arena tmp_arena;    // scratch (sort buffers, scans)
+  Arena mx_arena;     // mixed form: per-cell and per-position arrays
+  Arena mx_lists;     // mixed form: interaction lists
+  Arena mx_tables;    // mixed form: translation operators
+  int mx_tables_P = 0;
   DevStatus *status = nullptr;   // device
   DevStatus *h_status = nullptr; // pinned host mirror
   cudaEvent_t ev[6] = {};

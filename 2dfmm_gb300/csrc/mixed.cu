@@ -1,0 +1,880 @@
+// Mixed-precision FMM on the device (TREE2D_MODE_MIXED).
+//
+// The tree is the plain path's (same FP64 keys, same cells).  On it runs an
+// adaptive FMM (Carrier-Greengard-Rokhlin lists) for the point-vortex part
+// of the kernel, plus a short-range correction for the blob regularisation:
+//
+//   U(B)  leaf B: leaves adjacent to B (any level)       -> P2P, regularised
+//   V(C)  cell C: children of parent(C)'s colleagues not
+//         adjacent to C; 27 fixed offsets per child class -> M2L (dense
+//         contraction over all cells of a class, m2l.cu)
+//   W(B)  leaf B: descendants of B's colleagues not adjacent
+//         to B whose parent is adjacent                    -> M2P at B's targets
+//   X(C)  cell C: leaves coarser than C, adjacent to
+//         parent(C), not adjacent to C                     -> P2L into C
+//   K(B)  leaf B: leaves not adjacent to B whose box lies
+//         within rc of B's box (rc = cutoff * max sigma)   -> Gaussian correction
+//                                                             -G e^{-r^2/s^2}/r^2
+//
+// The far field treats blobs as point vortices; the exact kernel differs
+// from that by -G exp(-r^2/sigma^2)/r, which K(B) adds back for every pair
+// closer than rc that is not already a direct (U) pair.
+//
+// Expansions are scaled by the cell side h so coefficients stay O(1):
+//   multipole  phi(z) = (1/h) sum_k  a_k ((z - zc)/h)^-(k+1)
+//   local      psi(z) = (1/h) sum_l  b_l ((z - zc)/h)^l
+// With that scaling every translation operator is level independent:
+//   M2M/L2L: 4 matrices (child quadrant), M2L: 4 classes x 27 offsets.
+// Formulas: M2L b_l = sum_k a_k (-1)^l C(k+l,l) tau^-(k+l+1) (the Laurent
+// re-expansion of ver-fortran/src/fmm.f90:104-139, written for the C
+// path's convention phi = sum_j G_j/(z - z_j), u = Im phi/2pi, v = Re phi/2pi
+// of ver-c/src/fmm.c:115-117); L2L b'_k = sum_{l>=k} b_l C(l,k) s^(l-k)
+// (ver-fortran/src/fmm.f90:142-168); L2P = Horner (fmm.f90:198-206).
+//
+// Arithmetic: FP32 throughout (positions as FP32 offsets from their leaf
+// centre, formed from the FP64 centres), compensated (Kahan) sums for the
+// direct and correction terms, FP64 for the final per-target reduction.
+#include <cmath>
+#include <vector>
+
+#include "dev_common.cuh"
+#include "mixed.h"
+
+namespace t2d {
+namespace {
+
+constexpr float kInv2Pi = 0.15915494309189535f;
+
+// ---------------------------------------------------------------- lookups
+
+struct Found {
+  int kind;  // 0 empty, 1 cell at the requested level, 2 coarser leaf
+  int id;
+};
+
+__device__ __forceinline__ uint64_t interleave(unsigned jx, unsigned jy, int lev) {
+  uint64_t p = 0;
+  for (int i = lev - 1; i >= 0; i--) p = (p << 2) | ((jx >> i) & 1u) | (((jy >> i) & 1u) << 1);
+  return p;
+}
+
+// The tree cell covering grid position (jx, jy) of level `lev`.
+__device__ Found find_cell(const MixedView &m, int lev, unsigned jx, unsigned jy) {
+  const int n = m.n;
+  const uint64_t P = interleave(jx, jy, lev);
+  const int sh = 64 - 2 * lev;
+  const uint64_t Pk = sh >= 64 ? 0 : (P << sh);
+  int lo = 0, up = n;
+  while (lo < up) {
+    int mid = lo + ((up - lo) >> 1);
+    if (m.keys[mid] < Pk)
+      lo = mid + 1;
+    else
+      up = mid;
+  }
+  const int pos = lo;
+  if (pos < n && (sh >= 64 ? 0 : (m.keys[pos] >> sh)) == P) {
+    int lam = m.leaf_level[pos];
+    if (lam >= lev) {
+      int prev = pos > 0 ? m.cpl[pos - 1] : 0;
+      return {1, (int)m.cellbase[pos] + (lev - prev - 1)};
+    }
+    return {2, m.leaf_of[pos]};
+  }
+  int best = -1, nb = -1;
+  if (pos > 0) {
+    int c = min(common_levels(Pk, m.keys[pos - 1]), lev - 1);
+    if (c > best) best = c, nb = pos - 1;
+  }
+  if (pos < n) {
+    int c = min(common_levels(Pk, m.keys[pos]), lev - 1);
+    if (c > best) best = c, nb = pos;
+  }
+  if (nb >= 0 && m.leaf_level[nb] <= best) return {2, m.leaf_of[nb]};
+  return {0, -1};
+}
+
+// Boxes of cells a (level la) and b (level lb) touch or overlap.
+__device__ __forceinline__ bool adjacent(int la, unsigned ax, unsigned ay, int lb, unsigned bx, unsigned by) {
+  if (la > lb) {
+    int t = la;
+    la = lb;
+    lb = t;
+    unsigned u = ax;
+    ax = bx;
+    bx = u;
+    u = ay;
+    ay = by;
+    by = u;
+  }
+  const long long s = 1ll << (lb - la);
+  const long long x0 = (long long)ax * s, y0 = (long long)ay * s;
+  return (long long)bx >= x0 - 1 && (long long)bx <= x0 + s && (long long)by >= y0 - 1 && (long long)by <= y0 + s;
+}
+
+__device__ __forceinline__ bool adj_cells(const MixedView &m, int a, int b) {
+  return adjacent(m.level[a], m.ix[a], m.iy[a], m.level[b], m.ix[b], m.iy[b]);
+}
+
+// ------------------------------------------------------------ cell setup
+
+__global__ void k_cell_info(MixedView m) {
+  int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= m.ncell) return;
+  int lev = m.level[c];
+  uint64_t k = m.keys[m.begin[c]];
+  unsigned ix = 0, iy = 0;
+  for (int i = 1; i <= lev; i++) {
+    unsigned q = (unsigned)(k >> (64 - 2 * i)) & 3u;
+    ix = (ix << 1) | (q & 1u);
+    iy = (iy << 1) | (q >> 1);
+  }
+  m.ix[c] = ix;
+  m.iy[c] = iy;
+  m.h[c] = (float)m.region[c];
+  m.inv_h[c] = (float)(1.0 / m.region[c]);
+}
+
+// Per leaf: leaf_of for its positions, FP32 local coordinates, circulation,
+// 1/sigma^2.
+__global__ void k_leaf_setup(MixedView m, const double *x, const double *y, const double *cir, const double *cor) {
+  const int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (wid >= m.nleaf) return;
+  const int c = m.leaf_cell[wid];
+  const double cx = m.cx[c], cy = m.cy[c];
+  for (int i = m.begin[c] + lane; i < m.end[c]; i += 32) {
+    m.leaf_of[i] = c;
+    m.loc[i] = make_float2((float)(x[i] - cx), (float)(y[i] - cy));
+    m.gam[i] = (float)cir[i];
+    double s = cor[i];
+    m.s2inv[i] = (float)(1.0 / (s * s));
+  }
+}
+
+// Same-level 3x3 neighbourhood of every cell: exact cells and coarser leaves.
+__global__ void k_colleagues(MixedView m) {
+  int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= m.ncell) return;
+  const int lev = m.level[c];
+  const long long side = 1ll << lev;
+  for (int k = 0; k < 9; k++) {
+    int dx = k % 3 - 1, dy = k / 3 - 1;
+    long long jx = (long long)m.ix[c] + dx, jy = (long long)m.iy[c] + dy;
+    int ex = -1, co = -1;
+    if (lev >= 1 && jx >= 0 && jy >= 0 && jx < side && jy < side) {
+      if (dx == 0 && dy == 0) {
+        ex = c;
+      } else {
+        Found f = find_cell(m, lev, (unsigned)jx, (unsigned)jy);
+        if (f.kind == 1) ex = f.id;
+        if (f.kind == 2) co = f.id;
+      }
+    }
+    m.coll[c * 9 + k] = ex;
+    m.coarse[c * 9 + k] = co;
+  }
+}
+
+__constant__ signed char c_slot[4][6][6];  // [class][dy+2+qy][dx+2+qx] -> slot (or -1)
+
+// V and X lists of every cell of level >= 2.
+__global__ void k_vx_lists(MixedView m) {
+  int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= m.ncell) return;
+  int *V = m.vlist + (size_t)c * 27;
+  int *X = m.xlist + (size_t)c * 8;
+  for (int s = 0; s < 27; s++) V[s] = -1;
+  for (int s = 0; s < 8; s++) X[s] = -1;
+  const int lev = m.level[c];
+  if (lev < 2) return;
+  const int p = m.parent[c];
+  const unsigned ix = m.ix[c], iy = m.iy[c];
+  const int qx = ix & 1, qy = iy & 1, cls = qx + 2 * qy;
+  int nx = 0, nv = 0;
+  for (int k = 0; k < 9; k++) {
+    if (k == 4) continue;
+    const int e = m.coll[p * 9 + k];
+    if (e >= 0) {
+      if (m.leaf[e]) {
+        if (!adj_cells(m, e, c)) X[nx++] = e;
+      } else {
+        const int4 ch = reinterpret_cast<const int4 *>(m.child)[e];
+        for (int q = 0; q < 4; q++) {
+          const int cc = (&ch.x)[q];
+          if (cc < 0) continue;
+          int jx = (int)(2 * m.ix[e] + (q & 1)), jy = (int)(2 * m.iy[e] + (q >> 1));
+          int dx = jx - (int)ix, dy = jy - (int)iy;
+          if (abs(dx) <= 1 && abs(dy) <= 1) continue;
+          int s = c_slot[cls][dy + 2 + qy][dx + 2 + qx];
+          if (s >= 0) {
+            V[s] = cc;
+            nv++;
+          }
+        }
+      }
+    }
+    const int co = m.coarse[p * 9 + k];
+    if (co >= 0 && !adj_cells(m, co, c)) {
+      bool dup = false;
+      for (int j = 0; j < nx; j++) dup |= X[j] == co;
+      if (!dup) X[nx++] = co;
+    }
+  }
+  if (nv) atomicAdd(&m.st->n_m2l, (unsigned long long)nv);
+}
+
+// rc = cutoff * max sigma (sigma >= 0 as floats order like their bits).
+__global__ void k_sigma_max(const double *cor, int n, unsigned *out) {
+  float mx = 0.f;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+    mx = fmaxf(mx, (float)fabs(cor[i]));
+  for (int o = 16; o; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(out, __float_as_uint(mx));
+}
+
+__global__ void k_cutoff(unsigned *bits, float cutoff) {
+  float s = __uint_as_float(*bits);
+  float rc = cutoff * s * 1.0001f;  // slack for the FP32 rounding of sigma
+  *reinterpret_cast<float *>(bits) = isfinite(rc) ? rc : 0.f;
+}
+
+__global__ void k_parent(MixedView m) {
+  int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= m.ncell) return;
+  if (m.leaf[c]) return;
+  const int4 ch = reinterpret_cast<const int4 *>(m.child)[c];
+  for (int q = 0; q < 4; q++)
+    if ((&ch.x)[q] >= 0) m.parent[(&ch.x)[q]] = c;
+}
+
+// U and W lists of one leaf.  `emit(kind, id)` with kind 0 = U, 1 = W.
+template <class Emit>
+__device__ void uw_walk(const MixedView &m, int b, Emit emit) {
+  const int lev = m.level[b];
+  int coarse_seen[8];
+  int ncs = 0;
+  int stack[4 * kKeyLevels + 8];
+  for (int k = 0; k < 9; k++) {
+    const int co = m.coarse[b * 9 + k];
+    if (co >= 0) {
+      bool dup = false;
+      for (int j = 0; j < ncs; j++) dup |= coarse_seen[j] == co;
+      if (!dup) {
+        coarse_seen[ncs++] = co;
+        emit(0, co);
+      }
+    }
+    const int e = m.coll[b * 9 + k];
+    if (e < 0) continue;
+    if (m.leaf[e]) {
+      emit(0, e);
+      continue;
+    }
+    int top = 0;
+    stack[top++] = e;
+    while (top > 0) {
+      const int c = stack[--top];
+      const int4 ch = reinterpret_cast<const int4 *>(m.child)[c];
+      for (int q = 0; q < 4; q++) {
+        const int cc = (&ch.x)[q];
+        if (cc < 0) continue;
+        if (adjacent(lev, m.ix[b], m.iy[b], m.level[cc], m.ix[cc], m.iy[cc])) {
+          if (m.leaf[cc])
+            emit(0, cc);
+          else if (top < 4 * kKeyLevels + 8)
+            stack[top++] = cc;
+        } else {
+          emit(1, cc);
+        }
+      }
+    }
+  }
+}
+
+__device__ __forceinline__ float box_gap(const MixedView &m, int a, int b) {
+  double gx = fabs(m.cx[a] - m.cx[b]) - 0.5 * (m.region[a] + m.region[b]);
+  double gy = fabs(m.cy[a] - m.cy[b]) - 0.5 * (m.region[a] + m.region[b]);
+  gx = gx > 0 ? gx : 0;
+  gy = gy > 0 ? gy : 0;
+  return (float)sqrt(gx * gx + gy * gy);
+}
+
+// Correction leaves of leaf b: not adjacent, box within rc.
+template <class Emit>
+__device__ void corr_walk(const MixedView &m, int b, Emit emit) {
+  const float rc = *m.rc_ptr;
+  if (!(rc > 0.f)) return;
+  int stack[4 * kKeyLevels + 8];
+  int top = 0;
+  stack[top++] = 0;
+  while (top > 0) {
+    const int c = stack[--top];
+    const int4 ch = reinterpret_cast<const int4 *>(m.child)[c];
+    for (int q = 0; q < 4; q++) {
+      const int cc = (&ch.x)[q];
+      if (cc < 0) continue;
+      if (box_gap(m, cc, b) >= rc) continue;
+      if (m.leaf[cc]) {
+        if (!adj_cells(m, cc, b)) emit(2, cc);
+      } else if (top < 4 * kKeyLevels + 8) {
+        stack[top++] = cc;
+      }
+    }
+  }
+}
+
+__global__ void k_list_count(MixedView m) {
+  int l = blockIdx.x * blockDim.x + threadIdx.x;
+  if (l >= m.nleaf) return;
+  const int b = m.leaf_cell[l];
+  int cnt[3] = {0, 0, 0};
+  auto emit = [&](int kind, int) { cnt[kind]++; };
+  uw_walk(m, b, emit);
+  corr_walk(m, b, emit);
+  m.u_off[l] = cnt[0];
+  m.w_off[l] = cnt[1];
+  m.k_off[l] = cnt[2];
+}
+
+__global__ void k_list_fill(MixedView m) {
+  int l = blockIdx.x * blockDim.x + threadIdx.x;
+  if (l >= m.nleaf) return;
+  const int b = m.leaf_cell[l];
+  int pos[3] = {m.u_off[l], m.w_off[l], m.k_off[l]};
+  int *dst[3] = {m.u_idx, m.w_idx, m.k_idx};
+  auto emit = [&](int kind, int id) { dst[kind][pos[kind]++] = id; };
+  uw_walk(m, b, emit);
+  corr_walk(m, b, emit);
+}
+
+// exclusive scan of three count arrays of length len (one block); totals
+// appended at [len].
+__global__ void __launch_bounds__(1024) k_scan3(int *a, int *b, int *c, int len) {
+  __shared__ long long s[3][1024];
+  int *arr[3] = {a, b, c};
+  const int t = threadIdx.x;
+  const int per = (len + 1023) / 1024;
+  const int lo = t * per, hi = min(len, lo + per);
+  for (int k = 0; k < 3; k++) {
+    long long acc = 0;
+    for (int i = lo; i < hi; i++) acc += arr[k][i];
+    s[k][t] = acc;
+  }
+  __syncthreads();
+  for (int off = 1; off < 1024; off <<= 1) {
+    long long v[3];
+    for (int k = 0; k < 3; k++) v[k] = t >= off ? s[k][t - off] : 0;
+    __syncthreads();
+    for (int k = 0; k < 3; k++) s[k][t] += v[k];
+    __syncthreads();
+  }
+  for (int k = 0; k < 3; k++) {
+    long long run = t == 0 ? 0 : s[k][t - 1];
+    for (int i = lo; i < hi; i++) {
+      int x = arr[k][i];
+      arr[k][i] = (int)run;
+      run += x;
+    }
+    if (t == 1023) arr[k][len] = (int)s[k][1023];
+  }
+}
+
+// ------------------------------------------------------------ expansions
+// Coefficient storage: per cell 2P floats, real parts then imaginary parts.
+
+
+__device__ __forceinline__ float2 fmul(float2 a, float2 b) {
+  return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+
+// S2M: one warp per leaf, lane k owns a_k (k < P <= 32).
+__global__ void k_s2m_f32(MixedView m) {
+  const int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (wid >= m.nleaf) return;
+  const int c = m.leaf_cell[wid];
+  const float ih = m.inv_h[c];
+  const int P = m.P;
+  float2 acc = make_float2(0.f, 0.f);
+  for (int j = m.begin[c]; j < m.end[c]; j++) {
+    float2 z = m.loc[j];
+    z.x *= ih;
+    z.y *= ih;
+    // lane k: z^k by a product scan over lanes
+    float2 v = lane == 0 ? make_float2(1.f, 0.f) : z;
+    for (int off = 1; off < 32; off <<= 1) {
+      float2 o = make_float2(__shfl_up_sync(0xffffffffu, v.x, off), __shfl_up_sync(0xffffffffu, v.y, off));
+      if (lane >= off) v = fmul(o, v);
+    }
+    const float g = m.gam[j];
+    acc.x += g * v.x;
+    acc.y += g * v.y;
+  }
+  if (lane < P) {
+    m.M[(size_t)c * 2 * P + lane] = acc.x;
+    m.M[(size_t)c * 2 * P + P + lane] = acc.y;
+  }
+}
+
+// M2M into the internal cells of one level (grid-stride over all cells).
+__global__ void k_m2m_f32(MixedView m, int lev) {
+  const int lane = threadIdx.x & 31;
+  const int P = m.P;
+  for (int p = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; p < m.ncell; p += (gridDim.x * blockDim.x) >> 5) {
+    if (m.level[p] != lev || m.leaf[p]) continue;
+    const int4 ch = reinterpret_cast<const int4 *>(m.child)[p];
+    float2 acc = make_float2(0.f, 0.f);
+    for (int q = 0; q < 4; q++) {
+      const int c = (&ch.x)[q];
+      if (c < 0) continue;
+      const float *src = m.M + (size_t)c * 2 * P;
+      float2 a = lane < P ? make_float2(src[lane], src[P + lane]) : make_float2(0.f, 0.f);
+      for (int k = 0; k < P; k++) {
+        float2 ak = make_float2(__shfl_sync(0xffffffffu, a.x, k), __shfl_sync(0xffffffffu, a.y, k));
+        if (k <= lane && lane < P) {
+          const float2 t = m.m2m[((size_t)q * kMaxP + lane) * kMaxP + k];
+          acc.x += t.x * ak.x - t.y * ak.y;
+          acc.y += t.x * ak.y + t.y * ak.x;
+        }
+      }
+    }
+    if (lane < P) {
+      m.M[(size_t)p * 2 * P + lane] = acc.x;
+      m.M[(size_t)p * 2 * P + P + lane] = acc.y;
+    }
+  }
+}
+
+// P2L of the X lists: one warp per cell, lane l owns b_l.
+__global__ void k_p2l(MixedView m) {
+  const int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (c >= m.ncell) return;
+  const int *X = m.xlist + (size_t)c * 8;
+  if (X[0] < 0) return;
+  const int P = m.P;
+  const float ih = m.inv_h[c];
+  float2 acc = make_float2(0.f, 0.f);
+  for (int e = 0; e < 8 && X[e] >= 0; e++) {
+    const int d = X[e];
+    const float ox = (float)(m.cx[d] - m.cx[c]), oy = (float)(m.cy[d] - m.cy[c]);
+    for (int j = m.begin[d]; j < m.end[d]; j++) {
+      float2 z = m.loc[j];
+      z.x = (z.x + ox) * ih;
+      z.y = (z.y + oy) * ih;
+      // w = 1/z; lane l: w^(l+1) by a product scan
+      const float r2 = z.x * z.x + z.y * z.y;
+      const float2 w = make_float2(z.x / r2, -z.y / r2);
+      float2 v = w;
+      for (int off = 1; off < 32; off <<= 1) {
+        float2 o = make_float2(__shfl_up_sync(0xffffffffu, v.x, off), __shfl_up_sync(0xffffffffu, v.y, off));
+        if (lane >= off) v = fmul(o, v);
+      }
+      const float g = m.gam[j];
+      acc.x -= g * v.x;
+      acc.y -= g * v.y;
+    }
+  }
+  if (lane < P) {
+    m.L[(size_t)c * 2 * P + lane] += acc.x;
+    m.L[(size_t)c * 2 * P + P + lane] += acc.y;
+  }
+}
+
+// L2L from the internal cells of level lev-1 into their children.
+__global__ void k_l2l_f32(MixedView m, int lev) {
+  const int lane = threadIdx.x & 31;
+  const int P = m.P;
+  for (int p = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; p < m.ncell; p += (gridDim.x * blockDim.x) >> 5) {
+    if (m.level[p] != lev - 1 || m.leaf[p]) continue;
+    const float *src = m.L + (size_t)p * 2 * P;
+    float2 b = lane < P ? make_float2(src[lane], src[P + lane]) : make_float2(0.f, 0.f);
+    const int4 ch = reinterpret_cast<const int4 *>(m.child)[p];
+    for (int q = 0; q < 4; q++) {
+      const int c = (&ch.x)[q];
+      if (c < 0) continue;
+      float2 acc = make_float2(0.f, 0.f);
+      for (int l = 0; l < P; l++) {
+        float2 bl = make_float2(__shfl_sync(0xffffffffu, b.x, l), __shfl_sync(0xffffffffu, b.y, l));
+        if (l >= lane && lane < P) {
+          const float2 t = m.l2l[((size_t)q * kMaxP + lane) * kMaxP + l];
+          acc.x += t.x * bl.x - t.y * bl.y;
+          acc.y += t.x * bl.y + t.y * bl.x;
+        }
+      }
+      if (lane < P) {
+        m.L[(size_t)c * 2 * P + lane] += acc.x;
+        m.L[(size_t)c * 2 * P + P + lane] += acc.y;
+      }
+    }
+  }
+}
+
+__device__ __forceinline__ void kahan(float &s, float &cmp, float v) {
+  float y = v - cmp;
+  float t = s + y;
+  cmp = (t - s) - y;
+  s = t;
+}
+
+// Evaluation: one warp per leaf, targets in chunks of 32.
+__global__ void __launch_bounds__(128) k_eval_mixed(MixedView m, double *uv, const int *perm) {
+  const int l = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (l >= m.nleaf) return;
+  const int B = m.leaf_cell[l];
+  const int P = m.P;
+  const float ihB = m.inv_h[B];
+  const float *LB = m.L + (size_t)B * 2 * P;
+  const float rc2 = (*m.rc_ptr) * (*m.rc_ptr);
+  unsigned long long pairs = 0;
+  for (int t0 = m.begin[B]; t0 < m.end[B]; t0 += 32) {
+    const int t = t0 + lane;
+    const bool valid = t < m.end[B];
+    const float2 zt = valid ? m.loc[t] : make_float2(0.f, 0.f);
+    // far field: local expansion of B
+    float2 phi = make_float2(0.f, 0.f);
+    {
+      const float2 zeta = make_float2(zt.x * ihB, zt.y * ihB);
+      float2 acc = make_float2(LB[P - 1], LB[2 * P - 1]);
+      for (int k = P - 2; k >= 0; k--) {
+        acc = fmul(acc, zeta);
+        acc.x += LB[k];
+        acc.y += LB[P + k];
+      }
+      phi.x = acc.x * ihB;
+      phi.y = acc.y * ihB;
+    }
+    // W list: multipoles of small separated cells
+    for (int e = m.w_off[l]; e < m.w_off[l + 1]; e++) {
+      const int A = m.w_idx[e];
+      const float ih = m.inv_h[A];
+      const float ox = (float)(m.cx[B] - m.cx[A]), oy = (float)(m.cy[B] - m.cy[A]);
+      const float zx = (zt.x + ox) * ih, zy = (zt.y + oy) * ih;
+      const float r2 = zx * zx + zy * zy;
+      const float2 w = make_float2(zx / r2, -zy / r2);
+      const float *MA = m.M + (size_t)A * 2 * P;
+      float2 acc = make_float2(MA[P - 1], MA[2 * P - 1]);
+      for (int k = P - 2; k >= 0; k--) {
+        acc = fmul(acc, w);
+        acc.x += MA[k];
+        acc.y += MA[P + k];
+      }
+      acc = fmul(acc, w);
+      phi.x += acc.x * ih;
+      phi.y += acc.y * ih;
+    }
+    // near field: U list, regularised kernel; then the Gaussian correction
+    float ax = 0.f, ay = 0.f, cax = 0.f, cay = 0.f;
+    for (int pass = 0; pass < 2; pass++) {
+      const int e0 = pass == 0 ? m.u_off[l] : m.k_off[l];
+      const int e1 = pass == 0 ? m.u_off[l + 1] : m.k_off[l + 1];
+      const int *idx = pass == 0 ? m.u_idx : m.k_idx;
+      for (int e = e0; e < e1; e++) {
+        const int A = idx[e];
+        const float ox = (float)(m.cx[B] - m.cx[A]), oy = (float)(m.cy[B] - m.cy[A]);
+        const float tx = zt.x + ox, ty = zt.y + oy;
+        const int j0 = m.begin[A], j1 = m.end[A];
+        for (int j = j0; j < j1; j++) {
+          const float2 zs = m.loc[j];
+          const float rx = tx - zs.x, ry = ty - zs.y;
+          const float r2 = rx * rx + ry * ry;
+          float f;
+          if (pass == 0) {
+            if (!(r2 > 1e-20f)) continue;
+            const float x2 = r2 * m.s2inv[j];
+            const float e1f = x2 < 1e-3f ? x2 * (1.f - 0.5f * x2) : 1.f - __expf(-x2);
+            f = m.gam[j] * e1f / r2;
+          } else {
+            if (!(r2 < rc2)) continue;
+            f = -m.gam[j] * __expf(-r2 * m.s2inv[j]) / r2;
+          }
+          kahan(ax, cax, -f * ry);
+          kahan(ay, cay, f * rx);
+        }
+        pairs += (unsigned long long)(j1 - j0);
+      }
+    }
+    if (valid) {
+      // FP64 final reduction: u = Im(phi)/2pi + ax/2pi, v = Re(phi)/2pi + ay/2pi
+      const double u = ((double)phi.y + (double)ax - (double)cax) * (double)kInv2Pi;
+      const double v = ((double)phi.x + (double)ay - (double)cay) * (double)kInv2Pi;
+      const int o = perm[t];
+      uv[2 * (size_t)o] = u;
+      uv[2 * (size_t)o + 1] = v;
+    }
+  }
+  for (int o = 16; o; o >>= 1) pairs += __shfl_xor_sync(0xffffffffu, pairs, o);
+  if (lane == 0) atomicAdd(&m.st->n_pairs, pairs);
+}
+
+// ------------------------------------------------------------ host side
+
+double binom_d(int n, int k) {
+  if (k < 0 || k > n) return 0.0;
+  double r = 1.0;
+  for (int i = 1; i <= k; i++) r = r * (double)(n - k + i) / (double)i;
+  return r;
+}
+
+struct Cplx {
+  double re, im;
+};
+Cplx cmulh(Cplx a, Cplx b) { return {a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re}; }
+Cplx cpowi(Cplx z, int k) {
+  Cplx r{1, 0};
+  for (int i = 0; i < k; i++) r = cmulh(r, z);
+  return r;
+}
+Cplx cinv(Cplx z) {
+  double d = z.re * z.re + z.im * z.im;
+  return {z.re / d, -z.im / d};
+}
+
+// child centre offset from the parent centre in units of the parent side,
+// quadrant q (x+ if q odd, y- if q >= 2)
+Cplx quad_offset(int q) { return {(q & 1) ? 0.25 : -0.25, (q & 2) ? -0.25 : 0.25}; }
+
+bool g_tables_ready[64] = {};
+
+}  // namespace
+
+// Host tables: h_m2l [4][27][P][P] complex, h_m2m / h_l2l [4][kMaxP][kMaxP]
+// complex (M2M [q][n][k], L2L [q][k][l]); the slot table goes to constant
+// memory of the current device.
+cudaError_t mixed_tables(int P, float *h_m2l, float *h_m2m, float *h_l2l) {
+  // slot table: class (qx,qy) -> 6x6 offsets around the parent's block
+  static signed char slot[4][6][6];
+  int cnt[4] = {0, 0, 0, 0};
+  for (int cls = 0; cls < 4; cls++) {
+    int qx = cls & 1, qy = cls >> 1;
+    for (int a = 0; a < 6; a++)
+      for (int b = 0; b < 6; b++) slot[cls][a][b] = -1;
+    for (int dy = -2 - qy; dy <= 3 - qy; dy++)
+      for (int dx = -2 - qx; dx <= 3 - qx; dx++) {
+        if (abs(dx) <= 1 && abs(dy) <= 1) continue;
+        int s = cnt[cls]++;
+        slot[cls][dy + 2 + qy][dx + 2 + qx] = (signed char)s;
+        if (!h_m2l) continue;
+        // tau = (z_target - z_source)/h = -dx + i dy
+        Cplx tau{(double)-dx, (double)dy};
+        Cplx ti = cinv(tau);
+        for (int l = 0; l < P; l++)
+          for (int k = 0; k < P; k++) {
+            Cplx v = cpowi(ti, k + l + 1);
+            double f = ((l & 1) ? -1.0 : 1.0) * binom_d(k + l, l);
+            float *o = h_m2l + ((((size_t)cls * 27 + s) * P + l) * P + k) * 2;
+            o[0] = (float)(f * v.re);
+            o[1] = (float)(f * v.im);
+          }
+      }
+  }
+  auto m2m = reinterpret_cast<float(*)[kMaxP][kMaxP][2]>(h_m2m);
+  auto l2l = reinterpret_cast<float(*)[kMaxP][kMaxP][2]>(h_l2l);
+  for (int q = 0; q < 4 && h_m2m && h_l2l; q++) {
+    Cplx d = quad_offset(q);
+    for (int n = 0; n < kMaxP; n++)
+      for (int k = 0; k < kMaxP; k++) {
+        // M2M: a'_n += a_k 2^-k C(n,k) d^(n-k)   (k <= n)
+        Cplx v{0, 0};
+        if (k <= n) {
+          Cplx pw = cpowi(d, n - k);
+          double f = std::ldexp(binom_d(n, k), -k);
+          v = {f * pw.re, f * pw.im};
+        }
+        m2m[q][n][k][0] = (float)v.re;
+        m2m[q][n][k][1] = (float)v.im;
+        // L2L: b'_k += b_l C(l,k) d^(l-k) 2^-(k+1)   (l >= k); stored [k][l]
+        Cplx w{0, 0};
+        int kk = n, l = k;
+        if (l >= kk) {
+          Cplx pw = cpowi(d, l - kk);
+          double f = std::ldexp(binom_d(l, kk), -(kk + 1));
+          w = {f * pw.re, f * pw.im};
+        }
+        l2l[q][kk][l][0] = (float)w.re;
+        l2l[q][kk][l][1] = (float)w.im;
+      }
+  }
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev >= 0 && dev < 64 && g_tables_ready[dev]) return cudaSuccess;
+  cudaError_t e = cudaMemcpyToSymbol(c_slot, slot, sizeof(slot));
+  if (e == cudaSuccess && dev >= 0 && dev < 64) g_tables_ready[dev] = true;
+  return e;
+}
+
+int mixed_lists(MixedView &m, cudaStream_t s) {
+  const int cb = (m.ncell + 255) / 256, lb = (m.nleaf + 255) / 256;
+  k_cell_info<<<cb, 256, 0, s>>>(m);
+  k_parent<<<cb, 256, 0, s>>>(m);
+  k_colleagues<<<cb, 256, 0, s>>>(m);
+  k_vx_lists<<<cb, 256, 0, s>>>(m);
+  k_list_count<<<lb, 256, 0, s>>>(m);
+  k_scan3<<<1, 1024, 0, s>>>(m.u_off, m.w_off, m.k_off, m.nleaf);
+  g_launches.fetch_add(6, std::memory_order_relaxed);
+  T2D_CUDA_TRY(cudaGetLastError());
+  return TREE2D_OK;
+}
+
+int mixed_fill_lists(MixedView &m, cudaStream_t s) {
+  k_list_fill<<<(m.nleaf + 255) / 256, 256, 0, s>>>(m);
+  g_launches.fetch_add(1, std::memory_order_relaxed);
+  T2D_CUDA_TRY(cudaGetLastError());
+  return TREE2D_OK;
+}
+
+int mixed_leaf_setup(MixedView &m, const Tree &t, cudaStream_t s) {
+  k_leaf_setup<<<(int)(((long)m.nleaf * 32 + 255) / 256), 256, 0, s>>>(m, t.x, t.y, t.cir, t.cor);
+  g_launches.fetch_add(1, std::memory_order_relaxed);
+  T2D_CUDA_TRY(cudaGetLastError());
+  return TREE2D_OK;
+}
+
+int mixed_upward(MixedView &m, int depth, cudaStream_t s) {
+  k_s2m_f32<<<(int)(((long)m.nleaf * 32 + 255) / 256), 256, 0, s>>>(m);
+  g_launches.fetch_add(1, std::memory_order_relaxed);
+  const int blocks = 152 * 8;
+  for (int lev = depth - 1; lev >= 2; lev--) {
+    k_m2m_f32<<<blocks, 256, 0, s>>>(m, lev);
+    g_launches.fetch_add(1, std::memory_order_relaxed);
+  }
+  T2D_CUDA_TRY(cudaGetLastError());
+  return TREE2D_OK;
+}
+
+int mixed_downward(MixedView &m, int depth, cudaStream_t s) {
+  k_p2l<<<(int)(((long)m.ncell * 32 + 255) / 256), 256, 0, s>>>(m);
+  g_launches.fetch_add(1, std::memory_order_relaxed);
+  const int blocks = 152 * 8;
+  for (int lev = 3; lev <= depth; lev++) {
+    k_l2l_f32<<<blocks, 256, 0, s>>>(m, lev);
+    g_launches.fetch_add(1, std::memory_order_relaxed);
+  }
+  T2D_CUDA_TRY(cudaGetLastError());
+  return TREE2D_OK;
+}
+
+int mixed_evaluate(MixedView &m, double *uv, const int *perm, cudaStream_t s) {
+  k_eval_mixed<<<(int)(((long)m.nleaf * 32 + 127) / 128), 128, 0, s>>>(m, uv, perm);
+  g_launches.fetch_add(1, std::memory_order_relaxed);
+  T2D_CUDA_TRY(cudaGetLastError());
+  return TREE2D_OK;
+}
+
+
+int mixed_solve(Workspace &ws, const Tree &t, const MixedParams &mp, double *d_uv, cudaStream_t s,
+                tree2d_stats_t &st) {
+  const int P = mp.pterms;
+  if (P < 2 || P > kMaxP) return TREE2D_ERR_BAD_PARAMS;
+  const int n = t.n, nc = t.ncell, nl = t.nleaf;
+  // ---- operators (per P, cached)
+  if (ws.mx_tables_P != P) {
+    std::vector<float> m2l((size_t)4 * 27 * P * P * 2), m2m((size_t)4 * kMaxP * kMaxP * 2),
+        l2l((size_t)4 * kMaxP * kMaxP * 2);
+    T2D_CUDA_TRY(mixed_tables(P, m2l.data(), m2m.data(), l2l.data()));
+    size_t need = Arena::bytes_for(m2l.size(), 4) + 2 * Arena::bytes_for(m2m.size(), 4);
+    T2D_CUDA_TRY(ws.mx_tables.reserve(need));
+    ws.mx_tables.reset();
+    float *dm2l = ws.mx_tables.take<float>(m2l.size());
+    float *dm2m = ws.mx_tables.take<float>(m2m.size());
+    float *dl2l = ws.mx_tables.take<float>(l2l.size());
+    T2D_CUDA_TRY(cudaMemcpy(dm2l, m2l.data(), m2l.size() * 4, cudaMemcpyHostToDevice));
+    T2D_CUDA_TRY(cudaMemcpy(dm2m, m2m.data(), m2m.size() * 4, cudaMemcpyHostToDevice));
+    T2D_CUDA_TRY(cudaMemcpy(dl2l, l2l.data(), l2l.size() * 4, cudaMemcpyHostToDevice));
+    ws.mx_tables_P = P;
+  } else {
+    T2D_CUDA_TRY(mixed_tables(P, nullptr, nullptr, nullptr));
+  }
+  ws.mx_tables.reset();
+  const float *dm2l = ws.mx_tables.take<float>((size_t)4 * 27 * P * P * 2);
+  const float *dm2m = ws.mx_tables.take<float>((size_t)4 * kMaxP * kMaxP * 2);
+  const float *dl2l = ws.mx_tables.take<float>((size_t)4 * kMaxP * kMaxP * 2);
+
+  // ---- arrays
+  size_t need = 0;
+  need += Arena::bytes_for(nc, 4) * 5;            // ix iy h inv_h parent
+  need += Arena::bytes_for(n, 4) * 4;             // leaf_of gam s2inv + pad
+  need += Arena::bytes_for(n, 8);                 // loc
+  need += Arena::bytes_for((size_t)nc * 9, 4) * 2;
+  need += Arena::bytes_for((size_t)nc * 27, 4) + Arena::bytes_for((size_t)nc * 8, 4);
+  need += Arena::bytes_for((size_t)nl + 1, 4) * 3;
+  need += Arena::bytes_for((size_t)nc * 2 * P, 4) * 2;
+  need += 256;
+  T2D_CUDA_TRY(ws.mx_arena.reserve(need));
+  ws.mx_arena.reset();
+  MixedView m{};
+  m.n = n;
+  m.ncell = nc;
+  m.nleaf = nl;
+  m.P = P;
+  m.keys = t.keys;
+  m.cpl = t.cpl;
+  m.leaf_level = t.leaf_level;
+  m.cellbase = t.cellbase;
+  m.level = t.level;
+  m.begin = t.begin;
+  m.end = t.end;
+  m.child = t.child;
+  m.leaf_cell = t.leaf_cell;
+  m.leaf = t.leaf;
+  m.cx = t.cx;
+  m.cy = t.cy;
+  m.region = t.region;
+  m.ix = ws.mx_arena.take<unsigned>(nc);
+  m.iy = ws.mx_arena.take<unsigned>(nc);
+  m.h = ws.mx_arena.take<float>(nc);
+  m.inv_h = ws.mx_arena.take<float>(nc);
+  m.parent = ws.mx_arena.take<int>(nc);
+  m.leaf_of = ws.mx_arena.take<int>(n);
+  m.loc = ws.mx_arena.take<float2>(n);
+  m.gam = ws.mx_arena.take<float>(n);
+  m.s2inv = ws.mx_arena.take<float>(n);
+  m.coll = ws.mx_arena.take<int>((size_t)nc * 9);
+  m.coarse = ws.mx_arena.take<int>((size_t)nc * 9);
+  m.vlist = ws.mx_arena.take<int>((size_t)nc * 27);
+  m.xlist = ws.mx_arena.take<int>((size_t)nc * 8);
+  m.u_off = ws.mx_arena.take<int>((size_t)nl + 1);
+  m.w_off = ws.mx_arena.take<int>((size_t)nl + 1);
+  m.k_off = ws.mx_arena.take<int>((size_t)nl + 1);
+  m.M = ws.mx_arena.take<float>((size_t)nc * 2 * P);
+  m.L = ws.mx_arena.take<float>((size_t)nc * 2 * P);
+  unsigned *rc_bits = ws.mx_arena.take<unsigned>(1);
+  m.rc_ptr = reinterpret_cast<const float *>(rc_bits);
+  m.m2m = reinterpret_cast<const float2 *>(dm2m);
+  m.l2l = reinterpret_cast<const float2 *>(dl2l);
+  m.st = ws.status;
+  T2D_CUDA_TRY(cudaMemsetAsync(m.parent, 0xff, sizeof(int) * (size_t)nc, s));
+  T2D_CUDA_TRY(cudaMemsetAsync(rc_bits, 0, 4, s));
+  k_sigma_max<<<304, 256, 0, s>>>(t.cor, n, rc_bits);
+  k_cutoff<<<1, 1, 0, s>>>(rc_bits, (float)mp.cutoff);
+  g_launches.fetch_add(2, std::memory_order_relaxed);
+
+  int rc = mixed_leaf_setup(m, t, s);
+  if (rc) return rc;
+  rc = mixed_lists(m, s);
+  if (rc) return rc;
+  int tot[3];
+  T2D_CUDA_TRY(cudaMemcpyAsync(&tot[0], m.u_off + nl, 4, cudaMemcpyDeviceToHost, s));
+  T2D_CUDA_TRY(cudaMemcpyAsync(&tot[1], m.w_off + nl, 4, cudaMemcpyDeviceToHost, s));
+  T2D_CUDA_TRY(cudaMemcpyAsync(&tot[2], m.k_off + nl, 4, cudaMemcpyDeviceToHost, s));
+  T2D_CUDA_TRY(cudaStreamSynchronize(s));
+  size_t lneed = Arena::bytes_for(tot[0] + 1, 4) + Arena::bytes_for(tot[1] + 1, 4) + Arena::bytes_for(tot[2] + 1, 4);
+  T2D_CUDA_TRY(ws.mx_lists.reserve(lneed));
+  ws.mx_lists.reset();
+  m.u_idx = ws.mx_lists.take<int>(tot[0] + 1);
+  m.w_idx = ws.mx_lists.take<int>(tot[1] + 1);
+  m.k_idx = ws.mx_lists.take<int>(tot[2] + 1);
+  rc = mixed_fill_lists(m, s);
+  if (rc) return rc;
+  rc = mixed_upward(m, t.depth, s);
+  if (rc) return rc;
+  T2D_CUDA_TRY(cudaMemsetAsync(m.L, 0, sizeof(float) * (size_t)nc * 2 * P, s));
+  rc = m2l_cuda_cores(m, dm2l, s);
+  if (rc) return rc;
+  rc = mixed_downward(m, t.depth, s);
+  if (rc) return rc;
+  rc = mixed_evaluate(m, d_uv, t.perm, s);
+  if (rc) return rc;
+  (void)st;
+  return TREE2D_OK;
+}
+
+}  // namespace t2d

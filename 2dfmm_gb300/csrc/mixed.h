@@ -1,0 +1,56 @@
+// Mixed-precision FMM: device view and host entry points (mixed.cu, m2l.cu).
+#pragma once
+
+#include "internal.h"
+
+namespace t2d {
+
+constexpr int kMaxP = 32;  // largest expansion length of the mixed form
+
+// Everything the mixed kernels read or write, by value into each kernel.
+struct MixedView {
+  int n, ncell, nleaf, P;
+  const float *rc_ptr;  // device: cutoff radius of the regularisation correction
+  // from the tree
+  const uint64_t *keys;
+  const uint8_t *cpl, *leaf_level;
+  const unsigned *cellbase;
+  const int *level, *begin, *end, *child, *leaf_cell;
+  const unsigned char *leaf;
+  const double *cx, *cy, *region;
+  // mixed arrays
+  unsigned *ix, *iy;
+  float *h, *inv_h;
+  int *parent;
+  int *leaf_of;          // per position
+  float2 *loc;           // per position, offset from its leaf centre
+  float *gam, *s2inv;    // per position
+  int *coll, *coarse;    // 9 per cell
+  int *vlist;            // 27 per cell, slot order of the cell's class
+  int *xlist;            // 8 per cell
+  int *u_off, *w_off, *k_off;  // per leaf (+1)
+  int *u_idx, *w_idx, *k_idx;
+  float *M, *L;          // per cell, 2P floats (re[P], im[P])
+  const float2 *m2m, *l2l;  // [4][kMaxP][kMaxP] translation operators
+  DevStatus *st;
+};
+
+cudaError_t mixed_tables(int P, float *h_m2l, float *h_m2m, float *h_l2l);
+int mixed_leaf_setup(MixedView &m, const Tree &t, cudaStream_t s);
+int mixed_lists(MixedView &m, cudaStream_t s);
+int mixed_fill_lists(MixedView &m, cudaStream_t s);
+int mixed_upward(MixedView &m, int depth, cudaStream_t s);
+int mixed_downward(MixedView &m, int depth, cudaStream_t s);
+int mixed_evaluate(MixedView &m, double *uv, const int *perm, cudaStream_t s);
+
+// M2L over the V lists (m2l.cu): L[c] += sum_s T(class(c), s) M[V[c][s]].
+// `tables` is the device copy of the [4][27][P][P] complex operators.
+int m2l_cuda_cores(MixedView &m, const float *tables, cudaStream_t s);
+
+// Whole mixed solve on a built tree: lists, upward, M2L, downward,
+// evaluation; uv written in original blob order.  Synchronises the stream
+// once (to size the interaction lists).
+int mixed_solve(Workspace &ws, const Tree &t, const MixedParams &mp, double *d_uv, cudaStream_t s,
+                tree2d_stats_t &st);
+
+}  // namespace t2d

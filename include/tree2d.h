@@ -80,6 +80,14 @@ void tree2d_get_params(int *nterms, int *num_p, double *theta, double *r_min);
 int tree2d_set_mode(int mode);
 int tree2d_get_mode(void);
 
+/* Parameters of the mixed form: expansion length pterms (2..32) of its
+ * multipole and local expansions, the radius of the regularisation
+ * correction in units of the largest core radius (pairs closer than that
+ * which the far field treats as point vortices get exp(-r^2/sigma^2)
+ * added back), and whether M2L runs on the tensor cores (1) or on CUDA
+ * cores (0, for checking).  Defaults 16, 4.0, 1. */
+int tree2d_set_mixed_params(int pterms, double cutoff_sigmas, int use_tensor_cores);
+
 /* Evaluates n targets (xy interleaved, host memory) into uv (interleaved,
  * host memory) against the last make_tree.  Blob positions are answered
  * from the precomputed velocities, the rest in one GPU launch.  Returns a
