@@ -31,7 +31,7 @@ MODE_PLAIN, MODE_MIXED, MODE_LEARNED = 0, 1, 2
 EXPORTS = [
     "make_tree", "biot_tree", "tree2d_last_error", "tree2d_error_string", "tree2d_set_params",
     "tree2d_clear_params", "tree2d_get_params", "tree2d_set_mode", "tree2d_get_mode", "tree2d_set_mixed_params", "biot_tree_batch",
-    "tree2d_solve_device", "tree2d_solve_device_static", "tree2d_get_stats", "tree2d_export_tree", "tree2d_direct_device", "tree2d_fp64_probe", "tree2d_version",
+    "tree2d_solve_device", "tree2d_solve_device_static", "tree2d_get_stats", "tree2d_export_tree", "tree2d_direct_device", "tree2d_fp64_probe", "tree2d_pipe_probe", "tree2d_version",
 ]
 
 
@@ -47,7 +47,7 @@ class Stats(ctypes.Structure):
         ("depth", ctypes.c_int), ("mode", ctypes.c_int), ("n_m2s", ctypes.c_longlong),
         ("n_pairs", ctypes.c_longlong), ("n_m2l", ctypes.c_longlong), ("ms_build", ctypes.c_double),
         ("ms_upward", ctypes.c_double), ("ms_eval", ctypes.c_double), ("ms_total", ctypes.c_double),
-        ("n_launches", ctypes.c_longlong),
+        ("n_launches", ctypes.c_longlong), ("m2l_path", ctypes.c_int),
     ]
 
     def as_dict(self):
@@ -107,6 +107,8 @@ def load(path: str | None = None):
     L.tree2d_direct_device.restype = ctypes.c_int
     L.tree2d_fp64_probe.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, _dp]
     L.tree2d_fp64_probe.restype = ctypes.c_int
+    L.tree2d_pipe_probe.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p, _dp]
+    L.tree2d_pipe_probe.restype = ctypes.c_int
     L.tree2d_version.restype = ctypes.c_char_p
     _lib = L
     return L
@@ -239,6 +241,13 @@ def fp64_peak_tflops(blocks: int = 152 * 8, iters: int = 20000, stream: int = 0)
     """Measured FP64 FMA throughput of this GPU (TFLOP/s, FMA = 2 flops)."""
     ms = ctypes.c_double()
     _check(load().tree2d_fp64_probe(blocks, iters, stream or None, ctypes.byref(ms)), "fp64_probe")
+    return blocks * 256.0 * iters * 16.0 / (ms.value * 1e-3) / 1e12
+
+
+def fp32_peak_tflops(blocks: int = 152 * 8, iters: int = 200000, stream: int = 0) -> float:
+    """Measured FP32 FMA throughput of this GPU (TFLOP/s, FMA = 2 flops)."""
+    ms = ctypes.c_double()
+    _check(load().tree2d_pipe_probe(32, blocks, iters, stream or None, ctypes.byref(ms)), "pipe_probe")
     return blocks * 256.0 * iters * 16.0 / (ms.value * 1e-3) / 1e12
 
 

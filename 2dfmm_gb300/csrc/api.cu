@@ -202,6 +202,7 @@ int solve(Lib &L, Solver &S, int n, const double *d_xy, const double *d_cir, con
   T2D_CUDA_TRY(cudaMemcpyAsync(ws.h_status, ws.status, sizeof(DevStatus), cudaMemcpyDeviceToHost, s));
   T2D_CUDA_TRY(cudaStreamSynchronize(s));
   if (ws.h_status->err) return ws.h_status->err;
+  const int m2l_path = st.m2l_path;
   st.n_cells = S.tree.ncell;
   st.n_leaves = S.tree.nleaf;
   st.depth = S.tree.depth;
@@ -209,10 +210,17 @@ int solve(Lib &L, Solver &S, int n, const double *d_xy, const double *d_cir, con
   st.n_pairs = (long long)ws.h_status->n_pairs;
   st.n_m2l = (long long)ws.h_status->n_m2l;
   st.ms_build = elapsed(ws.ev[0], ws.ev[1]);
-  st.ms_upward = elapsed(ws.ev[1], ws.ev[2]);
-  st.ms_eval = elapsed(ws.ev[2], ws.ev[3]);
+  if (L.mode == TREE2D_MODE_PLAIN) {
+    st.ms_upward = elapsed(ws.ev[1], ws.ev[2]);
+    st.ms_eval = elapsed(ws.ev[2], ws.ev[3]);
+  } else {
+    // mixed: lists + upward + M2L + downward, then the evaluation kernel
+    st.ms_upward = elapsed(ws.ev[1], ws.ev[4]);
+    st.ms_eval = elapsed(ws.ev[4], ws.ev[5]);
+  }
   st.ms_total = elapsed(ws.ev[0], ws.ev[3]);
   st.n_launches = g_launches.load() - launches0;
+  st.m2l_path = m2l_path;
   return TREE2D_OK;
 }
 
@@ -614,15 +622,23 @@ int tree2d_direct_device(int ntgt, const double *d_txy, int nsrc, const double *
 }
 
 int tree2d_fp64_probe(int blocks, int iters, void *stream, double *ms) {
+  return tree2d_pipe_probe(64, blocks, iters, stream, ms);
+}
+
+int tree2d_pipe_probe(int bits, int blocks, int iters, void *stream, double *ms) {
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   double *buf = nullptr;
   cudaEvent_t a, b;
+  if (bits != 32 && bits != 64) return fail(TREE2D_ERR_BAD_INPUT);
   if (cudaMalloc(reinterpret_cast<void **>(&buf), 64) != cudaSuccess) return fail(TREE2D_ERR_CUDA);
   cudaEventCreate(&a);
   cudaEventCreate(&b);
-  dfma_probe(buf, blocks, iters / 8 + 1, s);  // warm-up
+  auto run = [&](int it) {
+    return bits == 64 ? dfma_probe(buf, blocks, it, s) : ffma_probe(reinterpret_cast<float *>(buf), blocks, it, s);
+  };
+  run(iters / 8 + 1);  // warm-up
   cudaEventRecord(a, s);
-  cudaError_t e = dfma_probe(buf, blocks, iters, s);
+  cudaError_t e = run(iters);
   cudaEventRecord(b, s);
   cudaEventSynchronize(b);
   float f = 0.f;
@@ -631,7 +647,7 @@ int tree2d_fp64_probe(int blocks, int iters, void *stream, double *ms) {
   cudaEventDestroy(b);
   cudaFree(buf);
   if (e != cudaSuccess) {
-    note_cuda_error(e, "dfma_probe");
+    note_cuda_error(e, "pipe_probe");
     return fail(TREE2D_ERR_CUDA);
   }
   if (ms) *ms = f;

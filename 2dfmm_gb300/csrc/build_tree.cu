@@ -117,16 +117,17 @@ __device__ __forceinline__ unsigned descend(double x, double y, double &cx, doub
   return q;
 }
 
+// `levels` digits, level 1 in the top two bits, zero below the last level.
 __global__ void __launch_bounds__(256) k_keys(const double *__restrict__ xy, int n, const RootBox *__restrict__ root,
-                                              uint64_t *__restrict__ keys, uint32_t *__restrict__ vals) {
+                                              uint64_t *__restrict__ keys, uint32_t *__restrict__ vals, int levels) {
   long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (i >= n) return;
   double x = xy[2 * i], y = xy[2 * i + 1];
   double cx = root->cx, cy = root->cy, R = root->region;
   uint64_t key = 0;
-#pragma unroll 8
-  for (int l = 0; l < kKeyLevels; l++) key = (key << 2) | descend(x, y, cx, cy, R);
-  keys[i] = key;
+#pragma unroll 4
+  for (int l = 0; l < levels; l++) key = (key << 2) | descend(x, y, cx, cy, R);
+  keys[i] = levels < kKeyLevels ? key << (64 - 2 * levels) : key;
   vals[i] = (uint32_t)i;
 }
 
@@ -143,7 +144,7 @@ __global__ void __launch_bounds__(256) k_cpl(const uint64_t *__restrict__ keys, 
 // after the step of width k, buf[t] = max(w[t .. t+k-1]).
 constexpr int kLLTile = 2048;
 __global__ void __launch_bounds__(256) k_leaf_level(const uint8_t *__restrict__ w, int n, int num_p,
-                                                    uint8_t *__restrict__ leaf_level, DevStatus *st) {
+                                                    uint8_t *__restrict__ leaf_level, DevStatus *st, int levels) {
   extern __shared__ uint8_t sbuf[];
   const int H = num_p - 1;
   const long tile0 = (long)blockIdx.x * kLLTile;
@@ -177,9 +178,13 @@ __global__ void __launch_bounds__(256) k_leaf_level(const uint8_t *__restrict__ 
     uint8_t a = cur[t];
     uint8_t b = cur[t + W - K];
     int s = a > b ? a : b;
-    if (s >= kKeyLevels) {
-      set_err(st, TREE2D_ERR_TOO_DEEP);
-      s = kKeyLevels - 1;
+    if (s >= levels) {
+      // a cell at the deepest key level still holds >= num_p blobs
+      if (levels < kKeyLevels)
+        atomicExch(&st->deeper, 1);
+      else
+        set_err(st, TREE2D_ERR_TOO_DEEP);
+      s = levels - 1;
     }
     leaf_level[i] = (uint8_t)(s + 1);
     local_max = max(local_max, s + 1);
@@ -456,6 +461,8 @@ int build_tree(Workspace &ws, int n, const double *d_xy, const double *d_cir, co
   unsigned long long *part = ws.tmp_arena.take<unsigned long long>(ntiles + 1);
   unsigned long long *total = ws.tmp_arena.take<unsigned long long>(1);
 
+  int levels = kShortKeyLevels;
+retry:
   T2D_CUDA_TRY(cudaMemsetAsync(ws.status, 0, sizeof(DevStatus), s));
 
   // 1. root box
@@ -464,10 +471,10 @@ int build_tree(Workspace &ws, int n, const double *d_xy, const double *d_cir, co
   k_root<<<1, 32, 0, s>>>(bpart, kBoxBlocks, t.root);
   ::t2d::g_launches.fetch_add(1, std::memory_order_relaxed);
   // 2. keys
-  k_keys<<<(n + 255) / 256, 256, 0, s>>>(d_xy, n, t.root, t.keys, vals);
+  k_keys<<<(n + 255) / 256, 256, 0, s>>>(d_xy, n, t.root, t.keys, vals, levels);
   ::t2d::g_launches.fetch_add(1, std::memory_order_relaxed);
   // 3. sort
-  T2D_CUDA_TRY(radix_sort_pairs(t.keys, vals, keys_alt, vals_alt, n, 64, sort_tmp, s));
+  T2D_CUDA_TRY(radix_sort_pairs(t.keys, vals, keys_alt, vals_alt, n, 64 - 2 * levels, 64, sort_tmp, s));
   // 4-5. leaf levels
   k_cpl<<<(n + 255) / 256, 256, 0, s>>>(t.keys, n, p.num_p, cpl, w);
   ::t2d::g_launches.fetch_add(1, std::memory_order_relaxed);
@@ -475,7 +482,7 @@ int build_tree(Workspace &ws, int n, const double *d_xy, const double *d_cir, co
     const int H = p.num_p - 1;
     size_t smem = 2 * (size_t)(kLLTile + H);
     if (smem > 48 * 1024) T2D_CUDA_TRY(cudaFuncSetAttribute(k_leaf_level, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    k_leaf_level<<<(n + kLLTile - 1) / kLLTile, 256, smem, s>>>(w, n, p.num_p, leaf_level, ws.status);
+    k_leaf_level<<<(n + kLLTile - 1) / kLLTile, 256, smem, s>>>(w, n, p.num_p, leaf_level, ws.status, levels);
     ::t2d::g_launches.fetch_add(1, std::memory_order_relaxed);
   }
   // 6. counts and scan
@@ -489,6 +496,11 @@ int build_tree(Workspace &ws, int n, const double *d_xy, const double *d_cir, co
   T2D_CUDA_TRY(cudaMemcpyAsync(h_total, total, 8, cudaMemcpyDeviceToHost, s));
   T2D_CUDA_TRY(cudaStreamSynchronize(s));
   if (ws.h_status->err) return ws.h_status->err;
+  if (ws.h_status->deeper && levels < kKeyLevels) {
+    levels = kKeyLevels;  // rare: a cell at the short depth still needs splitting
+    goto retry;
+  }
+  t.key_levels = levels;
   unsigned long long tot = *h_total;
   long long ncell = 1 + (long long)(tot >> 32);
   long long nleaf = (long long)(tot & 0xffffffffu);
@@ -549,9 +561,11 @@ int sort_targets(Workspace &ws, int n, const double *d_xy, const RootBox *d_root
   uint64_t *k2 = ws.tmp_arena.take<uint64_t>(n);
   uint32_t *v2 = ws.tmp_arena.take<uint32_t>(n);
   void *tmp = ws.tmp_arena.take<char>(radix_sort_temp_bytes(n));
-  k_keys<<<(n + 255) / 256, 256, 0, s>>>(d_xy, n, d_root, k, reinterpret_cast<uint32_t *>(d_order));
+  // order only (for coherent warps): the short key depth is enough
+  k_keys<<<(n + 255) / 256, 256, 0, s>>>(d_xy, n, d_root, k, reinterpret_cast<uint32_t *>(d_order), kShortKeyLevels);
   ::t2d::g_launches.fetch_add(1, std::memory_order_relaxed);
-  T2D_CUDA_TRY(radix_sort_pairs(k, reinterpret_cast<uint32_t *>(d_order), k2, v2, n, 64, tmp, s));
+  T2D_CUDA_TRY(radix_sort_pairs(k, reinterpret_cast<uint32_t *>(d_order), k2, v2, n, 64 - 2 * kShortKeyLevels, 64,
+                                tmp, s));
   return TREE2D_OK;
 }
 

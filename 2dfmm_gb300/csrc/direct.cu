@@ -10,24 +10,29 @@ namespace {
 constexpr int kThreads = 256;
 constexpr double kPi = 3.14159265358979323846;
 
+// grid.y splits the sources into chunks; each block adds its partial sums
+// into uv (zeroed by the caller) with FP64 atomics.
 __global__ void __launch_bounds__(kThreads) k_direct(int ntgt, const double *__restrict__ txy, int nsrc,
                                                      const double *__restrict__ sxy, const double *__restrict__ cir,
-                                                     const double *__restrict__ cor, double *__restrict__ uv) {
+                                                     const double *__restrict__ cor, double *__restrict__ uv,
+                                                     int chunk) {
   __shared__ double sx[kThreads], sy[kThreads], sg[kThreads], sr[kThreads];
   const long i = blockIdx.x * (long)kThreads + threadIdx.x;
   const bool valid = i < ntgt;
   const double x = valid ? txy[2 * i] : 0.0, y = valid ? txy[2 * i + 1] : 0.0;
   double ax = 0.0, ay = 0.0;
-  for (int base = 0; base < nsrc; base += kThreads) {
+  const int s0 = blockIdx.y * chunk;
+  const int s1 = min(nsrc, s0 + chunk);
+  for (int base = s0; base < s1; base += kThreads) {
     const int j = base + threadIdx.x;
-    if (j < nsrc) {
+    if (j < s1) {
       sx[threadIdx.x] = sxy[2 * (long)j];
       sy[threadIdx.x] = sxy[2 * (long)j + 1];
       sg[threadIdx.x] = cir[j];
       sr[threadIdx.x] = 1.0 / cor[j];
     }
     __syncthreads();
-    const int cnt = min(kThreads, nsrc - base);
+    const int cnt = min(kThreads, s1 - base);
     for (int k = 0; k < cnt; k++) {
       const double rx = x - sx[k];
       const double ry = y - sy[k];
@@ -45,9 +50,27 @@ __global__ void __launch_bounds__(kThreads) k_direct(int ntgt, const double *__r
     __syncthreads();
   }
   if (valid) {
-    uv[2 * i] = 0.5 * ax / kPi;
-    uv[2 * i + 1] = 0.5 * ay / kPi;
+    atomicAdd(&uv[2 * i], 0.5 * ax / kPi);
+    atomicAdd(&uv[2 * i + 1], 0.5 * ay / kPi);
   }
+}
+
+// FP32 pipe throughput probe: 8 independent FMA chains per thread.
+__global__ void __launch_bounds__(256) k_ffma_probe(float *out, int iters, float b, float c) {
+  float a0 = threadIdx.x * 1e-9f, a1 = a0 + 1e-3f, a2 = a0 + 2e-3f, a3 = a0 + 3e-3f;
+  float a4 = a0 + 4e-3f, a5 = a0 + 5e-3f, a6 = a0 + 6e-3f, a7 = a0 + 7e-3f;
+  for (int i = 0; i < iters; i++) {
+    a0 = fmaf(a0, b, c);
+    a1 = fmaf(a1, b, c);
+    a2 = fmaf(a2, b, c);
+    a3 = fmaf(a3, b, c);
+    a4 = fmaf(a4, b, c);
+    a5 = fmaf(a5, b, c);
+    a6 = fmaf(a6, b, c);
+    a7 = fmaf(a7, b, c);
+  }
+  float s = a0 + a1 + a2 + a3 + a4 + a5 + a6 + a7;
+  if (s == 12345.678f) out[0] = s;
 }
 
 // FP64 pipe throughput probe: 8 independent FMA chains per thread.
@@ -76,10 +99,25 @@ cudaError_t dfma_probe(double *out, int blocks, int iters, cudaStream_t s) {
   return cudaGetLastError();
 }
 
+cudaError_t ffma_probe(float *out, int blocks, int iters, cudaStream_t s) {
+  k_ffma_probe<<<blocks, 256, 0, s>>>(out, iters, 0.999999f, 1e-7f);
+  ::t2d::g_launches.fetch_add(1, std::memory_order_relaxed);
+  return cudaGetLastError();
+}
+
 cudaError_t direct_sum(int ntgt, const double *txy, int nsrc, const double *sxy, const double *cir,
                        const double *cor, double *uv, cudaStream_t s) {
   if (ntgt <= 0) return cudaSuccess;
-  k_direct<<<(ntgt + kThreads - 1) / kThreads, kThreads, 0, s>>>(ntgt, txy, nsrc, sxy, cir, cor, uv);
+  cudaError_t e = cudaMemsetAsync(uv, 0, sizeof(double) * 2 * (size_t)ntgt, s);
+  if (e != cudaSuccess) return e;
+  const int tblocks = (ntgt + kThreads - 1) / kThreads;
+  int chunks = max(1, (152 * 8) / tblocks);
+  int chunk = (nsrc + chunks - 1) / chunks;
+  chunk = ((chunk + kThreads - 1) / kThreads) * kThreads;
+  if (chunk < kThreads) chunk = kThreads;
+  chunks = (nsrc + chunk - 1) / chunk;
+  if (chunks < 1) chunks = 1;
+  k_direct<<<dim3(tblocks, chunks), kThreads, 0, s>>>(ntgt, txy, nsrc, sxy, cir, cor, uv, chunk);
   ::t2d::g_launches.fetch_add(1, std::memory_order_relaxed);
   return cudaGetLastError();
 }

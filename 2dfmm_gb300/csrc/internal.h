@@ -15,6 +15,10 @@ namespace t2d {
 // Key depth: 2 bits per level in a 64-bit key.  A cell holding >= num_p
 // blobs at this level cannot be split further (TREE2D_ERR_TOO_DEEP).
 constexpr int kKeyLevels = 32;
+// Keys are first formed to this depth (fewer FP64 steps and radix passes);
+// the build falls back to kKeyLevels when a cell at this depth still holds
+// >= num_p blobs.  The tree is the same either way.
+constexpr int kShortKeyLevels = 20;
 // Largest number of stored coefficients (nterms) the kernels support.
 constexpr int kMaxTerms = 32;
 
@@ -28,7 +32,7 @@ struct Params {
 // Parameters of the mixed-precision form.
 struct MixedParams {
   int pterms = 16;        // expansion length P (terms 0..P-1) of multipole and local
-  double cutoff = 4.0;    // regularisation correction radius, in units of max sigma
+  double cutoff = 3.0;    // regularisation correction radius, in units of max sigma
   int use_tensor_cores = 1;
 };
 
@@ -46,6 +50,7 @@ struct DevStatus {
   unsigned long long n_pairs;
   unsigned long long n_m2l;
   unsigned long long n_fallback;  // targets whose traversal stack overflowed
+  int deeper;              // build: keys of kShortKeyLevels levels do not suffice
 };
 
 // Bump allocator over one device allocation.  Buffers are 256-byte aligned.
@@ -104,6 +109,7 @@ struct Tree {
   uint8_t *cpl = nullptr;     // per position: levels shared with the next key
   uint8_t *leaf_level = nullptr;  // per position: level of its leaf
   unsigned *cellbase = nullptr;   // per position: id of the first cell it starts
+  int key_levels = 0;             // digits in the keys (kShortKeyLevels or kKeyLevels)
 };
 
 // Per-solver working state (one per library instance).
@@ -140,11 +146,12 @@ int gather_targets(int n, const double *d_xy, const int *d_order, double *tx, do
                    cudaStream_t s);
 
 // --- radix sort (sort.cu) --------------------------------------------
-// Stable LSD radix sort of (key, value) pairs on bits [0, end_bit).
+// Stable LSD radix sort of (key, value) pairs on bits [begin_bit, end_bit)
+// (the other bits must be equal in all keys or irrelevant to the order).
 // Buffers *_alt are scratch of the same size.  The result ends in keys/vals.
 size_t radix_sort_temp_bytes(int n);
 cudaError_t radix_sort_pairs(uint64_t *keys, uint32_t *vals, uint64_t *keys_alt, uint32_t *vals_alt,
-                             int n, int end_bit, void *temp, cudaStream_t s);
+                             int n, int begin_bit, int end_bit, void *temp, cudaStream_t s);
 
 // --- plain FP64 path (plain.cu) ---------------------------------------
 int plain_upward(Workspace &ws, const Tree &t, const Params &p, cudaStream_t s);
@@ -158,6 +165,7 @@ cudaError_t direct_sum(int ntgt, const double *txy, int nsrc, const double *sxy,
 
 // FP64 pipe probe: blocks x 256 threads x iters x 8 FMAs (2 flops each).
 cudaError_t dfma_probe(double *out, int blocks, int iters, cudaStream_t s);
+cudaError_t ffma_probe(float *out, int blocks, int iters, cudaStream_t s);
 
 // Parameters for a device solve, resolved under the library lock.
 int params_for_device_solve(Params &out);

@@ -2,13 +2,34 @@
 //   L[c] += sum_{s<27} T(class(c), s) M[V[c][s]],
 // T(q,s)_lk = (-1)^l C(k+l,l) tau^-(k+l+1), tau the fixed offset of slot s
 // for child class q (scaled expansions make T level independent).
+//
+// Tensor-core form (k_m2l_tc): per child class the V-list M2L of all cells
+// is one dense contraction
+//     D[r, o] = sum_K A[r, K] B_q[K, o],   K = 27 slots x 2P, o < 2P,
+// rows r = target cells of the class, A[r, s*2P + j] = M[V[c_r][s]][j]
+// (gathered, zero where the slot is empty), B_q the real form of the 27
+// complex operators.  One CTA (128 threads) owns 128 rows; per slot it
+// gathers its A chunk into shared memory, the B chunk arrives by a bulk
+// copy (cp.async.bulk, the B images are pre-laid out in global memory),
+// and one thread issues tcgen05.mma kind::tf32 (M=128, N=2P padded to 16,
+// K=8 per instruction) with the FP32 accumulator in TMEM.  Operands are
+// split into TF32 hi + lo parts and three products (hi*hi, hi*lo, lo*hi)
+// keep ~21 bits.  Shared-memory operands use the no-swizzle K-major layout
+// of 8-row x 16-byte core matrices (LBO = 128 B between K neighbours,
+// SBO = 2P/4 * 128 B between 8-row groups).
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
 #include "dev_common.cuh"
 #include "mixed.h"
 
 namespace t2d {
 namespace {
 
-// CUDA-core form: one warp per cell, lane l owns b_l.
+// ------------------------------------------------------------- CUDA cores
+
+// One warp per cell, lane l owns b_l.  The reference form for checking.
 __global__ void __launch_bounds__(256) k_m2l_cc(MixedView m, const float2 *__restrict__ T) {
   const int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   if (c >= m.ncell) return;
@@ -36,11 +57,351 @@ __global__ void __launch_bounds__(256) k_m2l_cc(MixedView m, const float2 *__res
   }
 }
 
+// ------------------------------------------------------------ tensor cores
+
+constexpr int kRows = 128;        // M of the MMA, rows per CTA
+constexpr int kThreadsTC = 128;
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+  uint64_t d = 0;
+  d |= static_cast<uint64_t>((saddr >> 4) & 0x3FFFu);
+  d |= static_cast<uint64_t>((lbo >> 4) & 0x3FFFu) << 16;
+  d |= static_cast<uint64_t>((sbo >> 4) & 0x3FFFu) << 32;
+  d |= static_cast<uint64_t>(1) << 46;  // descriptor version for tcgen05
+  return d;                             // base offset 0, no swizzle
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+
+// Bounded wait: false after `limit` polls (the caller records an error).
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, long limit) {
+  for (long i = 0; i < limit; i++)
+    if (mbar_try_wait(bar, parity)) return true;
+  return false;
+}
+
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_u32(dst)),
+               "l"(src), "r"(bytes), "r"(smem_u32(bar))
+               : "memory");
+}
+
+__device__ __forceinline__ uint32_t tf32_bits(float x) {
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+  return r;
+}
+
+__device__ __forceinline__ void mma_tf32(uint32_t tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                         uint32_t accum) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(
+          tmem),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accum)
+      : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(uint64_t *bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+               : "memory");
+}
+
+struct TcArgs {
+  MixedView m;
+  const int *cls_list;   // [4][ncell]
+  const int *cls_count;  // [4]
+  const float *bimg;     // [4][27][2 (hi,lo)][Npad x Kc] core-matrix images
+  int P, Kc, Npad, tmem_cols, ngroups;
+  long wait_limit;
+};
+
+// Shared memory: 2 stages x {A_hi, A_lo (128 x Kc), B_hi, B_lo (Npad x Kc)}.
+__global__ void __launch_bounds__(kThreadsTC) k_m2l_tc(TcArgs a) {
+  extern __shared__ __align__(1024) unsigned char smem[];
+  __shared__ uint64_t bar_mma[2], bar_b[2];
+  __shared__ uint32_t s_tmem;
+  __shared__ int s_fail;
+
+  const int cls = blockIdx.y;
+  const int count = a.cls_count[cls];
+  const int row0 = blockIdx.x * kRows;
+  if (row0 >= count) return;  // uniform for the block
+  const MixedView &m = a.m;
+  const int P = a.P, Kc = a.Kc, Npad = a.Npad;
+  const uint32_t a_bytes = kRows * Kc * 4, b_bytes = Npad * Kc * 4;
+  const uint32_t stage_bytes = 2 * a_bytes + 2 * b_bytes;
+  const uint32_t sbo_a = (Kc / 4) * 128, sbo_b = sbo_a, lbo = 128;
+  const int tid = threadIdx.x, warp = tid >> 5;
+
+  if (tid == 0) {
+    mbar_init(&bar_mma[0], 1);
+    mbar_init(&bar_mma[1], 1);
+    mbar_init(&bar_b[0], 1);
+    mbar_init(&bar_b[1], 1);
+    s_fail = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&s_tmem)),
+                 "r"(a.tmem_cols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = s_tmem;
+
+  const int row = row0 + tid;
+  const bool valid = row < count;
+  const int cell = valid ? a.cls_list[(size_t)cls * m.ncell + row] : -1;
+  const int *V = valid ? m.vlist + (size_t)cell * 27 : nullptr;
+  // M = 128, N = Npad, A/B TF32 K-major, D FP32
+  const uint32_t idesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(Npad >> 3) << 17) | ((uint32_t)(kRows >> 4) << 24);
+  const float *bbase = a.bimg + (size_t)cls * 27 * 2 * (Npad * Kc);
+
+  uint32_t phase_mma[2] = {0, 0}, phase_b[2] = {0, 0};
+  bool pending[2] = {false, false};
+  bool b_inflight[2] = {false, false};  // thread 0: bulk copy issued, not yet waited for
+  // Slot chunks are spread over `ngroups` accumulators (TMEM column blocks
+  // of Npad); each accumulates few MMAs and the partial sums are added in
+  // FP32 registers at the end, which keeps the accumulation error small.
+  bool gfirst[8] = {true, true, true, true, true, true, true, true};
+  int issued = 0;
+  for (int s = 0; s < 27; s++) {
+    const int src = valid ? V[s] : -1;
+    if (__syncthreads_or(s_fail)) break;         // a wait gave up: stop issuing
+    if (!__syncthreads_or(src >= 0)) continue;  // no row of the tile has this slot
+    const int st = issued & 1;
+    unsigned char *stage = smem + st * stage_bytes;
+    float *Ahi = reinterpret_cast<float *>(stage);
+    float *Alo = reinterpret_cast<float *>(stage + a_bytes);
+    float *Bhi = reinterpret_cast<float *>(stage + 2 * a_bytes);
+    float *Blo = reinterpret_cast<float *>(stage + 2 * a_bytes + b_bytes);
+    // the MMAs that last read this stage must be done before it is rewritten
+    if (pending[st]) {
+      if (mbar_wait(&bar_mma[st], phase_mma[st], a.wait_limit)) {
+        phase_mma[st] ^= 1;
+        pending[st] = false;
+      } else {
+        s_fail = 1;
+      }
+    }
+    if (__syncthreads_or(s_fail)) break;
+    // B chunk: one bulk copy of the pre-laid-out hi and lo images
+    if (tid == 0) {
+      mbar_expect_tx(&bar_b[st], 2 * b_bytes);
+      const float *bsrc = bbase + (size_t)s * 2 * (Npad * Kc);
+      bulk_g2s(Bhi, bsrc, 2 * b_bytes, &bar_b[st]);
+      b_inflight[st] = true;
+    }
+    // A chunk: this thread's row, split into TF32 hi and lo
+    {
+      const int r = tid;
+      const uint32_t rbase = (uint32_t)(r >> 3) * sbo_a + (uint32_t)(r & 7) * 16;
+      const float4 *msrc = src >= 0 ? reinterpret_cast<const float4 *>(m.M + (size_t)src * 2 * P) : nullptr;
+      for (int kk = 0; kk < Kc / 4; kk++) {
+        float4 v = msrc ? msrc[kk] : make_float4(0.f, 0.f, 0.f, 0.f);
+        float4 h, l;
+        h.x = __uint_as_float(tf32_bits(v.x));
+        h.y = __uint_as_float(tf32_bits(v.y));
+        h.z = __uint_as_float(tf32_bits(v.z));
+        h.w = __uint_as_float(tf32_bits(v.w));
+        l.x = v.x - h.x;
+        l.y = v.y - h.y;
+        l.z = v.z - h.z;
+        l.w = v.w - h.w;
+        const uint32_t off = rbase + (uint32_t)kk * lbo;
+        *reinterpret_cast<float4 *>(reinterpret_cast<unsigned char *>(Ahi) + off) = h;
+        *reinterpret_cast<float4 *>(reinterpret_cast<unsigned char *>(Alo) + off) = l;
+      }
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    __syncthreads();
+    bool b_ok = true;
+    if (tid == 0) {
+      b_ok = mbar_wait(&bar_b[st], phase_b[st], a.wait_limit);
+      if (b_ok) {
+        phase_b[st] ^= 1;
+        b_inflight[st] = false;
+      } else {
+        s_fail = 1;
+      }
+    }
+    if (tid == 0 && b_ok) {
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const uint32_t ah = smem_u32(Ahi), al = smem_u32(Alo), bh = smem_u32(Bhi), bl = smem_u32(Blo);
+      const int g = issued % a.ngroups;
+      const uint32_t dcol = tmem + (uint32_t)(g * Npad);
+      for (int t = 0; t < Kc / 8; t++) {
+        const uint32_t ko = (uint32_t)t * 2 * lbo;
+        const uint64_t dah = smem_desc(ah + ko, lbo, sbo_a), dal = smem_desc(al + ko, lbo, sbo_a);
+        const uint64_t dbh = smem_desc(bh + ko, lbo, sbo_b), dbl = smem_desc(bl + ko, lbo, sbo_b);
+        mma_tf32(dcol, dah, dbh, idesc, gfirst[g] ? 0u : 1u);
+        gfirst[g] = false;
+        mma_tf32(dcol, dah, dbl, idesc, 1u);
+        mma_tf32(dcol, dal, dbh, idesc, 1u);
+      }
+      mma_commit(&bar_mma[st]);
+    }
+    // every thread marks the stage busy only if its MMAs were issued
+    if (!__syncthreads_or(!b_ok)) {
+      pending[st] = true;
+      issued++;
+    }
+  }
+  // drain: every stage with MMAs in flight (bounded; a failed wait is
+  // retried once more below before TMEM and shared memory are released)
+  for (int st = 0; st < 2; st++) {
+    if (pending[st]) {
+      if (mbar_wait(&bar_mma[st], phase_mma[st], a.wait_limit)) {
+        phase_mma[st] ^= 1;
+        pending[st] = false;
+      } else {
+        s_fail = 1;
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (issued > 0 && !s_fail) {
+    // Row `tid` lives in TMEM lane tid; warp w reads lanes 32w..32w+31.  All
+    // lanes of the warp execute the loads (they are warp-collective); only
+    // lanes with a row write.
+    const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16);
+    float *dst = valid ? m.L + (size_t)cell * 2 * P : nullptr;
+    const int used = issued < a.ngroups ? issued : a.ngroups;
+    for (int c0 = 0; c0 < 2 * P; c0 += 8) {
+      float acc[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+      for (int g = 0; g < used; g++) {
+        uint32_t r[8];
+        asm volatile(
+            "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];\n"
+            : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+            : "r"(taddr + (uint32_t)(g * Npad + c0)));
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+        for (int j = 0; j < 8; j++) acc[j] += __uint_as_float(r[j]);
+      }
+      if (dst)
+        for (int j = 0; j < 8 && c0 + j < 2 * P; j++) dst[c0 + j] += acc[j];
+    }
+  }
+  if (s_fail) {
+    // a wait gave up: give MMAs still in flight one more bounded wait
+    // before the TMEM and shared memory are released
+    for (int st = 0; st < 2; st++) {
+      if (pending[st]) mbar_wait(&bar_mma[st], phase_mma[st], a.wait_limit);
+      if (tid == 0 && b_inflight[st]) mbar_wait(&bar_b[st], phase_b[st], a.wait_limit);
+    }
+  }
+  if (s_fail && tid == 0) set_err(m.st, TREE2D_ERR_TIMEOUT);
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(a.tmem_cols) : "memory");
+}
+
+// Cells of level >= 2, grouped by child class (order within a class is
+// irrelevant: every row's sum is its own).
+__global__ void k_class_lists(MixedView m, int *list, int *count) {
+  int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= m.ncell || m.level[c] < 2) return;
+  const int cls = (m.ix[c] & 1) + 2 * (m.iy[c] & 1);
+  const int pos = atomicAdd(&count[cls], 1);
+  list[(size_t)cls * m.ncell + pos] = c;
+}
+
+uint32_t tf32_round_host(float x) {
+  uint32_t b;
+  std::memcpy(&b, &x, 4);
+  if ((b & 0x7f800000u) != 0x7f800000u) b = (b + 0x1000u) & 0xffffe000u;  // to nearest, ties away
+  return b;
+}
+
 }  // namespace
 
 int m2l_cuda_cores(MixedView &m, const float *tables, cudaStream_t s) {
   k_m2l_cc<<<(int)(((long)m.ncell * 32 + 255) / 256), 256, 0, s>>>(m, reinterpret_cast<const float2 *>(tables));
   g_launches.fetch_add(1, std::memory_order_relaxed);
+  T2D_CUDA_TRY(cudaGetLastError());
+  return TREE2D_OK;
+}
+
+int m2l_npad(int P) { return ((2 * P + 15) / 16) * 16; }
+
+void m2l_b_images(int P, const float *h_m2l, std::vector<float> &img) {
+  const int Kc = 2 * P, Npad = m2l_npad(P);
+  const size_t chunk = (size_t)Npad * Kc;
+  img.assign((size_t)4 * 27 * 2 * chunk, 0.f);
+  const uint32_t sbo = (uint32_t)(Kc / 4) * 128;
+  for (int q = 0; q < 4; q++)
+    for (int s = 0; s < 27; s++) {
+      const float *T = h_m2l + ((size_t)q * 27 + s) * P * P * 2;  // [l][k] complex
+      float *hi = img.data() + ((size_t)q * 27 + s) * 2 * chunk;
+      float *lo = hi + chunk;
+      for (int k = 0; k < Kc; k++)
+        for (int o = 0; o < Npad; o++) {
+          // B[k][o]: rows k<P take a_re, k>=P a_im; columns o<P give b_re, o>=P b_im
+          float v = 0.f;
+          if (o < 2 * P) {
+            const int kk = k % P, l = o % P;
+            const float tre = T[((size_t)l * P + kk) * 2], tim = T[((size_t)l * P + kk) * 2 + 1];
+            const bool kim = k >= P, oim = o >= P;
+            v = !kim ? (!oim ? tre : tim) : (!oim ? -tim : tre);
+          }
+          const uint32_t hb = tf32_round_host(v);
+          float h;
+          std::memcpy(&h, &hb, 4);
+          const float l = v - h;
+          const size_t off = ((size_t)(o >> 3) * sbo + (size_t)(k >> 2) * 128 + (size_t)(o & 7) * 16 + (size_t)(k & 3) * 4) / 4;
+          hi[off] = h;
+          lo[off] = l;
+        }
+    }
+}
+
+int m2l_tensor_cores(MixedView &m, const float *bimg, int *cls_list, int *cls_count, cudaStream_t s) {
+  const int P = m.P, Kc = 2 * P, Npad = m2l_npad(P);
+  if (Kc % 8 != 0) return TREE2D_ERR_BAD_PARAMS;  // K of one MMA is 8 TF32 elements
+  T2D_CUDA_TRY(cudaMemsetAsync(cls_count, 0, 4 * sizeof(int), s));
+  k_class_lists<<<(m.ncell + 255) / 256, 256, 0, s>>>(m, cls_list, cls_count);
+  TcArgs a;
+  a.m = m;
+  a.cls_list = cls_list;
+  a.cls_count = cls_count;
+  a.bimg = bimg;
+  a.P = P;
+  a.Kc = Kc;
+  a.Npad = Npad;
+  a.tmem_cols = 256;                            // two CTAs per SM fill the 512 columns
+  a.ngroups = 256 / Npad < 8 ? 256 / Npad : 8;
+  a.wait_limit = 1l << 22;  // polls; a healthy wait ends within microseconds
+  const size_t smem = 2 * (2 * (size_t)kRows * Kc * 4 + 2 * (size_t)Npad * Kc * 4);
+  T2D_CUDA_TRY(cudaFuncSetAttribute(k_m2l_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  dim3 grid((m.ncell + kRows - 1) / kRows, 4);
+  k_m2l_tc<<<grid, kThreadsTC, smem, s>>>(a);
+  g_launches.fetch_add(2, std::memory_order_relaxed);
   T2D_CUDA_TRY(cudaGetLastError());
   return TREE2D_OK;
 }

@@ -766,27 +766,33 @@ int mixed_solve(Workspace &ws, const Tree &t, const MixedParams &mp, double *d_u
   if (P < 2 || P > kMaxP) return TREE2D_ERR_BAD_PARAMS;
   const int n = t.n, nc = t.ncell, nl = t.nleaf;
   // ---- operators (per P, cached)
+  const bool tc = mp.use_tensor_cores && (P % 4 == 0);
+  const size_t n_m2l = (size_t)4 * 27 * P * P * 2, n_tr = (size_t)4 * kMaxP * kMaxP * 2;
+  const size_t n_img = (size_t)4 * 27 * 2 * m2l_npad(P) * 2 * P;
   if (ws.mx_tables_P != P) {
-    std::vector<float> m2l((size_t)4 * 27 * P * P * 2), m2m((size_t)4 * kMaxP * kMaxP * 2),
-        l2l((size_t)4 * kMaxP * kMaxP * 2);
+    std::vector<float> m2l(n_m2l), m2m(n_tr), l2l(n_tr), img;
     T2D_CUDA_TRY(mixed_tables(P, m2l.data(), m2m.data(), l2l.data()));
-    size_t need = Arena::bytes_for(m2l.size(), 4) + 2 * Arena::bytes_for(m2m.size(), 4);
+    m2l_b_images(P, m2l.data(), img);
+    size_t need = Arena::bytes_for(n_m2l, 4) + 2 * Arena::bytes_for(n_tr, 4) + Arena::bytes_for(n_img, 4);
     T2D_CUDA_TRY(ws.mx_tables.reserve(need));
     ws.mx_tables.reset();
-    float *dm2l = ws.mx_tables.take<float>(m2l.size());
-    float *dm2m = ws.mx_tables.take<float>(m2m.size());
-    float *dl2l = ws.mx_tables.take<float>(l2l.size());
-    T2D_CUDA_TRY(cudaMemcpy(dm2l, m2l.data(), m2l.size() * 4, cudaMemcpyHostToDevice));
-    T2D_CUDA_TRY(cudaMemcpy(dm2m, m2m.data(), m2m.size() * 4, cudaMemcpyHostToDevice));
-    T2D_CUDA_TRY(cudaMemcpy(dl2l, l2l.data(), l2l.size() * 4, cudaMemcpyHostToDevice));
+    float *dm2l = ws.mx_tables.take<float>(n_m2l);
+    float *dm2m = ws.mx_tables.take<float>(n_tr);
+    float *dl2l = ws.mx_tables.take<float>(n_tr);
+    float *dimg = ws.mx_tables.take<float>(n_img);
+    T2D_CUDA_TRY(cudaMemcpy(dm2l, m2l.data(), n_m2l * 4, cudaMemcpyHostToDevice));
+    T2D_CUDA_TRY(cudaMemcpy(dm2m, m2m.data(), n_tr * 4, cudaMemcpyHostToDevice));
+    T2D_CUDA_TRY(cudaMemcpy(dl2l, l2l.data(), n_tr * 4, cudaMemcpyHostToDevice));
+    T2D_CUDA_TRY(cudaMemcpy(dimg, img.data(), n_img * 4, cudaMemcpyHostToDevice));
     ws.mx_tables_P = P;
   } else {
     T2D_CUDA_TRY(mixed_tables(P, nullptr, nullptr, nullptr));
   }
   ws.mx_tables.reset();
-  const float *dm2l = ws.mx_tables.take<float>((size_t)4 * 27 * P * P * 2);
-  const float *dm2m = ws.mx_tables.take<float>((size_t)4 * kMaxP * kMaxP * 2);
-  const float *dl2l = ws.mx_tables.take<float>((size_t)4 * kMaxP * kMaxP * 2);
+  const float *dm2l = ws.mx_tables.take<float>(n_m2l);
+  const float *dm2m = ws.mx_tables.take<float>(n_tr);
+  const float *dl2l = ws.mx_tables.take<float>(n_tr);
+  const float *dimg = ws.mx_tables.take<float>(n_img);
 
   // ---- arrays
   size_t need = 0;
@@ -797,6 +803,7 @@ int mixed_solve(Workspace &ws, const Tree &t, const MixedParams &mp, double *d_u
   need += Arena::bytes_for((size_t)nc * 27, 4) + Arena::bytes_for((size_t)nc * 8, 4);
   need += Arena::bytes_for((size_t)nl + 1, 4) * 3;
   need += Arena::bytes_for((size_t)nc * 2 * P, 4) * 2;
+  need += Arena::bytes_for((size_t)nc * 4, 4) + 1024;  // class lists + counts
   need += 256;
   T2D_CUDA_TRY(ws.mx_arena.reserve(need));
   ws.mx_arena.reset();
@@ -837,6 +844,8 @@ int mixed_solve(Workspace &ws, const Tree &t, const MixedParams &mp, double *d_u
   m.M = ws.mx_arena.take<float>((size_t)nc * 2 * P);
   m.L = ws.mx_arena.take<float>((size_t)nc * 2 * P);
   unsigned *rc_bits = ws.mx_arena.take<unsigned>(1);
+  int *cls_list = ws.mx_arena.take<int>((size_t)nc * 4);
+  int *cls_count = ws.mx_arena.take<int>(4);
   m.rc_ptr = reinterpret_cast<const float *>(rc_bits);
   m.m2m = reinterpret_cast<const float2 *>(dm2m);
   m.l2l = reinterpret_cast<const float2 *>(dl2l);
@@ -867,13 +876,15 @@ int mixed_solve(Workspace &ws, const Tree &t, const MixedParams &mp, double *d_u
   rc = mixed_upward(m, t.depth, s);
   if (rc) return rc;
   T2D_CUDA_TRY(cudaMemsetAsync(m.L, 0, sizeof(float) * (size_t)nc * 2 * P, s));
-  rc = m2l_cuda_cores(m, dm2l, s);
+  rc = tc ? m2l_tensor_cores(m, dimg, cls_list, cls_count, s) : m2l_cuda_cores(m, dm2l, s);
   if (rc) return rc;
+  st.m2l_path = tc ? 2 : 1;
   rc = mixed_downward(m, t.depth, s);
   if (rc) return rc;
+  T2D_CUDA_TRY(cudaEventRecord(ws.ev[4], s));
   rc = mixed_evaluate(m, d_uv, t.perm, s);
   if (rc) return rc;
-  (void)st;
+  T2D_CUDA_TRY(cudaEventRecord(ws.ev[5], s));
   return TREE2D_OK;
 }
 

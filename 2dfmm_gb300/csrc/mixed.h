@@ -1,6 +1,8 @@
 // Mixed-precision FMM: device view and host entry points (mixed.cu, m2l.cu).
 #pragma once
 
+#include <vector>
+
 #include "internal.h"
 
 namespace t2d {
@@ -46,6 +48,11 @@ int mixed_evaluate(MixedView &m, double *uv, const int *perm, cudaStream_t s);
 // M2L over the V lists (m2l.cu): L[c] += sum_s T(class(c), s) M[V[c][s]].
 // `tables` is the device copy of the [4][27][P][P] complex operators.
 int m2l_cuda_cores(MixedView &m, const float *tables, cudaStream_t s);
+// Tensor-core form: needs P % 4 == 0.  `bimg` are the B operator images
+// (m2l_b_images), cls_list/cls_count scratch of 4*ncell and 4 ints.
+int m2l_tensor_cores(MixedView &m, const float *bimg, int *cls_list, int *cls_count, cudaStream_t s);
+int m2l_npad(int P);
+void m2l_b_images(int P, const float *h_m2l, std::vector<float> &img);
 
 // Whole mixed solve on a built tree: lists, upward, M2L, downward,
 // evaluation; uv written in original blob order.  Synchronises the stream

@@ -1,7 +1,8 @@
 // Stable LSD radix sort of (uint64 key, uint32 value) pairs, 8 bits per
 // pass, reduce-then-scan form:
 //   upsweep   : per tile (4096 pairs) digit counts  -> counts[digit][tile]
-//   scan      : exclusive scan of counts in digit-major order (one block)
+//   scan      : per digit, exclusive scan of its tile counts (one block per
+//               digit); digit totals are scanned inside the downsweep
 //   downsweep : stable rank inside the tile (warp match + per-warp running
 //               counts), scatter to counts-scan offset + rank.
 // Tiles are processed warp-striped: warp w owns 512 consecutive pairs, its
@@ -17,6 +18,7 @@ constexpr int kWarps = kThreads / 32;
 constexpr int kItems = 16;                    // per thread
 constexpr int kTile = kThreads * kItems;      // 4096
 constexpr int kBins = 256;
+static_assert(kThreads == kBins, "the downsweep scans the digit totals with one thread per digit");
 
 __device__ __forceinline__ unsigned lanemask_lt() {
   unsigned m;
@@ -43,37 +45,56 @@ __global__ void __launch_bounds__(kThreads) k_upsweep(const uint64_t *__restrict
   for (int d = threadIdx.x; d < kBins; d += kThreads) counts[(size_t)d * ntiles + blockIdx.x] = hist[d];
 }
 
-// Exclusive scan of `len` counts with one block of 1024 threads.
-__global__ void __launch_bounds__(1024) k_scan_counts(unsigned *counts, long len) {
-  __shared__ unsigned long long part[1024];
+// One block per digit: exclusive scan of counts[d][0..ntiles) in place,
+// total -> totals[d].
+__global__ void __launch_bounds__(1024) k_scan_digit(unsigned *counts, int ntiles, unsigned *totals) {
+  __shared__ unsigned part[1024];
+  unsigned *c = counts + (size_t)blockIdx.x * ntiles;
   const int t = threadIdx.x;
-  const long per = (len + 1023) / 1024;
-  const long b = t * per, e = min(len, b + per);
-  unsigned long long s = 0;
-  for (long i = b; i < e; i++) s += counts[i];
+  const int per = (ntiles + 1023) / 1024;
+  const int b = t * per, e = min(ntiles, b + per);
+  unsigned s = 0;
+  for (int i = b; i < e; i++) s += c[i];
   part[t] = s;
   __syncthreads();
-  // Hillis-Steele over 1024 partials
   for (int off = 1; off < 1024; off <<= 1) {
-    unsigned long long v = t >= off ? part[t - off] : 0;
+    unsigned v = t >= off ? part[t - off] : 0u;
     __syncthreads();
     part[t] += v;
     __syncthreads();
   }
-  unsigned long long run = t == 0 ? 0 : part[t - 1];
-  for (long i = b; i < e; i++) {
-    unsigned c = counts[i];
-    counts[i] = (unsigned)run;
-    run += c;
+  unsigned run = t == 0 ? 0u : part[t - 1];
+  for (int i = b; i < e; i++) {
+    unsigned x = c[i];
+    c[i] = run;
+    run += x;
   }
+  if (t == 1023) totals[blockIdx.x] = part[1023];
 }
 
 __global__ void __launch_bounds__(kThreads) k_downsweep(const uint64_t *__restrict__ kin,
                                                         const uint32_t *__restrict__ vin,
                                                         uint64_t *__restrict__ kout, uint32_t *__restrict__ vout,
                                                         int n, int shift, const unsigned *__restrict__ offs,
-                                                        int ntiles) {
+                                                        int ntiles, const unsigned *__restrict__ totals) {
   __shared__ unsigned wcount[kWarps][kBins];
+  __shared__ unsigned dbase[kBins];
+  {
+    // exclusive scan of the 256 digit totals (kThreads == kBins)
+    const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+    const unsigned v = totals[t];
+    unsigned incl = v;
+    for (int o = 1; o < 32; o <<= 1) {
+      unsigned u = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += u;
+    }
+    __shared__ unsigned wsum[kWarps];
+    if (lane == 31) wsum[w] = incl;
+    __syncthreads();
+    unsigned base = 0;
+    for (int k = 0; k < w; k++) base += wsum[k];
+    dbase[t] = base + incl - v;
+  }
   for (int i = threadIdx.x; i < kWarps * kBins; i += kThreads) (&wcount[0][0])[i] = 0;
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -99,7 +120,7 @@ __global__ void __launch_bounds__(kThreads) k_downsweep(const uint64_t *__restri
   }
   __syncthreads();
   for (int d = threadIdx.x; d < kBins; d += kThreads) {
-    unsigned run = offs[(size_t)d * ntiles + blockIdx.x];
+    unsigned run = dbase[d] + offs[(size_t)d * ntiles + blockIdx.x];
 #pragma unroll
     for (int w = 0; w < kWarps; w++) {
       unsigned c = wcount[w][d];
@@ -124,23 +145,24 @@ __global__ void __launch_bounds__(kThreads) k_downsweep(const uint64_t *__restri
 
 size_t radix_sort_temp_bytes(int n) {
   long ntiles = (n + kTile - 1) / kTile;
-  return (size_t)kBins * (size_t)(ntiles > 0 ? ntiles : 1) * sizeof(unsigned);
+  return (size_t)kBins * (size_t)(ntiles > 0 ? ntiles : 1) * sizeof(unsigned) + kBins * sizeof(unsigned);
 }
 
 cudaError_t radix_sort_pairs(uint64_t *keys, uint32_t *vals, uint64_t *keys_alt, uint32_t *vals_alt, int n,
-                             int end_bit, void *temp, cudaStream_t s) {
+                             int begin_bit, int end_bit, void *temp, cudaStream_t s) {
   if (n <= 1) return cudaSuccess;
   const int ntiles = (n + kTile - 1) / kTile;
   unsigned *counts = static_cast<unsigned *>(temp);
+  unsigned *totals = counts + (size_t)kBins * ntiles;
   uint64_t *ka = keys, *kb = keys_alt;
   uint32_t *va = vals, *vb = vals_alt;
   int passes = 0;
-  for (int shift = 0; shift < end_bit; shift += 8, passes++) {
+  for (int shift = begin_bit; shift < end_bit; shift += 8, passes++) {
     k_upsweep<<<ntiles, kThreads, 0, s>>>(ka, n, shift, counts, ntiles);
     ::t2d::g_launches.fetch_add(1, std::memory_order_relaxed);
-    k_scan_counts<<<1, 1024, 0, s>>>(counts, (long)kBins * ntiles);
+    k_scan_digit<<<kBins, 1024, 0, s>>>(counts, ntiles, totals);
     ::t2d::g_launches.fetch_add(1, std::memory_order_relaxed);
-    k_downsweep<<<ntiles, kThreads, 0, s>>>(ka, va, kb, vb, n, shift, counts, ntiles);
+    k_downsweep<<<ntiles, kThreads, 0, s>>>(ka, va, kb, vb, n, shift, counts, ntiles, totals);
     ::t2d::g_launches.fetch_add(1, std::memory_order_relaxed);
     uint64_t *tk = ka;
     ka = kb;

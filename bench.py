@@ -46,7 +46,11 @@ def parse():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--mode", default="plain", choices=list(MODES))
+    ap.add_argument("--mode", default="mixed", choices=list(MODES))
+    ap.add_argument("--pterms", type=int, default=16, help="mixed form: expansion length")
+    ap.add_argument("--cutoff", type=float, default=3.0, help="mixed form: correction radius / max sigma")
+    ap.add_argument("--cuda-core-m2l", action="store_true", help="mixed form: M2L on CUDA cores")
+    ap.add_argument("--no-plain", action="store_true", help="skip timing the plain FP64 path beside")
     ap.add_argument("--workload", default="two_patch_sheet", choices=["two_patch_sheet", "lamb_oseen", "uniform"])
     ap.add_argument("--n", type=int, default=0, help="override the blob count (exploration only)")
     ap.add_argument("--err-targets", type=int, default=4096)
@@ -220,6 +224,74 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def _time_mode(P, torch, args, mode, arrays, stream, flush, clk=None):
+    """Warm-up, then `steps` timed solves (CUDA events on the launch stream,
+    L2 flushed between steps).  Returns (per-step ms, per-step stats)."""
+    xy, cir, cor, uv, n = arrays
+    P.set_mode(MODES[mode])
+    sp = stream.cuda_stream
+
+    def solve():
+        P.solve_device(xy.data_ptr(), cir.data_ptr(), cor.data_ptr(), uv.data_ptr(), n, sp)
+
+    for _ in range(args.warmup):
+        solve()
+    torch.cuda.synchronize()
+    times, sts = [], []
+    for _ in range(args.steps):
+        flush.fill_(1)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        solve()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        times.append(e0.elapsed_time(e1))
+        sts.append(P.stats())
+    return times, sts
+
+
+def _judge(P, torch, arrays, n, ntgt, sp):
+    """relL2 and max relative error of the last solve against the FP64 direct
+    sum on `ntgt` seeded sampled targets."""
+    xy, cir, cor, uv, _ = arrays
+    W = importlib.import_module("2dfmm_gb300.workloads")
+    idx = W.sample_targets(n, ntgt, seed=7)
+    tidx = torch.from_numpy(idx).to(xy.device)
+    txy = xy[tidx].contiguous()
+    ref = torch.empty_like(txy)
+    P.direct_device(txy.data_ptr(), len(idx), xy.data_ptr(), cir.data_ptr(), cor.data_ptr(), n, ref.data_ptr(), sp)
+    torch.cuda.synchronize()
+    got = uv[tidx]
+    rel_l2 = float(torch.linalg.norm(got - ref) / torch.linalg.norm(ref))
+    max_rel = float(((got - ref).norm(dim=1) / ref.norm(dim=1).clamp_min(1e-300)).max())
+    return {"relL2_vs_fp64_direct": rel_l2, "max_rel_vs_fp64_direct": max_rel, "targets": len(idx)}
+
+
+def _roofline(P, args, mode, b, wname, sts, sp):
+    p = b.nterms - 1
+    st = sts[-1]
+    ms = statistics.mean(s["ms_eval"] for s in sts)
+    tr = roofline_traffic().get(f"{mode}:{wname}")
+    if mode == "plain":
+        flops = st["n_m2s"] * (8 * p + 10) + st["n_pairs"] * 20
+        peak = P.fp64_peak_tflops(stream=sp)
+        return {"bound": "fp64", "achieved": flops / (ms * 1e-3) / 1e12, "peak": peak, "unit": "TFLOP/s",
+                "frac": flops / (ms * 1e-3) / 1e12 / peak, "traffic": tr,
+                "kernel": "k_eval (traversal + M2S + P2P, FP64)",
+                "peak_source": "measured: the library's DFMA probe (8 independent chains per thread)",
+                "algorithmic_flops_per_launch": flops, "ms_per_launch": ms}
+    # mixed: the evaluation kernel (direct pairs, correction pairs, L2P, M2P)
+    flops = st["n_pairs"] * 20 + b.n * 8 * args.pterms
+    peak = P.fp32_peak_tflops(stream=sp)
+    return {"bound": "fp32", "achieved": flops / (ms * 1e-3) / 1e12, "peak": peak, "unit": "TFLOP/s",
+            "frac": flops / (ms * 1e-3) / 1e12 / peak, "traffic": tr,
+            "kernel": "k_eval_mixed (P2P + correction pairs + L2P/M2P, FP32)",
+            "peak_source": "measured: the library's FFMA probe (8 independent chains per thread)",
+            "algorithmic_flops_per_launch": flops, "ms_per_launch": ms}
+
+
 def run_ours(args):
     import torch
     rank, world, local = dist_env()
@@ -232,76 +304,51 @@ def run_ours(args):
     P.load()
     b, wname = workload(args, rank)
     P.set_params(b.nterms, b.num_p, b.theta)
-    P.set_mode(MODES[args.mode])
+    P.set_mixed_params(args.pterms, args.cutoff, not args.cuda_core_m2l)
     n = b.n
     xy = torch.from_numpy(b.xy).to(dev).contiguous()
     cir = torch.from_numpy(b.cir).to(dev)
     cor = torch.from_numpy(b.cor).to(dev)
     uv = torch.empty((n, 2), dtype=torch.float64, device=dev)
+    arrays = (xy, cir, cor, uv, n)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)  # > 129 MB L2
     stream = torch.cuda.current_stream()
     sp = stream.cuda_stream
 
-    def solve():
-        P.solve_device(xy.data_ptr(), cir.data_ptr(), cor.data_ptr(), uv.data_ptr(), n, sp)
-
-    for _ in range(args.warmup):
-        solve()
-    torch.cuda.synchronize()
     if world > 1:
         torch.distributed.barrier()
-    times, st_list = [], []
     with Clocks(local) as clk:
-        for _ in range(args.steps):
-            flush.fill_(1)
-            e0 = torch.cuda.Event(enable_timing=True)
-            e1 = torch.cuda.Event(enable_timing=True)
-            torch.cuda.synchronize()
-            e0.record(stream)
-            solve()
-            e1.record(stream)
-            torch.cuda.synchronize()
-            times.append(e0.elapsed_time(e1))
-            st_list.append(P.stats())
+        times, sts = _time_mode(P, torch, args, args.mode, arrays, stream, flush)
+    clocks = clk.summary()
     total_ms = float(sum(times))
     if world > 1:
         t = torch.tensor([total_ms], device=dev)
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         total_ms = float(t.item())
     value = world * n * args.steps / (total_ms * 1e-3)
-    st = st_list[-1]
-    ms_eval = statistics.mean(s["ms_eval"] for s in st_list)
+    accuracy = _judge(P, torch, arrays, n, args.err_targets, sp)
+    roofline = _roofline(P, args, args.mode, b, wname, sts, sp)
 
-    # roofline of the dominant kernel (the evaluation kernel)
-    p = b.nterms - 1
-    flops = st["n_m2s"] * (8 * p + 10) + st["n_pairs"] * 20
-    achieved = flops / (ms_eval * 1e-3) / 1e12
-    peak = P.fp64_peak_tflops(stream=sp)
-    tr = roofline_traffic().get(f"{args.mode}:{wname}")
-    roofline = {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
-                "traffic": tr, "kernel": "k_eval (traversal + M2S + P2P, FP64)",
-                "peak_source": "measured on this GPU by the library's DFMA probe (tree2d_fp64_probe)",
-                "algorithmic_flops_per_launch": flops, "ms_per_launch": ms_eval}
-
-    # accuracy against the FP64 direct sum (outside the timed region)
-    W = importlib.import_module("2dfmm_gb300.workloads")
-    idx = W.sample_targets(n, args.err_targets, seed=7)
-    tidx = torch.from_numpy(idx).to(dev)
-    txy = xy[tidx].contiguous()
-    ref = torch.empty_like(txy)
-    P.direct_device(txy.data_ptr(), len(idx), xy.data_ptr(), cir.data_ptr(), cor.data_ptr(), n, ref.data_ptr(), sp)
-    torch.cuda.synchronize()
-    got = uv[tidx]
-    rel_l2 = float(torch.linalg.norm(got - ref) / torch.linalg.norm(ref))
-    max_rel = float(((got - ref).norm(dim=1) / ref.norm(dim=1).clamp_min(1e-300)).max())
+    # the plain FP64 path on the same set, for the mixed/plain ratio
+    plain = None
+    if args.mode != "plain" and not args.no_plain:
+        ptimes, psts = _time_mode(P, torch, args, "plain", arrays, stream, flush)
+        plain = {"value": n / (statistics.mean(ptimes) * 1e-3), "unit": UNIT,
+                 "ms_per_step": statistics.mean(ptimes),
+                 "accuracy": _judge(P, torch, arrays, n, args.err_targets, sp)}
+        plain["speedup_of_headline"] = value / world / plain["value"]
+        P.set_mode(MODES[args.mode])
 
     # end to end through the reference-facing calls, host buffers
+    P.set_mode(MODES[args.mode])
     h_xy = torch.empty((n, 2), dtype=torch.float64, pin_memory=True)
     h_cir = torch.empty(n, dtype=torch.float64, pin_memory=True)
     h_cor = torch.empty(n, dtype=torch.float64, pin_memory=True)
     h_xy.numpy()[:] = b.xy
     h_cir.numpy()[:] = b.cir
     h_cor.numpy()[:] = b.cor
+    P.solve_device(xy.data_ptr(), cir.data_ptr(), cor.data_ptr(), uv.data_ptr(), n, sp)
+    torch.cuda.synchronize()
     e2e_times = []
     e2e_steps = max(1, min(args.steps, 3))
     for k in range(1 + e2e_steps):
@@ -320,7 +367,8 @@ def run_ours(args):
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        v, det = cpu_reference(b, st["depth"], 1, 0, args.cpu_sample)
+        depth = sts[-1]["depth"]
+        v, det = cpu_reference(b, depth, 1, 0, args.cpu_sample)
         if v is None:
             cpu = {"value": None, "unit": UNIT, "cores": 0, "kind": "port", "sample": det["unavailable"]}
         else:
@@ -328,28 +376,34 @@ def run_ours(args):
                    "make_tree_s": det["make_tree_s"]}
 
     if rank == 0:
+        st = sts[-1]
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.mode == "plain" else "f32+bf16/tf32",
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64" if args.mode == "plain" else "f32 (tf32x3 tensor M2L, f64 final sum)",
             "data": "synthetic (seeded numpy PCG64), shapes and distributions of the configuration",
             "config": {"workload": wname, "n_blobs": n, "targets": "all blobs", "nterms": b.nterms,
                        "p": b.nterms - 1, "num_p": b.num_p, "theta": b.theta, "mode": args.mode,
+                       "mixed_pterms": args.pterms, "cutoff_sigmas": args.cutoff,
                        "parallelism": f"replicas x{world} (independent blob sets, no collective)",
                        "l2": "flushed between steps (256 MiB write); inputs 134 MB > L2"},
-            "gpu_launches": int(sum(s["n_launches"] for s in st_list)),
+            "gpu_launches": int(sum(s["n_launches"] for s in sts)),
             "e2e": {"value": world * n / e2e_t, "unit": UNIT, "h2d_bytes_per_step": n * 32,
                     "d2h_bytes_per_step": n * 16, "api": "make_tree + biot_tree_batch (host buffers)",
                     "matches_device_path": e2e_match},
             "roofline": roofline,
-            "accuracy": {"relL2_vs_fp64_direct": rel_l2, "max_rel_vs_fp64_direct": max_rel,
-                         "targets": len(idx)},
-            "stages_ms": {"build": statistics.mean(s["ms_build"] for s in st_list),
-                          "upward": statistics.mean(s["ms_upward"] for s in st_list), "eval": ms_eval},
+            "accuracy": accuracy,
+            "stages_ms": {"build": statistics.mean(s["ms_build"] for s in sts),
+                          "upward": statistics.mean(s["ms_upward"] for s in sts),
+                          "eval": statistics.mean(s["ms_eval"] for s in sts)},
             "tree": {"cells": st["n_cells"], "leaves": st["n_leaves"], "depth": st["depth"],
-                     "m2s_per_target": st["n_m2s"] / n, "pairs_per_target": st["n_pairs"] / n},
-            "clocks": clk.summary(),
+                     "m2s_per_target": st["n_m2s"] / n, "pairs_per_target": st["n_pairs"] / n,
+                     "m2l_pairs": st["n_m2l"]},
+            "clocks": clocks,
         }
+        if plain is not None:
+            line["plain_fp64"] = plain
         if cpu is not None:
             line["cpu_baseline"] = cpu
         print(json.dumps(line), flush=True)

@@ -85,7 +85,7 @@ int tree2d_get_mode(void);
  * correction in units of the largest core radius (pairs closer than that
  * which the far field treats as point vortices get exp(-r^2/sigma^2)
  * added back), and whether M2L runs on the tensor cores (1) or on CUDA
- * cores (0, for checking).  Defaults 16, 4.0, 1. */
+ * cores (0, for checking).  Defaults 16, 3.0, 1. */
 int tree2d_set_mixed_params(int pterms, double cutoff_sigmas, int use_tensor_cores);
 
 /* Evaluates n targets (xy interleaved, host memory) into uv (interleaved,
@@ -130,10 +130,12 @@ typedef struct {
   long long n_pairs;      /* direct (target, source) pairs            */
   long long n_m2l;        /* M2L (target cell, source cell) pairs     */
   double ms_build;        /* device time of the tree build            */
-  double ms_upward;       /* S2M + M2M                                */
-  double ms_eval;         /* evaluation at the targets                */
+  double ms_upward;       /* plain: S2M + M2M; mixed: lists, upward
+                             pass, M2L, P2L, L2L                      */
+  double ms_eval;         /* evaluation at the targets (one kernel)   */
   double ms_total;
   long long n_launches;   /* kernels launched by the solve            */
+  int m2l_path;           /* mixed: 1 = CUDA cores, 2 = tensor cores  */
 } tree2d_stats_t;
 int tree2d_get_stats(tree2d_stats_t *out);
 
@@ -157,6 +159,8 @@ int tree2d_direct_device(int ntgt, const double *d_txy, int nsrc, const double *
  * milliseconds through *ms (flops = blocks*256*iters*16).  A measurement
  * helper for roofline reporting; no counterpart in the reference. */
 int tree2d_fp64_probe(int blocks, int iters, void *stream, double *ms);
+/* The same for bits = 64 (DFMA) or 32 (FFMA). */
+int tree2d_pipe_probe(int bits, int blocks, int iters, void *stream, double *ms);
 
 /* Library version string. */
 const char *tree2d_version(void);

@@ -18,7 +18,7 @@ def solve_and_judge(P, torch, b, ntgt=1024, tensor_cores=True, pterms=16):
     dev = torch.device("cuda:0")
     P.set_params(b.nterms, b.num_p, b.theta)
     P.set_mode(P.MODE_MIXED)
-    P.set_mixed_params(pterms, 4.0, tensor_cores)
+    P.set_mixed_params(pterms, 3.0, tensor_cores)
     xy = torch.from_numpy(b.xy).to(dev)
     cir = torch.from_numpy(b.cir).to(dev)
     cor = torch.from_numpy(b.cor).to(dev)
@@ -62,3 +62,20 @@ def test_mixed_make_tree_and_batch_agree(gpu_lib):
     uv = P.biot_tree_batch(b.xy)
     P.set_mode(P.MODE_PLAIN)
     assert np.array_equal(uv, uv_dev)
+
+
+@pytest.mark.gpu
+def test_tensor_core_m2l_matches_cuda_core_m2l(gpu_lib):
+    """The tcgen05 (3xTF32) contraction and the FP32 CUDA-core M2L give the
+    same velocities to FP32 accuracy, and both meet the accuracy bar."""
+    torch = pytest.importorskip("torch")
+    P = gpu_lib
+    W = workloads()
+    b = W.two_patch_sheet(262_144, seed=11)
+    rel_tc, uv_tc = solve_and_judge(P, torch, b, tensor_cores=True)
+    assert P.stats()["m2l_path"] == 2
+    rel_cc, uv_cc = solve_and_judge(P, torch, b, tensor_cores=False)
+    assert P.stats()["m2l_path"] == 1
+    diff = np.linalg.norm(uv_tc - uv_cc) / np.linalg.norm(uv_cc)
+    assert diff <= 1e-6, diff
+    assert rel_tc <= REL_L2 and rel_cc <= REL_L2, (rel_tc, rel_cc)
