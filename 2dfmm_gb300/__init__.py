@@ -32,6 +32,8 @@ EXPORTS = [
     "make_tree", "biot_tree", "tree2d_last_error", "tree2d_error_string", "tree2d_set_params",
     "tree2d_clear_params", "tree2d_get_params", "tree2d_set_mode", "tree2d_get_mode", "tree2d_set_mixed_params", "biot_tree_batch",
     "tree2d_solve_device", "tree2d_solve_device_static", "tree2d_get_stats", "tree2d_export_tree", "tree2d_direct_device", "tree2d_fp64_probe", "tree2d_pipe_probe", "tree2d_version",
+    "tree2d_learn_param_count", "tree2d_learn_set_weights", "tree2d_learn_get_weights", "tree2d_learn_set_options",
+    "tree2d_learn_collect", "tree2d_learn_train", "tree2d_mlp_grad", "tree2d_mlp_forward",
 ]
 
 
@@ -110,6 +112,19 @@ def load(path: str | None = None):
     L.tree2d_pipe_probe.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p, _dp]
     L.tree2d_pipe_probe.restype = ctypes.c_int
     L.tree2d_version.restype = ctypes.c_char_p
+    fp = ctypes.POINTER(ctypes.c_float)
+    L.tree2d_learn_param_count.restype = ctypes.c_int
+    L.tree2d_learn_set_weights.argtypes = [fp, ctypes.c_int]
+    L.tree2d_learn_get_weights.argtypes = [fp, ctypes.c_int]
+    L.tree2d_learn_set_options.argtypes = [ctypes.c_float, ctypes.c_int, ctypes.c_double]
+    L.tree2d_learn_collect.argtypes = [ctypes.c_int, ctypes.c_uint, fp, _ip]
+    L.tree2d_learn_train.argtypes = [ctypes.c_int, fp, _ip, ctypes.c_int, ctypes.c_int, ctypes.c_float,
+                                     ctypes.c_uint, fp]
+    L.tree2d_mlp_grad.argtypes = [ctypes.c_int, fp, _ip, fp, fp, fp]
+    L.tree2d_mlp_forward.argtypes = [ctypes.c_int, fp, fp, fp, ctypes.c_int]
+    for f in ("tree2d_learn_set_weights", "tree2d_learn_get_weights", "tree2d_learn_set_options",
+              "tree2d_learn_collect", "tree2d_learn_train", "tree2d_mlp_grad", "tree2d_mlp_forward"):
+        getattr(L, f).restype = ctypes.c_int
     _lib = L
     return L
 
@@ -249,6 +264,67 @@ def fp32_peak_tflops(blocks: int = 152 * 8, iters: int = 200000, stream: int = 0
     ms = ctypes.c_double()
     _check(load().tree2d_pipe_probe(32, blocks, iters, stream or None, ctypes.byref(ms)), "pipe_probe")
     return blocks * 256.0 * iters * 16.0 / (ms.value * 1e-3) / 1e12
+
+
+# ---------------------------------------------------------------- learned form
+
+def _fp(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+
+
+def learn_param_count() -> int:
+    return load().tree2d_learn_param_count()
+
+
+def learn_set_weights(theta):
+    th = np.ascontiguousarray(theta, np.float32)
+    _check(load().tree2d_learn_set_weights(_fp(th), len(th)), "learn_set_weights")
+
+
+def learn_get_weights():
+    th = np.empty(learn_param_count(), np.float32)
+    _check(load().tree2d_learn_get_weights(_fp(th), len(th)), "learn_get_weights")
+    return th
+
+
+def learn_set_options(direct_bias: float = 1.0, order_margin: int = 1, budget: float = 2e-8):
+    _check(load().tree2d_learn_set_options(direct_bias, order_margin, budget), "learn_set_options")
+
+
+def learn_collect(max_samples: int, seed: int = 0):
+    X = np.empty((max_samples, 16), np.float32)
+    y = np.empty(max_samples, np.int32)
+    n = load().tree2d_learn_collect(max_samples, seed, _fp(X), y.ctypes.data_as(_ip))
+    if n < 0:
+        raise Tree2DError(-n, "learn_collect")
+    return X[:n].copy(), y[:n].copy()
+
+
+def learn_train(X, y, steps: int = 1000, batch: int = 4096, lr: float = 2e-3, seed: int = 0) -> float:
+    X = np.ascontiguousarray(X, np.float32)
+    y = np.ascontiguousarray(y, np.int32)
+    loss = np.zeros(1, np.float32)
+    _check(load().tree2d_learn_train(len(y), _fp(X), y.ctypes.data_as(_ip), steps, batch, lr, seed, _fp(loss)),
+           "learn_train")
+    return float(loss[0])
+
+
+def mlp_grad(X, y, theta):
+    X = np.ascontiguousarray(X, np.float32)
+    y = np.ascontiguousarray(y, np.int32)
+    th = np.ascontiguousarray(theta, np.float32)
+    g = np.empty_like(th)
+    loss = np.zeros(1, np.float32)
+    _check(load().tree2d_mlp_grad(len(y), _fp(X), y.ctypes.data_as(_ip), _fp(th), _fp(g), _fp(loss)), "mlp_grad")
+    return float(loss[0]), g
+
+
+def mlp_forward(X, theta, tensor_cores: bool = False):
+    X = np.ascontiguousarray(X, np.float32)
+    th = np.ascontiguousarray(theta, np.float32)
+    out = np.empty((len(X), 16), np.float32)
+    _check(load().tree2d_mlp_forward(len(X), _fp(X), _fp(th), _fp(out), int(tensor_cores)), "mlp_forward")
+    return out
 
 
 def version() -> str:

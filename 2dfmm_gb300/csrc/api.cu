@@ -9,6 +9,7 @@
 // launch per call would be latency bound.  biot_tree answers blob positions
 // from that table (matched bit for bit on x and y) and evaluates any other
 // point on the GPU with the same kernel.
+#include <algorithm>
 #include <atomic>
 #include <chrono>
 #include <cmath>
@@ -19,6 +20,7 @@
 #include <vector>
 
 #include "dev_common.cuh"
+#include "learn.h"
 #include "mixed.h"
 
 namespace t2d {
@@ -85,6 +87,8 @@ struct Lib {
   bool params_fixed = false;
   int mode = TREE2D_MODE_PLAIN;
   MixedParams mixed;
+  LearnedParams *lp = new LearnedParams();
+  long lp_version = 0;
   std::atomic<int> last_error{0};
   cudaStream_t stream = nullptr;
   bool stream_ready = false;
@@ -195,7 +199,11 @@ int solve(Lib &L, Solver &S, int n, const double *d_xy, const double *d_cir, con
     if (rc) return rc;
   } else {
     T2D_CUDA_TRY(cudaEventRecord(ws.ev[2], s));
-    rc = mixed_solve(ws, S.tree, L.mixed, d_uv, s, st);
+    MixedParams mp = L.mixed;
+    mp.learned = L.mode == TREE2D_MODE_LEARNED;
+    mp.lp = L.lp;
+    mp.lp_version = L.lp_version;
+    rc = mixed_solve(ws, S.tree, mp, d_uv, s, st);
     if (rc) return rc;
   }
   T2D_CUDA_TRY(cudaEventRecord(ws.ev[3], s));
@@ -541,7 +549,8 @@ void tree2d_get_params(int *nterms, int *num_p, double *theta, double *r_min) {
 int tree2d_set_mode(int mode) {
   Lib &L = lib();
   std::lock_guard<std::mutex> lk(L.mu);
-  if (mode != TREE2D_MODE_PLAIN && mode != TREE2D_MODE_MIXED) return fail(TREE2D_ERR_MODE);
+  if (mode != TREE2D_MODE_PLAIN && mode != TREE2D_MODE_MIXED && mode != TREE2D_MODE_LEARNED)
+    return fail(TREE2D_ERR_MODE);
   L.mode = mode;
   return TREE2D_OK;
 }
@@ -652,6 +661,235 @@ int tree2d_pipe_probe(int bits, int blocks, int iters, void *stream, double *ms)
   }
   if (ms) *ms = f;
   return TREE2D_OK;
+}
+
+// ---------------------------------------------------------------- learned form
+
+int tree2d_learn_set_weights(const float *theta, int n) {
+  Lib &L = lib();
+  std::lock_guard<std::mutex> lk(L.mu);
+  if (n != kMlpParams || !theta) return fail(TREE2D_ERR_BAD_INPUT);
+  for (int i = 0; i < n; i++)
+    if (!std::isfinite(theta[i])) return fail(TREE2D_ERR_BAD_INPUT);
+  std::memcpy(L.lp->theta, theta, sizeof(float) * n);
+  L.lp->have_weights = true;
+  L.lp_version++;
+  return TREE2D_OK;
+}
+
+int tree2d_learn_get_weights(float *theta, int n) {
+  Lib &L = lib();
+  std::lock_guard<std::mutex> lk(L.mu);
+  if (n != kMlpParams || !theta) return fail(TREE2D_ERR_BAD_INPUT);
+  if (!L.lp->have_weights) return fail(TREE2D_ERR_NO_TREE);
+  std::memcpy(theta, L.lp->theta, sizeof(float) * n);
+  return TREE2D_OK;
+}
+
+int tree2d_learn_set_options(float direct_bias, int order_margin, double budget) {
+  Lib &L = lib();
+  std::lock_guard<std::mutex> lk(L.mu);
+  if (!std::isfinite(direct_bias) || order_margin < 0 || order_margin > 12 || !(budget > 0.0))
+    return fail(TREE2D_ERR_BAD_PARAMS);
+  L.lp->direct_bias = direct_bias;
+  L.lp->order_margin = order_margin;
+  L.lp->budget = budget;
+  return TREE2D_OK;
+}
+
+int tree2d_learn_param_count(void) { return kMlpParams; }
+
+int tree2d_learn_collect(int max_samples, unsigned seed, float *features, int *labels) {
+  Lib &L = lib();
+  std::lock_guard<std::mutex> lk(L.mu);
+  Workspace &ws = L.dev.ws;
+  if (!ws.mxv || max_samples <= 0 || !features || !labels) return -fail(TREE2D_ERR_NO_TREE);
+  MixedView &m = *ws.mxv;
+  const long nu = ws.mx_tot[0], nk = ws.mx_tot[2];
+  if (nu + nk <= 0) return 0;
+  std::vector<int> uoff(m.nleaf + 1), koff(m.nleaf + 1);
+  cudaStream_t s = L.stream;
+  if (cudaMemcpy(uoff.data(), m.u_off, sizeof(int) * (m.nleaf + 1), cudaMemcpyDeviceToHost) != cudaSuccess ||
+      cudaMemcpy(koff.data(), m.k_off, sizeof(int) * (m.nleaf + 1), cudaMemcpyDeviceToHost) != cudaSuccess)
+    return -fail(TREE2D_ERR_CUDA);
+  const int ns = (int)std::min<long>(max_samples, nu + nk);
+  std::vector<int> smp(3 * (size_t)ns);
+  uint64_t st = 0x9e3779b97f4a7c15ull * (seed + 1);
+  for (int i = 0; i < ns; i++) {
+    st = mix64(st);
+    const long g = (long)(st % (uint64_t)(nu + nk));
+    const int kind = g < nu ? 0 : 1;
+    const int e = (int)(kind == 0 ? g : g - nu);
+    const std::vector<int> &off = kind == 0 ? uoff : koff;
+    const int l = (int)(std::upper_bound(off.begin(), off.end(), e) - off.begin()) - 1;
+    smp[3 * (size_t)i] = l;
+    smp[3 * (size_t)i + 1] = kind;
+    smp[3 * (size_t)i + 2] = e;
+  }
+  int *d_smp = nullptr, *d_lab = nullptr;
+  float *d_feat = nullptr, *d_uref = nullptr;
+  LeafStats *d_stats = nullptr;
+  auto cleanup = [&]() {
+    cudaFree(d_smp);
+    cudaFree(d_lab);
+    cudaFree(d_feat);
+    cudaFree(d_uref);
+    cudaFree(d_stats);
+  };
+  if (cudaMalloc(reinterpret_cast<void **>(&d_smp), sizeof(int) * smp.size()) != cudaSuccess ||
+      cudaMalloc(reinterpret_cast<void **>(&d_lab), sizeof(int) * (size_t)ns) != cudaSuccess ||
+      cudaMalloc(reinterpret_cast<void **>(&d_feat), sizeof(float) * (size_t)ns * kMlpIn) != cudaSuccess ||
+      cudaMalloc(reinterpret_cast<void **>(&d_uref), sizeof(float)) != cudaSuccess ||
+      cudaMalloc(reinterpret_cast<void **>(&d_stats), sizeof(LeafStats) * (size_t)m.ncell) != cudaSuccess) {
+    cleanup();
+    note_cuda_error(cudaErrorMemoryAllocation, "learn_collect");
+    return -fail(TREE2D_ERR_CUDA);
+  }
+  int rc = TREE2D_OK;
+  float uref = 0.f;
+  if (cudaMemcpy(d_smp, smp.data(), sizeof(int) * smp.size(), cudaMemcpyHostToDevice) != cudaSuccess) rc = TREE2D_ERR_CUDA;
+  if (!rc) rc = learned_leaf_stats(m, d_stats, s);
+  if (!rc) rc = learned_uref(m, d_stats, L.dev.tree.root, d_uref, s);
+  if (!rc && cudaMemcpyAsync(&uref, d_uref, 4, cudaMemcpyDeviceToHost, s) != cudaSuccess) rc = TREE2D_ERR_CUDA;
+  if (!rc && cudaStreamSynchronize(s) != cudaSuccess) rc = TREE2D_ERR_CUDA;
+  if (!rc) rc = learned_labels(m, d_stats, d_uref, L.lp->budget * (double)uref, ns, d_smp, d_feat, d_lab, s);
+  if (!rc && cudaStreamSynchronize(s) != cudaSuccess) rc = TREE2D_ERR_CUDA;
+  if (!rc && cudaMemcpy(features, d_feat, sizeof(float) * (size_t)ns * kMlpIn, cudaMemcpyDeviceToHost) != cudaSuccess)
+    rc = TREE2D_ERR_CUDA;
+  if (!rc && cudaMemcpy(labels, d_lab, sizeof(int) * (size_t)ns, cudaMemcpyDeviceToHost) != cudaSuccess)
+    rc = TREE2D_ERR_CUDA;
+  cleanup();
+  if (rc) return -fail(rc);
+  return ns;
+}
+
+// Host arrays in; weights updated in place (initialised from `seed` when
+// none are loaded).
+int tree2d_learn_train(int n, const float *X, const int *y, int steps, int batch, float lr, unsigned seed,
+                       float *loss) {
+  Lib &L = lib();
+  std::lock_guard<std::mutex> lk(L.mu);
+  if (n <= 0 || !X || !y || steps <= 0 || batch <= 0 || !(lr > 0.f)) return fail(TREE2D_ERR_BAD_INPUT);
+  int rc = ensure_stream(L);
+  if (rc) return fail(rc);
+  if (!L.lp->have_weights) {
+    // He-style initialisation from a seeded generator, biases zero
+    uint64_t st = 0x243f6a8885a308d3ull ^ seed;
+    const int fan[8] = {16, 0, 64, 0, 64, 0, 64, 0};
+    const int sz[8] = {1024, 64, 4096, 64, 4096, 64, 1024, 16};
+    int o = 0;
+    for (int b = 0; b < 8; b++)
+      for (int i = 0; i < sz[b]; i++, o++) {
+        if (!fan[b]) {
+          L.lp->theta[o] = 0.f;
+          continue;
+        }
+        st = mix64(st);
+        const double u1 = ((st >> 11) + 1.0) / 9007199254740993.0;
+        st = mix64(st);
+        const double u2 = (st >> 11) / 9007199254740992.0;
+        const double g = std::sqrt(-2.0 * std::log(u1)) * std::cos(6.283185307179586 * u2);
+        L.lp->theta[o] = (float)(g * std::sqrt(2.0 / fan[b]));
+      }
+  }
+  float *d_X = nullptr, *d_th = nullptr, *d_m = nullptr, *d_v = nullptr;
+  int *d_y = nullptr;
+  auto cleanup = [&]() {
+    cudaFree(d_X);
+    cudaFree(d_th);
+    cudaFree(d_m);
+    cudaFree(d_v);
+    cudaFree(d_y);
+  };
+  if (cudaMalloc(reinterpret_cast<void **>(&d_X), sizeof(float) * (size_t)n * kMlpIn) != cudaSuccess ||
+      cudaMalloc(reinterpret_cast<void **>(&d_y), sizeof(int) * (size_t)n) != cudaSuccess ||
+      cudaMalloc(reinterpret_cast<void **>(&d_th), sizeof(float) * kMlpParams) != cudaSuccess ||
+      cudaMalloc(reinterpret_cast<void **>(&d_m), sizeof(float) * kMlpParams) != cudaSuccess ||
+      cudaMalloc(reinterpret_cast<void **>(&d_v), sizeof(float) * kMlpParams) != cudaSuccess) {
+    cleanup();
+    note_cuda_error(cudaErrorMemoryAllocation, "learn_train");
+    return fail(TREE2D_ERR_CUDA);
+  }
+  cudaMemcpy(d_X, X, sizeof(float) * (size_t)n * kMlpIn, cudaMemcpyHostToDevice);
+  cudaMemcpy(d_y, y, sizeof(int) * (size_t)n, cudaMemcpyHostToDevice);
+  cudaMemcpy(d_th, L.lp->theta, sizeof(float) * kMlpParams, cudaMemcpyHostToDevice);
+  cudaMemset(d_m, 0, sizeof(float) * kMlpParams);
+  cudaMemset(d_v, 0, sizeof(float) * kMlpParams);
+  rc = mlp_train(n, d_X, d_y, d_th, d_m, d_v, steps, batch, lr, seed, loss, L.stream);
+  if (!rc && cudaMemcpy(L.lp->theta, d_th, sizeof(float) * kMlpParams, cudaMemcpyDeviceToHost) != cudaSuccess)
+    rc = TREE2D_ERR_CUDA;
+  cleanup();
+  if (rc) return fail(rc);
+  L.lp->have_weights = true;
+  L.lp_version++;
+  return TREE2D_OK;
+}
+
+int tree2d_mlp_grad(int n, const float *X, const int *y, const float *theta, float *grad, float *loss) {
+  Lib &L = lib();
+  std::lock_guard<std::mutex> lk(L.mu);
+  int rc = ensure_stream(L);
+  if (rc) return fail(rc);
+  float *d_X = nullptr, *d_th = nullptr, *d_g = nullptr;
+  int *d_y = nullptr;
+  cudaMalloc(reinterpret_cast<void **>(&d_X), sizeof(float) * (size_t)n * kMlpIn);
+  cudaMalloc(reinterpret_cast<void **>(&d_y), sizeof(int) * (size_t)n);
+  cudaMalloc(reinterpret_cast<void **>(&d_th), sizeof(float) * kMlpParams);
+  cudaMalloc(reinterpret_cast<void **>(&d_g), sizeof(float) * kMlpParams);
+  if (!d_X || !d_y || !d_th || !d_g) rc = TREE2D_ERR_CUDA;
+  if (!rc) {
+    cudaMemcpy(d_X, X, sizeof(float) * (size_t)n * kMlpIn, cudaMemcpyHostToDevice);
+    cudaMemcpy(d_y, y, sizeof(int) * (size_t)n, cudaMemcpyHostToDevice);
+    cudaMemcpy(d_th, theta, sizeof(float) * kMlpParams, cudaMemcpyHostToDevice);
+    rc = mlp_grad(n, d_X, d_y, d_th, d_g, loss, L.stream);
+  }
+  if (!rc && cudaMemcpy(grad, d_g, sizeof(float) * kMlpParams, cudaMemcpyDeviceToHost) != cudaSuccess)
+    rc = TREE2D_ERR_CUDA;
+  cudaFree(d_X);
+  cudaFree(d_y);
+  cudaFree(d_th);
+  cudaFree(d_g);
+  return rc ? fail(rc) : TREE2D_OK;
+}
+
+int tree2d_mlp_forward(int n, const float *X, const float *theta, float *logits, int tensor_cores) {
+  Lib &L = lib();
+  std::lock_guard<std::mutex> lk(L.mu);
+  int rc = ensure_stream(L);
+  if (rc) return fail(rc);
+  T2D_CUDA_TRY(workspace_init(L.dev.ws));
+  float *d_X = nullptr, *d_th = nullptr, *d_out = nullptr, *d_b = nullptr;
+  uint16_t *d_img = nullptr;
+  cudaMalloc(reinterpret_cast<void **>(&d_X), sizeof(float) * (size_t)n * kMlpIn);
+  cudaMalloc(reinterpret_cast<void **>(&d_th), sizeof(float) * kMlpParams);
+  cudaMalloc(reinterpret_cast<void **>(&d_out), sizeof(float) * (size_t)n * kMlpOut);
+  cudaMalloc(reinterpret_cast<void **>(&d_b), sizeof(float) * 208);
+  cudaMalloc(reinterpret_cast<void **>(&d_img), 2 * learn_weight_image_elems());
+  if (!d_X || !d_th || !d_out || !d_b || !d_img) rc = TREE2D_ERR_CUDA;
+  if (!rc) {
+    cudaMemcpy(d_X, X, sizeof(float) * (size_t)n * kMlpIn, cudaMemcpyHostToDevice);
+    cudaMemcpy(d_th, theta, sizeof(float) * kMlpParams, cudaMemcpyHostToDevice);
+    if (tensor_cores) {
+      std::vector<uint16_t> img;
+      std::vector<float> b;
+      learn_weight_images(theta, img, b);
+      cudaMemcpy(d_img, img.data(), img.size() * 2, cudaMemcpyHostToDevice);
+      cudaMemcpy(d_b, b.data(), b.size() * 4, cudaMemcpyHostToDevice);
+      cudaMemsetAsync(L.dev.ws.status, 0, sizeof(DevStatus), L.stream);
+      rc = mlp_forward_tc(n, d_X, d_img, d_b, d_out, L.dev.ws.status, L.stream);
+      if (!rc && cudaStreamSynchronize(L.stream) != cudaSuccess) rc = TREE2D_ERR_CUDA;
+    } else {
+      rc = mlp_forward_cc(n, d_X, d_th, d_out, L.stream);
+    }
+  }
+  if (!rc && cudaMemcpy(logits, d_out, sizeof(float) * (size_t)n * kMlpOut, cudaMemcpyDeviceToHost) != cudaSuccess)
+    rc = TREE2D_ERR_CUDA;
+  cudaFree(d_X);
+  cudaFree(d_th);
+  cudaFree(d_out);
+  cudaFree(d_b);
+  cudaFree(d_img);
+  return rc ? fail(rc) : TREE2D_OK;
 }
 
 const char *tree2d_version(void) { return "tree2d-gb300 0.1 (sm_103a)"; }

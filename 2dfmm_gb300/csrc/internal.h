@@ -29,11 +29,18 @@ struct Params {
   double r_min = 0; // read and kept, unused (as in the reference)
 };
 
+struct LearnedParams;
+struct MixedView;
+struct LeafStats;
+
 // Parameters of the mixed-precision form.
 struct MixedParams {
   int pterms = 16;        // expansion length P (terms 0..P-1) of multipole and local
   double cutoff = 3.0;    // regularisation correction radius, in units of max sigma
   int use_tensor_cores = 1;
+  int learned = 0;        // TREE2D_MODE_LEARNED: near-field decisions by the network
+  const LearnedParams *lp = nullptr;
+  long lp_version = 0;
 };
 
 // Root box, written on the device (quadtree.c:81-99 semantics).
@@ -80,6 +87,7 @@ class Arena {
     return p;
   }
   size_t used() const { return used_; }
+  size_t capacity() const { return cap_; }
   static size_t bytes_for(size_t count, size_t elem) { return (count * elem + 255) & ~size_t(255); }
 
  private:
@@ -121,6 +129,10 @@ struct Workspace {
   Arena mx_lists;     // mixed form: interaction lists
   Arena mx_tables;    // mixed form: translation operators
   int mx_tables_P = 0;
+  Arena lr_arena;     // learned form: weights, leaf statistics, decisions
+  long lr_version = -1;
+  MixedView *mxv = nullptr;  // the last mixed solve's view (kept for sampling)
+  long mx_tot[3] = {0, 0, 0};  // U, W, K list entries of that solve
   DevStatus *status = nullptr;   // device
   DevStatus *h_status = nullptr; // pinned host mirror
   cudaEvent_t ev[6] = {};

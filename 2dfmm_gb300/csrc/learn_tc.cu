@@ -1,0 +1,291 @@
+// Inference of the order-selection MLP on the tensor cores.
+//
+// A persistent CTA (128 threads) loads the BF16 weight images once (bulk
+// copy) and then, per tile of 128 interactions, computes the features of
+// its rows, and runs the four layers as tcgen05.mma kind::f16 (BF16 A and B,
+// FP32 accumulator in TMEM, M = 128, N = 64/64/64/16, K = 16 per
+// instruction): layer input tile in shared memory (no-swizzle K-major core
+// matrices), accumulator read back with tcgen05.ld, bias + GELU in
+// registers, BF16 store as the next layer's input.  The output is the class
+// per interaction (argmax over 14 logits, with a bias towards direct
+// evaluation), or the raw logits on the checking path.
+#include <cuda_bf16.h>
+
+#include <cstring>
+#include <vector>
+
+#include "dev_common.cuh"
+#include "learn.h"
+#include "tc_ptx.cuh"
+
+namespace t2d {
+namespace {
+
+constexpr int kTile = 128;
+constexpr uint32_t kW1Bytes = 64 * 16 * 2, kW2Bytes = 64 * 64 * 2, kW4Bytes = 16 * 64 * 2;
+constexpr uint32_t kWBytes = kW1Bytes + 2 * kW2Bytes + kW4Bytes;  // 20480
+constexpr uint32_t kActBytes = kTile * 64 * 2;                     // 16384
+
+struct InferArgs {
+  MixedView m;
+  const LeafStats *st;
+  const float *u_ref_ptr;
+  const uint16_t *wimg;
+  const float *bias;  // b1[64] b2[64] b3[64] b4[16]
+  float direct_bias;
+  long n_u, n_k;
+  unsigned char *u_dec, *k_dec;
+  const float *X;  // checking path: explicit features [nx][16]
+  long nx;
+  float *logits;   // checking path output [nx][16]
+  long wait_limit;
+};
+
+__device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
+  const uint32_t lo = __bfloat16_as_ushort(__float2bfloat16_rn(a));
+  const uint32_t hi = __bfloat16_as_ushort(__float2bfloat16_rn(b));
+  return lo | (hi << 16);
+}
+
+__device__ __forceinline__ float gelu_fast(float z) {
+  float t;
+  const float u = 0.7978845608028654f * (z + 0.044715f * z * z * z);
+  asm("tanh.approx.f32 %0, %1;" : "=f"(t) : "f"(u));
+  return 0.5f * z * (1.f + t);
+}
+
+// Row r of the activation tile, K = 8*nk elements: element k at
+// (r/8)*SBO + (k/8)*128 + (r%8)*16 + (k%8)*2, SBO = nk*128.
+__device__ __forceinline__ void store_row(unsigned char *tile, int r, const float *v, int K) {
+  const uint32_t sbo = (uint32_t)(K / 8) * 128;
+  unsigned char *base = tile + (uint32_t)(r >> 3) * sbo + (uint32_t)(r & 7) * 16;
+  for (int k8 = 0; k8 < K / 8; k8++) {
+    uint4 q;
+    q.x = pack_bf16(v[8 * k8 + 0], v[8 * k8 + 1]);
+    q.y = pack_bf16(v[8 * k8 + 2], v[8 * k8 + 3]);
+    q.z = pack_bf16(v[8 * k8 + 4], v[8 * k8 + 5]);
+    q.w = pack_bf16(v[8 * k8 + 6], v[8 * k8 + 7]);
+    *reinterpret_cast<uint4 *>(base + (uint32_t)k8 * 128) = q;
+  }
+}
+
+__device__ __forceinline__ int upper_index(const int *off, int n, int e) {
+  // largest l in [0, n) with off[l] <= e
+  int lo = 0, hi = n;
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (off[mid] <= e)
+      lo = mid;
+    else
+      hi = mid;
+  }
+  return lo;
+}
+
+__global__ void __launch_bounds__(kTile) k_mlp_infer(InferArgs a) {
+  extern __shared__ __align__(1024) unsigned char smem[];
+  __shared__ uint64_t bar_w, bar_mma;
+  __shared__ uint32_t s_tmem;
+  __shared__ int s_fail;
+  __shared__ float s_bias[64 * 3 + 16];
+  unsigned char *wsm = smem;
+  unsigned char *act = smem + kWBytes;
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const long total = a.X ? a.nx : a.n_u + a.n_k;
+  const long ntiles = (total + kTile - 1) / kTile;
+  if ((long)blockIdx.x >= ntiles) return;
+
+  if (tid == 0) {
+    mbar_init(&bar_w, 1);
+    mbar_init(&bar_mma, 1);
+    s_fail = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  for (int i = tid; i < 64 * 3 + 16; i += kTile) s_bias[i] = a.bias[i];
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&s_tmem)), "r"(64)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = s_tmem;
+  bool w_inflight = false;
+  if (tid == 0) {
+    mbar_expect_tx(&bar_w, kWBytes);
+    bulk_g2s(wsm, a.wimg, kWBytes, &bar_w);
+    w_inflight = !mbar_wait(&bar_w, 0, a.wait_limit);
+    if (w_inflight) s_fail = 1;
+  }
+  __syncthreads();
+
+  const uint32_t w1 = smem_u32(wsm), w2 = w1 + kW1Bytes, w3 = w2 + kW2Bytes, w4 = w3 + kW2Bytes;
+  const uint32_t aaddr = smem_u32(act);
+  const uint32_t id64 = (1u << 4) | (1u << 7) | (1u << 10) | ((64u >> 3) << 17) | ((uint32_t)(kTile >> 4) << 24);
+  const uint32_t id16 = (1u << 4) | (1u << 7) | (1u << 10) | ((16u >> 3) << 17) | ((uint32_t)(kTile >> 4) << 24);
+  const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16);
+  uint32_t phase = 0;
+  const MixedView &m = a.m;
+  const float u_ref = a.u_ref_ptr ? *a.u_ref_ptr : 1.f;
+
+  bool mma_inflight = false;
+  for (long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    if (__syncthreads_or(s_fail)) break;  // uniform exit after a wait gave up
+    const long gi = tile * kTile + tid;
+    const bool valid = gi < total;
+    int kind = 0;
+    long e = 0;
+    float v[64];
+    if (!valid) {
+      for (int k = 0; k < kMlpIn; k++) v[k] = 0.f;
+    } else if (a.X) {
+      for (int k = 0; k < kMlpIn; k++) v[k] = a.X[gi * kMlpIn + k];
+    } else {
+      kind = gi < a.n_u ? 0 : 1;
+      e = kind == 0 ? gi : gi - a.n_u;
+      const int l = upper_index(kind == 0 ? m.u_off : m.k_off, m.nleaf, (int)e);
+      const int B = m.leaf_cell[l];
+      const int A = kind == 0 ? m.u_idx[e] : m.k_idx[e];
+      interaction_features(m, a.st, B, A, kind, u_ref, v);
+    }
+    store_row(act, tid, v, 16);
+    // layer 1 .. 4
+    for (int layer = 0; layer < 4; layer++) {
+      const int K = layer == 0 ? 16 : 64;
+      const int N = layer == 3 ? 16 : 64;
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      __syncthreads();
+      if (tid == 0) {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const uint32_t wb = layer == 0 ? w1 : (layer == 1 ? w2 : (layer == 2 ? w3 : w4));
+        const uint32_t sbo = (uint32_t)(K / 8) * 128;
+        for (int t = 0; t < K / 16; t++) {
+          const uint64_t ad = smem_desc(aaddr + (uint32_t)t * 256, 128, sbo);
+          const uint64_t bd = smem_desc(wb + (uint32_t)t * 256, 128, sbo);
+          mma_bf16(tmem, ad, bd, N == 64 ? id64 : id16, t > 0 ? 1u : 0u);
+        }
+        mma_commit(&bar_mma);
+      }
+      if (mbar_wait(&bar_mma, phase, a.wait_limit)) {
+        phase ^= 1;
+      } else {
+        s_fail = 1;
+        mma_inflight = true;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      // accumulator row -> bias (+ GELU) in registers
+      const float *bs = s_bias + layer * 64;
+      for (int c0 = 0; c0 < N; c0 += 8) {
+        uint32_t r[8];
+        tmem_ld8(taddr + (uint32_t)c0, r);
+        for (int j = 0; j < 8; j++) {
+          const float z = __uint_as_float(r[j]) + bs[c0 + j];
+          v[c0 + j] = layer < 3 ? gelu_fast(z) : z;
+        }
+      }
+      if (layer < 3) store_row(act, tid, v, 64);
+    }
+    if (valid) {
+      if (a.X) {
+        for (int c = 0; c < kMlpOut; c++) a.logits[gi * kMlpOut + c] = v[c];
+      } else {
+        v[0] += a.direct_bias;
+        int best = 0;
+        for (int c = 1; c < kMlpClasses; c++)
+          if (v[c] > v[best]) best = c;
+        (kind == 0 ? a.u_dec : a.k_dec)[e] = (unsigned char)best;
+      }
+    }
+  }
+  if (s_fail) {
+    // one more bounded wait for work still in flight before TMEM and shared
+    // memory are released
+    if (mma_inflight) mbar_wait(&bar_mma, phase, a.wait_limit);
+    if (w_inflight) mbar_wait(&bar_w, 0, a.wait_limit);
+    if (tid == 0) set_err(m.st, TREE2D_ERR_TIMEOUT);
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(64) : "memory");
+}
+
+uint16_t bf16_host(float x) {
+  uint32_t b;
+  std::memcpy(&b, &x, 4);
+  const uint32_t r = b + 0x7FFFu + ((b >> 16) & 1u);
+  return (uint16_t)(r >> 16);
+}
+
+// W [N][K] row-major -> core-matrix image (rows = N, K contiguous in 16-byte
+// chunks; SBO = K/8*128).
+void image_of(const float *W, int N, int K, uint16_t *out) {
+  const int sbo = K / 8 * 128;
+  for (int j = 0; j < N; j++)
+    for (int k = 0; k < K; k++) {
+      const size_t byte = (size_t)(j / 8) * sbo + (size_t)(k / 8) * 128 + (size_t)(j % 8) * 16 + (size_t)(k % 8) * 2;
+      out[byte / 2] = bf16_host(W[(size_t)j * K + k]);
+    }
+}
+
+}  // namespace
+
+size_t learn_weight_image_elems() { return kWBytes / 2; }
+
+void learn_weight_images(const float *theta, std::vector<uint16_t> &img, std::vector<float> &bias) {
+  img.assign(kWBytes / 2, 0);
+  image_of(theta + 0, 64, 16, img.data());
+  image_of(theta + 1088, 64, 64, img.data() + kW1Bytes / 2);
+  image_of(theta + 5248, 64, 64, img.data() + (kW1Bytes + kW2Bytes) / 2);
+  image_of(theta + 9408, 16, 64, img.data() + (kW1Bytes + 2 * kW2Bytes) / 2);
+  bias.assign(64 * 3 + 16, 0.f);
+  std::memcpy(bias.data(), theta + 1024, 64 * 4);
+  std::memcpy(bias.data() + 64, theta + 5184, 64 * 4);
+  std::memcpy(bias.data() + 128, theta + 9344, 64 * 4);
+  std::memcpy(bias.data() + 192, theta + 10432, 16 * 4);
+}
+
+static int launch_infer(InferArgs &a, long total, cudaStream_t s) {
+  if (total <= 0) return TREE2D_OK;
+  const size_t smem = kWBytes + kActBytes;
+  T2D_CUDA_TRY(cudaFuncSetAttribute(k_mlp_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  const long ntiles = (total + kTile - 1) / kTile;
+  const int grid = (int)(ntiles < 152 * 6 ? ntiles : 152 * 6);
+  a.wait_limit = 1l << 22;
+  k_mlp_infer<<<grid, kTile, smem, s>>>(a);
+  g_launches.fetch_add(1, std::memory_order_relaxed);
+  T2D_CUDA_TRY(cudaGetLastError());
+  return TREE2D_OK;
+}
+
+int learned_decide(MixedView &m, const LeafStats *stats, const float *u_ref_ptr, const uint16_t *wimg,
+                   const float *bias, float direct_bias, long n_u, long n_k, unsigned char *u_dec,
+                   unsigned char *k_dec, cudaStream_t s) {
+  InferArgs a{};
+  a.m = m;
+  a.st = stats;
+  a.u_ref_ptr = u_ref_ptr;
+  a.wimg = wimg;
+  a.bias = bias;
+  a.direct_bias = direct_bias;
+  a.n_u = n_u;
+  a.n_k = n_k;
+  a.u_dec = u_dec;
+  a.k_dec = k_dec;
+  return launch_infer(a, n_u + n_k, s);
+}
+
+int mlp_forward_tc(int n, const float *X, const uint16_t *wimg, const float *bias, float *logits, DevStatus *st,
+                   cudaStream_t s) {
+  InferArgs a{};
+  a.m.st = st;
+  a.wimg = wimg;
+  a.bias = bias;
+  a.X = X;
+  a.nx = n;
+  a.logits = logits;
+  return launch_infer(a, n, s);
+}
+
+}  // namespace t2d

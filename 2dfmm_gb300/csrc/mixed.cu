@@ -39,6 +39,7 @@
 
 #include "dev_common.cuh"
 #include "mixed.h"
+#include "learn.h"
 
 namespace t2d {
 namespace {
@@ -133,6 +134,8 @@ __global__ void k_cell_info(MixedView m) {
   m.iy[c] = iy;
   m.h[c] = (float)m.region[c];
   m.inv_h[c] = (float)(1.0 / m.region[c]);
+  m.cxf[c] = (float)m.cx[c];
+  m.cyf[c] = (float)m.cy[c];
 }
 
 // Per leaf: leaf_of for its positions, FP32 local coordinates, circulation,
@@ -148,6 +151,7 @@ __global__ void k_leaf_setup(MixedView m, const double *x, const double *y, cons
     m.gam[i] = (float)cir[i];
     double s = cor[i];
     m.s2inv[i] = (float)(1.0 / (s * s));
+    m.src4[i] = make_float4(m.loc[i].x, m.loc[i].y, m.gam[i], m.s2inv[i]);
   }
 }
 
@@ -291,12 +295,12 @@ __device__ void uw_walk(const MixedView &m, int b, Emit emit) {
   }
 }
 
+// Distance between the boxes of cells a and b (FP32: only compared with rc).
 __device__ __forceinline__ float box_gap(const MixedView &m, int a, int b) {
-  double gx = fabs(m.cx[a] - m.cx[b]) - 0.5 * (m.region[a] + m.region[b]);
-  double gy = fabs(m.cy[a] - m.cy[b]) - 0.5 * (m.region[a] + m.region[b]);
-  gx = gx > 0 ? gx : 0;
-  gy = gy > 0 ? gy : 0;
-  return (float)sqrt(gx * gx + gy * gy);
+  const float half = 0.5f * (m.h[a] + m.h[b]);
+  const float gx = fmaxf(fabsf(m.cxf[a] - m.cxf[b]) - half, 0.f);
+  const float gy = fmaxf(fabsf(m.cyf[a] - m.cyf[b]) - half, 0.f);
+  return sqrtf(gx * gx + gy * gy);
 }
 
 // Correction leaves of leaf b: not adjacent, box within rc.
@@ -455,7 +459,7 @@ __global__ void k_p2l(MixedView m) {
   float2 acc = make_float2(0.f, 0.f);
   for (int e = 0; e < 8 && X[e] >= 0; e++) {
     const int d = X[e];
-    const float ox = (float)(m.cx[d] - m.cx[c]), oy = (float)(m.cy[d] - m.cy[c]);
+    const float ox = (float)(m.cx[d] - m.cx[c]), oy = (float)(m.cy[d] - m.cy[c]);  // once per X entry
     for (int j = m.begin[d]; j < m.end[d]; j++) {
       float2 z = m.loc[j];
       z.x = (z.x + ox) * ih;
@@ -515,90 +519,174 @@ __device__ __forceinline__ void kahan(float &s, float &cmp, float v) {
   s = t;
 }
 
-// Evaluation: one warp per leaf, targets in chunks of 32.
-__global__ void __launch_bounds__(128) k_eval_mixed(MixedView m, double *uv, const int *perm) {
-  const int l = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-  if (l >= m.nleaf) return;
-  const int B = m.leaf_cell[l];
+// Evaluation: one warp per leaf; each lane owns up to two targets (chunks
+// of 64 targets), so a leaf of <= 64 blobs walks its source lists once.
+// Sources are read as one float4 {x, y, G, 1/sigma^2} (offsets from their
+// leaf centre), the same address for the whole warp.
+__device__ __forceinline__ void far_field(const MixedView &m, int l, int B, float2 zt, float2 &phi) {
   const int P = m.P;
   const float ihB = m.inv_h[B];
   const float *LB = m.L + (size_t)B * 2 * P;
-  const float rc2 = (*m.rc_ptr) * (*m.rc_ptr);
-  unsigned long long pairs = 0;
-  for (int t0 = m.begin[B]; t0 < m.end[B]; t0 += 32) {
-    const int t = t0 + lane;
-    const bool valid = t < m.end[B];
-    const float2 zt = valid ? m.loc[t] : make_float2(0.f, 0.f);
-    // far field: local expansion of B
-    float2 phi = make_float2(0.f, 0.f);
+  const float2 zeta = make_float2(zt.x * ihB, zt.y * ihB);
+  float2 acc = make_float2(LB[P - 1], LB[2 * P - 1]);
+  for (int k = P - 2; k >= 0; k--) {
+    acc = fmul(acc, zeta);
+    acc.x += LB[k];
+    acc.y += LB[P + k];
+  }
+  phi.x = acc.x * ihB;
+  phi.y = acc.y * ihB;
+  for (int e = m.w_off[l]; e < m.w_off[l + 1]; e++) {
+    const int A = m.w_idx[e];
+    const float ih = m.inv_h[A];
+    const float zx = (zt.x + (m.cxf[B] - m.cxf[A])) * ih, zy = (zt.y + (m.cyf[B] - m.cyf[A])) * ih;
+    const float ir2 = 1.f / (zx * zx + zy * zy);
+    const float2 w = make_float2(zx * ir2, -zy * ir2);
+    const float *MA = m.M + (size_t)A * 2 * P;
+    float2 a = make_float2(MA[P - 1], MA[2 * P - 1]);
+    for (int k = P - 2; k >= 0; k--) {
+      a = fmul(a, w);
+      a.x += MA[k];
+      a.y += MA[P + k];
+    }
+    a = fmul(a, w);
+    phi.x += a.x * ih;
+    phi.y += a.y * ih;
+  }
+}
+
+// Direct (U list, regularised kernel) or correction (K list, Gaussian term
+// within rc) contributions of one source leaf to the lane's two targets.
+// Each leaf is summed in plain FP32 and then added with compensation, so
+// the compensated sum costs once per leaf, not once per pair.
+template <bool kCorrection>
+__device__ __forceinline__ void leaf_pairs(const float4 *__restrict__ src, int j0, int j1, float txa, float tya,
+                                           float txb, float tyb, bool two, float rc2, float &sxa, float &sya,
+                                           float &sxb, float &syb) {
+  for (int j = j0; j < j1; j++) {
+    const float4 sj = src[j];
     {
-      const float2 zeta = make_float2(zt.x * ihB, zt.y * ihB);
-      float2 acc = make_float2(LB[P - 1], LB[2 * P - 1]);
-      for (int k = P - 2; k >= 0; k--) {
-        acc = fmul(acc, zeta);
-        acc.x += LB[k];
-        acc.y += LB[P + k];
+      const float rx = txa - sj.x, ry = tya - sj.y;
+      const float r2 = fmaf(rx, rx, ry * ry);
+      float f = 0.f;
+      if (!kCorrection) {
+        if (r2 > 1e-20f) {
+          const float x2 = r2 * sj.w;
+          const float e1f = x2 < 1e-3f ? x2 * (1.f - 0.5f * x2) : 1.f - __expf(-x2);
+          f = __fdividef(sj.z * e1f, r2);
+        }
+      } else if (r2 < rc2) {
+        f = -__fdividef(sj.z * __expf(-r2 * sj.w), r2);
       }
-      phi.x = acc.x * ihB;
-      phi.y = acc.y * ihB;
+      sxa = fmaf(-f, ry, sxa);
+      sya = fmaf(f, rx, sya);
     }
-    // W list: multipoles of small separated cells
-    for (int e = m.w_off[l]; e < m.w_off[l + 1]; e++) {
-      const int A = m.w_idx[e];
-      const float ih = m.inv_h[A];
-      const float ox = (float)(m.cx[B] - m.cx[A]), oy = (float)(m.cy[B] - m.cy[A]);
-      const float zx = (zt.x + ox) * ih, zy = (zt.y + oy) * ih;
-      const float r2 = zx * zx + zy * zy;
-      const float2 w = make_float2(zx / r2, -zy / r2);
-      const float *MA = m.M + (size_t)A * 2 * P;
-      float2 acc = make_float2(MA[P - 1], MA[2 * P - 1]);
-      for (int k = P - 2; k >= 0; k--) {
-        acc = fmul(acc, w);
-        acc.x += MA[k];
-        acc.y += MA[P + k];
+    if (two) {
+      const float rx = txb - sj.x, ry = tyb - sj.y;
+      const float r2 = fmaf(rx, rx, ry * ry);
+      float f = 0.f;
+      if (!kCorrection) {
+        if (r2 > 1e-20f) {
+          const float x2 = r2 * sj.w;
+          const float e1f = x2 < 1e-3f ? x2 * (1.f - 0.5f * x2) : 1.f - __expf(-x2);
+          f = __fdividef(sj.z * e1f, r2);
+        }
+      } else if (r2 < rc2) {
+        f = -__fdividef(sj.z * __expf(-r2 * sj.w), r2);
       }
-      acc = fmul(acc, w);
-      phi.x += acc.x * ih;
-      phi.y += acc.y * ih;
+      sxb = fmaf(-f, ry, sxb);
+      syb = fmaf(f, rx, syb);
     }
-    // near field: U list, regularised kernel; then the Gaussian correction
-    float ax = 0.f, ay = 0.f, cax = 0.f, cay = 0.f;
+  }
+}
+
+// M2P of source leaf A at order p (terms 0..p-1) at a target offset z from
+// leaf B's centre, added to phi.
+__device__ __forceinline__ void m2p_order(const MixedView &m, int B, int A, int p, float2 z, float2 &phi) {
+  const int P = m.P;
+  const float ih = m.inv_h[A];
+  const float zx = (z.x + (m.cxf[B] - m.cxf[A])) * ih, zy = (z.y + (m.cyf[B] - m.cyf[A])) * ih;
+  const float ir2 = 1.f / (zx * zx + zy * zy);
+  const float2 w = make_float2(zx * ir2, -zy * ir2);
+  const float *MA = m.M + (size_t)A * 2 * P;
+  float2 a = make_float2(MA[p - 1], MA[P + p - 1]);
+  for (int k = p - 2; k >= 0; k--) {
+    a = fmul(a, w);
+    a.x += MA[k];
+    a.y += MA[P + k];
+  }
+  a = fmul(a, w);
+  phi.x += a.x * ih;
+  phi.y += a.y * ih;
+}
+
+struct Decisions {
+  const unsigned char *u, *k;  // class per U / K entry; null: all direct
+  int margin;
+};
+
+template <bool kLearned>
+__global__ void __launch_bounds__(128, 8) k_eval_mixed(MixedView m, double *uv, const int *perm, Decisions dec) {
+  const int l = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (l >= m.nleaf) return;
+  const int B = m.leaf_cell[l];
+  const float rc2 = (*m.rc_ptr) * (*m.rc_ptr);
+  const double inv2pi = 0.15915494309189533577;
+  unsigned long long pairs = 0;
+  for (int t0 = m.begin[B]; t0 < m.end[B]; t0 += 64) {
+    const int ta = t0 + lane, tb = t0 + 32 + lane;
+    const bool va = ta < m.end[B], vb = tb < m.end[B];
+    const bool two = __any_sync(0xffffffffu, vb);
+    const float2 za = va ? m.loc[ta] : make_float2(0.f, 0.f);
+    const float2 zb = vb ? m.loc[tb] : make_float2(0.f, 0.f);
+    float2 pa = make_float2(0.f, 0.f), pb = make_float2(0.f, 0.f);
+    far_field(m, l, B, za, pa);
+    if (two) far_field(m, l, B, zb, pb);
+    float axa = 0.f, aya = 0.f, cxa = 0.f, cya = 0.f;
+    float axb = 0.f, ayb = 0.f, cxb = 0.f, cyb = 0.f;
     for (int pass = 0; pass < 2; pass++) {
       const int e0 = pass == 0 ? m.u_off[l] : m.k_off[l];
       const int e1 = pass == 0 ? m.u_off[l + 1] : m.k_off[l + 1];
       const int *idx = pass == 0 ? m.u_idx : m.k_idx;
       for (int e = e0; e < e1; e++) {
         const int A = idx[e];
-        const float ox = (float)(m.cx[B] - m.cx[A]), oy = (float)(m.cy[B] - m.cy[A]);
-        const float tx = zt.x + ox, ty = zt.y + oy;
-        const int j0 = m.begin[A], j1 = m.end[A];
-        for (int j = j0; j < j1; j++) {
-          const float2 zs = m.loc[j];
-          const float rx = tx - zs.x, ry = ty - zs.y;
-          const float r2 = rx * rx + ry * ry;
-          float f;
-          if (pass == 0) {
-            if (!(r2 > 1e-20f)) continue;
-            const float x2 = r2 * m.s2inv[j];
-            const float e1f = x2 < 1e-3f ? x2 * (1.f - 0.5f * x2) : 1.f - __expf(-x2);
-            f = m.gam[j] * e1f / r2;
-          } else {
-            if (!(r2 < rc2)) continue;
-            f = -m.gam[j] * __expf(-r2 * m.s2inv[j]) / r2;
+        if (kLearned) {
+          const int d = pass == 0 ? dec.u[e] : dec.k[e];
+          if (d > 0) {
+            // accepted: the source leaf's multipole at the chosen order (U), or
+            // the correction left out (K)
+            if (pass == 0) {
+              const int p = min(min(class_order(d) + dec.margin, 16), m.P);
+              m2p_order(m, B, A, p, za, pa);
+              if (two) m2p_order(m, B, A, p, zb, pb);
+            }
+            continue;
           }
-          kahan(ax, cax, -f * ry);
-          kahan(ay, cay, f * rx);
         }
-        pairs += (unsigned long long)(j1 - j0);
+        const float ox = m.cxf[B] - m.cxf[A], oy = m.cyf[B] - m.cyf[A];
+        const int j0 = m.begin[A], j1 = m.end[A];
+        float sxa = 0.f, sya = 0.f, sxb = 0.f, syb = 0.f;
+        if (pass == 0)
+          leaf_pairs<false>(m.src4, j0, j1, za.x + ox, za.y + oy, zb.x + ox, zb.y + oy, two, rc2, sxa, sya, sxb, syb);
+        else
+          leaf_pairs<true>(m.src4, j0, j1, za.x + ox, za.y + oy, zb.x + ox, zb.y + oy, two, rc2, sxa, sya, sxb, syb);
+        kahan(axa, cxa, sxa);
+        kahan(aya, cya, sya);
+        kahan(axb, cxb, sxb);
+        kahan(ayb, cyb, syb);
+        pairs += (unsigned long long)(j1 - j0) * (unsigned long long)((va ? 1 : 0) + (vb ? 1 : 0));
       }
     }
-    if (valid) {
-      // FP64 final reduction: u = Im(phi)/2pi + ax/2pi, v = Re(phi)/2pi + ay/2pi
-      const double u = ((double)phi.y + (double)ax - (double)cax) * (double)kInv2Pi;
-      const double v = ((double)phi.x + (double)ay - (double)cay) * (double)kInv2Pi;
-      const int o = perm[t];
-      uv[2 * (size_t)o] = u;
-      uv[2 * (size_t)o + 1] = v;
+    // FP64 final reduction: u = Im(phi)/2pi + ax/2pi, v = Re(phi)/2pi + ay/2pi
+    if (va) {
+      const int o = perm[ta];
+      uv[2 * (size_t)o] = ((double)pa.y + (double)axa - (double)cxa) * inv2pi;
+      uv[2 * (size_t)o + 1] = ((double)pa.x + (double)aya - (double)cya) * inv2pi;
+    }
+    if (vb) {
+      const int o = perm[tb];
+      uv[2 * (size_t)o] = ((double)pb.y + (double)axb - (double)cxb) * inv2pi;
+      uv[2 * (size_t)o + 1] = ((double)pb.x + (double)ayb - (double)cyb) * inv2pi;
     }
   }
   for (int o = 16; o; o >>= 1) pairs += __shfl_xor_sync(0xffffffffu, pairs, o);
@@ -753,7 +841,8 @@ int mixed_downward(MixedView &m, int depth, cudaStream_t s) {
 }
 
 int mixed_evaluate(MixedView &m, double *uv, const int *perm, cudaStream_t s) {
-  k_eval_mixed<<<(int)(((long)m.nleaf * 32 + 127) / 128), 128, 0, s>>>(m, uv, perm);
+  Decisions none{nullptr, nullptr, 0};
+  k_eval_mixed<false><<<(int)(((long)m.nleaf * 32 + 127) / 128), 128, 0, s>>>(m, uv, perm, none);
   g_launches.fetch_add(1, std::memory_order_relaxed);
   T2D_CUDA_TRY(cudaGetLastError());
   return TREE2D_OK;
@@ -799,6 +888,7 @@ int mixed_solve(Workspace &ws, const Tree &t, const MixedParams &mp, double *d_u
   need += Arena::bytes_for(nc, 4) * 5;            // ix iy h inv_h parent
   need += Arena::bytes_for(n, 4) * 4;             // leaf_of gam s2inv + pad
   need += Arena::bytes_for(n, 8);                 // loc
+  need += Arena::bytes_for(n, 16) + Arena::bytes_for(nc, 4) * 2;  // src4, cxf, cyf
   need += Arena::bytes_for((size_t)nc * 9, 4) * 2;
   need += Arena::bytes_for((size_t)nc * 27, 4) + Arena::bytes_for((size_t)nc * 8, 4);
   need += Arena::bytes_for((size_t)nl + 1, 4) * 3;
@@ -834,6 +924,9 @@ int mixed_solve(Workspace &ws, const Tree &t, const MixedParams &mp, double *d_u
   m.loc = ws.mx_arena.take<float2>(n);
   m.gam = ws.mx_arena.take<float>(n);
   m.s2inv = ws.mx_arena.take<float>(n);
+  m.src4 = ws.mx_arena.take<float4>(n);
+  m.cxf = ws.mx_arena.take<float>(nc);
+  m.cyf = ws.mx_arena.take<float>(nc);
   m.coll = ws.mx_arena.take<int>((size_t)nc * 9);
   m.coarse = ws.mx_arena.take<int>((size_t)nc * 9);
   m.vlist = ws.mx_arena.take<int>((size_t)nc * 27);
@@ -881,10 +974,60 @@ int mixed_solve(Workspace &ws, const Tree &t, const MixedParams &mp, double *d_u
   st.m2l_path = tc ? 2 : 1;
   rc = mixed_downward(m, t.depth, s);
   if (rc) return rc;
+  // keep the view for sampling (training data)
+  if (!ws.mxv) ws.mxv = new MixedView();
+  *ws.mxv = m;
+  ws.mx_tot[0] = tot[0];
+  ws.mx_tot[1] = tot[1];
+  ws.mx_tot[2] = tot[2];
+  const bool learned = mp.learned && mp.lp && mp.lp->have_weights;
+  unsigned char *u_dec = nullptr, *k_dec = nullptr;
+  if (learned || mp.learned) {
+    // leaf statistics and u_ref (also used by sampling), then decisions
+    const size_t wim = learn_weight_image_elems();
+    size_t need = Arena::bytes_for(wim, 2) + Arena::bytes_for(208, 4) + Arena::bytes_for((size_t)nc, sizeof(LeafStats)) +
+                  Arena::bytes_for((size_t)tot[0] + 1, 1) + Arena::bytes_for((size_t)tot[2] + 1, 1) + 512;
+    const size_t cap0 = ws.lr_arena.capacity();
+    T2D_CUDA_TRY(ws.lr_arena.reserve(need));
+    if (ws.lr_arena.capacity() != cap0) ws.lr_version = -1;  // reallocated: weights must be uploaded again
+    ws.lr_arena.reset();
+    uint16_t *wimg = ws.lr_arena.take<uint16_t>(wim);
+    float *bias = ws.lr_arena.take<float>(208);
+    LeafStats *stats = ws.lr_arena.take<LeafStats>((size_t)nc);
+    u_dec = ws.lr_arena.take<unsigned char>((size_t)tot[0] + 1);
+    k_dec = ws.lr_arena.take<unsigned char>((size_t)tot[2] + 1);
+    float *uref = ws.lr_arena.take<float>(1);
+    rc = learned_leaf_stats(m, stats, s);
+    if (rc) return rc;
+    rc = learned_uref(m, stats, t.root, uref, s);
+    if (rc) return rc;
+    if (learned) {
+      if (ws.lr_version != mp.lp_version) {
+        std::vector<uint16_t> img;
+        std::vector<float> b;
+        learn_weight_images(mp.lp->theta, img, b);
+        T2D_CUDA_TRY(cudaMemcpy(wimg, img.data(), img.size() * 2, cudaMemcpyHostToDevice));
+        T2D_CUDA_TRY(cudaMemcpy(bias, b.data(), b.size() * 4, cudaMemcpyHostToDevice));
+        ws.lr_version = mp.lp_version;
+      }
+      rc = learned_decide(m, stats, uref, wimg, bias, mp.lp->direct_bias, tot[0], tot[2], u_dec, k_dec, s);
+      if (rc) return rc;
+    }
+  }
   T2D_CUDA_TRY(cudaEventRecord(ws.ev[4], s));
-  rc = mixed_evaluate(m, d_uv, t.perm, s);
+  rc = learned ? learned_evaluate(m, u_dec, k_dec, mp.lp->order_margin, d_uv, t.perm, s)
+               : mixed_evaluate(m, d_uv, t.perm, s);
   if (rc) return rc;
   T2D_CUDA_TRY(cudaEventRecord(ws.ev[5], s));
+  return TREE2D_OK;
+}
+
+int learned_evaluate(MixedView &m, const unsigned char *u_dec, const unsigned char *k_dec, int order_margin,
+                     double *uv, const int *perm, cudaStream_t s) {
+  Decisions d{u_dec, k_dec, order_margin};
+  k_eval_mixed<true><<<(int)(((long)m.nleaf * 32 + 127) / 128), 128, 0, s>>>(m, uv, perm, d);
+  g_launches.fetch_add(1, std::memory_order_relaxed);
+  T2D_CUDA_TRY(cudaGetLastError());
   return TREE2D_OK;
 }
 

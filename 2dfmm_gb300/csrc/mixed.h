@@ -27,6 +27,8 @@ struct MixedView {
   int *leaf_of;          // per position
   float2 *loc;           // per position, offset from its leaf centre
   float *gam, *s2inv;    // per position
+  float4 *src4;          // per position {loc.x, loc.y, G, 1/sigma^2}
+  float *cxf, *cyf;      // per cell, FP32 centre
   int *coll, *coarse;    // 9 per cell
   int *vlist;            // 27 per cell, slot order of the cell's class
   int *xlist;            // 8 per cell

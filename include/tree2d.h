@@ -162,6 +162,39 @@ int tree2d_fp64_probe(int blocks, int iters, void *stream, double *ms);
 /* The same for bits = 64 (DFMA) or 32 (FFMA). */
 int tree2d_pipe_probe(int bits, int blocks, int iters, void *stream, double *ms);
 
+/* ------------------------------------------------------------------ */
+/* Learned order selection (TREE2D_MODE_LEARNED).  A small network
+ * (16 features -> 64 -> 64 -> 64 -> 14 classes, GELU, BF16 weights, FP32
+ * accumulation) decides, for every near-field interaction of the mixed
+ * form, between direct evaluation and the source leaf's multipole at order
+ * p = 4..16.  Without weights the mode falls back to the fixed mixed form.
+ * No counterpart in the reference. */
+
+/* Number of network parameters (flat FP32 vector W1 b1 W2 b2 W3 b3 W4 b4). */
+int tree2d_learn_param_count(void);
+int tree2d_learn_set_weights(const float *theta, int n);
+int tree2d_learn_get_weights(float *theta, int n);
+/* direct_bias: added to the direct-evaluation logit; order_margin: chosen
+ * order raised by this much; budget: label tolerance per interaction in
+ * units of sum|G| / root side.  Defaults 1.0, 1, 2e-8. */
+int tree2d_learn_set_options(float direct_bias, int order_margin, double budget);
+/* Training data from the last tree2d_solve_device in mixed or learned mode:
+ * up to max_samples interactions drawn with `seed`, their features
+ * (features[max][16]) and the cheapest class whose error against the FP64
+ * exact contribution stays within the budget.  Returns the sample count,
+ * or minus a status code. */
+int tree2d_learn_collect(int max_samples, unsigned seed, float *features, int *labels);
+/* `steps` Adam steps on mini-batches of `batch` samples (host arrays),
+ * starting from the loaded weights (or a seeded initialisation). */
+int tree2d_learn_train(int n, const float *X, const int *y, int steps, int batch, float lr, unsigned seed,
+                       float *loss);
+/* Checking hooks: one forward + backward (mean cross-entropy) on n samples
+ * with parameters theta, and the logits of n feature vectors by the
+ * training path (CUDA cores, tensor_cores = 0) or the inference path
+ * (tensor cores, 1).  Host arrays. */
+int tree2d_mlp_grad(int n, const float *X, const int *y, const float *theta, float *grad, float *loss);
+int tree2d_mlp_forward(int n, const float *X, const float *theta, float *logits, int tensor_cores);
+
 /* Library version string. */
 const char *tree2d_version(void);
 

@@ -1,0 +1,90 @@
+"""Learned order selection: the network's training and inference kernels
+against the CPU oracle (oracle/mlp_oracle.py), and the learned mode on a
+small advected Lamb-Oseen run: it must keep relL2 <= 1e-6 against the FP64
+direct sum and do less direct work than the fixed mixed form."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from conftest import workloads
+import mlp_oracle as M  # noqa: E402
+
+
+def random_batch(n, seed):
+    rng = np.random.default_rng(seed)
+    X = rng.standard_normal((n, 16)).astype(np.float32)
+    X[:, 12:] = 0
+    y = rng.integers(0, M.N_CLASSES, n).astype(np.int32)
+    theta = (M.init(seed) + 0.05 * rng.standard_normal(M.N_PARAMS)).astype(np.float32)
+    return X, y, theta
+
+
+@pytest.mark.gpu
+def test_training_gradient_matches_oracle(gpu_lib):
+    P = gpu_lib
+    X, y, theta = random_batch(512, 3)
+    loss, g = P.mlp_grad(X, y, theta)
+    lref, gref = M.loss_and_grad(theta.astype(np.float64), X.astype(np.float64), y)
+    assert abs(loss - lref) <= 1e-3 * abs(lref)
+    assert np.linalg.norm(g - gref) <= 1e-2 * np.linalg.norm(gref)
+
+
+@pytest.mark.gpu
+def test_tensor_core_inference_matches_training_forward(gpu_lib):
+    P = gpu_lib
+    X, _, theta = random_batch(1000, 4)
+    cc = P.mlp_forward(X, theta, tensor_cores=False)
+    tc = P.mlp_forward(X, theta, tensor_cores=True)
+    ref, _ = M.forward(theta.astype(np.float64), X.astype(np.float64))
+    scale = np.abs(ref[:, :14]).max()
+    assert np.abs(cc[:, :14] - ref[:, :14]).max() <= 2e-2 * scale
+    assert np.abs(tc[:, :14] - ref[:, :14]).max() <= 5e-2 * scale
+    agree = (tc[:, :14].argmax(1) == ref[:, :14].argmax(1)).mean()
+    assert agree >= 0.95, agree
+
+
+def _solve(P, torch, b, mode):
+    dev = torch.device("cuda:0")
+    P.set_params(b.nterms, b.num_p, b.theta)
+    P.set_mode(mode)
+    P.set_mixed_params(16, 3.0, True)
+    xy = torch.from_numpy(b.xy).to(dev)
+    cir = torch.from_numpy(b.cir).to(dev)
+    cor = torch.from_numpy(b.cor).to(dev)
+    uv = torch.empty_like(xy)
+    P.solve_device(xy.data_ptr(), cir.data_ptr(), cor.data_ptr(), uv.data_ptr(), b.n)
+    torch.cuda.synchronize()
+    return uv, xy, cir, cor, P.stats()
+
+
+@pytest.mark.gpu
+def test_learned_mode_keeps_accuracy_and_saves_direct_work(gpu_lib):
+    torch = pytest.importorskip("torch")
+    P = gpu_lib
+    W = workloads()
+    b = W.lamb_oseen(131_072, seed=21)
+    # training data from the fixed mixed form
+    Xs, ys = [], []
+    for step in range(3):
+        _, _, _, _, _ = _solve(P, torch, b, P.MODE_MIXED)
+        X, y = P.learn_collect(20_000, seed=step)
+        Xs.append(X)
+        ys.append(y)
+        b.xy = b.xy + 1e-3 * np.random.default_rng(step).standard_normal(b.xy.shape) * 1e-3
+    X = np.concatenate(Xs)
+    y = np.concatenate(ys)
+    assert (y > 0).mean() > 0.05  # some interactions can be approximated
+    P.learn_train(X, y, steps=400, batch=2048, lr=2e-3, seed=1)
+    uv_m, xy, cir, cor, st_m = _solve(P, torch, b, P.MODE_MIXED)
+    uv_l, _, _, _, st_l = _solve(P, torch, b, P.MODE_LEARNED)
+    idx = torch.from_numpy(W.sample_targets(b.n, 1024, seed=3)).to(xy.device)
+    txy = xy[idx].contiguous()
+    ref = torch.empty_like(txy)
+    P.direct_device(txy.data_ptr(), len(idx), xy.data_ptr(), cir.data_ptr(), cor.data_ptr(), b.n, ref.data_ptr())
+    torch.cuda.synchronize()
+    rel_l = float(torch.linalg.norm(uv_l[idx] - ref) / torch.linalg.norm(ref))
+    rel_m = float(torch.linalg.norm(uv_m[idx] - ref) / torch.linalg.norm(ref))
+    P.set_mode(P.MODE_PLAIN)
+    assert rel_l <= 1e-6, (rel_l, rel_m)
+    assert st_l["n_pairs"] < st_m["n_pairs"], (st_l["n_pairs"], st_m["n_pairs"])

@@ -80,3 +80,32 @@ def test_two_patch_sheet_4m_properties_and_accuracy(gpu_lib):
     # carry the regularisation (1 - exp(-r^2/sigma^2) ~ 0.9), so the treecode
     # itself sits near relL2 ~ 5e-4 here.  This bounds that, not parity.
     assert relL2 < 2e-3, relL2
+
+
+@pytest.mark.gpu
+def test_deep_cluster_uses_full_key_depth(gpu_lib):
+    """A cluster 1e-6 wide needs leaves below level 20: the build must fall
+    back from its short keys to the full 32 levels and still give a valid
+    tree and the treecode's accuracy against the FP64 direct sum."""
+    torch = pytest.importorskip("torch")
+    P = gpu_lib
+    rng = np.random.default_rng(17)
+    xy = np.concatenate([rng.random((2000, 2)), 0.3 + 1e-6 * rng.standard_normal((1000, 2))])
+    cir = rng.standard_normal(3000) / 3000
+    cor = np.full(3000, 1e-7)
+    P.set_params(11, 33, 0.5)
+    P.set_mode(P.MODE_PLAIN)
+    P.make_tree(xy, cir, cor)
+    st = P.stats()
+    assert st["depth"] > 20
+    d = P.export_tree(3000, 11)
+    check_tree_invariants(d, 3000, 33)
+    uv = P.biot_tree_batch(xy)
+    dev = torch.device("cuda:0")
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)  # noqa: E731
+    out = torch.empty((3000, 2), dtype=torch.float64, device=dev)
+    txy, cc, rr = t(xy), t(cir), t(cor)
+    P.direct_device(txy.data_ptr(), 3000, txy.data_ptr(), cc.data_ptr(), rr.data_ptr(), 3000, out.data_ptr())
+    torch.cuda.synchronize()
+    ref = out.cpu().numpy()
+    assert np.linalg.norm(uv - ref) / np.linalg.norm(ref) < 1e-5
