@@ -34,6 +34,7 @@ EXPORTS = [
     "tree2d_solve_device", "tree2d_solve_device_static", "tree2d_get_stats", "tree2d_export_tree", "tree2d_direct_device", "tree2d_fp64_probe", "tree2d_pipe_probe", "tree2d_version",
     "tree2d_learn_param_count", "tree2d_learn_set_weights", "tree2d_learn_get_weights", "tree2d_learn_set_options",
     "tree2d_learn_collect", "tree2d_learn_train", "tree2d_mlp_grad", "tree2d_mlp_forward",
+    "tree2d_set_mirror", "tree2d_advect_device",
 ]
 
 
@@ -122,6 +123,11 @@ def load(path: str | None = None):
                                      ctypes.c_uint, fp]
     L.tree2d_mlp_grad.argtypes = [ctypes.c_int, fp, _ip, fp, fp, fp]
     L.tree2d_mlp_forward.argtypes = [ctypes.c_int, fp, fp, fp, ctypes.c_int]
+    L.tree2d_set_mirror.argtypes = [ctypes.c_int, ctypes.c_double]
+    L.tree2d_set_mirror.restype = ctypes.c_int
+    L.tree2d_advect_device.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_double,
+                                       ctypes.c_void_p]
+    L.tree2d_advect_device.restype = ctypes.c_int
     for f in ("tree2d_learn_set_weights", "tree2d_learn_get_weights", "tree2d_learn_set_options",
               "tree2d_learn_collect", "tree2d_learn_train", "tree2d_mlp_grad", "tree2d_mlp_forward"):
         getattr(L, f).restype = ctypes.c_int
@@ -266,6 +272,16 @@ def fp32_peak_tflops(blocks: int = 152 * 8, iters: int = 200000, stream: int = 0
     return blocks * 256.0 * iters * 16.0 / (ms.value * 1e-3) / 1e12
 
 
+def set_mirror(enable: bool, d_mirror: float = 0.0):
+    """Mirror wall at y = d_mirror (images as point vortices of opposite sign)."""
+    _check(load().tree2d_set_mirror(int(enable), d_mirror), "set_mirror")
+
+
+def advect_device(d_xy: int, d_uv: int, n: int, dt: float, stream: int = 0):
+    """Forward Euler on device arrays: xy += dt * uv."""
+    _check(load().tree2d_advect_device(n, d_xy, d_uv, dt, stream or None), "advect_device")
+
+
 # ---------------------------------------------------------------- learned form
 
 def _fp(a):
@@ -287,7 +303,7 @@ def learn_get_weights():
     return th
 
 
-def learn_set_options(direct_bias: float = 1.0, order_margin: int = 1, budget: float = 2e-8):
+def learn_set_options(direct_bias: float = 1.0, order_margin: int = 1, budget: float = 3e-7):
     _check(load().tree2d_learn_set_options(direct_bias, order_margin, budget), "learn_set_options")
 
 

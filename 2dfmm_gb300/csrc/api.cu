@@ -75,6 +75,7 @@ namespace {
 struct Solver {
   Workspace ws;
   Tree tree;
+  Arena mirror;   // blobs + images when a mirror wall is set
   bool plain_coef = false;  // FP64 coefficients present (plain upward ran)
   Arena io;       // device copies of host inputs and outputs
   Arena targets;  // evaluation-order targets
@@ -89,6 +90,8 @@ struct Lib {
   MixedParams mixed;
   LearnedParams *lp = new LearnedParams();
   long lp_version = 0;
+  bool mirror_on = false;
+  double mirror_d = 0.0;
   std::atomic<int> last_error{0};
   cudaStream_t stream = nullptr;
   bool stream_ready = false;
@@ -171,10 +174,32 @@ float elapsed(cudaEvent_t a, cudaEvent_t b) {
   return ms;
 }
 
+int solve_body(Lib &L, Solver &S, int n, const double *d_xy, const double *d_cir, const double *d_cor,
+               double *d_uv, cudaStream_t s, tree2d_stats_t &st);
+
 // Whole pipeline over n device-resident blobs; uv (interleaved, original
-// order) on the device.
+// order) on the device.  With a mirror wall the images are appended as
+// blobs n..2n-1 and only the first n velocities are returned.
 int solve(Lib &L, Solver &S, int n, const double *d_xy, const double *d_cir, const double *d_cor, double *d_uv,
           cudaStream_t s, tree2d_stats_t &st) {
+  if (!L.mirror_on || n == 0) return solve_body(L, S, n, d_xy, d_cir, d_cor, d_uv, s, st);
+  const size_t n2 = 2 * (size_t)n;
+  T2D_CUDA_TRY(S.mirror.reserve(Arena::bytes_for(2 * n2, 8) * 2 + Arena::bytes_for(n2, 8) * 2));
+  S.mirror.reset();
+  double *mxy = S.mirror.take<double>(2 * n2);
+  double *muv = S.mirror.take<double>(2 * n2);
+  double *mcir = S.mirror.take<double>(n2);
+  double *mcor = S.mirror.take<double>(n2);
+  T2D_CUDA_TRY(mirror_images(n, d_xy, d_cir, d_cor, L.mirror_d, mxy, mcir, mcor, s));
+  int rc = solve_body(L, S, (int)n2, mxy, mcir, mcor, muv, s, st);
+  if (rc) return rc;
+  T2D_CUDA_TRY(cudaMemcpyAsync(d_uv, muv, sizeof(double) * 2 * (size_t)n, cudaMemcpyDeviceToDevice, s));
+  T2D_CUDA_TRY(cudaStreamSynchronize(s));
+  return TREE2D_OK;
+}
+
+int solve_body(Lib &L, Solver &S, int n, const double *d_xy, const double *d_cir, const double *d_cor,
+               double *d_uv, cudaStream_t s, tree2d_stats_t &st) {
   T2D_CUDA_TRY(workspace_init(S.ws));
   std::memset(&st, 0, sizeof(st));
   st.n_blobs = n;
@@ -698,6 +723,27 @@ int tree2d_learn_set_options(float direct_bias, int order_margin, double budget)
 }
 
 int tree2d_learn_param_count(void) { return kMlpParams; }
+
+// ---------------------------------------------------------------- extensions
+
+int tree2d_set_mirror(int enable, double d_mirror) {
+  Lib &L = lib();
+  std::lock_guard<std::mutex> lk(L.mu);
+  if (enable && !std::isfinite(d_mirror)) return fail(TREE2D_ERR_BAD_PARAMS);
+  L.mirror_on = enable != 0;
+  L.mirror_d = d_mirror;
+  return TREE2D_OK;
+}
+
+int tree2d_advect_device(int n, double *d_xy, const double *d_uv, double dt, void *stream) {
+  if (n < 0 || !std::isfinite(dt)) return fail(TREE2D_ERR_BAD_INPUT);
+  cudaError_t e = advect(n, d_xy, d_uv, dt, static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) {
+    note_cuda_error(e, "advect");
+    return fail(TREE2D_ERR_CUDA);
+  }
+  return TREE2D_OK;
+}
 
 int tree2d_learn_collect(int max_samples, unsigned seed, float *features, int *labels) {
   Lib &L = lib();

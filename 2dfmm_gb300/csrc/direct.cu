@@ -99,6 +99,44 @@ cudaError_t dfma_probe(double *out, int blocks, int iters, cudaStream_t s) {
   return cudaGetLastError();
 }
 
+// Forward Euler step of the blob positions, x += dt * u (the solver's drift,
+// e_drift.f90:17-59), on the device: xy and uv interleaved.
+__global__ void k_advect(long n, double *xy, const double *uv, double dt) {
+  long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (i < 2 * n) xy[i] += dt * uv[i];
+}
+
+// Image blobs for a mirror wall at y = d: (x, 2d - y), circulation -G, core
+// radius 0 (a point vortex, as the solver's image term d_biot.f90:39-53).
+__global__ void k_mirror(long n, const double *xy, const double *cir, const double *cor, double d, double *oxy,
+                         double *ocir, double *ocor) {
+  long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  oxy[2 * i] = xy[2 * i];
+  oxy[2 * i + 1] = xy[2 * i + 1];
+  ocir[i] = cir[i];
+  ocor[i] = cor[i];
+  oxy[2 * (n + i)] = xy[2 * i];
+  oxy[2 * (n + i) + 1] = 2.0 * d - xy[2 * i + 1];
+  ocir[n + i] = -cir[i];
+  ocor[n + i] = 0.0;
+}
+
+cudaError_t advect(long n, double *xy, const double *uv, double dt, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  k_advect<<<(int)((2 * n + 255) / 256), 256, 0, s>>>(n, xy, uv, dt);
+  ::t2d::g_launches.fetch_add(1, std::memory_order_relaxed);
+  return cudaGetLastError();
+}
+
+cudaError_t mirror_images(long n, const double *xy, const double *cir, const double *cor, double d, double *oxy,
+                          double *ocir, double *ocor, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  k_mirror<<<(int)((n + 255) / 256), 256, 0, s>>>(n, xy, cir, cor, d, oxy, ocir, ocor);
+  ::t2d::g_launches.fetch_add(1, std::memory_order_relaxed);
+  return cudaGetLastError();
+}
+
 cudaError_t ffma_probe(float *out, int blocks, int iters, cudaStream_t s) {
   k_ffma_probe<<<blocks, 256, 0, s>>>(out, iters, 0.999999f, 1e-7f);
   ::t2d::g_launches.fetch_add(1, std::memory_order_relaxed);

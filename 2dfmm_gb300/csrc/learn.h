@@ -24,7 +24,7 @@ struct LearnedParams {
   float theta[kMlpParams];   // FP32 master copy (the network uses it rounded to BF16)
   float direct_bias = 1.0f;  // added to the direct logit: leans towards exact evaluation
   int order_margin = 1;      // chosen order raised by this much (capped at 16)
-  double budget = 2e-8;      // label budget: per-interaction error / (sum|G| / R0)
+  double budget = 3e-7;      // label budget: per-interaction error / (sum|G| / R0)
 };
 
 // Per-leaf source statistics for the features.

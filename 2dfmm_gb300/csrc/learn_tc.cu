@@ -69,19 +69,6 @@ __device__ __forceinline__ void store_row(unsigned char *tile, int r, const floa
   }
 }
 
-__device__ __forceinline__ int upper_index(const int *off, int n, int e) {
-  // largest l in [0, n) with off[l] <= e
-  int lo = 0, hi = n;
-  while (hi - lo > 1) {
-    const int mid = (lo + hi) >> 1;
-    if (off[mid] <= e)
-      lo = mid;
-    else
-      hi = mid;
-  }
-  return lo;
-}
-
 __global__ void __launch_bounds__(kTile) k_mlp_infer(InferArgs a) {
   extern __shared__ __align__(1024) unsigned char smem[];
   __shared__ uint64_t bar_w, bar_mma;
@@ -144,7 +131,7 @@ __global__ void __launch_bounds__(kTile) k_mlp_infer(InferArgs a) {
     } else {
       kind = gi < a.n_u ? 0 : 1;
       e = kind == 0 ? gi : gi - a.n_u;
-      const int l = upper_index(kind == 0 ? m.u_off : m.k_off, m.nleaf, (int)e);
+      const int l = (kind == 0 ? m.u_leaf : m.k_leaf)[e];
       const int B = m.leaf_cell[l];
       const int A = kind == 0 ? m.u_idx[e] : m.k_idx[e];
       interaction_features(m, a.st, B, A, kind, u_ref, v);

@@ -346,7 +346,11 @@ __global__ void k_list_fill(MixedView m) {
   const int b = m.leaf_cell[l];
   int pos[3] = {m.u_off[l], m.w_off[l], m.k_off[l]};
   int *dst[3] = {m.u_idx, m.w_idx, m.k_idx};
-  auto emit = [&](int kind, int id) { dst[kind][pos[kind]++] = id; };
+  int *own[3] = {m.u_leaf, nullptr, m.k_leaf};
+  auto emit = [&](int kind, int id) {
+    if (own[kind]) own[kind][pos[kind]] = l;
+    dst[kind][pos[kind]++] = id;
+  };
   uw_walk(m, b, emit);
   corr_walk(m, b, emit);
 }
@@ -958,12 +962,15 @@ int mixed_solve(Workspace &ws, const Tree &t, const MixedParams &mp, double *d_u
   T2D_CUDA_TRY(cudaMemcpyAsync(&tot[1], m.w_off + nl, 4, cudaMemcpyDeviceToHost, s));
   T2D_CUDA_TRY(cudaMemcpyAsync(&tot[2], m.k_off + nl, 4, cudaMemcpyDeviceToHost, s));
   T2D_CUDA_TRY(cudaStreamSynchronize(s));
-  size_t lneed = Arena::bytes_for(tot[0] + 1, 4) + Arena::bytes_for(tot[1] + 1, 4) + Arena::bytes_for(tot[2] + 1, 4);
+  size_t lneed = 2 * Arena::bytes_for(tot[0] + 1, 4) + Arena::bytes_for(tot[1] + 1, 4) +
+                 2 * Arena::bytes_for(tot[2] + 1, 4);
   T2D_CUDA_TRY(ws.mx_lists.reserve(lneed));
   ws.mx_lists.reset();
   m.u_idx = ws.mx_lists.take<int>(tot[0] + 1);
   m.w_idx = ws.mx_lists.take<int>(tot[1] + 1);
   m.k_idx = ws.mx_lists.take<int>(tot[2] + 1);
+  m.u_leaf = ws.mx_lists.take<int>(tot[0] + 1);
+  m.k_leaf = ws.mx_lists.take<int>(tot[2] + 1);
   rc = mixed_fill_lists(m, s);
   if (rc) return rc;
   rc = mixed_upward(m, t.depth, s);

@@ -34,6 +34,7 @@ struct MixedView {
   int *xlist;            // 8 per cell
   int *u_off, *w_off, *k_off;  // per leaf (+1)
   int *u_idx, *w_idx, *k_idx;
+  int *u_leaf, *k_leaf;  // leaf ordinal of each U / K entry
   float *M, *L;          // per cell, 2P floats (re[P], im[P])
   const float2 *m2m, *l2l;  // [4][kMaxP][kMaxP] translation operators
   DevStatus *st;

@@ -1,0 +1,171 @@
+"""Training and scoring of the learned order selector (configuration 5).
+
+The configuration-2 blob set (1,048,576 blobs, Lamb-Oseen-like) is advected
+by its own velocity with forward Euler (dt = 1e-3), the tree rebuilt every
+step.  Interaction samples (features + the cheapest acceptable class,
+labelled by the FMM against the FP64 exact contribution) are collected on
+steps 0-20, the network is trained on them on the GPU, and steps 21-100 are
+solved with the fixed mixed form and with the learned form on the same
+positions; every `score_every`-th step both are judged against the FP64
+direct sum on sampled targets, and the plain FP64 treecode (the reference's
+method, p = 12, theta 0.5) is timed and judged beside them.
+
+    python -m 2dfmm_gb300.learn --out learned_weights.npz
+
+writes the weights (with a versioned header) and prints a JSON summary.
+"""
+from __future__ import annotations
+
+import argparse
+import importlib
+import json
+import os
+import time
+
+import numpy as np
+
+WEIGHTS_VERSION = 1
+HERE = os.path.dirname(os.path.abspath(__file__))
+DEFAULT_WEIGHTS = os.path.join(HERE, "data", "learned_weights.npz")
+
+
+def save_weights(path, theta, meta):
+    os.makedirs(os.path.dirname(os.path.abspath(path)), exist_ok=True)
+    np.savez(path, version=WEIGHTS_VERSION, theta=np.asarray(theta, np.float32),
+             meta=json.dumps(meta))
+
+
+def load_weights(path=DEFAULT_WEIGHTS):
+    """Returns the weight vector, or None if absent or of another version."""
+    if not os.path.exists(path):
+        return None
+    d = np.load(path)
+    if int(d["version"]) != WEIGHTS_VERSION:
+        return None
+    return d["theta"].astype(np.float32)
+
+
+def _dev_arrays(torch, b):
+    dev = torch.device("cuda:0")
+    xy = torch.from_numpy(np.ascontiguousarray(b.xy)).to(dev)
+    cir = torch.from_numpy(b.cir).to(dev)
+    cor = torch.from_numpy(b.cor).to(dev)
+    return xy, cir, cor, torch.empty_like(xy)
+
+
+def _timed_solve(P, torch, arrays, n, mode):
+    xy, cir, cor, uv = arrays
+    P.set_mode(mode)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    P.solve_device(xy.data_ptr(), cir.data_ptr(), cor.data_ptr(), uv.data_ptr(), n)
+    e1.record()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1), P.stats()
+
+
+def _rel_l2(P, torch, arrays, n, idx, uv_list):
+    xy, cir, cor, _ = arrays
+    t = torch.from_numpy(idx).to(xy.device)
+    txy = xy[t].contiguous()
+    ref = torch.empty_like(txy)
+    P.direct_device(txy.data_ptr(), len(idx), xy.data_ptr(), cir.data_ptr(), cor.data_ptr(), n, ref.data_ptr())
+    torch.cuda.synchronize()
+    return [float(torch.linalg.norm(u[t] - ref) / torch.linalg.norm(ref)) for u in uv_list]
+
+
+def run(n=1_048_576, steps=100, dt=1e-3, train_until=20, samples=200_000, train_steps=2000, batch=4096,
+        lr=2e-3, score_every=10, score_targets=2048, pterms=16, cutoff=3.0, seed=0, out=None, quiet=False):
+    import torch
+    P = importlib.import_module("2dfmm_gb300")
+    W = importlib.import_module("2dfmm_gb300.workloads")
+    P.load()
+    b = W.lamb_oseen(n, seed=2)
+    P.set_params(b.nterms, b.num_p, b.theta)
+    P.set_mixed_params(pterms, cutoff, True)
+    per_step = int(np.ceil(samples / (train_until + 1)))
+    Xs, ys = [], []
+    log = {"collect": [], "score": []}
+    t0 = time.time()
+    for step in range(train_until + 1):
+        arrays = _dev_arrays(torch, b)
+        ms, st = _timed_solve(P, torch, arrays, n, P.MODE_MIXED)
+        X, y = P.learn_collect(per_step, seed=seed * 1000 + step)
+        Xs.append(X)
+        ys.append(y)
+        log["collect"].append({"step": step, "ms": ms, "samples": len(y), "approx_frac": float((y > 0).mean())})
+        b.xy = b.xy + dt * arrays[3].cpu().numpy()  # forward Euler on the mixed velocities
+    X = np.concatenate(Xs)[:samples]
+    y = np.concatenate(ys)[:samples]
+    t_collect = time.time() - t0
+    t1 = time.time()
+    loss = P.learn_train(X, y, steps=train_steps, batch=batch, lr=lr, seed=seed + 1)
+    t_train = time.time() - t1
+    theta = P.learn_get_weights()
+    hist = np.bincount(y, minlength=14).tolist()
+    summary = {"samples": int(len(y)), "label_histogram": hist, "final_loss": loss, "collect_s": t_collect,
+               "train_s": t_train}
+    if out:
+        save_weights(out, theta, summary)
+    # score steps 21..steps
+    tm, tl, tp = [], [], []
+    for step in range(train_until + 1, steps + 1):
+        arrays = _dev_arrays(torch, b)
+        ms_l, st_l = _timed_solve(P, torch, arrays, n, P.MODE_LEARNED)
+        uv_l = arrays[3].clone()
+        ms_m, st_m = _timed_solve(P, torch, arrays, n, P.MODE_MIXED)
+        uv_m = arrays[3].clone()
+        tm.append(ms_m)
+        tl.append(ms_l)
+        rec = {"step": step, "ms_mixed": ms_m, "ms_learned": ms_l, "pairs_mixed": st_m["n_pairs"],
+               "pairs_learned": st_l["n_pairs"]}
+        if (step - train_until - 1) % score_every == 0 or step == steps:
+            ms_p, _ = _timed_solve(P, torch, arrays, n, P.MODE_PLAIN)
+            uv_p = arrays[3].clone()
+            tp.append(ms_p)
+            idx = W.sample_targets(n, score_targets, seed=step)
+            r_m, r_l, r_p = _rel_l2(P, torch, arrays, n, idx, [uv_m, uv_l, uv_p])
+            rec.update({"ms_plain": ms_p, "relL2_mixed": r_m, "relL2_learned": r_l, "relL2_plain": r_p})
+        log["score"].append(rec)
+        if not quiet and "relL2_learned" in rec:
+            print(json.dumps(rec), flush=True)
+        b.xy = b.xy + dt * uv_m.cpu().numpy()
+    scored = [r for r in log["score"] if "relL2_learned" in r]
+    summary.update({
+        "steps_scored": len(log["score"]),
+        "mean_ms_mixed": float(np.mean(tm)), "mean_ms_learned": float(np.mean(tl)),
+        "mean_ms_plain": float(np.mean(tp)) if tp else None,
+        "speedup_learned_vs_mixed": float(np.mean(tm) / np.mean(tl)),
+        "speedup_learned_vs_plain": float(np.mean(tp) / np.mean(tl)) if tp else None,
+        "max_relL2_learned": max(r["relL2_learned"] for r in scored),
+        "max_relL2_mixed": max(r["relL2_mixed"] for r in scored),
+        "max_relL2_plain": max(r["relL2_plain"] for r in scored),
+        "pairs_ratio_learned_vs_mixed": float(np.mean([r["pairs_learned"] / r["pairs_mixed"] for r in log["score"]])),
+    })
+    P.set_mode(P.MODE_PLAIN)
+    return summary, log
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--n", type=int, default=1_048_576)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--train-until", type=int, default=20)
+    ap.add_argument("--samples", type=int, default=200_000)
+    ap.add_argument("--train-steps", type=int, default=2000)
+    ap.add_argument("--score-every", type=int, default=10)
+    ap.add_argument("--out", default=DEFAULT_WEIGHTS)
+    ap.add_argument("--log", default=None)
+    a = ap.parse_args()
+    summary, log = run(n=a.n, steps=a.steps, train_until=a.train_until, samples=a.samples,
+                       train_steps=a.train_steps, score_every=a.score_every, out=a.out)
+    print(json.dumps(summary), flush=True)
+    if a.log:
+        with open(a.log, "w") as f:
+            json.dump({"summary": summary, "log": log}, f)
+
+
+if __name__ == "__main__":
+    main()

@@ -104,6 +104,35 @@ def sample_targets(n, k, seed=7):
     return np.sort(rng.choice(n, size=k, replace=False))
 
 
+def write_snapshot(path, xy, cir, cor, header_records=4):
+    """Writes blobs in the snapshot's blob-block layout (Fortran unformatted
+    sequential records: nvor_b, then per blob x,y | three velocity pairs |
+    cir | cor | id), after `header_records` placeholder records standing for
+    the solver's header (read_snapshot skips them by pattern)."""
+    xy = np.asarray(xy, np.float64).reshape(-1, 2)
+    cir = np.asarray(cir, np.float64)
+    cor = np.asarray(cor, np.float64)
+
+    def rec(f, payload):
+        f.write(struct.pack("<i", len(payload)))
+        f.write(payload)
+        f.write(struct.pack("<i", len(payload)))
+
+    with open(path, "wb") as f:
+        for k in range(header_records):
+            rec(f, struct.pack("<2d", float(k), 0.0))
+        rec(f, struct.pack("<i", len(cir)))
+        zero = struct.pack("<2d", 0.0, 0.0)
+        for j in range(len(cir)):
+            rec(f, struct.pack("<2d", xy[j, 0], xy[j, 1]))
+            rec(f, zero)
+            rec(f, zero)
+            rec(f, zero)
+            rec(f, struct.pack("<d", cir[j]))
+            rec(f, struct.pack("<d", cor[j]))
+            rec(f, struct.pack("<i", j + 1))
+
+
 def read_snapshot(path):
     """Reads the blob block of a vortex-solver snapshot (``s_*****_step.dat``,
     Fortran unformatted sequential records, written by the solver's

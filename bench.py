@@ -35,7 +35,7 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-METRIC = "target evals/s at 4M blobs (two patches + sheet), all blobs as targets"
+METRIC = "target evals/s at 4M blobs (two patches + sheet), all blobs as targets, relL2 <= 1e-6 vs FP64 direct"
 UNIT = "targets/s"
 MODES = {"plain": 0, "mixed": 1, "learned": 2}
 
@@ -46,7 +46,8 @@ def parse():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--mode", default="mixed", choices=list(MODES))
+    ap.add_argument("--mode", default="learned", choices=list(MODES))
+    ap.add_argument("--weights", default=None, help="learned form: weights file (default: the packaged ones)")
     ap.add_argument("--pterms", type=int, default=16, help="mixed form: expansion length")
     ap.add_argument("--cutoff", type=float, default=3.0, help="mixed form: correction radius / max sigma")
     ap.add_argument("--cuda-core-m2l", action="store_true", help="mixed form: M2L on CUDA cores")
@@ -282,7 +283,8 @@ def _roofline(P, args, mode, b, wname, sts, sp):
                 "kernel": "k_eval (traversal + M2S + P2P, FP64)",
                 "peak_source": "measured: the library's DFMA probe (8 independent chains per thread)",
                 "algorithmic_flops_per_launch": flops, "ms_per_launch": ms}
-    # mixed: the evaluation kernel (direct pairs, correction pairs, L2P, M2P)
+    # mixed and learned: the evaluation kernel (direct pairs, correction
+    # pairs, L2P, M2P)
     flops = st["n_pairs"] * 20 + b.n * 8 * args.pterms
     peak = P.fp32_peak_tflops(stream=sp)
     return {"bound": "fp32", "achieved": flops / (ms * 1e-3) / 1e12, "peak": peak, "unit": "TFLOP/s",
@@ -305,6 +307,17 @@ def run_ours(args):
     b, wname = workload(args, rank)
     P.set_params(b.nterms, b.num_p, b.theta)
     P.set_mixed_params(args.pterms, args.cutoff, not args.cuda_core_m2l)
+    learned_note = None
+    if args.mode == "learned":
+        L = importlib.import_module("2dfmm_gb300.learn")
+        path = args.weights or L.DEFAULT_WEIGHTS
+        theta = L.load_weights(path)
+        if theta is None:
+            learned_note = f"none found at {os.path.relpath(path, ROOT)}: fixed mixed form (the fallback)"
+        else:
+            P.learn_set_weights(theta)
+            learned_note = (f"{os.path.relpath(path, ROOT)} (trained on configuration-5 steps 0-20 by "
+                            "2dfmm_gb300/learn.py)")
     n = b.n
     xy = torch.from_numpy(b.xy).to(dev).contiguous()
     cir = torch.from_numpy(b.cir).to(dev)
@@ -329,15 +342,19 @@ def run_ours(args):
     accuracy = _judge(P, torch, arrays, n, args.err_targets, sp)
     roofline = _roofline(P, args, args.mode, b, wname, sts, sp)
 
-    # the plain FP64 path on the same set, for the mixed/plain ratio
-    plain = None
-    if args.mode != "plain" and not args.no_plain:
-        ptimes, psts = _time_mode(P, torch, args, "plain", arrays, stream, flush)
-        plain = {"value": n / (statistics.mean(ptimes) * 1e-3), "unit": UNIT,
-                 "ms_per_step": statistics.mean(ptimes),
-                 "accuracy": _judge(P, torch, arrays, n, args.err_targets, sp)}
-        plain["speedup_of_headline"] = value / world / plain["value"]
-        P.set_mode(MODES[args.mode])
+    # the fixed mixed form and the plain FP64 path on the same set, timed the
+    # same way, for the ratios
+    beside = {}
+    others = [] if args.no_plain else ["plain"]
+    if args.mode == "learned":
+        others.insert(0, "mixed")
+    for other in others:
+        otimes, _ = _time_mode(P, torch, args, other, arrays, stream, flush)
+        o = {"value": n / (statistics.mean(otimes) * 1e-3), "unit": UNIT, "ms_per_step": statistics.mean(otimes),
+             "accuracy": _judge(P, torch, arrays, n, args.err_targets, sp)}
+        o["speedup_of_headline"] = value / world / o["value"]
+        beside["plain_fp64" if other == "plain" else "mixed_fixed"] = o
+    P.set_mode(MODES[args.mode])
 
     # end to end through the reference-facing calls, host buffers
     P.set_mode(MODES[args.mode])
@@ -381,7 +398,7 @@ def run_ours(args):
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None,
-            "dtype": "f64" if args.mode == "plain" else "f32 (tf32x3 tensor M2L, f64 final sum)",
+            "dtype": "f64" if args.mode == "plain" else "f32 (tf32x3 tensor M2L, bf16 MLP, f64 final sum)",
             "data": "synthetic (seeded numpy PCG64), shapes and distributions of the configuration",
             "config": {"workload": wname, "n_blobs": n, "targets": "all blobs", "nterms": b.nterms,
                        "p": b.nterms - 1, "num_p": b.num_p, "theta": b.theta, "mode": args.mode,
@@ -402,8 +419,9 @@ def run_ours(args):
                      "m2l_pairs": st["n_m2l"]},
             "clocks": clocks,
         }
-        if plain is not None:
-            line["plain_fp64"] = plain
+        line.update(beside)
+        if learned_note:
+            line["config"]["learned_weights"] = learned_note
         if cpu is not None:
             line["cpu_baseline"] = cpu
         print(json.dumps(line), flush=True)

@@ -176,7 +176,7 @@ int tree2d_learn_set_weights(const float *theta, int n);
 int tree2d_learn_get_weights(float *theta, int n);
 /* direct_bias: added to the direct-evaluation logit; order_margin: chosen
  * order raised by this much; budget: label tolerance per interaction in
- * units of sum|G| / root side.  Defaults 1.0, 1, 2e-8. */
+ * units of sum|G| / root side.  Defaults 1.0, 1, 3e-7. */
 int tree2d_learn_set_options(float direct_bias, int order_margin, double budget);
 /* Training data from the last tree2d_solve_device in mixed or learned mode:
  * up to max_samples interactions drawn with `seed`, their features
@@ -194,6 +194,17 @@ int tree2d_learn_train(int n, const float *X, const int *y, int steps, int batch
  * (tensor cores, 1).  Host arrays. */
 int tree2d_mlp_grad(int n, const float *X, const int *y, const float *theta, float *grad, float *loss);
 int tree2d_mlp_forward(int n, const float *X, const float *theta, float *logits, int tensor_cores);
+
+/* Mirror wall at y = d_mirror (enable = 1): every solve adds the image of
+ * each blob, (x, 2 d - y) with circulation -G as a point vortex (the
+ * solver's image term, ver-c/src/includes/d_biot.f90:39-53), and returns the
+ * velocities at the real blobs only.  The reference's tree path has no
+ * mirror support (README: not supported); this is an extension. */
+int tree2d_set_mirror(int enable, double d_mirror);
+
+/* Device-resident time step: d_xy += dt * d_uv (forward Euler, the
+ * solver's drift_b, e_drift.f90:17-59), on `stream`. */
+int tree2d_advect_device(int n, double *d_xy, const double *d_uv, double dt, void *stream);
 
 /* Library version string. */
 const char *tree2d_version(void);

@@ -68,3 +68,41 @@ def test_param_file_drives_make_tree(gpu_lib, tmp_path, monkeypatch):
     P.make_tree(g["xy"], g["cir"], g["cor"])
     uv = P.biot_tree_batch(g["txy"])
     assert np.abs(uv - g["uv"]).max() <= 1e-12 * np.abs(g["uv"]).max()
+
+
+@pytest.mark.gpu
+def test_mirror_wall_against_direct_sum_with_images(gpu_lib):
+    """A wall at y = d: images (x, 2d - y) with -G as point vortices."""
+    from conftest import oracle
+    P = gpu_lib
+    rng = np.random.default_rng(5)
+    xy = rng.random((3000, 2)) * [1.0, 0.5] + [0.0, 0.1]
+    cir = rng.standard_normal(3000) / 3000
+    cor = np.full(3000, 0.01)
+    d = 0.05
+    sxy = np.concatenate([xy, np.stack([xy[:, 0], 2 * d - xy[:, 1]], 1)])
+    ref = oracle().direct(xy, sxy, np.concatenate([cir, -cir]), np.concatenate([cor, np.zeros(3000)]))
+    P.set_params(11, 33, 0.5)
+    P.set_mirror(True, d)
+    try:
+        for mode, tol in ((P.MODE_PLAIN, 5e-6), (P.MODE_MIXED, 1e-6)):
+            P.set_mode(mode)
+            P.make_tree(xy, cir, cor)
+            uv = P.biot_tree_batch(xy)
+            assert np.linalg.norm(uv - ref) / np.linalg.norm(ref) <= tol, mode
+    finally:
+        P.set_mirror(False)
+        P.set_mode(P.MODE_PLAIN)
+
+
+@pytest.mark.gpu
+def test_advect_device(gpu_lib):
+    torch = pytest.importorskip("torch")
+    P = gpu_lib
+    dev = torch.device("cuda:0")
+    xy = torch.rand((1000, 2), dtype=torch.float64, device=dev)
+    uv = torch.randn((1000, 2), dtype=torch.float64, device=dev)
+    ref = xy + 1e-3 * uv
+    P.advect_device(xy.data_ptr(), uv.data_ptr(), 1000, 1e-3)
+    torch.cuda.synchronize()
+    assert torch.equal(xy, ref)
