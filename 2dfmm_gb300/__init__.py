@@ -31,7 +31,7 @@ MODE_PLAIN, MODE_MIXED, MODE_LEARNED = 0, 1, 2
 EXPORTS = [
     "make_tree", "biot_tree", "tree2d_last_error", "tree2d_error_string", "tree2d_set_params",
     "tree2d_clear_params", "tree2d_get_params", "tree2d_set_mode", "tree2d_get_mode", "tree2d_set_mixed_params", "biot_tree_batch",
-    "tree2d_solve_device", "tree2d_solve_device_static", "tree2d_get_stats", "tree2d_export_tree", "tree2d_direct_device", "tree2d_fp64_probe", "tree2d_pipe_probe", "tree2d_version",
+    "tree2d_solve_device", "tree2d_solve_device_static", "tree2d_get_stats", "tree2d_export_tree", "tree2d_direct_device", "tree2d_fp64_probe", "tree2d_pipe_probe", "tree2d_wait_probe", "tree2d_version",
     "tree2d_learn_param_count", "tree2d_learn_set_weights", "tree2d_learn_get_weights", "tree2d_learn_set_options",
     "tree2d_learn_collect", "tree2d_learn_train", "tree2d_mlp_grad", "tree2d_mlp_forward",
     "tree2d_set_mirror", "tree2d_advect_device",
@@ -112,6 +112,8 @@ def load(path: str | None = None):
     L.tree2d_fp64_probe.restype = ctypes.c_int
     L.tree2d_pipe_probe.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p, _dp]
     L.tree2d_pipe_probe.restype = ctypes.c_int
+    L.tree2d_wait_probe.argtypes = [ctypes.c_longlong, _ip]
+    L.tree2d_wait_probe.restype = ctypes.c_int
     L.tree2d_version.restype = ctypes.c_char_p
     fp = ctypes.POINTER(ctypes.c_float)
     L.tree2d_learn_param_count.restype = ctypes.c_int
@@ -208,9 +210,16 @@ def biot_tree(x: float, y: float):
     return u.value, v.value
 
 
-def biot_tree_batch(xy, check: bool = True):
+def biot_tree_batch(xy, check: bool = True, out=None):
+    """Velocities at the points xy ((m, 2)); `out`, if given, is a C-contiguous
+    float64 (m, 2) array that receives them (e.g. a page-locked buffer)."""
     xy = _f64(xy).reshape(-1, 2)
-    uv = np.empty_like(xy)
+    if out is None:
+        uv = np.empty_like(xy)
+    else:
+        uv = out
+        if uv.dtype != np.float64 or uv.shape != xy.shape or not uv.flags.c_contiguous:
+            raise ValueError("out must be a C-contiguous float64 array shaped like xy")
     rc = load().biot_tree_batch(len(xy), _ptr(xy), _ptr(uv))
     if check:
         _check(rc, "biot_tree_batch")
@@ -270,6 +279,14 @@ def fp32_peak_tflops(blocks: int = 152 * 8, iters: int = 200000, stream: int = 0
     ms = ctypes.c_double()
     _check(load().tree2d_pipe_probe(32, blocks, iters, stream or None, ctypes.byref(ms)), "pipe_probe")
     return blocks * 256.0 * iters * 16.0 / (ms.value * 1e-3) / 1e12
+
+
+def wait_probe(polls: int = 100_000) -> int:
+    """Runs the bounded-wait check kernel (a wait on a barrier nothing
+    completes) and returns the status it recorded: TREE2D_ERR_TIMEOUT."""
+    st = ctypes.c_int(-1)
+    _check(load().tree2d_wait_probe(polls, ctypes.byref(st)), "wait_probe")
+    return st.value
 
 
 def set_mirror(enable: bool, d_mirror: float = 0.0):

@@ -17,6 +17,7 @@
 #include <cstring>
 #include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "dev_common.cuh"
@@ -72,6 +73,43 @@ void note_cuda_error(cudaError_t e, const char *what) {
 
 namespace {
 
+// Page-locked host array (grown, never shrunk), so that the device->host
+// copy of the velocity table runs at full link speed.
+struct PinnedTable {
+  double *p = nullptr;
+  size_t cap = 0;
+  cudaError_t ensure(size_t elems) {
+    if (elems <= cap) return cudaSuccess;
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    cap = 0;
+    cudaError_t e = cudaMallocHost(reinterpret_cast<void **>(&p), sizeof(double) * elems);
+    if (e == cudaSuccess) cap = elems;
+    return e;
+  }
+  double operator[](size_t i) const { return p[i]; }
+};
+
+// Runs f(begin, end) over [0, n) on up to hardware_concurrency() threads,
+// chunks of at least `grain` items; the calling thread takes the first.
+template <class F>
+void parallel_chunks(long n, long grain, F f) {
+  const long hw = std::max(1u, std::thread::hardware_concurrency());
+  const long nt = std::min(hw, (n + grain - 1) / grain);
+  if (nt <= 1) {
+    if (n > 0) f(0L, n);
+    return;
+  }
+  const long per = (n + nt - 1) / nt;
+  std::vector<std::thread> th;
+  for (long t = 1; t < nt; t++) {
+    const long b = t * per, e = std::min(n, b + per);
+    if (b < e) th.emplace_back(f, b, e);
+  }
+  f(0L, std::min(n, per));
+  for (auto &x : th) x.join();
+}
+
 struct Solver {
   Workspace ws;
   Tree tree;
@@ -99,7 +137,7 @@ struct Lib {
   // results of the last make_tree
   std::atomic<bool> valid{false};
   std::atomic<unsigned long long> generation{0};
-  std::vector<double> h_xy, h_uv;
+  PinnedTable h_xy, h_uv;
   int n = 0;
   // position -> blob index, built on first need
   std::mutex hash_mu;
@@ -297,15 +335,10 @@ void ensure_hash(Lib &L) {
   L.hash_ready.store(true, std::memory_order_release);
 }
 
-// Index of a blob at exactly (x,y), or -1.
-long find_blob(Lib &L, double x, double y) {
-  thread_local unsigned long long gen = ~0ull;
-  thread_local long hint = -1;
-  unsigned long long g = L.generation.load(std::memory_order_acquire);
-  if (gen != g) {
-    gen = g;
-    hint = -1;
-  }
+// Index of a blob at exactly (x,y), or -1.  `hint` is the index found by
+// the previous lookup of the caller: the blob after it (and then it) is
+// tried first, so a sweep over the blobs in order costs one compare each.
+long find_blob_from(Lib &L, double x, double y, long &hint) {
   const long n = L.n;
   for (long c : {hint + 1, hint}) {
     if (c >= 0 && c < n && same_bits(L.h_xy[2 * c], x) && same_bits(L.h_xy[2 * c + 1], y)) {
@@ -324,6 +357,18 @@ long find_blob(Lib &L, double x, double y) {
     }
     h = (h + 1) & L.hash_mask;
   }
+}
+
+// As find_blob_from, with the hint kept per calling thread (biot_tree).
+long find_blob(Lib &L, double x, double y) {
+  thread_local unsigned long long gen = ~0ull;
+  thread_local long hint = -1;
+  unsigned long long g = L.generation.load(std::memory_order_acquire);
+  if (gen != g) {
+    gen = g;
+    hint = -1;
+  }
+  return find_blob_from(L, x, y, hint);
 }
 
 // GPU evaluation of m arbitrary points (host xy) into host uv; L.mu held.
@@ -436,21 +481,37 @@ void make_tree(int nvor_b, const double *vor_b, const double *cir_b, const doubl
       return;
     }
   }
+  // The host copy of the positions (the lookup table's keys) is taken on a
+  // helper thread while the GPU solves.
+  cudaError_t ealloc = L.h_xy.ensure(2 * (size_t)n);
+  if (ealloc == cudaSuccess) ealloc = L.h_uv.ensure(2 * (size_t)n);
+  if (ealloc != cudaSuccess) {
+    note_cuda_error(ealloc, "make_tree host tables");
+    fail(TREE2D_ERR_CUDA);
+    return;
+  }
+  std::thread copier;
+  if (n > 0) {
+    copier = std::thread([&L, vor_b, n] {
+      parallel_chunks(2 * (long)n, 1 << 20, [&](long b, long e) {
+        std::memcpy(L.h_xy.p + b, vor_b + b, sizeof(double) * (size_t)(e - b));
+      });
+    });
+  }
   rc = solve(L, S, n, d_xy, d_cir, d_cor, d_uv, L.stream, L.stats);
   L.last_was_dev = false;
+  if (rc == TREE2D_OK && n > 0) {
+    cudaError_t e = cudaMemcpyAsync(L.h_uv.p, d_uv, sizeof(double) * 2 * (size_t)n, cudaMemcpyDeviceToHost, L.stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(L.stream);
+    if (e != cudaSuccess) {
+      note_cuda_error(e, "make_tree download");
+      rc = TREE2D_ERR_CUDA;
+    }
+  }
+  if (copier.joinable()) copier.join();
   if (rc) {
     fail(rc);
     return;
-  }
-  L.h_xy.assign(vor_b, vor_b + 2 * (size_t)n);
-  L.h_uv.resize(2 * (size_t)n);
-  if (n > 0) {
-    cudaError_t e = cudaMemcpy(L.h_uv.data(), d_uv, sizeof(double) * 2 * (size_t)n, cudaMemcpyDeviceToHost);
-    if (e != cudaSuccess) {
-      note_cuda_error(e, "make_tree download");
-      fail(TREE2D_ERR_CUDA);
-      return;
-    }
   }
   L.n = n;
   L.valid.store(true);
@@ -490,16 +551,29 @@ int biot_tree_batch(int n, const double *xy, double *uv) {
     for (long i = 0; i < 2 * (long)n; i++) uv[i] = NAN;
     return fail(TREE2D_ERR_NO_TREE);
   }
-  std::vector<int> miss;
-  for (int i = 0; i < n; i++) {
-    long k = find_blob(L, xy[2 * (size_t)i], xy[2 * (size_t)i + 1]);
-    if (k >= 0) {
-      uv[2 * (size_t)i] = L.h_uv[2 * k];
-      uv[2 * (size_t)i + 1] = L.h_uv[2 * k + 1];
-    } else {
-      miss.push_back(i);
+  // Table lookups on all host threads (one hint per chunk), misses
+  // collected per chunk and evaluated on the GPU together.
+  const long grain = 1 << 16;
+  const long nchunks = std::max(1L, ((long)n + grain - 1) / grain);
+  std::vector<std::vector<int>> miss_part(nchunks);
+  parallel_chunks((long)nchunks, 1, [&](long cb, long ce) {
+    for (long c = cb; c < ce; c++) {
+      // first guess: query i is blob i (a sweep over the blobs in order)
+      long hint = c * grain - 1;
+      const long e = std::min((long)n, (c + 1) * grain);
+      for (long i = c * grain; i < e; i++) {
+        long k = find_blob_from(L, xy[2 * (size_t)i], xy[2 * (size_t)i + 1], hint);
+        if (k >= 0) {
+          uv[2 * (size_t)i] = L.h_uv[2 * k];
+          uv[2 * (size_t)i + 1] = L.h_uv[2 * k + 1];
+        } else {
+          miss_part[c].push_back((int)i);
+        }
+      }
     }
-  }
+  });
+  std::vector<int> miss;
+  for (auto &m : miss_part) miss.insert(miss.end(), m.begin(), m.end());
   if (miss.empty()) return TREE2D_OK;
   std::vector<double> mxy(2 * miss.size()), muv(2 * miss.size());
   for (size_t j = 0; j < miss.size(); j++) {
@@ -657,6 +731,20 @@ int tree2d_direct_device(int ntgt, const double *d_txy, int nsrc, const double *
 
 int tree2d_fp64_probe(int blocks, int iters, void *stream, double *ms) {
   return tree2d_pipe_probe(64, blocks, iters, stream, ms);
+}
+
+int tree2d_wait_probe(long long polls, int *status) {
+  if (polls < 1 || !status) return fail(TREE2D_ERR_BAD_INPUT);
+  int *d = nullptr;
+  if (cudaMalloc(reinterpret_cast<void **>(&d), sizeof(int)) != cudaSuccess) return fail(TREE2D_ERR_CUDA);
+  cudaError_t e = wait_probe((long)polls, d, nullptr);
+  if (e == cudaSuccess) e = cudaMemcpy(status, d, sizeof(int), cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  if (e != cudaSuccess) {
+    note_cuda_error(e, "wait_probe");
+    return fail(TREE2D_ERR_CUDA);
+  }
+  return TREE2D_OK;
 }
 
 int tree2d_pipe_probe(int bits, int blocks, int iters, void *stream, double *ms) {

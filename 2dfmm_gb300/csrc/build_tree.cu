@@ -83,15 +83,24 @@ __global__ void __launch_bounds__(256) k_bbox(const double *__restrict__ xy, con
   }
 }
 
+// One warp: the lanes reduce strided parts, then a shuffle reduction.
 __global__ void k_root(const Box4 *part, int nparts, RootBox *root) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  Box4 r = part[0];
-  for (int k = 1; k < nparts; k++) {
-    r.x = fmax(r.x, part[k].x);
-    r.y = fmin(r.y, part[k].y);
-    r.z = fmax(r.z, part[k].z);
-    r.w = fmin(r.w, part[k].w);
+  if (blockIdx.x != 0) return;
+  const int lane = threadIdx.x & 31;
+  if (threadIdx.x >= 32) return;
+  Box4 r{-INFINITY, INFINITY, -INFINITY, INFINITY};
+  for (int k = lane; k < nparts; k += 32) {
+    const Box4 p = part[k];
+    r.x = fmax(r.x, p.x);
+    r.y = fmin(r.y, p.y);
+    r.z = fmax(r.z, p.z);
+    r.w = fmin(r.w, p.w);
   }
+  r.x = warp_max(r.x);
+  r.y = warp_min(r.y);
+  r.z = warp_max(r.z);
+  r.w = warp_min(r.w);
+  if (lane != 0) return;
   // quadtree.c:87-98
   double rx = __dadd_rn(fabs(__dsub_rn(r.x, r.y)), 0.0001);
   double ry = __dadd_rn(fabs(__dsub_rn(r.z, r.w)), 0.0001);
@@ -117,16 +126,91 @@ __device__ __forceinline__ unsigned descend(double x, double y, double &cx, doub
   return q;
 }
 
+// Order-preserving map of a non-NaN double to an unsigned integer (-0 is
+// taken as +0, as the FP64 comparisons treat them): a >= b iff
+// okey(a) >= okey(b).  Lets the key descent compare on the integer pipe.
+__device__ __forceinline__ uint64_t okey(double d) {
+  uint64_t u = (uint64_t)__double_as_longlong(d);
+  if (u == 0x8000000000000000ull) u = 0;
+  return (u >> 63) ? ~u : (u | 0x8000000000000000ull);
+}
+__device__ __forceinline__ double okey_inv(uint64_t k) {
+  const uint64_t u = (k >> 63) ? (k & 0x7fffffffffffffffull) : ~k;
+  return __longlong_as_double((long long)u);
+}
+
+// Centre table of the first `lt` levels: entry (l, i) of the x
+// table is the x centre of the level-l cells in column i, formed by the
+// same sequence of FP64 operations as the descent (c +- 0.25 R per level,
+// quadtree.c:61-79), so comparing against it gives the reference's digits.
+// Level l occupies entries [2^l - 1, 2^(l+1) - 1) (2^lt - 1 per axis); the
+// y table follows, with row i counted from the top (bit 1 = y <= cy = lower
+// half).  16 levels (1 MB) for large sets, 12 (64 KB) otherwise.
+inline int centre_levels(int n) { return n > 65536 ? 16 : 12; }
+inline size_t centre_entries(int lt) { return ((size_t)1 << lt) - 1; }
+
+__global__ void __launch_bounds__(256) k_centre_table(const RootBox *__restrict__ root, uint64_t *__restrict__ tab,
+                                                      int lt) {
+  const int per = (1 << lt) - 1;
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= 2 * per) return;
+  const int axis = g >= per;
+  const int e = g - axis * per;
+  const int l = 31 - __clz(e + 1);
+  const unsigned i = (unsigned)(e + 1 - (1 << l));
+  double c = axis ? root->cy : root->cx, R = root->region;
+  for (int j = 0; j < l; j++) {
+    const unsigned bit = (i >> (l - 1 - j)) & 1u;
+    const double h = __dmul_rn(0.25, R);
+    if (axis == 0)
+      c = bit ? __dadd_rn(c, h) : __dsub_rn(c, h);
+    else
+      c = bit ? __dsub_rn(c, h) : __dadd_rn(c, h);
+    R = __dmul_rn(0.5, R);
+  }
+  tab[g] = okey(c);
+}
+
 // `levels` digits, level 1 in the top two bits, zero below the last level.
+// With a centre table of `tlev` levels the first digits are integer
+// compares against it; the rest continue the FP64 descent from the centre
+// of the level-tlev cell.
 __global__ void __launch_bounds__(256) k_keys(const double *__restrict__ xy, int n, const RootBox *__restrict__ root,
-                                              uint64_t *__restrict__ keys, uint32_t *__restrict__ vals, int levels) {
+                                              const uint64_t *__restrict__ tab, int tlev, uint64_t *__restrict__ keys,
+                                              uint32_t *__restrict__ vals, int levels) {
   long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (i >= n) return;
   double x = xy[2 * i], y = xy[2 * i + 1];
   double cx = root->cx, cy = root->cy, R = root->region;
   uint64_t key = 0;
+  int l = 0;
+  if (tab) {
+    const uint64_t xk = okey(x), yk = okey(y);
+    const int lt = min(levels, tlev);
+    const int ybase = (1 << tlev) - 1;
+    unsigned ix = 0, iy = 0;
 #pragma unroll 4
-  for (int l = 0; l < levels; l++) key = (key << 2) | descend(x, y, cx, cy, R);
+    for (; l < lt; l++) {
+      const int off = (1 << l) - 1;
+      const unsigned bx = xk >= __ldg(tab + off + ix) ? 1u : 0u;
+      const unsigned by = yk <= __ldg(tab + ybase + off + iy) ? 1u : 0u;
+      key = (key << 2) | bx | (by << 1);
+      ix = 2 * ix + bx;
+      iy = 2 * iy + by;
+    }
+    if (l < levels) {
+      // centre of the level-lt cell: its parent's centre +- a quarter side
+      const int off = (1 << (lt - 1)) - 1;
+      const double px = okey_inv(tab[off + (ix >> 1)]), py = okey_inv(tab[ybase + off + (iy >> 1)]);
+      for (int j = 0; j < lt - 1; j++) R = __dmul_rn(0.5, R);
+      const double h = __dmul_rn(0.25, R);
+      cx = (ix & 1u) ? __dadd_rn(px, h) : __dsub_rn(px, h);
+      cy = (iy & 1u) ? __dsub_rn(py, h) : __dadd_rn(py, h);
+      R = __dmul_rn(0.5, R);
+    }
+  }
+#pragma unroll 4
+  for (; l < levels; l++) key = (key << 2) | descend(x, y, cx, cy, R);
   keys[i] = levels < kKeyLevels ? key << (64 - 2 * levels) : key;
   vals[i] = (uint32_t)i;
 }
@@ -265,7 +349,42 @@ struct EmitArgs {
   unsigned char *leaf;
   double *cx, *cy, *region;
   int *leaf_cell;
+  const uint64_t *tab;  // centre table of `tlev` levels (k_centre_table)
+  int tlev;
 };
+
+// x (even) or y (odd) bits of the top 2*l key bits, compacted: the column
+// or row index of the level-l cell holding the key.
+__device__ __forceinline__ unsigned key_axis(uint64_t key, int l, int axis) {
+  if (l == 0) return 0u;
+  uint64_t v = (key >> (64 - 2 * l) >> axis) & 0x5555555555555555ull;
+  v = (v | (v >> 1)) & 0x3333333333333333ull;
+  v = (v | (v >> 2)) & 0x0f0f0f0f0f0f0f0full;
+  v = (v | (v >> 4)) & 0x00ff00ff00ff00ffull;
+  v = (v | (v >> 8)) & 0x0000ffff0000ffffull;
+  v = (v | (v >> 16)) & 0x00000000ffffffffull;
+  return (unsigned)v;
+}
+
+// Centre and side of the level-`lev` cell holding `key`, bit-identical to
+// the reference's descent: read from the centre table up to its last level,
+// then continued in FP64 (c +- 0.25 R per level).
+__device__ __forceinline__ void cell_geometry(const EmitArgs &a, uint64_t key, int lev, double R0, double &cx,
+                                              double &cy, double &R) {
+  const int l0 = min(lev, a.tlev - 1);
+  const int off = (1 << l0) - 1, ybase = (1 << a.tlev) - 1;
+  cx = okey_inv(a.tab[off + key_axis(key, l0, 0)]);
+  cy = okey_inv(a.tab[ybase + off + key_axis(key, l0, 1)]);
+  R = R0;
+  for (int j = 0; j < l0; j++) R = __dmul_rn(0.5, R);  // exact: R0 * 2^-l0
+  for (int l = l0 + 1; l <= lev; l++) {
+    const unsigned q = (unsigned)(key >> (64 - 2 * l)) & 3u;
+    const double h = __dmul_rn(0.25, R);
+    cx = (q & 1u) ? __dadd_rn(cx, h) : __dsub_rn(cx, h);
+    cy = (q & 2u) ? __dsub_rn(cy, h) : __dadd_rn(cy, h);
+    R = __dmul_rn(0.5, R);
+  }
+}
 
 __global__ void __launch_bounds__(kScanThreads) k_emit_cells(EmitArgs a) {
   const long base = (long)blockIdx.x * kScanTile + (long)threadIdx.x * kScanItems;
@@ -301,14 +420,10 @@ __global__ void __launch_bounds__(kScanThreads) k_emit_cells(EmitArgs a) {
       int prev = i > 0 ? a.cpl[i - 1] : 0;
       int lam = a.leaf_level[i];
       uint64_t key = a.keys[i];
-      double cx = cx0, cy = cy0, R = R0;
-      for (int lev = 1; lev <= lam; lev++) {
-        unsigned q = (unsigned)(key >> (64 - 2 * lev)) & 3u;
-        double h = __dmul_rn(0.25, R);
-        cx = (q & 1u) ? __dadd_rn(cx, h) : __dsub_rn(cx, h);
-        cy = (q & 2u) ? __dsub_rn(cy, h) : __dadd_rn(cy, h);
-        R = __dmul_rn(0.5, R);
-        if (lev > prev) {
+      for (int lev = prev + 1; lev <= lam; lev++) {
+        double cx, cy, R;
+        cell_geometry(a, key, lev, R0, cx, cy, R);
+        {
           unsigned id = cell0 + (unsigned)(lev - prev - 1);
           a.level[id] = lev;
           a.begin[id] = (int)i;
@@ -450,6 +565,8 @@ int build_tree(Workspace &ws, int n, const double *d_xy, const double *d_cir, co
   tneed += radix_sort_temp_bytes(n) + 256;
   tneed += Arena::bytes_for(kBoxBlocks, sizeof(Box4));
   tneed += Arena::bytes_for(ntiles + 1, 8) + 256;
+  const int tlev = centre_levels(n);
+  tneed += Arena::bytes_for(2 * centre_entries(tlev), 8);
   T2D_CUDA_TRY(ws.tmp_arena.reserve(tneed));
   ws.tmp_arena.reset();
   uint64_t *keys_alt = ws.tmp_arena.take<uint64_t>(n);
@@ -460,6 +577,7 @@ int build_tree(Workspace &ws, int n, const double *d_xy, const double *d_cir, co
   Box4 *bpart = ws.tmp_arena.take<Box4>(kBoxBlocks);
   unsigned long long *part = ws.tmp_arena.take<unsigned long long>(ntiles + 1);
   unsigned long long *total = ws.tmp_arena.take<unsigned long long>(1);
+  uint64_t *ctab = ws.tmp_arena.take<uint64_t>(2 * centre_entries(tlev));
 
   int levels = kShortKeyLevels;
 retry:
@@ -471,8 +589,9 @@ retry:
   k_root<<<1, 32, 0, s>>>(bpart, kBoxBlocks, t.root);
   ::t2d::g_launches.fetch_add(1, std::memory_order_relaxed);
   // 2. keys
-  k_keys<<<(n + 255) / 256, 256, 0, s>>>(d_xy, n, t.root, t.keys, vals, levels);
-  ::t2d::g_launches.fetch_add(1, std::memory_order_relaxed);
+  k_centre_table<<<(int)((2 * centre_entries(tlev) + 255) / 256), 256, 0, s>>>(t.root, ctab, tlev);
+  k_keys<<<(n + 255) / 256, 256, 0, s>>>(d_xy, n, t.root, ctab, tlev, t.keys, vals, levels);
+  ::t2d::g_launches.fetch_add(2, std::memory_order_relaxed);
   // 3. sort
   T2D_CUDA_TRY(radix_sort_pairs(t.keys, vals, keys_alt, vals_alt, n, 64 - 2 * levels, 64, sort_tmp, s));
   // 4-5. leaf levels
@@ -533,7 +652,7 @@ retry:
 
   // 7. cells
   EmitArgs ea{t.keys, cpl, leaf_level, part, t.root, n, cellbase, t.level, t.begin, t.leaf, t.cx, t.cy, t.region,
-              t.leaf_cell};
+              t.leaf_cell, ctab, tlev};
   k_emit_cells<<<ntiles, kScanThreads, 0, s>>>(ea);
   ::t2d::g_launches.fetch_add(1, std::memory_order_relaxed);
   k_cell_end<<<(t.ncell + 255) / 256, 256, 0, s>>>(t.keys, n, t.ncell, t.level, t.begin, t.end);
@@ -562,7 +681,8 @@ int sort_targets(Workspace &ws, int n, const double *d_xy, const RootBox *d_root
   uint32_t *v2 = ws.tmp_arena.take<uint32_t>(n);
   void *tmp = ws.tmp_arena.take<char>(radix_sort_temp_bytes(n));
   // order only (for coherent warps): the short key depth is enough
-  k_keys<<<(n + 255) / 256, 256, 0, s>>>(d_xy, n, d_root, k, reinterpret_cast<uint32_t *>(d_order), kShortKeyLevels);
+  k_keys<<<(n + 255) / 256, 256, 0, s>>>(d_xy, n, d_root, nullptr, 0, k, reinterpret_cast<uint32_t *>(d_order),
+                                          kShortKeyLevels);
   ::t2d::g_launches.fetch_add(1, std::memory_order_relaxed);
   T2D_CUDA_TRY(radix_sort_pairs(k, reinterpret_cast<uint32_t *>(d_order), k2, v2, n, 64 - 2 * kShortKeyLevels, 64,
                                 tmp, s));

@@ -3,6 +3,7 @@
 // (ver-c/src/fmm.c:121-142, r > 1e-10) applied to every source.  Sources are
 // staged through shared memory in tiles; one thread per target.
 #include "dev_common.cuh"
+#include "tc_ptx.cuh"
 
 namespace t2d {
 namespace {
@@ -93,6 +94,27 @@ __global__ void __launch_bounds__(256) k_dfma_probe(double *out, int iters, doub
 
 }  // namespace
 
+// Bounded-wait check: lane 0 waits on a shared-memory mbarrier that nothing
+// arrives on, with the same bounded poll the tensor-core kernels use, and
+// records TREE2D_ERR_TIMEOUT when the wait gives up (1 = the wait ended,
+// which no arrival can cause here).  The kernel always returns, so the
+// context stays usable.
+__global__ void k_wait_probe(long polls, int *out) {
+  __shared__ uint64_t bar;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) *out = mbar_wait(&bar, 0, polls) ? 1 : TREE2D_ERR_TIMEOUT;
+}
+
+cudaError_t wait_probe(long polls, int *out, cudaStream_t s) {
+  k_wait_probe<<<1, 32, 0, s>>>(polls, out);
+  ::t2d::g_launches.fetch_add(1, std::memory_order_relaxed);
+  return cudaGetLastError();
+}
+
 cudaError_t dfma_probe(double *out, int blocks, int iters, cudaStream_t s) {
   k_dfma_probe<<<blocks, 256, 0, s>>>(out, iters, 0.999999, 1e-7);
   ::t2d::g_launches.fetch_add(1, std::memory_order_relaxed);
@@ -100,10 +122,12 @@ cudaError_t dfma_probe(double *out, int blocks, int iters, cudaStream_t s) {
 }
 
 // Forward Euler step of the blob positions, x += dt * u (the solver's drift,
-// e_drift.f90:17-59), on the device: xy and uv interleaved.
+// e_drift.f90:17-59), on the device: xy and uv interleaved.  The product
+// and the sum are rounded separately (no FMA contraction), as the host
+// expression x + dt*u evaluates without fused multiply-add.
 __global__ void k_advect(long n, double *xy, const double *uv, double dt) {
   long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
-  if (i < 2 * n) xy[i] += dt * uv[i];
+  if (i < 2 * n) xy[i] = __dadd_rn(xy[i], __dmul_rn(dt, uv[i]));
 }
 
 // Image blobs for a mirror wall at y = d: (x, 2d - y), circulation -G, core

@@ -178,6 +178,7 @@ cudaError_t direct_sum(int ntgt, const double *txy, int nsrc, const double *sxy,
 // FP64 pipe probe: blocks x 256 threads x iters x 8 FMAs (2 flops each).
 cudaError_t dfma_probe(double *out, int blocks, int iters, cudaStream_t s);
 cudaError_t ffma_probe(float *out, int blocks, int iters, cudaStream_t s);
+cudaError_t wait_probe(long polls, int *out, cudaStream_t s);
 cudaError_t advect(long n, double *xy, const double *uv, double dt, cudaStream_t s);
 // Blobs followed by their images in a wall at y = d (2n entries out).
 cudaError_t mirror_images(long n, const double *xy, const double *cir, const double *cor, double d, double *oxy,

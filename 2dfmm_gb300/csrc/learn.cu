@@ -42,7 +42,7 @@ __global__ void k_leaf_stats(MixedView m, LeafStats *out) {
     mx += s.z * zx;
     my += s.z * zy;
     m2 += g * (zx * zx + zy * zy);
-    sg = fmaxf(sg, rsqrtf(fmaxf(s.w, 1e-30f)));
+    sg = fmaxf(sg, rsqrtf(fmaxf(-s.w * 0.69314718f, 1e-30f)));  // s.w = -log2(e)/sigma^2
   }
   for (int o = 16; o; o >>= 1) {
     ga += __shfl_xor_sync(0xffffffffu, ga, o);
@@ -75,7 +75,6 @@ __global__ void k_labels(MixedView m, const LeafStats *st, const float *u_ref_pt
   const int B = m.leaf_cell[l];
   const int A = kind == 0 ? m.u_idx[e] : m.k_idx[e];
   const float u_ref = *u_ref_ptr;
-  const double rc = (double)(*m.rc_ptr);
   const int P = m.P;
   const double ox = m.cx[B] - m.cx[A], oy = m.cy[B] - m.cy[A];
   const float oxf = m.cxf[B] - m.cxf[A], oyf = m.cyf[B] - m.cyf[A];
@@ -95,14 +94,15 @@ __global__ void k_labels(MixedView m, const LeafStats *st, const float *u_ref_pt
       const double rx = ((double)zt.x - (double)s.x) + ox, ry = ((double)zt.y - (double)s.y) + oy;
       const double r2 = rx * rx + ry * ry;
       const double r = sqrt(r2);
+      // s.w = -log2(e)/sigma^2, so exp(-r^2/sigma^2) = 2^(r^2 s.w)
       if (kind == 0) {
         if (r > 1e-10) {
-          const double f = (double)s.z * (1.0 - exp(-r2 * (double)s.w)) / r2;
+          const double f = (double)s.z * (1.0 - exp2(r2 * (double)s.w)) / r2;
           ex -= f * ry;
           ey += f * rx;
         }
-      } else if (r < rc) {
-        const double f = -(double)s.z * exp(-r2 * (double)s.w) / r2;
+      } else if (r > 1e-10) {
+        const double f = -(double)s.z * exp2(r2 * (double)s.w) / r2;
         ex -= f * ry;
         ey += f * rx;
       }

@@ -41,17 +41,23 @@ struct InferArgs {
   long wait_limit;
 };
 
+// Two floats rounded to BF16 (round to nearest even), a in the low half.
 __device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
-  const uint32_t lo = __bfloat16_as_ushort(__float2bfloat16_rn(a));
-  const uint32_t hi = __bfloat16_as_ushort(__float2bfloat16_rn(b));
-  return lo | (hi << 16);
+  const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+  return *reinterpret_cast<const uint32_t *>(&h);
 }
 
-__device__ __forceinline__ float gelu_fast(float z) {
-  float t;
-  const float u = 0.7978845608028654f * (z + 0.044715f * z * z * z);
-  asm("tanh.approx.f32 %0, %1;" : "=f"(t) : "f"(u));
-  return 0.5f * z * (1.f + t);
+// GELU (tanh form) of two values, packed to BF16 for the next layer's
+// input: the tanh runs on the SFU in BF16x2 (one instruction for both
+// values; its ~2^-8 error is the order of the BF16 rounding of the result),
+// the rest in FP32.
+__device__ __forceinline__ uint32_t gelu2_bf16(float z0, float z1) {
+  const float u0 = 0.7978845608028654f * fmaf(0.044715f * z0, z0 * z0, z0);
+  const float u1 = 0.7978845608028654f * fmaf(0.044715f * z1, z1 * z1, z1);
+  uint32_t t;
+  asm("tanh.approx.bf16x2 %0, %1;" : "=r"(t) : "r"(pack_bf16(u0, u1)));
+  const float t0 = __uint_as_float(t << 16), t1 = __uint_as_float(t & 0xffff0000u);
+  return pack_bf16(0.5f * z0 * (1.f + t0), 0.5f * z1 * (1.f + t1));
 }
 
 // Row r of the activation tile, K = 8*nk elements: element k at
@@ -123,7 +129,7 @@ __global__ void __launch_bounds__(kTile) k_mlp_infer(InferArgs a) {
     const bool valid = gi < total;
     int kind = 0;
     long e = 0;
-    float v[64];
+    float v[kMlpIn];
     if (!valid) {
       for (int k = 0; k < kMlpIn; k++) v[k] = 0.f;
     } else if (a.X) {
@@ -162,17 +168,32 @@ __global__ void __launch_bounds__(kTile) k_mlp_infer(InferArgs a) {
         mma_inflight = true;
       }
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      // accumulator row -> bias (+ GELU) in registers
+      // accumulator row -> bias + GELU -> BF16 row of the next layer's input
+      // (32 columns per TMEM load), or bias -> logits after the last layer
       const float *bs = s_bias + layer * 64;
-      for (int c0 = 0; c0 < N; c0 += 8) {
-        uint32_t r[8];
-        tmem_ld8(taddr + (uint32_t)c0, r);
-        for (int j = 0; j < 8; j++) {
-          const float z = __uint_as_float(r[j]) + bs[c0 + j];
-          v[c0 + j] = layer < 3 ? gelu_fast(z) : z;
+      if (layer < 3) {
+        unsigned char *rowp = act + (uint32_t)(tid >> 3) * 1024u + (uint32_t)(tid & 7) * 16u;  // SBO = 8*128
+        for (int c0 = 0; c0 < 64; c0 += 32) {
+          uint32_t r[32];
+          tmem_ld32(taddr + (uint32_t)c0, r);
+          tmem_wait();
+#pragma unroll
+          for (int q = 0; q < 4; q++) {
+            uint4 w;
+            const int c = c0 + 8 * q;
+            w.x = gelu2_bf16(__uint_as_float(r[8 * q + 0]) + bs[c + 0], __uint_as_float(r[8 * q + 1]) + bs[c + 1]);
+            w.y = gelu2_bf16(__uint_as_float(r[8 * q + 2]) + bs[c + 2], __uint_as_float(r[8 * q + 3]) + bs[c + 3]);
+            w.z = gelu2_bf16(__uint_as_float(r[8 * q + 4]) + bs[c + 4], __uint_as_float(r[8 * q + 5]) + bs[c + 5]);
+            w.w = gelu2_bf16(__uint_as_float(r[8 * q + 6]) + bs[c + 6], __uint_as_float(r[8 * q + 7]) + bs[c + 7]);
+            *reinterpret_cast<uint4 *>(rowp + (uint32_t)(c / 8) * 128u) = w;
+          }
         }
+      } else {
+        uint32_t r[16];
+        tmem_ld16(taddr, r);
+        tmem_wait();
+        for (int j = 0; j < 16; j++) v[j] = __uint_as_float(r[j]) + bs[j];
       }
-      if (layer < 3) store_row(act, tid, v, 64);
     }
     if (valid) {
       if (a.X) {

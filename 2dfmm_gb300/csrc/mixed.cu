@@ -151,7 +151,7 @@ __global__ void k_leaf_setup(MixedView m, const double *x, const double *y, cons
     m.gam[i] = (float)cir[i];
     double s = cor[i];
     m.s2inv[i] = (float)(1.0 / (s * s));
-    m.src4[i] = make_float4(m.loc[i].x, m.loc[i].y, m.gam[i], m.s2inv[i]);
+    m.src4[i] = make_float4(m.loc[i].x, m.loc[i].y, m.gam[i], (float)(-1.4426950408889634 / (s * s)));
   }
 }
 
@@ -251,50 +251,6 @@ __global__ void k_parent(MixedView m) {
     if ((&ch.x)[q] >= 0) m.parent[(&ch.x)[q]] = c;
 }
 
-// U and W lists of one leaf.  `emit(kind, id)` with kind 0 = U, 1 = W.
-template <class Emit>
-__device__ void uw_walk(const MixedView &m, int b, Emit emit) {
-  const int lev = m.level[b];
-  int coarse_seen[8];
-  int ncs = 0;
-  int stack[4 * kKeyLevels + 8];
-  for (int k = 0; k < 9; k++) {
-    const int co = m.coarse[b * 9 + k];
-    if (co >= 0) {
-      bool dup = false;
-      for (int j = 0; j < ncs; j++) dup |= coarse_seen[j] == co;
-      if (!dup) {
-        coarse_seen[ncs++] = co;
-        emit(0, co);
-      }
-    }
-    const int e = m.coll[b * 9 + k];
-    if (e < 0) continue;
-    if (m.leaf[e]) {
-      emit(0, e);
-      continue;
-    }
-    int top = 0;
-    stack[top++] = e;
-    while (top > 0) {
-      const int c = stack[--top];
-      const int4 ch = reinterpret_cast<const int4 *>(m.child)[c];
-      for (int q = 0; q < 4; q++) {
-        const int cc = (&ch.x)[q];
-        if (cc < 0) continue;
-        if (adjacent(lev, m.ix[b], m.iy[b], m.level[cc], m.ix[cc], m.iy[cc])) {
-          if (m.leaf[cc])
-            emit(0, cc);
-          else if (top < 4 * kKeyLevels + 8)
-            stack[top++] = cc;
-        } else {
-          emit(1, cc);
-        }
-      }
-    }
-  }
-}
-
 // Distance between the boxes of cells a and b (FP32: only compared with rc).
 __device__ __forceinline__ float box_gap(const MixedView &m, int a, int b) {
   const float half = 0.5f * (m.h[a] + m.h[b]);
@@ -303,87 +259,209 @@ __device__ __forceinline__ float box_gap(const MixedView &m, int a, int b) {
   return sqrtf(gx * gx + gy * gy);
 }
 
-// Correction leaves of leaf b: not adjacent, box within rc.
-template <class Emit>
-__device__ void corr_walk(const MixedView &m, int b, Emit emit) {
+// U, W and K lists of leaf B, one warp per leaf.
+//   U: leaves adjacent to B (any level, B itself included): the coarser
+//      leaves among B's neighbours, the same-level neighbours that are
+//      leaves, and the adjacent leaves below the others;
+//   W: cells below B's same-level neighbours that are not adjacent to B
+//      but whose parent is;
+//   K: leaves not adjacent to B whose box lies within rc of B's box (the
+//      blob-core correction).
+// The walk keeps one stack per warp in shared memory; every round pops up
+// to 8 cells and lane (entry, quadrant) classifies one child, so a leaf's
+// lists take tens of rounds instead of hundreds of serial steps.  Stack
+// entries of the correction walk carry kTagK.  A round pops k <= 8 and
+// pushes <= 32, and the cells it pushes lie one level below the ones it
+// popped, so the stack holds at most 24 entries per level plus one round:
+// 24 * 32 + 32 < kWalkStack for the deepest tree (32 levels).
+constexpr int kWalkWarps = 4;
+constexpr int kWalkStack = 1024;
+constexpr unsigned kTagK = 0x80000000u;
+
+template <bool kFill>
+__global__ void __launch_bounds__(32 * kWalkWarps) k_lists(MixedView m) {
+  __shared__ unsigned s_stack[kWalkWarps][kWalkStack];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int l = blockIdx.x * kWalkWarps + warp;
+  if (l >= m.nleaf) return;  // uniform over the warp
+  unsigned *stk = s_stack[warp];
+  const unsigned lt = (1u << lane) - 1u;
+  const int b = m.leaf_cell[l];
+  const int lev = m.level[b];
+  const unsigned bx = m.ix[b], by = m.iy[b];
   const float rc = *m.rc_ptr;
-  if (!(rc > 0.f)) return;
-  int stack[4 * kKeyLevels + 8];
+  int base[3] = {0, 0, 0};
+  if (kFill) {
+    base[0] = m.u_off[l];
+    base[1] = m.w_off[l];
+    base[2] = m.k_off[l];
+  }
+  int *const dst[3] = {m.u_idx, m.w_idx, m.k_idx};
+  int *const own[3] = {m.u_leaf, nullptr, m.k_leaf};
+  // each lane offers (kind, id), kind -1 = nothing; outputs keep lane order
+  auto emit = [&](int kind, int id) {
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      const unsigned bal = __ballot_sync(0xffffffffu, kind == k);
+      if (kFill && kind == k) {
+        const int pos = base[k] + __popc(bal & lt);
+        dst[k][pos] = id;
+        if (own[k]) own[k][pos] = l;
+      }
+      base[k] += __popc(bal);
+    }
+  };
   int top = 0;
-  stack[top++] = 0;
+  auto push = [&](bool want, unsigned v) {
+    const unsigned bal = __ballot_sync(0xffffffffu, want);
+    if (want) stk[top + __popc(bal & lt)] = v;
+    top += __popc(bal);
+  };
+  {
+    // the 3x3 neighbourhood: coarser leaves (each once), same-level cells
+    int co = -1, e = -1;
+    if (lane < 9) {
+      co = m.coarse[b * 9 + lane];
+      e = m.coll[b * 9 + lane];
+    }
+    const unsigned same = __match_any_sync(0xffffffffu, co);
+    emit(co >= 0 && (same & lt) == 0 ? 0 : -1, co);
+    const bool eleaf = e >= 0 && m.leaf[e];
+    emit(eleaf ? 0 : -1, e);
+    push(e >= 0 && !eleaf, (unsigned)e);
+    push(lane == 0 && rc > 0.f, kTagK);  // the root, for the correction walk
+  }
+  __syncwarp();
   while (top > 0) {
-    const int c = stack[--top];
-    const int4 ch = reinterpret_cast<const int4 *>(m.child)[c];
-    for (int q = 0; q < 4; q++) {
-      const int cc = (&ch.x)[q];
-      if (cc < 0) continue;
-      if (box_gap(m, cc, b) >= rc) continue;
-      if (m.leaf[cc]) {
-        if (!adj_cells(m, cc, b)) emit(2, cc);
-      } else if (top < 4 * kKeyLevels + 8) {
-        stack[top++] = cc;
+    const int k = min(8, top);
+    const int ent = lane >> 2, q = lane & 3;
+    const bool act = ent < k;
+    const unsigned v = act ? stk[top - 1 - ent] : 0u;
+    __syncwarp();
+    top -= k;
+    int kind = -1, cc = -1;
+    bool grow = false;
+    unsigned gv = 0;
+    if (act) {
+      const int c = (int)(v & ~kTagK);
+      cc = m.child[4 * c + q];
+      if (cc >= 0) {
+        if (v & kTagK) {
+          if (box_gap(m, cc, b) < rc) {
+            if (m.leaf[cc]) {
+              if (!adj_cells(m, cc, b)) kind = 2;
+            } else {
+              grow = true;
+              gv = (unsigned)cc | kTagK;
+            }
+          }
+        } else if (adjacent(lev, bx, by, m.level[cc], m.ix[cc], m.iy[cc])) {
+          if (m.leaf[cc]) {
+            kind = 0;
+          } else {
+            grow = true;
+            gv = (unsigned)cc;
+          }
+        } else {
+          kind = 1;
+        }
       }
     }
+    emit(kind, cc);
+    if (top + 32 > kWalkStack) {  // unreachable for trees of <= 32 levels
+      if (lane == 0) set_err(m.st, TREE2D_ERR_TOO_DEEP);
+      break;
+    }
+    push(grow, gv);
+    __syncwarp();
+  }
+  if (!kFill && lane == 0) {
+    m.u_off[l] = base[0];
+    m.w_off[l] = base[1];
+    m.k_off[l] = base[2];
   }
 }
 
-__global__ void k_list_count(MixedView m) {
-  int l = blockIdx.x * blockDim.x + threadIdx.x;
-  if (l >= m.nleaf) return;
-  const int b = m.leaf_cell[l];
-  int cnt[3] = {0, 0, 0};
-  auto emit = [&](int kind, int) { cnt[kind]++; };
-  uw_walk(m, b, emit);
-  corr_walk(m, b, emit);
-  m.u_off[l] = cnt[0];
-  m.w_off[l] = cnt[1];
-  m.k_off[l] = cnt[2];
-}
+// Exclusive scan of three count arrays of length len in place, totals at
+// [len]: per-tile sums (kScanTile3 entries per block), a scan of the tile
+// sums, then each tile scanned with its offset.
+constexpr int kScan3Threads = 512, kScan3Items = 8, kScanTile3 = kScan3Threads * kScan3Items;
 
-__global__ void k_list_fill(MixedView m) {
-  int l = blockIdx.x * blockDim.x + threadIdx.x;
-  if (l >= m.nleaf) return;
-  const int b = m.leaf_cell[l];
-  int pos[3] = {m.u_off[l], m.w_off[l], m.k_off[l]};
-  int *dst[3] = {m.u_idx, m.w_idx, m.k_idx};
-  int *own[3] = {m.u_leaf, nullptr, m.k_leaf};
-  auto emit = [&](int kind, int id) {
-    if (own[kind]) own[kind][pos[kind]] = l;
-    dst[kind][pos[kind]++] = id;
-  };
-  uw_walk(m, b, emit);
-  corr_walk(m, b, emit);
-}
-
-// exclusive scan of three count arrays of length len (one block); totals
-// appended at [len].
-__global__ void __launch_bounds__(1024) k_scan3(int *a, int *b, int *c, int len) {
-  __shared__ long long s[3][1024];
-  int *arr[3] = {a, b, c};
-  const int t = threadIdx.x;
-  const int per = (len + 1023) / 1024;
-  const int lo = t * per, hi = min(len, lo + per);
-  for (int k = 0; k < 3; k++) {
-    long long acc = 0;
-    for (int i = lo; i < hi; i++) acc += arr[k][i];
-    s[k][t] = acc;
+__device__ __forceinline__ int block_exclusive_scan(int v, int *sh, int &total) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  int x = v;
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) sh[w] = x;
+  __syncthreads();
+  if (w == 0) {
+    const int nw = blockDim.x >> 5;
+    int t = lane < nw ? sh[lane] : 0;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, t, o);
+      if (lane >= o) t += y;
+    }
+    if (lane < nw) sh[lane] = t;
   }
   __syncthreads();
-  for (int off = 1; off < 1024; off <<= 1) {
-    long long v[3];
-    for (int k = 0; k < 3; k++) v[k] = t >= off ? s[k][t - off] : 0;
-    __syncthreads();
-    for (int k = 0; k < 3; k++) s[k][t] += v[k];
-    __syncthreads();
-  }
+  total = sh[(blockDim.x >> 5) - 1];
+  const int r = (w ? sh[w - 1] : 0) + x - v;
+  __syncthreads();
+  return r;
+}
+
+__global__ void __launch_bounds__(kScan3Threads) k_scan3_tiles(const int *a, const int *b, const int *c, int len,
+                                                               int *tile_sums, int ntiles) {
+  __shared__ int sh[32];
+  const int *arr[3] = {a, b, c};
   for (int k = 0; k < 3; k++) {
-    long long run = t == 0 ? 0 : s[k][t - 1];
-    for (int i = lo; i < hi; i++) {
-      int x = arr[k][i];
-      arr[k][i] = (int)run;
-      run += x;
+    int v = 0;
+    const long i0 = (long)blockIdx.x * kScanTile3 + threadIdx.x * kScan3Items;
+    for (int j = 0; j < kScan3Items; j++)
+      if (i0 + j < len) v += arr[k][i0 + j];
+    int tot;
+    block_exclusive_scan(v, sh, tot);
+    if (threadIdx.x == 0) tile_sums[k * (ntiles + 1) + blockIdx.x] = tot;
+  }
+}
+
+__global__ void __launch_bounds__(1024) k_scan3_sums(int *tile_sums, int ntiles) {
+  __shared__ int sh[32];
+  for (int k = 0; k < 3; k++) {
+    int *t = tile_sums + k * (ntiles + 1);
+    int run = 0;
+    for (int base = 0; base < ntiles; base += 1024) {
+      const int i = base + threadIdx.x;
+      const int v = i < ntiles ? t[i] : 0;
+      int tot;
+      const int ex = block_exclusive_scan(v, sh, tot);
+      if (i < ntiles) t[i] = run + ex;
+      run += tot;
     }
-    if (t == 1023) arr[k][len] = (int)s[k][1023];
+    if (threadIdx.x == 0) t[ntiles] = run;
+  }
+}
+
+__global__ void __launch_bounds__(kScan3Threads) k_scan3_apply(int *a, int *b, int *c, int len, const int *tile_sums,
+                                                               int ntiles) {
+  __shared__ int sh[32];
+  int *arr[3] = {a, b, c};
+  for (int k = 0; k < 3; k++) {
+    const long i0 = (long)blockIdx.x * kScanTile3 + threadIdx.x * kScan3Items;
+    int v[kScan3Items], sum = 0;
+    for (int j = 0; j < kScan3Items; j++) {
+      v[j] = i0 + j < len ? arr[k][i0 + j] : 0;
+      sum += v[j];
+    }
+    int tot;
+    int run = block_exclusive_scan(sum, sh, tot) + tile_sums[k * (ntiles + 1) + blockIdx.x];
+    for (int j = 0; j < kScan3Items; j++) {
+      if (i0 + j < len) arr[k][i0 + j] = run;
+      run += v[j];
+    }
+    if (blockIdx.x == ntiles - 1 && threadIdx.x == 0) arr[k][len] = tile_sums[k * (ntiles + 1) + ntiles];
   }
 }
 
@@ -559,48 +637,60 @@ __device__ __forceinline__ void far_field(const MixedView &m, int l, int B, floa
   }
 }
 
-// Direct (U list, regularised kernel) or correction (K list, Gaussian term
-// within rc) contributions of one source leaf to the lane's two targets.
-// Each leaf is summed in plain FP32 and then added with compensation, so
-// the compensated sum costs once per leaf, not once per pair.
+// 2^t on the SFU (PTX ex2.approx: relative error ~2^-22, FTZ).
+__device__ __forceinline__ float sfu_exp2(float t) {
+  float r;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(t));
+  return r;
+}
+
+// One pair: source (x, y, G, t) with t = -log2(e)/sigma^2, target (tx, ty).
+// r2 carries a 1e-30 floor, so a coincident pair has a finite factor and
+// contributes f * (0, 0) = 0, as the reference skips r <= 1e-10
+// (fmm.c:132); nothing else sees the floor (it is below FP32 resolution of
+// any r2 that matters).
+//   direct (U):     f = G (1 - exp(-r^2/s^2)) / r^2, with 1 - e^-x taken
+//                   from its series x (1 - x/2) below x = 1e-3, where the
+//                   subtraction would cancel;
+//   correction (K): f = -G exp(-r^2/s^2) / r^2 for every pair of the two
+//                   leaves (the list holds the leaves within rc; pairs beyond
+//                   rc add their tiny exact terms).
+template <bool kCorrection>
+__device__ __forceinline__ void pair(const float4 sj, float tx, float ty, float &sx, float &sy) {
+  const float rx = tx - sj.x, ry = ty - sj.y;
+  const float r2 = fmaf(rx, rx, fmaf(ry, ry, 1e-30f));
+  const float t = r2 * sj.w;
+  const float e = sfu_exp2(t);
+  float f;
+  if (!kCorrection) {
+    const float x2 = t * -0.69314718f;
+    const float e1f = t > -1.44269504e-3f ? x2 * fmaf(-0.5f, x2, 1.f) : 1.f - e;
+    f = __fdividef(sj.z * e1f, r2);
+  } else {
+    f = -__fdividef(sj.z * e, r2);
+  }
+  sx = fmaf(-f, ry, sx);
+  sy = fmaf(f, rx, sy);
+}
+
+// Direct (U list) or correction (K list) contributions of one source leaf
+// to the lane's two targets.  Each leaf is summed in plain FP32 and then
+// added with compensation, so the compensated sum costs once per leaf, not
+// once per pair.
 template <bool kCorrection>
 __device__ __forceinline__ void leaf_pairs(const float4 *__restrict__ src, int j0, int j1, float txa, float tya,
-                                           float txb, float tyb, bool two, float rc2, float &sxa, float &sya,
-                                           float &sxb, float &syb) {
-  for (int j = j0; j < j1; j++) {
-    const float4 sj = src[j];
-    {
-      const float rx = txa - sj.x, ry = tya - sj.y;
-      const float r2 = fmaf(rx, rx, ry * ry);
-      float f = 0.f;
-      if (!kCorrection) {
-        if (r2 > 1e-20f) {
-          const float x2 = r2 * sj.w;
-          const float e1f = x2 < 1e-3f ? x2 * (1.f - 0.5f * x2) : 1.f - __expf(-x2);
-          f = __fdividef(sj.z * e1f, r2);
-        }
-      } else if (r2 < rc2) {
-        f = -__fdividef(sj.z * __expf(-r2 * sj.w), r2);
-      }
-      sxa = fmaf(-f, ry, sxa);
-      sya = fmaf(f, rx, sya);
+                                           float txb, float tyb, bool two, float &sxa, float &sya, float &sxb,
+                                           float &syb) {
+  if (two) {
+#pragma unroll 2
+    for (int j = j0; j < j1; j++) {
+      const float4 sj = src[j];
+      pair<kCorrection>(sj, txa, tya, sxa, sya);
+      pair<kCorrection>(sj, txb, tyb, sxb, syb);
     }
-    if (two) {
-      const float rx = txb - sj.x, ry = tyb - sj.y;
-      const float r2 = fmaf(rx, rx, ry * ry);
-      float f = 0.f;
-      if (!kCorrection) {
-        if (r2 > 1e-20f) {
-          const float x2 = r2 * sj.w;
-          const float e1f = x2 < 1e-3f ? x2 * (1.f - 0.5f * x2) : 1.f - __expf(-x2);
-          f = __fdividef(sj.z * e1f, r2);
-        }
-      } else if (r2 < rc2) {
-        f = -__fdividef(sj.z * __expf(-r2 * sj.w), r2);
-      }
-      sxb = fmaf(-f, ry, sxb);
-      syb = fmaf(f, rx, syb);
-    }
+  } else {
+#pragma unroll 4
+    for (int j = j0; j < j1; j++) pair<kCorrection>(src[j], txa, tya, sxa, sya);
   }
 }
 
@@ -634,7 +724,6 @@ __global__ void __launch_bounds__(128, 8) k_eval_mixed(MixedView m, double *uv, 
   const int l = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   if (l >= m.nleaf) return;
   const int B = m.leaf_cell[l];
-  const float rc2 = (*m.rc_ptr) * (*m.rc_ptr);
   const double inv2pi = 0.15915494309189533577;
   unsigned long long pairs = 0;
   for (int t0 = m.begin[B]; t0 < m.end[B]; t0 += 64) {
@@ -671,9 +760,9 @@ __global__ void __launch_bounds__(128, 8) k_eval_mixed(MixedView m, double *uv, 
         const int j0 = m.begin[A], j1 = m.end[A];
         float sxa = 0.f, sya = 0.f, sxb = 0.f, syb = 0.f;
         if (pass == 0)
-          leaf_pairs<false>(m.src4, j0, j1, za.x + ox, za.y + oy, zb.x + ox, zb.y + oy, two, rc2, sxa, sya, sxb, syb);
+          leaf_pairs<false>(m.src4, j0, j1, za.x + ox, za.y + oy, zb.x + ox, zb.y + oy, two, sxa, sya, sxb, syb);
         else
-          leaf_pairs<true>(m.src4, j0, j1, za.x + ox, za.y + oy, zb.x + ox, zb.y + oy, two, rc2, sxa, sya, sxb, syb);
+          leaf_pairs<true>(m.src4, j0, j1, za.x + ox, za.y + oy, zb.x + ox, zb.y + oy, two, sxa, sya, sxb, syb);
         kahan(axa, cxa, sxa);
         kahan(aya, cya, sya);
         kahan(axb, cxb, sxb);
@@ -794,20 +883,23 @@ cudaError_t mixed_tables(int P, float *h_m2l, float *h_m2m, float *h_l2l) {
 }
 
 int mixed_lists(MixedView &m, cudaStream_t s) {
-  const int cb = (m.ncell + 255) / 256, lb = (m.nleaf + 255) / 256;
+  const int cb = (m.ncell + 255) / 256;
   k_cell_info<<<cb, 256, 0, s>>>(m);
   k_parent<<<cb, 256, 0, s>>>(m);
   k_colleagues<<<cb, 256, 0, s>>>(m);
   k_vx_lists<<<cb, 256, 0, s>>>(m);
-  k_list_count<<<lb, 256, 0, s>>>(m);
-  k_scan3<<<1, 1024, 0, s>>>(m.u_off, m.w_off, m.k_off, m.nleaf);
-  g_launches.fetch_add(6, std::memory_order_relaxed);
+  k_lists<false><<<(m.nleaf + kWalkWarps - 1) / kWalkWarps, 32 * kWalkWarps, 0, s>>>(m);
+  const int ntiles = max(1, (m.nleaf + kScanTile3 - 1) / kScanTile3);
+  k_scan3_tiles<<<ntiles, kScan3Threads, 0, s>>>(m.u_off, m.w_off, m.k_off, m.nleaf, m.scan_tmp, ntiles);
+  k_scan3_sums<<<1, 1024, 0, s>>>(m.scan_tmp, ntiles);
+  k_scan3_apply<<<ntiles, kScan3Threads, 0, s>>>(m.u_off, m.w_off, m.k_off, m.nleaf, m.scan_tmp, ntiles);
+  g_launches.fetch_add(8, std::memory_order_relaxed);
   T2D_CUDA_TRY(cudaGetLastError());
   return TREE2D_OK;
 }
 
 int mixed_fill_lists(MixedView &m, cudaStream_t s) {
-  k_list_fill<<<(m.nleaf + 255) / 256, 256, 0, s>>>(m);
+  k_lists<true><<<(m.nleaf + kWalkWarps - 1) / kWalkWarps, 32 * kWalkWarps, 0, s>>>(m);
   g_launches.fetch_add(1, std::memory_order_relaxed);
   T2D_CUDA_TRY(cudaGetLastError());
   return TREE2D_OK;
@@ -896,6 +988,7 @@ int mixed_solve(Workspace &ws, const Tree &t, const MixedParams &mp, double *d_u
   need += Arena::bytes_for((size_t)nc * 9, 4) * 2;
   need += Arena::bytes_for((size_t)nc * 27, 4) + Arena::bytes_for((size_t)nc * 8, 4);
   need += Arena::bytes_for((size_t)nl + 1, 4) * 3;
+  need += Arena::bytes_for(3 * ((size_t)nl / kScanTile3 + 2), 4);  // scan tile sums
   need += Arena::bytes_for((size_t)nc * 2 * P, 4) * 2;
   need += Arena::bytes_for((size_t)nc * 4, 4) + 1024;  // class lists + counts
   need += 256;
@@ -938,6 +1031,7 @@ int mixed_solve(Workspace &ws, const Tree &t, const MixedParams &mp, double *d_u
   m.u_off = ws.mx_arena.take<int>((size_t)nl + 1);
   m.w_off = ws.mx_arena.take<int>((size_t)nl + 1);
   m.k_off = ws.mx_arena.take<int>((size_t)nl + 1);
+  m.scan_tmp = ws.mx_arena.take<int>(3 * ((size_t)nl / kScanTile3 + 2));
   m.M = ws.mx_arena.take<float>((size_t)nc * 2 * P);
   m.L = ws.mx_arena.take<float>((size_t)nc * 2 * P);
   unsigned *rc_bits = ws.mx_arena.take<unsigned>(1);

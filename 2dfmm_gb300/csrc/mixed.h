@@ -33,6 +33,7 @@ struct MixedView {
   int *vlist;            // 27 per cell, slot order of the cell's class
   int *xlist;            // 8 per cell
   int *u_off, *w_off, *k_off;  // per leaf (+1)
+  int *scan_tmp;               // tile sums of the list-size scan
   int *u_idx, *w_idx, *k_idx;
   int *u_leaf, *k_leaf;  // leaf ordinal of each U / K entry
   float *M, *L;          // per cell, 2P floats (re[P], im[P])

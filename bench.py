@@ -54,7 +54,7 @@ def parse():
     ap.add_argument("--no-plain", action="store_true", help="skip timing the plain FP64 path beside")
     ap.add_argument("--workload", default="two_patch_sheet", choices=["two_patch_sheet", "lamb_oseen", "uniform"])
     ap.add_argument("--n", type=int, default=0, help="override the blob count (exploration only)")
-    ap.add_argument("--err-targets", type=int, default=4096)
+    ap.add_argument("--err-targets", type=int, default=65536)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-sample", type=int, default=0, help="targets per CPU step (0: auto)")
     return ap.parse_args()
@@ -77,6 +77,23 @@ def dist_env():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     return rank, world, local
+
+
+def max_over_ranks(x, world, device="cpu"):
+    """The largest of a per-rank time over all ranks (the job ends with the
+    slowest replica); identity on one rank."""
+    if world <= 1:
+        return float(x)
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(n_per_rank, steps, total_ms, world):
+    """Whole-job targets/s of `world` replicas that each solve `steps` sets of
+    `n_per_rank` blobs (every blob a target) in at most `total_ms`."""
+    return world * n_per_rank * steps / (total_ms * 1e-3)
 
 
 # --------------------------------------------------------------------------
@@ -253,10 +270,11 @@ def _time_mode(P, torch, args, mode, arrays, stream, flush, clk=None):
     return times, sts
 
 
-def _judge(P, torch, arrays, n, ntgt, sp):
-    """relL2 and max relative error of the last solve against the FP64 direct
-    sum on `ntgt` seeded sampled targets."""
-    xy, cir, cor, uv, _ = arrays
+def _direct_reference(P, torch, arrays, n, ntgt, sp):
+    """FP64 direct sum (the judge) at `ntgt` seeded targets sampled without
+    replacement from the blobs; computed once per run and reused for every
+    form judged."""
+    xy, cir, cor, _, _ = arrays
     W = importlib.import_module("2dfmm_gb300.workloads")
     idx = W.sample_targets(n, ntgt, seed=7)
     tidx = torch.from_numpy(idx).to(xy.device)
@@ -264,10 +282,17 @@ def _judge(P, torch, arrays, n, ntgt, sp):
     ref = torch.empty_like(txy)
     P.direct_device(txy.data_ptr(), len(idx), xy.data_ptr(), cir.data_ptr(), cor.data_ptr(), n, ref.data_ptr(), sp)
     torch.cuda.synchronize()
+    return tidx, ref
+
+
+def _judge(uv, judge):
+    """relL2 and max relative error of the last solve's velocities against
+    the FP64 direct sum."""
+    tidx, ref = judge
     got = uv[tidx]
-    rel_l2 = float(torch.linalg.norm(got - ref) / torch.linalg.norm(ref))
+    rel_l2 = float((got - ref).norm() / ref.norm())
     max_rel = float(((got - ref).norm(dim=1) / ref.norm(dim=1).clamp_min(1e-300)).max())
-    return {"relL2_vs_fp64_direct": rel_l2, "max_rel_vs_fp64_direct": max_rel, "targets": len(idx)}
+    return {"relL2_vs_fp64_direct": rel_l2, "max_rel_vs_fp64_direct": max_rel, "targets": int(len(tidx))}
 
 
 def _roofline(P, args, mode, b, wname, sts, sp):
@@ -333,13 +358,10 @@ def run_ours(args):
     with Clocks(local) as clk:
         times, sts = _time_mode(P, torch, args, args.mode, arrays, stream, flush)
     clocks = clk.summary()
-    total_ms = float(sum(times))
-    if world > 1:
-        t = torch.tensor([total_ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
-    value = world * n * args.steps / (total_ms * 1e-3)
-    accuracy = _judge(P, torch, arrays, n, args.err_targets, sp)
+    total_ms = max_over_ranks(float(sum(times)), world, dev)
+    value = replica_throughput(n, args.steps, total_ms, world)
+    judge = _direct_reference(P, torch, arrays, n, args.err_targets, sp)
+    accuracy = _judge(uv, judge)
     roofline = _roofline(P, args, args.mode, b, wname, sts, sp)
 
     # the fixed mixed form and the plain FP64 path on the same set, timed the
@@ -351,7 +373,7 @@ def run_ours(args):
     for other in others:
         otimes, _ = _time_mode(P, torch, args, other, arrays, stream, flush)
         o = {"value": n / (statistics.mean(otimes) * 1e-3), "unit": UNIT, "ms_per_step": statistics.mean(otimes),
-             "accuracy": _judge(P, torch, arrays, n, args.err_targets, sp)}
+             "accuracy": _judge(uv, judge)}
         o["speedup_of_headline"] = value / world / o["value"]
         beside["plain_fp64" if other == "plain" else "mixed_fixed"] = o
     P.set_mode(MODES[args.mode])
@@ -364,22 +386,22 @@ def run_ours(args):
     h_xy.numpy()[:] = b.xy
     h_cir.numpy()[:] = b.cir
     h_cor.numpy()[:] = b.cor
+    h_uv = torch.empty((n, 2), dtype=torch.float64, pin_memory=True)
     P.solve_device(xy.data_ptr(), cir.data_ptr(), cor.data_ptr(), uv.data_ptr(), n, sp)
     torch.cuda.synchronize()
     e2e_times = []
     e2e_steps = max(1, min(args.steps, 3))
+    e2e_split = []
     for k in range(1 + e2e_steps):
         t0 = time.perf_counter()
         P.make_tree(h_xy.numpy(), h_cir.numpy(), h_cor.numpy())
-        out = P.biot_tree_batch(h_xy.numpy())
+        t1 = time.perf_counter()
+        out = P.biot_tree_batch(h_xy.numpy(), out=h_uv.numpy())
         dt = time.perf_counter() - t0
         if k >= 1:
             e2e_times.append(dt)
-    e2e_t = statistics.mean(e2e_times)
-    if world > 1:
-        t = torch.tensor([e2e_t], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_t = float(t.item())
+            e2e_split.append((1e3 * (t1 - t0), 1e3 * (t0 + dt - t1)))
+    e2e_t = max_over_ranks(statistics.mean(e2e_times), world, dev)
     e2e_match = bool(np.array_equal(out, uv.cpu().numpy()))
 
     cpu = None
@@ -408,6 +430,8 @@ def run_ours(args):
             "gpu_launches": int(sum(s["n_launches"] for s in sts)),
             "e2e": {"value": world * n / e2e_t, "unit": UNIT, "h2d_bytes_per_step": n * 32,
                     "d2h_bytes_per_step": n * 16, "api": "make_tree + biot_tree_batch (host buffers)",
+                    "make_tree_ms": statistics.mean(a for a, _ in e2e_split),
+                    "biot_tree_batch_ms": statistics.mean(b_ for _, b_ in e2e_split),
                     "matches_device_path": e2e_match},
             "roofline": roofline,
             "accuracy": accuracy,

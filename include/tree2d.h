@@ -161,6 +161,13 @@ int tree2d_direct_device(int ntgt, const double *d_txy, int nsrc, const double *
 int tree2d_fp64_probe(int blocks, int iters, void *stream, double *ms);
 /* The same for bits = 64 (DFMA) or 32 (FFMA). */
 int tree2d_pipe_probe(int bits, int blocks, int iters, void *stream, double *ms);
+/* Failure-detection check of the bounded device waits: one kernel waits on
+ * a shared-memory barrier that nothing completes, giving up after `polls`
+ * polls exactly as the tensor-core kernels' waits do, and *status receives
+ * TREE2D_ERR_TIMEOUT (what those kernels record when a wait gives up).
+ * Returns TREE2D_OK when the probe itself ran.  No counterpart in the
+ * reference. */
+int tree2d_wait_probe(long long polls, int *status);
 
 /* ------------------------------------------------------------------ */
 /* Learned order selection (TREE2D_MODE_LEARNED).  A small network

@@ -95,3 +95,44 @@ def test_device_solve_equals_make_tree(gpu_lib):
     assert np.array_equal(uv.cpu().numpy(), uv_host[:n])
     st = P.stats()
     assert st["n_blobs"] == n and st["n_m2s"] > 0 and st["n_pairs"] > 0
+
+
+@pytest.mark.gpu
+def test_batch_lookup_many_chunks(gpu_lib):
+    """biot_tree_batch over more points than one lookup chunk (65,536), in
+    shuffled order with off-blob points interleaved: every blob answer equals
+    the device solve's value for that blob, every off-blob answer equals a
+    single biot_tree call at that point, and a page-locked `out` buffer
+    receives the same values."""
+    torch = pytest.importorskip("torch")
+    P = gpu_lib
+    import importlib
+    W = importlib.import_module("2dfmm_gb300.workloads")
+    b = W.uniform(200_000, seed=11)
+    P.set_params(b.nterms, b.num_p, b.theta)
+    P.set_mode(P.MODE_PLAIN)
+    P.make_tree(b.xy, b.cir, b.cor)
+    rng = np.random.default_rng(5)
+    perm = rng.permutation(b.n)
+    off = rng.random((3000, 2)) * 0.9 + 0.05
+    q = np.concatenate([b.xy[perm], off])
+    order = rng.permutation(len(q))
+    q = q[order]
+    uv = P.biot_tree_batch(q)
+    dev = torch.device("cuda:0")
+    d_xy = torch.from_numpy(b.xy).to(dev).contiguous()
+    d_cir = torch.from_numpy(b.cir).to(dev)
+    d_cor = torch.from_numpy(b.cor).to(dev)
+    d_uv = torch.empty_like(d_xy)
+    P.solve_device(d_xy.data_ptr(), d_cir.data_ptr(), d_cor.data_ptr(), d_uv.data_ptr(), b.n)
+    torch.cuda.synchronize()
+    full = np.concatenate([d_uv.cpu().numpy()[perm], np.full((len(off), 2), np.nan)])[order]
+    hit = order < b.n
+    assert np.array_equal(uv[hit], full[hit])
+    miss_idx = np.flatnonzero(~hit)
+    for i in miss_idx[:: max(1, len(miss_idx) // 40)]:
+        u, v = P.biot_tree(*q[i])
+        assert u == uv[i, 0] and v == uv[i, 1]
+    out = torch.empty((len(q), 2), dtype=torch.float64, pin_memory=True).numpy()
+    uv2 = P.biot_tree_batch(q, out=out)
+    assert uv2 is out and np.array_equal(out, uv)
