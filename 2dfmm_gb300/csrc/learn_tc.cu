@@ -47,17 +47,26 @@ __device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
   return *reinterpret_cast<const uint32_t *>(&h);
 }
 
-// GELU (tanh form) of two values, packed to BF16 for the next layer's
-// input: the tanh runs on the SFU in BF16x2 (one instruction for both
-// values; its ~2^-8 error is the order of the BF16 rounding of the result),
-// the rest in FP32.
+// GELU (tanh form) of two values, returned as the BF16 pair of the next
+// layer's input.  The pre-activations are rounded to BF16 and the whole
+// GELU runs in packed BF16x2 arithmetic (FMA pipe) with the tanh on the SFU
+// (one instruction for both values): the result is stored in BF16 anyway,
+// and every step rounds at that same 2^-9 relative level.
+//   u = z (c0 + c1 z^2),  c0 = sqrt(2/pi), c1 = 0.044715 sqrt(2/pi)
+//   g = h + h tanh(u),    h = z / 2
 __device__ __forceinline__ uint32_t gelu2_bf16(float z0, float z1) {
-  const float u0 = 0.7978845608028654f * fmaf(0.044715f * z0, z0 * z0, z0);
-  const float u1 = 0.7978845608028654f * fmaf(0.044715f * z1, z1 * z1, z1);
-  uint32_t t;
-  asm("tanh.approx.bf16x2 %0, %1;" : "=r"(t) : "r"(pack_bf16(u0, u1)));
-  const float t0 = __uint_as_float(t << 16), t1 = __uint_as_float(t & 0xffff0000u);
-  return pack_bf16(0.5f * z0 * (1.f + t0), 0.5f * z1 * (1.f + t1));
+  const uint32_t z = pack_bf16(z0, z1);
+  const uint32_t c0 = 0x3F4C3F4Cu;  // 0.797... in both halves (BF16 0x3F4C)
+  const uint32_t c1 = 0x3D123D12u;  // 0.0357 in both halves (BF16 0x3D12)
+  const uint32_t half = 0x3F003F00u;  // 0.5
+  uint32_t z2, p, u, t, h, g;
+  asm("mul.rn.bf16x2 %0, %1, %1;" : "=r"(z2) : "r"(z));
+  asm("fma.rn.bf16x2 %0, %1, %2, %3;" : "=r"(p) : "r"(z2), "r"(c1), "r"(c0));
+  asm("mul.rn.bf16x2 %0, %1, %2;" : "=r"(u) : "r"(z), "r"(p));
+  asm("tanh.approx.bf16x2 %0, %1;" : "=r"(t) : "r"(u));
+  asm("mul.rn.bf16x2 %0, %1, %2;" : "=r"(h) : "r"(z), "r"(half));
+  asm("fma.rn.bf16x2 %0, %1, %2, %1;" : "=r"(g) : "r"(h), "r"(t));
+  return g;
 }
 
 // Row r of the activation tile, K = 8*nk elements: element k at

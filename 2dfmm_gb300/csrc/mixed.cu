@@ -149,9 +149,10 @@ __global__ void k_leaf_setup(MixedView m, const double *x, const double *y, cons
     m.leaf_of[i] = c;
     m.loc[i] = make_float2((float)(x[i] - cx), (float)(y[i] - cy));
     m.gam[i] = (float)cir[i];
-    double s = cor[i];
-    m.s2inv[i] = (float)(1.0 / (s * s));
-    m.src4[i] = make_float4(m.loc[i].x, m.loc[i].y, m.gam[i], (float)(-1.4426950408889634 / (s * s)));
+    const double s = cor[i];
+    const double w = 1.0 / (s * s);
+    m.s2inv[i] = (float)w;
+    m.src4[i] = make_float4(m.loc[i].x, m.loc[i].y, m.gam[i], (float)(-1.4426950408889634 * w));
   }
 }
 
