@@ -31,7 +31,7 @@ MODE_PLAIN, MODE_MIXED, MODE_LEARNED = 0, 1, 2
 EXPORTS = [
     "make_tree", "biot_tree", "tree2d_last_error", "tree2d_error_string", "tree2d_set_params",
     "tree2d_clear_params", "tree2d_get_params", "tree2d_set_mode", "tree2d_get_mode", "tree2d_set_mixed_params", "biot_tree_batch",
-    "tree2d_solve_device", "tree2d_solve_device_static", "tree2d_get_stats", "tree2d_export_tree", "tree2d_direct_device", "tree2d_fp64_probe", "tree2d_pipe_probe", "tree2d_wait_probe", "tree2d_version",
+    "tree2d_solve_device", "tree2d_solve_device_static", "tree2d_solve_sets", "tree2d_set_tuning", "tree2d_get_stats", "tree2d_export_tree", "tree2d_direct_device", "tree2d_fp64_probe", "tree2d_pipe_probe", "tree2d_wait_probe", "tree2d_version",
     "tree2d_learn_param_count", "tree2d_learn_set_weights", "tree2d_learn_get_weights", "tree2d_learn_set_options",
     "tree2d_learn_collect", "tree2d_learn_train", "tree2d_mlp_grad", "tree2d_mlp_forward",
     "tree2d_set_mirror", "tree2d_advect_device",
@@ -50,7 +50,7 @@ class Stats(ctypes.Structure):
         ("depth", ctypes.c_int), ("mode", ctypes.c_int), ("n_m2s", ctypes.c_longlong),
         ("n_pairs", ctypes.c_longlong), ("n_m2l", ctypes.c_longlong), ("ms_build", ctypes.c_double),
         ("ms_upward", ctypes.c_double), ("ms_eval", ctypes.c_double), ("ms_total", ctypes.c_double),
-        ("n_launches", ctypes.c_longlong), ("m2l_path", ctypes.c_int),
+        ("n_launches", ctypes.c_longlong), ("m2l_path", ctypes.c_int), ("eval_variant", ctypes.c_int),
     ]
 
     def as_dict(self):
@@ -112,6 +112,11 @@ def load(path: str | None = None):
     L.tree2d_fp64_probe.restype = ctypes.c_int
     L.tree2d_pipe_probe.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p, _dp]
     L.tree2d_pipe_probe.restype = ctypes.c_int
+    L.tree2d_set_tuning.argtypes = [ctypes.c_int, ctypes.c_int]
+    L.tree2d_set_tuning.restype = ctypes.c_int
+    L.tree2d_solve_sets.argtypes = [ctypes.c_int, _ip, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                    ctypes.c_void_p, ctypes.c_void_p]
+    L.tree2d_solve_sets.restype = ctypes.c_int
     L.tree2d_wait_probe.argtypes = [ctypes.c_longlong, _ip]
     L.tree2d_wait_probe.restype = ctypes.c_int
     L.tree2d_version.restype = ctypes.c_char_p
@@ -229,6 +234,20 @@ def biot_tree_batch(xy, check: bool = True, out=None):
 def solve_device(d_xy: int, d_cir: int, d_cor: int, d_uv: int, n: int, stream: int = 0):
     """Device-resident solve over raw device pointers (ints)."""
     _check(load().tree2d_solve_device(n, d_xy, d_cir, d_cor, d_uv, stream or None), "solve_device")
+
+
+def set_tuning(autotune: bool = True, eval_variant: int = -1):
+    """Near-field kernel tuning (bit-identical variants): autotune on the
+    first solve of each size class, or force a variant 0..3."""
+    _check(load().tree2d_set_tuning(int(autotune), eval_variant), "set_tuning")
+
+
+def solve_sets(d_xy: int, d_cir: int, d_cor: int, d_uv: int, offsets, stream: int = 0):
+    """Batched mixed solve of independent sets in one tree (device pointers;
+    `offsets` = nsets + 1 blob offsets, host)."""
+    off = np.ascontiguousarray(offsets, dtype=np.int32)
+    _check(load().tree2d_solve_sets(len(off) - 1, off.ctypes.data_as(_ip), d_xy, d_cir, d_cor, d_uv,
+                                    stream or None), "solve_sets")
 
 
 def solve_device_static(d_xy: int, d_cir: int, d_cor: int, d_uv: int, n: int, stream: int = 0) -> int:

@@ -112,6 +112,7 @@ void parallel_chunks(long n, long grain, F f) {
 
 struct Solver {
   Workspace ws;
+  Arena sets;     // device copy of the set offsets of a batched solve
   Tree tree;
   Arena mirror;   // blobs + images when a mirror wall is set
   bool plain_coef = false;  // FP64 coefficients present (plain upward ran)
@@ -213,7 +214,7 @@ float elapsed(cudaEvent_t a, cudaEvent_t b) {
 }
 
 int solve_body(Lib &L, Solver &S, int n, const double *d_xy, const double *d_cir, const double *d_cor,
-               double *d_uv, cudaStream_t s, tree2d_stats_t &st);
+               double *d_uv, cudaStream_t s, tree2d_stats_t &st, const int *d_set_off = nullptr, int nsets = 1);
 
 // Whole pipeline over n device-resident blobs; uv (interleaved, original
 // order) on the device.  With a mirror wall the images are appended as
@@ -237,7 +238,7 @@ int solve(Lib &L, Solver &S, int n, const double *d_xy, const double *d_cir, con
 }
 
 int solve_body(Lib &L, Solver &S, int n, const double *d_xy, const double *d_cir, const double *d_cor,
-               double *d_uv, cudaStream_t s, tree2d_stats_t &st) {
+               double *d_uv, cudaStream_t s, tree2d_stats_t &st, const int *d_set_off, int nsets) {
   T2D_CUDA_TRY(workspace_init(S.ws));
   std::memset(&st, 0, sizeof(st));
   st.n_blobs = n;
@@ -249,7 +250,7 @@ int solve_body(Lib &L, Solver &S, int n, const double *d_xy, const double *d_cir
   Workspace &ws = S.ws;
   const long long launches0 = g_launches.load();
   T2D_CUDA_TRY(cudaEventRecord(ws.ev[0], s));
-  int rc = build_tree(ws, n, d_xy, d_cir, d_cor, L.params, S.tree, s);
+  int rc = build_tree(ws, n, d_xy, d_cir, d_cor, L.params, S.tree, s, d_set_off, nsets);
   if (rc) return rc;
   T2D_CUDA_TRY(cudaEventRecord(ws.ev[1], s));
   S.plain_coef = false;
@@ -656,6 +657,15 @@ int tree2d_set_mode(int mode) {
 
 int tree2d_get_mode(void) { return lib().mode; }
 
+int tree2d_set_tuning(int autotune, int eval_variant) {
+  Lib &L = lib();
+  std::lock_guard<std::mutex> lk(L.mu);
+  if (eval_variant < -1 || eval_variant > 3) return fail(TREE2D_ERR_BAD_PARAMS);
+  L.mixed.autotune = autotune ? 1 : 0;
+  L.mixed.eval_variant = eval_variant;
+  return TREE2D_OK;
+}
+
 int tree2d_set_mixed_params(int pterms, double cutoff_sigmas, int use_tensor_cores) {
   Lib &L = lib();
   std::lock_guard<std::mutex> lk(L.mu);
@@ -678,6 +688,45 @@ int tree2d_solve_device(int n, const double *d_xy, const double *d_cir, const do
   if (rc) return fail(rc);
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   rc = solve(L, L.dev, n, d_xy, d_cir, d_cor, d_uv, s, L.dev_stats);
+  L.last_was_dev = true;
+  if (rc) return fail(rc);
+  return TREE2D_OK;
+}
+
+int tree2d_solve_sets(int nsets, const int *set_offsets, const double *d_xy, const double *d_cir,
+                      const double *d_cor, double *d_uv, void *stream) {
+  Lib &L = lib();
+  std::lock_guard<std::mutex> lk(L.mu);
+  int rc = resolve_params(L);
+  if (rc) return fail(rc);
+  if (nsets < 1 || !set_offsets || set_offsets[0] != 0) return fail(TREE2D_ERR_BAD_INPUT);
+  for (int k = 0; k < nsets; k++)
+    if (set_offsets[k + 1] < set_offsets[k]) return fail(TREE2D_ERR_BAD_INPUT);
+  const int n = set_offsets[nsets];
+  if (n > 0 && (!d_xy || !d_cir || !d_cor || !d_uv)) return fail(TREE2D_ERR_BAD_INPUT);
+  // one tree over all sets: the mixed form only (the plain treecode's
+  // traversal starts at the tree root), and no mirror wall
+  if (L.mode == TREE2D_MODE_PLAIN || L.mirror_on) return fail(TREE2D_ERR_MODE);
+  rc = ensure_stream(L);
+  if (rc) return fail(rc);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  Solver &S = L.dev;
+  const int *d_off = nullptr;
+  if (nsets > 1) {
+    cudaError_t e = S.sets.reserve(Arena::bytes_for((size_t)nsets + 1, 4));
+    int *d = nullptr;
+    if (e == cudaSuccess) {
+      S.sets.reset();
+      d = S.sets.take<int>((size_t)nsets + 1);
+      e = cudaMemcpyAsync(d, set_offsets, sizeof(int) * ((size_t)nsets + 1), cudaMemcpyHostToDevice, s);
+    }
+    if (e != cudaSuccess) {
+      note_cuda_error(e, "solve_sets offsets");
+      return fail(TREE2D_ERR_CUDA);
+    }
+    d_off = d;
+  }
+  rc = solve_body(L, S, n, d_xy, d_cir, d_cor, d_uv, s, L.dev_stats, d_off, nsets);
   L.last_was_dev = true;
   if (rc) return fail(rc);
   return TREE2D_OK;

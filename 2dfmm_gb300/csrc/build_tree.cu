@@ -83,6 +83,21 @@ __global__ void __launch_bounds__(256) k_bbox(const double *__restrict__ xy, con
   }
 }
 
+// Root box of a blob set from its coordinate extremes (quadtree.c:87-98).
+__device__ __forceinline__ RootBox root_from_box(const Box4 &r) {
+  const double rx = __dadd_rn(fabs(__dsub_rn(r.x, r.y)), 0.0001);
+  const double ry = __dadd_rn(fabs(__dsub_rn(r.z, r.w)), 0.0001);
+  RootBox b;
+  b.region = rx > ry ? rx : ry;
+  b.cx = __dmul_rn(0.5, __dadd_rn(r.x, r.y));
+  b.cy = __dmul_rn(0.5, __dadd_rn(r.z, r.w));
+  b.xmax = r.x;
+  b.xmin = r.y;
+  b.ymax = r.z;
+  b.ymin = r.w;
+  return b;
+}
+
 // One warp: the lanes reduce strided parts, then a shuffle reduction.
 __global__ void k_root(const Box4 *part, int nparts, RootBox *root) {
   if (blockIdx.x != 0) return;
@@ -101,18 +116,47 @@ __global__ void k_root(const Box4 *part, int nparts, RootBox *root) {
   r.z = warp_max(r.z);
   r.w = warp_min(r.w);
   if (lane != 0) return;
-  // quadtree.c:87-98
-  double rx = __dadd_rn(fabs(__dsub_rn(r.x, r.y)), 0.0001);
-  double ry = __dadd_rn(fabs(__dsub_rn(r.z, r.w)), 0.0001);
-  RootBox b;
-  b.region = rx > ry ? rx : ry;
-  b.cx = __dmul_rn(0.5, __dadd_rn(r.x, r.y));
-  b.cy = __dmul_rn(0.5, __dadd_rn(r.z, r.w));
-  b.xmax = r.x;
-  b.xmin = r.y;
-  b.ymax = r.z;
-  b.ymin = r.w;
-  *root = b;
+  *root = root_from_box(r);
+}
+
+// Batched sets: one block per set reduces its blob range [off[s], off[s+1])
+// to the set's root box (the same formulas as a single set's), checks the
+// inputs, and writes the set id of each of its blobs.
+__global__ void __launch_bounds__(256) k_bbox_sets(const double *__restrict__ xy, const double *__restrict__ cir,
+                                                   const double *__restrict__ cor, const int *__restrict__ off,
+                                                   RootBox *roots, int *set_of, DevStatus *st) {
+  const int set = blockIdx.x;
+  const int b = off[set], e = off[set + 1];
+  double xmax = -INFINITY, xmin = INFINITY, ymax = -INFINITY, ymin = INFINITY;
+  bool bad = false;
+  for (int i = b + threadIdx.x; i < e; i += blockDim.x) {
+    const double x = xy[2 * (long)i], y = xy[2 * (long)i + 1];
+    const double c = cir[i], r = cor[i];
+    bad |= !(isfinite(x) && isfinite(y) && isfinite(c)) || isnan(r);
+    xmax = fmax(xmax, x);
+    xmin = fmin(xmin, x);
+    ymax = fmax(ymax, y);
+    ymin = fmin(ymin, y);
+    set_of[i] = set;
+  }
+  __shared__ Box4 sh[8];
+  xmax = warp_max(xmax);
+  xmin = warp_min(xmin);
+  ymax = warp_max(ymax);
+  ymin = warp_min(ymin);
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (lane == 0) sh[w] = Box4{xmax, xmin, ymax, ymin};
+  if (__syncthreads_or(bad) && threadIdx.x == 0) set_err(st, TREE2D_ERR_BAD_INPUT);
+  if (threadIdx.x == 0) {
+    Box4 r = sh[0];
+    for (int k = 1; k < (int)(blockDim.x >> 5); k++) {
+      r.x = fmax(r.x, sh[k].x);
+      r.y = fmin(r.y, sh[k].y);
+      r.z = fmax(r.z, sh[k].z);
+      r.w = fmin(r.w, sh[k].w);
+    }
+    roots[set] = root_from_box(r);
+  }
 }
 
 // One level of the reference's descent: digit of (x,y) against the centre,
@@ -152,6 +196,8 @@ inline size_t centre_entries(int lt) { return ((size_t)1 << lt) - 1; }
 __global__ void __launch_bounds__(256) k_centre_table(const RootBox *__restrict__ root, uint64_t *__restrict__ tab,
                                                       int lt) {
   const int per = (1 << lt) - 1;
+  root += blockIdx.y;  // batched sets: one table per set root
+  tab += (size_t)blockIdx.y * 2 * per;
   const int g = blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= 2 * per) return;
   const int axis = g >= per;
@@ -175,12 +221,32 @@ __global__ void __launch_bounds__(256) k_centre_table(const RootBox *__restrict_
 // With a centre table of `tlev` levels the first digits are integer
 // compares against it; the rest continue the FP64 descent from the centre
 // of the level-tlev cell.
+// Batched sets (`set_of` non-null): the digits are those of the blob's own
+// set root, preceded by `lev0` digits that place the set's root in tile
+// (2a, 2b) of a 2^lev0 x 2^lev0 grid (set = b * 2^(lev0-1) + a): the set
+// roots become the level-lev0 cells of one tree, and the empty tiles
+// between them keep every set's cells from touching another set's.
+__device__ __forceinline__ uint64_t set_prefix(int set, int lev0) {
+  const unsigned w = 1u << (lev0 - 1);
+  const unsigned tx = 2u * ((unsigned)set % w), ty = 2u * ((unsigned)set / w);
+  uint64_t p = 0;
+  for (int j = lev0 - 1; j >= 0; j--) p = (p << 2) | ((tx >> j) & 1u) | (((ty >> j) & 1u) << 1);
+  return p;
+}
+
 __global__ void __launch_bounds__(256) k_keys(const double *__restrict__ xy, int n, const RootBox *__restrict__ root,
                                               const uint64_t *__restrict__ tab, int tlev, uint64_t *__restrict__ keys,
-                                              uint32_t *__restrict__ vals, int levels) {
+                                              uint32_t *__restrict__ vals, int levels, const int *__restrict__ set_of,
+                                              int lev0) {
   long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (i >= n) return;
   double x = xy[2 * i], y = xy[2 * i + 1];
+  int set = 0;
+  if (set_of) {
+    set = set_of[i];
+    root += set;
+    if (tab) tab += (size_t)set * 2 * ((1 << tlev) - 1);
+  }
   double cx = root->cx, cy = root->cy, R = root->region;
   uint64_t key = 0;
   int l = 0;
@@ -211,7 +277,12 @@ __global__ void __launch_bounds__(256) k_keys(const double *__restrict__ xy, int
   }
 #pragma unroll 4
   for (; l < levels; l++) key = (key << 2) | descend(x, y, cx, cy, R);
-  keys[i] = levels < kKeyLevels ? key << (64 - 2 * levels) : key;
+  int total = levels;
+  if (set_of) {
+    key |= set_prefix(set, lev0) << (2 * levels);
+    total += lev0;
+  }
+  keys[i] = total < kKeyLevels ? key << (64 - 2 * total) : key;
   vals[i] = (uint32_t)i;
 }
 
@@ -227,8 +298,11 @@ __global__ void __launch_bounds__(256) k_cpl(const uint64_t *__restrict__ keys, 
 // (H = num_p-1) and the log-step doubling ping-pongs between them:
 // after the step of width k, buf[t] = max(w[t .. t+k-1]).
 constexpr int kLLTile = 2048;
+// `lev0` > 0 (batched sets): the container cells above the set roots and
+// the set roots themselves are always split, as a single set's root is.
 __global__ void __launch_bounds__(256) k_leaf_level(const uint8_t *__restrict__ w, int n, int num_p,
-                                                    uint8_t *__restrict__ leaf_level, DevStatus *st, int levels) {
+                                                    uint8_t *__restrict__ leaf_level, DevStatus *st, int levels,
+                                                    int lev0) {
   extern __shared__ uint8_t sbuf[];
   const int H = num_p - 1;
   const long tile0 = (long)blockIdx.x * kLLTile;
@@ -262,6 +336,7 @@ __global__ void __launch_bounds__(256) k_leaf_level(const uint8_t *__restrict__ 
     uint8_t a = cur[t];
     uint8_t b = cur[t + W - K];
     int s = a > b ? a : b;
+    s = s > lev0 ? s : lev0;
     if (s >= levels) {
       // a cell at the deepest key level still holds >= num_p blobs
       if (levels < kKeyLevels)
@@ -349,8 +424,9 @@ struct EmitArgs {
   unsigned char *leaf;
   double *cx, *cy, *region;
   int *leaf_cell;
-  const uint64_t *tab;  // centre table of `tlev` levels (k_centre_table)
+  const uint64_t *tab;  // centre table(s) of `tlev` levels (k_centre_table), one per set
   int tlev;
+  int lev0;             // batched sets: levels above the set roots (0 = one set)
 };
 
 // x (even) or y (odd) bits of the top 2*l key bits, compacted: the column
@@ -366,16 +442,38 @@ __device__ __forceinline__ unsigned key_axis(uint64_t key, int l, int axis) {
   return (unsigned)v;
 }
 
+// Set of a key in a batched tree: its first lev0 digits name tile
+// (2a, 2b), set = b * 2^(lev0-1) + a (the layout k_keys writes).
+__device__ __forceinline__ int set_of_key(uint64_t key, int lev0) {
+  const unsigned tx = key_axis(key, lev0, 0), ty = key_axis(key, lev0, 1);
+  return (int)((ty >> 1) * (1u << (lev0 - 1)) + (tx >> 1));
+}
+
 // Centre and side of the level-`lev` cell holding `key`, bit-identical to
 // the reference's descent: read from the centre table up to its last level,
-// then continued in FP64 (c +- 0.25 R per level).
-__device__ __forceinline__ void cell_geometry(const EmitArgs &a, uint64_t key, int lev, double R0, double &cx,
-                                              double &cy, double &R) {
+// then continued in FP64 (c +- 0.25 R per level).  In a batched tree the
+// geometry is that of the key's own set (the container cells above the set
+// roots have none: zero).
+__device__ __forceinline__ void cell_geometry(const EmitArgs &a, uint64_t key, int lev, double &cx, double &cy,
+                                              double &R) {
+  const uint64_t *tab = a.tab;
+  const RootBox *root = a.root;
+  if (a.lev0 > 0) {
+    if (lev < a.lev0) {
+      cx = cy = R = 0.0;
+      return;
+    }
+    const int set = set_of_key(key, a.lev0);
+    root += set;
+    tab += (size_t)set * 2 * ((1 << a.tlev) - 1);
+    key <<= 2 * a.lev0;
+    lev -= a.lev0;
+  }
   const int l0 = min(lev, a.tlev - 1);
   const int off = (1 << l0) - 1, ybase = (1 << a.tlev) - 1;
-  cx = okey_inv(a.tab[off + key_axis(key, l0, 0)]);
-  cy = okey_inv(a.tab[ybase + off + key_axis(key, l0, 1)]);
-  R = R0;
+  cx = okey_inv(tab[off + key_axis(key, l0, 0)]);
+  cy = okey_inv(tab[ybase + off + key_axis(key, l0, 1)]);
+  R = root->region;
   for (int j = 0; j < l0; j++) R = __dmul_rn(0.5, R);  // exact: R0 * 2^-l0
   for (int l = l0 + 1; l <= lev; l++) {
     const unsigned q = (unsigned)(key >> (64 - 2 * l)) & 3u;
@@ -422,7 +520,7 @@ __global__ void __launch_bounds__(kScanThreads) k_emit_cells(EmitArgs a) {
       uint64_t key = a.keys[i];
       for (int lev = prev + 1; lev <= lam; lev++) {
         double cx, cy, R;
-        cell_geometry(a, key, lev, R0, cx, cy, R);
+        cell_geometry(a, key, lev, cx, cy, R);
         {
           unsigned id = cell0 + (unsigned)(lev - prev - 1);
           a.level[id] = lev;
@@ -441,9 +539,9 @@ __global__ void __launch_bounds__(kScanThreads) k_emit_cells(EmitArgs a) {
     a.level[0] = 0;
     a.begin[0] = 0;
     a.leaf[0] = 0;
-    a.cx[0] = cx0;
-    a.cy[0] = cy0;
-    a.region[0] = R0;
+    a.cx[0] = a.lev0 ? 0.0 : cx0;  // a batched tree's root is a container
+    a.cy[0] = a.lev0 ? 0.0 : cy0;
+    a.region[0] = a.lev0 ? 0.0 : R0;
   }
 }
 
@@ -515,9 +613,10 @@ __global__ void __launch_bounds__(256) k_leaf_order(const uint32_t *__restrict__
   }
 }
 
+// Blob arrays in tree order, plus 1/sigma^2 for the direct pairs.
 __global__ void __launch_bounds__(256) k_gather(const double *__restrict__ xy, const double *__restrict__ cir,
                                                 const double *__restrict__ cor, const int *__restrict__ perm, int n,
-                                                double *x, double *y, double *c, double *r) {
+                                                double *x, double *y, double *c, double *r, double *icor2) {
   long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (i >= n) return;
   int p = perm[i];
@@ -525,35 +624,48 @@ __global__ void __launch_bounds__(256) k_gather(const double *__restrict__ xy, c
   y[i] = xy[2 * (long)p + 1];
   c[i] = cir[p];
   r[i] = cor[p];
+  icor2[i] = 1.0 / (cor[p] * cor[p]);
 }
 
 }  // namespace
 
 int build_tree(Workspace &ws, int n, const double *d_xy, const double *d_cir, const double *d_cor, const Params &p,
-               Tree &t, cudaStream_t s) {
+               Tree &t, cudaStream_t s, const int *d_set_off, int nsets) {
   t.n = n;
   t.nterms = p.nterms;
+  const bool batched = nsets > 1;
+  int lev0 = 0;  // levels of container cells above the set roots
+  if (batched) {
+    lev0 = 1;
+    while ((1ll << (2 * (lev0 - 1))) < (long long)nsets) lev0++;
+    if (lev0 + kShortKeyLevels > kKeyLevels) return TREE2D_ERR_TOO_LARGE;
+  }
+  t.nsets = batched ? nsets : 1;
+  t.lev0 = lev0;
+  t.set_off = batched ? d_set_off : nullptr;
+  t.set_cor = batched ? d_cor : nullptr;
   const int ntiles = (n + kScanTile - 1) / kScanTile;
   // ---- blob-sized buffers
   size_t need = 0;
-  need += Arena::bytes_for(n, 8) * 4;           // x y cir cor
+  need += Arena::bytes_for(n, 8) * 5;           // x y cir cor icor2
   need += Arena::bytes_for(n, 4);               // perm
   need += Arena::bytes_for(n, 8);               // keys (sorted)
   need += Arena::bytes_for(n, 4);               // cellbase
   need += Arena::bytes_for(n, 1) * 2;           // cpl, leaf_level
-  need += Arena::bytes_for(1, sizeof(RootBox));
+  need += Arena::bytes_for(t.nsets, sizeof(RootBox));
   T2D_CUDA_TRY(ws.blob_arena.reserve(need));
   ws.blob_arena.reset();
   t.x = ws.blob_arena.take<double>(n);
   t.y = ws.blob_arena.take<double>(n);
   t.cir = ws.blob_arena.take<double>(n);
   t.cor = ws.blob_arena.take<double>(n);
+  t.icor2 = ws.blob_arena.take<double>(n);
   t.perm = ws.blob_arena.take<int>(n);
   t.keys = ws.blob_arena.take<uint64_t>(n);
   unsigned *cellbase = ws.blob_arena.take<unsigned>(n);
   uint8_t *cpl = ws.blob_arena.take<uint8_t>(n);
   uint8_t *leaf_level = ws.blob_arena.take<uint8_t>(n);
-  t.root = ws.blob_arena.take<RootBox>(1);
+  t.root = ws.blob_arena.take<RootBox>(t.nsets);  // one per set
   t.cpl = cpl;
   t.leaf_level = leaf_level;
   t.cellbase = cellbase;
@@ -565,8 +677,9 @@ int build_tree(Workspace &ws, int n, const double *d_xy, const double *d_cir, co
   tneed += radix_sort_temp_bytes(n) + 256;
   tneed += Arena::bytes_for(kBoxBlocks, sizeof(Box4));
   tneed += Arena::bytes_for(ntiles + 1, 8) + 256;
-  const int tlev = centre_levels(n);
-  tneed += Arena::bytes_for(2 * centre_entries(tlev), 8);
+  const int tlev = batched ? 12 : centre_levels(n);
+  tneed += Arena::bytes_for(2 * centre_entries(tlev) * t.nsets, 8);
+  if (batched) tneed += Arena::bytes_for(n, 4);  // set of each blob
   T2D_CUDA_TRY(ws.tmp_arena.reserve(tneed));
   ws.tmp_arena.reset();
   uint64_t *keys_alt = ws.tmp_arena.take<uint64_t>(n);
@@ -577,23 +690,30 @@ int build_tree(Workspace &ws, int n, const double *d_xy, const double *d_cir, co
   Box4 *bpart = ws.tmp_arena.take<Box4>(kBoxBlocks);
   unsigned long long *part = ws.tmp_arena.take<unsigned long long>(ntiles + 1);
   unsigned long long *total = ws.tmp_arena.take<unsigned long long>(1);
-  uint64_t *ctab = ws.tmp_arena.take<uint64_t>(2 * centre_entries(tlev));
+  uint64_t *ctab = ws.tmp_arena.take<uint64_t>(2 * centre_entries(tlev) * t.nsets);
+  int *set_of = batched ? ws.tmp_arena.take<int>(n) : nullptr;
 
-  int levels = kShortKeyLevels;
+  int levels = kShortKeyLevels;  // digits below the set root
 retry:
   T2D_CUDA_TRY(cudaMemsetAsync(ws.status, 0, sizeof(DevStatus), s));
 
-  // 1. root box
-  k_bbox<<<kBoxBlocks, 256, 0, s>>>(d_xy, d_cir, d_cor, n, bpart, ws.status);
-  ::t2d::g_launches.fetch_add(1, std::memory_order_relaxed);
-  k_root<<<1, 32, 0, s>>>(bpart, kBoxBlocks, t.root);
-  ::t2d::g_launches.fetch_add(1, std::memory_order_relaxed);
+  // 1. root box (per set)
+  if (batched) {
+    k_bbox_sets<<<nsets, 256, 0, s>>>(d_xy, d_cir, d_cor, d_set_off, t.root, set_of, ws.status);
+    ::t2d::g_launches.fetch_add(1, std::memory_order_relaxed);
+  } else {
+    k_bbox<<<kBoxBlocks, 256, 0, s>>>(d_xy, d_cir, d_cor, n, bpart, ws.status);
+    k_root<<<1, 32, 0, s>>>(bpart, kBoxBlocks, t.root);
+    ::t2d::g_launches.fetch_add(2, std::memory_order_relaxed);
+  }
   // 2. keys
-  k_centre_table<<<(int)((2 * centre_entries(tlev) + 255) / 256), 256, 0, s>>>(t.root, ctab, tlev);
-  k_keys<<<(n + 255) / 256, 256, 0, s>>>(d_xy, n, t.root, ctab, tlev, t.keys, vals, levels);
+  const int total_levels = levels + lev0;
+  k_centre_table<<<dim3((unsigned)((2 * centre_entries(tlev) + 255) / 256), (unsigned)t.nsets), 256, 0, s>>>(
+      t.root, ctab, tlev);
+  k_keys<<<(n + 255) / 256, 256, 0, s>>>(d_xy, n, t.root, ctab, tlev, t.keys, vals, levels, set_of, lev0);
   ::t2d::g_launches.fetch_add(2, std::memory_order_relaxed);
   // 3. sort
-  T2D_CUDA_TRY(radix_sort_pairs(t.keys, vals, keys_alt, vals_alt, n, 64 - 2 * levels, 64, sort_tmp, s));
+  T2D_CUDA_TRY(radix_sort_pairs(t.keys, vals, keys_alt, vals_alt, n, 64 - 2 * total_levels, 64, sort_tmp, s));
   // 4-5. leaf levels
   k_cpl<<<(n + 255) / 256, 256, 0, s>>>(t.keys, n, p.num_p, cpl, w);
   ::t2d::g_launches.fetch_add(1, std::memory_order_relaxed);
@@ -601,7 +721,8 @@ retry:
     const int H = p.num_p - 1;
     size_t smem = 2 * (size_t)(kLLTile + H);
     if (smem > 48 * 1024) T2D_CUDA_TRY(cudaFuncSetAttribute(k_leaf_level, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    k_leaf_level<<<(n + kLLTile - 1) / kLLTile, 256, smem, s>>>(w, n, p.num_p, leaf_level, ws.status, levels);
+    k_leaf_level<<<(n + kLLTile - 1) / kLLTile, 256, smem, s>>>(w, n, p.num_p, leaf_level, ws.status, total_levels,
+                                                                lev0);
     ::t2d::g_launches.fetch_add(1, std::memory_order_relaxed);
   }
   // 6. counts and scan
@@ -615,11 +736,11 @@ retry:
   T2D_CUDA_TRY(cudaMemcpyAsync(h_total, total, 8, cudaMemcpyDeviceToHost, s));
   T2D_CUDA_TRY(cudaStreamSynchronize(s));
   if (ws.h_status->err) return ws.h_status->err;
-  if (ws.h_status->deeper && levels < kKeyLevels) {
-    levels = kKeyLevels;  // rare: a cell at the short depth still needs splitting
+  if (ws.h_status->deeper && total_levels < kKeyLevels) {
+    levels = kKeyLevels - lev0;  // rare: a cell at the short depth still needs splitting
     goto retry;
   }
-  t.key_levels = levels;
+  t.key_levels = total_levels;
   unsigned long long tot = *h_total;
   long long ncell = 1 + (long long)(tot >> 32);
   long long nleaf = (long long)(tot & 0xffffffffu);
@@ -652,7 +773,7 @@ retry:
 
   // 7. cells
   EmitArgs ea{t.keys, cpl, leaf_level, part, t.root, n, cellbase, t.level, t.begin, t.leaf, t.cx, t.cy, t.region,
-              t.leaf_cell, ctab, tlev};
+              t.leaf_cell, ctab, tlev, lev0};
   k_emit_cells<<<ntiles, kScanThreads, 0, s>>>(ea);
   ::t2d::g_launches.fetch_add(1, std::memory_order_relaxed);
   k_cell_end<<<(t.ncell + 255) / 256, 256, 0, s>>>(t.keys, n, t.ncell, t.level, t.begin, t.end);
@@ -665,7 +786,7 @@ retry:
     k_leaf_order<<<(int)(((long)t.nleaf * 32 + 255) / 256), 256, 0, s>>>(vals, t.nleaf, t.leaf_cell, t.begin, t.end,
                                                                           t.perm);
     ::t2d::g_launches.fetch_add(1, std::memory_order_relaxed);
-  k_gather<<<(n + 255) / 256, 256, 0, s>>>(d_xy, d_cir, d_cor, t.perm, n, t.x, t.y, t.cir, t.cor);
+  k_gather<<<(n + 255) / 256, 256, 0, s>>>(d_xy, d_cir, d_cor, t.perm, n, t.x, t.y, t.cir, t.cor, t.icor2);
   ::t2d::g_launches.fetch_add(1, std::memory_order_relaxed);
   T2D_CUDA_TRY(cudaGetLastError());
   return TREE2D_OK;
@@ -682,7 +803,7 @@ int sort_targets(Workspace &ws, int n, const double *d_xy, const RootBox *d_root
   void *tmp = ws.tmp_arena.take<char>(radix_sort_temp_bytes(n));
   // order only (for coherent warps): the short key depth is enough
   k_keys<<<(n + 255) / 256, 256, 0, s>>>(d_xy, n, d_root, nullptr, 0, k, reinterpret_cast<uint32_t *>(d_order),
-                                          kShortKeyLevels);
+                                          kShortKeyLevels, nullptr, 0);
   ::t2d::g_launches.fetch_add(1, std::memory_order_relaxed);
   T2D_CUDA_TRY(radix_sort_pairs(k, reinterpret_cast<uint32_t *>(d_order), k2, v2, n, 64 - 2 * kShortKeyLevels, 64,
                                 tmp, s));

@@ -6,6 +6,7 @@
 #include <atomic>
 #include <cstddef>
 #include <cstdint>
+#include <map>
 #include <string>
 
 #include "../../include/tree2d.h"
@@ -41,6 +42,8 @@ struct MixedParams {
   int learned = 0;        // TREE2D_MODE_LEARNED: near-field decisions by the network
   const LearnedParams *lp = nullptr;
   long lp_version = 0;
+  int autotune = 1;       // time the near-field variants on a new size class
+  int eval_variant = -1;  // >= 0: force this near-field variant
 };
 
 // Root box, written on the device (quadtree.c:81-99 semantics).
@@ -103,6 +106,7 @@ class Arena {
 struct Tree {
   int n = 0, ncell = 0, nleaf = 0, depth = 0, nterms = 0;
   double *x = nullptr, *y = nullptr, *cir = nullptr, *cor = nullptr;
+  double *icor2 = nullptr;    // 1 / cor^2 per blob (tree order)
   int *perm = nullptr;        // tree position -> original blob index
   int *level = nullptr, *begin = nullptr, *end = nullptr;
   int *child = nullptr;       // 4 per cell, quadrant order, -1 = no blob there
@@ -118,6 +122,10 @@ struct Tree {
   uint8_t *leaf_level = nullptr;  // per position: level of its leaf
   unsigned *cellbase = nullptr;   // per position: id of the first cell it starts
   int key_levels = 0;             // digits in the keys (kShortKeyLevels or kKeyLevels)
+  int nsets = 1;                  // blob sets in the tree (batched solve: > 1)
+  const int *set_off = nullptr;   // batched: device offsets of the sets (nsets + 1)
+  const double *set_cor = nullptr;  // batched: core radii in input order (valid during the solve)
+  int lev0 = 0;                   // batched: levels of container cells above the set roots
 };
 
 // Per-solver working state (one per library instance).
@@ -133,9 +141,10 @@ struct Workspace {
   long lr_version = -1;
   MixedView *mxv = nullptr;  // the last mixed solve's view (kept for sampling)
   long mx_tot[3] = {0, 0, 0};  // U, W, K list entries of that solve
+  std::map<uint64_t, int> eval_tuned;  // size class -> fastest near-field variant
   DevStatus *status = nullptr;   // device
   DevStatus *h_status = nullptr; // pinned host mirror
-  cudaEvent_t ev[6] = {};
+  cudaEvent_t ev[8] = {};
   bool init = false;
 };
 
@@ -144,8 +153,12 @@ cudaError_t workspace_init(Workspace &ws);
 // --- tree build (build_tree.cu) --------------------------------------
 // Builds the tree over n blobs (xy interleaved, device).  Synchronises the
 // stream once to size the cell arrays.  Returns a TREE2D status.
+// Batched (nsets > 1): the blobs are nsets independent sets, set k at
+// [d_set_off[k], d_set_off[k+1]) (device offsets); each set gets its own root
+// box and exactly the cells it would get alone, below lev0 levels of
+// container cells that keep the sets apart (t.lev0, t.root[k] per set).
 int build_tree(Workspace &ws, int n, const double *d_xy, const double *d_cir, const double *d_cor,
-               const Params &p, Tree &t, cudaStream_t s);
+               const Params &p, Tree &t, cudaStream_t s, const int *d_set_off = nullptr, int nsets = 1);
 
 // Keys of arbitrary points against an existing root box, then sorted:
 // order[i] = index of the i-th target in key order.

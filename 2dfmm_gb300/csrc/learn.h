@@ -81,10 +81,6 @@ int learned_decide(MixedView &m, const LeafStats *stats, const float *u_ref_ptr,
 void learn_weight_images(const float *theta, std::vector<uint16_t> &img, std::vector<float> &bias);
 size_t learn_weight_image_elems();
 
-// Evaluation with decisions (learn.cu).
-int learned_evaluate(MixedView &m, const unsigned char *u_dec, const unsigned char *k_dec, int order_margin,
-                     double *uv, const int *perm, cudaStream_t s);
-
 // Training data: for `ns` sampled interactions (leaf ordinal, list kind,
 // entry index), features and the cheapest acceptable class against the FP64
 // exact contribution (label generator, learn.cu).

@@ -34,7 +34,7 @@ namespace {
 __global__ void __launch_bounds__(256) k_m2l_cc(MixedView m, const float2 *__restrict__ T) {
   const int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   if (c >= m.ncell) return;
-  if (m.level[c] < 2) return;
+  if (m.level[c] - m.lev0 < 2) return;
   const int P = m.P;
   const int cls = (m.ix[c] & 1) + 2 * (m.iy[c] & 1);
   const int *V = m.vlist + (size_t)c * 27;
@@ -258,11 +258,11 @@ __global__ void __launch_bounds__(kThreadsTC) k_m2l_tc(TcArgs a) {
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(a.tmem_cols) : "memory");
 }
 
-// Cells of level >= 2, grouped by child class (order within a class is
+// Cells of level >= 2 (below their set root), grouped by child class (order within a class is
 // irrelevant: every row's sum is its own).
 __global__ void k_class_lists(MixedView m, int *list, int *count) {
   int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= m.ncell || m.level[c] < 2) return;
+  if (c >= m.ncell || m.level[c] - m.lev0 < 2) return;
   const int cls = (m.ix[c] & 1) + 2 * (m.iy[c] & 1);
   const int pos = atomicAdd(&count[cls], 1);
   list[(size_t)cls * m.ncell + pos] = c;

@@ -40,6 +40,7 @@
 #include "dev_common.cuh"
 #include "mixed.h"
 #include "learn.h"
+#include "tc_ptx.cuh"
 
 namespace t2d {
 namespace {
@@ -191,7 +192,7 @@ __global__ void k_vx_lists(MixedView m) {
   for (int s = 0; s < 27; s++) V[s] = -1;
   for (int s = 0; s < 8; s++) X[s] = -1;
   const int lev = m.level[c];
-  if (lev < 2) return;
+  if (lev - m.lev0 < 2) return;  // levels counted from the cell's set root
   const int p = m.parent[c];
   const unsigned ix = m.ix[c], iy = m.iy[c];
   const int qx = ix & 1, qy = iy & 1, cls = qx + 2 * qy;
@@ -237,10 +238,21 @@ __global__ void k_sigma_max(const double *cor, int n, unsigned *out) {
   if ((threadIdx.x & 31) == 0) atomicMax(out, __float_as_uint(mx));
 }
 
-__global__ void k_cutoff(unsigned *bits, float cutoff) {
-  float s = __uint_as_float(*bits);
+__global__ void k_cutoff(unsigned *bits, float cutoff, int count) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= count) return;
+  float s = __uint_as_float(bits[i]);
   float rc = cutoff * s * 1.0001f;  // slack for the FP32 rounding of sigma
-  *reinterpret_cast<float *>(bits) = isfinite(rc) ? rc : 0.f;
+  reinterpret_cast<float *>(bits)[i] = isfinite(rc) ? rc : 0.f;
+}
+
+// Batched sets: max sigma of each set (one block per set, input order).
+__global__ void k_sigma_max_sets(const double *cor, const int *off, unsigned *out) {
+  const int set = blockIdx.x;
+  float mx = 0.f;
+  for (int i = off[set] + threadIdx.x; i < off[set + 1]; i += blockDim.x) mx = fmaxf(mx, (float)fabs(cor[i]));
+  for (int o = 16; o; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(out + set, __float_as_uint(mx));
 }
 
 __global__ void k_parent(MixedView m) {
@@ -290,7 +302,16 @@ __global__ void __launch_bounds__(32 * kWalkWarps) k_lists(MixedView m) {
   const int b = m.leaf_cell[l];
   const int lev = m.level[b];
   const unsigned bx = m.ix[b], by = m.iy[b];
-  const float rc = *m.rc_ptr;
+  // the correction walk starts at the leaf's set root (the tree root for a
+  // single set); a batched tree keeps one cutoff per set
+  int root = b;
+  while (m.level[root] > m.lev0) root = m.parent[root];
+  float rc = *m.rc_ptr;
+  if (m.rc_set) {
+    const int sh = lev - m.lev0;
+    const unsigned tx = bx >> sh, ty = by >> sh;
+    rc = m.rc_set[(ty >> 1) * (1u << (m.lev0 - 1)) + (tx >> 1)];
+  }
   int base[3] = {0, 0, 0};
   if (kFill) {
     base[0] = m.u_off[l];
@@ -330,7 +351,7 @@ __global__ void __launch_bounds__(32 * kWalkWarps) k_lists(MixedView m) {
     const bool eleaf = e >= 0 && m.leaf[e];
     emit(eleaf ? 0 : -1, e);
     push(e >= 0 && !eleaf, (unsigned)e);
-    push(lane == 0 && rc > 0.f, kTagK);  // the root, for the correction walk
+    push(lane == 0 && rc > 0.f, (unsigned)root | kTagK);  // the set root, for the correction walk
   }
   __syncwarp();
   while (top > 0) {
@@ -470,8 +491,11 @@ __global__ void __launch_bounds__(kScan3Threads) k_scan3_apply(int *a, int *b, i
 // Coefficient storage: per cell 2P floats, real parts then imaginary parts.
 
 
+// Complex product with every rounding spelled out (explicit FMA and
+// round-to-nearest products), so that no kernel variant can contract it
+// differently: the near-field variants must agree bit for bit.
 __device__ __forceinline__ float2 fmul(float2 a, float2 b) {
-  return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+  return make_float2(fmaf(a.x, b.x, -__fmul_rn(a.y, b.y)), fmaf(a.x, b.y, __fmul_rn(a.y, b.x)));
 }
 
 // S2M: one warp per leaf, lane k owns a_k (k < P <= 32).
@@ -602,6 +626,27 @@ __device__ __forceinline__ void kahan(float &s, float &cmp, float v) {
   s = t;
 }
 
+// M2P of source leaf A at order p (terms 0..p-1) at a target offset z from
+// leaf B's centre, added to phi.
+__device__ __forceinline__ void m2p_order(const MixedView &m, int B, int A, int p, float2 z, float2 &phi) {
+  const int P = m.P;
+  const float ih = m.inv_h[A];
+  const float zx = __fmul_rn(__fadd_rn(z.x, (float)(m.cx[B] - m.cx[A])), ih);
+  const float zy = __fmul_rn(__fadd_rn(z.y, (float)(m.cy[B] - m.cy[A])), ih);
+  const float ir2 = __fdiv_rn(1.f, fmaf(zx, zx, __fmul_rn(zy, zy)));
+  const float2 w = make_float2(__fmul_rn(zx, ir2), -__fmul_rn(zy, ir2));
+  const float *MA = m.M + (size_t)A * 2 * P;
+  float2 a = make_float2(MA[p - 1], MA[P + p - 1]);
+  for (int k = p - 2; k >= 0; k--) {
+    a = fmul(a, w);
+    a.x = __fadd_rn(a.x, MA[k]);
+    a.y = __fadd_rn(a.y, MA[P + k]);
+  }
+  a = fmul(a, w);
+  phi.x = fmaf(a.x, ih, phi.x);
+  phi.y = fmaf(a.y, ih, phi.y);
+}
+
 // Evaluation: one warp per leaf; each lane owns up to two targets (chunks
 // of 64 targets), so a leaf of <= 64 blobs walks its source lists once.
 // Sources are read as one float4 {x, y, G, 1/sigma^2} (offsets from their
@@ -610,32 +655,16 @@ __device__ __forceinline__ void far_field(const MixedView &m, int l, int B, floa
   const int P = m.P;
   const float ihB = m.inv_h[B];
   const float *LB = m.L + (size_t)B * 2 * P;
-  const float2 zeta = make_float2(zt.x * ihB, zt.y * ihB);
+  const float2 zeta = make_float2(__fmul_rn(zt.x, ihB), __fmul_rn(zt.y, ihB));
   float2 acc = make_float2(LB[P - 1], LB[2 * P - 1]);
   for (int k = P - 2; k >= 0; k--) {
     acc = fmul(acc, zeta);
-    acc.x += LB[k];
-    acc.y += LB[P + k];
+    acc.x = __fadd_rn(acc.x, LB[k]);
+    acc.y = __fadd_rn(acc.y, LB[P + k]);
   }
-  phi.x = acc.x * ihB;
-  phi.y = acc.y * ihB;
-  for (int e = m.w_off[l]; e < m.w_off[l + 1]; e++) {
-    const int A = m.w_idx[e];
-    const float ih = m.inv_h[A];
-    const float zx = (zt.x + (m.cxf[B] - m.cxf[A])) * ih, zy = (zt.y + (m.cyf[B] - m.cyf[A])) * ih;
-    const float ir2 = 1.f / (zx * zx + zy * zy);
-    const float2 w = make_float2(zx * ir2, -zy * ir2);
-    const float *MA = m.M + (size_t)A * 2 * P;
-    float2 a = make_float2(MA[P - 1], MA[2 * P - 1]);
-    for (int k = P - 2; k >= 0; k--) {
-      a = fmul(a, w);
-      a.x += MA[k];
-      a.y += MA[P + k];
-    }
-    a = fmul(a, w);
-    phi.x += a.x * ih;
-    phi.y += a.y * ih;
-  }
+  phi.x = __fmul_rn(acc.x, ihB);
+  phi.y = __fmul_rn(acc.y, ihB);
+  for (int e = m.w_off[l]; e < m.w_off[l + 1]; e++) m2p_order(m, B, m.w_idx[e], P, zt, phi);
 }
 
 // 2^t on the SFU (PTX ex2.approx: relative error ~2^-22, FTZ).
@@ -658,17 +687,17 @@ __device__ __forceinline__ float sfu_exp2(float t) {
 //                   rc add their tiny exact terms).
 template <bool kCorrection>
 __device__ __forceinline__ void pair(const float4 sj, float tx, float ty, float &sx, float &sy) {
-  const float rx = tx - sj.x, ry = ty - sj.y;
+  const float rx = __fsub_rn(tx, sj.x), ry = __fsub_rn(ty, sj.y);
   const float r2 = fmaf(rx, rx, fmaf(ry, ry, 1e-30f));
-  const float t = r2 * sj.w;
+  const float t = __fmul_rn(r2, sj.w);
   const float e = sfu_exp2(t);
   float f;
   if (!kCorrection) {
-    const float x2 = t * -0.69314718f;
-    const float e1f = t > -1.44269504e-3f ? x2 * fmaf(-0.5f, x2, 1.f) : 1.f - e;
-    f = __fdividef(sj.z * e1f, r2);
+    const float x2 = __fmul_rn(t, -0.69314718f);
+    const float e1f = t > -1.44269504e-3f ? __fmul_rn(x2, fmaf(-0.5f, x2, 1.f)) : __fsub_rn(1.f, e);
+    f = __fdividef(__fmul_rn(sj.z, e1f), r2);
   } else {
-    f = -__fdividef(sj.z * e, r2);
+    f = -__fdividef(__fmul_rn(sj.z, e), r2);
   }
   sx = fmaf(-f, ry, sx);
   sy = fmaf(f, rx, sy);
@@ -695,36 +724,169 @@ __device__ __forceinline__ void leaf_pairs(const float4 *__restrict__ src, int j
   }
 }
 
-// M2P of source leaf A at order p (terms 0..p-1) at a target offset z from
-// leaf B's centre, added to phi.
-__device__ __forceinline__ void m2p_order(const MixedView &m, int B, int A, int p, float2 z, float2 &phi) {
-  const int P = m.P;
-  const float ih = m.inv_h[A];
-  const float zx = (z.x + (m.cxf[B] - m.cxf[A])) * ih, zy = (z.y + (m.cyf[B] - m.cyf[A])) * ih;
-  const float ir2 = 1.f / (zx * zx + zy * zy);
-  const float2 w = make_float2(zx * ir2, -zy * ir2);
-  const float *MA = m.M + (size_t)A * 2 * P;
-  float2 a = make_float2(MA[p - 1], MA[P + p - 1]);
-  for (int k = p - 2; k >= 0; k--) {
-    a = fmul(a, w);
-    a.x += MA[k];
-    a.y += MA[P + k];
-  }
-  a = fmul(a, w);
-  phi.x += a.x * ih;
-  phi.y += a.y * ih;
-}
-
 struct Decisions {
   const unsigned char *u, *k;  // class per U / K entry; null: all direct
   int margin;
 };
 
-template <bool kLearned>
-__global__ void __launch_bounds__(128, 8) k_eval_mixed(MixedView m, double *uv, const int *perm, Decisions dec) {
+// Near field of every leaf: one warp per target leaf, two targets per lane.
+// The warp walks its direct entries (U list, then K list; in the learned
+// form the entries the network accepted are M2P'd first and skipped here)
+// and stages each source leaf's blobs in shared memory with a bulk copy
+// (cp.async.bulk, one 16-byte record per blob, completion on a per-buffer
+// mbarrier), double-buffered: the next leaf is in flight while the lanes
+// sum the current one.  Leaves larger than a stage buffer, and every leaf
+// after a wait that gave up (recorded as TREE2D_ERR_TIMEOUT), are read from
+// global memory instead, so the result never depends on the staging.
+constexpr int kEvalWarps = 4;
+constexpr int kStage = 64;  // blobs per stage buffer
+constexpr long kEvalWaitLimit = 1l << 22;  // polls; a healthy copy lands within microseconds
+
+template <bool kLearned, int kWarps>
+__global__ void __launch_bounds__(32 * kWarps, 32 / kWarps) k_eval_staged(MixedView m, double *uv, const int *perm,
+                                                                           Decisions dec, long wait_limit) {
+  __shared__ __align__(128) float4 s_src[kWarps][2][kStage];
+  __shared__ __align__(8) uint64_t s_bar[kWarps][2];
+  const int warp = threadIdx.x >> 5;
+  const int l = blockIdx.x * kWarps + warp, lane = threadIdx.x & 31;
+  if (l >= m.nleaf) return;  // uniform over the warp; nothing below syncs the block
+  uint64_t *bar = s_bar[warp];
+  if (lane == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncwarp();
+  unsigned parity = 0;    // bit b: parity of buffer b's next completion
+  unsigned inflight = 0;  // bit b: a copy into buffer b not yet waited for
+  bool staging = true;    // false after a wait gave up
+  const int B = m.leaf_cell[l];
+  const double cxB = m.cx[B], cyB = m.cy[B];
+  const double inv2pi = 0.15915494309189533577;
+  unsigned long long pairs = 0;
+  const int u0 = m.u_off[l], nu = m.u_off[l + 1] - u0;
+  const int k0 = m.k_off[l], nk = m.k_off[l + 1] - k0;
+  // position q of the walk: U entries, then K entries
+  auto src_leaf = [&](int q) { return q < nu ? m.u_idx[u0 + q] : m.k_idx[k0 + q - nu]; };
+  auto direct = [&](int q) {
+    if (!kLearned) return true;
+    return (q < nu ? dec.u[u0 + q] : dec.k[k0 + q - nu]) == 0;
+  };
+  auto next_direct = [&](int q) {
+    while (q < nu + nk && !direct(q)) q++;
+    return q;
+  };
+  // copy source leaf of position q into buffer b (warp-uniform decision)
+  auto stage = [&](int q, int b) {
+    const int A = src_leaf(q);
+    const int j0 = m.begin[A], cnt = m.end[A] - j0;
+    if (!staging || cnt > kStage) return false;
+    if (lane == 0) {
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      mbar_expect_tx(&bar[b], (uint32_t)cnt * 16u);
+      bulk_g2s(s_src[warp][b], m.src4 + j0, (uint32_t)cnt * 16u, &bar[b]);
+    }
+    inflight |= 1u << b;
+    return true;
+  };
+  for (int t0 = m.begin[B]; t0 < m.end[B]; t0 += 64) {
+    const int ta = t0 + lane, tb = t0 + 32 + lane;
+    const bool va = ta < m.end[B], vb = tb < m.end[B];
+    const bool two = __any_sync(0xffffffffu, vb);
+    const float2 za = va ? m.loc[ta] : make_float2(0.f, 0.f);
+    const float2 zb = vb ? m.loc[tb] : make_float2(0.f, 0.f);
+    float2 pa = make_float2(0.f, 0.f), pb = make_float2(0.f, 0.f);
+    int q = next_direct(0);
+    int buf = 0;
+    bool staged = q < nu + nk && stage(q, buf);
+    far_field(m, l, B, za, pa);
+    if (two) far_field(m, l, B, zb, pb);
+    if (kLearned) {
+      // accepted U entries: the source leaf's multipole at the chosen order
+      // (accepted K entries: the correction is left out)
+      for (int e = u0; e < u0 + nu; e++) {
+        const int d = dec.u[e];
+        if (d > 0) {
+          const int A = m.u_idx[e];
+          const int p = min(min(class_order(d) + dec.margin, 16), m.P);
+          m2p_order(m, B, A, p, za, pa);
+          if (two) m2p_order(m, B, A, p, zb, pb);
+        }
+      }
+    }
+    float axa = 0.f, aya = 0.f, cxa = 0.f, cya = 0.f;
+    float axb = 0.f, ayb = 0.f, cxb = 0.f, cyb = 0.f;
+    while (q < nu + nk) {
+      const int qn = next_direct(q + 1);
+      const bool staged_next = qn < nu + nk && stage(qn, buf ^ 1);
+      const int A = src_leaf(q);
+      // offset of the source leaf's centre in FP64, then rounded: FP32 centres
+        // would carry ~1e-7 absolute error into every close pair
+        const float ox = (float)(cxB - m.cx[A]), oy = (float)(cyB - m.cy[A]);
+      const int j0 = m.begin[A], cnt = m.end[A] - j0;
+      bool use_smem = false;
+      if (staged) {
+        if (mbar_wait(&bar[buf], (parity >> buf) & 1u, wait_limit)) {
+          parity ^= 1u << buf;
+          inflight &= ~(1u << buf);
+          use_smem = true;
+        } else {
+          staging = false;  // the copy stays in flight; read global memory from now on
+          if (lane == 0) set_err(m.st, TREE2D_ERR_TIMEOUT);
+        }
+      }
+      float sxa = 0.f, sya = 0.f, sxb = 0.f, syb = 0.f;
+      const float txa = __fadd_rn(za.x, ox), tya = __fadd_rn(za.y, oy), txb = __fadd_rn(zb.x, ox), tyb = __fadd_rn(zb.y, oy);
+      if (q < nu) {
+        if (use_smem)
+          leaf_pairs<false>(s_src[warp][buf], 0, cnt, txa, tya, txb, tyb, two, sxa, sya, sxb, syb);
+        else
+          leaf_pairs<false>(m.src4 + j0, 0, cnt, txa, tya, txb, tyb, two, sxa, sya, sxb, syb);
+      } else {
+        if (use_smem)
+          leaf_pairs<true>(s_src[warp][buf], 0, cnt, txa, tya, txb, tyb, two, sxa, sya, sxb, syb);
+        else
+          leaf_pairs<true>(m.src4 + j0, 0, cnt, txa, tya, txb, tyb, two, sxa, sya, sxb, syb);
+      }
+      kahan(axa, cxa, sxa);
+      kahan(aya, cya, sya);
+      kahan(axb, cxb, sxb);
+      kahan(ayb, cyb, syb);
+      pairs += (unsigned long long)cnt * (unsigned long long)((va ? 1 : 0) + (vb ? 1 : 0));
+      __syncwarp();  // every lane is done with this buffer before it is refilled
+      q = qn;
+      buf ^= 1;
+      staged = staged_next;
+    }
+    // FP64 final reduction: u = Im(phi)/2pi + ax/2pi, v = Re(phi)/2pi + ay/2pi
+    if (va) {
+      const int o = perm[ta];
+      uv[2 * (size_t)o] = ((double)pa.y + (double)axa - (double)cxa) * inv2pi;
+      uv[2 * (size_t)o + 1] = ((double)pa.x + (double)aya - (double)cya) * inv2pi;
+    }
+    if (vb) {
+      const int o = perm[tb];
+      uv[2 * (size_t)o] = ((double)pb.y + (double)axb - (double)cxb) * inv2pi;
+      uv[2 * (size_t)o + 1] = ((double)pb.x + (double)ayb - (double)cyb) * inv2pi;
+    }
+  }
+  // copies still in flight after a wait gave up: wait (bounded) before the
+  // shared memory is released
+  for (int b = 0; b < 2; b++)
+    if (inflight & (1u << b)) mbar_wait(&bar[b], (parity >> b) & 1u, wait_limit);
+  for (int o = 16; o; o >>= 1) pairs += __shfl_xor_sync(0xffffffffu, pairs, o);
+  if (lane == 0) atomicAdd(&m.st->n_pairs, pairs);
+}
+
+// The same near field with the source blobs read straight from global
+// memory (through L1), the other variant the tuner times.
+template <bool kLearned, int kWarps>
+__global__ void __launch_bounds__(32 * kWarps, 32 / kWarps) k_eval_mixed(MixedView m, double *uv, const int *perm,
+                                                                          Decisions dec, long) {
   const int l = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   if (l >= m.nleaf) return;
   const int B = m.leaf_cell[l];
+  const double cxB = m.cx[B], cyB = m.cy[B];
   const double inv2pi = 0.15915494309189533577;
   unsigned long long pairs = 0;
   for (int t0 = m.begin[B]; t0 < m.end[B]; t0 += 64) {
@@ -757,13 +919,15 @@ __global__ void __launch_bounds__(128, 8) k_eval_mixed(MixedView m, double *uv, 
             continue;
           }
         }
-        const float ox = m.cxf[B] - m.cxf[A], oy = m.cyf[B] - m.cyf[A];
+        // offset of the source leaf's centre in FP64, then rounded: FP32 centres
+        // would carry ~1e-7 absolute error into every close pair
+        const float ox = (float)(cxB - m.cx[A]), oy = (float)(cyB - m.cy[A]);
         const int j0 = m.begin[A], j1 = m.end[A];
         float sxa = 0.f, sya = 0.f, sxb = 0.f, syb = 0.f;
         if (pass == 0)
-          leaf_pairs<false>(m.src4, j0, j1, za.x + ox, za.y + oy, zb.x + ox, zb.y + oy, two, sxa, sya, sxb, syb);
+          leaf_pairs<false>(m.src4, j0, j1, __fadd_rn(za.x, ox), __fadd_rn(za.y, oy), __fadd_rn(zb.x, ox), __fadd_rn(zb.y, oy), two, sxa, sya, sxb, syb);
         else
-          leaf_pairs<true>(m.src4, j0, j1, za.x + ox, za.y + oy, zb.x + ox, zb.y + oy, two, sxa, sya, sxb, syb);
+          leaf_pairs<true>(m.src4, j0, j1, __fadd_rn(za.x, ox), __fadd_rn(za.y, oy), __fadd_rn(zb.x, ox), __fadd_rn(zb.y, oy), two, sxa, sya, sxb, syb);
         kahan(axa, cxa, sxa);
         kahan(aya, cya, sya);
         kahan(axb, cxb, sxb);
@@ -917,7 +1081,7 @@ int mixed_upward(MixedView &m, int depth, cudaStream_t s) {
   k_s2m_f32<<<(int)(((long)m.nleaf * 32 + 255) / 256), 256, 0, s>>>(m);
   g_launches.fetch_add(1, std::memory_order_relaxed);
   const int blocks = 152 * 8;
-  for (int lev = depth - 1; lev >= 2; lev--) {
+  for (int lev = depth - 1; lev >= 2 + m.lev0; lev--) {
     k_m2m_f32<<<blocks, 256, 0, s>>>(m, lev);
     g_launches.fetch_add(1, std::memory_order_relaxed);
   }
@@ -929,7 +1093,7 @@ int mixed_downward(MixedView &m, int depth, cudaStream_t s) {
   k_p2l<<<(int)(((long)m.ncell * 32 + 255) / 256), 256, 0, s>>>(m);
   g_launches.fetch_add(1, std::memory_order_relaxed);
   const int blocks = 152 * 8;
-  for (int lev = 3; lev <= depth; lev++) {
+  for (int lev = 3 + m.lev0; lev <= depth; lev++) {
     k_l2l_f32<<<blocks, 256, 0, s>>>(m, lev);
     g_launches.fetch_add(1, std::memory_order_relaxed);
   }
@@ -937,14 +1101,77 @@ int mixed_downward(MixedView &m, int depth, cudaStream_t s) {
   return TREE2D_OK;
 }
 
-int mixed_evaluate(MixedView &m, double *uv, const int *perm, cudaStream_t s) {
-  Decisions none{nullptr, nullptr, 0};
-  k_eval_mixed<false><<<(int)(((long)m.nleaf * 32 + 127) / 128), 128, 0, s>>>(m, uv, perm, none);
+// Near-field variants (bit-identical results): 0/1 read the source blobs
+// from global memory with 4/8 warps per block, 2/3 stage them in shared
+// memory by bulk copies with 4/8 warps per block.
+constexpr int kEvalVariants = 4;
+
+template <bool kLearned>
+cudaError_t launch_eval(int v, const MixedView &m, double *uv, const int *perm, Decisions d, cudaStream_t s) {
+  switch (v) {
+    case 0:
+      k_eval_mixed<kLearned, 4><<<(m.nleaf + 3) / 4, 128, 0, s>>>(m, uv, perm, d, kEvalWaitLimit);
+      break;
+    case 1:
+      k_eval_mixed<kLearned, 8><<<(m.nleaf + 7) / 8, 256, 0, s>>>(m, uv, perm, d, kEvalWaitLimit);
+      break;
+    case 2:
+      k_eval_staged<kLearned, 4><<<(m.nleaf + 3) / 4, 128, 0, s>>>(m, uv, perm, d, kEvalWaitLimit);
+      break;
+    default:
+      k_eval_staged<kLearned, 8><<<(m.nleaf + 7) / 8, 256, 0, s>>>(m, uv, perm, d, kEvalWaitLimit);
+      break;
+  }
   g_launches.fetch_add(1, std::memory_order_relaxed);
-  T2D_CUDA_TRY(cudaGetLastError());
-  return TREE2D_OK;
+  return cudaGetLastError();
 }
 
+// The near field with the variant the tuner chose for this size class: on
+// the first solve of a (device, form, P, leaf-count octave) class every
+// variant runs once, timed by CUDA events on the stream, and the fastest is
+// kept (each run writes the same velocities, so the last one stands).
+int near_field(Workspace &ws, const MixedParams &mp, MixedView &m, bool learned, Decisions d, double *uv,
+               const int *perm, cudaStream_t s, tree2d_stats_t &st) {
+  auto run = [&](int v) {
+    return learned ? launch_eval<true>(v, m, uv, perm, d, s) : launch_eval<false>(v, m, uv, perm, d, s);
+  };
+  int v = mp.eval_variant;
+  if (v < 0 && mp.autotune) {
+    int dev = 0;
+    T2D_CUDA_TRY(cudaGetDevice(&dev));
+    int octave = 0;
+    while (octave < 40 && (1ll << (octave + 1)) <= (long long)m.nleaf) octave++;
+    const uint64_t key = ((uint64_t)dev << 40) | ((uint64_t)(learned ? 1 : 0) << 32) | ((uint64_t)m.P << 16) |
+                         (uint64_t)octave;
+    auto it = ws.eval_tuned.find(key);
+    if (it != ws.eval_tuned.end()) {
+      v = it->second;
+    } else {
+      float best = 0.f;
+      int bv = 0;
+      for (int c = 0; c < kEvalVariants; c++) {
+        T2D_CUDA_TRY(cudaMemsetAsync(&ws.status->n_pairs, 0, sizeof(unsigned long long), s));
+        T2D_CUDA_TRY(cudaEventRecord(ws.ev[6], s));
+        T2D_CUDA_TRY(run(c));
+        T2D_CUDA_TRY(cudaEventRecord(ws.ev[7], s));
+        T2D_CUDA_TRY(cudaEventSynchronize(ws.ev[7]));
+        float ms = 0.f;
+        T2D_CUDA_TRY(cudaEventElapsedTime(&ms, ws.ev[6], ws.ev[7]));
+        if (c == 0 || ms < best) {
+          best = ms;
+          bv = c;
+        }
+      }
+      ws.eval_tuned[key] = bv;
+      st.eval_variant = bv;
+      return TREE2D_OK;
+    }
+  }
+  if (v < 0 || v >= kEvalVariants) v = 0;
+  T2D_CUDA_TRY(run(v));
+  st.eval_variant = v;
+  return TREE2D_OK;
+}
 
 int mixed_solve(Workspace &ws, const Tree &t, const MixedParams &mp, double *d_uv, cudaStream_t s,
                 tree2d_stats_t &st) {
@@ -990,6 +1217,7 @@ int mixed_solve(Workspace &ws, const Tree &t, const MixedParams &mp, double *d_u
   need += Arena::bytes_for((size_t)nc * 27, 4) + Arena::bytes_for((size_t)nc * 8, 4);
   need += Arena::bytes_for((size_t)nl + 1, 4) * 3;
   need += Arena::bytes_for(3 * ((size_t)nl / kScanTile3 + 2), 4);  // scan tile sums
+  need += Arena::bytes_for((size_t)t.nsets, 4);                     // cutoff per set
   need += Arena::bytes_for((size_t)nc * 2 * P, 4) * 2;
   need += Arena::bytes_for((size_t)nc * 4, 4) + 1024;  // class lists + counts
   need += 256;
@@ -1036,17 +1264,26 @@ int mixed_solve(Workspace &ws, const Tree &t, const MixedParams &mp, double *d_u
   m.M = ws.mx_arena.take<float>((size_t)nc * 2 * P);
   m.L = ws.mx_arena.take<float>((size_t)nc * 2 * P);
   unsigned *rc_bits = ws.mx_arena.take<unsigned>(1);
+  unsigned *rc_set_bits = t.nsets > 1 ? ws.mx_arena.take<unsigned>((size_t)t.nsets) : nullptr;
   int *cls_list = ws.mx_arena.take<int>((size_t)nc * 4);
   int *cls_count = ws.mx_arena.take<int>(4);
   m.rc_ptr = reinterpret_cast<const float *>(rc_bits);
+  m.rc_set = reinterpret_cast<const float *>(rc_set_bits);
+  m.lev0 = t.lev0;
   m.m2m = reinterpret_cast<const float2 *>(dm2m);
   m.l2l = reinterpret_cast<const float2 *>(dl2l);
   m.st = ws.status;
   T2D_CUDA_TRY(cudaMemsetAsync(m.parent, 0xff, sizeof(int) * (size_t)nc, s));
   T2D_CUDA_TRY(cudaMemsetAsync(rc_bits, 0, 4, s));
   k_sigma_max<<<304, 256, 0, s>>>(t.cor, n, rc_bits);
-  k_cutoff<<<1, 1, 0, s>>>(rc_bits, (float)mp.cutoff);
+  k_cutoff<<<1, 32, 0, s>>>(rc_bits, (float)mp.cutoff, 1);
   g_launches.fetch_add(2, std::memory_order_relaxed);
+  if (rc_set_bits) {
+    T2D_CUDA_TRY(cudaMemsetAsync(rc_set_bits, 0, 4 * (size_t)t.nsets, s));
+    k_sigma_max_sets<<<t.nsets, 256, 0, s>>>(t.set_cor, t.set_off, rc_set_bits);
+    k_cutoff<<<(t.nsets + 255) / 256, 256, 0, s>>>(rc_set_bits, (float)mp.cutoff, t.nsets);
+    g_launches.fetch_add(2, std::memory_order_relaxed);
+  }
 
   int rc = mixed_leaf_setup(m, t, s);
   if (rc) return rc;
@@ -1082,9 +1319,11 @@ int mixed_solve(Workspace &ws, const Tree &t, const MixedParams &mp, double *d_u
   ws.mx_tot[0] = tot[0];
   ws.mx_tot[1] = tot[1];
   ws.mx_tot[2] = tot[2];
-  const bool learned = mp.learned && mp.lp && mp.lp->have_weights;
+  // (a batched tree runs the fixed mixed form: the network's reference
+  // scale u_ref is one per tree)
+  const bool learned = mp.learned && mp.lp && mp.lp->have_weights && t.lev0 == 0;
   unsigned char *u_dec = nullptr, *k_dec = nullptr;
-  if (learned || mp.learned) {
+  if ((learned || mp.learned) && t.lev0 == 0) {
     // leaf statistics and u_ref (also used by sampling), then decisions
     const size_t wim = learn_weight_image_elems();
     size_t need = Arena::bytes_for(wim, 2) + Arena::bytes_for(208, 4) + Arena::bytes_for((size_t)nc, sizeof(LeafStats)) +
@@ -1117,19 +1356,10 @@ int mixed_solve(Workspace &ws, const Tree &t, const MixedParams &mp, double *d_u
     }
   }
   T2D_CUDA_TRY(cudaEventRecord(ws.ev[4], s));
-  rc = learned ? learned_evaluate(m, u_dec, k_dec, mp.lp->order_margin, d_uv, t.perm, s)
-               : mixed_evaluate(m, d_uv, t.perm, s);
+  const Decisions dec = learned ? Decisions{u_dec, k_dec, mp.lp->order_margin} : Decisions{nullptr, nullptr, 0};
+  rc = near_field(ws, mp, m, learned, dec, d_uv, t.perm, s, st);
   if (rc) return rc;
   T2D_CUDA_TRY(cudaEventRecord(ws.ev[5], s));
-  return TREE2D_OK;
-}
-
-int learned_evaluate(MixedView &m, const unsigned char *u_dec, const unsigned char *k_dec, int order_margin,
-                     double *uv, const int *perm, cudaStream_t s) {
-  Decisions d{u_dec, k_dec, order_margin};
-  k_eval_mixed<true><<<(int)(((long)m.nleaf * 32 + 127) / 128), 128, 0, s>>>(m, uv, perm, d);
-  g_launches.fetch_add(1, std::memory_order_relaxed);
-  T2D_CUDA_TRY(cudaGetLastError());
   return TREE2D_OK;
 }
 

@@ -13,6 +13,8 @@ constexpr int kMaxP = 32;  // largest expansion length of the mixed form
 struct MixedView {
   int n, ncell, nleaf, P;
   const float *rc_ptr;  // device: cutoff radius of the regularisation correction
+  const float *rc_set;  // batched sets: cutoff radius per set (else null)
+  int lev0;             // batched sets: levels of container cells above the set roots
   // from the tree
   const uint64_t *keys;
   const uint8_t *cpl, *leaf_level;
@@ -47,7 +49,6 @@ int mixed_lists(MixedView &m, cudaStream_t s);
 int mixed_fill_lists(MixedView &m, cudaStream_t s);
 int mixed_upward(MixedView &m, int depth, cudaStream_t s);
 int mixed_downward(MixedView &m, int depth, cudaStream_t s);
-int mixed_evaluate(MixedView &m, double *uv, const int *perm, cudaStream_t s);
 
 // M2L over the V lists (m2l.cu): L[c] += sum_s T(class(c), s) M[V[c][s]].
 // `tables` is the device copy of the [4][27][P][P] complex operators.

@@ -131,11 +131,14 @@ __global__ void __launch_bounds__(kEvalWarps * 32) k_eval(EvalArgs a) {
         for (int j = b; j < e; j++) {
           const double rx = __dsub_rn(x, t.x[j]);
           const double ry = __dsub_rn(y, t.y[j]);
-          const double r = __dsqrt_rn(__dadd_rn(__dmul_rn(rx, rx), __dmul_rn(ry, ry)));
-          if (r > 1.0e-10) {
-            const double rv2 = 1.0 / __dmul_rn(r, r);
-            const double xai = r / t.cor[j];
-            const double x2 = __dmul_rn(xai, xai);
+          // The reference forms r = sqrt(r2), (r/sigma)^2 and 1/(r*r); here
+          // r2 and r2/sigma^2 (with 1/sigma^2 precomputed per blob) give the
+          // same quantities within an ulp or two and save the square root
+          // and a division per pair.  r > 1e-10 <=> r2 > 1e-20.
+          const double r2 = __dadd_rn(__dmul_rn(rx, rx), __dmul_rn(ry, ry));
+          if (r2 > 1.0e-20) {
+            const double rv2 = 1.0 / r2;
+            const double x2 = __dmul_rn(r2, t.icor2[j]);
             // 1 - exp(-x2) rounds to exactly 1.0 once exp(-x2) < 2^-54
             // (x2 > 37.4); the shortcut keeps the result bit-identical.
             const double e1 = x2 > 40.0 ? 1.0 : 1.0 - exp(-x2);

@@ -136,6 +136,9 @@ typedef struct {
   double ms_total;
   long long n_launches;   /* kernels launched by the solve            */
   int m2l_path;           /* mixed: 1 = CUDA cores, 2 = tensor cores  */
+  int eval_variant;       /* mixed: near-field kernel variant that ran
+                             (0/1: global loads, 4/8 warps per block;
+                              2/3: blobs staged by bulk copies, 4/8)    */
 } tree2d_stats_t;
 int tree2d_get_stats(tree2d_stats_t *out);
 
@@ -153,6 +156,27 @@ long long tree2d_export_tree(int *perm, long long cap, int *level, int *begin, i
  * approximate modes): targets and sources in device memory. */
 int tree2d_direct_device(int ntgt, const double *d_txy, int nsrc, const double *d_sxy,
                          const double *d_cir, const double *d_cor, double *d_uv, void *stream);
+
+/* Near-field kernel tuning of the mixed/learned forms.  The variants give
+ * bit-identical results and differ only in speed: source blobs read from
+ * global memory or staged in shared memory by bulk copies, 4 or 8 warps
+ * per block.  autotune = 1 (default): the first solve of each (device,
+ * form, P, leaf-count class) times every variant with CUDA events and keeps
+ * the fastest; eval_variant >= 0 forces one (0..3); eval_variant = -1 with
+ * autotune = 0 runs variant 0.  No counterpart in the reference. */
+int tree2d_set_tuning(int autotune, int eval_variant);
+
+/* Batched solve of nsets independent blob sets in one tree: set k is blobs
+ * [set_offsets[k], set_offsets[k+1]) of the device arrays (set_offsets is a
+ * host array of nsets + 1 ints, set_offsets[0] = 0, non-decreasing).  Each
+ * set gets its own root box and exactly the cells, lists and cutoff it would
+ * get alone, so every set's velocities equal those of solving it by itself;
+ * the sets share every launch (one tree build, one pass of each expansion
+ * kernel, one evaluation).  Mixed form only: TREE2D_ERR_MODE in the plain
+ * mode or with a mirror wall (the learned mode runs the fixed mixed form
+ * here).  No counterpart in the reference. */
+int tree2d_solve_sets(int nsets, const int *set_offsets, const double *d_xy, const double *d_cir,
+                      const double *d_cor, double *d_uv, void *stream);
 
 /* Measures the FP64 FMA pipe: runs blocks x 256 threads x iters x 8
  * dependent-chain FMAs on `stream` and returns the elapsed device time in

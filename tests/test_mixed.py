@@ -79,3 +79,50 @@ def test_tensor_core_m2l_matches_cuda_core_m2l(gpu_lib):
     diff = np.linalg.norm(uv_tc - uv_cc) / np.linalg.norm(uv_cc)
     assert diff <= 1e-6, diff
     assert rel_tc <= REL_L2 and rel_cc <= REL_L2, (rel_tc, rel_cc)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("mode", ["mixed", "learned"])
+def test_near_field_variants_bit_identical(gpu_lib, mode):
+    """The tuner's near-field variants (global loads / bulk-copy staging,
+    4 / 8 warps per block) give the same velocities bit for bit, and the
+    tuner picks one of them."""
+    torch = pytest.importorskip("torch")
+    import importlib
+    P = gpu_lib
+    W = importlib.import_module("2dfmm_gb300.workloads")
+    L = importlib.import_module("2dfmm_gb300.learn")
+    b = W.lamb_oseen(131_072, seed=8)
+    P.set_params(b.nterms, b.num_p, b.theta)
+    P.set_mixed_params(16, 3.0, True)
+    if mode == "learned":
+        theta = L.load_weights()
+        if theta is None:
+            pytest.skip("no packaged weights")
+        P.learn_set_weights(theta)
+    P.set_mode(P.MODE_LEARNED if mode == "learned" else P.MODE_MIXED)
+    dev = torch.device("cuda:0")
+    xy = torch.from_numpy(b.xy).to(dev)
+    cir = torch.from_numpy(b.cir).to(dev)
+    cor = torch.from_numpy(b.cor).to(dev)
+    outs = []
+    try:
+        for v in range(4):
+            P.set_tuning(False, v)
+            uv = torch.empty_like(xy)
+            P.solve_device(xy.data_ptr(), cir.data_ptr(), cor.data_ptr(), uv.data_ptr(), b.n)
+            torch.cuda.synchronize()
+            assert P.stats()["eval_variant"] == v
+            outs.append((uv.cpu().numpy(), P.stats()["n_pairs"]))
+        for uv, npairs in outs[1:]:
+            assert np.array_equal(uv, outs[0][0]) and npairs == outs[0][1]
+        P.set_tuning(True, -1)
+        for _ in range(2):  # the first solve tunes, the second uses the choice
+            uv = torch.empty_like(xy)
+            P.solve_device(xy.data_ptr(), cir.data_ptr(), cor.data_ptr(), uv.data_ptr(), b.n)
+            torch.cuda.synchronize()
+            assert np.array_equal(uv.cpu().numpy(), outs[0][0])
+            assert 0 <= P.stats()["eval_variant"] <= 3 and P.stats()["n_pairs"] == outs[0][1]
+    finally:
+        P.set_tuning(True, -1)
+        P.set_mode(P.MODE_PLAIN)
