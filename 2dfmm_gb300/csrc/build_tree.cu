@@ -638,7 +638,7 @@ int build_tree(Workspace &ws, int n, const double *d_xy, const double *d_cir, co
   if (batched) {
     lev0 = 1;
     while ((1ll << (2 * (lev0 - 1))) < (long long)nsets) lev0++;
-    if (lev0 + kShortKeyLevels > kKeyLevels) return TREE2D_ERR_TOO_LARGE;
+    if (lev0 + 12 > kKeyLevels) return TREE2D_ERR_TOO_LARGE;
   }
   t.nsets = batched ? nsets : 1;
   t.lev0 = lev0;
@@ -693,7 +693,15 @@ int build_tree(Workspace &ws, int n, const double *d_xy, const double *d_cir, co
   uint64_t *ctab = ws.tmp_arena.take<uint64_t>(2 * centre_entries(tlev) * t.nsets);
   int *set_of = batched ? ws.tmp_arena.take<int>(n) : nullptr;
 
-  int levels = kShortKeyLevels;  // digits below the set root
+  // Digits below the set root on the first attempt: as few as the tree is
+  // likely to need (the previous tree's depth + 2, at least 16 for one set
+  // and 12 per set in a batch), so that the keys come from the centre table
+  // alone and the sort makes fewer passes.  A deeper tree is caught by the
+  // leaf-level pass and rebuilt with the full 32-digit keys.
+  const int floor_levels = batched ? 12 : 16;
+  int levels = ws.last_depth - lev0 + 2;
+  if (levels < floor_levels) levels = floor_levels;
+  if (levels > kShortKeyLevels) levels = kShortKeyLevels;
 retry:
   T2D_CUDA_TRY(cudaMemsetAsync(ws.status, 0, sizeof(DevStatus), s));
 
@@ -741,6 +749,7 @@ retry:
     goto retry;
   }
   t.key_levels = total_levels;
+  ws.last_depth = ws.h_status->depth;
   unsigned long long tot = *h_total;
   long long ncell = 1 + (long long)(tot >> 32);
   long long nleaf = (long long)(tot & 0xffffffffu);

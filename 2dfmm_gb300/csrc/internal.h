@@ -142,6 +142,7 @@ struct Workspace {
   MixedView *mxv = nullptr;  // the last mixed solve's view (kept for sampling)
   long mx_tot[3] = {0, 0, 0};  // U, W, K list entries of that solve
   std::map<uint64_t, int> eval_tuned;  // size class -> fastest near-field variant
+  int last_depth = 0;  // depth of the last tree built (sizes the next keys)
   DevStatus *status = nullptr;   // device
   DevStatus *h_status = nullptr; // pinned host mirror
   cudaEvent_t ev[8] = {};

@@ -498,31 +498,53 @@ __device__ __forceinline__ float2 fmul(float2 a, float2 b) {
   return make_float2(fmaf(a.x, b.x, -__fmul_rn(a.y, b.y)), fmaf(a.x, b.y, __fmul_rn(a.y, b.x)));
 }
 
-// S2M: one warp per leaf, lane k owns a_k (k < P <= 32).
-__global__ void k_s2m_f32(MixedView m) {
+// Coefficients are formed in chunks of kCoefChunk: every lane takes its own
+// blobs and accumulates the chunk's terms for them in registers, then the
+// warp sums the 32 lanes' partials through shared memory (lane t ends with
+// the real (t even) or imaginary (t odd) part of coefficient t/2 of the
+// chunk).  This costs one transposed reduction per chunk instead of a
+// shuffle scan per blob.
+constexpr int kCoefChunk = 16;
+constexpr int kCoefPitch = 2 * kCoefChunk + 1;  // padded row of the reduction buffer
+
+__device__ __forceinline__ float warp_chunk_sum(const float (&acc)[2 * kCoefChunk], float *sh, int lane) {
+#pragma unroll
+  for (int i = 0; i < 2 * kCoefChunk; i++) sh[lane * kCoefPitch + i] = acc[i];
+  __syncwarp();
+  float s = 0.f;
+  for (int r = 0; r < 32; r++) s += sh[r * kCoefPitch + lane];
+  __syncwarp();
+  return s;
+}
+
+// S2M: one warp per leaf, a_k = sum_j G_j ((z_j - c)/h)^k.
+__global__ void __launch_bounds__(256) k_s2m_f32(MixedView m) {
+  __shared__ float sh[8][32 * kCoefPitch];
   const int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   if (wid >= m.nleaf) return;
+  float *buf = sh[threadIdx.x >> 5];
   const int c = m.leaf_cell[wid];
   const float ih = m.inv_h[c];
   const int P = m.P;
-  float2 acc = make_float2(0.f, 0.f);
-  for (int j = m.begin[c]; j < m.end[c]; j++) {
-    float2 z = m.loc[j];
-    z.x *= ih;
-    z.y *= ih;
-    // lane k: z^k by a product scan over lanes
-    float2 v = lane == 0 ? make_float2(1.f, 0.f) : z;
-    for (int off = 1; off < 32; off <<= 1) {
-      float2 o = make_float2(__shfl_up_sync(0xffffffffu, v.x, off), __shfl_up_sync(0xffffffffu, v.y, off));
-      if (lane >= off) v = fmul(o, v);
+  for (int c0 = 0; c0 < P; c0 += kCoefChunk) {
+    float acc[2 * kCoefChunk];
+#pragma unroll
+    for (int i = 0; i < 2 * kCoefChunk; i++) acc[i] = 0.f;
+    for (int j = m.begin[c] + lane; j < m.end[c]; j += 32) {
+      const float2 z = make_float2(m.loc[j].x * ih, m.loc[j].y * ih);
+      const float g = m.gam[j];
+      float2 pw = make_float2(1.f, 0.f);
+      for (int k = 0; k < c0; k++) pw = fmul(pw, z);
+#pragma unroll
+      for (int k = 0; k < kCoefChunk; k++) {
+        acc[2 * k] = fmaf(g, pw.x, acc[2 * k]);
+        acc[2 * k + 1] = fmaf(g, pw.y, acc[2 * k + 1]);
+        pw = fmul(pw, z);
+      }
     }
-    const float g = m.gam[j];
-    acc.x += g * v.x;
-    acc.y += g * v.y;
-  }
-  if (lane < P) {
-    m.M[(size_t)c * 2 * P + lane] = acc.x;
-    m.M[(size_t)c * 2 * P + P + lane] = acc.y;
+    const float sum = warp_chunk_sum(acc, buf, lane);
+    const int k = c0 + (lane >> 1);
+    if (k < P) m.M[(size_t)c * 2 * P + ((lane & 1) ? P + k : k)] = sum;
   }
 }
 
@@ -555,38 +577,44 @@ __global__ void k_m2m_f32(MixedView m, int lev) {
   }
 }
 
-// P2L of the X lists: one warp per cell, lane l owns b_l.
-__global__ void k_p2l(MixedView m) {
+// P2L: the blobs of cell c's X leaves (coarser leaves adjacent to its
+// parent, not to c) into c's local expansion, b_l -= G w^(l+1), w = 1/z,
+// z the blob's offset from c's centre in units of c's side.  One warp per
+// cell, lanes over blobs, chunked coefficients as S2M.
+__global__ void __launch_bounds__(256) k_p2l(MixedView m) {
+  __shared__ float sh[8][32 * kCoefPitch];
   const int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   if (c >= m.ncell) return;
   const int *X = m.xlist + (size_t)c * 8;
   if (X[0] < 0) return;
+  float *buf = sh[threadIdx.x >> 5];
   const int P = m.P;
   const float ih = m.inv_h[c];
-  float2 acc = make_float2(0.f, 0.f);
-  for (int e = 0; e < 8 && X[e] >= 0; e++) {
-    const int d = X[e];
-    const float ox = (float)(m.cx[d] - m.cx[c]), oy = (float)(m.cy[d] - m.cy[c]);  // once per X entry
-    for (int j = m.begin[d]; j < m.end[d]; j++) {
-      float2 z = m.loc[j];
-      z.x = (z.x + ox) * ih;
-      z.y = (z.y + oy) * ih;
-      // w = 1/z; lane l: w^(l+1) by a product scan
-      const float r2 = z.x * z.x + z.y * z.y;
-      const float2 w = make_float2(z.x / r2, -z.y / r2);
-      float2 v = w;
-      for (int off = 1; off < 32; off <<= 1) {
-        float2 o = make_float2(__shfl_up_sync(0xffffffffu, v.x, off), __shfl_up_sync(0xffffffffu, v.y, off));
-        if (lane >= off) v = fmul(o, v);
+  for (int c0 = 0; c0 < P; c0 += kCoefChunk) {
+    float acc[2 * kCoefChunk];
+#pragma unroll
+    for (int i = 0; i < 2 * kCoefChunk; i++) acc[i] = 0.f;
+    for (int e = 0; e < 8 && X[e] >= 0; e++) {
+      const int d = X[e];
+      const float ox = (float)(m.cx[d] - m.cx[c]), oy = (float)(m.cy[d] - m.cy[c]);
+      for (int j = m.begin[d] + lane; j < m.end[d]; j += 32) {
+        const float zx = (m.loc[j].x + ox) * ih, zy = (m.loc[j].y + oy) * ih;
+        const float r2 = zx * zx + zy * zy;
+        const float2 w = make_float2(zx / r2, -zy / r2);
+        const float g = m.gam[j];
+        float2 pw = w;
+        for (int k = 0; k < c0; k++) pw = fmul(pw, w);
+#pragma unroll
+        for (int k = 0; k < kCoefChunk; k++) {
+          acc[2 * k] = fmaf(-g, pw.x, acc[2 * k]);
+          acc[2 * k + 1] = fmaf(-g, pw.y, acc[2 * k + 1]);
+          pw = fmul(pw, w);
+        }
       }
-      const float g = m.gam[j];
-      acc.x -= g * v.x;
-      acc.y -= g * v.y;
     }
-  }
-  if (lane < P) {
-    m.L[(size_t)c * 2 * P + lane] += acc.x;
-    m.L[(size_t)c * 2 * P + P + lane] += acc.y;
+    const float sum = warp_chunk_sum(acc, buf, lane);
+    const int k = c0 + (lane >> 1);
+    if (k < P) m.L[(size_t)c * 2 * P + ((lane & 1) ? P + k : k)] += sum;
   }
 }
 

@@ -22,6 +22,21 @@
 namespace t2d {
 namespace {
 
+// 1/x for a positive normal x: the SFU's approximate reciprocal refined by
+// two Newton-Raphson steps for f(y) = 1/y - x, y <- y + y (1 - x y), each
+// with the residual 1 - x y formed by one FMA.  Every step squares the
+// relative error, so the ~2^-20 seed ends within an ulp or so of the
+// correctly rounded 1/x, which is all the 1e-12 bar needs; it replaces the
+// IEEE division of the pair and M2S terms (the FP64 pipe is this kernel's
+// bound).
+__device__ __forceinline__ double rcp_nr(double x) {
+  double y;
+  asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
+  y = fma(y, fma(-x, y, 1.0), y);
+  y = fma(y, fma(-x, y, 1.0), y);
+  return y;
+}
+
 __constant__ double c_binom[kMaxTerms][kMaxTerms];
 
 constexpr double kPi = 3.14159265358979323846;
@@ -137,7 +152,7 @@ __global__ void __launch_bounds__(kEvalWarps * 32) k_eval(EvalArgs a) {
           // and a division per pair.  r > 1e-10 <=> r2 > 1e-20.
           const double r2 = __dadd_rn(__dmul_rn(rx, rx), __dmul_rn(ry, ry));
           if (r2 > 1.0e-20) {
-            const double rv2 = 1.0 / r2;
+            const double rv2 = rcp_nr(r2);
             const double x2 = __dmul_rn(r2, t.icor2[j]);
             // 1 - exp(-x2) rounds to exactly 1.0 once exp(-x2) < 2^-54
             // (x2 > 37.4); the shortcut keeps the result bit-identical.
@@ -170,7 +185,7 @@ __global__ void __launch_bounds__(kEvalWarps * 32) k_eval(EvalArgs a) {
         if (act && !desc && nt >= 2) {
           // M2S, fmm.c:60-67: sum_{k<nt-1} a_k w^{k+1}, w = 1/(z - zc)
           const double d2 = dx * dx + dy * dy;
-          const double inv = 1.0 / d2;
+          const double inv = rcp_nr(d2);
           const double2 w = make_double2(dx * inv, -dy * inv);
           const double2 *cf = t.coef + (size_t)cc * nt;
           double2 acc = cf[nt - 2];
