@@ -69,33 +69,47 @@ struct TcArgs {
   const int *cls_count;  // [4]
   const float *bimg;     // [4][27][2 (hi,lo)][Npad x Kc] core-matrix images
   int P, Kc, Npad, tmem_cols, ngroups;
+  int nbs;               // B stages: 3 (slot i+1's images prefetched) or 2
   long wait_limit;
 };
 
-// Shared memory: 2 stages x {A_hi, A_lo (128 x Kc), B_hi, B_lo (Npad x Kc)}.
+constexpr int kMaxKc4 = 2 * kMaxP / 4;  // float4s in one multipole row (2P floats)
+
+// Shared memory: the tile's V lists [27][128], 2 A stages x {A_hi, A_lo}
+// (128 x Kc each) and nbs B stages x {B_hi, B_lo} (Npad x Kc each).
+//
+// The slots any row of the tile uses are found once (a block-wide OR of the
+// rows' masks), and the walk over them is software-pipelined: while slot i
+// is split into TF32 hi/lo and multiplied, each thread already holds slot
+// i+1's multipole row in registers, and (with 3 B stages) slot i+1's
+// operator images are in flight by bulk copy, so the gather latency is
+// paid once per tile rather than once per slot.
 __global__ void __launch_bounds__(kThreadsTC) k_m2l_tc(TcArgs a) {
   extern __shared__ __align__(1024) unsigned char smem[];
-  __shared__ uint64_t bar_mma[2], bar_b[2];
+  __shared__ uint64_t bar_mma[2], bar_b[3];
   __shared__ uint32_t s_tmem;
   __shared__ int s_fail;
+  __shared__ unsigned s_mask;
 
   const int cls = blockIdx.y;
   const int count = a.cls_count[cls];
   const int row0 = blockIdx.x * kRows;
   if (row0 >= count) return;  // uniform for the block
   const MixedView &m = a.m;
-  const int P = a.P, Kc = a.Kc, Npad = a.Npad;
+  const int P = a.P, Kc = a.Kc, Npad = a.Npad, nbs = a.nbs;
   const uint32_t a_bytes = kRows * Kc * 4, b_bytes = Npad * Kc * 4;
-  const uint32_t stage_bytes = 2 * a_bytes + 2 * b_bytes;
   const uint32_t sbo_a = (Kc / 4) * 128, sbo_b = sbo_a, lbo = 128;
   const int tid = threadIdx.x, warp = tid >> 5;
+  int *sV = reinterpret_cast<int *>(smem);                       // [27][kRows]
+  unsigned char *astage = smem + 27 * kRows * 4;                 // 2 x (hi, lo)
+  unsigned char *bstage = astage + 2 * 2 * a_bytes;              // nbs x (hi, lo)
 
   if (tid == 0) {
     mbar_init(&bar_mma[0], 1);
     mbar_init(&bar_mma[1], 1);
-    mbar_init(&bar_b[0], 1);
-    mbar_init(&bar_b[1], 1);
+    for (int k = 0; k < 3; k++) mbar_init(&bar_b[k], 1);
     s_fail = 0;
+    s_mask = 0u;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 0) {
@@ -112,53 +126,82 @@ __global__ void __launch_bounds__(kThreadsTC) k_m2l_tc(TcArgs a) {
   const int row = row0 + tid;
   const bool valid = row < count;
   const int cell = valid ? a.cls_list[(size_t)cls * m.ncell + row] : -1;
-  const int *V = valid ? m.vlist + (size_t)cell * 27 : nullptr;
+  {
+    unsigned mine = 0u;
+    const int *V = valid ? m.vlist + (size_t)cell * 27 : nullptr;
+    for (int s = 0; s < 27; s++) {
+      const int src = valid ? V[s] : -1;
+      sV[s * kRows + tid] = src;
+      if (src >= 0) mine |= 1u << s;
+    }
+    atomicOr(&s_mask, mine);
+  }
+  __syncthreads();
+  const unsigned mask = s_mask;
+  const int nslots = __popc(mask);
   // M = 128, N = Npad, A/B TF32 K-major, D FP32
   const uint32_t idesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(Npad >> 3) << 17) | ((uint32_t)(kRows >> 4) << 24);
   const float *bbase = a.bimg + (size_t)cls * 27 * 2 * (Npad * Kc);
 
-  uint32_t phase_mma[2] = {0, 0}, phase_b[2] = {0, 0};
+  uint32_t phase_mma[2] = {0, 0}, phase_b[3] = {0, 0, 0};
   bool pending[2] = {false, false};
-  bool b_inflight[2] = {false, false};  // thread 0: bulk copy issued, not yet waited for
+  bool b_inflight[3] = {false, false, false};  // thread 0: bulk copy issued, not yet waited for
   // Slot chunks are spread over `ngroups` accumulators (TMEM column blocks
   // of Npad); each accumulates few MMAs and the partial sums are added in
   // FP32 registers at the end, which keeps the accumulation error small.
   bool gfirst[8] = {true, true, true, true, true, true, true, true};
-  int issued = 0;
-  for (int s = 0; s < 27; s++) {
-    const int src = valid ? V[s] : -1;
-    if (__syncthreads_or(s_fail)) break;         // a wait gave up: stop issuing
-    if (!__syncthreads_or(src >= 0)) continue;  // no row of the tile has this slot
-    const int st = issued & 1;
-    unsigned char *stage = smem + st * stage_bytes;
-    float *Ahi = reinterpret_cast<float *>(stage);
-    float *Alo = reinterpret_cast<float *>(stage + a_bytes);
-    float *Bhi = reinterpret_cast<float *>(stage + 2 * a_bytes);
-    float *Blo = reinterpret_cast<float *>(stage + 2 * a_bytes + b_bytes);
-    // the MMAs that last read this stage must be done before it is rewritten
-    if (pending[st]) {
-      if (mbar_wait(&bar_mma[st], phase_mma[st], a.wait_limit)) {
-        phase_mma[st] ^= 1;
-        pending[st] = false;
+  auto slot_at = [&](unsigned rest) { return __ffs(rest) - 1; };  // lowest remaining slot
+  auto copy_b = [&](int slot, int bs) {
+    if (tid != 0) return;
+    mbar_expect_tx(&bar_b[bs], 2 * b_bytes);
+    bulk_g2s(bstage + (size_t)bs * 2 * b_bytes, bbase + (size_t)slot * 2 * (Npad * Kc), 2 * b_bytes, &bar_b[bs]);
+    b_inflight[bs] = true;
+  };
+  auto load_row = [&](int slot, float4 (&r)[kMaxKc4]) {
+    const int src = sV[slot * kRows + tid];
+    const float4 *msrc = src >= 0 ? reinterpret_cast<const float4 *>(m.M + (size_t)src * 2 * P) : nullptr;
+#pragma unroll
+    for (int kk = 0; kk < kMaxKc4; kk++)
+      r[kk] = (msrc && kk < Kc / 4) ? msrc[kk] : make_float4(0.f, 0.f, 0.f, 0.f);
+  };
+
+  unsigned rest = mask;
+  float4 cur[kMaxKc4], nxt[kMaxKc4];
+  int slot = -1, issued = 0;
+  if (nslots > 0) {
+    slot = slot_at(rest);
+    rest &= rest - 1;
+    load_row(slot, cur);
+    copy_b(slot, 0);
+  }
+  for (int i = 0; i < nslots; i++) {
+    const int ast = i & 1, bs = i % nbs;
+    const int next = rest ? slot_at(rest) : -1;
+    if (next >= 0) load_row(next, nxt);  // in flight while this slot is staged and multiplied
+    // the MMAs that last read this A stage (and, with 3 B stages, the B
+    // stage of slot i+1) must be done before they are rewritten
+    if (pending[ast]) {
+      if (mbar_wait(&bar_mma[ast], phase_mma[ast], a.wait_limit)) {
+        phase_mma[ast] ^= 1;
+        pending[ast] = false;
       } else {
         s_fail = 1;
       }
     }
     if (__syncthreads_or(s_fail)) break;
-    // B chunk: one bulk copy of the pre-laid-out hi and lo images
-    if (tid == 0) {
-      mbar_expect_tx(&bar_b[st], 2 * b_bytes);
-      const float *bsrc = bbase + (size_t)s * 2 * (Npad * Kc);
-      bulk_g2s(Bhi, bsrc, 2 * b_bytes, &bar_b[st]);
-      b_inflight[st] = true;
+    if (nbs == 3 && next >= 0) copy_b(next, (i + 1) % 3);
+    if (nbs == 2) {
+      if (i > 0) copy_b(slot, bs);  // slot 0's copy went out before the loop
     }
     // A chunk: this thread's row, split into TF32 hi and lo
     {
-      const int r = tid;
-      const uint32_t rbase = (uint32_t)(r >> 3) * sbo_a + (uint32_t)(r & 7) * 16;
-      const float4 *msrc = src >= 0 ? reinterpret_cast<const float4 *>(m.M + (size_t)src * 2 * P) : nullptr;
-      for (int kk = 0; kk < Kc / 4; kk++) {
-        float4 v = msrc ? msrc[kk] : make_float4(0.f, 0.f, 0.f, 0.f);
+      float *Ahi = reinterpret_cast<float *>(astage + (size_t)ast * 2 * a_bytes);
+      float *Alo = reinterpret_cast<float *>(astage + (size_t)ast * 2 * a_bytes + a_bytes);
+      const uint32_t rbase = (uint32_t)(tid >> 3) * sbo_a + (uint32_t)(tid & 7) * 16;
+#pragma unroll
+      for (int kk = 0; kk < kMaxKc4; kk++) {
+        if (kk >= Kc / 4) break;
+        const float4 v = cur[kk];
         float4 h, l;
         h.x = __uint_as_float(tf32_bits(v.x));
         h.y = __uint_as_float(tf32_bits(v.y));
@@ -177,17 +220,18 @@ __global__ void __launch_bounds__(kThreadsTC) k_m2l_tc(TcArgs a) {
     __syncthreads();
     bool b_ok = true;
     if (tid == 0) {
-      b_ok = mbar_wait(&bar_b[st], phase_b[st], a.wait_limit);
+      b_ok = mbar_wait(&bar_b[bs], phase_b[bs], a.wait_limit);
       if (b_ok) {
-        phase_b[st] ^= 1;
-        b_inflight[st] = false;
+        phase_b[bs] ^= 1;
+        b_inflight[bs] = false;
       } else {
         s_fail = 1;
       }
     }
     if (tid == 0 && b_ok) {
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      const uint32_t ah = smem_u32(Ahi), al = smem_u32(Alo), bh = smem_u32(Bhi), bl = smem_u32(Blo);
+      const uint32_t ah = smem_u32(astage + (size_t)ast * 2 * a_bytes), al = ah + a_bytes;
+      const uint32_t bh = smem_u32(bstage + (size_t)bs * 2 * b_bytes), bl = bh + b_bytes;
       const int g = issued % a.ngroups;
       const uint32_t dcol = tmem + (uint32_t)(g * Npad);
       for (int t = 0; t < Kc / 8; t++) {
@@ -199,12 +243,17 @@ __global__ void __launch_bounds__(kThreadsTC) k_m2l_tc(TcArgs a) {
         mma_tf32(dcol, dah, dbl, idesc, 1u);
         mma_tf32(dcol, dal, dbh, idesc, 1u);
       }
-      mma_commit(&bar_mma[st]);
+      mma_commit(&bar_mma[ast]);
     }
     // every thread marks the stage busy only if its MMAs were issued
-    if (!__syncthreads_or(!b_ok)) {
-      pending[st] = true;
-      issued++;
+    if (__syncthreads_or(!b_ok)) break;
+    pending[ast] = true;
+    issued++;
+    if (next >= 0) {
+#pragma unroll
+      for (int kk = 0; kk < kMaxKc4; kk++) cur[kk] = nxt[kk];
+      slot = next;
+      rest &= rest - 1;
     }
   }
   // drain: every stage with MMAs in flight (bounded; a failed wait is
@@ -244,12 +293,12 @@ __global__ void __launch_bounds__(kThreadsTC) k_m2l_tc(TcArgs a) {
     }
   }
   if (s_fail) {
-    // a wait gave up: give MMAs still in flight one more bounded wait
-    // before the TMEM and shared memory are released
-    for (int st = 0; st < 2; st++) {
+    // a wait gave up: give MMAs and copies still in flight one more bounded
+    // wait before the TMEM and shared memory are released
+    for (int st = 0; st < 2; st++)
       if (pending[st]) mbar_wait(&bar_mma[st], phase_mma[st], a.wait_limit);
-      if (tid == 0 && b_inflight[st]) mbar_wait(&bar_b[st], phase_b[st], a.wait_limit);
-    }
+    for (int bs = 0; bs < 3; bs++)
+      if (tid == 0 && b_inflight[bs]) mbar_wait(&bar_b[bs], phase_b[bs], a.wait_limit);
   }
   if (s_fail && tid == 0) set_err(m.st, TREE2D_ERR_TIMEOUT);
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -260,12 +309,22 @@ __global__ void __launch_bounds__(kThreadsTC) k_m2l_tc(TcArgs a) {
 
 // Cells of level >= 2 (below their set root), grouped by child class (order within a class is
 // irrelevant: every row's sum is its own).
+// One atomic per warp and class (the lanes of a class take consecutive
+// positions in ballot order).
 __global__ void k_class_lists(MixedView m, int *list, int *count) {
-  int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= m.ncell || m.level[c] - m.lev0 < 2) return;
-  const int cls = (m.ix[c] & 1) + 2 * (m.iy[c] & 1);
-  const int pos = atomicAdd(&count[cls], 1);
-  list[(size_t)cls * m.ncell + pos] = c;
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  const bool in = c < m.ncell && m.level[c] - m.lev0 >= 2;
+  const int cls = in ? (int)((m.ix[c] & 1) + 2 * (m.iy[c] & 1)) : -1;
+  for (int k = 0; k < 4; k++) {
+    const unsigned bal = __ballot_sync(0xffffffffu, cls == k);
+    if (!bal) continue;
+    const int leader = __ffs(bal) - 1;
+    int base = 0;
+    if (lane == leader) base = atomicAdd(&count[k], __popc(bal));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (cls == k) list[(size_t)k * m.ncell + base + __popc(bal & ((1u << lane) - 1u))] = c;
+  }
 }
 
 uint32_t tf32_round_host(float x) {
@@ -333,7 +392,10 @@ int m2l_tensor_cores(MixedView &m, const float *bimg, int *cls_list, int *cls_co
   a.tmem_cols = 256;                            // two CTAs per SM fill the 512 columns
   a.ngroups = 256 / Npad < 8 ? 256 / Npad : 8;
   a.wait_limit = 1l << 22;  // polls; a healthy wait ends within microseconds
-  const size_t smem = 2 * (2 * (size_t)kRows * Kc * 4 + 2 * (size_t)Npad * Kc * 4);
+  const size_t fixed = (size_t)27 * kRows * 4 + 2 * (2 * (size_t)kRows * Kc * 4);
+  const size_t bst = 2 * (size_t)Npad * Kc * 4;
+  a.nbs = fixed + 3 * bst <= 110 * 1024 ? 3 : 2;  // 3 B stages while two CTAs still fit an SM
+  const size_t smem = fixed + (size_t)a.nbs * bst;
   T2D_CUDA_TRY(cudaFuncSetAttribute(k_m2l_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   dim3 grid((m.ncell + kRows - 1) / kRows, 4);
   k_m2l_tc<<<grid, kThreadsTC, smem, s>>>(a);

@@ -255,6 +255,44 @@ __global__ void k_sigma_max_sets(const double *cor, const int *off, unsigned *ou
   if ((threadIdx.x & 31) == 0) atomicMax(out + set, __float_as_uint(mx));
 }
 
+// Cells grouped by level (a counting sort), so that the per-level
+// expansion passes visit only their own level's cells.  level_off[l] holds
+// the count of level l-1 first, then the exclusive offsets, and
+// level_off[kKeyLevels + 2 + l] is the fill cursor of level l.
+__global__ void k_level_hist(MixedView m) {
+  __shared__ int h[kKeyLevels + 1];
+  for (int i = threadIdx.x; i <= kKeyLevels; i += blockDim.x) h[i] = 0;
+  __syncthreads();
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c < m.ncell) atomicAdd(&h[m.level[c]], 1);
+  __syncthreads();
+  for (int i = threadIdx.x; i <= kKeyLevels; i += blockDim.x)
+    if (h[i]) atomicAdd(&m.level_off[i + 1], h[i]);
+}
+
+__global__ void k_level_scan(MixedView m) {
+  if (threadIdx.x != 0) return;
+  int run = 0;
+  for (int l = 0; l <= kKeyLevels; l++) {
+    run += m.level_off[l + 1];
+    m.level_off[l + 1] = run;
+    m.level_off[kKeyLevels + 2 + l] = m.level_off[l];
+  }
+}
+
+// One atomic per warp and level: lanes of equal level share a reservation.
+__global__ void k_level_fill(MixedView m) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  const int lev = c < m.ncell ? m.level[c] : -1;
+  const unsigned grp = __match_any_sync(0xffffffffu, lev);
+  const int leader = __ffs(grp) - 1;
+  int base = 0;
+  if (lev >= 0 && lane == leader) base = atomicAdd(&m.level_off[kKeyLevels + 2 + lev], __popc(grp));
+  base = __shfl_sync(0xffffffffu, base, leader);
+  if (lev >= 0) m.by_level[base + __popc(grp & ((1u << lane) - 1u))] = c;
+}
+
 __global__ void k_parent(MixedView m) {
   int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= m.ncell) return;
@@ -552,8 +590,11 @@ __global__ void __launch_bounds__(256) k_s2m_f32(MixedView m) {
 __global__ void k_m2m_f32(MixedView m, int lev) {
   const int lane = threadIdx.x & 31;
   const int P = m.P;
-  for (int p = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; p < m.ncell; p += (gridDim.x * blockDim.x) >> 5) {
-    if (m.level[p] != lev || m.leaf[p]) continue;
+  const int *cells = m.by_level + m.level_off[lev];
+  const int cnt = m.level_off[lev + 1] - m.level_off[lev];
+  for (int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < cnt; i += (gridDim.x * blockDim.x) >> 5) {
+    const int p = cells[i];
+    if (m.leaf[p]) continue;
     const int4 ch = reinterpret_cast<const int4 *>(m.child)[p];
     float2 acc = make_float2(0.f, 0.f);
     for (int q = 0; q < 4; q++) {
@@ -622,8 +663,11 @@ __global__ void __launch_bounds__(256) k_p2l(MixedView m) {
 __global__ void k_l2l_f32(MixedView m, int lev) {
   const int lane = threadIdx.x & 31;
   const int P = m.P;
-  for (int p = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; p < m.ncell; p += (gridDim.x * blockDim.x) >> 5) {
-    if (m.level[p] != lev - 1 || m.leaf[p]) continue;
+  const int *cells = m.by_level + m.level_off[lev - 1];
+  const int cnt = m.level_off[lev] - m.level_off[lev - 1];
+  for (int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < cnt; i += (gridDim.x * blockDim.x) >> 5) {
+    const int p = cells[i];
+    if (m.leaf[p]) continue;
     const float *src = m.L + (size_t)p * 2 * P;
     float2 b = lane < P ? make_float2(src[lane], src[P + lane]) : make_float2(0.f, 0.f);
     const int4 ch = reinterpret_cast<const int4 *>(m.child)[p];
@@ -1078,6 +1122,11 @@ cudaError_t mixed_tables(int P, float *h_m2l, float *h_m2m, float *h_l2l) {
 int mixed_lists(MixedView &m, cudaStream_t s) {
   const int cb = (m.ncell + 255) / 256;
   k_cell_info<<<cb, 256, 0, s>>>(m);
+  T2D_CUDA_TRY(cudaMemsetAsync(m.level_off, 0, sizeof(int) * (2 * kKeyLevels + 4), s));
+  k_level_hist<<<cb, 256, 0, s>>>(m);
+  k_level_scan<<<1, 32, 0, s>>>(m);
+  k_level_fill<<<cb, 256, 0, s>>>(m);
+  g_launches.fetch_add(3, std::memory_order_relaxed);
   k_parent<<<cb, 256, 0, s>>>(m);
   k_colleagues<<<cb, 256, 0, s>>>(m);
   k_vx_lists<<<cb, 256, 0, s>>>(m);
@@ -1246,6 +1295,7 @@ int mixed_solve(Workspace &ws, const Tree &t, const MixedParams &mp, double *d_u
   need += Arena::bytes_for((size_t)nl + 1, 4) * 3;
   need += Arena::bytes_for(3 * ((size_t)nl / kScanTile3 + 2), 4);  // scan tile sums
   need += Arena::bytes_for((size_t)t.nsets, 4);                     // cutoff per set
+  need += Arena::bytes_for(nc, 4) + Arena::bytes_for(2 * kKeyLevels + 4, 4);  // cells by level
   need += Arena::bytes_for((size_t)nc * 2 * P, 4) * 2;
   need += Arena::bytes_for((size_t)nc * 4, 4) + 1024;  // class lists + counts
   need += 256;
@@ -1289,6 +1339,8 @@ int mixed_solve(Workspace &ws, const Tree &t, const MixedParams &mp, double *d_u
   m.w_off = ws.mx_arena.take<int>((size_t)nl + 1);
   m.k_off = ws.mx_arena.take<int>((size_t)nl + 1);
   m.scan_tmp = ws.mx_arena.take<int>(3 * ((size_t)nl / kScanTile3 + 2));
+  m.by_level = ws.mx_arena.take<int>(nc);
+  m.level_off = ws.mx_arena.take<int>(2 * kKeyLevels + 4);
   m.M = ws.mx_arena.take<float>((size_t)nc * 2 * P);
   m.L = ws.mx_arena.take<float>((size_t)nc * 2 * P);
   unsigned *rc_bits = ws.mx_arena.take<unsigned>(1);

@@ -36,6 +36,8 @@ struct MixedView {
   int *xlist;            // 8 per cell
   int *u_off, *w_off, *k_off;  // per leaf (+1)
   int *scan_tmp;               // tile sums of the list-size scan
+  int *by_level;               // cell ids grouped by level (order within a level arbitrary)
+  int *level_off;              // [kKeyLevels + 2]: start of each level in by_level, then cursors
   int *u_idx, *w_idx, *k_idx;
   int *u_leaf, *k_leaf;  // leaf ordinal of each U / K entry
   float *M, *L;          // per cell, 2P floats (re[P], im[P])
