@@ -119,14 +119,19 @@ __global__ void k_root(const Box4 *part, int nparts, RootBox *root) {
   *root = root_from_box(r);
 }
 
-// Batched sets: one block per set reduces its blob range [off[s], off[s+1])
-// to the set's root box (the same formulas as a single set's), checks the
-// inputs, and writes the set id of each of its blobs.
+// Batched sets: blocks (set, slice) reduce slice `slice` of the set's blob
+// range [off[s], off[s+1]) to a partial box, check the inputs and write the
+// set id of each blob; k_roots_sets then forms each set's root box from its
+// kSetSlices partials (the same formulas as a single set's).
+constexpr int kSetSlices = 16;
+
 __global__ void __launch_bounds__(256) k_bbox_sets(const double *__restrict__ xy, const double *__restrict__ cir,
                                                    const double *__restrict__ cor, const int *__restrict__ off,
-                                                   RootBox *roots, int *set_of, DevStatus *st) {
+                                                   Box4 *part, int *set_of, DevStatus *st) {
   const int set = blockIdx.x;
-  const int b = off[set], e = off[set + 1];
+  const int n0 = off[set], len = off[set + 1] - n0;
+  const int per = (len + kSetSlices - 1) / kSetSlices;
+  const int b = n0 + min(len, per * (int)blockIdx.y), e = n0 + min(len, per * ((int)blockIdx.y + 1));
   double xmax = -INFINITY, xmin = INFINITY, ymax = -INFINITY, ymin = INFINITY;
   bool bad = false;
   for (int i = b + threadIdx.x; i < e; i += blockDim.x) {
@@ -155,8 +160,22 @@ __global__ void __launch_bounds__(256) k_bbox_sets(const double *__restrict__ xy
       r.z = fmax(r.z, sh[k].z);
       r.w = fmin(r.w, sh[k].w);
     }
-    roots[set] = root_from_box(r);
+    part[(size_t)set * kSetSlices + blockIdx.y] = r;
   }
+}
+
+__global__ void k_roots_sets(const Box4 *part, int nsets, RootBox *roots) {
+  const int set = blockIdx.x * blockDim.x + threadIdx.x;
+  if (set >= nsets) return;
+  Box4 r = part[(size_t)set * kSetSlices];
+  for (int k = 1; k < kSetSlices; k++) {
+    const Box4 p = part[(size_t)set * kSetSlices + k];
+    r.x = fmax(r.x, p.x);
+    r.y = fmin(r.y, p.y);
+    r.z = fmax(r.z, p.z);
+    r.w = fmin(r.w, p.w);
+  }
+  roots[set] = root_from_box(r);
 }
 
 // One level of the reference's descent: digit of (x,y) against the centre,
@@ -679,7 +698,7 @@ int build_tree(Workspace &ws, int n, const double *d_xy, const double *d_cir, co
   tneed += Arena::bytes_for(ntiles + 1, 8) + 256;
   const int tlev = batched ? 12 : centre_levels(n);
   tneed += Arena::bytes_for(2 * centre_entries(tlev) * t.nsets, 8);
-  if (batched) tneed += Arena::bytes_for(n, 4);  // set of each blob
+  if (batched) tneed += Arena::bytes_for(n, 4) + Arena::bytes_for((size_t)nsets * kSetSlices, sizeof(Box4));
   T2D_CUDA_TRY(ws.tmp_arena.reserve(tneed));
   ws.tmp_arena.reset();
   uint64_t *keys_alt = ws.tmp_arena.take<uint64_t>(n);
@@ -692,6 +711,7 @@ int build_tree(Workspace &ws, int n, const double *d_xy, const double *d_cir, co
   unsigned long long *total = ws.tmp_arena.take<unsigned long long>(1);
   uint64_t *ctab = ws.tmp_arena.take<uint64_t>(2 * centre_entries(tlev) * t.nsets);
   int *set_of = batched ? ws.tmp_arena.take<int>(n) : nullptr;
+  Box4 *set_part = batched ? ws.tmp_arena.take<Box4>((size_t)nsets * kSetSlices) : nullptr;
 
   // Digits below the set root on the first attempt: as few as the tree is
   // likely to need (the previous tree's depth + 2, at least 16 for one set
@@ -707,8 +727,10 @@ retry:
 
   // 1. root box (per set)
   if (batched) {
-    k_bbox_sets<<<nsets, 256, 0, s>>>(d_xy, d_cir, d_cor, d_set_off, t.root, set_of, ws.status);
-    ::t2d::g_launches.fetch_add(1, std::memory_order_relaxed);
+    k_bbox_sets<<<dim3((unsigned)nsets, kSetSlices), 256, 0, s>>>(d_xy, d_cir, d_cor, d_set_off, set_part, set_of,
+                                                                  ws.status);
+    k_roots_sets<<<(nsets + 127) / 128, 128, 0, s>>>(set_part, nsets, t.root);
+    ::t2d::g_launches.fetch_add(2, std::memory_order_relaxed);
   } else {
     k_bbox<<<kBoxBlocks, 256, 0, s>>>(d_xy, d_cir, d_cor, n, bpart, ws.status);
     k_root<<<1, 32, 0, s>>>(bpart, kBoxBlocks, t.root);

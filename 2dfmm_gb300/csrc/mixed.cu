@@ -150,10 +150,12 @@ __global__ void k_leaf_setup(MixedView m, const double *x, const double *y, cons
     m.leaf_of[i] = c;
     m.loc[i] = make_float2((float)(x[i] - cx), (float)(y[i] - cy));
     m.gam[i] = (float)cir[i];
-    const double s = cor[i];
-    const double w = 1.0 / (s * s);
-    m.s2inv[i] = (float)w;
-    m.src4[i] = make_float4(m.loc[i].x, m.loc[i].y, m.gam[i], (float)(-1.4426950408889634 * w));
+    // 1/sigma^2 is only kept in FP32, so it is formed in FP32 (the FP64
+    // divide is slow on this GPU and buys nothing after the rounding)
+    const float sf = (float)cor[i];
+    const float w = 1.f / (sf * sf);
+    m.s2inv[i] = w;
+    m.src4[i] = make_float4(m.loc[i].x, m.loc[i].y, m.gam[i], -1.44269504f * w);
   }
 }
 
