@@ -150,6 +150,7 @@ __global__ void __launch_bounds__(kThreadsTC) k_m2l_tc(TcArgs a) {
   // of Npad); each accumulates few MMAs and the partial sums are added in
   // FP32 registers at the end, which keeps the accumulation error small.
   bool gfirst[8] = {true, true, true, true, true, true, true, true};
+  int issued = 0;  // steps whose MMAs were committed (or attempted)
   auto slot_at = [&](unsigned rest) { return __ffs(rest) - 1; };  // lowest remaining slot
   auto copy_b = [&](int slot, int bs) {
     if (tid != 0) return;
@@ -165,21 +166,17 @@ __global__ void __launch_bounds__(kThreadsTC) k_m2l_tc(TcArgs a) {
       r[kk] = (msrc && kk < Kc / 4) ? msrc[kk] : make_float4(0.f, 0.f, 0.f, 0.f);
   };
 
-  unsigned rest = mask;
-  float4 cur[kMaxKc4], nxt[kMaxKc4];
-  int slot = -1, issued = 0;
-  if (nslots > 0) {
-    slot = slot_at(rest);
-    rest &= rest - 1;
-    load_row(slot, cur);
-    copy_b(slot, 0);
-  }
-  for (int i = 0; i < nslots; i++) {
+  // One processed slot: the multipole rows of `slot` are in `use`; the rows
+  // of the next slot are loaded into `fill` (consumed one step later, so
+  // their latency overlaps a whole step).  A single block barrier per slot
+  // (after the A stage is written) also carries the failure flag: a thread
+  // that saw a wait give up stops the walk for the whole block at the next
+  // barrier.
+  auto step = [&](int i, int slot, int next, float4 (&use)[kMaxKc4], float4 (&fill)[kMaxKc4]) -> bool {
     const int ast = i & 1, bs = i % nbs;
-    const int next = rest ? slot_at(rest) : -1;
-    if (next >= 0) load_row(next, nxt);  // in flight while this slot is staged and multiplied
+    if (next >= 0) load_row(next, fill);
     // the MMAs that last read this A stage (and, with 3 B stages, the B
-    // stage of slot i+1) must be done before they are rewritten
+    // stage of the next slot) must be done before they are rewritten
     if (pending[ast]) {
       if (mbar_wait(&bar_mma[ast], phase_mma[ast], a.wait_limit)) {
         phase_mma[ast] ^= 1;
@@ -188,12 +185,8 @@ __global__ void __launch_bounds__(kThreadsTC) k_m2l_tc(TcArgs a) {
         s_fail = 1;
       }
     }
-    if (__syncthreads_or(s_fail)) break;
     if (nbs == 3 && next >= 0) copy_b(next, (i + 1) % 3);
-    if (nbs == 2) {
-      if (i > 0) copy_b(slot, bs);  // slot 0's copy went out before the loop
-    }
-    // A chunk: this thread's row, split into TF32 hi and lo
+    if (nbs == 2 && i > 0) copy_b(slot, bs);  // slot 0's copy went out before the walk
     {
       float *Ahi = reinterpret_cast<float *>(astage + (size_t)ast * 2 * a_bytes);
       float *Alo = reinterpret_cast<float *>(astage + (size_t)ast * 2 * a_bytes + a_bytes);
@@ -201,7 +194,7 @@ __global__ void __launch_bounds__(kThreadsTC) k_m2l_tc(TcArgs a) {
 #pragma unroll
       for (int kk = 0; kk < kMaxKc4; kk++) {
         if (kk >= Kc / 4) break;
-        const float4 v = cur[kk];
+        const float4 v = use[kk];
         float4 h, l;
         h.x = __uint_as_float(tf32_bits(v.x));
         h.y = __uint_as_float(tf32_bits(v.y));
@@ -217,44 +210,58 @@ __global__ void __launch_bounds__(kThreadsTC) k_m2l_tc(TcArgs a) {
       }
     }
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    __syncthreads();
-    bool b_ok = true;
+    if (__syncthreads_or(s_fail)) return false;
     if (tid == 0) {
-      b_ok = mbar_wait(&bar_b[bs], phase_b[bs], a.wait_limit);
-      if (b_ok) {
+      if (mbar_wait(&bar_b[bs], phase_b[bs], a.wait_limit)) {
         phase_b[bs] ^= 1;
         b_inflight[bs] = false;
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const uint32_t ah = smem_u32(astage + (size_t)ast * 2 * a_bytes), al = ah + a_bytes;
+        const uint32_t bh = smem_u32(bstage + (size_t)bs * 2 * b_bytes), bl = bh + b_bytes;
+        const int g = i % a.ngroups;
+        const uint32_t dcol = tmem + (uint32_t)(g * Npad);
+        for (int t = 0; t < Kc / 8; t++) {
+          const uint32_t ko = (uint32_t)t * 2 * lbo;
+          const uint64_t dah = smem_desc(ah + ko, lbo, sbo_a), dal = smem_desc(al + ko, lbo, sbo_a);
+          const uint64_t dbh = smem_desc(bh + ko, lbo, sbo_b), dbl = smem_desc(bl + ko, lbo, sbo_b);
+          mma_tf32(dcol, dah, dbh, idesc, gfirst[g] ? 0u : 1u);
+          gfirst[g] = false;
+          mma_tf32(dcol, dah, dbl, idesc, 1u);
+          mma_tf32(dcol, dal, dbh, idesc, 1u);
+        }
+        mma_commit(&bar_mma[ast]);
       } else {
+        // no MMAs for this stage: the others find out at the next barrier
+        // (their wait on this stage gives up too, bounded)
         s_fail = 1;
       }
     }
-    if (tid == 0 && b_ok) {
-      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      const uint32_t ah = smem_u32(astage + (size_t)ast * 2 * a_bytes), al = ah + a_bytes;
-      const uint32_t bh = smem_u32(bstage + (size_t)bs * 2 * b_bytes), bl = bh + b_bytes;
-      const int g = issued % a.ngroups;
-      const uint32_t dcol = tmem + (uint32_t)(g * Npad);
-      for (int t = 0; t < Kc / 8; t++) {
-        const uint32_t ko = (uint32_t)t * 2 * lbo;
-        const uint64_t dah = smem_desc(ah + ko, lbo, sbo_a), dal = smem_desc(al + ko, lbo, sbo_a);
-        const uint64_t dbh = smem_desc(bh + ko, lbo, sbo_b), dbl = smem_desc(bl + ko, lbo, sbo_b);
-        mma_tf32(dcol, dah, dbh, idesc, gfirst[g] ? 0u : 1u);
-        gfirst[g] = false;
-        mma_tf32(dcol, dah, dbl, idesc, 1u);
-        mma_tf32(dcol, dal, dbh, idesc, 1u);
-      }
-      mma_commit(&bar_mma[ast]);
-    }
-    // every thread marks the stage busy only if its MMAs were issued
-    if (__syncthreads_or(!b_ok)) break;
     pending[ast] = true;
-    issued++;
-    if (next >= 0) {
-#pragma unroll
-      for (int kk = 0; kk < kMaxKc4; kk++) cur[kk] = nxt[kk];
-      slot = next;
-      rest &= rest - 1;
-    }
+    issued = i + 1;
+    return true;
+  };
+
+  unsigned rest = mask;
+  float4 buf0[kMaxKc4], buf1[kMaxKc4];
+  int slot = -1;
+  if (nslots > 0) {
+    slot = slot_at(rest);
+    rest &= rest - 1;
+    load_row(slot, buf0);
+    copy_b(slot, 0);
+  }
+  for (int i = 0; i < nslots; i += 2) {
+    // two steps per turn so that the row buffers swap roles statically
+    int next = rest ? slot_at(rest) : -1;
+    if (!step(i, slot, next, buf0, buf1)) break;
+    if (next < 0) break;
+    slot = next;
+    rest &= rest - 1;
+    next = rest ? slot_at(rest) : -1;
+    if (!step(i + 1, slot, next, buf1, buf0)) break;
+    if (next < 0) break;
+    slot = next;
+    rest &= rest - 1;
   }
   // drain: every stage with MMAs in flight (bounded; a failed wait is
   // retried once more below before TMEM and shared memory are released)

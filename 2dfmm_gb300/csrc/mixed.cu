@@ -187,6 +187,11 @@ __constant__ signed char c_slot[4][6][6];  // [class][dy+2+qy][dx+2+qx] -> slot 
 
 // V and X lists of every cell of level >= 2.
 __global__ void k_vx_lists(MixedView m) {
+  // the slot table in shared memory: the lanes index it divergently, which
+  // constant memory would serialise
+  __shared__ signed char slot[4][6][6];
+  for (int i = threadIdx.x; i < 4 * 6 * 6; i += blockDim.x) (&slot[0][0][0])[i] = (&c_slot[0][0][0])[i];
+  __syncthreads();
   int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= m.ncell) return;
   int *V = m.vlist + (size_t)c * 27;
@@ -213,7 +218,7 @@ __global__ void k_vx_lists(MixedView m) {
           int jx = (int)(2 * m.ix[e] + (q & 1)), jy = (int)(2 * m.iy[e] + (q >> 1));
           int dx = jx - (int)ix, dy = jy - (int)iy;
           if (abs(dx) <= 1 && abs(dy) <= 1) continue;
-          int s = c_slot[cls][dy + 2 + qy][dx + 2 + qx];
+          int s = slot[cls][dy + 2 + qy][dx + 2 + qx];
           if (s >= 0) {
             V[s] = cc;
             nv++;
