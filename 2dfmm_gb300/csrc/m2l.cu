@@ -281,22 +281,32 @@ __global__ void __launch_bounds__(kThreadsTC) k_m2l_tc(TcArgs a) {
     // Row `tid` lives in TMEM lane tid; warp w reads lanes 32w..32w+31.  All
     // lanes of the warp execute the loads (they are warp-collective); only
     // lanes with a row write.
+    // The local expansions are still zero here (P2L and L2L run after
+    // M2L, and each cell is one row of one class), so the row is stored,
+    // not added; 32 accumulator columns per TMEM load.
     const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16);
     float *dst = valid ? m.L + (size_t)cell * 2 * P : nullptr;
     const int used = issued < a.ngroups ? issued : a.ngroups;
-    for (int c0 = 0; c0 < 2 * P; c0 += 8) {
-      float acc[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    for (int c0 = 0; c0 < 2 * P; c0 += 32) {
+      float acc[32];
+#pragma unroll
+      for (int j = 0; j < 32; j++) acc[j] = 0.f;
       for (int g = 0; g < used; g++) {
-        uint32_t r[8];
-        asm volatile(
-            "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];\n"
-            : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
-            : "r"(taddr + (uint32_t)(g * Npad + c0)));
-        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-        for (int j = 0; j < 8; j++) acc[j] += __uint_as_float(r[j]);
+        uint32_t r[32];
+        tmem_ld32(taddr + (uint32_t)(g * Npad + c0), r);
+        tmem_wait();
+#pragma unroll
+        for (int j = 0; j < 32; j++) acc[j] += __uint_as_float(r[j]);
       }
-      if (dst)
-        for (int j = 0; j < 8 && c0 + j < 2 * P; j++) dst[c0 + j] += acc[j];
+      if (dst) {
+        if (c0 + 32 <= 2 * P) {
+#pragma unroll
+          for (int j = 0; j < 32; j += 4)
+            *reinterpret_cast<float4 *>(dst + c0 + j) = make_float4(acc[j], acc[j + 1], acc[j + 2], acc[j + 3]);
+        } else {
+          for (int j = 0; c0 + j < 2 * P; j++) dst[c0 + j] = acc[j];
+        }
+      }
     }
   }
   if (s_fail) {
