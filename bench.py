@@ -52,6 +52,8 @@ def parse():
     ap.add_argument("--cutoff", type=float, default=3.0, help="mixed form: correction radius / max sigma")
     ap.add_argument("--cuda-core-m2l", action="store_true", help="mixed form: M2L on CUDA cores")
     ap.add_argument("--no-plain", action="store_true", help="skip timing the plain FP64 path beside")
+    ap.add_argument("--eval-variant", type=int, default=-1,
+                    help="mixed/learned: force a near-field kernel variant 0..3 (default: the tuner's choice)")
     ap.add_argument("--workload", default="two_patch_sheet",
                     choices=["two_patch_sheet", "lamb_oseen", "uniform", "batch_sets"])
     ap.add_argument("--nsets", type=int, default=512, help="batch_sets: number of independent sets")
@@ -335,6 +337,7 @@ def run_ours(args):
     b, wname = workload(args, rank)
     P.set_params(b.nterms, b.num_p, b.theta)
     P.set_mixed_params(args.pterms, args.cutoff, not args.cuda_core_m2l)
+    P.set_tuning(args.eval_variant < 0, args.eval_variant)
     learned_note = None
     if args.mode == "learned":
         L = importlib.import_module("2dfmm_gb300.learn")
@@ -482,6 +485,7 @@ def run_batch(args):
     P.set_params(b0.nterms, b0.num_p, b0.theta)
     P.set_mode(MODES["mixed"])
     P.set_mixed_params(args.pterms, args.cutoff, not args.cuda_core_m2l)
+    P.set_tuning(args.eval_variant < 0, args.eval_variant)
     off = np.concatenate([[0], np.cumsum([b.n for b in sets])]).astype(np.int32)
     n = int(off[-1])
     h_xy = np.concatenate([b.xy for b in sets])
