@@ -1,7 +1,8 @@
 // FP64 direct O(N*M) sum of the regularised Biot-Savart kernel: the judge
 // of the approximate modes.  The pair kernel is direct_evaluate's
 // (ver-c/src/fmm.c:121-142, r > 1e-10) applied to every source.  Sources are
-// staged through shared memory in tiles; one thread per target.
+// staged through shared memory in tiles (with 1/sigma^2 per source); one
+// thread per target.
 #include "dev_common.cuh"
 #include "tc_ptx.cuh"
 
@@ -11,13 +12,24 @@ namespace {
 constexpr int kThreads = 256;
 constexpr double kPi = 3.14159265358979323846;
 
+// 1/x for a positive normal x: the SFU's approximate reciprocal refined by
+// two Newton-Raphson steps y <- y + y (1 - x y) (each squares the relative
+// error), ending within an ulp or so of the correctly rounded quotient.
+__device__ __forceinline__ double rcp_nr(double x) {
+  double y;
+  asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
+  y = fma(y, fma(-x, y, 1.0), y);
+  y = fma(y, fma(-x, y, 1.0), y);
+  return y;
+}
+
 // grid.y splits the sources into chunks; each block adds its partial sums
 // into uv (zeroed by the caller) with FP64 atomics.
 __global__ void __launch_bounds__(kThreads) k_direct(int ntgt, const double *__restrict__ txy, int nsrc,
                                                      const double *__restrict__ sxy, const double *__restrict__ cir,
                                                      const double *__restrict__ cor, double *__restrict__ uv,
                                                      int chunk) {
-  __shared__ double sx[kThreads], sy[kThreads], sg[kThreads], sr[kThreads];
+  __shared__ double sx[kThreads], sy[kThreads], sg[kThreads], sr2[kThreads];
   const long i = blockIdx.x * (long)kThreads + threadIdx.x;
   const bool valid = i < ntgt;
   const double x = valid ? txy[2 * i] : 0.0, y = valid ? txy[2 * i + 1] : 0.0;
@@ -30,20 +42,21 @@ __global__ void __launch_bounds__(kThreads) k_direct(int ntgt, const double *__r
       sx[threadIdx.x] = sxy[2 * (long)j];
       sy[threadIdx.x] = sxy[2 * (long)j + 1];
       sg[threadIdx.x] = cir[j];
-      sr[threadIdx.x] = 1.0 / cor[j];
+      sr2[threadIdx.x] = 1.0 / (cor[j] * cor[j]);
     }
     __syncthreads();
     const int cnt = min(kThreads, s1 - base);
+    // (r/sigma)^2 as r2 / sigma^2 and 1/r2 by a Newton-refined reciprocal:
+    // the same quantities within an ulp or two, without a square root or
+    // an IEEE division per pair; r > 1e-10 <=> r2 > 1e-20
     for (int k = 0; k < cnt; k++) {
       const double rx = x - sx[k];
       const double ry = y - sy[k];
       const double r2 = rx * rx + ry * ry;
-      const double r = sqrt(r2);
-      if (r > 1.0e-10) {
-        const double xai = r * sr[k];
-        const double x2 = xai * xai;
+      if (r2 > 1.0e-20) {
+        const double x2 = r2 * sr2[k];
         const double e1 = x2 > 40.0 ? 1.0 : 1.0 - exp(-x2);
-        const double rv = sg[k] * e1 / r2;
+        const double rv = sg[k] * e1 * rcp_nr(r2);
         ax -= rv * ry;
         ay += rv * rx;
       }
