@@ -121,6 +121,7 @@ __global__ void __launch_bounds__(kEvalWarps * 32) k_eval(EvalArgs a) {
   const int nt = a.nt;
   const double x = valid ? a.tx[i] : 0.0, y = valid ? a.ty[i] : 0.0;
   const double theta = a.theta;
+  const double theta2 = __dmul_rn(theta, theta);
   double2 phi = make_double2(0.0, 0.0);
   double ud0 = 0.0, ud1 = 0.0;
   unsigned long long n_m2s = 0, n_pairs = 0;
@@ -175,16 +176,28 @@ __global__ void __launch_bounds__(kEvalWarps * 32) k_eval(EvalArgs a) {
         const double ccx = t.cx[cc], ccy = t.cy[cc], creg = t.region[cc];
         bool desc = false;
         double dx = 0.0, dy = 0.0;
+        double d2 = 0.0;
         if (act) {
           dx = __dsub_rn(x, ccx);
           dy = __dsub_rn(y, ccy);
-          const double r = __dsqrt_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)));
-          desc = creg > __dmul_rn(theta, r);
+          d2 = __dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy));
+          // The reference's test is region > theta * sqrt(d2), each step
+          // rounded.  Squared, with a relative margin of 1e-13 (the rounding
+          // of either side is below 1e-15), it decides the same way without
+          // the square root; only a test within the margin takes the exact
+          // rounded path.
+          const double c2 = __dmul_rn(creg, creg), q = __dmul_rn(theta2, d2);
+          if (c2 > __dmul_rn(q, 1.0 + 1e-13)) {
+            desc = true;
+          } else if (c2 < __dmul_rn(q, 1.0 - 1e-13)) {
+            desc = false;
+          } else {
+            desc = creg > __dmul_rn(theta, __dsqrt_rn(d2));
+          }
         }
         const unsigned dmask = __ballot_sync(0xffffffffu, desc);
         if (act && !desc && nt >= 2) {
           // M2S, fmm.c:60-67: sum_{k<nt-1} a_k w^{k+1}, w = 1/(z - zc)
-          const double d2 = dx * dx + dy * dy;
           const double inv = rcp_nr(d2);
           const double2 w = make_double2(dx * inv, -dy * inv);
           const double2 *cf = t.coef + (size_t)cc * nt;

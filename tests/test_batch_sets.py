@@ -83,3 +83,35 @@ def test_batched_sets_reject_plain_mode_and_bad_offsets(gpu_lib):
         P.solve_sets(d_xy.data_ptr(), d_cir.data_ptr(), d_cor.data_ptr(), d_uv.data_ptr(), bad)
     assert P.last_error() == P.ERR_BAD_INPUT
     P.set_mode(P.MODE_PLAIN)
+
+
+@pytest.mark.gpu
+def test_batched_sets_with_empty_and_tiny_sets(gpu_lib):
+    """Empty sets and one-blob sets in the batch: the others are unchanged."""
+    torch = pytest.importorskip("torch")
+    P = gpu_lib
+    W = workloads()
+    big = W.batch_sets(nsets=2, seed=77, lo=3000, hi=6000)
+    one = W.batch_sets(nsets=1, seed=78, lo=2048, hi=2048)[0]
+    one.xy, one.cir, one.cor = one.xy[:1], one.cir[:1], one.cor[:1]
+    empty = W.batch_sets(nsets=1, seed=79, lo=2048, hi=2048)[0]
+    empty.xy, empty.cir, empty.cor = empty.xy[:0], empty.cir[:0], empty.cor[:0]
+    sets = [big[0], empty, one, big[1], empty]
+    P.set_params(big[0].nterms, big[0].num_p, big[0].theta)
+    P.set_mode(P.MODE_MIXED)
+    P.set_mixed_params(16, 3.0, True)
+    xy, cir, cor, off = _concat(sets)
+    d_xy, d_cir, d_cor = _dev(torch, xy), _dev(torch, cir), _dev(torch, cor)
+    d_uv = torch.empty_like(d_xy)
+    P.solve_sets(d_xy.data_ptr(), d_cir.data_ptr(), d_cor.data_ptr(), d_uv.data_ptr(), off)
+    torch.cuda.synchronize()
+    uv = d_uv.cpu().numpy()
+    assert np.all(uv[off[2]:off[3]] == 0.0)  # a lone blob induces nothing on itself
+    for k in (0, 3):
+        b = sets[k]
+        s_xy, s_cir, s_cor = _dev(torch, b.xy), _dev(torch, b.cir), _dev(torch, b.cor)
+        s_uv = torch.empty_like(s_xy)
+        P.solve_device(s_xy.data_ptr(), s_cir.data_ptr(), s_cor.data_ptr(), s_uv.data_ptr(), b.n)
+        torch.cuda.synchronize()
+        assert np.array_equal(uv[off[k]:off[k + 1]], s_uv.cpu().numpy())
+    P.set_mode(P.MODE_PLAIN)
