@@ -1,4 +1,4 @@
-// FP64 direct O(N*M) sum of the regularised Biot-Savart kernel: the judge
+// FP64 direct O(N*M) sum of the regularised Biot-Savart kernel: the yardstick
 // of the approximate modes.  The pair kernel is direct_evaluate's
 // (ver-c/src/fmm.c:121-142, r > 1e-10) applied to every source.  Sources are
 // staged through shared memory in tiles (with 1/sigma^2 per source); one

@@ -6,9 +6,9 @@ step.  Interaction samples (features + the cheapest acceptable class,
 labelled by the FMM against the FP64 exact contribution) are collected on
 steps 0-20, the network is trained on them on the GPU, and steps 21-100 are
 solved with the fixed mixed form and with the learned form on the same
-positions; every `score_every`-th step both are judged against the FP64
+positions; every `score_every`-th step both are yardstickd against the FP64
 direct sum on sampled targets, and the plain FP64 treecode (the reference's
-method, p = 12, theta 0.5) is timed and judged beside them.
+method, p = 12, theta 0.5) is timed and yardstickd beside them.
 
     python -m 2dfmm_gb300.learn --out learned_weights.npz
 

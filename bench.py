@@ -57,7 +57,7 @@ def parse():
     ap.add_argument("--workload", default="two_patch_sheet",
                     choices=["two_patch_sheet", "lamb_oseen", "uniform", "batch_sets"])
     ap.add_argument("--nsets", type=int, default=512, help="batch_sets: number of independent sets")
-    ap.add_argument("--set-targets", type=int, default=4096, help="batch_sets: judged targets per set")
+    ap.add_argument("--set-targets", type=int, default=4096, help="batch_sets: targets per set measured against the direct sum")
     ap.add_argument("--n", type=int, default=0, help="override the blob count (exploration only)")
     ap.add_argument("--err-targets", type=int, default=65536)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -276,9 +276,9 @@ def _time_mode(P, torch, args, mode, arrays, stream, flush, clk=None):
 
 
 def _direct_reference(P, torch, arrays, n, ntgt, sp):
-    """FP64 direct sum (the judge) at `ntgt` seeded targets sampled without
+    """FP64 direct sum (the accuracy yardstick) at `ntgt` seeded targets sampled without
     replacement from the blobs; computed once per run and reused for every
-    form judged."""
+    form measured."""
     xy, cir, cor, _, _ = arrays
     W = importlib.import_module("2dfmm_gb300.workloads")
     idx = W.sample_targets(n, ntgt, seed=7)
@@ -290,10 +290,10 @@ def _direct_reference(P, torch, arrays, n, ntgt, sp):
     return tidx, ref
 
 
-def _judge(uv, judge):
+def _accuracy(uv, yardstick):
     """relL2 and max relative error of the last solve's velocities against
     the FP64 direct sum."""
-    tidx, ref = judge
+    tidx, ref = yardstick
     got = uv[tidx]
     rel_l2 = float((got - ref).norm() / ref.norm())
     max_rel = float(((got - ref).norm(dim=1) / ref.norm(dim=1).clamp_min(1e-300)).max())
@@ -366,8 +366,8 @@ def run_ours(args):
     clocks = clk.summary()
     total_ms = max_over_ranks(float(sum(times)), world, dev)
     value = replica_throughput(n, args.steps, total_ms, world)
-    judge = _direct_reference(P, torch, arrays, n, args.err_targets, sp)
-    accuracy = _judge(uv, judge)
+    yardstick = _direct_reference(P, torch, arrays, n, args.err_targets, sp)
+    accuracy = _accuracy(uv, yardstick)
     roofline = _roofline(P, args, args.mode, b, wname, sts, sp)
 
     # the fixed mixed form and the plain FP64 path on the same set, timed the
@@ -379,7 +379,7 @@ def run_ours(args):
     for other in others:
         otimes, _ = _time_mode(P, torch, args, other, arrays, stream, flush)
         o = {"value": n / (statistics.mean(otimes) * 1e-3), "unit": UNIT, "ms_per_step": statistics.mean(otimes),
-             "accuracy": _judge(uv, judge)}
+             "accuracy": _accuracy(uv, yardstick)}
         o["speedup_of_headline"] = value / world / o["value"]
         beside["plain_fp64" if other == "plain" else "mixed_fixed"] = o
     P.set_mode(MODES[args.mode])
@@ -467,7 +467,7 @@ BATCH_METRIC = "target evals/s over 512 uneven blob sets solved as one batch, re
 def run_batch(args):
     """Configuration 4: `nsets` independent sets (sizes log-uniform in
     [2,048, 200,000]) solved by one batched mixed solve per step
-    (tree2d_solve_sets); every blob is a target.  Each set is judged against
+    (tree2d_solve_sets); every blob is a target.  Each set is measured against
     its own FP64 direct sum on `set_targets` sampled targets.  Beside it the
     same sets solved one call at a time."""
     import torch

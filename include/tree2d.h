@@ -152,7 +152,7 @@ int tree2d_get_stats(tree2d_stats_t *out);
 long long tree2d_export_tree(int *perm, long long cap, int *level, int *begin, int *end, int *leaf,
                              double *cx, double *cy, double *region, double *coef);
 
-/* FP64 direct O(N*M) sum of the regularised kernel (the judge of the
+/* FP64 direct O(N*M) sum of the regularised kernel (the yardstick of the
  * approximate modes): targets and sources in device memory. */
 int tree2d_direct_device(int ntgt, const double *d_txy, int nsrc, const double *d_sxy,
                          const double *d_cir, const double *d_cor, double *d_uv, void *stream);

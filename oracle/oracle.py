@@ -131,7 +131,7 @@ class Oracle:
 
 
 def direct(txy, sxy, cir, cor, threads: int = 0):
-    """FP64 direct sum of the regularised Biot-Savart kernel (the judge)."""
+    """FP64 direct sum of the regularised Biot-Savart kernel (the accuracy yardstick)."""
     L = lib()
     txy = _f64(txy).reshape(-1, 2)
     sxy = _f64(sxy).reshape(-1, 2)

@@ -33,7 +33,7 @@
  * bit-exact against the reference built from its own sources.  Compile with
  * -ffp-contract=off so that no platform fuses those expressions.
  *
- * Also here: the FP64 direct O(N*M) sum that judges approximate results; it
+ * Also here: the FP64 direct O(N*M) sum that measures approximate results; it
  * applies the regularised kernel of direct_evaluate (fmm.c:121-142, r > 1e-10)
  * to every source, i.e. biot_b of ver-c/src/includes/d_biot.f90:2-64 with the
  * path's threshold.
@@ -493,7 +493,7 @@ long ora_dump_tree(int *perm, long cap, int *level, int *begin, int *end, int *l
 }
 
 /* ---------------------------------------------------------------------- */
-/* FP64 direct sum (the judge)                                             */
+/* FP64 direct sum (the accuracy yardstick)                                             */
 
 void ora_direct(int ntgt, const double *txy, int nsrc, const double *sxy, const double *cir,
                 const double *cor, double *uv, int threads) {

@@ -1,4 +1,4 @@
-"""FP64 direct-sum judge kernel against the oracle's direct sum."""
+"""FP64 direct-sum kernel (the accuracy yardstick) against the oracle's direct sum."""
 from __future__ import annotations
 
 import numpy as np

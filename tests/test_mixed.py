@@ -1,6 +1,6 @@
 """Mixed-precision FMM (TREE2D_MODE_MIXED) against the FP64 direct sum.
 
-The mixed form is judged by its error against the exact sum, not by parity
+The mixed form is measured by its error against the exact sum, not by parity
 with the reference: relL2 <= 1e-6 on seeded sampled targets (configuration
 1 at full size, the configuration-2 and configuration-3 distributions at
 reduced size here; the full configuration 3 is measured by bench.py)."""
@@ -14,7 +14,7 @@ from conftest import workloads
 REL_L2 = 1e-6
 
 
-def solve_and_judge(P, torch, b, ntgt=1024, tensor_cores=True, pterms=16):
+def solve_and_measure(P, torch, b, ntgt=1024, tensor_cores=True, pterms=16):
     dev = torch.device("cuda:0")
     P.set_params(b.nterms, b.num_p, b.theta)
     P.set_mode(P.MODE_MIXED)
@@ -43,7 +43,7 @@ def test_mixed_accuracy_against_direct_sum(gpu_lib, which):
     b = {"uniform": lambda: W.uniform(),
          "lamb_oseen": lambda: W.lamb_oseen(262_144, seed=2),
          "two_patch_sheet": lambda: W.two_patch_sheet(524_288, seed=3)}[which]()
-    rel, uv = solve_and_judge(gpu_lib, torch, b)
+    rel, uv = solve_and_measure(gpu_lib, torch, b)
     assert np.isfinite(uv).all()
     assert rel <= REL_L2, rel
 
@@ -55,7 +55,7 @@ def test_mixed_make_tree_and_batch_agree(gpu_lib):
     P = gpu_lib
     W = workloads()
     b = W.lamb_oseen(65_536, seed=5)
-    _, uv_dev = solve_and_judge(P, torch, b, ntgt=64)
+    _, uv_dev = solve_and_measure(P, torch, b, ntgt=64)
     P.set_params(b.nterms, b.num_p, b.theta)
     P.set_mode(P.MODE_MIXED)
     P.make_tree(b.xy, b.cir, b.cor)
@@ -72,9 +72,9 @@ def test_tensor_core_m2l_matches_cuda_core_m2l(gpu_lib):
     P = gpu_lib
     W = workloads()
     b = W.two_patch_sheet(262_144, seed=11)
-    rel_tc, uv_tc = solve_and_judge(P, torch, b, tensor_cores=True)
+    rel_tc, uv_tc = solve_and_measure(P, torch, b, tensor_cores=True)
     assert P.stats()["m2l_path"] == 2
-    rel_cc, uv_cc = solve_and_judge(P, torch, b, tensor_cores=False)
+    rel_cc, uv_cc = solve_and_measure(P, torch, b, tensor_cores=False)
     assert P.stats()["m2l_path"] == 1
     diff = np.linalg.norm(uv_tc - uv_cc) / np.linalg.norm(uv_cc)
     assert diff <= 1e-6, diff
