@@ -57,6 +57,12 @@ cudaError_t workspace_init(Workspace &ws) {
     e = cudaEventCreate(&ev);
     if (e != cudaSuccess) return e;
   }
+  e = cudaStreamCreateWithFlags(&ws.side, cudaStreamNonBlocking);
+  if (e != cudaSuccess) return e;
+  e = cudaEventCreateWithFlags(&ws.fork_ev, cudaEventDisableTiming);
+  if (e != cudaSuccess) return e;
+  e = cudaEventCreateWithFlags(&ws.join_ev, cudaEventDisableTiming);
+  if (e != cudaSuccess) return e;
   ws.init = true;
   return cudaSuccess;
 }

@@ -146,6 +146,8 @@ struct Workspace {
   DevStatus *status = nullptr;   // device
   DevStatus *h_status = nullptr; // pinned host mirror
   cudaEvent_t ev[8] = {};
+  cudaStream_t side = nullptr;    // second stream (learned decisions beside the expansions)
+  cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
   bool init = false;
 };
 

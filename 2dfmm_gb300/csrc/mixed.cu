@@ -1392,25 +1392,22 @@ int mixed_solve(Workspace &ws, const Tree &t, const MixedParams &mp, double *d_u
   m.k_leaf = ws.mx_lists.take<int>(tot[2] + 1);
   rc = mixed_fill_lists(m, s);
   if (rc) return rc;
-  rc = mixed_upward(m, t.depth, s);
-  if (rc) return rc;
-  T2D_CUDA_TRY(cudaMemsetAsync(m.L, 0, sizeof(float) * (size_t)nc * 2 * P, s));
-  rc = tc ? m2l_tensor_cores(m, dimg, cls_list, cls_count, s) : m2l_cuda_cores(m, dm2l, s);
-  if (rc) return rc;
-  st.m2l_path = tc ? 2 : 1;
-  rc = mixed_downward(m, t.depth, s);
-  if (rc) return rc;
   // keep the view for sampling (training data)
   if (!ws.mxv) ws.mxv = new MixedView();
   *ws.mxv = m;
   ws.mx_tot[0] = tot[0];
   ws.mx_tot[1] = tot[1];
   ws.mx_tot[2] = tot[2];
-  // (a batched tree runs the fixed mixed form: the network's reference
-  // scale u_ref is one per tree)
+  // The network's decisions need only the lists and the leaves' source
+  // statistics, not the expansions: they run on a second stream, forked
+  // here and joined before the near field, beside the upward pass, M2L and
+  // the downward pass (both chains are latency-bound and share the GPU
+  // well).  A batched tree runs the fixed mixed form: the network's
+  // reference scale u_ref is one per tree.
   const bool learned = mp.learned && mp.lp && mp.lp->have_weights && t.lev0 == 0;
   unsigned char *u_dec = nullptr, *k_dec = nullptr;
-  if ((learned || mp.learned) && t.lev0 == 0) {
+  const bool side = (learned || mp.learned) && t.lev0 == 0;
+  if (side) {
     // leaf statistics and u_ref (also used by sampling), then decisions
     const size_t wim = learn_weight_image_elems();
     size_t need = Arena::bytes_for(wim, 2) + Arena::bytes_for(208, 4) + Arena::bytes_for((size_t)nc, sizeof(LeafStats)) +
@@ -1425,23 +1422,36 @@ int mixed_solve(Workspace &ws, const Tree &t, const MixedParams &mp, double *d_u
     u_dec = ws.lr_arena.take<unsigned char>((size_t)tot[0] + 1);
     k_dec = ws.lr_arena.take<unsigned char>((size_t)tot[2] + 1);
     float *uref = ws.lr_arena.take<float>(1);
-    rc = learned_leaf_stats(m, stats, s);
+    if (learned && ws.lr_version != mp.lp_version) {
+      std::vector<uint16_t> img;
+      std::vector<float> b;
+      learn_weight_images(mp.lp->theta, img, b);
+      T2D_CUDA_TRY(cudaMemcpy(wimg, img.data(), img.size() * 2, cudaMemcpyHostToDevice));
+      T2D_CUDA_TRY(cudaMemcpy(bias, b.data(), b.size() * 4, cudaMemcpyHostToDevice));
+      ws.lr_version = mp.lp_version;
+    }
+    cudaStream_t s2 = ws.side;
+    T2D_CUDA_TRY(cudaEventRecord(ws.fork_ev, s));
+    T2D_CUDA_TRY(cudaStreamWaitEvent(s2, ws.fork_ev, 0));
+    rc = learned_leaf_stats(m, stats, s2);
     if (rc) return rc;
-    rc = learned_uref(m, stats, t.root, uref, s);
+    rc = learned_uref(m, stats, t.root, uref, s2);
     if (rc) return rc;
     if (learned) {
-      if (ws.lr_version != mp.lp_version) {
-        std::vector<uint16_t> img;
-        std::vector<float> b;
-        learn_weight_images(mp.lp->theta, img, b);
-        T2D_CUDA_TRY(cudaMemcpy(wimg, img.data(), img.size() * 2, cudaMemcpyHostToDevice));
-        T2D_CUDA_TRY(cudaMemcpy(bias, b.data(), b.size() * 4, cudaMemcpyHostToDevice));
-        ws.lr_version = mp.lp_version;
-      }
-      rc = learned_decide(m, stats, uref, wimg, bias, mp.lp->direct_bias, tot[0], tot[2], u_dec, k_dec, s);
+      rc = learned_decide(m, stats, uref, wimg, bias, mp.lp->direct_bias, tot[0], tot[2], u_dec, k_dec, s2);
       if (rc) return rc;
     }
+    T2D_CUDA_TRY(cudaEventRecord(ws.join_ev, s2));
   }
+  rc = mixed_upward(m, t.depth, s);
+  if (rc) return rc;
+  T2D_CUDA_TRY(cudaMemsetAsync(m.L, 0, sizeof(float) * (size_t)nc * 2 * P, s));
+  rc = tc ? m2l_tensor_cores(m, dimg, cls_list, cls_count, s) : m2l_cuda_cores(m, dm2l, s);
+  if (rc) return rc;
+  st.m2l_path = tc ? 2 : 1;
+  rc = mixed_downward(m, t.depth, s);
+  if (rc) return rc;
+  if (side) T2D_CUDA_TRY(cudaStreamWaitEvent(s, ws.join_ev, 0));
   T2D_CUDA_TRY(cudaEventRecord(ws.ev[4], s));
   const Decisions dec = learned ? Decisions{u_dec, k_dec, mp.lp->order_margin} : Decisions{nullptr, nullptr, 0};
   rc = near_field(ws, mp, m, learned, dec, d_uv, t.perm, s, st);
