@@ -45,8 +45,6 @@
 namespace t2d {
 namespace {
 
-constexpr float kInv2Pi = 0.15915494309189535f;
-
 // ---------------------------------------------------------------- lookups
 
 struct Found {
@@ -817,7 +815,6 @@ struct Decisions {
 // sum the current one.  Leaves larger than a stage buffer, and every leaf
 // after a wait that gave up (recorded as TREE2D_ERR_TIMEOUT), are read from
 // global memory instead, so the result never depends on the staging.
-constexpr int kEvalWarps = 4;
 constexpr int kStage = 64;  // blobs per stage buffer
 constexpr long kEvalWaitLimit = 1l << 22;  // polls; a healthy copy lands within microseconds
 
