@@ -32,7 +32,7 @@ EXPORTS = [
     "make_tree", "biot_tree", "tree2d_last_error", "tree2d_error_string", "tree2d_set_params",
     "tree2d_clear_params", "tree2d_get_params", "tree2d_set_mode", "tree2d_get_mode", "tree2d_set_mixed_params", "biot_tree_batch",
     "tree2d_solve_device", "tree2d_solve_device_static", "tree2d_solve_sets", "tree2d_set_tuning", "tree2d_get_stats", "tree2d_export_tree", "tree2d_direct_device", "tree2d_fp64_probe", "tree2d_pipe_probe", "tree2d_wait_probe", "tree2d_version",
-    "tree2d_learn_param_count", "tree2d_learn_set_weights", "tree2d_learn_get_weights", "tree2d_learn_set_options",
+    "tree2d_learn_param_count", "tree2d_learn_set_weights", "tree2d_learn_set_envelope", "tree2d_learn_get_weights", "tree2d_learn_set_options",
     "tree2d_learn_collect", "tree2d_learn_train", "tree2d_mlp_grad", "tree2d_mlp_forward",
     "tree2d_set_mirror", "tree2d_advect_device",
 ]
@@ -51,6 +51,7 @@ class Stats(ctypes.Structure):
         ("n_pairs", ctypes.c_longlong), ("n_m2l", ctypes.c_longlong), ("ms_build", ctypes.c_double),
         ("ms_upward", ctypes.c_double), ("ms_eval", ctypes.c_double), ("ms_total", ctypes.c_double),
         ("n_launches", ctypes.c_longlong), ("m2l_path", ctypes.c_int), ("eval_variant", ctypes.c_int),
+        ("learned_active", ctypes.c_int), ("n_list_u", ctypes.c_longlong), ("n_list_k", ctypes.c_longlong),
     ]
 
     def as_dict(self):
@@ -125,6 +126,8 @@ def load(path: str | None = None):
     L.tree2d_learn_set_weights.argtypes = [fp, ctypes.c_int]
     L.tree2d_learn_get_weights.argtypes = [fp, ctypes.c_int]
     L.tree2d_learn_set_options.argtypes = [ctypes.c_float, ctypes.c_int, ctypes.c_double]
+    L.tree2d_learn_set_envelope.argtypes = [ctypes.c_double]
+    L.tree2d_learn_set_envelope.restype = ctypes.c_int
     L.tree2d_learn_collect.argtypes = [ctypes.c_int, ctypes.c_uint, fp, _ip]
     L.tree2d_learn_train.argtypes = [ctypes.c_int, fp, _ip, ctypes.c_int, ctypes.c_int, ctypes.c_float,
                                      ctypes.c_uint, fp]
@@ -341,6 +344,12 @@ def learn_get_weights():
 
 def learn_set_options(direct_bias: float = 1.0, order_margin: int = 1, budget: float = 3e-7):
     _check(load().tree2d_learn_set_options(direct_bias, order_margin, budget), "learn_set_options")
+
+
+def learn_set_envelope(k_per_leaf_max: float):
+    """Training envelope: the largest mean K-list entries per leaf the
+    network was trained on (denser solves run the fixed mixed form)."""
+    _check(load().tree2d_learn_set_envelope(k_per_leaf_max), "learn_set_envelope")
 
 
 def learn_collect(max_samples: int, seed: int = 0):

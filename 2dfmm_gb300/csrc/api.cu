@@ -616,7 +616,8 @@ const char *tree2d_error_string(int code) {
     case TREE2D_ERR_TIMEOUT: return "a bounded device loop gave up (traversal stack overflow)";
     case TREE2D_ERR_MODE: return "unknown or unavailable mode";
     case TREE2D_ERR_TOO_LARGE:
-      return "input larger than the fixed scratch of tree2d_solve_device_static (65536 blobs, 32 MiB)";
+      return "problem too large for this path (the fixed scratch of tree2d_solve_device_static: 65536 blobs, "
+             "32 MiB; or more than 2^31 - 1 interaction-list entries)";
     default: return "unknown error";
   }
 }
@@ -862,6 +863,14 @@ int tree2d_learn_set_options(float direct_bias, int order_margin, double budget)
   L.lp->direct_bias = direct_bias;
   L.lp->order_margin = order_margin;
   L.lp->budget = budget;
+  return TREE2D_OK;
+}
+
+int tree2d_learn_set_envelope(double k_per_leaf_max) {
+  Lib &L = lib();
+  std::lock_guard<std::mutex> lk(L.mu);
+  if (!(k_per_leaf_max >= 0.0) || !std::isfinite(k_per_leaf_max)) return fail(TREE2D_ERR_BAD_PARAMS);
+  L.lp->k_per_leaf_max = k_per_leaf_max;
   return TREE2D_OK;
 }
 

@@ -25,6 +25,7 @@ struct LearnedParams {
   float direct_bias = 1.0f;  // added to the direct logit: leans towards exact evaluation
   int order_margin = 1;      // chosen order raised by this much (capped at 16)
   double budget = 3e-7;      // label budget: per-interaction error / (sum|G| / R0)
+  double k_per_leaf_max = 0; // training envelope (mean K entries per leaf); 0 = none
 };
 
 // Per-leaf source statistics for the features.

@@ -492,21 +492,20 @@ __global__ void __launch_bounds__(kScan3Threads) k_scan3_tiles(const int *a, con
   }
 }
 
-__global__ void __launch_bounds__(1024) k_scan3_sums(int *tile_sums, int ntiles) {
-  __shared__ int sh[32];
-  for (int k = 0; k < 3; k++) {
-    int *t = tile_sums + k * (ntiles + 1);
-    int run = 0;
-    for (int base = 0; base < ntiles; base += 1024) {
-      const int i = base + threadIdx.x;
-      const int v = i < ntiles ? t[i] : 0;
-      int tot;
-      const int ex = block_exclusive_scan(v, sh, tot);
-      if (i < ntiles) t[i] = run + ex;
-      run += tot;
-    }
-    if (threadIdx.x == 0) t[ntiles] = run;
+// One thread per array: 64-bit running sums over the tile sums.  List
+// positions are ints, so a total beyond INT_MAX is reported as -1 (the host
+// then stops before any list is filled).
+__global__ void k_scan3_sums(int *tile_sums, int ntiles) {
+  const int k = threadIdx.x;
+  if (k >= 3) return;
+  int *t = tile_sums + k * (ntiles + 1);
+  long long run = 0;
+  for (int i = 0; i < ntiles; i++) {
+    const int v = t[i];
+    t[i] = (int)(run < 2147483647ll ? run : 2147483647ll);
+    run += v;
   }
+  t[ntiles] = run > 2147483647ll ? -1 : (int)run;
 }
 
 __global__ void __launch_bounds__(kScan3Threads) k_scan3_apply(int *a, int *b, int *c, int len, const int *tile_sums,
@@ -1137,7 +1136,7 @@ int mixed_lists(MixedView &m, cudaStream_t s) {
   k_lists<false><<<(m.nleaf + kWalkWarps - 1) / kWalkWarps, 32 * kWalkWarps, 0, s>>>(m);
   const int ntiles = max(1, (m.nleaf + kScanTile3 - 1) / kScanTile3);
   k_scan3_tiles<<<ntiles, kScan3Threads, 0, s>>>(m.u_off, m.w_off, m.k_off, m.nleaf, m.scan_tmp, ntiles);
-  k_scan3_sums<<<1, 1024, 0, s>>>(m.scan_tmp, ntiles);
+  k_scan3_sums<<<1, 32, 0, s>>>(m.scan_tmp, ntiles);
   k_scan3_apply<<<ntiles, kScan3Threads, 0, s>>>(m.u_off, m.w_off, m.k_off, m.nleaf, m.scan_tmp, ntiles);
   g_launches.fetch_add(8, std::memory_order_relaxed);
   T2D_CUDA_TRY(cudaGetLastError());
@@ -1378,15 +1377,20 @@ int mixed_solve(Workspace &ws, const Tree &t, const MixedParams &mp, double *d_u
   T2D_CUDA_TRY(cudaMemcpyAsync(&tot[1], m.w_off + nl, 4, cudaMemcpyDeviceToHost, s));
   T2D_CUDA_TRY(cudaMemcpyAsync(&tot[2], m.k_off + nl, 4, cudaMemcpyDeviceToHost, s));
   T2D_CUDA_TRY(cudaStreamSynchronize(s));
-  size_t lneed = 2 * Arena::bytes_for(tot[0] + 1, 4) + Arena::bytes_for(tot[1] + 1, 4) +
-                 2 * Arena::bytes_for(tot[2] + 1, 4);
+  if (tot[0] < 0 || tot[1] < 0 || tot[2] < 0) {
+    // more than 2^31 - 1 entries in one list kind (int positions)
+    note_cuda_error(cudaErrorMemoryAllocation, "interaction lists beyond 2^31 entries");
+    return TREE2D_ERR_TOO_LARGE;
+  }
+  size_t lneed = 2 * Arena::bytes_for((size_t)tot[0] + 1, 4) + Arena::bytes_for((size_t)tot[1] + 1, 4) +
+                 2 * Arena::bytes_for((size_t)tot[2] + 1, 4);
   T2D_CUDA_TRY(ws.mx_lists.reserve(lneed));
   ws.mx_lists.reset();
-  m.u_idx = ws.mx_lists.take<int>(tot[0] + 1);
-  m.w_idx = ws.mx_lists.take<int>(tot[1] + 1);
-  m.k_idx = ws.mx_lists.take<int>(tot[2] + 1);
-  m.u_leaf = ws.mx_lists.take<int>(tot[0] + 1);
-  m.k_leaf = ws.mx_lists.take<int>(tot[2] + 1);
+  m.u_idx = ws.mx_lists.take<int>((size_t)tot[0] + 1);
+  m.w_idx = ws.mx_lists.take<int>((size_t)tot[1] + 1);
+  m.k_idx = ws.mx_lists.take<int>((size_t)tot[2] + 1);
+  m.u_leaf = ws.mx_lists.take<int>((size_t)tot[0] + 1);
+  m.k_leaf = ws.mx_lists.take<int>((size_t)tot[2] + 1);
   rc = mixed_fill_lists(m, s);
   if (rc) return rc;
   // keep the view for sampling (training data)
@@ -1401,7 +1405,14 @@ int mixed_solve(Workspace &ws, const Tree &t, const MixedParams &mp, double *d_u
   // the downward pass (both chains are latency-bound and share the GPU
   // well).  A batched tree runs the fixed mixed form: the network's
   // reference scale u_ref is one per tree.
-  const bool learned = mp.learned && mp.lp && mp.lp->have_weights && t.lev0 == 0;
+  // the network decides only inside its training envelope: denser lists
+  // than it was trained on would add up more accepted errors per target
+  // than its per-interaction budget allows for
+  const bool in_envelope = mp.lp && (mp.lp->k_per_leaf_max <= 0.0 || (double)tot[2] <= mp.lp->k_per_leaf_max * nl);
+  const bool learned = mp.learned && mp.lp && mp.lp->have_weights && t.lev0 == 0 && in_envelope;
+  st.learned_active = learned ? 1 : 0;
+  st.n_list_u = tot[0];
+  st.n_list_k = tot[2];
   unsigned char *u_dec = nullptr, *k_dec = nullptr;
   const bool side = (learned || mp.learned) && t.lev0 == 0;
   if (side) {

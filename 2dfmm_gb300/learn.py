@@ -28,11 +28,23 @@ WEIGHTS_VERSION = 1
 HERE = os.path.dirname(os.path.abspath(__file__))
 DEFAULT_WEIGHTS = os.path.join(HERE, "data", "learned_weights.npz")
 
+# The network's labels bound the error of one accepted interaction; the
+# accepted errors of a target add up over its list, so a solve whose lists
+# are much denser than the training solves' needs more accuracy per
+# interaction than the network learned to keep.  The library therefore
+# applies the decisions only up to ENVELOPE_FACTOR x the training solves'
+# largest mean K-list length per leaf and runs the fixed mixed form beyond.
+# Measured with the packaged network (trained at 45.5 K entries per leaf) on
+# the two-patch + sheet distribution: 103.7 per leaf (2.3x, 4M blobs,
+# configuration 3) gives relL2 7.7e-7; 136 (3.0x, 8M) 1.14e-6; 354 (7.8x,
+# 16M) 2.3e-6, while the fixed mixed form stays at 4.7-5.1e-7 throughout.
+ENVELOPE_FACTOR = 2.5
 
-def save_weights(path, theta, meta):
+
+def save_weights(path, theta, meta, k_per_leaf_train=None):
     os.makedirs(os.path.dirname(os.path.abspath(path)), exist_ok=True)
-    np.savez(path, version=WEIGHTS_VERSION, theta=np.asarray(theta, np.float32),
-             meta=json.dumps(meta))
+    extra = {} if k_per_leaf_train is None else {"k_per_leaf_train": np.float64(k_per_leaf_train)}
+    np.savez(path, version=WEIGHTS_VERSION, theta=np.asarray(theta, np.float32), meta=json.dumps(meta), **extra)
 
 
 def load_weights(path=DEFAULT_WEIGHTS):
@@ -43,6 +55,18 @@ def load_weights(path=DEFAULT_WEIGHTS):
     if int(d["version"]) != WEIGHTS_VERSION:
         return None
     return d["theta"].astype(np.float32)
+
+
+def load_envelope(path=DEFAULT_WEIGHTS):
+    """K-list entries per leaf up to which the network's decisions apply
+    (ENVELOPE_FACTOR x the training solves' largest mean), or 0 (no
+    limit) for a weights file without the training figure."""
+    if not os.path.exists(path):
+        return 0.0
+    d = np.load(path)
+    if "k_per_leaf_train" not in d.files:
+        return 0.0
+    return float(d["k_per_leaf_train"]) * ENVELOPE_FACTOR
 
 
 def _dev_arrays(torch, b):
@@ -89,9 +113,11 @@ def run(n=1_048_576, steps=100, dt=1e-3, train_until=20, samples=200_000, train_
     Xs, ys = [], []
     log = {"collect": [], "score": []}
     t0 = time.time()
+    k_per_leaf = 0.0
     for step in range(train_until + 1):
         arrays = _dev_arrays(torch, b)
         ms, st = _timed_solve(P, torch, arrays, n, P.MODE_MIXED)
+        k_per_leaf = max(k_per_leaf, st["n_list_k"] / max(1, st["n_leaves"]))
         X, y = P.learn_collect(per_step, seed=seed * 1000 + step)
         Xs.append(X)
         ys.append(y)
@@ -106,9 +132,10 @@ def run(n=1_048_576, steps=100, dt=1e-3, train_until=20, samples=200_000, train_
     theta = P.learn_get_weights()
     hist = np.bincount(y, minlength=14).tolist()
     summary = {"samples": int(len(y)), "label_histogram": hist, "final_loss": loss, "collect_s": t_collect,
-               "train_s": t_train}
+               "train_s": t_train, "k_per_leaf_train": k_per_leaf}
     if out:
-        save_weights(out, theta, summary)
+        save_weights(out, theta, summary, k_per_leaf_train=k_per_leaf)
+    P.learn_set_envelope(k_per_leaf * ENVELOPE_FACTOR)
     # score steps 21..steps
     tm, tl, tp = [], [], []
     for step in range(train_until + 1, steps + 1):

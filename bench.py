@@ -347,8 +347,10 @@ def run_ours(args):
             learned_note = f"none found at {os.path.relpath(path, ROOT)}: fixed mixed form (the fallback)"
         else:
             P.learn_set_weights(theta)
+            envelope = L.load_envelope(path)
+            P.learn_set_envelope(envelope)
             learned_note = (f"{os.path.relpath(path, ROOT)} (trained on configuration-5 steps 0-20 by "
-                            "2dfmm_gb300/learn.py)")
+                            f"2dfmm_gb300/learn.py); decisions applied up to {envelope:.1f} K-list entries per leaf")
     n = b.n
     xy = torch.from_numpy(b.xy).to(dev).contiguous()
     cir = torch.from_numpy(b.cir).to(dev)
@@ -436,6 +438,8 @@ def run_ours(args):
             "gpu_launches": int(sum(s["n_launches"] for s in sts)),
             "tuned": {"eval_variant": int(st["eval_variant"]),
                       "variants": "0/1 global loads, 2/3 bulk-copy staging; 4/8 warps per block"},
+            "learned_active": bool(st["learned_active"]),
+            "k_list_per_leaf": st["n_list_k"] / max(1, st["n_leaves"]),
             "e2e": {"value": world * n / e2e_t, "unit": UNIT, "h2d_bytes_per_step": n * 32,
                     "d2h_bytes_per_step": n * 16, "api": "make_tree + biot_tree_batch (host buffers)",
                     "make_tree_ms": statistics.mean(a for a, _ in e2e_split),

@@ -58,7 +58,8 @@ void biot_tree(double x, double y, double *u, double *v);
 #define TREE2D_ERR_NO_DEVICE 7     /* no CUDA device                               */
 #define TREE2D_ERR_TIMEOUT 8       /* a bounded device loop gave up                */
 #define TREE2D_ERR_MODE 9          /* unknown mode                                 */
-#define TREE2D_ERR_TOO_LARGE 10    /* beyond the fixed scratch of the static solve */
+#define TREE2D_ERR_TOO_LARGE 10    /* beyond the fixed scratch of the static solve,
+                                      or more than 2^31 - 1 interaction-list entries */
 
 /* Evaluation modes (tree2d_set_mode). */
 #define TREE2D_MODE_PLAIN 0        /* FP64 treecode, reference semantics             */
@@ -139,6 +140,12 @@ typedef struct {
   int eval_variant;       /* mixed: near-field kernel variant that ran
                              (0/1: global loads, 4/8 warps per block;
                               2/3: blobs staged by bulk copies, 4/8)    */
+  int learned_active;     /* learned: 1 if the network's decisions were
+                             applied, 0 if the solve ran the fixed mixed
+                             form (no weights, a batched tree, or lists
+                             outside the network's training envelope)   */
+  long long n_list_u;     /* mixed: U (direct) list entries             */
+  long long n_list_k;     /* mixed: K (correction) list entries         */
 } tree2d_stats_t;
 int tree2d_get_stats(tree2d_stats_t *out);
 
@@ -209,6 +216,13 @@ int tree2d_learn_get_weights(float *theta, int n);
  * order raised by this much; budget: label tolerance per interaction in
  * units of sum|G| / root side.  Defaults 1.0, 1, 3e-7. */
 int tree2d_learn_set_options(float direct_bias, int order_margin, double budget);
+/* Training envelope of the loaded network: the largest mean number of K
+ * (correction) list entries per leaf the training solves had.  A solve
+ * whose lists are denser than this runs the fixed mixed form instead (the
+ * network's per-interaction error budget does not bound the sum over more
+ * interactions than it was trained on); tree2d_get_stats reports it in
+ * learned_active.  0 = no limit (the default). */
+int tree2d_learn_set_envelope(double k_per_leaf_max);
 /* Training data from the last tree2d_solve_device in mixed or learned mode:
  * up to max_samples interactions drawn with `seed`, their features
  * (features[max][16]) and the cheapest class whose error against the FP64

@@ -88,3 +88,31 @@ def test_learned_mode_keeps_accuracy_and_saves_direct_work(gpu_lib):
     P.set_mode(P.MODE_PLAIN)
     assert rel_l <= 1e-6, (rel_l, rel_m)
     assert st_l["n_pairs"] < st_m["n_pairs"], (st_l["n_pairs"], st_m["n_pairs"])
+
+
+@pytest.mark.gpu
+def test_training_envelope_falls_back_to_the_mixed_form(gpu_lib):
+    """Lists denser than the network's training envelope run the fixed mixed
+    form (bit-identical to it), and the stats say so."""
+    torch = pytest.importorskip("torch")
+    import importlib
+    P = gpu_lib
+    L = importlib.import_module("2dfmm_gb300.learn")
+    theta = L.load_weights()
+    if theta is None:
+        pytest.skip("no packaged weights")
+    W = workloads()
+    b = W.lamb_oseen(131_072, seed=23)
+    P.learn_set_weights(theta)
+    try:
+        P.learn_set_envelope(0.0)  # no limit: the network decides
+        uv_l, _, _, _, st_l = _solve(P, torch, b, P.MODE_LEARNED)
+        assert st_l["learned_active"] == 1 and st_l["n_list_k"] > 0
+        P.learn_set_envelope(1.0)  # far below any real list density
+        uv_g, _, _, _, st_g = _solve(P, torch, b, P.MODE_LEARNED)
+        uv_m, _, _, _, st_m = _solve(P, torch, b, P.MODE_MIXED)
+        assert st_g["learned_active"] == 0
+        assert np.array_equal(uv_g.cpu().numpy(), uv_m.cpu().numpy())
+    finally:
+        P.learn_set_envelope(0.0)
+        P.set_mode(P.MODE_PLAIN)
