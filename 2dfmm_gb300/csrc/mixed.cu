@@ -1415,6 +1415,21 @@ int mixed_solve(Workspace &ws, const Tree &t, const MixedParams &mp, double *d_u
   st.n_list_k = tot[2];
   unsigned char *u_dec = nullptr, *k_dec = nullptr;
   const bool side = (learned || mp.learned) && t.lev0 == 0;
+  // after the fork, an early return first waits for the second stream, so
+  // that no kernel of this solve still runs when its buffers are reused
+  bool forked = false;
+  auto drain = [&](int code) {
+    if (forked) cudaStreamSynchronize(ws.side);
+    return code;
+  };
+#define T2D_TRY_DRAIN(expr)                 \
+  do {                                      \
+    cudaError_t e_ = (expr);                \
+    if (e_ != cudaSuccess) {                \
+      note_cuda_error(e_, #expr);           \
+      return drain(TREE2D_ERR_CUDA);        \
+    }                                       \
+  } while (0)
   if (side) {
     // leaf statistics and u_ref (also used by sampling), then decisions
     const size_t wim = learn_weight_image_elems();
@@ -1441,30 +1456,32 @@ int mixed_solve(Workspace &ws, const Tree &t, const MixedParams &mp, double *d_u
     cudaStream_t s2 = ws.side;
     T2D_CUDA_TRY(cudaEventRecord(ws.fork_ev, s));
     T2D_CUDA_TRY(cudaStreamWaitEvent(s2, ws.fork_ev, 0));
+    forked = true;
     rc = learned_leaf_stats(m, stats, s2);
-    if (rc) return rc;
+    if (rc) return drain(rc);
     rc = learned_uref(m, stats, t.root, uref, s2);
-    if (rc) return rc;
+    if (rc) return drain(rc);
     if (learned) {
       rc = learned_decide(m, stats, uref, wimg, bias, mp.lp->direct_bias, tot[0], tot[2], u_dec, k_dec, s2);
-      if (rc) return rc;
+      if (rc) return drain(rc);
     }
-    T2D_CUDA_TRY(cudaEventRecord(ws.join_ev, s2));
+    T2D_TRY_DRAIN(cudaEventRecord(ws.join_ev, s2));
   }
   rc = mixed_upward(m, t.depth, s);
-  if (rc) return rc;
-  T2D_CUDA_TRY(cudaMemsetAsync(m.L, 0, sizeof(float) * (size_t)nc * 2 * P, s));
+  if (rc) return drain(rc);
+  T2D_TRY_DRAIN(cudaMemsetAsync(m.L, 0, sizeof(float) * (size_t)nc * 2 * P, s));
   rc = tc ? m2l_tensor_cores(m, dimg, cls_list, cls_count, s) : m2l_cuda_cores(m, dm2l, s);
-  if (rc) return rc;
+  if (rc) return drain(rc);
   st.m2l_path = tc ? 2 : 1;
   rc = mixed_downward(m, t.depth, s);
-  if (rc) return rc;
-  if (side) T2D_CUDA_TRY(cudaStreamWaitEvent(s, ws.join_ev, 0));
+  if (rc) return drain(rc);
+  if (side) T2D_TRY_DRAIN(cudaStreamWaitEvent(s, ws.join_ev, 0));
   T2D_CUDA_TRY(cudaEventRecord(ws.ev[4], s));
   const Decisions dec = learned ? Decisions{u_dec, k_dec, mp.lp->order_margin} : Decisions{nullptr, nullptr, 0};
   rc = near_field(ws, mp, m, learned, dec, d_uv, t.perm, s, st);
   if (rc) return rc;
   T2D_CUDA_TRY(cudaEventRecord(ws.ev[5], s));
+#undef T2D_TRY_DRAIN
   return TREE2D_OK;
 }
 
