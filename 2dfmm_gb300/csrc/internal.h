@@ -61,6 +61,8 @@ struct DevStatus {
   unsigned long long n_m2l;
   unsigned long long n_fallback;  // targets whose traversal stack overflowed
   int deeper;              // build: keys of kShortKeyLevels levels do not suffice
+  int list_overflow;       // mixed: a leaf's lists did not fit the one-walk scratch
+  int list_max;            // mixed: most list entries (U + W + K) of one leaf
 };
 
 // Bump allocator over one device allocation.  Buffers are 256-byte aligned.
@@ -143,6 +145,7 @@ struct Workspace {
   long mx_tot[3] = {0, 0, 0};  // U, W, K list entries of that solve
   std::map<uint64_t, int> eval_tuned;  // size class -> fastest near-field variant
   int last_depth = 0;  // depth of the last tree built (sizes the next keys)
+  int list_cap = 256;  // entries per leaf of the one-walk list scratch (from the last solve)
   DevStatus *status = nullptr;   // device
   DevStatus *h_status = nullptr; // pinned host mirror
   cudaEvent_t ev[8] = {};

@@ -334,8 +334,13 @@ constexpr int kWalkWarps = 4;
 constexpr int kWalkStack = 1024;
 constexpr unsigned kTagK = 0x80000000u;
 
-template <bool kFill>
+// kMode 0: count the entries of each list kind; 1: write the lists at the
+// scanned offsets; 2: count and also store the walk's entries ((kind << 30)
+// | id, in emission order) in the leaf's scratch row, which k_lists_compact
+// turns into the same lists without a second walk.
+template <int kMode>
 __global__ void __launch_bounds__(32 * kWalkWarps) k_lists(MixedView m) {
+  constexpr bool kFill = kMode == 1;
   __shared__ unsigned s_stack[kWalkWarps][kWalkStack];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int l = blockIdx.x * kWalkWarps + warp;
@@ -363,8 +368,14 @@ __global__ void __launch_bounds__(32 * kWalkWarps) k_lists(MixedView m) {
   }
   int *const dst[3] = {m.u_idx, m.w_idx, m.k_idx};
   int *const own[3] = {m.u_leaf, nullptr, m.k_leaf};
+  int *const row = kMode == 2 ? m.list_scratch + (size_t)l * m.list_cap : nullptr;
   // each lane offers (kind, id), kind -1 = nothing; outputs keep lane order
   auto emit = [&](int kind, int id) {
+    if (kMode == 2) {
+      const unsigned any = __ballot_sync(0xffffffffu, kind >= 0);
+      const int pos = base[0] + base[1] + base[2] + __popc(any & lt);
+      if (kind >= 0 && pos < m.list_cap) row[pos] = (int)(((unsigned)kind << 30) | (unsigned)id);
+    }
 #pragma unroll
     for (int k = 0; k < 3; k++) {
       const unsigned bal = __ballot_sync(0xffffffffu, kind == k);
@@ -444,6 +455,40 @@ __global__ void __launch_bounds__(32 * kWalkWarps) k_lists(MixedView m) {
     m.u_off[l] = base[0];
     m.w_off[l] = base[1];
     m.k_off[l] = base[2];
+    if (kMode == 2) {
+      const int total = base[0] + base[1] + base[2];
+      atomicMax(&m.st->list_max, total);
+      if (total > m.list_cap) atomicExch(&m.st->list_overflow, 1);
+    }
+  }
+}
+
+// The lists from the one-walk scratch: one warp per leaf reads its row in
+// emission order and writes each kind at its scanned offsets, in the order
+// the filling walk would (lane order within an emission).
+__global__ void __launch_bounds__(256) k_lists_compact(MixedView m) {
+  const int l = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (l >= m.nleaf) return;
+  const unsigned lt = (1u << lane) - 1u;
+  int base[3] = {m.u_off[l], m.w_off[l], m.k_off[l]};
+  const int n = (m.u_off[l + 1] - base[0]) + (m.w_off[l + 1] - base[1]) + (m.k_off[l + 1] - base[2]);
+  const int *row = m.list_scratch + (size_t)l * m.list_cap;
+  int *const dst[3] = {m.u_idx, m.w_idx, m.k_idx};
+  int *const own[3] = {m.u_leaf, nullptr, m.k_leaf};
+  for (int c0 = 0; c0 < n; c0 += 32) {
+    const int e = c0 + lane;
+    const unsigned enc = e < n ? (unsigned)row[e] : 0u;
+    const int kind = e < n ? (int)(enc >> 30) : -1, id = (int)(enc & 0x3fffffffu);
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      const unsigned bal = __ballot_sync(0xffffffffu, kind == k);
+      if (kind == k) {
+        const int pos = base[k] + __popc(bal & lt);
+        dst[k][pos] = id;
+        if (own[k]) own[k][pos] = l;
+      }
+      base[k] += __popc(bal);
+    }
   }
 }
 
@@ -1133,7 +1178,10 @@ int mixed_lists(MixedView &m, cudaStream_t s) {
   k_parent<<<cb, 256, 0, s>>>(m);
   k_colleagues<<<cb, 256, 0, s>>>(m);
   k_vx_lists<<<cb, 256, 0, s>>>(m);
-  k_lists<false><<<(m.nleaf + kWalkWarps - 1) / kWalkWarps, 32 * kWalkWarps, 0, s>>>(m);
+  if (m.list_scratch)
+    k_lists<2><<<(m.nleaf + kWalkWarps - 1) / kWalkWarps, 32 * kWalkWarps, 0, s>>>(m);
+  else
+    k_lists<0><<<(m.nleaf + kWalkWarps - 1) / kWalkWarps, 32 * kWalkWarps, 0, s>>>(m);
   const int ntiles = max(1, (m.nleaf + kScanTile3 - 1) / kScanTile3);
   k_scan3_tiles<<<ntiles, kScan3Threads, 0, s>>>(m.u_off, m.w_off, m.k_off, m.nleaf, m.scan_tmp, ntiles);
   k_scan3_sums<<<1, 32, 0, s>>>(m.scan_tmp, ntiles);
@@ -1143,8 +1191,11 @@ int mixed_lists(MixedView &m, cudaStream_t s) {
   return TREE2D_OK;
 }
 
-int mixed_fill_lists(MixedView &m, cudaStream_t s) {
-  k_lists<true><<<(m.nleaf + kWalkWarps - 1) / kWalkWarps, 32 * kWalkWarps, 0, s>>>(m);
+int mixed_fill_lists(MixedView &m, bool from_scratch, cudaStream_t s) {
+  if (from_scratch)
+    k_lists_compact<<<(int)(((long)m.nleaf * 32 + 255) / 256), 256, 0, s>>>(m);
+  else
+    k_lists<1><<<(m.nleaf + kWalkWarps - 1) / kWalkWarps, 32 * kWalkWarps, 0, s>>>(m);
   g_launches.fetch_add(1, std::memory_order_relaxed);
   T2D_CUDA_TRY(cudaGetLastError());
   return TREE2D_OK;
@@ -1299,6 +1350,11 @@ int mixed_solve(Workspace &ws, const Tree &t, const MixedParams &mp, double *d_u
   need += Arena::bytes_for(3 * ((size_t)nl / kScanTile3 + 2), 4);  // scan tile sums
   need += Arena::bytes_for((size_t)t.nsets, 4);                     // cutoff per set
   need += Arena::bytes_for(nc, 4) + Arena::bytes_for(2 * kKeyLevels + 4, 4);  // cells by level
+  // one-walk list scratch, sized from the previous solve's largest leaf
+  // (a leaf beyond it makes this solve walk twice instead); kept below 4 GB
+  const int cap = ws.list_cap;
+  const bool one_walk = (size_t)nl * (size_t)cap * 4 <= (size_t(4) << 30) && nc < (1 << 30);
+  if (one_walk) need += Arena::bytes_for((size_t)nl * cap, 4);
   need += Arena::bytes_for((size_t)nc * 2 * P, 4) * 2;
   need += Arena::bytes_for((size_t)nc * 4, 4) + 1024;  // class lists + counts
   need += 256;
@@ -1343,6 +1399,8 @@ int mixed_solve(Workspace &ws, const Tree &t, const MixedParams &mp, double *d_u
   m.k_off = ws.mx_arena.take<int>((size_t)nl + 1);
   m.scan_tmp = ws.mx_arena.take<int>(3 * ((size_t)nl / kScanTile3 + 2));
   m.by_level = ws.mx_arena.take<int>(nc);
+  m.list_cap = cap;
+  m.list_scratch = one_walk ? ws.mx_arena.take<int>((size_t)nl * cap) : nullptr;
   m.level_off = ws.mx_arena.take<int>(2 * kKeyLevels + 4);
   m.M = ws.mx_arena.take<float>((size_t)nc * 2 * P);
   m.L = ws.mx_arena.take<float>((size_t)nc * 2 * P);
@@ -1376,7 +1434,15 @@ int mixed_solve(Workspace &ws, const Tree &t, const MixedParams &mp, double *d_u
   T2D_CUDA_TRY(cudaMemcpyAsync(&tot[0], m.u_off + nl, 4, cudaMemcpyDeviceToHost, s));
   T2D_CUDA_TRY(cudaMemcpyAsync(&tot[1], m.w_off + nl, 4, cudaMemcpyDeviceToHost, s));
   T2D_CUDA_TRY(cudaMemcpyAsync(&tot[2], m.k_off + nl, 4, cudaMemcpyDeviceToHost, s));
+  T2D_CUDA_TRY(cudaMemcpyAsync(ws.h_status, ws.status, sizeof(DevStatus), cudaMemcpyDeviceToHost, s));
   T2D_CUDA_TRY(cudaStreamSynchronize(s));
+  const bool from_scratch = one_walk && !ws.h_status->list_overflow;
+  {
+    // the next solve's scratch rows: 1.25 x this solve's largest leaf
+    int want = ws.h_status->list_max + ws.h_status->list_max / 4 + 32;
+    want = (want + 31) & ~31;
+    ws.list_cap = want < 64 ? 64 : (want > 8192 ? 8192 : want);
+  }
   if (tot[0] < 0 || tot[1] < 0 || tot[2] < 0) {
     // more than 2^31 - 1 entries in one list kind (int positions)
     note_cuda_error(cudaErrorMemoryAllocation, "interaction lists beyond 2^31 entries");
@@ -1391,7 +1457,7 @@ int mixed_solve(Workspace &ws, const Tree &t, const MixedParams &mp, double *d_u
   m.k_idx = ws.mx_lists.take<int>((size_t)tot[2] + 1);
   m.u_leaf = ws.mx_lists.take<int>((size_t)tot[0] + 1);
   m.k_leaf = ws.mx_lists.take<int>((size_t)tot[2] + 1);
-  rc = mixed_fill_lists(m, s);
+  rc = mixed_fill_lists(m, from_scratch, s);
   if (rc) return rc;
   // keep the view for sampling (training data)
   if (!ws.mxv) ws.mxv = new MixedView();

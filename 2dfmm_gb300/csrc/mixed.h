@@ -37,6 +37,8 @@ struct MixedView {
   int *u_off, *w_off, *k_off;  // per leaf (+1)
   int *scan_tmp;               // tile sums of the list-size scan
   int *by_level;               // cell ids grouped by level (order within a level arbitrary)
+  int *list_scratch;           // one-walk list build: list_cap entries per leaf (or null)
+  int list_cap;
   int *level_off;              // [kKeyLevels + 2]: start of each level in by_level, then cursors
   int *u_idx, *w_idx, *k_idx;
   int *u_leaf, *k_leaf;  // leaf ordinal of each U / K entry
@@ -48,7 +50,7 @@ struct MixedView {
 cudaError_t mixed_tables(int P, float *h_m2l, float *h_m2m, float *h_l2l);
 int mixed_leaf_setup(MixedView &m, const Tree &t, cudaStream_t s);
 int mixed_lists(MixedView &m, cudaStream_t s);
-int mixed_fill_lists(MixedView &m, cudaStream_t s);
+int mixed_fill_lists(MixedView &m, bool from_scratch, cudaStream_t s);
 int mixed_upward(MixedView &m, int depth, cudaStream_t s);
 int mixed_downward(MixedView &m, int depth, cudaStream_t s);
 

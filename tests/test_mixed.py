@@ -126,3 +126,36 @@ def test_near_field_variants_bit_identical(gpu_lib, mode):
     finally:
         P.set_tuning(True, -1)
         P.set_mode(P.MODE_PLAIN)
+
+
+@pytest.mark.gpu
+def test_one_walk_lists_equal_two_walk_lists(gpu_lib):
+    """The interaction lists are built in one walk into per-leaf scratch rows
+    sized from the previous solve, or in two walks (count, then fill) when a
+    leaf overflows its row.  Both give the same lists, hence the same
+    velocities bit for bit."""
+    torch = pytest.importorskip("torch")
+    import importlib
+    P = gpu_lib
+    W = importlib.import_module("2dfmm_gb300.workloads")
+    dev = torch.device("cuda:0")
+    P.set_mode(P.MODE_MIXED)
+    P.set_mixed_params(16, 3.0, True)
+
+    def solve(b):
+        P.set_params(b.nterms, b.num_p, b.theta)
+        xy = torch.from_numpy(b.xy).to(dev)
+        cir = torch.from_numpy(b.cir).to(dev)
+        cor = torch.from_numpy(b.cor).to(dev)
+        uv = torch.empty_like(xy)
+        P.solve_device(xy.data_ptr(), cir.data_ptr(), cor.data_ptr(), uv.data_ptr(), b.n)
+        torch.cuda.synchronize()
+        return uv.cpu().numpy(), P.stats()
+
+    solve(W.uniform(3000, seed=4))  # small lists: the next rows are short
+    dense = W.uniform(100_000, seed=5, sigma=0.05)  # cores over many leaves: long correction lists
+    uv_a, st_a = solve(dense)  # rows too short: two walks
+    uv_b, st_b = solve(dense)  # rows sized from the first solve: one walk
+    assert st_a["n_list_k"] / st_a["n_leaves"] > 100
+    assert np.array_equal(uv_a, uv_b) and st_a["n_pairs"] == st_b["n_pairs"]
+    P.set_mode(P.MODE_PLAIN)
