@@ -183,55 +183,93 @@ __global__ void k_colleagues(MixedView m) {
 
 __constant__ signed char c_slot[4][6][6];  // [class][dy+2+qy][dx+2+qx] -> slot (or -1)
 
-// V and X lists of every cell of level >= 2.
-__global__ void k_vx_lists(MixedView m) {
+// V and X lists of every cell of level >= 2 (counted from its set root).
+// One warp per internal cell p builds the lists of p's children: the four
+// siblings share p's 3x3 neighbourhood, so lane k loads colleague k of p
+// (its children, or itself when it is a leaf, and the coarser leaf at that
+// position) once for all four, then every child takes from each lane:
+//   V: the colleague's children that are not adjacent to the child, at the
+//      slot of their offset (unique per offset, so the lanes write apart);
+//   X: the colleague when it is a leaf, or the coarser leaf, when not
+//      adjacent to the child (a position has at most one of the two; a
+//      coarser leaf seen at several positions is kept once), in position
+//      order.
+__global__ void __launch_bounds__(256) k_vx_lists(MixedView m) {
   // the slot table in shared memory: the lanes index it divergently, which
   // constant memory would serialise
   __shared__ signed char slot[4][6][6];
   for (int i = threadIdx.x; i < 4 * 6 * 6; i += blockDim.x) (&slot[0][0][0])[i] = (&c_slot[0][0][0])[i];
   __syncthreads();
-  int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= m.ncell) return;
-  int *V = m.vlist + (size_t)c * 27;
-  int *X = m.xlist + (size_t)c * 8;
-  for (int s = 0; s < 27; s++) V[s] = -1;
-  for (int s = 0; s < 8; s++) X[s] = -1;
-  const int lev = m.level[c];
-  if (lev - m.lev0 < 2) return;  // levels counted from the cell's set root
-  const int p = m.parent[c];
-  const unsigned ix = m.ix[c], iy = m.iy[c];
-  const int qx = ix & 1, qy = iy & 1, cls = qx + 2 * qy;
-  int nx = 0, nv = 0;
-  for (int k = 0; k < 9; k++) {
-    if (k == 4) continue;
-    const int e = m.coll[p * 9 + k];
+  const int p = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (p >= m.ncell) return;  // uniform over the warp
+  const unsigned lt = (1u << lane) - 1u;
+  if (p == 0) {  // the root is nobody's child
+    if (lane < 27) m.vlist[lane] = -1;
+    if (lane < 8) m.xlist[lane] = -1;
+  }
+  if (m.leaf[p]) return;
+  const int4 chp = reinterpret_cast<const int4 *>(m.child)[p];
+  // lane k < 8: position k of p's 3x3 neighbourhood (the centre skipped)
+  int e = -1, co = -1, elev = 0, colev = 0;
+  unsigned ex = 0, ey = 0, cox = 0, coy = 0;
+  bool eleaf = false;
+  int4 ech = make_int4(-1, -1, -1, -1);
+  if (lane < 8) {
+    const int k = lane < 4 ? lane : lane + 1;
+    e = m.coll[p * 9 + k];
+    co = m.coarse[p * 9 + k];
     if (e >= 0) {
-      if (m.leaf[e]) {
-        if (!adj_cells(m, e, c)) X[nx++] = e;
-      } else {
-        const int4 ch = reinterpret_cast<const int4 *>(m.child)[e];
-        for (int q = 0; q < 4; q++) {
-          const int cc = (&ch.x)[q];
-          if (cc < 0) continue;
-          int jx = (int)(2 * m.ix[e] + (q & 1)), jy = (int)(2 * m.iy[e] + (q >> 1));
-          int dx = jx - (int)ix, dy = jy - (int)iy;
-          if (abs(dx) <= 1 && abs(dy) <= 1) continue;
-          int s = slot[cls][dy + 2 + qy][dx + 2 + qx];
-          if (s >= 0) {
-            V[s] = cc;
-            nv++;
-          }
+      eleaf = m.leaf[e];
+      elev = m.level[e];
+      ex = m.ix[e];
+      ey = m.iy[e];
+      if (!eleaf) ech = reinterpret_cast<const int4 *>(m.child)[e];
+    }
+    if (co >= 0) {
+      colev = m.level[co];
+      cox = m.ix[co];
+      coy = m.iy[co];
+    }
+  }
+  unsigned long long nv = 0;
+  for (int q = 0; q < 4; q++) {
+    const int c = (&chp.x)[q];
+    if (c < 0) continue;  // uniform
+    int *V = m.vlist + (size_t)c * 27;
+    int *X = m.xlist + (size_t)c * 8;
+    if (lane < 27) V[lane] = -1;
+    if (lane < 8) X[lane] = -1;
+    const int lev = m.level[c];
+    if (lev - m.lev0 < 2) continue;  // uniform: levels counted from the cell's set root
+    __syncwarp();  // the -1 fill is done before any slot is written
+    const unsigned ix = m.ix[c], iy = m.iy[c];
+    const int qx = ix & 1, qy = iy & 1, cls = qx + 2 * qy;
+    if (e >= 0 && !eleaf) {
+      for (int qq = 0; qq < 4; qq++) {
+        const int cc = (&ech.x)[qq];
+        if (cc < 0) continue;
+        const int jx = (int)(2 * ex + (qq & 1)), jy = (int)(2 * ey + (qq >> 1));
+        const int dx = jx - (int)ix, dy = jy - (int)iy;
+        if (abs(dx) <= 1 && abs(dy) <= 1) continue;
+        const int sl = slot[cls][dy + 2 + qy][dx + 2 + qx];
+        if (sl >= 0) {
+          V[sl] = cc;
+          nv++;
         }
       }
     }
-    const int co = m.coarse[p * 9 + k];
-    if (co >= 0 && !adj_cells(m, co, c)) {
-      bool dup = false;
-      for (int j = 0; j < nx; j++) dup |= X[j] == co;
-      if (!dup) X[nx++] = co;
-    }
+    // X candidate of this position: the colleague leaf or the coarser leaf
+    int xc = -1;
+    if (e >= 0 && eleaf && !adjacent(elev, ex, ey, lev, ix, iy)) xc = e;
+    if (co >= 0 && !adjacent(colev, cox, coy, lev, ix, iy)) xc = co;
+    // a coarser leaf met at several positions is kept at its first one
+    const unsigned same = __match_any_sync(0xffffffffu, xc);
+    if (xc >= 0 && (same & lt) != 0 && xc == co) xc = -1;
+    const unsigned bal = __ballot_sync(0xffffffffu, xc >= 0);
+    if (xc >= 0) X[__popc(bal & lt)] = xc;
   }
-  if (nv) atomicAdd(&m.st->n_m2l, (unsigned long long)nv);
+  for (int o = 16; o; o >>= 1) nv += __shfl_xor_sync(0xffffffffu, nv, o);
+  if (lane == 0 && nv) atomicAdd(&m.st->n_m2l, nv);
 }
 
 // rc = cutoff * max sigma (sigma >= 0 as floats order like their bits).
@@ -1177,7 +1215,7 @@ int mixed_lists(MixedView &m, cudaStream_t s) {
   g_launches.fetch_add(3, std::memory_order_relaxed);
   k_parent<<<cb, 256, 0, s>>>(m);
   k_colleagues<<<cb, 256, 0, s>>>(m);
-  k_vx_lists<<<cb, 256, 0, s>>>(m);
+  k_vx_lists<<<(int)(((long)m.ncell * 32 + 255) / 256), 256, 0, s>>>(m);
   if (m.list_scratch)
     k_lists<2><<<(m.nleaf + kWalkWarps - 1) / kWalkWarps, 32 * kWalkWarps, 0, s>>>(m);
   else
