@@ -124,6 +124,7 @@ struct Solver {
   bool plain_coef = false;  // FP64 coefficients present (plain upward ran)
   Arena io;       // device copies of host inputs and outputs
   Arena targets;  // evaluation-order targets
+  Arena lookup;   // query points and answers of a batch lookup
 };
 
 struct Lib {
@@ -139,11 +140,18 @@ struct Lib {
   double mirror_d = 0.0;
   std::atomic<int> last_error{0};
   cudaStream_t stream = nullptr;
+  cudaStream_t copy_stream = nullptr;  // uploads and downloads beside the solve stream
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_inputs = nullptr;
+  int *h_count = nullptr;              // pinned: miss count of a batch lookup
   bool stream_ready = false;
   Solver main, dev;
-  // results of the last make_tree
+  // results of the last make_tree: positions and velocities on the device
+  // (original order); host copies made on first need (single-point lookups,
+  // batch queries the device lookup could not place)
   std::atomic<bool> valid{false};
   std::atomic<unsigned long long> generation{0};
+  const double *d_xy = nullptr, *d_uv = nullptr;
+  std::atomic<bool> host_ready{false};
   PinnedTable h_xy, h_uv;
   int n = 0;
   // position -> blob index, built on first need
@@ -171,6 +179,10 @@ int ensure_stream(Lib &L) {
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return TREE2D_ERR_NO_DEVICE;
   T2D_CUDA_TRY(cudaStreamCreateWithFlags(&L.stream, cudaStreamNonBlocking));
+  T2D_CUDA_TRY(cudaStreamCreateWithFlags(&L.copy_stream, cudaStreamNonBlocking));
+  for (cudaEvent_t *e : {&L.ev_fork, &L.ev_join, &L.ev_inputs})
+    T2D_CUDA_TRY(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+  T2D_CUDA_TRY(cudaMallocHost(reinterpret_cast<void **>(&L.h_count), sizeof(int)));
   L.stream_ready = true;
   return TREE2D_OK;
 }
@@ -220,14 +232,19 @@ float elapsed(cudaEvent_t a, cudaEvent_t b) {
 }
 
 int solve_body(Lib &L, Solver &S, int n, const double *d_xy, const double *d_cir, const double *d_cor,
-               double *d_uv, cudaStream_t s, tree2d_stats_t &st, const int *d_set_off = nullptr, int nsets = 1);
+               double *d_uv, cudaStream_t s, tree2d_stats_t &st, const int *d_set_off = nullptr, int nsets = 1,
+               cudaEvent_t cir_cor_ready = nullptr);
 
 // Whole pipeline over n device-resident blobs; uv (interleaved, original
 // order) on the device.  With a mirror wall the images are appended as
 // blobs n..2n-1 and only the first n velocities are returned.
+// `cir_cor_ready`: an event to wait for before the circulations and core
+// radii are read (they may still be on their way to the device).
 int solve(Lib &L, Solver &S, int n, const double *d_xy, const double *d_cir, const double *d_cor, double *d_uv,
-          cudaStream_t s, tree2d_stats_t &st) {
-  if (!L.mirror_on || n == 0) return solve_body(L, S, n, d_xy, d_cir, d_cor, d_uv, s, st);
+          cudaStream_t s, tree2d_stats_t &st, cudaEvent_t cir_cor_ready = nullptr) {
+  if (!L.mirror_on || n == 0)
+    return solve_body(L, S, n, d_xy, d_cir, d_cor, d_uv, s, st, nullptr, 1, cir_cor_ready);
+  if (cir_cor_ready) T2D_CUDA_TRY(cudaStreamWaitEvent(s, cir_cor_ready, 0));
   const size_t n2 = 2 * (size_t)n;
   T2D_CUDA_TRY(S.mirror.reserve(Arena::bytes_for(2 * n2, 8) * 2 + Arena::bytes_for(n2, 8) * 2));
   S.mirror.reset();
@@ -244,7 +261,8 @@ int solve(Lib &L, Solver &S, int n, const double *d_xy, const double *d_cir, con
 }
 
 int solve_body(Lib &L, Solver &S, int n, const double *d_xy, const double *d_cir, const double *d_cor,
-               double *d_uv, cudaStream_t s, tree2d_stats_t &st, const int *d_set_off, int nsets) {
+               double *d_uv, cudaStream_t s, tree2d_stats_t &st, const int *d_set_off, int nsets,
+               cudaEvent_t cir_cor_ready) {
   T2D_CUDA_TRY(workspace_init(S.ws));
   std::memset(&st, 0, sizeof(st));
   st.n_blobs = n;
@@ -256,7 +274,7 @@ int solve_body(Lib &L, Solver &S, int n, const double *d_xy, const double *d_cir
   Workspace &ws = S.ws;
   const long long launches0 = g_launches.load();
   T2D_CUDA_TRY(cudaEventRecord(ws.ev[0], s));
-  int rc = build_tree(ws, n, d_xy, d_cir, d_cor, L.params, S.tree, s, d_set_off, nsets);
+  int rc = build_tree(ws, n, d_xy, d_cir, d_cor, L.params, S.tree, s, d_set_off, nsets, cir_cor_ready);
   if (rc) return rc;
   T2D_CUDA_TRY(cudaEventRecord(ws.ev[1], s));
   S.plain_coef = false;
@@ -317,6 +335,22 @@ uint64_t pos_hash(double x, double y) {
 }
 
 bool same_bits(double a, double b) { return std::memcmp(&a, &b, 8) == 0; }
+
+// Host copies of the last make_tree's positions and velocities (the
+// single-point lookup's table), downloaded on first need.  L.mu held.
+int ensure_host_tables(Lib &L) {
+  if (L.host_ready.load(std::memory_order_acquire)) return TREE2D_OK;
+  const size_t m = 2 * (size_t)L.n;
+  if (m > 0) {
+    T2D_CUDA_TRY(L.h_xy.ensure(m));
+    T2D_CUDA_TRY(L.h_uv.ensure(m));
+    T2D_CUDA_TRY(cudaMemcpyAsync(L.h_xy.p, L.d_xy, sizeof(double) * m, cudaMemcpyDeviceToHost, L.stream));
+    T2D_CUDA_TRY(cudaMemcpyAsync(L.h_uv.p, L.d_uv, sizeof(double) * m, cudaMemcpyDeviceToHost, L.stream));
+    T2D_CUDA_TRY(cudaStreamSynchronize(L.stream));
+  }
+  L.host_ready.store(true, std::memory_order_release);
+  return TREE2D_OK;
+}
 
 void ensure_hash(Lib &L) {
   if (L.hash_ready.load(std::memory_order_acquire)) return;
@@ -423,6 +457,53 @@ int eval_points(Lib &L, int m, const double *xy, double *uv) {
 
 }  // namespace
 
+// Batch lookup on the device: the queries go up in chunks on two streams
+// (one chunk's upload overlaps the previous chunk's download), query i is
+// matched against blob i, and the answers come back into uv.  Queries that
+// do not sit bitwise on their blob are returned in `miss` (ascending), with
+// NaN in uv.  L.mu held.
+int lookup_on_device(Lib &L, int n, const double *xy, double *uv, std::vector<int> &miss) {
+  miss.clear();
+  if (L.n == 0) {
+    miss.resize(n);
+    for (int i = 0; i < n; i++) miss[i] = i;
+    return TREE2D_OK;
+  }
+  Solver &S = L.main;
+  T2D_CUDA_TRY(S.lookup.reserve(Arena::bytes_for(2 * (size_t)n, 8) * 2 + Arena::bytes_for(n, 4) +
+                                Arena::bytes_for(1, 4)));
+  S.lookup.reset();
+  double *q = S.lookup.take<double>(2 * (size_t)n);
+  double *out = S.lookup.take<double>(2 * (size_t)n);
+  int *midx = S.lookup.take<int>(n);
+  int *cnt = S.lookup.take<int>(1);
+  cudaStream_t st[2] = {L.stream, L.copy_stream};
+  T2D_CUDA_TRY(cudaMemsetAsync(cnt, 0, sizeof(int), st[0]));
+  T2D_CUDA_TRY(cudaEventRecord(L.ev_fork, st[0]));
+  T2D_CUDA_TRY(cudaStreamWaitEvent(st[1], L.ev_fork, 0));
+  const long chunk = std::max(1L << 20, ((long)n + 3) / 4);
+  int k = 0;
+  for (long b = 0; b < n; b += chunk, k ^= 1) {
+    const long e = std::min((long)n, b + chunk);
+    const size_t bytes = sizeof(double) * 2 * (size_t)(e - b);
+    T2D_CUDA_TRY(cudaMemcpyAsync(q + 2 * b, xy + 2 * b, bytes, cudaMemcpyHostToDevice, st[k]));
+    T2D_CUDA_TRY(lookup_blobs(b, e, q, L.n, L.d_xy, L.d_uv, out, midx, cnt, st[k]));
+    T2D_CUDA_TRY(cudaMemcpyAsync(uv + 2 * b, out + 2 * b, bytes, cudaMemcpyDeviceToHost, st[k]));
+  }
+  T2D_CUDA_TRY(cudaEventRecord(L.ev_join, st[1]));
+  T2D_CUDA_TRY(cudaStreamWaitEvent(st[0], L.ev_join, 0));
+  T2D_CUDA_TRY(cudaMemcpyAsync(L.h_count, cnt, sizeof(int), cudaMemcpyDeviceToHost, st[0]));
+  T2D_CUDA_TRY(cudaStreamSynchronize(st[0]));
+  const int nm = *L.h_count;
+  if (nm > 0) {
+    miss.resize(nm);
+    T2D_CUDA_TRY(cudaMemcpyAsync(miss.data(), midx, sizeof(int) * (size_t)nm, cudaMemcpyDeviceToHost, st[0]));
+    T2D_CUDA_TRY(cudaStreamSynchronize(st[0]));
+    std::sort(miss.begin(), miss.end());
+  }
+  return TREE2D_OK;
+}
+
 // Parameters in force for a device solve (as tree2d_solve_device resolves
 // them), taken under the library lock.
 int params_for_device_solve(Params &out) {
@@ -446,6 +527,7 @@ void make_tree(int nvor_b, const double *vor_b, const double *cir_b, const doubl
   Lib &L = lib();
   std::lock_guard<std::mutex> lk(L.mu);
   L.valid.store(false);
+  L.host_ready.store(false);
   L.hash_ready.store(false);
   L.generation.fetch_add(1);
   L.last_error.store(TREE2D_OK);
@@ -466,6 +548,7 @@ void make_tree(int nvor_b, const double *vor_b, const double *cir_b, const doubl
   const int n = nvor_b;
   Solver &S = L.main;
   double *d_xy = nullptr, *d_cir = nullptr, *d_cor = nullptr, *d_uv = nullptr;
+  cudaEvent_t cir_cor_ready = nullptr;
   if (n > 0) {
     size_t need = Arena::bytes_for(2 * (size_t)n, 8) * 2 + Arena::bytes_for(n, 8) * 2;
     cudaError_t e = S.io.reserve(need);
@@ -479,47 +562,38 @@ void make_tree(int nvor_b, const double *vor_b, const double *cir_b, const doubl
     d_uv = S.io.take<double>(2 * (size_t)n);
     d_cir = S.io.take<double>(n);
     d_cor = S.io.take<double>(n);
-    cudaStream_t s = L.stream;
-    if (cudaMemcpyAsync(d_xy, vor_b, sizeof(double) * 2 * (size_t)n, cudaMemcpyHostToDevice, s) != cudaSuccess ||
-        cudaMemcpyAsync(d_cir, cir_b, sizeof(double) * (size_t)n, cudaMemcpyHostToDevice, s) != cudaSuccess ||
-        cudaMemcpyAsync(d_cor, cor_b, sizeof(double) * (size_t)n, cudaMemcpyHostToDevice, s) != cudaSuccess) {
+    // The positions go up on the solve's stream; the circulations and core
+    // radii on the copy stream, landing while the keys are formed and
+    // sorted (the build waits for them only before its gather).
+    cudaStream_t s = L.stream, c = L.copy_stream;
+    if (cudaEventRecord(L.ev_fork, s) != cudaSuccess || cudaStreamWaitEvent(c, L.ev_fork, 0) != cudaSuccess ||
+        cudaMemcpyAsync(d_xy, vor_b, sizeof(double) * 2 * (size_t)n, cudaMemcpyHostToDevice, s) != cudaSuccess ||
+        cudaMemcpyAsync(d_cir, cir_b, sizeof(double) * (size_t)n, cudaMemcpyHostToDevice, c) != cudaSuccess ||
+        cudaMemcpyAsync(d_cor, cor_b, sizeof(double) * (size_t)n, cudaMemcpyHostToDevice, c) != cudaSuccess ||
+        cudaEventRecord(L.ev_inputs, c) != cudaSuccess) {
       note_cuda_error(cudaGetLastError(), "make_tree upload");
+      cudaStreamSynchronize(c);
       fail(TREE2D_ERR_CUDA);
       return;
     }
+    cir_cor_ready = L.ev_inputs;
   }
-  // The host copy of the positions (the lookup table's keys) is taken on a
-  // helper thread while the GPU solves.
-  cudaError_t ealloc = L.h_xy.ensure(2 * (size_t)n);
-  if (ealloc == cudaSuccess) ealloc = L.h_uv.ensure(2 * (size_t)n);
-  if (ealloc != cudaSuccess) {
-    note_cuda_error(ealloc, "make_tree host tables");
-    fail(TREE2D_ERR_CUDA);
-    return;
-  }
-  std::thread copier;
-  if (n > 0) {
-    copier = std::thread([&L, vor_b, n] {
-      parallel_chunks(2 * (long)n, 1 << 20, [&](long b, long e) {
-        std::memcpy(L.h_xy.p + b, vor_b + b, sizeof(double) * (size_t)(e - b));
-      });
-    });
-  }
-  rc = solve(L, S, n, d_xy, d_cir, d_cor, d_uv, L.stream, L.stats);
+  rc = solve(L, S, n, d_xy, d_cir, d_cor, d_uv, L.stream, L.stats, cir_cor_ready);
   L.last_was_dev = false;
-  if (rc == TREE2D_OK && n > 0) {
-    cudaError_t e = cudaMemcpyAsync(L.h_uv.p, d_uv, sizeof(double) * 2 * (size_t)n, cudaMemcpyDeviceToHost, L.stream);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(L.stream);
-    if (e != cudaSuccess) {
-      note_cuda_error(e, "make_tree download");
+  // the copy stream is idle before the buffers can be reused
+  if (n > 0) {
+    cudaError_t e = cudaStreamSynchronize(L.copy_stream);
+    if (e != cudaSuccess && rc == TREE2D_OK) {
+      note_cuda_error(e, "make_tree upload");
       rc = TREE2D_ERR_CUDA;
     }
   }
-  if (copier.joinable()) copier.join();
   if (rc) {
     fail(rc);
     return;
   }
+  L.d_xy = d_xy;
+  L.d_uv = d_uv;
   L.n = n;
   L.valid.store(true);
 }
@@ -531,6 +605,16 @@ void biot_tree(double x, double y, double *u, double *v) {
     *v = NAN;
     L.last_error.store(TREE2D_ERR_NO_TREE);
     return;
+  }
+  if (!L.host_ready.load(std::memory_order_acquire)) {
+    std::lock_guard<std::mutex> lk(L.mu);
+    int rc = ensure_host_tables(L);
+    if (rc) {
+      fail(rc);
+      *u = NAN;
+      *v = NAN;
+      return;
+    }
   }
   long k = find_blob(L, x, y);
   if (k >= 0) {
@@ -558,40 +642,56 @@ int biot_tree_batch(int n, const double *xy, double *uv) {
     for (long i = 0; i < 2 * (long)n; i++) uv[i] = NAN;
     return fail(TREE2D_ERR_NO_TREE);
   }
-  // Table lookups on all host threads (one hint per chunk), misses
-  // collected per chunk and evaluated on the GPU together.
-  const long grain = 1 << 16;
-  const long nchunks = std::max(1L, ((long)n + grain - 1) / grain);
-  std::vector<std::vector<int>> miss_part(nchunks);
-  parallel_chunks((long)nchunks, 1, [&](long cb, long ce) {
-    for (long c = cb; c < ce; c++) {
-      // first guess: query i is blob i (a sweep over the blobs in order)
-      long hint = c * grain - 1;
-      const long e = std::min((long)n, (c + 1) * grain);
-      for (long i = c * grain; i < e; i++) {
-        long k = find_blob_from(L, xy[2 * (size_t)i], xy[2 * (size_t)i + 1], hint);
+  if (n == 0) return TREE2D_OK;
+  std::lock_guard<std::mutex> lk(L.mu);
+  std::vector<int> miss;
+  int rc = lookup_on_device(L, n, xy, uv, miss);
+  if (rc) {
+    // no copy into uv may still be in flight
+    cudaStreamSynchronize(L.stream);
+    cudaStreamSynchronize(L.copy_stream);
+    for (long i = 0; i < 2 * (long)n; i++) uv[i] = NAN;
+    return fail(rc);
+  }
+  if (miss.empty()) return TREE2D_OK;
+  // Queries the device could not place: the host table (hash over the
+  // positions), then the treecode for points off the blobs.
+  rc = ensure_host_tables(L);
+  if (rc) {
+    for (int i : miss) uv[2 * (size_t)i] = uv[2 * (size_t)i + 1] = NAN;
+    return fail(rc);
+  }
+  const long nm = (long)miss.size();
+  const long grain = 1 << 14;
+  const long nparts = (nm + grain - 1) / grain;
+  std::vector<std::vector<int>> off_part(nparts);
+  parallel_chunks(nparts, 1, [&](long pb, long pe) {
+    for (long c = pb; c < pe; c++) {
+      long hint = -1;
+      for (long j = c * grain; j < std::min(nm, (c + 1) * grain); j++) {
+        const size_t i = (size_t)miss[j];
+        long k = find_blob_from(L, xy[2 * i], xy[2 * i + 1], hint);
         if (k >= 0) {
-          uv[2 * (size_t)i] = L.h_uv[2 * k];
-          uv[2 * (size_t)i + 1] = L.h_uv[2 * k + 1];
+          uv[2 * i] = L.h_uv[2 * k];
+          uv[2 * i + 1] = L.h_uv[2 * k + 1];
         } else {
-          miss_part[c].push_back((int)i);
+          off_part[c].push_back((int)i);
         }
       }
     }
   });
-  std::vector<int> miss;
-  for (auto &m : miss_part) miss.insert(miss.end(), m.begin(), m.end());
-  if (miss.empty()) return TREE2D_OK;
-  std::vector<double> mxy(2 * miss.size()), muv(2 * miss.size());
-  for (size_t j = 0; j < miss.size(); j++) {
-    mxy[2 * j] = xy[2 * (size_t)miss[j]];
-    mxy[2 * j + 1] = xy[2 * (size_t)miss[j] + 1];
+  std::vector<int> off;
+  for (auto &m : off_part) off.insert(off.end(), m.begin(), m.end());
+  if (off.empty()) return TREE2D_OK;
+  std::vector<double> mxy(2 * off.size()), muv(2 * off.size());
+  for (size_t j = 0; j < off.size(); j++) {
+    mxy[2 * j] = xy[2 * (size_t)off[j]];
+    mxy[2 * j + 1] = xy[2 * (size_t)off[j] + 1];
   }
-  std::lock_guard<std::mutex> lk(L.mu);
-  int rc = eval_points(L, (int)miss.size(), mxy.data(), muv.data());
-  for (size_t j = 0; j < miss.size(); j++) {
-    uv[2 * (size_t)miss[j]] = rc ? NAN : muv[2 * j];
-    uv[2 * (size_t)miss[j] + 1] = rc ? NAN : muv[2 * j + 1];
+  rc = eval_points(L, (int)off.size(), mxy.data(), muv.data());
+  for (size_t j = 0; j < off.size(); j++) {
+    uv[2 * (size_t)off[j]] = rc ? NAN : muv[2 * j];
+    uv[2 * (size_t)off[j] + 1] = rc ? NAN : muv[2 * j + 1];
   }
   return rc ? fail(rc) : TREE2D_OK;
 }

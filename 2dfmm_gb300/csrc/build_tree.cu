@@ -49,15 +49,15 @@ __device__ __forceinline__ double warp_min(double v) {
   return v;
 }
 
-__global__ void __launch_bounds__(256) k_bbox(const double *__restrict__ xy, const double *__restrict__ cir,
-                                              const double *__restrict__ cor, int n, Box4 *part,
-                                              DevStatus *st) {
+// Bounding box of the positions (non-finite positions are bad input; the
+// circulations and core radii are checked where they are first read, in
+// k_gather).
+__global__ void __launch_bounds__(256) k_bbox(const double *__restrict__ xy, int n, Box4 *part, DevStatus *st) {
   double xmax = -INFINITY, xmin = INFINITY, ymax = -INFINITY, ymin = INFINITY;
   bool bad = false;
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
     double x = xy[2 * i], y = xy[2 * i + 1];
-    double c = cir[i], r = cor[i];
-    bad |= !(isfinite(x) && isfinite(y) && isfinite(c)) || isnan(r);
+    bad |= !(isfinite(x) && isfinite(y));
     xmax = fmax(xmax, x);
     xmin = fmin(xmin, x);
     ymax = fmax(ymax, y);
@@ -632,24 +632,28 @@ __global__ void __launch_bounds__(256) k_leaf_order(const uint32_t *__restrict__
   }
 }
 
-// Blob arrays in tree order, plus 1/sigma^2 for the direct pairs.
+// Blob arrays in tree order, plus 1/sigma^2 for the direct pairs; a
+// non-finite circulation or a NaN core radius is bad input.
 __global__ void __launch_bounds__(256) k_gather(const double *__restrict__ xy, const double *__restrict__ cir,
                                                 const double *__restrict__ cor, const int *__restrict__ perm, int n,
-                                                double *x, double *y, double *c, double *r, double *icor2) {
+                                                double *x, double *y, double *c, double *r, double *icor2,
+                                                DevStatus *st) {
   long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (i >= n) return;
   int p = perm[i];
+  const double g = cir[p], rc = cor[p];
+  if (!isfinite(g) || isnan(rc)) set_err(st, TREE2D_ERR_BAD_INPUT);
   x[i] = xy[2 * (long)p];
   y[i] = xy[2 * (long)p + 1];
-  c[i] = cir[p];
-  r[i] = cor[p];
-  icor2[i] = 1.0 / (cor[p] * cor[p]);
+  c[i] = g;
+  r[i] = rc;
+  icor2[i] = 1.0 / (rc * rc);
 }
 
 }  // namespace
 
 int build_tree(Workspace &ws, int n, const double *d_xy, const double *d_cir, const double *d_cor, const Params &p,
-               Tree &t, cudaStream_t s, const int *d_set_off, int nsets) {
+               Tree &t, cudaStream_t s, const int *d_set_off, int nsets, cudaEvent_t cir_cor_ready) {
   t.n = n;
   t.nterms = p.nterms;
   const bool batched = nsets > 1;
@@ -732,7 +736,7 @@ retry:
     k_roots_sets<<<(nsets + 127) / 128, 128, 0, s>>>(set_part, nsets, t.root);
     ::t2d::g_launches.fetch_add(2, std::memory_order_relaxed);
   } else {
-    k_bbox<<<kBoxBlocks, 256, 0, s>>>(d_xy, d_cir, d_cor, n, bpart, ws.status);
+    k_bbox<<<kBoxBlocks, 256, 0, s>>>(d_xy, n, bpart, ws.status);
     k_root<<<1, 32, 0, s>>>(bpart, kBoxBlocks, t.root);
     ::t2d::g_launches.fetch_add(2, std::memory_order_relaxed);
   }
@@ -813,11 +817,14 @@ retry:
                                                     t.child);
   ::t2d::g_launches.fetch_add(1, std::memory_order_relaxed);
   // 8. in-leaf order, 9. gather
-  if (t.nleaf > 0)
+  if (t.nleaf > 0) {
     k_leaf_order<<<(int)(((long)t.nleaf * 32 + 255) / 256), 256, 0, s>>>(vals, t.nleaf, t.leaf_cell, t.begin, t.end,
                                                                           t.perm);
     ::t2d::g_launches.fetch_add(1, std::memory_order_relaxed);
-  k_gather<<<(n + 255) / 256, 256, 0, s>>>(d_xy, d_cir, d_cor, t.perm, n, t.x, t.y, t.cir, t.cor, t.icor2);
+  }
+  if (cir_cor_ready) T2D_CUDA_TRY(cudaStreamWaitEvent(s, cir_cor_ready, 0));
+  k_gather<<<(n + 255) / 256, 256, 0, s>>>(d_xy, d_cir, d_cor, t.perm, n, t.x, t.y, t.cir, t.cor, t.icor2,
+                                           ws.status);
   ::t2d::g_launches.fetch_add(1, std::memory_order_relaxed);
   T2D_CUDA_TRY(cudaGetLastError());
   return TREE2D_OK;

@@ -159,6 +159,41 @@ __global__ void k_mirror(long n, const double *xy, const double *cir, const doub
   ocor[n + i] = 0.0;
 }
 
+// Velocities of query points [b, e) at the blob positions: query i takes
+// blob i's velocity when the two positions have the same bit patterns (a
+// sweep over the blobs in order, the common case); any other query gets NaN
+// here and its index appended to `miss` (in no particular order) for the
+// host to resolve.
+__global__ void k_lookup(long b, long e, const double2 *__restrict__ q, long nb, const double2 *__restrict__ bxy,
+                         const double2 *__restrict__ buv, double2 *__restrict__ out, int *__restrict__ miss,
+                         int *__restrict__ nmiss) {
+  const long i = b + blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (i >= e) return;
+  const double2 p = q[i];
+  bool hit = false;
+  if (i < nb) {
+    const double2 c = bxy[i];
+    hit = __double_as_longlong(p.x) == __double_as_longlong(c.x) && __double_as_longlong(p.y) == __double_as_longlong(c.y);
+  }
+  if (hit) {
+    out[i] = buv[i];
+  } else {
+    out[i] = make_double2(__longlong_as_double(0x7ff8000000000000ll), __longlong_as_double(0x7ff8000000000000ll));
+    miss[atomicAdd(nmiss, 1)] = (int)i;
+  }
+}
+
+cudaError_t lookup_blobs(long b, long e, const double *q, long nb, const double *bxy, const double *buv, double *out,
+                         int *miss, int *nmiss, cudaStream_t s) {
+  if (e <= b) return cudaSuccess;
+  k_lookup<<<(unsigned)((e - b + 255) / 256), 256, 0, s>>>(b, e, reinterpret_cast<const double2 *>(q), nb,
+                                                         reinterpret_cast<const double2 *>(bxy),
+                                                         reinterpret_cast<const double2 *>(buv),
+                                                         reinterpret_cast<double2 *>(out), miss, nmiss);
+  ::t2d::g_launches.fetch_add(1, std::memory_order_relaxed);
+  return cudaGetLastError();
+}
+
 cudaError_t advect(long n, double *xy, const double *uv, double dt, cudaStream_t s) {
   if (n <= 0) return cudaSuccess;
   k_advect<<<(int)((2 * n + 255) / 256), 256, 0, s>>>(n, xy, uv, dt);

@@ -163,8 +163,12 @@ cudaError_t workspace_init(Workspace &ws);
 // [d_set_off[k], d_set_off[k+1]) (device offsets); each set gets its own root
 // box and exactly the cells it would get alone, below lev0 levels of
 // container cells that keep the sets apart (t.lev0, t.root[k] per set).
+// `cir_cor_ready`, when given, is an event the stream waits for before the
+// circulations and core radii are first read (the positions must be ready
+// when the call is made); the caller may still be uploading them.
 int build_tree(Workspace &ws, int n, const double *d_xy, const double *d_cir, const double *d_cor,
-               const Params &p, Tree &t, cudaStream_t s, const int *d_set_off = nullptr, int nsets = 1);
+               const Params &p, Tree &t, cudaStream_t s, const int *d_set_off = nullptr, int nsets = 1,
+               cudaEvent_t cir_cor_ready = nullptr);
 
 // Keys of arbitrary points against an existing root box, then sorted:
 // order[i] = index of the i-th target in key order.
@@ -199,6 +203,11 @@ cudaError_t dfma_probe(double *out, int blocks, int iters, cudaStream_t s);
 cudaError_t ffma_probe(float *out, int blocks, int iters, cudaStream_t s);
 cudaError_t wait_probe(long polls, int *out, cudaStream_t s);
 cudaError_t advect(long n, double *xy, const double *uv, double dt, cudaStream_t s);
+// Query points [b, e) (xy interleaved, 16-byte aligned, as all the arrays
+// here) looked up at the nb blob positions bxy: out[i] = buv[i] where query i
+// is bitwise at blob i, else NaN and i appended to miss (count in *nmiss).
+cudaError_t lookup_blobs(long b, long e, const double *q, long nb, const double *bxy, const double *buv, double *out,
+                         int *miss, int *nmiss, cudaStream_t s);
 // Blobs followed by their images in a wall at y = d (2n entries out).
 cudaError_t mirror_images(long n, const double *xy, const double *cir, const double *cor, double d, double *oxy,
                           double *ocir, double *ocor, cudaStream_t s);

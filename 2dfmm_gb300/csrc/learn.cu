@@ -77,7 +77,7 @@ __global__ void k_labels(MixedView m, const LeafStats *st, const float *u_ref_pt
   const float u_ref = *u_ref_ptr;
   const int P = m.P;
   const double ox = m.cx[B] - m.cx[A], oy = m.cy[B] - m.cy[A];
-  const float oxf = (float)(m.cx[B] - m.cx[A]), oyf = (float)(m.cy[B] - m.cy[A]);
+  const float oxf = centre_offset(m.cxf, m.cxl, B, A), oyf = centre_offset(m.cyf, m.cyl, B, A);
   const float ihA = m.inv_h[A];
   const float *MA = m.M + (size_t)A * 2 * P;
   double err[14];

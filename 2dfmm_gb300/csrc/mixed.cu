@@ -135,6 +135,8 @@ __global__ void k_cell_info(MixedView m) {
   m.inv_h[c] = (float)(1.0 / m.region[c]);
   m.cxf[c] = (float)m.cx[c];
   m.cyf[c] = (float)m.cy[c];
+  m.cxl[c] = (float)(m.cx[c] - (double)m.cxf[c]);
+  m.cyl[c] = (float)(m.cy[c] - (double)m.cyf[c]);
 }
 
 // Per leaf: leaf_of for its positions, FP32 local coordinates, circulation,
@@ -724,7 +726,7 @@ __global__ void __launch_bounds__(256) k_p2l(MixedView m) {
     for (int i = 0; i < 2 * kCoefChunk; i++) acc[i] = 0.f;
     for (int e = 0; e < 8 && X[e] >= 0; e++) {
       const int d = X[e];
-      const float ox = (float)(m.cx[d] - m.cx[c]), oy = (float)(m.cy[d] - m.cy[c]);
+      const float ox = centre_offset(m.cxf, m.cxl, d, c), oy = centre_offset(m.cyf, m.cyl, d, c);
       for (int j = m.begin[d] + lane; j < m.end[d]; j += 32) {
         const float zx = (m.loc[j].x + ox) * ih, zy = (m.loc[j].y + oy) * ih;
         const float r2 = zx * zx + zy * zy;
@@ -790,8 +792,8 @@ __device__ __forceinline__ void kahan(float &s, float &cmp, float v) {
 __device__ __forceinline__ void m2p_order(const MixedView &m, int B, int A, int p, float2 z, float2 &phi) {
   const int P = m.P;
   const float ih = m.inv_h[A];
-  const float zx = __fmul_rn(__fadd_rn(z.x, (float)(m.cx[B] - m.cx[A])), ih);
-  const float zy = __fmul_rn(__fadd_rn(z.y, (float)(m.cy[B] - m.cy[A])), ih);
+  const float zx = __fmul_rn(__fadd_rn(z.x, centre_offset(m.cxf, m.cxl, B, A)), ih);
+  const float zy = __fmul_rn(__fadd_rn(z.y, centre_offset(m.cyf, m.cyl, B, A)), ih);
   const float ir2 = __fdiv_rn(1.f, fmaf(zx, zx, __fmul_rn(zy, zy)));
   const float2 w = make_float2(__fmul_rn(zx, ir2), -__fmul_rn(zy, ir2));
   const float *MA = m.M + (size_t)A * 2 * P;
@@ -919,7 +921,6 @@ __global__ void __launch_bounds__(32 * kWarps, 32 / kWarps) k_eval_staged(MixedV
   unsigned inflight = 0;  // bit b: a copy into buffer b not yet waited for
   bool staging = true;    // false after a wait gave up
   const int B = m.leaf_cell[l];
-  const double cxB = m.cx[B], cyB = m.cy[B];
   const double inv2pi = 0.15915494309189533577;
   unsigned long long pairs = 0;
   const int u0 = m.u_off[l], nu = m.u_off[l + 1] - u0;
@@ -978,9 +979,9 @@ __global__ void __launch_bounds__(32 * kWarps, 32 / kWarps) k_eval_staged(MixedV
       const int qn = next_direct(q + 1);
       const bool staged_next = qn < nu + nk && stage(qn, buf ^ 1);
       const int A = src_leaf(q);
-      // offset of the source leaf's centre in FP64, then rounded: FP32 centres
-        // would carry ~1e-7 absolute error into every close pair
-        const float ox = (float)(cxB - m.cx[A]), oy = (float)(cyB - m.cy[A]);
+      // offset of the source leaf's centre from the two-float centres: FP32
+      // centres alone would carry ~3e-8 absolute error into every close pair
+      const float ox = centre_offset(m.cxf, m.cxl, B, A), oy = centre_offset(m.cyf, m.cyl, B, A);
       const int j0 = m.begin[A], cnt = m.end[A] - j0;
       bool use_smem = false;
       if (staged) {
@@ -1044,7 +1045,6 @@ __global__ void __launch_bounds__(32 * kWarps, 32 / kWarps) k_eval_mixed(MixedVi
   const int l = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   if (l >= m.nleaf) return;
   const int B = m.leaf_cell[l];
-  const double cxB = m.cx[B], cyB = m.cy[B];
   const double inv2pi = 0.15915494309189533577;
   unsigned long long pairs = 0;
   for (int t0 = m.begin[B]; t0 < m.end[B]; t0 += 64) {
@@ -1077,9 +1077,9 @@ __global__ void __launch_bounds__(32 * kWarps, 32 / kWarps) k_eval_mixed(MixedVi
             continue;
           }
         }
-        // offset of the source leaf's centre in FP64, then rounded: FP32 centres
-        // would carry ~1e-7 absolute error into every close pair
-        const float ox = (float)(cxB - m.cx[A]), oy = (float)(cyB - m.cy[A]);
+        // offset of the source leaf's centre from the two-float centres: FP32
+        // centres alone would carry ~3e-8 absolute error into every close pair
+        const float ox = centre_offset(m.cxf, m.cxl, B, A), oy = centre_offset(m.cyf, m.cyl, B, A);
         const int j0 = m.begin[A], j1 = m.end[A];
         float sxa = 0.f, sya = 0.f, sxb = 0.f, syb = 0.f;
         if (pass == 0)
@@ -1381,7 +1381,7 @@ int mixed_solve(Workspace &ws, const Tree &t, const MixedParams &mp, double *d_u
   need += Arena::bytes_for(nc, 4) * 5;            // ix iy h inv_h parent
   need += Arena::bytes_for(n, 4) * 4;             // leaf_of gam s2inv + pad
   need += Arena::bytes_for(n, 8);                 // loc
-  need += Arena::bytes_for(n, 16) + Arena::bytes_for(nc, 4) * 2;  // src4, cxf, cyf
+  need += Arena::bytes_for(n, 16) + Arena::bytes_for(nc, 4) * 4;  // src4, cxf, cyf, cxl, cyl
   need += Arena::bytes_for((size_t)nc * 9, 4) * 2;
   need += Arena::bytes_for((size_t)nc * 27, 4) + Arena::bytes_for((size_t)nc * 8, 4);
   need += Arena::bytes_for((size_t)nl + 1, 4) * 3;
@@ -1428,6 +1428,8 @@ int mixed_solve(Workspace &ws, const Tree &t, const MixedParams &mp, double *d_u
   m.src4 = ws.mx_arena.take<float4>(n);
   m.cxf = ws.mx_arena.take<float>(nc);
   m.cyf = ws.mx_arena.take<float>(nc);
+  m.cxl = ws.mx_arena.take<float>(nc);
+  m.cyl = ws.mx_arena.take<float>(nc);
   m.coll = ws.mx_arena.take<int>((size_t)nc * 9);
   m.coarse = ws.mx_arena.take<int>((size_t)nc * 9);
   m.vlist = ws.mx_arena.take<int>((size_t)nc * 27);

@@ -30,7 +30,8 @@ struct MixedView {
   float2 *loc;           // per position, offset from its leaf centre
   float *gam, *s2inv;    // per position
   float4 *src4;          // per position {loc.x, loc.y, G, 1/sigma^2}
-  float *cxf, *cyf;      // per cell, FP32 centre
+  float *cxf, *cyf;      // per cell, FP32 centre (rounded)
+  float *cxl, *cyl;      // per cell, the rest: centre - (double)cxf, in FP32
   int *coll, *coarse;    // 9 per cell
   int *vlist;            // 27 per cell, slot order of the cell's class
   int *xlist;            // 8 per cell
@@ -46,6 +47,19 @@ struct MixedView {
   const float2 *m2m, *l2l;  // [4][kMaxP][kMaxP] translation operators
   DevStatus *st;
 };
+
+// Offset hi[b]+lo[b] - (hi[a]+lo[a]) of two cell centres in FP32, from the
+// two-float form of each centre (hi = the centre rounded to FP32, lo = the
+// rest, exact to ~2^-48 of the centre).  The hi difference is exact when the
+// two are within a factor of two of each other (Sterbenz), as neighbouring
+// cells away from the axes are, and otherwise rounded at the scale of the
+// difference; the lo difference is exact to far below that.  The result is
+// within about an ulp of the FP64 difference rounded to FP32, with no FP64
+// arithmetic.  Without the lo parts an offset would carry up to half an
+// ulp of the coordinate (~3e-8 at 0.5), too much for pairs 1e-3 apart.
+__device__ __forceinline__ float centre_offset(const float *hi, const float *lo, int b, int a) {
+  return __fadd_rn(__fsub_rn(hi[b], hi[a]), __fsub_rn(lo[b], lo[a]));
+}
 
 cudaError_t mixed_tables(int P, float *h_m2l, float *h_m2m, float *h_l2l);
 int mixed_leaf_setup(MixedView &m, const Tree &t, cudaStream_t s);

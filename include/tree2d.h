@@ -91,8 +91,10 @@ int tree2d_set_mixed_params(int pterms, double cutoff_sigmas, int use_tensor_cor
 
 /* Evaluates n targets (xy interleaved, host memory) into uv (interleaved,
  * host memory) against the last make_tree.  Blob positions are answered
- * from the precomputed velocities, the rest in one GPU launch.  Returns a
- * status; on error uv is filled with NaN. */
+ * from the precomputed velocities, the rest in one GPU launch.  The points
+ * are matched on the GPU (target i against blob i, bit for bit; page-locked
+ * xy and uv let the copies overlap), the others through a host table.
+ * Returns a status; on error uv is filled with NaN. */
 int biot_tree_batch(int n, const double *xy, double *uv);
 
 /* Device-resident solve: builds the tree over n blobs whose arrays are in

@@ -29,6 +29,32 @@ def test_non_finite_input_is_rejected(gpu_lib):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("mode", ["plain", "mixed"])
+@pytest.mark.parametrize("field,value", [("cir", np.inf), ("cir", np.nan), ("cor", np.nan)])
+def test_non_finite_circulation_or_core_is_rejected(gpu_lib, mode, field, value):
+    """Circulations and core radii are uploaded beside the tree build and
+    checked where the build first reads them: a bad value still fails the
+    make_tree call, and the next valid call succeeds."""
+    P = gpu_lib
+    P.set_params(11, 33, 0.5)
+    P.set_mode(P.MODE_PLAIN if mode == "plain" else P.MODE_MIXED)
+    try:
+        rng = np.random.default_rng(2)
+        xy = rng.random((5000, 2))
+        cir = rng.standard_normal(5000) / 5000
+        cor = np.full(5000, 0.01)
+        bad = {"cir": cir.copy(), "cor": cor.copy()}
+        bad[field][1234] = value
+        rc = P.make_tree(xy, bad["cir"], bad["cor"], check=False)
+        assert rc == P.ERR_BAD_INPUT
+        assert P.make_tree(xy, cir, cor, check=False) == 0
+        uv = P.biot_tree_batch(xy)
+        assert np.isfinite(uv).all()
+    finally:
+        P.set_mode(P.MODE_PLAIN)
+
+
+@pytest.mark.gpu
 def test_too_many_coincident_blobs(gpu_lib):
     """num_p blobs at one point can never be separated: the reference grows
     its max level forever; the library reports TREE2D_ERR_TOO_DEEP."""

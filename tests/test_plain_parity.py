@@ -136,3 +136,48 @@ def test_batch_lookup_many_chunks(gpu_lib):
     out = torch.empty((len(q), 2), dtype=torch.float64, pin_memory=True).numpy()
     uv2 = P.biot_tree_batch(q, out=out)
     assert uv2 is out and np.array_equal(out, uv)
+
+
+@pytest.mark.gpu
+def test_batch_lookup_in_order_device_chunks(gpu_lib):
+    """Queries at the blobs in their own order, more than one device lookup
+    chunk (1,048,576 points) so both copy streams take part, a few blobs
+    moved and a few points appended: the in-order answers equal the device
+    solve bit for bit, and the moved and appended points equal single-point
+    calls there."""
+    torch = pytest.importorskip("torch")
+    P = gpu_lib
+    import importlib
+    W = importlib.import_module("2dfmm_gb300.workloads")
+    b = W.uniform(2_500_000, seed=12, nterms=9, num_p=65)
+    P.set_params(b.nterms, b.num_p, b.theta)
+    P.set_mode(P.MODE_MIXED)
+    try:
+        P.make_tree(b.xy, b.cir, b.cor)
+        q = np.concatenate([b.xy, np.array([[0.31, 0.62], [0.77, 0.15]])])
+        moved = np.array([5, 1_048_575, 1_048_576, 2_000_001])
+        q[moved] += 1e-7
+        pinned = torch.empty(q.shape, dtype=torch.float64, pin_memory=True).numpy()
+        pinned[:] = q
+        out = torch.empty(q.shape, dtype=torch.float64, pin_memory=True).numpy()
+        uv = P.biot_tree_batch(pinned, out=out)
+        dev = torch.device("cuda:0")
+        d_xy = torch.from_numpy(b.xy).to(dev).contiguous()
+        d_cir = torch.from_numpy(b.cir).to(dev)
+        d_cor = torch.from_numpy(b.cor).to(dev)
+        d_uv = torch.empty_like(d_xy)
+        torch.cuda.synchronize()
+        P.solve_device(d_xy.data_ptr(), d_cir.data_ptr(), d_cor.data_ptr(), d_uv.data_ptr(), b.n)
+        torch.cuda.synchronize()
+        ref = d_uv.cpu().numpy()
+        keep = np.ones(b.n, bool)
+        keep[moved] = False
+        assert np.array_equal(uv[: b.n][keep], ref[keep])
+        for i in list(moved) + [b.n, b.n + 1]:
+            u, v = P.biot_tree(*q[i])
+            assert u == uv[i, 0] and v == uv[i, 1]
+            assert np.isfinite(u) and np.isfinite(v)
+        # pageable buffers give the same answers
+        assert np.array_equal(P.biot_tree_batch(q.copy()), uv)
+    finally:
+        P.set_mode(P.MODE_PLAIN)
