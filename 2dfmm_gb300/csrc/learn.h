@@ -41,7 +41,9 @@ struct LeafStats {
 // u_ref = sum|G| / R0.  Features: log distance over the source side, log
 // box gap over the source's core radius, offset direction, the source's
 // |G| moments of order 0 (against u_ref), 1 and 2, occupancies, list kind,
-// size ratio, self flag.
+// size ratio, self flag.  The network reads them rounded to BF16 (2^-9), so
+// the SFU's logarithm and approximate quotients (~2^-22) are used; every
+// argument of a logarithm is a positive normal number.
 __device__ __forceinline__ void interaction_features(const MixedView &m, const LeafStats *st, int B, int A, int type, float u_ref,
                                      float *f) {
   const float dx = m.cxf[B] - m.cxf[A], dy = m.cyf[B] - m.cyf[A];
@@ -53,18 +55,18 @@ __device__ __forceinline__ void interaction_features(const MixedView &m, const L
   const LeafStats s = st[A];
   const float sig = fmaxf(s.sig, 1e-30f);
   const int nA = m.end[A] - m.begin[A], nB = m.end[B] - m.begin[B];
-  f[0] = log2f(fmaxf(dc, 1e-3f * hA) / hA) * 0.25f;
-  f[1] = log2f(fmaxf(gap, 1e-3f * sig) / sig) * 0.25f;
-  f[2] = dc > 0.f ? dx / dc : 0.f;
-  f[3] = dc > 0.f ? dy / dc : 0.f;
-  const float scale = s.g_abs / (6.2831853f * fmaxf(dc, hA) * fmaxf(u_ref, 1e-30f));
-  f[4] = fminf(fmaxf(log2f(scale + 1e-30f), -60.f), 10.f) * (1.f / 16.f);
+  f[0] = __log2f(__fdividef(fmaxf(dc, 1e-3f * hA), hA)) * 0.25f;
+  f[1] = __log2f(__fdividef(fmaxf(gap, 1e-3f * sig), sig)) * 0.25f;
+  f[2] = dc > 0.f ? __fdividef(dx, dc) : 0.f;
+  f[3] = dc > 0.f ? __fdividef(dy, dc) : 0.f;
+  const float scale = __fdividef(s.g_abs, 6.2831853f * fmaxf(dc, hA) * fmaxf(u_ref, 1e-30f));
+  f[4] = fminf(fmaxf(__log2f(scale + 1e-30f), -60.f), 10.f) * (1.f / 16.f);
   f[5] = s.m1;
   f[6] = 2.f * s.m2;
-  f[7] = log2f((float)nA + 1.f) * (1.f / 6.f);
-  f[8] = log2f((float)nB + 1.f) * (1.f / 6.f);
+  f[7] = __log2f((float)nA + 1.f) * (1.f / 6.f);
+  f[8] = __log2f((float)nB + 1.f) * (1.f / 6.f);
   f[9] = (float)type;
-  f[10] = log2f(hB / hA) * 0.25f;
+  f[10] = __log2f(__fdividef(hB, hA)) * 0.25f;
   f[11] = A == B ? 1.f : 0.f;
   for (int k = kNumFeatures; k < kMlpIn; k++) f[k] = 0.f;
 }

@@ -47,25 +47,27 @@ __device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
   return *reinterpret_cast<const uint32_t *>(&h);
 }
 
-// GELU (tanh form) of two values, returned as the BF16 pair of the next
-// layer's input.  The pre-activations are rounded to BF16 and the whole
-// GELU runs in packed BF16x2 arithmetic (FMA pipe) with the tanh on the SFU
-// (one instruction for both values): the result is stored in BF16 anyway,
-// and every step rounds at that same 2^-9 relative level.
+// Twice the GELU (tanh form) of two values, returned as the BF16 pair of
+// the next layer's input.  The pre-activations are rounded to BF16 and the
+// whole GELU runs in packed BF16x2 arithmetic (FMA pipe) with the tanh on
+// the SFU (one instruction for both values): the result is stored in BF16
+// anyway, and every step rounds at that same 2^-9 relative level.
 //   u = z (c0 + c1 z^2),  c0 = sqrt(2/pi), c1 = 0.044715 sqrt(2/pi)
-//   g = h + h tanh(u),    h = z / 2
-__device__ __forceinline__ uint32_t gelu2_bf16(float z0, float z1) {
+//   2 g = z + z tanh(u)
+// The factor 2 is taken out of the next layer's weights (their images are
+// halved, learn_weight_images), which is exact in binary floating point:
+// z + z t rounds to exactly twice (z/2) + (z/2) t, and each product of a
+// halved weight with a doubled input is the same FP32 number as before.
+__device__ __forceinline__ uint32_t gelu2x_bf16(float z0, float z1) {
   const uint32_t z = pack_bf16(z0, z1);
   const uint32_t c0 = 0x3F4C3F4Cu;  // 0.797... in both halves (BF16 0x3F4C)
   const uint32_t c1 = 0x3D123D12u;  // 0.0357 in both halves (BF16 0x3D12)
-  const uint32_t half = 0x3F003F00u;  // 0.5
-  uint32_t z2, p, u, t, h, g;
+  uint32_t z2, p, u, t, g;
   asm("mul.rn.bf16x2 %0, %1, %1;" : "=r"(z2) : "r"(z));
   asm("fma.rn.bf16x2 %0, %1, %2, %3;" : "=r"(p) : "r"(z2), "r"(c1), "r"(c0));
   asm("mul.rn.bf16x2 %0, %1, %2;" : "=r"(u) : "r"(z), "r"(p));
   asm("tanh.approx.bf16x2 %0, %1;" : "=r"(t) : "r"(u));
-  asm("mul.rn.bf16x2 %0, %1, %2;" : "=r"(h) : "r"(z), "r"(half));
-  asm("fma.rn.bf16x2 %0, %1, %2, %1;" : "=r"(g) : "r"(h), "r"(t));
+  asm("fma.rn.bf16x2 %0, %1, %2, %1;" : "=r"(g) : "r"(z), "r"(t));
   return g;
 }
 
@@ -89,7 +91,7 @@ __global__ void __launch_bounds__(kTile) k_mlp_infer(InferArgs a) {
   __shared__ uint64_t bar_w, bar_mma;
   __shared__ uint32_t s_tmem;
   __shared__ int s_fail;
-  __shared__ float s_bias[64 * 3 + 16];
+  __shared__ __align__(16) float s_bias[64 * 3 + 16];
   unsigned char *wsm = smem;
   unsigned char *act = smem + kWBytes;
   const int tid = threadIdx.x, warp = tid >> 5;
@@ -190,10 +192,12 @@ __global__ void __launch_bounds__(kTile) k_mlp_infer(InferArgs a) {
           for (int q = 0; q < 4; q++) {
             uint4 w;
             const int c = c0 + 8 * q;
-            w.x = gelu2_bf16(__uint_as_float(r[8 * q + 0]) + bs[c + 0], __uint_as_float(r[8 * q + 1]) + bs[c + 1]);
-            w.y = gelu2_bf16(__uint_as_float(r[8 * q + 2]) + bs[c + 2], __uint_as_float(r[8 * q + 3]) + bs[c + 3]);
-            w.z = gelu2_bf16(__uint_as_float(r[8 * q + 4]) + bs[c + 4], __uint_as_float(r[8 * q + 5]) + bs[c + 5]);
-            w.w = gelu2_bf16(__uint_as_float(r[8 * q + 6]) + bs[c + 6], __uint_as_float(r[8 * q + 7]) + bs[c + 7]);
+            const float4 b0 = *reinterpret_cast<const float4 *>(bs + c);
+            const float4 b1 = *reinterpret_cast<const float4 *>(bs + c + 4);
+            w.x = gelu2x_bf16(__uint_as_float(r[8 * q + 0]) + b0.x, __uint_as_float(r[8 * q + 1]) + b0.y);
+            w.y = gelu2x_bf16(__uint_as_float(r[8 * q + 2]) + b0.z, __uint_as_float(r[8 * q + 3]) + b0.w);
+            w.z = gelu2x_bf16(__uint_as_float(r[8 * q + 4]) + b1.x, __uint_as_float(r[8 * q + 5]) + b1.y);
+            w.w = gelu2x_bf16(__uint_as_float(r[8 * q + 6]) + b1.z, __uint_as_float(r[8 * q + 7]) + b1.w);
             *reinterpret_cast<uint4 *>(rowp + (uint32_t)(c / 8) * 128u) = w;
           }
         }
@@ -201,7 +205,13 @@ __global__ void __launch_bounds__(kTile) k_mlp_infer(InferArgs a) {
         uint32_t r[16];
         tmem_ld16(taddr, r);
         tmem_wait();
-        for (int j = 0; j < 16; j++) v[j] = __uint_as_float(r[j]) + bs[j];
+        for (int j = 0; j < 16; j += 4) {
+          const float4 b = *reinterpret_cast<const float4 *>(bs + j);
+          v[j] = __uint_as_float(r[j]) + b.x;
+          v[j + 1] = __uint_as_float(r[j + 1]) + b.y;
+          v[j + 2] = __uint_as_float(r[j + 2]) + b.z;
+          v[j + 3] = __uint_as_float(r[j + 3]) + b.w;
+        }
       }
     }
     if (valid) {
@@ -235,14 +245,15 @@ uint16_t bf16_host(float x) {
   return (uint16_t)(r >> 16);
 }
 
-// W [N][K] row-major -> core-matrix image (rows = N, K contiguous in 16-byte
-// chunks; SBO = K/8*128).
-void image_of(const float *W, int N, int K, uint16_t *out) {
+// scale * W [N][K] row-major -> core-matrix image (rows = N, K contiguous in
+// 16-byte chunks; SBO = K/8*128).  scale is a power of two, so the BF16
+// image is exactly scale times the BF16 rounding of W.
+void image_of(const float *W, int N, int K, float scale, uint16_t *out) {
   const int sbo = K / 8 * 128;
   for (int j = 0; j < N; j++)
     for (int k = 0; k < K; k++) {
       const size_t byte = (size_t)(j / 8) * sbo + (size_t)(k / 8) * 128 + (size_t)(j % 8) * 16 + (size_t)(k % 8) * 2;
-      out[byte / 2] = bf16_host(W[(size_t)j * K + k]);
+      out[byte / 2] = bf16_host(scale * W[(size_t)j * K + k]);
     }
 }
 
@@ -252,10 +263,11 @@ size_t learn_weight_image_elems() { return kWBytes / 2; }
 
 void learn_weight_images(const float *theta, std::vector<uint16_t> &img, std::vector<float> &bias) {
   img.assign(kWBytes / 2, 0);
-  image_of(theta + 0, 64, 16, img.data());
-  image_of(theta + 1088, 64, 64, img.data() + kW1Bytes / 2);
-  image_of(theta + 5248, 64, 64, img.data() + (kW1Bytes + kW2Bytes) / 2);
-  image_of(theta + 9408, 16, 64, img.data() + (kW1Bytes + 2 * kW2Bytes) / 2);
+  // layers 2-4 read twice the GELU (gelu2x_bf16): their weights are halved
+  image_of(theta + 0, 64, 16, 1.0f, img.data());
+  image_of(theta + 1088, 64, 64, 0.5f, img.data() + kW1Bytes / 2);
+  image_of(theta + 5248, 64, 64, 0.5f, img.data() + (kW1Bytes + kW2Bytes) / 2);
+  image_of(theta + 9408, 16, 64, 0.5f, img.data() + (kW1Bytes + 2 * kW2Bytes) / 2);
   bias.assign(64 * 3 + 16, 0.f);
   std::memcpy(bias.data(), theta + 1024, 64 * 4);
   std::memcpy(bias.data() + 64, theta + 5184, 64 * 4);
