@@ -126,7 +126,7 @@ def load(path: str | None = None):
     L.tree2d_learn_set_weights.argtypes = [fp, ctypes.c_int]
     L.tree2d_learn_get_weights.argtypes = [fp, ctypes.c_int]
     L.tree2d_learn_set_options.argtypes = [ctypes.c_float, ctypes.c_int, ctypes.c_double]
-    L.tree2d_learn_set_envelope.argtypes = [ctypes.c_double]
+    L.tree2d_learn_set_envelope.argtypes = [ctypes.c_double, ctypes.c_double]
     L.tree2d_learn_set_envelope.restype = ctypes.c_int
     L.tree2d_learn_collect.argtypes = [ctypes.c_int, ctypes.c_uint, fp, _ip]
     L.tree2d_learn_train.argtypes = [ctypes.c_int, fp, _ip, ctypes.c_int, ctypes.c_int, ctypes.c_float,
@@ -185,7 +185,7 @@ def set_mode(mode: int):
     _check(load().tree2d_set_mode(mode), "set_mode")
 
 
-def set_mixed_params(pterms: int = 16, cutoff_sigmas: float = 4.0, use_tensor_cores: bool = True):
+def set_mixed_params(pterms: int = 16, cutoff_sigmas: float = 2.5, use_tensor_cores: bool = True):
     _check(load().tree2d_set_mixed_params(pterms, cutoff_sigmas, int(use_tensor_cores)), "set_mixed_params")
 
 
@@ -346,10 +346,11 @@ def learn_set_options(direct_bias: float = 1.0, order_margin: int = 1, budget: f
     _check(load().tree2d_learn_set_options(direct_bias, order_margin, budget), "learn_set_options")
 
 
-def learn_set_envelope(k_per_leaf_max: float):
+def learn_set_envelope(k_per_leaf_max: float, cutoff_sigmas: float = 0.0):
     """Training envelope: the largest mean K-list entries per leaf the
-    network was trained on (denser solves run the fixed mixed form)."""
-    _check(load().tree2d_learn_set_envelope(k_per_leaf_max), "learn_set_envelope")
+    network was trained on, counted at correction radius `cutoff_sigmas`
+    (0: the radius in force); denser solves run the fixed mixed form."""
+    _check(load().tree2d_learn_set_envelope(k_per_leaf_max, cutoff_sigmas), "learn_set_envelope")
 
 
 def learn_collect(max_samples: int, seed: int = 0):

@@ -966,11 +966,14 @@ int tree2d_learn_set_options(float direct_bias, int order_margin, double budget)
   return TREE2D_OK;
 }
 
-int tree2d_learn_set_envelope(double k_per_leaf_max) {
+int tree2d_learn_set_envelope(double k_per_leaf_max, double cutoff_sigmas) {
   Lib &L = lib();
   std::lock_guard<std::mutex> lk(L.mu);
   if (!(k_per_leaf_max >= 0.0) || !std::isfinite(k_per_leaf_max)) return fail(TREE2D_ERR_BAD_PARAMS);
+  if (!(cutoff_sigmas >= 0.0) || !std::isfinite(cutoff_sigmas) || cutoff_sigmas > 64.0)
+    return fail(TREE2D_ERR_BAD_PARAMS);
   L.lp->k_per_leaf_max = k_per_leaf_max;
+  L.lp->cutoff_train = cutoff_sigmas;
   return TREE2D_OK;
 }
 

@@ -37,7 +37,7 @@ struct LeafStats;
 // Parameters of the mixed-precision form.
 struct MixedParams {
   int pterms = 16;        // expansion length P (terms 0..P-1) of multipole and local
-  double cutoff = 3.0;    // regularisation correction radius, in units of max sigma
+  double cutoff = 2.5;    // regularisation correction radius, in units of max sigma
   int use_tensor_cores = 1;
   int learned = 0;        // TREE2D_MODE_LEARNED: near-field decisions by the network
   const LearnedParams *lp = nullptr;
@@ -63,6 +63,7 @@ struct DevStatus {
   int deeper;              // build: keys of kShortKeyLevels levels do not suffice
   int list_overflow;       // mixed: a leaf's lists did not fit the one-walk scratch
   int list_max;            // mixed: most list entries (U + W + K) of one leaf
+  unsigned long long k_env;  // mixed: leaves beyond the correction radius but within the walk radius
 };
 
 // Bump allocator over one device allocation.  Buffers are 256-byte aligned.

@@ -362,7 +362,11 @@ __device__ __forceinline__ float box_gap(const MixedView &m, int a, int b) {
 //   W: cells below B's same-level neighbours that are not adjacent to B
 //      but whose parent is;
 //   K: leaves not adjacent to B whose box lies within rc of B's box (the
-//      blob-core correction).
+//      blob-core correction).  The correction walk descends to the walk
+//      radius walk_scale * rc: the counting passes also count the
+//      non-adjacent leaves between rc and that radius (the learned form's
+//      training envelope is a K-list density at a larger radius); every
+//      pass walks the same cells, so the lists keep one emission order.
 // The walk keeps one stack per warp in shared memory; every round pops up
 // to 8 cells and lane (entry, quadrant) classifies one child, so a leaf's
 // lists take tens of rounds instead of hundreds of serial steps.  Stack
@@ -400,6 +404,8 @@ __global__ void __launch_bounds__(32 * kWalkWarps) k_lists(MixedView m) {
     const unsigned tx = bx >> sh, ty = by >> sh;
     rc = m.rc_set[(ty >> 1) * (1u << (m.lev0 - 1)) + (tx >> 1)];
   }
+  const float rw = rc * m.walk_scale;
+  unsigned env = 0;  // this lane's leaves in [rc, rw)
   int base[3] = {0, 0, 0};
   if (kFill) {
     base[0] = m.u_off[l];
@@ -463,9 +469,15 @@ __global__ void __launch_bounds__(32 * kWalkWarps) k_lists(MixedView m) {
       cc = m.child[4 * c + q];
       if (cc >= 0) {
         if (v & kTagK) {
-          if (box_gap(m, cc, b) < rc) {
+          const float g = box_gap(m, cc, b);
+          if (g < rw) {
             if (m.leaf[cc]) {
-              if (!adj_cells(m, cc, b)) kind = 2;
+              if (!adj_cells(m, cc, b)) {
+                if (g < rc)
+                  kind = 2;
+                else
+                  env++;
+              }
             } else {
               grow = true;
               gv = (unsigned)cc | kTagK;
@@ -490,6 +502,10 @@ __global__ void __launch_bounds__(32 * kWalkWarps) k_lists(MixedView m) {
     }
     push(grow, gv);
     __syncwarp();
+  }
+  if (!kFill && m.walk_scale > 1.f) {
+    for (int o = 16; o; o >>= 1) env += __shfl_xor_sync(0xffffffffu, env, o);
+    if (lane == 0 && env) atomicAdd(&m.st->k_env, (unsigned long long)env);
   }
   if (!kFill && lane == 0) {
     m.u_off[l] = base[0];
@@ -1451,6 +1467,12 @@ int mixed_solve(Workspace &ws, const Tree &t, const MixedParams &mp, double *d_u
   m.rc_ptr = reinterpret_cast<const float *>(rc_bits);
   m.rc_set = reinterpret_cast<const float *>(rc_set_bits);
   m.lev0 = t.lev0;
+  // the learned form's envelope counts K entries at the radius its network
+  // was trained with; when that is larger than the one in force, the
+  // correction walk goes out to it and counts the extra leaves
+  const bool envelope_walk = mp.learned && mp.lp && mp.lp->have_weights && mp.lp->k_per_leaf_max > 0.0 &&
+                             mp.lp->cutoff_train > mp.cutoff && t.lev0 == 0;
+  m.walk_scale = envelope_walk ? (float)(mp.lp->cutoff_train / mp.cutoff) : 1.f;
   m.m2m = reinterpret_cast<const float2 *>(dm2m);
   m.l2l = reinterpret_cast<const float2 *>(dl2l);
   m.st = ws.status;
@@ -1513,8 +1535,10 @@ int mixed_solve(Workspace &ws, const Tree &t, const MixedParams &mp, double *d_u
   // reference scale u_ref is one per tree.
   // the network decides only inside its training envelope: denser lists
   // than it was trained on would add up more accepted errors per target
-  // than its per-interaction budget allows for
-  const bool in_envelope = mp.lp && (mp.lp->k_per_leaf_max <= 0.0 || (double)tot[2] <= mp.lp->k_per_leaf_max * nl);
+  // than its per-interaction budget allows for (K entries counted out to
+  // the training radius)
+  const double k_env = (double)tot[2] + (double)ws.h_status->k_env;
+  const bool in_envelope = mp.lp && (mp.lp->k_per_leaf_max <= 0.0 || k_env <= mp.lp->k_per_leaf_max * nl);
   const bool learned = mp.learned && mp.lp && mp.lp->have_weights && t.lev0 == 0 && in_envelope;
   st.learned_active = learned ? 1 : 0;
   st.n_list_u = tot[0];

@@ -41,9 +41,11 @@ DEFAULT_WEIGHTS = os.path.join(HERE, "data", "learned_weights.npz")
 ENVELOPE_FACTOR = 2.5
 
 
-def save_weights(path, theta, meta, k_per_leaf_train=None):
+def save_weights(path, theta, meta, k_per_leaf_train=None, cutoff_train=None):
     os.makedirs(os.path.dirname(os.path.abspath(path)), exist_ok=True)
     extra = {} if k_per_leaf_train is None else {"k_per_leaf_train": np.float64(k_per_leaf_train)}
+    if cutoff_train is not None:
+        extra["cutoff_train"] = np.float64(cutoff_train)
     np.savez(path, version=WEIGHTS_VERSION, theta=np.asarray(theta, np.float32), meta=json.dumps(meta), **extra)
 
 
@@ -58,15 +60,19 @@ def load_weights(path=DEFAULT_WEIGHTS):
 
 
 def load_envelope(path=DEFAULT_WEIGHTS):
-    """K-list entries per leaf up to which the network's decisions apply
-    (ENVELOPE_FACTOR x the training solves' largest mean), or 0 (no
-    limit) for a weights file without the training figure."""
+    """(K-list entries per leaf up to which the network's decisions apply,
+    correction radius they are counted at): ENVELOPE_FACTOR x the training
+    solves' largest mean, at the training radius (3.0 max sigma for files
+    that do not record it); (0, 0) = no limit, for a weights file without
+    the training figure.  The pair is the argument list of
+    learn_set_envelope."""
     if not os.path.exists(path):
-        return 0.0
+        return 0.0, 0.0
     d = np.load(path)
     if "k_per_leaf_train" not in d.files:
-        return 0.0
-    return float(d["k_per_leaf_train"]) * ENVELOPE_FACTOR
+        return 0.0, 0.0
+    cutoff = float(d["cutoff_train"]) if "cutoff_train" in d.files else 3.0
+    return float(d["k_per_leaf_train"]) * ENVELOPE_FACTOR, cutoff
 
 
 def _dev_arrays(torch, b):
@@ -134,8 +140,8 @@ def run(n=1_048_576, steps=100, dt=1e-3, train_until=20, samples=200_000, train_
     summary = {"samples": int(len(y)), "label_histogram": hist, "final_loss": loss, "collect_s": t_collect,
                "train_s": t_train, "k_per_leaf_train": k_per_leaf}
     if out:
-        save_weights(out, theta, summary, k_per_leaf_train=k_per_leaf)
-    P.learn_set_envelope(k_per_leaf * ENVELOPE_FACTOR)
+        save_weights(out, theta, summary, k_per_leaf_train=k_per_leaf, cutoff_train=cutoff)
+    P.learn_set_envelope(k_per_leaf * ENVELOPE_FACTOR, cutoff)
     # score steps 21..steps
     tm, tl, tp = [], [], []
     for step in range(train_until + 1, steps + 1):

@@ -49,7 +49,7 @@ def parse():
     ap.add_argument("--mode", default="learned", choices=list(MODES))
     ap.add_argument("--weights", default=None, help="learned form: weights file (default: the packaged ones)")
     ap.add_argument("--pterms", type=int, default=16, help="mixed form: expansion length")
-    ap.add_argument("--cutoff", type=float, default=3.0, help="mixed form: correction radius / max sigma")
+    ap.add_argument("--cutoff", type=float, default=2.5, help="mixed form: correction radius / max sigma")
     ap.add_argument("--cuda-core-m2l", action="store_true", help="mixed form: M2L on CUDA cores")
     ap.add_argument("--no-plain", action="store_true", help="skip timing the plain FP64 path beside")
     ap.add_argument("--eval-variant", type=int, default=-1,
@@ -347,10 +347,11 @@ def run_ours(args):
             learned_note = f"none found at {os.path.relpath(path, ROOT)}: fixed mixed form (the fallback)"
         else:
             P.learn_set_weights(theta)
-            envelope = L.load_envelope(path)
-            P.learn_set_envelope(envelope)
+            envelope, env_cutoff = L.load_envelope(path)
+            P.learn_set_envelope(envelope, env_cutoff)
             learned_note = (f"{os.path.relpath(path, ROOT)} (trained on configuration-5 steps 0-20 by "
-                            f"2dfmm_gb300/learn.py); decisions applied up to {envelope:.1f} K-list entries per leaf")
+                            f"2dfmm_gb300/learn.py); decisions applied up to {envelope:.1f} K-list entries per "
+                            f"leaf counted at {env_cutoff:g} max sigma")
     n = b.n
     xy = torch.from_numpy(b.xy).to(dev).contiguous()
     cir = torch.from_numpy(b.cir).to(dev)

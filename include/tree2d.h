@@ -86,7 +86,7 @@ int tree2d_get_mode(void);
  * correction in units of the largest core radius (pairs closer than that
  * which the far field treats as point vortices get exp(-r^2/sigma^2)
  * added back), and whether M2L runs on the tensor cores (1) or on CUDA
- * cores (0, for checking).  Defaults 16, 3.0, 1. */
+ * cores (0, for checking).  Defaults 16, 2.5, 1. */
 int tree2d_set_mixed_params(int pterms, double cutoff_sigmas, int use_tensor_cores);
 
 /* Evaluates n targets (xy interleaved, host memory) into uv (interleaved,
@@ -219,12 +219,17 @@ int tree2d_learn_get_weights(float *theta, int n);
  * units of sum|G| / root side.  Defaults 1.0, 1, 3e-7. */
 int tree2d_learn_set_options(float direct_bias, int order_margin, double budget);
 /* Training envelope of the loaded network: the largest mean number of K
- * (correction) list entries per leaf the training solves had.  A solve
- * whose lists are denser than this runs the fixed mixed form instead (the
- * network's per-interaction error budget does not bound the sum over more
+ * (correction) list entries per leaf the training solves had, counted with
+ * the correction radius cutoff_sigmas (units of the largest core radius; 0
+ * = the radius in force).  A solve whose lists, counted at that radius, are
+ * denser than this runs the fixed mixed form instead (the network's
+ * per-interaction error budget does not bound the sum over more
  * interactions than it was trained on); tree2d_get_stats reports it in
- * learned_active.  0 = no limit (the default). */
-int tree2d_learn_set_envelope(double k_per_leaf_max);
+ * learned_active.  When cutoff_sigmas is above the radius in force, the
+ * list walk goes out to it to count; below it, the entries are counted at
+ * the radius in force (more of them: the conservative side).
+ * k_per_leaf_max 0 = no limit (the default). */
+int tree2d_learn_set_envelope(double k_per_leaf_max, double cutoff_sigmas);
 /* Training data from the last tree2d_solve_device in mixed or learned mode:
  * up to max_samples interactions drawn with `seed`, their features
  * (features[max][16]) and the cheapest class whose error against the FP64

@@ -44,11 +44,11 @@ def test_tensor_core_inference_matches_training_forward(gpu_lib):
     assert agree >= 0.95, agree
 
 
-def _solve(P, torch, b, mode):
+def _solve(P, torch, b, mode, cutoff=3.0):
     dev = torch.device("cuda:0")
     P.set_params(b.nterms, b.num_p, b.theta)
     P.set_mode(mode)
-    P.set_mixed_params(16, 3.0, True)
+    P.set_mixed_params(16, cutoff, True)
     xy = torch.from_numpy(b.xy).to(dev)
     cir = torch.from_numpy(b.cir).to(dev)
     cor = torch.from_numpy(b.cor).to(dev)
@@ -113,6 +113,52 @@ def test_training_envelope_falls_back_to_the_mixed_form(gpu_lib):
         uv_m, _, _, _, st_m = _solve(P, torch, b, P.MODE_MIXED)
         assert st_g["learned_active"] == 0
         assert np.array_equal(uv_g.cpu().numpy(), uv_m.cpu().numpy())
+    finally:
+        P.learn_set_envelope(0.0)
+        P.set_mode(P.MODE_PLAIN)
+
+
+@pytest.mark.gpu
+def test_envelope_counted_at_the_training_radius(gpu_lib):
+    """With the correction radius in force (2.5 max sigma) below the one the
+    envelope was counted at (3.0), the list walk goes out to 3.0 to count:
+    an envelope between the two densities makes the solve fall back, the
+    same envelope counted at the radius in force does not, and the lists
+    themselves stay those of 2.5 (the longer walk only counts)."""
+    torch = pytest.importorskip("torch")
+    import importlib
+    P = gpu_lib
+    L = importlib.import_module("2dfmm_gb300.learn")
+    theta = L.load_weights()
+    if theta is None:
+        pytest.skip("no packaged weights")
+    W = workloads()
+    # cores wide against the leaves, so that 2.5 and 3.0 max sigma reach
+    # different leaves
+    b = W.lamb_oseen(131_072, seed=23, sigma=0.008)
+    P.learn_set_weights(theta)
+    try:
+        P.learn_set_envelope(0.0)
+        _, _, _, _, st30 = _solve(P, torch, b, P.MODE_MIXED, cutoff=3.0)
+        uv25, _, _, _, st25 = _solve(P, torch, b, P.MODE_MIXED, cutoff=2.5)
+        k30 = st30["n_list_k"] / st30["n_leaves"]
+        k25 = st25["n_list_k"] / st25["n_leaves"]
+        assert st30["n_leaves"] == st25["n_leaves"] and k25 < k30
+        mid = 0.5 * (k25 + k30)
+        P.learn_set_envelope(mid, 3.0)
+        uv_f, _, _, _, st_f = _solve(P, torch, b, P.MODE_LEARNED, cutoff=2.5)
+        assert st_f["learned_active"] == 0 and st_f["n_list_k"] == st25["n_list_k"]
+        # the fallback is the fixed mixed form at 2.5; the longer walk only
+        # changes the order the correction leaves are visited in
+        ref = uv25.cpu().numpy()
+        got = uv_f.cpu().numpy()
+        assert np.linalg.norm(got - ref) <= 1e-6 * np.linalg.norm(ref)
+        P.learn_set_envelope(mid, 0.0)
+        _, _, _, _, st_a = _solve(P, torch, b, P.MODE_LEARNED, cutoff=2.5)
+        assert st_a["learned_active"] == 1 and st_a["n_list_k"] == st25["n_list_k"]
+        P.learn_set_envelope(1e9, 3.0)
+        _, _, _, _, st_b = _solve(P, torch, b, P.MODE_LEARNED, cutoff=2.5)
+        assert st_b["learned_active"] == 1 and st_b["n_list_k"] == st25["n_list_k"]
     finally:
         P.learn_set_envelope(0.0)
         P.set_mode(P.MODE_PLAIN)
