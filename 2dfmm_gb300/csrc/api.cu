@@ -63,6 +63,15 @@ cudaError_t workspace_init(Workspace &ws) {
   if (e != cudaSuccess) return e;
   e = cudaEventCreateWithFlags(&ws.join_ev, cudaEventDisableTiming);
   if (e != cudaSuccess) return e;
+  int least = 0, greatest = 0;
+  e = cudaDeviceGetStreamPriorityRange(&least, &greatest);
+  if (e != cudaSuccess) return e;
+  e = cudaStreamCreateWithPriority(&ws.hi, cudaStreamNonBlocking, greatest);
+  if (e != cudaSuccess) return e;
+  e = cudaEventCreateWithFlags(&ws.hi_fork, cudaEventDisableTiming);
+  if (e != cudaSuccess) return e;
+  e = cudaEventCreateWithFlags(&ws.hi_join, cudaEventDisableTiming);
+  if (e != cudaSuccess) return e;
   ws.init = true;
   return cudaSuccess;
 }

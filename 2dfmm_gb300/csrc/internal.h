@@ -152,6 +152,8 @@ struct Workspace {
   cudaEvent_t ev[8] = {};
   cudaStream_t side = nullptr;    // second stream (learned decisions beside the expansions)
   cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
+  cudaStream_t hi = nullptr;      // highest-priority stream: the expansions while the decisions run
+  cudaEvent_t hi_fork = nullptr, hi_join = nullptr;
   bool init = false;
 };
 

@@ -1549,7 +1549,10 @@ int mixed_solve(Workspace &ws, const Tree &t, const MixedParams &mp, double *d_u
   // that no kernel of this solve still runs when its buffers are reused
   bool forked = false;
   auto drain = [&](int code) {
-    if (forked) cudaStreamSynchronize(ws.side);
+    if (forked) {
+      cudaStreamSynchronize(ws.side);
+      cudaStreamSynchronize(ws.hi);
+    }
     return code;
   };
 #define T2D_TRY_DRAIN(expr)                 \
@@ -1597,15 +1600,29 @@ int mixed_solve(Workspace &ws, const Tree &t, const MixedParams &mp, double *d_u
     }
     T2D_TRY_DRAIN(cudaEventRecord(ws.join_ev, s2));
   }
-  rc = mixed_upward(m, t.depth, s);
+  // Beside the decisions, the expansions run on the highest-priority
+  // stream: their chain of short per-level kernels is the critical path,
+  // and the inference CTAs (low priority, a few tiles each) fill the SMs
+  // around it instead of holding them.
+  cudaStream_t su = s;
+  if (side) {
+    T2D_TRY_DRAIN(cudaEventRecord(ws.hi_fork, s));
+    T2D_TRY_DRAIN(cudaStreamWaitEvent(ws.hi, ws.hi_fork, 0));
+    su = ws.hi;
+  }
+  rc = mixed_upward(m, t.depth, su);
   if (rc) return drain(rc);
-  T2D_TRY_DRAIN(cudaMemsetAsync(m.L, 0, sizeof(float) * (size_t)nc * 2 * P, s));
-  rc = tc ? m2l_tensor_cores(m, dimg, cls_list, cls_count, s) : m2l_cuda_cores(m, dm2l, s);
+  T2D_TRY_DRAIN(cudaMemsetAsync(m.L, 0, sizeof(float) * (size_t)nc * 2 * P, su));
+  rc = tc ? m2l_tensor_cores(m, dimg, cls_list, cls_count, su) : m2l_cuda_cores(m, dm2l, su);
   if (rc) return drain(rc);
   st.m2l_path = tc ? 2 : 1;
-  rc = mixed_downward(m, t.depth, s);
+  rc = mixed_downward(m, t.depth, su);
   if (rc) return drain(rc);
-  if (side) T2D_TRY_DRAIN(cudaStreamWaitEvent(s, ws.join_ev, 0));
+  if (side) {
+    T2D_TRY_DRAIN(cudaEventRecord(ws.hi_join, ws.hi));
+    T2D_TRY_DRAIN(cudaStreamWaitEvent(s, ws.hi_join, 0));
+    T2D_TRY_DRAIN(cudaStreamWaitEvent(s, ws.join_ev, 0));
+  }
   T2D_CUDA_TRY(cudaEventRecord(ws.ev[4], s));
   const Decisions dec = learned ? Decisions{u_dec, k_dec, mp.lp->order_margin} : Decisions{nullptr, nullptr, 0};
   rc = near_field(ws, mp, m, learned, dec, d_uv, t.perm, s, st);
