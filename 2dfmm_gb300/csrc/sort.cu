@@ -4,7 +4,8 @@
 //   scan      : per digit, exclusive scan of its tile counts (one block per
 //               digit); digit totals are scanned inside the downsweep
 //   downsweep : stable rank inside the tile (warp match + per-warp running
-//               counts), scatter to counts-scan offset + rank.
+//               counts), staged in shared memory in digit order, then
+//               written to counts-scan offset + rank with coalesced stores.
 // Tiles are processed warp-striped: warp w owns 512 consecutive pairs, its
 // lanes take 32 consecutive pairs per step, so (warp, step, lane) is the
 // input order and the ranking is stable.
@@ -19,6 +20,7 @@ constexpr int kItems = 16;                    // per thread
 constexpr int kTile = kThreads * kItems;      // 4096
 constexpr int kBins = 256;
 static_assert(kThreads == kBins, "the downsweep scans the digit totals with one thread per digit");
+constexpr int kStageBytes = kTile * (8 + 4);  // the downsweep's staging of one tile (48 KB)
 
 __device__ __forceinline__ unsigned lanemask_lt() {
   unsigned m;
@@ -72,33 +74,48 @@ __global__ void __launch_bounds__(1024) k_scan_digit(unsigned *counts, int ntile
   if (t == 1023) totals[blockIdx.x] = part[1023];
 }
 
+// Exclusive scan of one value per thread over the block (kThreads values,
+// thread order).  `wsum` is kWarps words of shared scratch; the call
+// synchronises the block before it returns.
+__device__ __forceinline__ unsigned block_exclusive_scan(unsigned v, unsigned *wsum) {
+  const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+  unsigned incl = v;
+  for (int o = 1; o < 32; o <<= 1) {
+    const unsigned u = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += u;
+  }
+  if (lane == 31) wsum[w] = incl;
+  __syncthreads();
+  unsigned base = 0;
+  for (int k = 0; k < w; k++) base += wsum[k];
+  __syncthreads();
+  return base + incl - v;
+}
+
+// The tile's pairs are ranked (stable: warp, step, lane order within a
+// digit), staged in shared memory in digit order, and written out from
+// there: consecutive threads write consecutive positions of a digit's run,
+// so the stores coalesce instead of scattering one pair per digit.
 __global__ void __launch_bounds__(kThreads) k_downsweep(const uint64_t *__restrict__ kin,
                                                         const uint32_t *__restrict__ vin,
                                                         uint64_t *__restrict__ kout, uint32_t *__restrict__ vout,
                                                         int n, int shift, const unsigned *__restrict__ offs,
                                                         int ntiles, const unsigned *__restrict__ totals) {
+  extern __shared__ __align__(16) unsigned char stage[];
+  uint64_t *sk = reinterpret_cast<uint64_t *>(stage);             // kTile keys, tile digit order
+  uint32_t *sv = reinterpret_cast<uint32_t *>(stage + kTile * 8);  // kTile values
   __shared__ unsigned wcount[kWarps][kBins];
-  __shared__ unsigned dbase[kBins];
-  {
-    // exclusive scan of the 256 digit totals (kThreads == kBins)
-    const int t = threadIdx.x, lane = t & 31, w = t >> 5;
-    const unsigned v = totals[t];
-    unsigned incl = v;
-    for (int o = 1; o < 32; o <<= 1) {
-      unsigned u = __shfl_up_sync(0xffffffffu, incl, o);
-      if (lane >= o) incl += u;
-    }
-    __shared__ unsigned wsum[kWarps];
-    if (lane == 31) wsum[w] = incl;
-    __syncthreads();
-    unsigned base = 0;
-    for (int k = 0; k < w; k++) base += wsum[k];
-    dbase[t] = base + incl - v;
-  }
+  __shared__ unsigned lbase[kBins];  // tile-local start of each digit's run
+  __shared__ unsigned gbase[kBins];  // global position of that start
+  __shared__ unsigned wsum[kWarps];
+  // digit d's global start: exclusive scan of the digit totals, plus the
+  // tiles before this one (kThreads == kBins: thread t owns digit t)
+  const unsigned dbase = block_exclusive_scan(totals[threadIdx.x], wsum);
   for (int i = threadIdx.x; i < kWarps * kBins; i += kThreads) (&wcount[0][0])[i] = 0;
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const long base = (long)blockIdx.x * kTile + warp * (kItems * 32);
+  const long tile0 = (long)blockIdx.x * kTile;
+  const long base = tile0 + warp * (kItems * 32);
   uint64_t k[kItems];
   uint32_t v[kItems];
   unsigned r[kItems];
@@ -119,25 +136,39 @@ __global__ void __launch_bounds__(kThreads) k_downsweep(const uint64_t *__restri
     r[j] = c + rank;
   }
   __syncthreads();
-  for (int d = threadIdx.x; d < kBins; d += kThreads) {
-    unsigned run = dbase[d] + offs[(size_t)d * ntiles + blockIdx.x];
+  // per digit: the warps' counts become their starts inside the digit's run
+  unsigned cnt = 0;
+  {
+    const int d = threadIdx.x;
 #pragma unroll
     for (int w = 0; w < kWarps; w++) {
-      unsigned c = wcount[w][d];
-      wcount[w][d] = run;
-      run += c;
+      const unsigned c = wcount[w][d];
+      wcount[w][d] = cnt;
+      cnt += c;
     }
   }
+  const unsigned lb = block_exclusive_scan(cnt, wsum);
+  lbase[threadIdx.x] = lb;
+  gbase[threadIdx.x] = dbase + offs[(size_t)threadIdx.x * ntiles + blockIdx.x];
   __syncthreads();
 #pragma unroll
   for (int j = 0; j < kItems; j++) {
     long i = base + j * 32 + lane;
     if (i < n) {
-      unsigned d = (unsigned)((k[j] >> shift) & 0xff);
-      unsigned pos = wcount[warp][d] + r[j];
-      kout[pos] = k[j];
-      vout[pos] = v[j];
+      const unsigned d = (unsigned)((k[j] >> shift) & 0xff);
+      const unsigned lp = lbase[d] + wcount[warp][d] + r[j];
+      sk[lp] = k[j];
+      sv[lp] = v[j];
     }
+  }
+  __syncthreads();
+  const int tile_n = (int)min((long)kTile, (long)n - tile0);
+  for (int p = threadIdx.x; p < tile_n; p += kThreads) {
+    const uint64_t key = sk[p];
+    const unsigned d = (unsigned)((key >> shift) & 0xff);
+    const unsigned pos = gbase[d] + ((unsigned)p - lbase[d]);
+    kout[pos] = key;
+    vout[pos] = sv[p];
   }
 }
 
@@ -157,12 +188,14 @@ cudaError_t radix_sort_pairs(uint64_t *keys, uint32_t *vals, uint64_t *keys_alt,
   uint64_t *ka = keys, *kb = keys_alt;
   uint32_t *va = vals, *vb = vals_alt;
   int passes = 0;
+  cudaError_t e = cudaFuncSetAttribute(k_downsweep, cudaFuncAttributeMaxDynamicSharedMemorySize, kStageBytes);
+  if (e != cudaSuccess) return e;
   for (int shift = begin_bit; shift < end_bit; shift += 8, passes++) {
     k_upsweep<<<ntiles, kThreads, 0, s>>>(ka, n, shift, counts, ntiles);
     ::t2d::g_launches.fetch_add(1, std::memory_order_relaxed);
     k_scan_digit<<<kBins, 1024, 0, s>>>(counts, ntiles, totals);
     ::t2d::g_launches.fetch_add(1, std::memory_order_relaxed);
-    k_downsweep<<<ntiles, kThreads, 0, s>>>(ka, va, kb, vb, n, shift, counts, ntiles, totals);
+    k_downsweep<<<ntiles, kThreads, kStageBytes, s>>>(ka, va, kb, vb, n, shift, counts, ntiles, totals);
     ::t2d::g_launches.fetch_add(1, std::memory_order_relaxed);
     uint64_t *tk = ka;
     ka = kb;
