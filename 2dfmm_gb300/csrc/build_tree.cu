@@ -31,7 +31,7 @@
 namespace t2d {
 namespace {
 
-constexpr int kBoxBlocks = 304;   // 2 x 152 SMs
+constexpr int kBoxBlocks = 1216;  // 8 x 152 SMs: enough loads in flight to stream the positions
 
 struct __align__(16) Box4 {
   double x, y, z, w;  // xmax, xmin, ymax, ymin
@@ -49,37 +49,61 @@ __device__ __forceinline__ double warp_min(double v) {
   return v;
 }
 
+// Order-preserving map of a non-NaN double to an unsigned integer (-0 is
+// taken as +0, as the FP64 comparisons treat them): a >= b iff
+// okey(a) >= okey(b).  Lets the key descent compare on the integer pipe.
+__device__ __forceinline__ uint64_t okey(double d) {
+  uint64_t u = (uint64_t)__double_as_longlong(d);
+  if (u == 0x8000000000000000ull) u = 0;
+  return (u >> 63) ? ~u : (u | 0x8000000000000000ull);
+}
+__device__ __forceinline__ double okey_inv(uint64_t k) {
+  const uint64_t u = (k >> 63) ? (k & 0x7fffffffffffffffull) : ~k;
+  return __longlong_as_double((long long)u);
+}
+
 // Bounding box of the positions (non-finite positions are bad input; the
 // circulations and core radii are checked where they are first read, in
-// k_gather).
+// k_gather).  The extremes are kept as order-preserving integers (okey), so
+// the comparisons run on the integer pipe, not the slow FP64 one; a block
+// writes its extremes back as doubles (-0 as +0, which compares the same).
 __global__ void __launch_bounds__(256) k_bbox(const double *__restrict__ xy, int n, Box4 *part, DevStatus *st) {
-  double xmax = -INFINITY, xmin = INFINITY, ymax = -INFINITY, ymin = INFINITY;
+  uint64_t xmax = okey(-INFINITY), xmin = okey(INFINITY), ymax = xmax, ymin = xmin;
   bool bad = false;
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
-    double x = xy[2 * i], y = xy[2 * i + 1];
+    const double x = xy[2 * i], y = xy[2 * i + 1];  // the caller's array: 8-byte alignment only
     bad |= !(isfinite(x) && isfinite(y));
-    xmax = fmax(xmax, x);
-    xmin = fmin(xmin, x);
-    ymax = fmax(ymax, y);
-    ymin = fmin(ymin, y);
+    const uint64_t kx = okey(x), ky = okey(y);
+    xmax = kx > xmax ? kx : xmax;
+    xmin = kx < xmin ? kx : xmin;
+    ymax = ky > ymax ? ky : ymax;
+    ymin = ky < ymin ? ky : ymin;
   }
-  __shared__ Box4 s[8];
-  xmax = warp_max(xmax);
-  xmin = warp_min(xmin);
-  ymax = warp_max(ymax);
-  ymin = warp_min(ymin);
-  int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  if (lane == 0) s[w] = Box4{xmax, xmin, ymax, ymin};
+  for (int o = 16; o; o >>= 1) {
+    const uint64_t a = __shfl_xor_sync(0xffffffffu, xmax, o), b = __shfl_xor_sync(0xffffffffu, xmin, o);
+    const uint64_t c = __shfl_xor_sync(0xffffffffu, ymax, o), d = __shfl_xor_sync(0xffffffffu, ymin, o);
+    xmax = a > xmax ? a : xmax;
+    xmin = b < xmin ? b : xmin;
+    ymax = c > ymax ? c : ymax;
+    ymin = d < ymin ? d : ymin;
+  }
+  __shared__ uint64_t s[8][4];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (lane == 0) {
+    s[w][0] = xmax;
+    s[w][1] = xmin;
+    s[w][2] = ymax;
+    s[w][3] = ymin;
+  }
   if (__syncthreads_or(bad) && threadIdx.x == 0) set_err(st, TREE2D_ERR_BAD_INPUT);
   if (threadIdx.x == 0) {
-    Box4 r = s[0];
     for (int k = 1; k < (int)(blockDim.x >> 5); k++) {
-      r.x = fmax(r.x, s[k].x);
-      r.y = fmin(r.y, s[k].y);
-      r.z = fmax(r.z, s[k].z);
-      r.w = fmin(r.w, s[k].w);
+      xmax = s[k][0] > xmax ? s[k][0] : xmax;
+      xmin = s[k][1] < xmin ? s[k][1] : xmin;
+      ymax = s[k][2] > ymax ? s[k][2] : ymax;
+      ymin = s[k][3] < ymin ? s[k][3] : ymin;
     }
-    part[blockIdx.x] = r;
+    part[blockIdx.x] = Box4{okey_inv(xmax), okey_inv(xmin), okey_inv(ymax), okey_inv(ymin)};
   }
 }
 
@@ -99,26 +123,32 @@ __device__ __forceinline__ RootBox root_from_box(const Box4 &r) {
 }
 
 // One warp: the lanes reduce strided parts, then a shuffle reduction.
-__global__ void k_root(const Box4 *part, int nparts, RootBox *root) {
-  if (blockIdx.x != 0) return;
-  const int lane = threadIdx.x & 31;
-  if (threadIdx.x >= 32) return;
-  Box4 r{-INFINITY, INFINITY, -INFINITY, INFINITY};
-  for (int k = lane; k < nparts; k += 32) {
+// The root box from the blocks' extremes: one block of kRootThreads.
+constexpr int kRootThreads = 256;
+__global__ void __launch_bounds__(kRootThreads) k_root(const Box4 *part, int nparts, RootBox *root) {
+  uint64_t e[4] = {okey(-INFINITY), okey(INFINITY), okey(-INFINITY), okey(INFINITY)};
+  for (int k = threadIdx.x; k < nparts; k += kRootThreads) {
     const Box4 p = part[k];
-    r.x = fmax(r.x, p.x);
-    r.y = fmin(r.y, p.y);
-    r.z = fmax(r.z, p.z);
-    r.w = fmin(r.w, p.w);
+    const uint64_t v[4] = {okey(p.x), okey(p.y), okey(p.z), okey(p.w)};
+#pragma unroll
+    for (int q = 0; q < 4; q++) e[q] = (q & 1) ? (v[q] < e[q] ? v[q] : e[q]) : (v[q] > e[q] ? v[q] : e[q]);
   }
-  r.x = warp_max(r.x);
-  r.y = warp_min(r.y);
-  r.z = warp_max(r.z);
-  r.w = warp_min(r.w);
-  if (lane != 0) return;
-  *root = root_from_box(r);
+  __shared__ uint64_t s[kRootThreads / 32][4];
+#pragma unroll
+  for (int q = 0; q < 4; q++) {
+    for (int o = 16; o; o >>= 1) {
+      const uint64_t a = __shfl_xor_sync(0xffffffffu, e[q], o);
+      e[q] = (q & 1) ? (a < e[q] ? a : e[q]) : (a > e[q] ? a : e[q]);
+    }
+    if ((threadIdx.x & 31) == 0) s[threadIdx.x >> 5][q] = e[q];
+  }
+  __syncthreads();
+  if (threadIdx.x != 0) return;
+  for (int w = 1; w < kRootThreads / 32; w++)
+#pragma unroll
+    for (int q = 0; q < 4; q++) e[q] = (q & 1) ? (s[w][q] < e[q] ? s[w][q] : e[q]) : (s[w][q] > e[q] ? s[w][q] : e[q]);
+  *root = root_from_box(Box4{okey_inv(e[0]), okey_inv(e[1]), okey_inv(e[2]), okey_inv(e[3])});
 }
-
 // Batched sets: blocks (set, slice) reduce slice `slice` of the set's blob
 // range [off[s], off[s+1]) to a partial box, check the inputs and write the
 // set id of each blob; k_roots_sets then forms each set's root box from its
@@ -189,18 +219,6 @@ __device__ __forceinline__ unsigned descend(double x, double y, double &cx, doub
   return q;
 }
 
-// Order-preserving map of a non-NaN double to an unsigned integer (-0 is
-// taken as +0, as the FP64 comparisons treat them): a >= b iff
-// okey(a) >= okey(b).  Lets the key descent compare on the integer pipe.
-__device__ __forceinline__ uint64_t okey(double d) {
-  uint64_t u = (uint64_t)__double_as_longlong(d);
-  if (u == 0x8000000000000000ull) u = 0;
-  return (u >> 63) ? ~u : (u | 0x8000000000000000ull);
-}
-__device__ __forceinline__ double okey_inv(uint64_t k) {
-  const uint64_t u = (k >> 63) ? (k & 0x7fffffffffffffffull) : ~k;
-  return __longlong_as_double((long long)u);
-}
 
 // Centre table of the first `lt` levels: entry (l, i) of the x
 // table is the x centre of the level-l cells in column i, formed by the
@@ -253,6 +271,34 @@ __device__ __forceinline__ uint64_t set_prefix(int set, int lev0) {
   return p;
 }
 
+// Index of the level-lt cell along one axis, from f = the position's
+// fraction of the root box along it (0..1, in the direction the index grows),
+// computed in FP32: |f - exact| < 2.5 * 2^-24 (a rounded offset from the
+// centre, a rounded reciprocal of the side, one fused multiply-add), i.e.
+// below 0.01 of a level-16 cell.  With u = f * 2^lt, the decisions of all
+// levels follow from floor(u) unless u lies within kCandEps of an integer k,
+// the split of exactly one level j (k an odd multiple of 2^(lt-1-j)); that
+// decision is read from the table -- okey >= centre for x, okey <= centre for
+// y (the reference's y >= / <= comparisons) -- and puts the cell at k or k-1.
+// Deeper splits are at least half a cell away, so no other decision moves.
+constexpr float kCandEps = 0.05f;
+
+__device__ __forceinline__ unsigned axis_index(float f, int lt, uint64_t okey_pos, const uint64_t *__restrict__ tab_axis,
+                                               bool le) {
+  const float span = (float)(1u << lt);
+  const float u = f * span;
+  const float k = rintf(u);
+  unsigned i = (unsigned)fminf(fmaxf(floorf(u), 0.f), span - 1.f);
+  if (fabsf(u - k) < kCandEps && k > 0.f && k < span) {
+    const unsigned kk = (unsigned)k;
+    const int j = lt - __ffs(kk);  // level whose split is at kk
+    const uint64_t c = __ldg(tab_axis + (1 << j) - 1 + (kk >> (lt - j)));
+    const bool upper = le ? okey_pos <= c : okey_pos >= c;
+    i = upper ? kk : kk - 1;
+  }
+  return i;
+}
+
 __global__ void __launch_bounds__(256) k_keys(const double *__restrict__ xy, int n, const RootBox *__restrict__ root,
                                               const uint64_t *__restrict__ tab, int tlev, uint64_t *__restrict__ keys,
                                               uint32_t *__restrict__ vals, int levels, const int *__restrict__ set_of,
@@ -273,15 +319,17 @@ __global__ void __launch_bounds__(256) k_keys(const double *__restrict__ xy, int
     const uint64_t xk = okey(x), yk = okey(y);
     const int lt = min(levels, tlev);
     const int ybase = (1 << tlev) - 1;
-    unsigned ix = 0, iy = 0;
-#pragma unroll 4
+    // The level-lt cell from the position's fraction of the root box, in
+    // FP32 (FP64 arithmetic is slow on this part): at most one level's
+    // decision along each axis can differ from the reference's, the one
+    // whose split passes within the FP32 error of the position; that
+    // decision alone is taken from the table (axis_index).
+    const float rinv = __frcp_rn((float)R);
+    unsigned ix = axis_index(fmaf((float)(x - cx), rinv, 0.5f), lt, xk, tab, false);
+    unsigned iy = axis_index(fmaf((float)(cy - y), rinv, 0.5f), lt, yk, tab + ybase, true);
     for (; l < lt; l++) {
-      const int off = (1 << l) - 1;
-      const unsigned bx = xk >= __ldg(tab + off + ix) ? 1u : 0u;
-      const unsigned by = yk <= __ldg(tab + ybase + off + iy) ? 1u : 0u;
-      key = (key << 2) | bx | (by << 1);
-      ix = 2 * ix + bx;
-      iy = 2 * iy + by;
+      const int sh = lt - 1 - l;
+      key = (key << 2) | ((ix >> sh) & 1u) | (((iy >> sh) & 1u) << 1);
     }
     if (l < levels) {
       // centre of the level-lt cell: its parent's centre +- a quarter side
@@ -737,7 +785,7 @@ retry:
     ::t2d::g_launches.fetch_add(2, std::memory_order_relaxed);
   } else {
     k_bbox<<<kBoxBlocks, 256, 0, s>>>(d_xy, n, bpart, ws.status);
-    k_root<<<1, 32, 0, s>>>(bpart, kBoxBlocks, t.root);
+    k_root<<<1, kRootThreads, 0, s>>>(bpart, kBoxBlocks, t.root);
     ::t2d::g_launches.fetch_add(2, std::memory_order_relaxed);
   }
   // 2. keys

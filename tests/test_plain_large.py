@@ -109,3 +109,57 @@ def test_deep_cluster_uses_full_key_depth(gpu_lib):
     torch.cuda.synchronize()
     ref = out.cpu().numpy()
     assert np.linalg.norm(uv - ref) / np.linalg.norm(ref) < 1e-5
+
+
+def _points_on_cell_edges(rng, paths=3000, levels=9):
+    """Points exactly on the reference's cell centres (the split lines of
+    their cells) and one ulp either side, at levels 1..`levels`, inside a box
+    fixed by two corner blobs: root side 1 + 1e-4 about (0.5, 0.5), centres
+    by the reference's recursion c +- R/4, R/2 per level."""
+    pts = [np.array([[0.0, 0.0], [1.0, 1.0]])]
+    seen = set()
+    for _ in range(paths):
+        cx, cy, R = 0.5, 0.5, 1.0 + 1e-4
+        stop = int(rng.integers(1, levels + 1))
+        for _l in range(stop):
+            h = 0.25 * R
+            cx = cx + h if rng.random() < 0.5 else cx - h
+            cy = cy - h if rng.random() < 0.5 else cy + h
+            R = 0.5 * R
+        if (cx, cy) in seen:  # one cluster per centre: two could never be separated
+            continue
+        seen.add((cx, cy))
+        for dx in (-np.inf, 0, np.inf):
+            for dy in (-np.inf, 0, np.inf):
+                x = cx if dx == 0 else np.nextafter(cx, dx)
+                y = cy if dy == 0 else np.nextafter(cy, dy)
+                pts.append(np.array([[x, y]]))
+    xy = np.concatenate(pts)
+    return xy[(xy[:, 0] >= 0) & (xy[:, 0] <= 1) & (xy[:, 1] >= 0) & (xy[:, 1] <= 1)]
+
+
+@pytest.mark.gpu
+def test_keys_on_cell_edges_match_oracle(gpu_lib):
+    """Blobs on the split lines of cells at every level and one ulp off
+    them: the key kernel's candidate cells (from the position's fraction of
+    the root box) must be corrected to the reference's own decisions, so the
+    tree equals the oracle's cell for cell."""
+    P = gpu_lib
+    rng = np.random.default_rng(29)
+    xy = np.concatenate([_points_on_cell_edges(rng), rng.random((4000, 2))])
+    n = len(xy)
+    cir = rng.standard_normal(n) / n
+    cor = np.full(n, 0.003)
+    # leaves of up to 9 blobs: each 3x3 cluster about a centre is split by
+    # that centre's lines when it shares a cell with anything else
+    P.set_params(9, 10, 0.5)
+    P.set_mode(P.MODE_PLAIN)
+    P.make_tree(xy, cir, cor)
+    d = P.export_tree(n, 9)
+    O = oracle()
+    o = O.Oracle(9, 10, 0.5)
+    o.make_tree(xy, cir, cor)
+    od = o.dump(n)
+    assert np.array_equal(d["perm"], od["perm"])
+    assert np.array_equal(d["level"], od["level"]) and np.array_equal(d["begin"], od["begin"])
+    assert np.array_equal(d["cx"].view(np.uint64), od["cx"].view(np.uint64))
