@@ -48,6 +48,8 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--mode", default="learned", choices=list(MODES))
     ap.add_argument("--weights", default=None, help="learned form: weights file (default: the packaged ones)")
+    ap.add_argument("--direct-bias", type=float, default=1.0, help="learned form: logit bias towards direct evaluation")
+    ap.add_argument("--order-margin", type=int, default=1, help="learned form: orders added to the network's choice")
     ap.add_argument("--pterms", type=int, default=16, help="mixed form: expansion length")
     ap.add_argument("--cutoff", type=float, default=2.5, help="mixed form: correction radius / max sigma")
     ap.add_argument("--cuda-core-m2l", action="store_true", help="mixed form: M2L on CUDA cores")
@@ -347,6 +349,7 @@ def run_ours(args):
             learned_note = f"none found at {os.path.relpath(path, ROOT)}: fixed mixed form (the fallback)"
         else:
             P.learn_set_weights(theta)
+            P.learn_set_options(args.direct_bias, args.order_margin)
             envelope, env_cutoff = L.load_envelope(path)
             P.learn_set_envelope(envelope, env_cutoff)
             learned_note = (f"{os.path.relpath(path, ROOT)} (trained on configuration-5 steps 0-20 by "
