@@ -146,9 +146,12 @@ __global__ void __launch_bounds__(kThreadsTC) k_m2l_tc(TcArgs a) {
   uint32_t phase_mma[2] = {0, 0}, phase_b[3] = {0, 0, 0};
   bool pending[2] = {false, false};
   bool b_inflight[3] = {false, false, false};  // thread 0: bulk copy issued, not yet waited for
-  // Slot chunks are spread over `ngroups` accumulators (TMEM column blocks
-  // of Npad); each accumulates few MMAs and the partial sums are added in
-  // FP32 registers at the end, which keeps the accumulation error small.
+  // Slots are spread over `ngroups` accumulators (TMEM column blocks of
+  // Npad) by slot number, slot % ngroups; each accumulates few MMAs and the
+  // partial sums are added in FP32 registers at the end, in group order,
+  // which keeps the accumulation error small.  A row's sums depend only on
+  // its own slots (a slot another row of the tile uses adds exact zeros),
+  // so the result does not depend on which cells share the tile.
   bool gfirst[8] = {true, true, true, true, true, true, true, true};
   int issued = 0;  // steps whose MMAs were committed (or attempted)
   auto slot_at = [&](unsigned rest) { return __ffs(rest) - 1; };  // lowest remaining slot
@@ -218,7 +221,7 @@ __global__ void __launch_bounds__(kThreadsTC) k_m2l_tc(TcArgs a) {
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         const uint32_t ah = smem_u32(astage + (size_t)ast * 2 * a_bytes), al = ah + a_bytes;
         const uint32_t bh = smem_u32(bstage + (size_t)bs * 2 * b_bytes), bl = bh + b_bytes;
-        const int g = i % a.ngroups;
+        const int g = slot % a.ngroups;
         const uint32_t dcol = tmem + (uint32_t)(g * Npad);
         for (int t = 0; t < Kc / 8; t++) {
           const uint32_t ko = (uint32_t)t * 2 * lbo;
@@ -286,12 +289,14 @@ __global__ void __launch_bounds__(kThreadsTC) k_m2l_tc(TcArgs a) {
     // not added; 32 accumulator columns per TMEM load.
     const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16);
     float *dst = valid ? m.L + (size_t)cell * 2 * P : nullptr;
-    const int used = issued < a.ngroups ? issued : a.ngroups;
+    unsigned gmask = 0u;  // groups that received MMAs
+    for (unsigned r = mask; r; r &= r - 1) gmask |= 1u << ((__ffs(r) - 1) % a.ngroups);
     for (int c0 = 0; c0 < 2 * P; c0 += 32) {
       float acc[32];
 #pragma unroll
       for (int j = 0; j < 32; j++) acc[j] = 0.f;
-      for (int g = 0; g < used; g++) {
+      for (int g = 0; g < a.ngroups; g++) {
+        if (!((gmask >> g) & 1u)) continue;
         uint32_t r[32];
         tmem_ld32(taddr + (uint32_t)(g * Npad + c0), r);
         tmem_wait();
@@ -325,7 +330,7 @@ __global__ void __launch_bounds__(kThreadsTC) k_m2l_tc(TcArgs a) {
 }
 
 // Cells of level >= 2 (below their set root), grouped by child class (order within a class is
-// irrelevant: every row's sum is its own).
+// irrelevant: every row's sum is its own, k_m2l_tc).
 // One atomic per warp and class (the lanes of a class take consecutive
 // positions in ballot order).
 __global__ void k_class_lists(MixedView m, int *list, int *count) {

@@ -159,3 +159,41 @@ def test_one_walk_lists_equal_two_walk_lists(gpu_lib):
     assert st_a["n_list_k"] / st_a["n_leaves"] > 100
     assert np.array_equal(uv_a, uv_b) and st_a["n_pairs"] == st_b["n_pairs"]
     P.set_mode(P.MODE_PLAIN)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("mode", ["mixed", "learned"])
+def test_repeated_solves_bit_identical(gpu_lib, mode):
+    """Two solves of the same 1M-blob set give the same velocities bit for
+    bit: no result depends on the order in which atomics placed cells in the
+    M2L class lists (each row's accumulator groups follow its own slots)."""
+    torch = pytest.importorskip("torch")
+    import importlib
+    P = gpu_lib
+    W = importlib.import_module("2dfmm_gb300.workloads")
+    L = importlib.import_module("2dfmm_gb300.learn")
+    b = W.two_patch_sheet(1_048_576, seed=31)
+    P.set_params(b.nterms, b.num_p, b.theta)
+    P.set_mixed_params(16, 2.5, True)
+    if mode == "learned":
+        theta = L.load_weights()
+        if theta is None:
+            pytest.skip("no packaged weights")
+        P.learn_set_weights(theta)
+        P.learn_set_envelope(*L.load_envelope())
+    P.set_mode(P.MODE_LEARNED if mode == "learned" else P.MODE_MIXED)
+    dev = torch.device("cuda:0")
+    xy = torch.from_numpy(b.xy).to(dev)
+    cir = torch.from_numpy(b.cir).to(dev)
+    cor = torch.from_numpy(b.cor).to(dev)
+    outs = []
+    try:
+        for _ in range(3):
+            uv = torch.empty_like(xy)
+            P.solve_device(xy.data_ptr(), cir.data_ptr(), cor.data_ptr(), uv.data_ptr(), b.n)
+            torch.cuda.synchronize()
+            outs.append(uv.cpu().numpy())
+        assert np.array_equal(outs[1], outs[0]) and np.array_equal(outs[2], outs[0])
+    finally:
+        P.learn_set_envelope(0.0)
+        P.set_mode(P.MODE_PLAIN)
