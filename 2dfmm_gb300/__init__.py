@@ -30,7 +30,7 @@ MODE_PLAIN, MODE_MIXED, MODE_LEARNED = 0, 1, 2
 # Every symbol include/tree2d.h declares.
 EXPORTS = [
     "make_tree", "biot_tree", "tree2d_last_error", "tree2d_error_string", "tree2d_set_params",
-    "tree2d_clear_params", "tree2d_get_params", "tree2d_set_mode", "tree2d_get_mode", "tree2d_set_mixed_params", "biot_tree_batch",
+    "tree2d_clear_params", "tree2d_get_params", "tree2d_set_mode", "tree2d_get_mode", "tree2d_set_mixed_params", "tree2d_set_mixed_leaf", "biot_tree_batch",
     "tree2d_solve_device", "tree2d_solve_device_static", "tree2d_solve_sets", "tree2d_set_tuning", "tree2d_get_stats", "tree2d_export_tree", "tree2d_direct_device", "tree2d_fp64_probe", "tree2d_pipe_probe", "tree2d_wait_probe", "tree2d_version",
     "tree2d_learn_param_count", "tree2d_learn_set_weights", "tree2d_learn_set_envelope", "tree2d_learn_get_weights", "tree2d_learn_set_options",
     "tree2d_learn_collect", "tree2d_learn_train", "tree2d_mlp_grad", "tree2d_mlp_forward",
@@ -52,6 +52,7 @@ class Stats(ctypes.Structure):
         ("ms_upward", ctypes.c_double), ("ms_eval", ctypes.c_double), ("ms_total", ctypes.c_double),
         ("n_launches", ctypes.c_longlong), ("m2l_path", ctypes.c_int), ("eval_variant", ctypes.c_int),
         ("learned_active", ctypes.c_int), ("n_list_u", ctypes.c_longlong), ("n_list_k", ctypes.c_longlong),
+        ("leaf_blobs", ctypes.c_int), ("n_list_k_blobs", ctypes.c_longlong),
     ]
 
     def as_dict(self):
@@ -94,6 +95,8 @@ def load(path: str | None = None):
     L.tree2d_get_mode.restype = ctypes.c_int
     L.tree2d_set_mixed_params.argtypes = [ctypes.c_int, ctypes.c_double, ctypes.c_int]
     L.tree2d_set_mixed_params.restype = ctypes.c_int
+    L.tree2d_set_mixed_leaf.argtypes = [ctypes.c_int]
+    L.tree2d_set_mixed_leaf.restype = ctypes.c_int
     L.biot_tree_batch.argtypes = [ctypes.c_int, _dp, _dp]
     L.biot_tree_batch.restype = ctypes.c_int
     L.tree2d_solve_device.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
@@ -187,6 +190,12 @@ def set_mode(mode: int):
 
 def set_mixed_params(pterms: int = 16, cutoff_sigmas: float = 2.5, use_tensor_cores: bool = True):
     _check(load().tree2d_set_mixed_params(pterms, cutoff_sigmas, int(use_tensor_cores)), "set_mixed_params")
+
+
+def set_mixed_leaf(max_blobs: int = -1):
+    """Most blobs per leaf of the mixed forms' tree: -1 by set size (64 /
+    96 / 128 from 512K / 2M blobs), 0 the parameters' num_p - 1, > 0 fixed."""
+    _check(load().tree2d_set_mixed_leaf(max_blobs), "set_mixed_leaf")
 
 
 def get_mode() -> int:
@@ -346,11 +355,12 @@ def learn_set_options(direct_bias: float = 1.0, order_margin: int = 1, budget: f
     _check(load().tree2d_learn_set_options(direct_bias, order_margin, budget), "learn_set_options")
 
 
-def learn_set_envelope(k_per_leaf_max: float, cutoff_sigmas: float = 0.0):
-    """Training envelope: the largest mean K-list entries per leaf the
-    network was trained on, counted at correction radius `cutoff_sigmas`
-    (0: the radius in force); denser solves run the fixed mixed form."""
-    _check(load().tree2d_learn_set_envelope(k_per_leaf_max, cutoff_sigmas), "learn_set_envelope")
+def learn_set_envelope(k_blobs_per_leaf_max: float, cutoff_sigmas: float = 0.0):
+    """Training envelope: the largest mean number of source blobs in a
+    leaf's K-list leaves that the network was trained on, counted at
+    correction radius `cutoff_sigmas` (0: the radius in force); denser
+    solves run the fixed mixed form."""
+    _check(load().tree2d_learn_set_envelope(k_blobs_per_leaf_max, cutoff_sigmas), "learn_set_envelope")
 
 
 def learn_collect(max_samples: int, seed: int = 0):

@@ -283,7 +283,11 @@ int solve_body(Lib &L, Solver &S, int n, const double *d_xy, const double *d_cir
   Workspace &ws = S.ws;
   const long long launches0 = g_launches.load();
   T2D_CUDA_TRY(cudaEventRecord(ws.ev[0], s));
-  int rc = build_tree(ws, n, d_xy, d_cir, d_cor, L.params, S.tree, s, d_set_off, nsets, cir_cor_ready);
+  // the mixed forms build their own leaf size (the plain form the reference's)
+  Params bp = L.params;
+  if (L.mode != TREE2D_MODE_PLAIN) bp.num_p = mixed_leaf_blobs(L.mixed, n / (nsets > 0 ? nsets : 1), L.params.num_p) + 1;
+  st.leaf_blobs = bp.num_p - 1;
+  int rc = build_tree(ws, n, d_xy, d_cir, d_cor, bp, S.tree, s, d_set_off, nsets, cir_cor_ready);
   if (rc) return rc;
   T2D_CUDA_TRY(cudaEventRecord(ws.ev[1], s));
   S.plain_coef = false;
@@ -782,6 +786,14 @@ int tree2d_set_tuning(int autotune, int eval_variant) {
   return TREE2D_OK;
 }
 
+int tree2d_set_mixed_leaf(int max_blobs) {
+  Lib &L = lib();
+  std::lock_guard<std::mutex> lk(L.mu);
+  if (max_blobs < -1 || max_blobs > 65535) return fail(TREE2D_ERR_BAD_PARAMS);
+  L.mixed.leaf_blobs = max_blobs;
+  return TREE2D_OK;
+}
+
 int tree2d_set_mixed_params(int pterms, double cutoff_sigmas, int use_tensor_cores) {
   Lib &L = lib();
   std::lock_guard<std::mutex> lk(L.mu);
@@ -975,13 +987,13 @@ int tree2d_learn_set_options(float direct_bias, int order_margin, double budget)
   return TREE2D_OK;
 }
 
-int tree2d_learn_set_envelope(double k_per_leaf_max, double cutoff_sigmas) {
+int tree2d_learn_set_envelope(double k_blobs_per_leaf_max, double cutoff_sigmas) {
   Lib &L = lib();
   std::lock_guard<std::mutex> lk(L.mu);
-  if (!(k_per_leaf_max >= 0.0) || !std::isfinite(k_per_leaf_max)) return fail(TREE2D_ERR_BAD_PARAMS);
+  if (!(k_blobs_per_leaf_max >= 0.0) || !std::isfinite(k_blobs_per_leaf_max)) return fail(TREE2D_ERR_BAD_PARAMS);
   if (!(cutoff_sigmas >= 0.0) || !std::isfinite(cutoff_sigmas) || cutoff_sigmas > 64.0)
     return fail(TREE2D_ERR_BAD_PARAMS);
-  L.lp->k_per_leaf_max = k_per_leaf_max;
+  L.lp->k_blobs_max = k_blobs_per_leaf_max;
   L.lp->cutoff_train = cutoff_sigmas;
   return TREE2D_OK;
 }

@@ -44,7 +44,21 @@ struct MixedParams {
   long lp_version = 0;
   int autotune = 1;       // time the near-field variants on a new size class
   int eval_variant = -1;  // >= 0: force this near-field variant
+  int leaf_blobs = -1;    // most blobs per leaf of the mixed forms' tree: -1 by set size
+                          // (mixed_leaf_blobs), 0 the parameters' num_p - 1, > 0 this
 };
+
+// Most blobs per leaf of the tree the mixed forms build (the plain form keeps
+// the parameters' num_p - 1, the reference's).  By set size (n_set blobs per
+// set): a leaf's near field grows with its size while the per-leaf work (lists,
+// decisions, expansions, M2L) shrinks, and in larger, denser sets more of each
+// leaf's list is correction entries, so larger leaves pay: 64 below 512K
+// blobs, 96 below 2M, 128 from 2M.
+inline int mixed_leaf_blobs(const MixedParams &mp, long n_set, int num_p) {
+  if (mp.leaf_blobs > 0) return mp.leaf_blobs;
+  if (mp.leaf_blobs == 0) return num_p - 1;
+  return n_set < (512l << 10) ? 64 : (n_set < (2l << 20) ? 96 : 128);
+}
 
 // Root box, written on the device (quadtree.c:81-99 semantics).
 struct RootBox {
@@ -63,7 +77,7 @@ struct DevStatus {
   int deeper;              // build: keys of kShortKeyLevels levels do not suffice
   int list_overflow;       // mixed: a leaf's lists did not fit the one-walk scratch
   int list_max;            // mixed: most list entries (U + W + K) of one leaf
-  unsigned long long k_env;  // mixed: leaves beyond the correction radius but within the walk radius
+  unsigned long long k_blobs;  // mixed: source blobs of the K leaves of all leaves, out to the walk radius
 };
 
 // Bump allocator over one device allocation.  Buffers are 256-byte aligned.

@@ -25,7 +25,7 @@ struct LearnedParams {
   float direct_bias = 1.0f;  // added to the direct logit: leans towards exact evaluation
   int order_margin = 1;      // chosen order raised by this much (capped at 16)
   double budget = 3e-7;      // label budget: per-interaction error / (sum|G| / R0)
-  double k_per_leaf_max = 0; // training envelope (mean K entries per leaf); 0 = none
+  double k_blobs_max = 0;    // training envelope: mean source blobs of the K leaves per leaf; 0 = none
   double cutoff_train = 0;   // correction radius (units of max sigma) the envelope was counted at; 0 = the one in force
 };
 

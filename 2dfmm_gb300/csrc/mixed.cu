@@ -363,10 +363,11 @@ __device__ __forceinline__ float box_gap(const MixedView &m, int a, int b) {
 //      but whose parent is;
 //   K: leaves not adjacent to B whose box lies within rc of B's box (the
 //      blob-core correction).  The correction walk descends to the walk
-//      radius walk_scale * rc: the counting passes also count the
-//      non-adjacent leaves between rc and that radius (the learned form's
-//      training envelope is a K-list density at a larger radius); every
-//      pass walks the same cells, so the lists keep one emission order.
+//      radius walk_scale * rc, and the counting passes add up the source
+//      blobs of the non-adjacent leaves out to that radius (st->k_blobs:
+//      the learned form's training envelope is a K-list density, counted
+//      at the training radius); every pass walks the same cells, so the
+//      lists keep one emission order.
 // The walk keeps one stack per warp in shared memory; every round pops up
 // to 8 cells and lane (entry, quadrant) classifies one child, so a leaf's
 // lists take tens of rounds instead of hundreds of serial steps.  Stack
@@ -405,7 +406,7 @@ __global__ void __launch_bounds__(32 * kWalkWarps) k_lists(MixedView m) {
     rc = m.rc_set[(ty >> 1) * (1u << (m.lev0 - 1)) + (tx >> 1)];
   }
   const float rw = rc * m.walk_scale;
-  unsigned env = 0;  // this lane's leaves in [rc, rw)
+  unsigned long long kb = 0;  // this lane's K-leaf source blobs out to rw
   int base[3] = {0, 0, 0};
   if (kFill) {
     base[0] = m.u_off[l];
@@ -473,10 +474,8 @@ __global__ void __launch_bounds__(32 * kWalkWarps) k_lists(MixedView m) {
           if (g < rw) {
             if (m.leaf[cc]) {
               if (!adj_cells(m, cc, b)) {
-                if (g < rc)
-                  kind = 2;
-                else
-                  env++;
+                if (g < rc) kind = 2;
+                if (!kFill) kb += (unsigned long long)(m.end[cc] - m.begin[cc]);
               }
             } else {
               grow = true;
@@ -503,9 +502,9 @@ __global__ void __launch_bounds__(32 * kWalkWarps) k_lists(MixedView m) {
     push(grow, gv);
     __syncwarp();
   }
-  if (!kFill && m.walk_scale > 1.f) {
-    for (int o = 16; o; o >>= 1) env += __shfl_xor_sync(0xffffffffu, env, o);
-    if (lane == 0 && env) atomicAdd(&m.st->k_env, (unsigned long long)env);
+  if (!kFill) {
+    for (int o = 16; o; o >>= 1) kb += __shfl_xor_sync(0xffffffffu, kb, o);
+    if (lane == 0 && kb) atomicAdd(&m.st->k_blobs, kb);
   }
   if (!kFill && lane == 0) {
     m.u_off[l] = base[0];
@@ -1473,7 +1472,7 @@ int mixed_solve(Workspace &ws, const Tree &t, const MixedParams &mp, double *d_u
   // the learned form's envelope counts K entries at the radius its network
   // was trained with; when that is larger than the one in force, the
   // correction walk goes out to it and counts the extra leaves
-  const bool envelope_walk = mp.learned && mp.lp && mp.lp->have_weights && mp.lp->k_per_leaf_max > 0.0 &&
+  const bool envelope_walk = mp.learned && mp.lp && mp.lp->have_weights && mp.lp->k_blobs_max > 0.0 &&
                              mp.lp->cutoff_train > mp.cutoff && t.lev0 == 0;
   m.walk_scale = envelope_walk ? (float)(mp.lp->cutoff_train / mp.cutoff) : 1.f;
   m.m2m = reinterpret_cast<const float2 *>(dm2m);
@@ -1538,14 +1537,16 @@ int mixed_solve(Workspace &ws, const Tree &t, const MixedParams &mp, double *d_u
   // reference scale u_ref is one per tree.
   // the network decides only inside its training envelope: denser lists
   // than it was trained on would add up more accepted errors per target
-  // than its per-interaction budget allows for (K entries counted out to
-  // the training radius)
-  const double k_env = (double)tot[2] + (double)ws.h_status->k_env;
-  const bool in_envelope = mp.lp && (mp.lp->k_per_leaf_max <= 0.0 || k_env <= mp.lp->k_per_leaf_max * nl);
+  // than its per-interaction budget allows for.  The density is the K
+  // leaves' source blobs per leaf, counted out to the training radius: it
+  // does not depend on the leaf size, which a count of entries would.
+  const double k_blobs = (double)ws.h_status->k_blobs;
+  const bool in_envelope = mp.lp && (mp.lp->k_blobs_max <= 0.0 || k_blobs <= mp.lp->k_blobs_max * nl);
   const bool learned = mp.learned && mp.lp && mp.lp->have_weights && t.lev0 == 0 && in_envelope;
   st.learned_active = learned ? 1 : 0;
   st.n_list_u = tot[0];
   st.n_list_k = tot[2];
+  st.n_list_k_blobs = (long long)ws.h_status->k_blobs;
   unsigned char *u_dec = nullptr, *k_dec = nullptr;
   const bool side = (learned || mp.learned) && t.lev0 == 0;
   // after the fork, an early return first waits for the second stream, so

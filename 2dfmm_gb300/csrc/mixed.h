@@ -15,7 +15,7 @@ struct MixedView {
   const float *rc_ptr;  // device: cutoff radius of the regularisation correction
   const float *rc_set;  // batched sets: cutoff radius per set (else null)
   float walk_scale;     // correction walk radius / rc (>= 1): the counting walks also count
-                        // the leaves between rc and walk_scale * rc (into st->k_env)
+                        // the leaves between rc and walk_scale * rc (their blobs, into st->k_blobs)
   int lev0;             // batched sets: levels of container cells above the set roots
   // from the tree
   const uint64_t *keys;

@@ -33,17 +33,24 @@ DEFAULT_WEIGHTS = os.path.join(HERE, "data", "learned_weights.npz")
 # are much denser than the training solves' needs more accuracy per
 # interaction than the network learned to keep.  The library therefore
 # applies the decisions only up to ENVELOPE_FACTOR x the training solves'
-# largest mean K-list length per leaf and runs the fixed mixed form beyond.
-# Measured with the packaged network (trained at 45.5 K entries per leaf) on
-# the two-patch + sheet distribution: 103.7 per leaf (2.3x, 4M blobs,
-# configuration 3) gives relL2 7.7e-7; 136 (3.0x, 8M) 1.14e-6; 354 (7.8x,
-# 16M) 2.3e-6, while the fixed mixed form stays at 4.7-5.1e-7 throughout.
+# largest mean K-list density and runs the fixed mixed form beyond.  The
+# density is the source blobs of a leaf's K-list leaves (n_list_k_blobs per
+# leaf), counted out to the training correction radius: a count of entries
+# would change with the leaf size.  Measured with the packaged network on
+# the two-patch + sheet distribution, as multiples of the training density:
+# 4M blobs (configuration 3) at 64- and 128-blob leaves run at relL2 7.7e-7
+# and 5.1e-7; 8M at 64 and 128 give 1.14e-6 and 1.04e-6 (the fixed mixed
+# form stays at 4.7-5.3e-7 throughout).  The multiples are in the design
+# notes.
 ENVELOPE_FACTOR = 2.5
+ENVELOPE_LEAF_BLOBS = 64   # leaf size of the training solves (configuration 5, num_p 65)
 
 
-def save_weights(path, theta, meta, k_per_leaf_train=None, cutoff_train=None):
+def save_weights(path, theta, meta, k_blobs_per_leaf_train=None, cutoff_train=None, extra=None):
     os.makedirs(os.path.dirname(os.path.abspath(path)), exist_ok=True)
-    extra = {} if k_per_leaf_train is None else {"k_per_leaf_train": np.float64(k_per_leaf_train)}
+    extra = dict(extra or {})
+    if k_blobs_per_leaf_train is not None:
+        extra["k_blobs_per_leaf_train"] = np.float64(k_blobs_per_leaf_train)
     if cutoff_train is not None:
         extra["cutoff_train"] = np.float64(cutoff_train)
     np.savez(path, version=WEIGHTS_VERSION, theta=np.asarray(theta, np.float32), meta=json.dumps(meta), **extra)
@@ -60,19 +67,18 @@ def load_weights(path=DEFAULT_WEIGHTS):
 
 
 def load_envelope(path=DEFAULT_WEIGHTS):
-    """(K-list entries per leaf up to which the network's decisions apply,
-    correction radius they are counted at): ENVELOPE_FACTOR x the training
-    solves' largest mean, at the training radius (3.0 max sigma for files
-    that do not record it); (0, 0) = no limit, for a weights file without
-    the training figure.  The pair is the argument list of
-    learn_set_envelope."""
+    """(K-list source blobs per leaf up to which the network's decisions
+    apply, correction radius they are counted at): ENVELOPE_FACTOR x the
+    training solves' largest mean, at the training radius; (0, 0) = no
+    limit, for a weights file without the training figure.  The pair is the
+    argument list of learn_set_envelope."""
     if not os.path.exists(path):
         return 0.0, 0.0
     d = np.load(path)
-    if "k_per_leaf_train" not in d.files:
+    if "k_blobs_per_leaf_train" not in d.files:
         return 0.0, 0.0
     cutoff = float(d["cutoff_train"]) if "cutoff_train" in d.files else 3.0
-    return float(d["k_per_leaf_train"]) * ENVELOPE_FACTOR, cutoff
+    return float(d["k_blobs_per_leaf_train"]) * ENVELOPE_FACTOR, cutoff
 
 
 def _dev_arrays(torch, b):
@@ -107,7 +113,8 @@ def _rel_l2(P, torch, arrays, n, idx, uv_list):
 
 
 def run(n=1_048_576, steps=100, dt=1e-3, train_until=20, samples=200_000, train_steps=2000, batch=4096,
-        lr=2e-3, score_every=10, score_targets=2048, pterms=16, cutoff=3.0, seed=0, out=None, quiet=False):
+        lr=2e-3, score_every=10, score_targets=2048, pterms=16, cutoff=3.0, seed=0, out=None, quiet=False,
+        leaf_blobs=ENVELOPE_LEAF_BLOBS):
     import torch
     P = importlib.import_module("2dfmm_gb300")
     W = importlib.import_module("2dfmm_gb300.workloads")
@@ -115,15 +122,16 @@ def run(n=1_048_576, steps=100, dt=1e-3, train_until=20, samples=200_000, train_
     b = W.lamb_oseen(n, seed=2)
     P.set_params(b.nterms, b.num_p, b.theta)
     P.set_mixed_params(pterms, cutoff, True)
+    P.set_mixed_leaf(leaf_blobs)
     per_step = int(np.ceil(samples / (train_until + 1)))
     Xs, ys = [], []
     log = {"collect": [], "score": []}
     t0 = time.time()
-    k_per_leaf = 0.0
+    k_blobs = 0.0
     for step in range(train_until + 1):
         arrays = _dev_arrays(torch, b)
         ms, st = _timed_solve(P, torch, arrays, n, P.MODE_MIXED)
-        k_per_leaf = max(k_per_leaf, st["n_list_k"] / max(1, st["n_leaves"]))
+        k_blobs = max(k_blobs, st["n_list_k_blobs"] / max(1, st["n_leaves"]))
         X, y = P.learn_collect(per_step, seed=seed * 1000 + step)
         Xs.append(X)
         ys.append(y)
@@ -138,10 +146,10 @@ def run(n=1_048_576, steps=100, dt=1e-3, train_until=20, samples=200_000, train_
     theta = P.learn_get_weights()
     hist = np.bincount(y, minlength=14).tolist()
     summary = {"samples": int(len(y)), "label_histogram": hist, "final_loss": loss, "collect_s": t_collect,
-               "train_s": t_train, "k_per_leaf_train": k_per_leaf}
+               "train_s": t_train, "k_blobs_per_leaf_train": k_blobs, "leaf_blobs": leaf_blobs}
     if out:
-        save_weights(out, theta, summary, k_per_leaf_train=k_per_leaf, cutoff_train=cutoff)
-    P.learn_set_envelope(k_per_leaf * ENVELOPE_FACTOR, cutoff)
+        save_weights(out, theta, summary, k_blobs_per_leaf_train=k_blobs, cutoff_train=cutoff)
+    P.learn_set_envelope(k_blobs * ENVELOPE_FACTOR, cutoff)
     # score steps 21..steps
     tm, tl, tp = [], [], []
     for step in range(train_until + 1, steps + 1):
@@ -178,7 +186,40 @@ def run(n=1_048_576, steps=100, dt=1e-3, train_until=20, samples=200_000, train_
         "pairs_ratio_learned_vs_mixed": float(np.mean([r["pairs_learned"] / r["pairs_mixed"] for r in log["score"]])),
     })
     P.set_mode(P.MODE_PLAIN)
+    P.set_mixed_leaf(-1)
     return summary, log
+
+
+def measure_envelope(path=DEFAULT_WEIGHTS, n=1_048_576, train_until=20, dt=1e-3, pterms=16, cutoff=3.0,
+                     leaf_blobs=ENVELOPE_LEAF_BLOBS):
+    """Records in the weights file at `path` the training solves' largest
+    mean K-list source blobs per leaf: the configuration-5 steps 0..train_until
+    that `run` collects its samples from (fixed mixed form, advected by its
+    own velocities), with the leaf size and correction radius of that
+    training.  For weights files written before the figure existed."""
+    import torch
+    P = importlib.import_module("2dfmm_gb300")
+    W = importlib.import_module("2dfmm_gb300.workloads")
+    P.load()
+    b = W.lamb_oseen(n, seed=2)
+    P.set_params(b.nterms, b.num_p, b.theta)
+    P.set_mixed_params(pterms, cutoff, True)
+    P.set_mixed_leaf(leaf_blobs)
+    k_blobs = 0.0
+    for _step in range(train_until + 1):
+        arrays = _dev_arrays(torch, b)
+        _ms, st = _timed_solve(P, torch, arrays, n, P.MODE_MIXED)
+        k_blobs = max(k_blobs, st["n_list_k_blobs"] / max(1, st["n_leaves"]))
+        b.xy = b.xy + dt * arrays[3].cpu().numpy()
+    P.set_mode(P.MODE_PLAIN)
+    P.set_mixed_leaf(-1)
+    d = dict(np.load(path))
+    meta = json.loads(str(d.pop("meta")))
+    meta["k_blobs_per_leaf_train"] = k_blobs
+    theta = d.pop("theta")
+    d.pop("version")
+    save_weights(path, theta, meta, k_blobs_per_leaf_train=k_blobs, cutoff_train=cutoff, extra=d)
+    return k_blobs
 
 
 def main():
@@ -191,7 +232,12 @@ def main():
     ap.add_argument("--score-every", type=int, default=10)
     ap.add_argument("--out", default=DEFAULT_WEIGHTS)
     ap.add_argument("--log", default=None)
+    ap.add_argument("--measure-envelope", action="store_true",
+                    help="only record the training density in the weights file at --out")
     a = ap.parse_args()
+    if a.measure_envelope:
+        print(json.dumps({"k_blobs_per_leaf_train": measure_envelope(a.out, n=a.n, train_until=a.train_until)}))
+        return
     summary, log = run(n=a.n, steps=a.steps, train_until=a.train_until, samples=a.samples,
                        train_steps=a.train_steps, score_every=a.score_every, out=a.out)
     print(json.dumps(summary), flush=True)

@@ -61,6 +61,8 @@ def parse():
     ap.add_argument("--nsets", type=int, default=512, help="batch_sets: number of independent sets")
     ap.add_argument("--set-targets", type=int, default=4096, help="batch_sets: targets per set measured against the direct sum")
     ap.add_argument("--n", type=int, default=0, help="override the blob count (exploration only)")
+    ap.add_argument("--leaf-blobs", type=int, default=-1,
+                    help="mixed/learned: most blobs per leaf (-1: by set size, 0: the configuration's num_p - 1)")
     ap.add_argument("--err-targets", type=int, default=65536)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-sample", type=int, default=0, help="targets per CPU step (0: auto)")
@@ -339,6 +341,7 @@ def run_ours(args):
     b, wname = workload(args, rank)
     P.set_params(b.nterms, b.num_p, b.theta)
     P.set_mixed_params(args.pterms, args.cutoff, not args.cuda_core_m2l)
+    P.set_mixed_leaf(args.leaf_blobs)
     P.set_tuning(args.eval_variant < 0, args.eval_variant)
     learned_note = None
     if args.mode == "learned":
@@ -353,8 +356,8 @@ def run_ours(args):
             envelope, env_cutoff = L.load_envelope(path)
             P.learn_set_envelope(envelope, env_cutoff)
             learned_note = (f"{os.path.relpath(path, ROOT)} (trained on configuration-5 steps 0-20 by "
-                            f"2dfmm_gb300/learn.py); decisions applied up to {envelope:.1f} K-list entries per "
-                            f"leaf counted at {env_cutoff:g} max sigma")
+                            f"2dfmm_gb300/learn.py); decisions applied up to {envelope:.1f} K-list source blobs "
+                            f"per leaf counted at {env_cutoff:g} max sigma")
     n = b.n
     xy = torch.from_numpy(b.xy).to(dev).contiguous()
     cir = torch.from_numpy(b.cir).to(dev)
@@ -437,6 +440,7 @@ def run_ours(args):
             "config": {"workload": wname, "n_blobs": n, "targets": "all blobs", "nterms": b.nterms,
                        "p": b.nterms - 1, "num_p": b.num_p, "theta": b.theta, "mode": args.mode,
                        "mixed_pterms": args.pterms, "cutoff_sigmas": args.cutoff,
+                       "leaf_blobs": int(st["leaf_blobs"]),
                        "parallelism": f"replicas x{world} (independent blob sets, no collective)",
                        "l2": "flushed between steps (256 MiB write); inputs 134 MB > L2"},
             "gpu_launches": int(sum(s["n_launches"] for s in sts)),
@@ -444,6 +448,7 @@ def run_ours(args):
                       "variants": "0/1 global loads, 2/3 bulk-copy staging; 4/8 warps per block"},
             "learned_active": bool(st["learned_active"]),
             "k_list_per_leaf": st["n_list_k"] / max(1, st["n_leaves"]),
+            "k_list_blobs_per_leaf": st["n_list_k_blobs"] / max(1, st["n_leaves"]),
             "e2e": {"value": world * n / e2e_t, "unit": UNIT, "h2d_bytes_per_step": n * 48,
                     "d2h_bytes_per_step": n * 16,
                     "api": "make_tree + biot_tree_batch (host buffers; the blobs go up in make_tree, "
@@ -493,6 +498,7 @@ def run_batch(args):
     sets = W.batch_sets(nsets=args.nsets, seed=4 + rank)
     b0 = sets[0]
     P.set_params(b0.nterms, b0.num_p, b0.theta)
+    P.set_mixed_leaf(args.leaf_blobs)
     P.set_mode(MODES["mixed"])
     P.set_mixed_params(args.pterms, args.cutoff, not args.cuda_core_m2l)
     P.set_tuning(args.eval_variant < 0, args.eval_variant)
@@ -594,6 +600,7 @@ def run_batch(args):
                        "set_sizes": [int(b.n) for b in sets][:4] + ["..."], "nterms": b0.nterms, "p": b0.nterms - 1,
                        "num_p": b0.num_p, "theta": b0.theta, "mode": "mixed (batched: one tree over all sets)",
                        "mixed_pterms": args.pterms, "cutoff_sigmas": args.cutoff,
+                       "leaf_blobs": int(st["leaf_blobs"]),
                        "parallelism": f"replicas x{world} (independent batches, no collective)",
                        "l2": "flushed between steps (256 MiB write)"},
             "gpu_launches": int(sum(x["n_launches"] for x in sts)),

@@ -89,6 +89,13 @@ int tree2d_get_mode(void);
  * cores (0, for checking).  Defaults 16, 2.5, 1. */
 int tree2d_set_mixed_params(int pterms, double cutoff_sigmas, int use_tensor_cores);
 
+/* Most blobs per leaf of the tree the mixed and learned forms build (the
+ * plain form always uses the parameters' num_p - 1, as the reference does):
+ * -1 (the default) chooses by the blobs per set: 64 below 524,288, 96 below
+ * 2,097,152, 128 above (a batched solve uses its mean set size); 0 uses
+ * num_p - 1; 1..65535 fixes it. */
+int tree2d_set_mixed_leaf(int max_blobs);
+
 /* Evaluates n targets (xy interleaved, host memory) into uv (interleaved,
  * host memory) against the last make_tree.  Blob positions are answered
  * from the precomputed velocities, the rest in one GPU launch.  The points
@@ -148,6 +155,10 @@ typedef struct {
                              outside the network's training envelope)   */
   long long n_list_u;     /* mixed: U (direct) list entries             */
   long long n_list_k;     /* mixed: K (correction) list entries         */
+  int leaf_blobs;         /* most blobs per leaf of the tree built        */
+  long long n_list_k_blobs; /* mixed: source blobs of the K lists, summed
+                             over the leaves; learned: out to the
+                             envelope's radius (the envelope statistic) */
 } tree2d_stats_t;
 int tree2d_get_stats(tree2d_stats_t *out);
 
@@ -218,18 +229,19 @@ int tree2d_learn_get_weights(float *theta, int n);
  * order raised by this much; budget: label tolerance per interaction in
  * units of sum|G| / root side.  Defaults 1.0, 1, 3e-7. */
 int tree2d_learn_set_options(float direct_bias, int order_margin, double budget);
-/* Training envelope of the loaded network: the largest mean number of K
- * (correction) list entries per leaf the training solves had, counted with
- * the correction radius cutoff_sigmas (units of the largest core radius; 0
- * = the radius in force).  A solve whose lists, counted at that radius, are
- * denser than this runs the fixed mixed form instead (the network's
- * per-interaction error budget does not bound the sum over more
+/* Training envelope of the loaded network: the largest mean number of
+ * source blobs in a leaf's K (correction) list leaves that the training
+ * solves had, counted with the correction radius cutoff_sigmas (units of the
+ * largest core radius; 0 = the radius in force).  A solve whose lists,
+ * counted at that radius, hold more runs the fixed mixed form instead (the
+ * network's per-interaction error budget does not bound the sum over more
  * interactions than it was trained on); tree2d_get_stats reports it in
- * learned_active.  When cutoff_sigmas is above the radius in force, the
- * list walk goes out to it to count; below it, the entries are counted at
- * the radius in force (more of them: the conservative side).
- * k_per_leaf_max 0 = no limit (the default). */
-int tree2d_learn_set_envelope(double k_per_leaf_max, double cutoff_sigmas);
+ * learned_active and the solve's own figure in n_list_k_blobs.  Blobs, not
+ * entries, make the figure independent of the leaf size.  When
+ * cutoff_sigmas is above the radius in force, the list walk goes out to it
+ * to count; below it, the blobs are counted at the radius in force (more of
+ * them: the conservative side).  0 = no limit (the default). */
+int tree2d_learn_set_envelope(double k_blobs_per_leaf_max, double cutoff_sigmas);
 /* Training data from the last tree2d_solve_device in mixed or learned mode:
  * up to max_samples interactions drawn with `seed`, their features
  * (features[max][16]) and the cheapest class whose error against the FP64

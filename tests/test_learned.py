@@ -141,13 +141,14 @@ def test_envelope_counted_at_the_training_radius(gpu_lib):
         P.learn_set_envelope(0.0)
         _, _, _, _, st30 = _solve(P, torch, b, P.MODE_MIXED, cutoff=3.0)
         uv25, _, _, _, st25 = _solve(P, torch, b, P.MODE_MIXED, cutoff=2.5)
-        k30 = st30["n_list_k"] / st30["n_leaves"]
-        k25 = st25["n_list_k"] / st25["n_leaves"]
+        k30 = st30["n_list_k_blobs"] / st30["n_leaves"]
+        k25 = st25["n_list_k_blobs"] / st25["n_leaves"]
         assert st30["n_leaves"] == st25["n_leaves"] and k25 < k30
         mid = 0.5 * (k25 + k30)
         P.learn_set_envelope(mid, 3.0)
         uv_f, _, _, _, st_f = _solve(P, torch, b, P.MODE_LEARNED, cutoff=2.5)
         assert st_f["learned_active"] == 0 and st_f["n_list_k"] == st25["n_list_k"]
+        assert st_f["n_list_k_blobs"] == st30["n_list_k_blobs"]  # counted out to 3.0
         # the fallback is the fixed mixed form at 2.5; the longer walk only
         # changes the order the correction leaves are visited in
         ref = uv25.cpu().numpy()
@@ -156,6 +157,7 @@ def test_envelope_counted_at_the_training_radius(gpu_lib):
         P.learn_set_envelope(mid, 0.0)
         _, _, _, _, st_a = _solve(P, torch, b, P.MODE_LEARNED, cutoff=2.5)
         assert st_a["learned_active"] == 1 and st_a["n_list_k"] == st25["n_list_k"]
+        assert st_a["n_list_k_blobs"] == st25["n_list_k_blobs"]  # counted at 2.5
         P.learn_set_envelope(1e9, 3.0)
         _, _, _, _, st_b = _solve(P, torch, b, P.MODE_LEARNED, cutoff=2.5)
         assert st_b["learned_active"] == 1 and st_b["n_list_k"] == st25["n_list_k"]
