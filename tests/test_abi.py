@@ -45,6 +45,12 @@ def test_param_validation(lib):
     assert lib.tree2d_set_params(11, 33, 0.5, 0.01) == 0
     assert P.get_params() == (11, 33, 0.5, 0.01)
     assert lib.tree2d_set_mode(7) == P.ERR_MODE
+    assert lib.tree2d_set_mixed_leaf(-2) == P.ERR_BAD_PARAMS
+    assert lib.tree2d_set_mixed_leaf(65536) == P.ERR_BAD_PARAMS
+    assert lib.tree2d_set_mixed_leaf(100) == 0 and lib.tree2d_set_mixed_leaf(-1) == 0
+    assert lib.tree2d_learn_set_envelope(-1.0, 3.0) == P.ERR_BAD_PARAMS
+    assert lib.tree2d_learn_set_envelope(1.0, -3.0) == P.ERR_BAD_PARAMS
+    assert lib.tree2d_learn_set_envelope(0.0, 0.0) == 0
     P.clear_params()
 
 

@@ -197,3 +197,25 @@ def test_repeated_solves_bit_identical(gpu_lib, mode):
     finally:
         P.learn_set_envelope(0.0)
         P.set_mode(P.MODE_PLAIN)
+
+
+@pytest.mark.gpu
+def test_mixed_leaf_size_rule_and_override(gpu_lib):
+    """The mixed forms build their own leaf size (64 blobs for sets below
+    524,288 by default, or the one set), the plain form the parameters'
+    num_p - 1; every choice keeps relL2 <= 1e-6."""
+    torch = pytest.importorskip("torch")
+    P = gpu_lib
+    W = workloads()
+    b = W.uniform(20_000, seed=3)  # num_p 33
+    try:
+        for leaf, want in ((-1, 64), (0, 32), (100, 100)):
+            P.set_mixed_leaf(leaf)
+            rel, _ = solve_and_measure(P, torch, b)
+            st = P.stats()
+            assert st["leaf_blobs"] == want and rel <= REL_L2, (leaf, st["leaf_blobs"], rel)
+        P.set_mode(P.MODE_PLAIN)
+        P.make_tree(b.xy, b.cir, b.cor)
+        assert P.stats()["leaf_blobs"] == 32
+    finally:
+        P.set_mixed_leaf(-1)
