@@ -56,6 +56,8 @@ def test_param_validation(lib):
 
 def test_biot_tree_without_tree_gives_nan(lib):
     P = pkg()
+    lib.make_tree(-1, None, None, None)  # a failed make_tree leaves no tree (whatever ran before)
+    assert P.last_error() != 0
     u, v = P.biot_tree(0.1, 0.2)
     assert np.isnan(u) and np.isnan(v)
     uv = P.biot_tree_batch(np.zeros((3, 2)), check=False)
