@@ -767,10 +767,11 @@ int build_tree(Workspace &ws, int n, const double *d_xy, const double *d_cir, co
 
   // Digits below the set root on the first attempt: as few as the tree is
   // likely to need (the previous tree's depth + 2, at least 16 for one set
-  // and 12 per set in a batch), so that the keys come from the centre table
-  // alone and the sort makes fewer passes.  A deeper tree is caught by the
-  // leaf-level pass and rebuilt with the full 32-digit keys.
-  const int floor_levels = batched ? 12 : 16;
+  // and 10 per set in a batch, where the set prefix takes up to 6 more), so
+  // that the keys come from the centre table alone and the sort makes fewer
+  // passes (4 of 8 bits up to 16 digits in all).  A deeper tree is caught by
+  // the leaf-level pass and rebuilt with the full 32-digit keys.
+  const int floor_levels = batched ? 10 : 16;
   int levels = ws.last_depth - lev0 + 2;
   if (levels < floor_levels) levels = floor_levels;
   if (levels > kShortKeyLevels) levels = kShortKeyLevels;
