@@ -62,49 +62,62 @@ __device__ __forceinline__ double okey_inv(uint64_t k) {
   return __longlong_as_double((long long)u);
 }
 
-// Bounding box of the positions (non-finite positions are bad input; the
-// circulations and core radii are checked where they are first read, in
-// k_gather).  The extremes are kept as order-preserving integers (okey), so
-// the comparisons run on the integer pipe, not the slow FP64 one; a block
-// writes its extremes back as doubles (-0 as +0, which compares the same).
-__global__ void __launch_bounds__(256) k_bbox(const double *__restrict__ xy, int n, Box4 *part, DevStatus *st) {
-  uint64_t xmax = okey(-INFINITY), xmin = okey(INFINITY), ymax = xmax, ymin = xmin;
-  bool bad = false;
-  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
-    const double x = xy[2 * i], y = xy[2 * i + 1];  // the caller's array: 8-byte alignment only
-    bad |= !(isfinite(x) && isfinite(y));
+// Extremes of the positions as order-preserving integers (okey), so that the
+// comparisons run on the integer pipe, not the slow FP64 one.
+struct Extremes {
+  uint64_t xmax, xmin, ymax, ymin;
+  __device__ void init() {
+    xmax = ymax = okey(-INFINITY);
+    xmin = ymin = okey(INFINITY);
+  }
+  __device__ void add(double x, double y) {
     const uint64_t kx = okey(x), ky = okey(y);
     xmax = kx > xmax ? kx : xmax;
     xmin = kx < xmin ? kx : xmin;
     ymax = ky > ymax ? ky : ymax;
     ymin = ky < ymin ? ky : ymin;
   }
-  for (int o = 16; o; o >>= 1) {
-    const uint64_t a = __shfl_xor_sync(0xffffffffu, xmax, o), b = __shfl_xor_sync(0xffffffffu, xmin, o);
-    const uint64_t c = __shfl_xor_sync(0xffffffffu, ymax, o), d = __shfl_xor_sync(0xffffffffu, ymin, o);
-    xmax = a > xmax ? a : xmax;
-    xmin = b < xmin ? b : xmin;
-    ymax = c > ymax ? c : ymax;
-    ymin = d < ymin ? d : ymin;
+  __device__ void add(const Extremes &o) {
+    xmax = o.xmax > xmax ? o.xmax : xmax;
+    xmin = o.xmin < xmin ? o.xmin : xmin;
+    ymax = o.ymax > ymax ? o.ymax : ymax;
+    ymin = o.ymin < ymin ? o.ymin : ymin;
   }
-  __shared__ uint64_t s[8][4];
-  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  if (lane == 0) {
-    s[w][0] = xmax;
-    s[w][1] = xmin;
-    s[w][2] = ymax;
-    s[w][3] = ymin;
+  // over the block (blockDim.x <= 256); the result is valid in thread 0
+  __device__ void reduce_block() {
+    for (int o = 16; o; o >>= 1) {
+      Extremes t;
+      t.xmax = __shfl_xor_sync(0xffffffffu, xmax, o);
+      t.xmin = __shfl_xor_sync(0xffffffffu, xmin, o);
+      t.ymax = __shfl_xor_sync(0xffffffffu, ymax, o);
+      t.ymin = __shfl_xor_sync(0xffffffffu, ymin, o);
+      add(t);
+    }
+    __shared__ Extremes s[8];
+    if ((threadIdx.x & 31) == 0) s[threadIdx.x >> 5] = *this;
+    __syncthreads();
+    if (threadIdx.x == 0)
+      for (int k = 1; k < (int)(blockDim.x >> 5); k++) add(s[k]);
+  }
+  // as doubles (-0 as +0, which compares the same)
+  __device__ Box4 box() const { return Box4{okey_inv(xmax), okey_inv(xmin), okey_inv(ymax), okey_inv(ymin)}; }
+};
+
+// Bounding box of the positions (non-finite positions are bad input; the
+// circulations and core radii are checked where they are first read, in
+// k_gather).
+__global__ void __launch_bounds__(256) k_bbox(const double *__restrict__ xy, int n, Box4 *part, DevStatus *st) {
+  Extremes ex;
+  ex.init();
+  bool bad = false;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+    const double x = xy[2 * i], y = xy[2 * i + 1];  // the caller's array: 8-byte alignment only
+    bad |= !(isfinite(x) && isfinite(y));
+    ex.add(x, y);
   }
   if (__syncthreads_or(bad) && threadIdx.x == 0) set_err(st, TREE2D_ERR_BAD_INPUT);
-  if (threadIdx.x == 0) {
-    for (int k = 1; k < (int)(blockDim.x >> 5); k++) {
-      xmax = s[k][0] > xmax ? s[k][0] : xmax;
-      xmin = s[k][1] < xmin ? s[k][1] : xmin;
-      ymax = s[k][2] > ymax ? s[k][2] : ymax;
-      ymin = s[k][3] < ymin ? s[k][3] : ymin;
-    }
-    part[blockIdx.x] = Box4{okey_inv(xmax), okey_inv(xmin), okey_inv(ymax), okey_inv(ymin)};
-  }
+  ex.reduce_block();
+  if (threadIdx.x == 0) part[blockIdx.x] = ex.box();
 }
 
 // Root box of a blob set from its coordinate extremes (quadtree.c:87-98).
@@ -150,48 +163,29 @@ __global__ void __launch_bounds__(kRootThreads) k_root(const Box4 *part, int npa
   *root = root_from_box(Box4{okey_inv(e[0]), okey_inv(e[1]), okey_inv(e[2]), okey_inv(e[3])});
 }
 // Batched sets: blocks (set, slice) reduce slice `slice` of the set's blob
-// range [off[s], off[s+1]) to a partial box, check the inputs and write the
-// set id of each blob; k_roots_sets then forms each set's root box from its
+// range [off[s], off[s+1]) to a partial box, check the positions and write
+// the set id of each blob; k_roots_sets then forms each set's root box from its
 // kSetSlices partials (the same formulas as a single set's).
 constexpr int kSetSlices = 16;
 
-__global__ void __launch_bounds__(256) k_bbox_sets(const double *__restrict__ xy, const double *__restrict__ cir,
-                                                   const double *__restrict__ cor, const int *__restrict__ off,
+__global__ void __launch_bounds__(256) k_bbox_sets(const double *__restrict__ xy, const int *__restrict__ off,
                                                    Box4 *part, int *set_of, DevStatus *st) {
   const int set = blockIdx.x;
   const int n0 = off[set], len = off[set + 1] - n0;
   const int per = (len + kSetSlices - 1) / kSetSlices;
   const int b = n0 + min(len, per * (int)blockIdx.y), e = n0 + min(len, per * ((int)blockIdx.y + 1));
-  double xmax = -INFINITY, xmin = INFINITY, ymax = -INFINITY, ymin = INFINITY;
+  Extremes ex;
+  ex.init();
   bool bad = false;
   for (int i = b + threadIdx.x; i < e; i += blockDim.x) {
     const double x = xy[2 * (long)i], y = xy[2 * (long)i + 1];
-    const double c = cir[i], r = cor[i];
-    bad |= !(isfinite(x) && isfinite(y) && isfinite(c)) || isnan(r);
-    xmax = fmax(xmax, x);
-    xmin = fmin(xmin, x);
-    ymax = fmax(ymax, y);
-    ymin = fmin(ymin, y);
+    bad |= !(isfinite(x) && isfinite(y));
+    ex.add(x, y);
     set_of[i] = set;
   }
-  __shared__ Box4 sh[8];
-  xmax = warp_max(xmax);
-  xmin = warp_min(xmin);
-  ymax = warp_max(ymax);
-  ymin = warp_min(ymin);
-  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  if (lane == 0) sh[w] = Box4{xmax, xmin, ymax, ymin};
   if (__syncthreads_or(bad) && threadIdx.x == 0) set_err(st, TREE2D_ERR_BAD_INPUT);
-  if (threadIdx.x == 0) {
-    Box4 r = sh[0];
-    for (int k = 1; k < (int)(blockDim.x >> 5); k++) {
-      r.x = fmax(r.x, sh[k].x);
-      r.y = fmin(r.y, sh[k].y);
-      r.z = fmax(r.z, sh[k].z);
-      r.w = fmin(r.w, sh[k].w);
-    }
-    part[(size_t)set * kSetSlices + blockIdx.y] = r;
-  }
+  ex.reduce_block();
+  if (threadIdx.x == 0) part[(size_t)set * kSetSlices + blockIdx.y] = ex.box();
 }
 
 __global__ void k_roots_sets(const Box4 *part, int nsets, RootBox *roots) {
@@ -252,6 +246,36 @@ __global__ void __launch_bounds__(256) k_centre_table(const RootBox *__restrict_
     R = __dmul_rn(0.5, R);
   }
   tab[g] = okey(c);
+}
+
+// Batched sets: the table of one set and one axis per block, built level by
+// level in shared memory.  Each entry is its parent's centre plus or minus a
+// quarter of the parent's side: the same FP64 operation, on the same operands,
+// as the last step of k_centre_table's descent, so the values are equal
+// (one operation per entry instead of one per level).
+constexpr int kSetTableLevels = 12;
+__global__ void __launch_bounds__(256) k_centre_table_sets(const RootBox *__restrict__ root,
+                                                           uint64_t *__restrict__ tab, int lt) {
+  __shared__ double c[(1 << kSetTableLevels) - 1];
+  const int per = (1 << lt) - 1;
+  const int set = blockIdx.x >> 1, axis = blockIdx.x & 1;
+  root += set;
+  tab += (size_t)set * 2 * per + (size_t)axis * per;
+  double R = root->region;
+  if (threadIdx.x == 0) c[0] = axis ? root->cy : root->cx;
+  __syncthreads();
+  for (int l = 1; l < lt; l++) {
+    const double h = __dmul_rn(0.25, R);  // R = R0 * 2^-(l-1)
+    const int off = (1 << l) - 1, poff = (1 << (l - 1)) - 1;
+    for (int i = threadIdx.x; i < (1 << l); i += blockDim.x) {
+      const double p = c[poff + (i >> 1)];
+      const bool bit = i & 1;
+      c[off + i] = axis == 0 ? (bit ? __dadd_rn(p, h) : __dsub_rn(p, h)) : (bit ? __dsub_rn(p, h) : __dadd_rn(p, h));
+    }
+    R = __dmul_rn(0.5, R);
+    __syncthreads();
+  }
+  for (int g = threadIdx.x; g < per; g += blockDim.x) tab[g] = okey(c[g]);
 }
 
 // `levels` digits, level 1 in the top two bits, zero below the last level.
@@ -780,8 +804,7 @@ retry:
 
   // 1. root box (per set)
   if (batched) {
-    k_bbox_sets<<<dim3((unsigned)nsets, kSetSlices), 256, 0, s>>>(d_xy, d_cir, d_cor, d_set_off, set_part, set_of,
-                                                                  ws.status);
+    k_bbox_sets<<<dim3((unsigned)nsets, kSetSlices), 256, 0, s>>>(d_xy, d_set_off, set_part, set_of, ws.status);
     k_roots_sets<<<(nsets + 127) / 128, 128, 0, s>>>(set_part, nsets, t.root);
     ::t2d::g_launches.fetch_add(2, std::memory_order_relaxed);
   } else {
@@ -791,8 +814,11 @@ retry:
   }
   // 2. keys
   const int total_levels = levels + lev0;
-  k_centre_table<<<dim3((unsigned)((2 * centre_entries(tlev) + 255) / 256), (unsigned)t.nsets), 256, 0, s>>>(
-      t.root, ctab, tlev);
+  if (batched && tlev <= kSetTableLevels)
+    k_centre_table_sets<<<2 * (unsigned)t.nsets, 256, 0, s>>>(t.root, ctab, tlev);
+  else
+    k_centre_table<<<dim3((unsigned)((2 * centre_entries(tlev) + 255) / 256), (unsigned)t.nsets), 256, 0, s>>>(
+        t.root, ctab, tlev);
   k_keys<<<(n + 255) / 256, 256, 0, s>>>(d_xy, n, t.root, ctab, tlev, t.keys, vals, levels, set_of, lev0);
   ::t2d::g_launches.fetch_add(2, std::memory_order_relaxed);
   // 3. sort

@@ -274,13 +274,30 @@ __global__ void __launch_bounds__(256) k_vx_lists(MixedView m) {
   if (lane == 0 && nv) atomicAdd(&m.st->n_m2l, nv);
 }
 
-// rc = cutoff * max sigma (sigma >= 0 as floats order like their bits).
+// rc = cutoff * max sigma.  |cor| is taken as the bit pattern of a
+// non-negative double, whose integer order is the value order, so the
+// largest is found on the integer pipe (not the slow FP64 one) and rounded
+// to FP32 once; the result is stored as FP32 bits (non-negative floats order
+// like their bits too, for the atomicMax).  NaN counts as 0.
+__device__ __forceinline__ unsigned long long abs_bits(double v) {
+  const unsigned long long u = (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffull;
+  return u > 0x7ff0000000000000ull ? 0ull : u;
+}
+__device__ __forceinline__ unsigned warp_max_as_float_bits(unsigned long long mx) {
+  for (int o = 16; o; o >>= 1) {
+    const unsigned long long t = __shfl_xor_sync(0xffffffffu, mx, o);
+    mx = t > mx ? t : mx;
+  }
+  return __float_as_uint((float)__longlong_as_double((long long)mx));
+}
 __global__ void k_sigma_max(const double *cor, int n, unsigned *out) {
-  float mx = 0.f;
-  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
-    mx = fmaxf(mx, (float)fabs(cor[i]));
-  for (int o = 16; o; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-  if ((threadIdx.x & 31) == 0) atomicMax(out, __float_as_uint(mx));
+  unsigned long long mx = 0;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+    const unsigned long long u = abs_bits(cor[i]);
+    mx = u > mx ? u : mx;
+  }
+  const unsigned f = warp_max_as_float_bits(mx);
+  if ((threadIdx.x & 31) == 0) atomicMax(out, f);
 }
 
 __global__ void k_cutoff(unsigned *bits, float cutoff, int count) {
@@ -291,13 +308,21 @@ __global__ void k_cutoff(unsigned *bits, float cutoff, int count) {
   reinterpret_cast<float *>(bits)[i] = isfinite(rc) ? rc : 0.f;
 }
 
-// Batched sets: max sigma of each set (one block per set, input order).
+// Batched sets: max sigma of each set, blocks (set, slice) over slice
+// `slice` of the set's input range.
+constexpr int kSigmaSlices = 16;
 __global__ void k_sigma_max_sets(const double *cor, const int *off, unsigned *out) {
   const int set = blockIdx.x;
-  float mx = 0.f;
-  for (int i = off[set] + threadIdx.x; i < off[set + 1]; i += blockDim.x) mx = fmaxf(mx, (float)fabs(cor[i]));
-  for (int o = 16; o; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-  if ((threadIdx.x & 31) == 0) atomicMax(out + set, __float_as_uint(mx));
+  const int n0 = off[set], len = off[set + 1] - n0;
+  const int per = (len + kSigmaSlices - 1) / kSigmaSlices;
+  const int b = n0 + min(len, per * (int)blockIdx.y), e = n0 + min(len, per * ((int)blockIdx.y + 1));
+  unsigned long long mx = 0;
+  for (int i = b + threadIdx.x; i < e; i += blockDim.x) {
+    const unsigned long long u = abs_bits(cor[i]);
+    mx = u > mx ? u : mx;
+  }
+  const unsigned f = warp_max_as_float_bits(mx);
+  if ((threadIdx.x & 31) == 0) atomicMax(out + set, f);
 }
 
 // Cells grouped by level (a counting sort), so that the per-level
@@ -1485,7 +1510,7 @@ int mixed_solve(Workspace &ws, const Tree &t, const MixedParams &mp, double *d_u
   g_launches.fetch_add(2, std::memory_order_relaxed);
   if (rc_set_bits) {
     T2D_CUDA_TRY(cudaMemsetAsync(rc_set_bits, 0, 4 * (size_t)t.nsets, s));
-    k_sigma_max_sets<<<t.nsets, 256, 0, s>>>(t.set_cor, t.set_off, rc_set_bits);
+    k_sigma_max_sets<<<dim3((unsigned)t.nsets, kSigmaSlices), 256, 0, s>>>(t.set_cor, t.set_off, rc_set_bits);
     k_cutoff<<<(t.nsets + 255) / 256, 256, 0, s>>>(rc_set_bits, (float)mp.cutoff, t.nsets);
     g_launches.fetch_add(2, std::memory_order_relaxed);
   }
