@@ -231,6 +231,8 @@ def main():
     ap.add_argument("--train-steps", type=int, default=2000)
     ap.add_argument("--score-every", type=int, default=10)
     ap.add_argument("--out", default=DEFAULT_WEIGHTS)
+    ap.add_argument("--leaf-blobs", type=int, default=ENVELOPE_LEAF_BLOBS, help="leaf size of the training solves")
+    ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--log", default=None)
     ap.add_argument("--measure-envelope", action="store_true",
                     help="only record the training density in the weights file at --out")
@@ -239,7 +241,8 @@ def main():
         print(json.dumps({"k_blobs_per_leaf_train": measure_envelope(a.out, n=a.n, train_until=a.train_until)}))
         return
     summary, log = run(n=a.n, steps=a.steps, train_until=a.train_until, samples=a.samples,
-                       train_steps=a.train_steps, score_every=a.score_every, out=a.out)
+                       train_steps=a.train_steps, score_every=a.score_every, out=a.out, seed=a.seed,
+                       leaf_blobs=a.leaf_blobs)
     print(json.dumps(summary), flush=True)
     if a.log:
         with open(a.log, "w") as f:
