@@ -939,7 +939,7 @@ struct Decisions {
 // sum the current one.  Leaves larger than a stage buffer, and every leaf
 // after a wait that gave up (recorded as TREE2D_ERR_TIMEOUT), are read from
 // global memory instead, so the result never depends on the staging.
-constexpr int kStage = 64;  // blobs per stage buffer
+constexpr int kStage = 128;  // blobs per stage buffer: the largest leaf of the default leaf sizes
 constexpr long kEvalWaitLimit = 1l << 22;  // polls; a healthy copy lands within microseconds
 
 template <bool kLearned, int kWarps>
