@@ -53,6 +53,8 @@ cudaError_t workspace_init(Workspace &ws) {
   if (e != cudaSuccess) return e;
   e = cudaMallocHost(reinterpret_cast<void **>(&ws.h_status), 4096);
   if (e != cudaSuccess) return e;
+  e = cudaMallocHost(reinterpret_cast<void **>(&ws.h_levels), sizeof(int) * (kKeyLevels + 2));
+  if (e != cudaSuccess) return e;
   for (auto &ev : ws.ev) {
     e = cudaEventCreate(&ev);
     if (e != cudaSuccess) return e;

@@ -163,6 +163,7 @@ struct Workspace {
   int list_cap = 256;  // entries per leaf of the one-walk list scratch (from the last solve)
   DevStatus *status = nullptr;   // device
   DevStatus *h_status = nullptr; // pinned host mirror
+  int *h_levels = nullptr;        // pinned: the mixed form's per-level cell offsets (kKeyLevels + 2)
   cudaEvent_t ev[8] = {};
   cudaStream_t side = nullptr;    // second stream (learned decisions beside the expansions)
   cudaEvent_t fork_ev = nullptr, join_ev = nullptr;

@@ -1286,24 +1286,32 @@ int mixed_leaf_setup(MixedView &m, const Tree &t, cudaStream_t s) {
   return TREE2D_OK;
 }
 
-int mixed_upward(MixedView &m, int depth, cudaStream_t s) {
+// Blocks of 8 warps for a per-level pass over cnt cells (one warp per cell,
+// grid-stride beyond 8 blocks per SM): a level of few cells gets few blocks.
+static int level_blocks(const int *lev_off, int lev) {
+  const int full = 152 * 8;
+  if (!lev_off) return full;
+  const int cnt = lev_off[lev + 1] - lev_off[lev];
+  const int b = (cnt + 7) / 8;
+  return b < 1 ? 1 : (b > full ? full : b);
+}
+
+int mixed_upward(MixedView &m, int depth, const int *lev_off, cudaStream_t s) {
   k_s2m_f32<<<(int)(((long)m.nleaf * 32 + 255) / 256), 256, 0, s>>>(m);
   g_launches.fetch_add(1, std::memory_order_relaxed);
-  const int blocks = 152 * 8;
   for (int lev = depth - 1; lev >= 2 + m.lev0; lev--) {
-    k_m2m_f32<<<blocks, 256, 0, s>>>(m, lev);
+    k_m2m_f32<<<level_blocks(lev_off, lev), 256, 0, s>>>(m, lev);
     g_launches.fetch_add(1, std::memory_order_relaxed);
   }
   T2D_CUDA_TRY(cudaGetLastError());
   return TREE2D_OK;
 }
 
-int mixed_downward(MixedView &m, int depth, cudaStream_t s) {
+int mixed_downward(MixedView &m, int depth, const int *lev_off, cudaStream_t s) {
   k_p2l<<<(int)(((long)m.ncell * 32 + 255) / 256), 256, 0, s>>>(m);
   g_launches.fetch_add(1, std::memory_order_relaxed);
-  const int blocks = 152 * 8;
   for (int lev = 3 + m.lev0; lev <= depth; lev++) {
-    k_l2l_f32<<<blocks, 256, 0, s>>>(m, lev);
+    k_l2l_f32<<<level_blocks(lev_off, lev - 1), 256, 0, s>>>(m, lev);
     g_launches.fetch_add(1, std::memory_order_relaxed);
   }
   T2D_CUDA_TRY(cudaGetLastError());
@@ -1524,6 +1532,8 @@ int mixed_solve(Workspace &ws, const Tree &t, const MixedParams &mp, double *d_u
   T2D_CUDA_TRY(cudaMemcpyAsync(&tot[1], m.w_off + nl, 4, cudaMemcpyDeviceToHost, s));
   T2D_CUDA_TRY(cudaMemcpyAsync(&tot[2], m.k_off + nl, 4, cudaMemcpyDeviceToHost, s));
   T2D_CUDA_TRY(cudaMemcpyAsync(ws.h_status, ws.status, sizeof(DevStatus), cudaMemcpyDeviceToHost, s));
+  if (ws.h_levels)
+    T2D_CUDA_TRY(cudaMemcpyAsync(ws.h_levels, m.level_off, sizeof(int) * (kKeyLevels + 2), cudaMemcpyDeviceToHost, s));
   T2D_CUDA_TRY(cudaStreamSynchronize(s));
   const bool from_scratch = one_walk && !ws.h_status->list_overflow;
   {
@@ -1639,13 +1649,13 @@ int mixed_solve(Workspace &ws, const Tree &t, const MixedParams &mp, double *d_u
     T2D_TRY_DRAIN(cudaStreamWaitEvent(ws.hi, ws.hi_fork, 0));
     su = ws.hi;
   }
-  rc = mixed_upward(m, t.depth, su);
+  rc = mixed_upward(m, t.depth, ws.h_levels, su);
   if (rc) return drain(rc);
   T2D_TRY_DRAIN(cudaMemsetAsync(m.L, 0, sizeof(float) * (size_t)nc * 2 * P, su));
   rc = tc ? m2l_tensor_cores(m, dimg, cls_list, cls_count, su) : m2l_cuda_cores(m, dm2l, su);
   if (rc) return drain(rc);
   st.m2l_path = tc ? 2 : 1;
-  rc = mixed_downward(m, t.depth, su);
+  rc = mixed_downward(m, t.depth, ws.h_levels, su);
   if (rc) return drain(rc);
   if (side) {
     T2D_TRY_DRAIN(cudaEventRecord(ws.hi_join, ws.hi));

@@ -67,8 +67,10 @@ cudaError_t mixed_tables(int P, float *h_m2l, float *h_m2m, float *h_l2l);
 int mixed_leaf_setup(MixedView &m, const Tree &t, cudaStream_t s);
 int mixed_lists(MixedView &m, cudaStream_t s);
 int mixed_fill_lists(MixedView &m, bool from_scratch, cudaStream_t s);
-int mixed_upward(MixedView &m, int depth, cudaStream_t s);
-int mixed_downward(MixedView &m, int depth, cudaStream_t s);
+// lev_off: the per-level cell offsets on the host (level_off's first
+// kKeyLevels + 2 entries), to size each level's grid; null = full grids.
+int mixed_upward(MixedView &m, int depth, const int *lev_off, cudaStream_t s);
+int mixed_downward(MixedView &m, int depth, const int *lev_off, cudaStream_t s);
 
 // M2L over the V lists (m2l.cu): L[c] += sum_s T(class(c), s) M[V[c][s]].
 // `tables` is the device copy of the [4][27][P][P] complex operators.
