@@ -323,10 +323,12 @@ __device__ __forceinline__ unsigned axis_index(float f, int lt, uint64_t okey_po
   return i;
 }
 
+// `packed` (at most 16 digits in all): one word per blob, the key in the
+// high 32 bits and the blob's index in the low 32 (vals unused).
 __global__ void __launch_bounds__(256) k_keys(const double *__restrict__ xy, int n, const RootBox *__restrict__ root,
                                               const uint64_t *__restrict__ tab, int tlev, uint64_t *__restrict__ keys,
                                               uint32_t *__restrict__ vals, int levels, const int *__restrict__ set_of,
-                                              int lev0) {
+                                              int lev0, int packed) {
   long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (i >= n) return;
   double x = xy[2 * i], y = xy[2 * i + 1];
@@ -372,6 +374,10 @@ __global__ void __launch_bounds__(256) k_keys(const double *__restrict__ xy, int
   if (set_of) {
     key |= set_prefix(set, lev0) << (2 * levels);
     total += lev0;
+  }
+  if (packed) {
+    keys[i] = (key << (64 - 2 * total)) | (uint64_t)(uint32_t)i;
+    return;
   }
   keys[i] = total < kKeyLevels ? key << (64 - 2 * total) : key;
   vals[i] = (uint32_t)i;
@@ -819,10 +825,22 @@ retry:
   else
     k_centre_table<<<dim3((unsigned)((2 * centre_entries(tlev) + 255) / 256), (unsigned)t.nsets), 256, 0, s>>>(
         t.root, ctab, tlev);
-  k_keys<<<(n + 255) / 256, 256, 0, s>>>(d_xy, n, t.root, ctab, tlev, t.keys, vals, levels, set_of, lev0);
+  // Up to 16 digits the key and the blob index share one word: the sort
+  // then moves 8 bytes per blob and pass instead of 12, and its last pass
+  // writes them out split.  The words start in the buffer that the last
+  // pass does not read, so that its output lands in t.keys.
+  const bool packed = 2 * total_levels <= 32 && n >= 2;
+  const int passes = (2 * total_levels + 7) / 8;
+  uint64_t *words = packed && (passes & 1) ? keys_alt : t.keys;
+  k_keys<<<(n + 255) / 256, 256, 0, s>>>(d_xy, n, t.root, ctab, tlev, words, vals, levels, set_of, lev0,
+                                         packed ? 1 : 0);
   ::t2d::g_launches.fetch_add(2, std::memory_order_relaxed);
   // 3. sort
-  T2D_CUDA_TRY(radix_sort_pairs(t.keys, vals, keys_alt, vals_alt, n, 64 - 2 * total_levels, 64, sort_tmp, s));
+  if (packed)
+    T2D_CUDA_TRY(radix_sort_packed(words, words == t.keys ? keys_alt : t.keys, n, 64 - 2 * total_levels, t.keys,
+                                   vals, sort_tmp, s));
+  else
+    T2D_CUDA_TRY(radix_sort_pairs(t.keys, vals, keys_alt, vals_alt, n, 64 - 2 * total_levels, 64, sort_tmp, s));
   // 4-5. leaf levels
   k_cpl<<<(n + 255) / 256, 256, 0, s>>>(t.keys, n, p.num_p, cpl, w);
   ::t2d::g_launches.fetch_add(1, std::memory_order_relaxed);
@@ -916,7 +934,7 @@ int sort_targets(Workspace &ws, int n, const double *d_xy, const RootBox *d_root
   void *tmp = ws.tmp_arena.take<char>(radix_sort_temp_bytes(n));
   // order only (for coherent warps): the short key depth is enough
   k_keys<<<(n + 255) / 256, 256, 0, s>>>(d_xy, n, d_root, nullptr, 0, k, reinterpret_cast<uint32_t *>(d_order),
-                                          kShortKeyLevels, nullptr, 0);
+                                          kShortKeyLevels, nullptr, 0, 0);
   ::t2d::g_launches.fetch_add(1, std::memory_order_relaxed);
   T2D_CUDA_TRY(radix_sort_pairs(k, reinterpret_cast<uint32_t *>(d_order), k2, v2, n, 64 - 2 * kShortKeyLevels, 64,
                                 tmp, s));

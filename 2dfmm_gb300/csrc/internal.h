@@ -203,6 +203,15 @@ int gather_targets(int n, const double *d_xy, const int *d_order, double *tx, do
 // (the other bits must be equal in all keys or irrelevant to the order).
 // Buffers *_alt are scratch of the same size.  The result ends in keys/vals.
 size_t radix_sort_temp_bytes(int n);
+// The same sort of packed words (key in the high 32 bits, value in the low
+// 32) on bits [begin_bit, 64), begin_bit >= 32, n >= 2: 8 bytes per element
+// and pass instead of 12.  The passes alternate between words and words_alt
+// (their contents are scratch afterwards); the last pass writes the keys
+// (low half cleared) to keys_out and the values to vals_out.  The last pass
+// reads words when the pass count ceil((64 - begin_bit) / 8) is odd and
+// words_alt when it is even: keys_out may be the other one.
+cudaError_t radix_sort_packed(uint64_t *words, uint64_t *words_alt, int n, int begin_bit, uint64_t *keys_out,
+                              uint32_t *vals_out, void *temp, cudaStream_t s);
 cudaError_t radix_sort_pairs(uint64_t *keys, uint32_t *vals, uint64_t *keys_alt, uint32_t *vals_alt,
                              int n, int begin_bit, int end_bit, void *temp, cudaStream_t s);
 

@@ -21,6 +21,7 @@ constexpr int kTile = kThreads * kItems;      // 4096
 constexpr int kBins = 256;
 static_assert(kThreads == kBins, "the downsweep scans the digit totals with one thread per digit");
 constexpr int kStageBytes = kTile * (8 + 4);  // the downsweep's staging of one tile (48 KB)
+constexpr int kStagePackedBytes = kTile * 8;  // packed keys only (32 KB)
 
 __device__ __forceinline__ unsigned lanemask_lt() {
   unsigned m;
@@ -96,14 +97,18 @@ __device__ __forceinline__ unsigned block_exclusive_scan(unsigned v, unsigned *w
 // digit), staged in shared memory in digit order, and written out from
 // there: consecutive threads write consecutive positions of a digit's run,
 // so the stores coalesce instead of scattering one pair per digit.
+// kPacked: the keys are words whose high 32 bits are the key and whose low
+// 32 bits are the value (vin unused); with `split` the pass writes them out
+// as a key (low half cleared) and a value.
+template <bool kPacked>
 __global__ void __launch_bounds__(kThreads) k_downsweep(const uint64_t *__restrict__ kin,
                                                         const uint32_t *__restrict__ vin,
                                                         uint64_t *__restrict__ kout, uint32_t *__restrict__ vout,
                                                         int n, int shift, const unsigned *__restrict__ offs,
-                                                        int ntiles, const unsigned *__restrict__ totals) {
+                                                        int ntiles, const unsigned *__restrict__ totals, int split) {
   extern __shared__ __align__(16) unsigned char stage[];
   uint64_t *sk = reinterpret_cast<uint64_t *>(stage);             // kTile keys, tile digit order
-  uint32_t *sv = reinterpret_cast<uint32_t *>(stage + kTile * 8);  // kTile values
+  uint32_t *sv = reinterpret_cast<uint32_t *>(stage + kTile * 8);  // kTile values (unpacked only)
   __shared__ unsigned wcount[kWarps][kBins];
   __shared__ unsigned lbase[kBins];  // tile-local start of each digit's run
   __shared__ unsigned gbase[kBins];  // global position of that start
@@ -117,7 +122,7 @@ __global__ void __launch_bounds__(kThreads) k_downsweep(const uint64_t *__restri
   const long tile0 = (long)blockIdx.x * kTile;
   const long base = tile0 + warp * (kItems * 32);
   uint64_t k[kItems];
-  uint32_t v[kItems];
+  uint32_t v[kPacked ? 1 : kItems];
   unsigned r[kItems];
   const unsigned ltmask = lanemask_lt();
 #pragma unroll
@@ -125,7 +130,7 @@ __global__ void __launch_bounds__(kThreads) k_downsweep(const uint64_t *__restri
     long i = base + j * 32 + lane;
     bool valid = i < n;
     k[j] = valid ? kin[i] : 0;
-    v[j] = valid ? vin[i] : 0;
+    if (!kPacked) v[j] = valid ? vin[i] : 0;
     unsigned d = valid ? (unsigned)((k[j] >> shift) & 0xff) : 0x100u;
     unsigned peers = __match_any_sync(0xffffffffu, d);
     unsigned rank = __popc(peers & ltmask);
@@ -158,7 +163,7 @@ __global__ void __launch_bounds__(kThreads) k_downsweep(const uint64_t *__restri
       const unsigned d = (unsigned)((k[j] >> shift) & 0xff);
       const unsigned lp = lbase[d] + wcount[warp][d] + r[j];
       sk[lp] = k[j];
-      sv[lp] = v[j];
+      if (!kPacked) sv[lp] = v[j];
     }
   }
   __syncthreads();
@@ -167,8 +172,15 @@ __global__ void __launch_bounds__(kThreads) k_downsweep(const uint64_t *__restri
     const uint64_t key = sk[p];
     const unsigned d = (unsigned)((key >> shift) & 0xff);
     const unsigned pos = gbase[d] + ((unsigned)p - lbase[d]);
-    kout[pos] = key;
-    vout[pos] = sv[p];
+    if (!kPacked) {
+      kout[pos] = key;
+      vout[pos] = sv[p];
+    } else if (split) {
+      kout[pos] = key & 0xffffffff00000000ull;
+      vout[pos] = (uint32_t)key;
+    } else {
+      kout[pos] = key;
+    }
   }
 }
 
@@ -188,14 +200,14 @@ cudaError_t radix_sort_pairs(uint64_t *keys, uint32_t *vals, uint64_t *keys_alt,
   uint64_t *ka = keys, *kb = keys_alt;
   uint32_t *va = vals, *vb = vals_alt;
   int passes = 0;
-  cudaError_t e = cudaFuncSetAttribute(k_downsweep, cudaFuncAttributeMaxDynamicSharedMemorySize, kStageBytes);
+  cudaError_t e = cudaFuncSetAttribute(k_downsweep<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kStageBytes);
   if (e != cudaSuccess) return e;
   for (int shift = begin_bit; shift < end_bit; shift += 8, passes++) {
     k_upsweep<<<ntiles, kThreads, 0, s>>>(ka, n, shift, counts, ntiles);
     ::t2d::g_launches.fetch_add(1, std::memory_order_relaxed);
     k_scan_digit<<<kBins, 1024, 0, s>>>(counts, ntiles, totals);
     ::t2d::g_launches.fetch_add(1, std::memory_order_relaxed);
-    k_downsweep<<<ntiles, kThreads, kStageBytes, s>>>(ka, va, kb, vb, n, shift, counts, ntiles, totals);
+    k_downsweep<false><<<ntiles, kThreads, kStageBytes, s>>>(ka, va, kb, vb, n, shift, counts, ntiles, totals, 0);
     ::t2d::g_launches.fetch_add(1, std::memory_order_relaxed);
     uint64_t *tk = ka;
     ka = kb;
@@ -207,6 +219,33 @@ cudaError_t radix_sort_pairs(uint64_t *keys, uint32_t *vals, uint64_t *keys_alt,
   if (passes & 1) {
     cudaMemcpyAsync(keys, ka, sizeof(uint64_t) * (size_t)n, cudaMemcpyDeviceToDevice, s);
     cudaMemcpyAsync(vals, va, sizeof(uint32_t) * (size_t)n, cudaMemcpyDeviceToDevice, s);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t radix_sort_packed(uint64_t *words, uint64_t *words_alt, int n, int begin_bit, uint64_t *keys_out,
+                              uint32_t *vals_out, void *temp, cudaStream_t s) {
+  if (begin_bit < 32 || begin_bit >= 64 || n < 2) return cudaErrorInvalidValue;
+  const int passes = (64 - begin_bit + 7) / 8;
+  const int ntiles = (n + kTile - 1) / kTile;
+  unsigned *counts = static_cast<unsigned *>(temp);
+  unsigned *totals = counts + (size_t)kBins * ntiles;
+  cudaError_t e = cudaFuncSetAttribute(k_downsweep<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       kStagePackedBytes);
+  if (e != cudaSuccess) return e;
+  uint64_t *ka = words, *kb = words_alt;
+  for (int p = 0; p < passes; p++) {
+    const int shift = begin_bit + 8 * p;
+    const bool last = p == passes - 1;
+    k_upsweep<<<ntiles, kThreads, 0, s>>>(ka, n, shift, counts, ntiles);
+    k_scan_digit<<<kBins, 1024, 0, s>>>(counts, ntiles, totals);
+    k_downsweep<true><<<ntiles, kThreads, kStagePackedBytes, s>>>(ka, nullptr, last ? keys_out : kb,
+                                                                  last ? vals_out : nullptr, n, shift, counts,
+                                                                  ntiles, totals, last ? 1 : 0);
+    ::t2d::g_launches.fetch_add(3, std::memory_order_relaxed);
+    uint64_t *t = ka;
+    ka = kb;
+    kb = t;
   }
   return cudaGetLastError();
 }
