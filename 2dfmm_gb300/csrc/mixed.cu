@@ -715,34 +715,65 @@ __global__ void __launch_bounds__(256) k_s2m_f32(MixedView m) {
   }
 }
 
-// M2M into the internal cells of one level (grid-stride over all cells).
-__global__ void k_m2m_f32(MixedView m, int lev) {
-  const int lane = threadIdx.x & 31;
+// The [4][P][P] block of a [4][kMaxP][kMaxP] translation table, copied
+// into shared memory by the whole block.
+__device__ __forceinline__ void stage_translation(const float2 *__restrict__ tab, int P, float2 *s_tab) {
+  const int pp = P * P;
+  for (int i = threadIdx.x; i < 4 * pp; i += blockDim.x) {
+    const int q = i / pp, r = i - q * pp, row = r / P, col = r - row * P;
+    s_tab[i] = tab[((size_t)q * kMaxP + row) * kMaxP + col];
+  }
+  __syncthreads();
+}
+
+// M2M into the internal cells of one level (grid-stride over all cells,
+// one warp per cell).  The operator sits in shared memory; with P <= 16
+// (kG = 16) each half-warp takes two of the four children, lane = output
+// coefficient, and the halves' sums meet by one shuffle: the children's
+// sums are independent chains, ((q0 + q1) + (q2 + q3)) at the end.
+template <int kG>
+__global__ void __launch_bounds__(256) k_m2m_f32(MixedView m, int lev) {
+  extern __shared__ float2 s_tab[];  // [4][P][P]: [q][n][k]
   const int P = m.P;
+  stage_translation(m.m2m, P, s_tab);
+  constexpr int kCh = 4 * kG / 32;  // children per lane
+  const int lane = threadIdx.x & 31, n = lane % kG, q0 = (lane / kG) * kCh, base = lane - n;
   const int *cells = m.by_level + m.level_off[lev];
   const int cnt = m.level_off[lev + 1] - m.level_off[lev];
   for (int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < cnt; i += (gridDim.x * blockDim.x) >> 5) {
     const int p = cells[i];
     if (m.leaf[p]) continue;
     const int4 ch = reinterpret_cast<const int4 *>(m.child)[p];
-    float2 acc = make_float2(0.f, 0.f);
-    for (int q = 0; q < 4; q++) {
-      const int c = (&ch.x)[q];
-      if (c < 0) continue;
-      const float *src = m.M + (size_t)c * 2 * P;
-      float2 a = lane < P ? make_float2(src[lane], src[P + lane]) : make_float2(0.f, 0.f);
-      for (int k = 0; k < P; k++) {
-        float2 ak = make_float2(__shfl_sync(0xffffffffu, a.x, k), __shfl_sync(0xffffffffu, a.y, k));
-        if (k <= lane && lane < P) {
-          const float2 t = m.m2m[((size_t)q * kMaxP + lane) * kMaxP + k];
-          acc.x += t.x * ak.x - t.y * ak.y;
-          acc.y += t.x * ak.y + t.y * ak.x;
+    float2 a[kCh], acc[kCh];
+#pragma unroll
+    for (int c = 0; c < kCh; c++) {
+      const int cc = (&ch.x)[q0 + c];
+      a[c] = cc >= 0 && n < P ? make_float2(m.M[(size_t)cc * 2 * P + n], m.M[(size_t)cc * 2 * P + P + n])
+                              : make_float2(0.f, 0.f);
+      acc[c] = make_float2(0.f, 0.f);
+    }
+#pragma unroll 4
+    for (int k = 0; k < P; k++) {
+#pragma unroll
+      for (int c = 0; c < kCh; c++) {
+        const float2 ak = make_float2(__shfl_sync(0xffffffffu, a[c].x, base + k),
+                                      __shfl_sync(0xffffffffu, a[c].y, base + k));
+        if (k <= n && n < P) {
+          const float2 t = s_tab[((q0 + c) * P + n) * P + k];
+          acc[c].x += t.x * ak.x - t.y * ak.y;
+          acc[c].y += t.x * ak.y + t.y * ak.x;
         }
       }
     }
+    float2 sum = make_float2(acc[0].x + acc[1].x, acc[0].y + acc[1].y);
+    if (kCh == 4) sum = make_float2(sum.x + (acc[2].x + acc[3].x), sum.y + (acc[2].y + acc[3].y));
+    if (kG == 16) {
+      const float ox = __shfl_xor_sync(0xffffffffu, sum.x, 16), oy = __shfl_xor_sync(0xffffffffu, sum.y, 16);
+      sum = make_float2(sum.x + ox, sum.y + oy);  // the same value in both halves
+    }
     if (lane < P) {
-      m.M[(size_t)p * 2 * P + lane] = acc.x;
-      m.M[(size_t)p * 2 * P + P + lane] = acc.y;
+      m.M[(size_t)p * 2 * P + lane] = sum.x;
+      m.M[(size_t)p * 2 * P + P + lane] = sum.y;
     }
   }
 }
@@ -788,33 +819,179 @@ __global__ void __launch_bounds__(256) k_p2l(MixedView m) {
   }
 }
 
-// L2L from the internal cells of level lev-1 into their children.
-__global__ void k_l2l_f32(MixedView m, int lev) {
-  const int lane = threadIdx.x & 31;
+// M2M and L2L with four threads per parent cell, one per child quadrant q,
+// for kP terms (the default 16): the coefficients sit in registers, the
+// operator in shared memory (each quadrant's block padded by one entry so
+// that the four quadrants' reads fall in different banks; the eight cells
+// of a warp read the same addresses, a broadcast), and the passes issue one
+// shared load per complex multiply-add.  M2M adds the four children's
+// shifted expansions as ((q0 + q1) + (q2 + q3)) by two shuffles within the
+// quad; L2L writes each child from its own thread.
+constexpr int kQuadThreads = 128;
+
+template <int kP>
+__device__ __forceinline__ void stage_translation_padded(const float2 *__restrict__ tab, float2 *s_tab) {
+  constexpr int pp = kP * kP;
+  for (int i = threadIdx.x; i < 4 * pp; i += blockDim.x) {
+    const int q = i / pp, r = i - q * pp, row = r / kP, col = r - row * kP;
+    s_tab[q * (pp + 1) + r] = tab[((size_t)q * kMaxP + row) * kMaxP + col];
+  }
+  __syncthreads();
+}
+
+__device__ __forceinline__ int child_of(const int4 ch, int q) {
+  return q == 0 ? ch.x : q == 1 ? ch.y : q == 2 ? ch.z : ch.w;
+}
+
+template <int kP>
+__global__ void __launch_bounds__(kQuadThreads) k_m2m_quad(MixedView m, int lev) {
+  __shared__ float2 s_tab[4 * (kP * kP + 1)];  // [q][n][k], padded per q
+  stage_translation_padded<kP>(m.m2m, s_tab);
+  const int lane = threadIdx.x & 31, q = lane & 3;
+  const unsigned qmask = 0xfu << (lane & ~3);
+  const int *cells = m.by_level + m.level_off[lev];
+  const int cnt = m.level_off[lev + 1] - m.level_off[lev];
+  const float2 *t = s_tab + q * (kP * kP + 1);
+  for (int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 2; i < cnt; i += (gridDim.x * blockDim.x) >> 2) {
+    const int p = cells[i];
+    if (m.leaf[p]) continue;  // the same cell, so the same branch, for the whole quad
+    const int c = child_of(reinterpret_cast<const int4 *>(m.child)[p], q);
+    float2 acc[kP];
+#pragma unroll
+    for (int n = 0; n < kP; n++) acc[n] = make_float2(0.f, 0.f);
+    if (c >= 0) {
+      const float4 *src = reinterpret_cast<const float4 *>(m.M + (size_t)c * 2 * kP);
+      float a[2 * kP];
+#pragma unroll
+      for (int j = 0; j < kP / 2; j++) {
+        const float4 v = src[j];
+        a[4 * j] = v.x;
+        a[4 * j + 1] = v.y;
+        a[4 * j + 2] = v.z;
+        a[4 * j + 3] = v.w;
+      }
+#pragma unroll
+      for (int n = 0; n < kP; n++)
+#pragma unroll
+        for (int k = 0; k <= n; k++) {
+          const float2 tk = t[n * kP + k];
+          const float ax = a[k], ay = a[kP + k];
+          acc[n].x += tk.x * ax - tk.y * ay;
+          acc[n].y += tk.x * ay + tk.y * ax;
+        }
+    }
+#pragma unroll
+    for (int n = 0; n < kP; n++) {
+      acc[n].x += __shfl_xor_sync(qmask, acc[n].x, 1);
+      acc[n].y += __shfl_xor_sync(qmask, acc[n].y, 1);
+      acc[n].x += __shfl_xor_sync(qmask, acc[n].x, 2);
+      acc[n].y += __shfl_xor_sync(qmask, acc[n].y, 2);
+    }
+    // thread q stores coefficients 4q .. 4q+3 of the kP / 4 groups it owns
+    float4 *dst = reinterpret_cast<float4 *>(m.M + (size_t)p * 2 * kP);
+#pragma unroll
+    for (int j = 0; j < kP / 4; j++) {
+      if ((j & 3) != q) continue;
+      dst[j] = make_float4(acc[4 * j].x, acc[4 * j + 1].x, acc[4 * j + 2].x, acc[4 * j + 3].x);
+      dst[kP / 4 + j] = make_float4(acc[4 * j].y, acc[4 * j + 1].y, acc[4 * j + 2].y, acc[4 * j + 3].y);
+    }
+  }
+}
+
+template <int kP>
+__global__ void __launch_bounds__(kQuadThreads) k_l2l_quad(MixedView m, int lev) {
+  __shared__ float2 s_tab[4 * (kP * kP + 1)];  // [q][k][l], padded per q
+  stage_translation_padded<kP>(m.l2l, s_tab);
+  const int q = threadIdx.x & 3;
+  const int *cells = m.by_level + m.level_off[lev - 1];
+  const int cnt = m.level_off[lev] - m.level_off[lev - 1];
+  const float2 *t = s_tab + q * (kP * kP + 1);
+  for (int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 2; i < cnt; i += (gridDim.x * blockDim.x) >> 2) {
+    const int p = cells[i];
+    if (m.leaf[p]) continue;
+    const int c = child_of(reinterpret_cast<const int4 *>(m.child)[p], q);
+    if (c < 0) continue;
+    const float4 *src = reinterpret_cast<const float4 *>(m.L + (size_t)p * 2 * kP);
+    float b[2 * kP];
+#pragma unroll
+    for (int j = 0; j < kP / 2; j++) {
+      const float4 v = src[j];
+      b[4 * j] = v.x;
+      b[4 * j + 1] = v.y;
+      b[4 * j + 2] = v.z;
+      b[4 * j + 3] = v.w;
+    }
+    float4 *dst = reinterpret_cast<float4 *>(m.L + (size_t)c * 2 * kP);
+#pragma unroll
+    for (int j = 0; j < kP / 4; j++) {
+      float2 acc[4];
+#pragma unroll
+      for (int u = 0; u < 4; u++) {
+        const int k = 4 * j + u;
+        acc[u] = make_float2(0.f, 0.f);
+#pragma unroll
+        for (int l = k; l < kP; l++) {
+          const float2 tl = t[k * kP + l];
+          const float bx = b[l], by = b[kP + l];
+          acc[u].x += tl.x * bx - tl.y * by;
+          acc[u].y += tl.x * by + tl.y * bx;
+        }
+      }
+      float4 re = dst[j], im = dst[kP / 4 + j];
+      re.x += acc[0].x;
+      re.y += acc[1].x;
+      re.z += acc[2].x;
+      re.w += acc[3].x;
+      im.x += acc[0].y;
+      im.y += acc[1].y;
+      im.z += acc[2].y;
+      im.w += acc[3].y;
+      dst[j] = re;
+      dst[kP / 4 + j] = im;
+    }
+  }
+}
+
+// L2L from the internal cells of level lev-1 into their children (one
+// warp per parent, the operator in shared memory).  With P <= 16 (kG = 16)
+// each half-warp translates two of the four children, lane = coefficient.
+template <int kG>
+__global__ void __launch_bounds__(256) k_l2l_f32(MixedView m, int lev) {
+  extern __shared__ float2 s_tab[];  // [4][P][P]: [q][k][l]
   const int P = m.P;
+  stage_translation(m.l2l, P, s_tab);
+  constexpr int kCh = 4 * kG / 32;
+  const int lane = threadIdx.x & 31, k = lane % kG, q0 = (lane / kG) * kCh;
   const int *cells = m.by_level + m.level_off[lev - 1];
   const int cnt = m.level_off[lev] - m.level_off[lev - 1];
   for (int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < cnt; i += (gridDim.x * blockDim.x) >> 5) {
     const int p = cells[i];
     if (m.leaf[p]) continue;
     const float *src = m.L + (size_t)p * 2 * P;
-    float2 b = lane < P ? make_float2(src[lane], src[P + lane]) : make_float2(0.f, 0.f);
+    const float2 b = k < P ? make_float2(src[k], src[P + k]) : make_float2(0.f, 0.f);
     const int4 ch = reinterpret_cast<const int4 *>(m.child)[p];
-    for (int q = 0; q < 4; q++) {
-      const int c = (&ch.x)[q];
-      if (c < 0) continue;
-      float2 acc = make_float2(0.f, 0.f);
-      for (int l = 0; l < P; l++) {
-        float2 bl = make_float2(__shfl_sync(0xffffffffu, b.x, l), __shfl_sync(0xffffffffu, b.y, l));
-        if (l >= lane && lane < P) {
-          const float2 t = m.l2l[((size_t)q * kMaxP + lane) * kMaxP + l];
-          acc.x += t.x * bl.x - t.y * bl.y;
-          acc.y += t.x * bl.y + t.y * bl.x;
+    float2 acc[kCh];
+#pragma unroll
+    for (int c = 0; c < kCh; c++) acc[c] = make_float2(0.f, 0.f);
+#pragma unroll 4
+    for (int l = 0; l < P; l++) {
+      const float2 bl = make_float2(__shfl_sync(0xffffffffu, b.x, l), __shfl_sync(0xffffffffu, b.y, l));
+      if (l >= k && k < P) {
+#pragma unroll
+        for (int c = 0; c < kCh; c++) {
+          const float2 t = s_tab[((q0 + c) * P + k) * P + l];
+          acc[c].x += t.x * bl.x - t.y * bl.y;
+          acc[c].y += t.x * bl.y + t.y * bl.x;
         }
       }
-      if (lane < P) {
-        m.L[(size_t)c * 2 * P + lane] += acc.x;
-        m.L[(size_t)c * 2 * P + P + lane] += acc.y;
+    }
+    if (k < P) {
+#pragma unroll
+      for (int c = 0; c < kCh; c++) {
+        const int cc = (&ch.x)[q0 + c];
+        if (cc < 0) continue;
+        m.L[(size_t)cc * 2 * P + k] += acc[c].x;
+        m.L[(size_t)cc * 2 * P + P + k] += acc[c].y;
       }
     }
   }
@@ -1296,11 +1473,26 @@ static int level_blocks(const int *lev_off, int lev) {
   return b < 1 ? 1 : (b > full ? full : b);
 }
 
+// Blocks of kQuadThreads for a per-level pass with four threads per cell.
+static int quad_blocks(const int *lev_off, int lev) {
+  const int full = 152 * 8;
+  if (!lev_off) return full;
+  const int cnt = lev_off[lev + 1] - lev_off[lev];
+  const int b = (cnt + kQuadThreads / 4 - 1) / (kQuadThreads / 4);
+  return b < 1 ? 1 : (b > full ? full : b);
+}
+
 int mixed_upward(MixedView &m, int depth, const int *lev_off, cudaStream_t s) {
   k_s2m_f32<<<(int)(((long)m.nleaf * 32 + 255) / 256), 256, 0, s>>>(m);
   g_launches.fetch_add(1, std::memory_order_relaxed);
+  const size_t tab_bytes = 4 * sizeof(float2) * m.P * m.P;
   for (int lev = depth - 1; lev >= 2 + m.lev0; lev--) {
-    k_m2m_f32<<<level_blocks(lev_off, lev), 256, 0, s>>>(m, lev);
+    if (m.P == 16)
+      k_m2m_quad<16><<<quad_blocks(lev_off, lev), kQuadThreads, 0, s>>>(m, lev);
+    else if (m.P < 16)
+      k_m2m_f32<16><<<level_blocks(lev_off, lev), 256, tab_bytes, s>>>(m, lev);
+    else
+      k_m2m_f32<32><<<level_blocks(lev_off, lev), 256, tab_bytes, s>>>(m, lev);
     g_launches.fetch_add(1, std::memory_order_relaxed);
   }
   T2D_CUDA_TRY(cudaGetLastError());
@@ -1310,8 +1502,14 @@ int mixed_upward(MixedView &m, int depth, const int *lev_off, cudaStream_t s) {
 int mixed_downward(MixedView &m, int depth, const int *lev_off, cudaStream_t s) {
   k_p2l<<<(int)(((long)m.ncell * 32 + 255) / 256), 256, 0, s>>>(m);
   g_launches.fetch_add(1, std::memory_order_relaxed);
+  const size_t tab_bytes = 4 * sizeof(float2) * m.P * m.P;
   for (int lev = 3 + m.lev0; lev <= depth; lev++) {
-    k_l2l_f32<<<level_blocks(lev_off, lev - 1), 256, 0, s>>>(m, lev);
+    if (m.P == 16)
+      k_l2l_quad<16><<<quad_blocks(lev_off, lev - 1), kQuadThreads, 0, s>>>(m, lev);
+    else if (m.P < 16)
+      k_l2l_f32<16><<<level_blocks(lev_off, lev - 1), 256, tab_bytes, s>>>(m, lev);
+    else
+      k_l2l_f32<32><<<level_blocks(lev_off, lev - 1), 256, tab_bytes, s>>>(m, lev);
     g_launches.fetch_add(1, std::memory_order_relaxed);
   }
   T2D_CUDA_TRY(cudaGetLastError());

@@ -219,3 +219,21 @@ def test_mixed_leaf_size_rule_and_override(gpu_lib):
         assert P.stats()["leaf_blobs"] == 32
     finally:
         P.set_mixed_leaf(-1)
+
+
+@pytest.mark.gpu
+def test_mixed_expansion_lengths(gpu_lib):
+    """Expansion lengths on both sides of 16 (the M2M / L2L passes give a
+    half-warp per coefficient up to 16 and a whole warp above): the error
+    falls with P, and 24 terms hold relL2 <= 1e-6 as 16 do.  The M2L runs on
+    the CUDA cores here, whose pass takes any length up to 32."""
+    torch = pytest.importorskip("torch")
+    P = gpu_lib
+    W = workloads()
+    b = W.lamb_oseen(131_072, seed=4)
+    try:
+        rel = {p: solve_and_measure(P, torch, b, tensor_cores=False, pterms=p)[0] for p in (8, 16, 24)}
+    finally:
+        P.set_mixed_params(16, 2.5, True)
+    assert rel[24] <= REL_L2 and rel[16] <= REL_L2, rel
+    assert rel[8] > rel[16] and rel[8] <= 1e-2, rel
