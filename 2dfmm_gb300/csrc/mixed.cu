@@ -1052,6 +1052,13 @@ __device__ __forceinline__ float sfu_exp2(float t) {
   return r;
 }
 
+// 1/x on the SFU (PTX rcp.approx: relative error ~2^-23, FTZ).
+__device__ __forceinline__ float sfu_rcp(float x) {
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+
 // One pair: source (x, y, G, t) with t = -log2(e)/sigma^2, target (tx, ty).
 // r2 carries a 1e-30 floor, so a coincident pair has a finite factor and
 // contributes f * (0, 0) = 0, as the reference skips r <= 1e-10
@@ -1063,22 +1070,53 @@ __device__ __forceinline__ float sfu_exp2(float t) {
 //   correction (K): f = -G exp(-r^2/s^2) / r^2 for every pair of the two
 //                   leaves (the list holds the leaves within rc; pairs beyond
 //                   rc add their tiny exact terms).
+// The quotient is G (...) times the SFU reciprocal of r2.
 template <bool kCorrection>
 __device__ __forceinline__ void pair(const float4 sj, float tx, float ty, float &sx, float &sy) {
   const float rx = __fsub_rn(tx, sj.x), ry = __fsub_rn(ty, sj.y);
   const float r2 = fmaf(rx, rx, fmaf(ry, ry, 1e-30f));
   const float t = __fmul_rn(r2, sj.w);
   const float e = sfu_exp2(t);
+  const float ir2 = sfu_rcp(r2);
   float f;
   if (!kCorrection) {
     const float x2 = __fmul_rn(t, -0.69314718f);
-    const float e1f = t > -1.44269504e-3f ? __fmul_rn(x2, fmaf(-0.5f, x2, 1.f)) : __fsub_rn(1.f, e);
-    f = __fdividef(__fmul_rn(sj.z, e1f), r2);
+    const float ser = __fmul_rn(x2, fmaf(-0.5f, x2, 1.f)), ome = __fsub_rn(1.f, e);
+    const float e1f = t > -1.44269504e-3f ? ser : ome;
+    f = __fmul_rn(__fmul_rn(sj.z, e1f), ir2);
   } else {
-    f = -__fdividef(__fmul_rn(sj.z, e), r2);
+    f = -__fmul_rn(__fmul_rn(sj.z, e), ir2);
   }
   sx = fmaf(-f, ry, sx);
   sy = fmaf(f, rx, sy);
+}
+
+// The same pair for two targets at once, on packed FP32x2 arithmetic: one
+// instruction forms both targets' value of every step, with the rounding
+// of the scalar step (each component rounds as the scalar operation does),
+// so a target's sum does not depend on whether its lane holds one target
+// or two.
+__device__ __forceinline__ float2 f2(float v) { return make_float2(v, v); }
+
+template <bool kCorrection>
+__device__ __forceinline__ void pair2(const float4 sj, float2 tx, float2 ty, float2 &sx, float2 &sy) {
+  const float2 rx = __fadd2_rn(tx, f2(-sj.x)), ry = __fadd2_rn(ty, f2(-sj.y));
+  const float2 r2 = __ffma2_rn(rx, rx, __ffma2_rn(ry, ry, f2(1e-30f)));
+  const float2 t = __fmul2_rn(r2, f2(sj.w));
+  const float2 e = make_float2(sfu_exp2(t.x), sfu_exp2(t.y));
+  const float2 ir2 = make_float2(sfu_rcp(r2.x), sfu_rcp(r2.y));
+  float2 f;
+  if (!kCorrection) {
+    const float2 x2 = __fmul2_rn(t, f2(-0.69314718f));
+    const float2 ser = __fmul2_rn(x2, __ffma2_rn(f2(-0.5f), x2, f2(1.f)));
+    const float2 ome = __fadd2_rn(f2(1.f), make_float2(-e.x, -e.y));
+    const float2 e1f = make_float2(t.x > -1.44269504e-3f ? ser.x : ome.x, t.y > -1.44269504e-3f ? ser.y : ome.y);
+    f = __fmul2_rn(__fmul2_rn(f2(sj.z), e1f), ir2);
+  } else {
+    f = __fmul2_rn(__fmul2_rn(f2(-sj.z), e), ir2);
+  }
+  sx = __ffma2_rn(make_float2(-f.x, -f.y), ry, sx);
+  sy = __ffma2_rn(f, rx, sy);
 }
 
 // Direct (U list) or correction (K list) contributions of one source leaf
@@ -1090,12 +1128,14 @@ __device__ __forceinline__ void leaf_pairs(const float4 *__restrict__ src, int j
                                            float txb, float tyb, bool two, float &sxa, float &sya, float &sxb,
                                            float &syb) {
   if (two) {
+    const float2 tx = make_float2(txa, txb), ty = make_float2(tya, tyb);
+    float2 sx = make_float2(sxa, sxb), sy = make_float2(sya, syb);
 #pragma unroll 2
-    for (int j = j0; j < j1; j++) {
-      const float4 sj = src[j];
-      pair<kCorrection>(sj, txa, tya, sxa, sya);
-      pair<kCorrection>(sj, txb, tyb, sxb, syb);
-    }
+    for (int j = j0; j < j1; j++) pair2<kCorrection>(src[j], tx, ty, sx, sy);
+    sxa = sx.x;
+    sxb = sx.y;
+    sya = sy.x;
+    syb = sy.y;
   } else {
 #pragma unroll 4
     for (int j = j0; j < j1; j++) pair<kCorrection>(src[j], txa, tya, sxa, sya);
