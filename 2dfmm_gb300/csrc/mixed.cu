@@ -665,6 +665,18 @@ __device__ __forceinline__ float2 fmul(float2 a, float2 b) {
   return make_float2(fmaf(a.x, b.x, -__fmul_rn(a.y, b.y)), fmaf(a.x, b.y, __fmul_rn(a.y, b.x)));
 }
 
+// Packed FP32x2 forms for a lane's two targets: f2 broadcasts a scalar,
+// C2 holds one complex value per target (x: real parts, y: imaginary), and
+// cmul2 is fmul on each target with the same roundings.
+__device__ __forceinline__ float2 f2(float v) { return make_float2(v, v); }
+__device__ __forceinline__ float2 neg2(float2 v) { return make_float2(-v.x, -v.y); }
+struct C2 {
+  float2 x, y;
+};
+__device__ __forceinline__ C2 cmul2(C2 a, C2 b) {
+  return C2{__ffma2_rn(a.x, b.x, neg2(__fmul2_rn(a.y, b.y))), __ffma2_rn(a.x, b.y, __fmul2_rn(a.y, b.x))};
+}
+
 // Coefficients are formed in chunks of kCoefChunk: every lane takes its own
 // blobs and accumulates the chunk's terms for them in registers, then the
 // warp sums the 32 lanes' partials through shared memory (lane t ends with
@@ -1025,6 +1037,32 @@ __device__ __forceinline__ void m2p_order(const MixedView &m, int B, int A, int 
   phi.y = fmaf(a.y, ih, phi.y);
 }
 
+// m2p_order for the lane's two targets (offsets za, zb from B's centre) in
+// packed arithmetic: each target's value is m2p_order's, bit for bit, and
+// the multipole is read once for both.
+__device__ __forceinline__ void m2p_order2(const MixedView &m, int B, int A, int p, float2 za, float2 zb, float2 &pa,
+                                           float2 &pb) {
+  const int P = m.P;
+  const float ih = m.inv_h[A];
+  const float2 zx = __fmul2_rn(__fadd2_rn(make_float2(za.x, zb.x), f2(centre_offset(m.cxf, m.cxl, B, A))), f2(ih));
+  const float2 zy = __fmul2_rn(__fadd2_rn(make_float2(za.y, zb.y), f2(centre_offset(m.cyf, m.cyl, B, A))), f2(ih));
+  const float2 r2 = __ffma2_rn(zx, zx, __fmul2_rn(zy, zy));
+  const float2 ir2 = make_float2(__fdiv_rn(1.f, r2.x), __fdiv_rn(1.f, r2.y));
+  const C2 w{__fmul2_rn(zx, ir2), neg2(__fmul2_rn(zy, ir2))};
+  const float *MA = m.M + (size_t)A * 2 * P;
+  C2 a{f2(MA[p - 1]), f2(MA[P + p - 1])};
+  for (int k = p - 2; k >= 0; k--) {
+    a = cmul2(a, w);
+    a.x = __fadd2_rn(a.x, f2(MA[k]));
+    a.y = __fadd2_rn(a.y, f2(MA[P + k]));
+  }
+  a = cmul2(a, w);
+  const float2 px = __ffma2_rn(a.x, f2(ih), make_float2(pa.x, pb.x));
+  const float2 py = __ffma2_rn(a.y, f2(ih), make_float2(pa.y, pb.y));
+  pa = make_float2(px.x, py.x);
+  pb = make_float2(px.y, py.y);
+}
+
 // Evaluation: one warp per leaf; each lane owns up to two targets (chunks
 // of 64 targets), so a leaf of <= 64 blobs walks its source lists once.
 // Sources are read as one float4 {x, y, G, 1/sigma^2} (offsets from their
@@ -1043,6 +1081,26 @@ __device__ __forceinline__ void far_field(const MixedView &m, int l, int B, floa
   phi.x = __fmul_rn(acc.x, ihB);
   phi.y = __fmul_rn(acc.y, ihB);
   for (int e = m.w_off[l]; e < m.w_off[l + 1]; e++) m2p_order(m, B, m.w_idx[e], P, zt, phi);
+}
+
+// far_field for the lane's two targets in packed arithmetic (each target's
+// value is far_field's, bit for bit).
+__device__ __forceinline__ void far_field2(const MixedView &m, int l, int B, float2 za, float2 zb, float2 &pa,
+                                           float2 &pb) {
+  const int P = m.P;
+  const float ihB = m.inv_h[B];
+  const float *LB = m.L + (size_t)B * 2 * P;
+  const C2 zeta{__fmul2_rn(make_float2(za.x, zb.x), f2(ihB)), __fmul2_rn(make_float2(za.y, zb.y), f2(ihB))};
+  C2 acc{f2(LB[P - 1]), f2(LB[2 * P - 1])};
+  for (int k = P - 2; k >= 0; k--) {
+    acc = cmul2(acc, zeta);
+    acc.x = __fadd2_rn(acc.x, f2(LB[k]));
+    acc.y = __fadd2_rn(acc.y, f2(LB[P + k]));
+  }
+  const float2 px = __fmul2_rn(acc.x, f2(ihB)), py = __fmul2_rn(acc.y, f2(ihB));
+  pa = make_float2(px.x, py.x);
+  pb = make_float2(px.y, py.y);
+  for (int e = m.w_off[l]; e < m.w_off[l + 1]; e++) m2p_order2(m, B, m.w_idx[e], P, za, zb, pa, pb);
 }
 
 // 2^t on the SFU (PTX ex2.approx: relative error ~2^-22, FTZ).
@@ -1096,7 +1154,6 @@ __device__ __forceinline__ void pair(const float4 sj, float tx, float ty, float 
 // of the scalar step (each component rounds as the scalar operation does),
 // so a target's sum does not depend on whether its lane holds one target
 // or two.
-__device__ __forceinline__ float2 f2(float v) { return make_float2(v, v); }
 
 template <bool kCorrection>
 __device__ __forceinline__ void pair2(const float4 sj, float2 tx, float2 ty, float2 &sx, float2 &sy) {
@@ -1215,8 +1272,10 @@ __global__ void __launch_bounds__(32 * kWarps, 32 / kWarps) k_eval_staged(MixedV
     int q = next_direct(0);
     int buf = 0;
     bool staged = q < nu + nk && stage(q, buf);
-    far_field(m, l, B, za, pa);
-    if (two) far_field(m, l, B, zb, pb);
+    if (two)
+      far_field2(m, l, B, za, zb, pa, pb);
+    else
+      far_field(m, l, B, za, pa);
     if (kLearned) {
       // accepted U entries: the source leaf's multipole at the chosen order
       // (accepted K entries: the correction is left out)
@@ -1225,8 +1284,10 @@ __global__ void __launch_bounds__(32 * kWarps, 32 / kWarps) k_eval_staged(MixedV
         if (d > 0) {
           const int A = m.u_idx[e];
           const int p = min(min(class_order(d) + dec.margin, 16), m.P);
-          m2p_order(m, B, A, p, za, pa);
-          if (two) m2p_order(m, B, A, p, zb, pb);
+          if (two)
+            m2p_order2(m, B, A, p, za, zb, pa, pb);
+          else
+            m2p_order(m, B, A, p, za, pa);
         }
       }
     }
@@ -1311,8 +1372,10 @@ __global__ void __launch_bounds__(32 * kWarps, 32 / kWarps) k_eval_mixed(MixedVi
     const float2 za = va ? m.loc[ta] : make_float2(0.f, 0.f);
     const float2 zb = vb ? m.loc[tb] : make_float2(0.f, 0.f);
     float2 pa = make_float2(0.f, 0.f), pb = make_float2(0.f, 0.f);
-    far_field(m, l, B, za, pa);
-    if (two) far_field(m, l, B, zb, pb);
+    if (two)
+      far_field2(m, l, B, za, zb, pa, pb);
+    else
+      far_field(m, l, B, za, pa);
     float axa = 0.f, aya = 0.f, cxa = 0.f, cya = 0.f;
     float axb = 0.f, ayb = 0.f, cxb = 0.f, cyb = 0.f;
     for (int pass = 0; pass < 2; pass++) {
@@ -1328,8 +1391,10 @@ __global__ void __launch_bounds__(32 * kWarps, 32 / kWarps) k_eval_mixed(MixedVi
             // the correction left out (K)
             if (pass == 0) {
               const int p = min(min(class_order(d) + dec.margin, 16), m.P);
-              m2p_order(m, B, A, p, za, pa);
-              if (two) m2p_order(m, B, A, p, zb, pb);
+              if (two)
+                m2p_order2(m, B, A, p, za, zb, pa, pb);
+              else
+                m2p_order(m, B, A, p, za, pa);
             }
             continue;
           }
