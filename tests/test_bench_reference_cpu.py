@@ -30,3 +30,17 @@ def test_reference_arm_prints_the_contract_line():
     assert line["value"] > 0 and line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["cores"] >= 1
     assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["e2e"]["value"] == line["value"]
     assert line["config"]["n_blobs"] == 3000
+
+
+def test_roofline_traffic_figures_parse():
+    """The per-launch DRAM bytes that `bench.py` puts in its roofline object
+    come from the committed ncu summary: one figure per form at the headline
+    workload, each a plausible per-launch byte count (more than the blobs'
+    own 16 bytes each, less than 16 GB)."""
+    sys.path.insert(0, ROOT)
+    import bench
+    t = bench.roofline_traffic()
+    for mode in ("plain", "mixed", "learned"):
+        key = f"{mode}:two_patch_sheet_4M"
+        assert key in t, key
+        assert 16 * 4_194_304 < t[key] < 16 << 30, (key, t[key])
