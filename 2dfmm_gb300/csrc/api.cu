@@ -520,14 +520,22 @@ int lookup_on_device(Lib &L, int n, const double *xy, double *uv, std::vector<in
 }
 
 // Parameters in force for a device solve (as tree2d_solve_device resolves
-// them), taken under the library lock.
-int params_for_device_solve(Params &out) {
+// them), with the mode and whether a mirror wall is set, taken under the
+// library lock.
+int params_for_device_solve(Params &out, int *mode, bool *mirror) {
   Lib &L = lib();
   std::lock_guard<std::mutex> lk(L.mu);
   int rc = resolve_params(L);
   if (rc) return fail(rc);
   out = L.params;
+  if (mode) *mode = L.mode;
+  if (mirror) *mirror = L.mirror_on;
   return TREE2D_OK;
+}
+
+void note_error_text(const char *text) {
+  std::lock_guard<std::mutex> lk(g_msg_mu);
+  g_cuda_msg = text;
 }
 
 int record_error(int code) { return fail(code); }

@@ -730,6 +730,45 @@ __global__ void __launch_bounds__(256) k_gather(const double *__restrict__ xy, c
 
 }  // namespace
 
+size_t build_blob_bytes(int n, int nsets) {
+  const int ns = nsets > 1 ? nsets : 1;
+  size_t need = 0;
+  need += Arena::bytes_for(n, 8) * 5;  // x y cir cor icor2
+  need += Arena::bytes_for(n, 4);      // perm
+  need += Arena::bytes_for(n, 8);      // keys (sorted)
+  need += Arena::bytes_for(n, 4);      // cellbase
+  need += Arena::bytes_for(n, 1) * 2;  // cpl, leaf_level
+  need += Arena::bytes_for(ns, sizeof(RootBox));
+  return need;
+}
+
+size_t build_tmp_bytes(int n, int nsets) {
+  const bool batched = nsets > 1;
+  const int ns = batched ? nsets : 1;
+  const int ntiles = (n + kScanTile - 1) / kScanTile;
+  size_t tneed = 0;
+  tneed += Arena::bytes_for(n, 8) + Arena::bytes_for(n, 4) * 2;  // keys_alt, vals, vals_alt
+  tneed += Arena::bytes_for(n, 1);                              // w
+  tneed += radix_sort_temp_bytes(n) + 256;
+  tneed += Arena::bytes_for(kBoxBlocks, sizeof(Box4));
+  tneed += Arena::bytes_for(ntiles + 1, 8) + 256;
+  const int tlev = batched ? 12 : centre_levels(n);
+  tneed += Arena::bytes_for(2 * centre_entries(tlev) * ns, 8);
+  if (batched) tneed += Arena::bytes_for(n, 4) + Arena::bytes_for((size_t)nsets * kSetSlices, sizeof(Box4));
+  return tneed;
+}
+
+size_t build_cell_bytes(long long ncell, long long nleaf, int nterms) {
+  size_t cneed = 0;
+  cneed += Arena::bytes_for(ncell, 4) * 3;           // level begin end
+  cneed += Arena::bytes_for(ncell * 4, 4);           // child
+  cneed += Arena::bytes_for(ncell, 1);               // leaf
+  cneed += Arena::bytes_for(ncell, 8) * 3;           // cx cy region
+  cneed += Arena::bytes_for(nleaf > 0 ? nleaf : 1, 4);  // leaf_cell
+  cneed += Arena::bytes_for(ncell * nterms, 16);     // coef
+  return cneed;
+}
+
 int build_tree(Workspace &ws, int n, const double *d_xy, const double *d_cir, const double *d_cor, const Params &p,
                Tree &t, cudaStream_t s, const int *d_set_off, int nsets, cudaEvent_t cir_cor_ready) {
   t.n = n;
@@ -747,14 +786,7 @@ int build_tree(Workspace &ws, int n, const double *d_xy, const double *d_cir, co
   t.set_cor = batched ? d_cor : nullptr;
   const int ntiles = (n + kScanTile - 1) / kScanTile;
   // ---- blob-sized buffers
-  size_t need = 0;
-  need += Arena::bytes_for(n, 8) * 5;           // x y cir cor icor2
-  need += Arena::bytes_for(n, 4);               // perm
-  need += Arena::bytes_for(n, 8);               // keys (sorted)
-  need += Arena::bytes_for(n, 4);               // cellbase
-  need += Arena::bytes_for(n, 1) * 2;           // cpl, leaf_level
-  need += Arena::bytes_for(t.nsets, sizeof(RootBox));
-  T2D_CUDA_TRY(ws.blob_arena.reserve(need));
+  T2D_CUDA_TRY(ws.blob_arena.reserve(build_blob_bytes(n, nsets)));
   ws.blob_arena.reset();
   t.x = ws.blob_arena.take<double>(n);
   t.y = ws.blob_arena.take<double>(n);
@@ -772,16 +804,8 @@ int build_tree(Workspace &ws, int n, const double *d_xy, const double *d_cir, co
   t.cellbase = cellbase;
 
   // ---- scratch
-  size_t tneed = 0;
-  tneed += Arena::bytes_for(n, 8) + Arena::bytes_for(n, 4) * 2;  // keys_alt, vals, vals_alt
-  tneed += Arena::bytes_for(n, 1);                              // w
-  tneed += radix_sort_temp_bytes(n) + 256;
-  tneed += Arena::bytes_for(kBoxBlocks, sizeof(Box4));
-  tneed += Arena::bytes_for(ntiles + 1, 8) + 256;
   const int tlev = batched ? 12 : centre_levels(n);
-  tneed += Arena::bytes_for(2 * centre_entries(tlev) * t.nsets, 8);
-  if (batched) tneed += Arena::bytes_for(n, 4) + Arena::bytes_for((size_t)nsets * kSetSlices, sizeof(Box4));
-  T2D_CUDA_TRY(ws.tmp_arena.reserve(tneed));
+  T2D_CUDA_TRY(ws.tmp_arena.reserve(build_tmp_bytes(n, nsets)));
   ws.tmp_arena.reset();
   uint64_t *keys_alt = ws.tmp_arena.take<uint64_t>(n);
   uint32_t *vals = ws.tmp_arena.take<uint32_t>(n);
@@ -879,14 +903,7 @@ retry:
   const int nt = p.nterms;
 
   // ---- cell-sized buffers
-  size_t cneed = 0;
-  cneed += Arena::bytes_for(ncell, 4) * 3;       // level begin end
-  cneed += Arena::bytes_for(ncell * 4, 4);       // child
-  cneed += Arena::bytes_for(ncell, 1);           // leaf
-  cneed += Arena::bytes_for(ncell, 8) * 3;       // cx cy region
-  cneed += Arena::bytes_for(nleaf, 4);           // leaf_cell
-  cneed += Arena::bytes_for(ncell * nt, 16);     // coef
-  T2D_CUDA_TRY(ws.cell_arena.reserve(cneed));
+  T2D_CUDA_TRY(ws.cell_arena.reserve(build_cell_bytes(ncell, nleaf, nt)));
   ws.cell_arena.reset();
   t.level = ws.cell_arena.take<int>(ncell);
   t.begin = ws.cell_arena.take<int>(ncell);

@@ -187,6 +187,13 @@ cudaError_t workspace_init(Workspace &ws);
 int build_tree(Workspace &ws, int n, const double *d_xy, const double *d_cir, const double *d_cor,
                const Params &p, Tree &t, cudaStream_t s, const int *d_set_off = nullptr, int nsets = 1,
                cudaEvent_t cir_cor_ready = nullptr);
+// Bytes build_tree reserves in ws.blob_arena and ws.tmp_arena for n blobs in
+// nsets sets (what a caller with fixed arenas must provide).
+size_t build_blob_bytes(int n, int nsets);
+size_t build_tmp_bytes(int n, int nsets);
+// Bytes build_tree reserves in ws.cell_arena for a tree of ncell cells and
+// nleaf leaves with nterms coefficients per cell.
+size_t build_cell_bytes(long long ncell, long long nleaf, int nterms);
 
 // Keys of arbitrary points against an existing root box, then sorted:
 // order[i] = index of the i-th target in key order.
@@ -239,8 +246,10 @@ cudaError_t lookup_blobs(long b, long e, const double *q, long nb, const double 
 cudaError_t mirror_images(long n, const double *xy, const double *cir, const double *cor, double d, double *oxy,
                           double *ocir, double *ocor, cudaStream_t s);
 
-// Parameters for a device solve, resolved under the library lock.
-int params_for_device_solve(Params &out);
+// Parameters for a device solve, resolved under the library lock; `mode`
+// and `mirror` (when not null) receive the mode in force and whether a
+// mirror wall is set.
+int params_for_device_solve(Params &out, int *mode = nullptr, bool *mirror = nullptr);
 // Stores `code` as the library's last error and returns it.
 int record_error(int code);
 
@@ -249,5 +258,7 @@ extern std::atomic<long long> g_launches;
 
 // error text of the last CUDA failure (for tree2d_error_string)
 void note_cuda_error(cudaError_t e, const char *what);
+// replaces that text (a failure that is not a CUDA error left it stale)
+void note_error_text(const char *text);
 
 }  // namespace t2d

@@ -113,13 +113,16 @@ int biot_tree_batch(int n, const double *xy, double *uv);
 int tree2d_solve_device(int n, const double *d_xy, const double *d_cir, const double *d_cor,
                         double *d_uv, void *stream);
 
-/* Same solve as tree2d_solve_device (plain mode), for callers that cannot
- * allocate GPU memory: a host program whose device memory belongs to a pool
- * it must not go around, or an embedding that fixes its memory footprint at
- * start-up.  The call allocates nothing: all scratch lives in one 32 MiB
- * file-scope device array per GPU, resident until the process exits.  The
- * caller still passes inputs and outputs.  Limits: n <= 65536 blobs and as
- * many cells as fit in the array; beyond that it returns
+/* The plain-mode solve of tree2d_solve_device (same kernels, same results
+ * bit for bit), for callers that cannot allocate GPU memory: a host program
+ * whose device memory belongs to a pool it must not go around, or an
+ * embedding that fixes its memory footprint at start-up.  The call
+ * allocates nothing: all scratch lives in one 32 MiB file-scope device
+ * array per GPU, resident until the process exits.  The caller still passes
+ * inputs and outputs.  Plain form only: with TREE2D_MODE_MIXED or
+ * TREE2D_MODE_LEARNED in force, or a mirror wall set (tree2d_set_mirror),
+ * it returns TREE2D_ERR_MODE and computes nothing.  Limits: n <= 65536
+ * blobs and as many cells as fit in the array; beyond that it returns
  * TREE2D_ERR_TOO_LARGE.  Every call shares the array and it keeps the last
  * call's contents (what the solve reads it clears first); calls that
  * overlap on the GPU race, so do not run two at once on different streams.

@@ -18,11 +18,6 @@ import pytest
 from conftest import load_golden, workloads
 
 
-def _tol_ok(a, b):
-    mag = np.linalg.norm(b, axis=1, keepdims=True)
-    return bool((np.abs(a - b) <= 1e-12 * np.abs(b) + 1e-13 * mag).all())
-
-
 def _solve_both(P, torch, b):
     dev = torch.device("cuda:0")
     xy = torch.from_numpy(np.ascontiguousarray(b["xy"])).to(dev)
@@ -61,8 +56,58 @@ def test_static_solve_matches_allocating_solve_twice(gpu_lib):
         rc, out, ref, grew = _solve_both(P, torch, case)
         assert rc == P.OK, P.error_string(rc)
         assert np.isfinite(out).all()
-        assert _tol_ok(out, ref)
+        # the same kernels on the same tree: equal bit for bit, so scratch left
+        # over from the previous call cannot hide behind a tolerance
+        assert np.array_equal(out, ref)
         assert grew <= 0, f"device free memory fell by {grew} bytes during the call"
+
+
+@pytest.mark.gpu
+def test_static_solve_at_its_size_limit(gpu_lib):
+    """65,536 blobs, the largest input the fixed array takes: the regions are
+    sized from the tree build's own reservation, so this must fit."""
+    torch = pytest.importorskip("torch")
+    P = gpu_lib
+    P.set_mode(P.MODE_PLAIN)
+    u = workloads().uniform(P.STATIC_MAX_BLOBS, seed=32)
+    case = dict(xy=u.xy, cir=u.cir, cor=u.cor, nterms=u.nterms, num_p=u.num_p, theta=u.theta)
+    rc, out, ref, grew = _solve_both(P, torch, case)
+    assert rc == P.OK, P.error_string(rc)
+    assert np.array_equal(out, ref)
+    assert grew <= 0
+
+
+@pytest.mark.gpu
+def test_static_solve_refuses_mixed_mode_and_mirror(gpu_lib):
+    """The static solve is the plain form only: in another mode, or with a
+    mirror wall, it must say so rather than answer without the images or
+    with another method."""
+    torch = pytest.importorskip("torch")
+    P = gpu_lib
+    b = load_golden("tiny33")
+    dev = torch.device("cuda:0")
+    xy = torch.from_numpy(np.ascontiguousarray(b["xy"])).to(dev)
+    cir = torch.from_numpy(np.ascontiguousarray(b["cir"])).to(dev)
+    cor = torch.from_numpy(np.ascontiguousarray(b["cor"])).to(dev)
+    n = len(b["cir"])
+    out = torch.full((n, 2), float("nan"), dtype=torch.float64, device=dev)
+    P.set_params(int(b["nterms"]), int(b["num_p"]), float(b["theta"]))
+    try:
+        for mode in (P.MODE_MIXED, P.MODE_LEARNED):
+            P.set_mode(mode)
+            rc = P.solve_device_static(xy.data_ptr(), cir.data_ptr(), cor.data_ptr(), out.data_ptr(), n)
+            assert rc == P.ERR_MODE
+        P.set_mode(P.MODE_PLAIN)
+        P.set_mirror(True, -0.5)
+        rc = P.solve_device_static(xy.data_ptr(), cir.data_ptr(), cor.data_ptr(), out.data_ptr(), n)
+        assert rc == P.ERR_MODE
+        torch.cuda.synchronize()
+        assert torch.isnan(out).all()  # nothing was computed
+    finally:
+        P.set_mirror(False, 0.0)
+        P.set_mode(P.MODE_PLAIN)
+    rc = P.solve_device_static(xy.data_ptr(), cir.data_ptr(), cor.data_ptr(), out.data_ptr(), n)
+    assert rc == P.OK
 
 
 @pytest.mark.gpu
