@@ -32,18 +32,50 @@ _lp = ctypes.POINTER(ctypes.c_long)
 
 def build(force: bool = False) -> str:
     """Compiles liboracle.so with the recipe in oracle/Makefile."""
-    src = os.path.join(HERE, "tree2d_oracle.c")
-    if force or not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < os.path.getmtime(src):
+    srcs = [os.path.join(HERE, f) for f in ("tree2d_oracle.c", "tree2d_sparse.c")]
+    if force or not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < max(map(os.path.getmtime, srcs)):
         subprocess.run(["make", "-s", "-C", HERE, "liboracle.so"], check=True)
     return LIB_PATH
 
 
-def build_reference(ref_src: str = "/root/reference/ver-c/src") -> str | None:
-    """Builds _ref/ref_driver from the reference sources when they are present."""
-    if not os.path.isdir(ref_src):
+REF_STAGE = os.path.join(HERE, "_ref", "src")
+REF_FILES = ("quadtree.c", "quadtree.h", "fmm.c", "fmm.h", "morton_order.c", "morton_order.h")
+
+
+def reference_sources(ref_src: str | None = None) -> str | None:
+    """Directory holding the reference's ver-c/src files: `ref_src` or
+    $TREE2D_REF_SRC when given and present, else the unmodified copy staged
+    in _ref/src (git-ignored; it travels with the working tree to a machine
+    without the reference), else None."""
+    for cand in (ref_src, os.environ.get("TREE2D_REF_SRC")):
+        if cand and all(os.path.isfile(os.path.join(cand, f)) for f in REF_FILES):
+            return cand
+    if all(os.path.isfile(os.path.join(REF_STAGE, f)) for f in REF_FILES):
+        return REF_STAGE
+    return None
+
+
+def build_reference(ref_src: str | None = None) -> str | None:
+    """Builds _ref/ref_driver from the reference's own sources when they are
+    available (see reference_sources); a given source directory is first
+    staged, unmodified, into _ref/src so that the build can be repeated where
+    the reference is absent.  Returns the driver's path or None."""
+    src = reference_sources(ref_src)
+    if src is None:
         return None
-    subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF_SRC={ref_src}"], check=True)
+    if os.path.abspath(src) != os.path.abspath(REF_STAGE):
+        subprocess.run(["make", "-s", "-C", HERE, "stage", f"REF_SRC={src}"], check=True)
+    subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True)
+    if not _runs(REF_DRIVER):  # built for another machine: rebuild here
+        subprocess.run(["make", "-s", "-B", "-C", HERE, "ref"], check=True)
     return REF_DRIVER
+
+
+def _runs(path: str) -> bool:
+    try:
+        return subprocess.run([path], capture_output=True).returncode == 2  # its usage exit
+    except OSError:
+        return False
 
 
 def lib():
@@ -63,6 +95,14 @@ def lib():
             L.ora_dump_tree.restype = ctypes.c_long
             L.ora_direct.argtypes = [ctypes.c_int, _dp, ctypes.c_int, _dp, _dp, _dp, _dp, ctypes.c_int]
             L.ora_max_threads.restype = ctypes.c_int
+            L.ora_sp_make_tree.argtypes = [ctypes.c_int, _dp, _dp, _dp, ctypes.c_int]
+            L.ora_sp_make_tree.restype = ctypes.c_int
+            L.ora_sp_levels.restype = ctypes.c_int
+            L.ora_sp_num_nodes.restype = ctypes.c_long
+            L.ora_sp_biot_many.argtypes = [ctypes.c_int, _dp, _dp, ctypes.c_int, _lp, _lp]
+            L.ora_sp_biot_ext.argtypes = [ctypes.c_int, _dp, _dp, ctypes.c_int]
+            L.ora_sp_dump_tree.argtypes = [_ip, ctypes.c_long, _ip, _ip, _ip, _ip, _dp, _dp, _dp, _dp]
+            L.ora_sp_dump_tree.restype = ctypes.c_long
             _lib = L
     return _lib
 
@@ -109,6 +149,10 @@ class Oracle:
     def levels(self) -> int:
         return self.L.ora_levels()
 
+    def close(self):
+        """Releases the tree (tens of GB for deep dense trees)."""
+        self.L.ora_free()
+
     def num_nodes(self) -> int:
         return self.L.ora_num_nodes()
 
@@ -128,6 +172,60 @@ class Oracle:
                              _p(cx), _p(cy), _p(reg), _p(coef))
         return dict(perm=perm, level=lev, begin=beg, end=end, leaf=leaf, cx=cx, cy=cy, region=reg,
                     coef=coef[..., 0] + 1j * coef[..., 1])
+
+
+class SparseOracle:
+    """The reference tree built without the dense node array
+    (tree2d_sparse.c): the same tree, coefficients and velocities as Oracle,
+    for trees too deep for the dense layout, plus the treecode's value in
+    extended precision.  One sparse tree exists at a time."""
+
+    def __init__(self, nterms: int, num_p: int, theta: float, r_min: float = 0.01):
+        self.L = lib()
+        self.L.ora_set_params(nterms, num_p, theta, r_min)
+        self.nterms = nterms
+
+    def make_tree(self, xy, cir, cor, level_cap: int = 60) -> int:
+        xy = _f64(xy).reshape(-1, 2)
+        cir = _f64(cir)
+        cor = _f64(cor)
+        rc = self.L.ora_sp_make_tree(len(cir), _p(xy), _p(cir), _p(cor), level_cap)
+        if rc != 0:
+            raise RuntimeError(f"sparse oracle make_tree failed: {rc}")
+        return rc
+
+    def levels(self) -> int:
+        return self.L.ora_sp_levels()
+
+    def biot(self, txy, threads: int = 0, counters: bool = False):
+        txy = _f64(txy).reshape(-1, 2)
+        uv = np.empty_like(txy)
+        a = ctypes.c_long(0)
+        b = ctypes.c_long(0)
+        self.L.ora_sp_biot_many(len(txy), _p(txy), _p(uv), threads, ctypes.byref(a), ctypes.byref(b))
+        return (uv, a.value, b.value) if counters else uv
+
+    def biot_ext(self, txy, threads: int = 0):
+        """The same treecode (same accepted cells and pairs) evaluated in
+        extended precision: its value to far below FP64 rounding."""
+        txy = _f64(txy).reshape(-1, 2)
+        uv = np.empty_like(txy)
+        self.L.ora_sp_biot_ext(len(txy), _p(txy), _p(uv), threads)
+        return uv
+
+    def dump(self, n: int):
+        nc = self.L.ora_sp_dump_tree(None, 0, None, None, None, None, None, None, None, None)
+        perm = np.empty(n, np.int32)
+        lev, beg, end, leaf = (np.empty(nc, np.int32) for _ in range(4))
+        cx, cy, reg = (np.empty(nc) for _ in range(3))
+        coef = np.empty((nc, self.nterms, 2))
+        self.L.ora_sp_dump_tree(_p(perm, _ip), nc, _p(lev, _ip), _p(beg, _ip), _p(end, _ip), _p(leaf, _ip),
+                                _p(cx), _p(cy), _p(reg), _p(coef))
+        return dict(perm=perm, level=lev, begin=beg, end=end, leaf=leaf, cx=cx, cy=cy, region=reg,
+                    coef=coef[..., 0] + 1j * coef[..., 1])
+
+    def close(self):
+        self.L.ora_sp_reset()
 
 
 def direct(txy, sxy, cir, cor, threads: int = 0):

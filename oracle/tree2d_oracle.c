@@ -24,8 +24,10 @@
  * The data layout is the reference's: a dense, complete quadtree of
  * (4^(L+1)-1)/3 nodes in level order, a max-level that persists between
  * calls and grows by one per failed attempt, and a per-call traversal stack
- * of num_nodes entries.  Those choices are kept on purpose: they set the
- * reference's cost, and this file doubles as its timed CPU stand-in.
+ * of num_nodes int entries (the split and the traversal stacks are -1-filled
+ * ints, quadtree.c:183-188 and fmm.c:83-87).  Those choices are kept on
+ * purpose: they set the reference's cost, and this file doubles as its
+ * timed CPU stand-in where the reference's own build is not available.
  *
  * Every floating-point expression that decides a result is written in the
  * same form as the reference (complex arithmetic, cpow for powers, pow(.,2)
@@ -125,6 +127,10 @@ int ora_set_params(int nterms, int num_p, double theta, double r_min) {
  * reference starts at 1). */
 void ora_reset(void) { g.max_level = 1; }
 
+static void free_tree(void);
+/* Releases the tree (the dense array can take tens of GB). */
+void ora_free(void) { free_tree(); }
+
 /* ---------------------------------------------------------------------- */
 /* tree construction                                                       */
 
@@ -193,12 +199,15 @@ static int build_attempt(int L) {
   for (int i = 0; i < g.nblob; i++) root->ids[i] = i;
   if (g.nblob > 0) root_box(root);
 
-  long *stack = (long *)malloc(sizeof(long) * (size_t)g.num_nodes);
-  long top = 0;
+  /* an int stack of num_nodes entries, -1-filled, as quadtree.c:183-188 */
+  int *stack = (int *)malloc(sizeof(int) * (size_t)g.num_nodes);
   stack[0] = 0;
+  for (long i = 1; i < g.num_nodes; i++) stack[i] = -1;
+  long top = 0;
   int rc = 0;
   while (top >= 0) {
-    long p = stack[top--];
+    long p = stack[top];
+    stack[top--] = -1;
     ora_node *pn = &g.node[p];
     if (pn->level + 1 > L) {
       rc = -1;
@@ -226,7 +235,7 @@ static int build_attempt(int L) {
       if (cn->nb < g.num_p)
         cn->leaf = 1;
       else
-        stack[++top] = ch[q];
+        stack[++top] = (int)ch[q];
     }
   }
   free(stack);
@@ -361,10 +370,11 @@ static void p2p(double x, double y, const ora_node *nd, double ud[2]) {
 static void biot_one(double x, double y, double *u, double *v, long *n_m2s, long *n_pairs) {
   double complex phi = 0.0;
   double ud[2] = {0.0, 0.0};
-  long *stack = (long *)malloc(sizeof(long) * (size_t)g.num_nodes);
-  for (long i = 0; i < g.num_nodes; i++) stack[i] = -1;
-  long top = 0;
+  /* an int stack of num_nodes entries, -1-filled, per call (fmm.c:83-87) */
+  int *stack = (int *)malloc(sizeof(int) * (size_t)g.num_nodes);
   stack[0] = 0;
+  for (long i = 1; i < g.num_nodes; i++) stack[i] = -1;
+  long top = 0;
   double complex z = x + y * I;
   while (top >= 0) {
     long t = stack[top];
@@ -380,7 +390,7 @@ static void biot_one(double x, double y, double *u, double *v, long *n_m2s, long
         const ora_node *cn = &g.node[ch[q]];
         double r = sqrt(pow(x - cn->c[0], 2) + pow(y - cn->c[1], 2));
         if (cn->region > g.theta * r) {
-          stack[++top] = ch[q];
+          stack[++top] = (int)ch[q];
         } else {
           m2s(z, &phi, cn);
           if (n_m2s) *n_m2s += 1;

@@ -75,7 +75,12 @@ def cases(refdir):
     return out
 
 
-def main(refdir="/root/reference"):
+def main(refdir=None):
+    """`refdir` (or $TREE2D_REF_ROOT) is the reference checkout, the directory
+    that holds ver-c/."""
+    refdir = refdir or os.environ.get("TREE2D_REF_ROOT")
+    if not refdir:
+        raise SystemExit("usage: make_golden.py <reference checkout>  (or set TREE2D_REF_ROOT)")
     drv = O.build_reference(os.path.join(refdir, "ver-c", "src"))
     if drv is None:
         raise SystemExit("reference sources not found")

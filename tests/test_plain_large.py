@@ -1,14 +1,36 @@
-"""Plain path at configuration sizes: against the oracle on sampled targets
-(1,048,576-blob Lamb-Oseen set, config 2) and, at 4,194,304 blobs
-(config 3), through size-independent properties of the tree and the
-accuracy the reference's method has against the FP64 direct sum."""
+"""Plain path at configuration sizes, against the oracle: the 1,048,576-blob
+Lamb-Oseen set (configuration 2) and the 4,194,304-blob two-patch + sheet
+set (configuration 3) -- whole tree bit for bit, sampled targets within the
+parity bar -- plus a cluster deeper than the dense oracle can hold, against
+the sparse restatement of the reference tree, and the accuracy the
+reference's method has against the FP64 direct sum."""
 from __future__ import annotations
+
+import os
 
 import numpy as np
 import pytest
 
 from conftest import oracle, workloads
-from test_plain_parity import assert_parity
+from test_plain_parity import assert_parity, ext_for
+
+
+def _mem_available_gb():
+    try:
+        with open("/proc/meminfo") as f:
+            for line in f:
+                if line.startswith("MemAvailable:"):
+                    return int(line.split()[1]) / 1e6
+    except OSError:
+        pass
+    return 0.0
+
+
+def assert_same_tree(d, od):
+    for k in ("perm", "level", "begin", "end", "leaf"):
+        assert np.array_equal(d[k], od[k]), k
+    for k in ("cx", "cy", "region"):
+        assert np.array_equal(d[k].view(np.uint64), od[k].view(np.uint64)), k
 
 
 @pytest.mark.gpu
@@ -25,12 +47,44 @@ def test_lamb_oseen_1m_against_oracle(gpu_lib):
     o = O.Oracle(b.nterms, b.num_p, b.theta)
     o.make_tree(b.xy, b.cir, b.cor)
     ref = o.biot(b.xy[idx])
-    assert_parity(uv, ref)
+    assert_parity(uv, ref, b.xy[idx], ext_for(b.xy, b.cir, b.cor, b.nterms, b.num_p, b.theta),
+                  label="lamb_oseen_1M")
     # the tree of the oracle and of the GPU agree cell for cell
+    assert_same_tree(P.export_tree(b.n, b.nterms), o.dump(b.n))
+
+
+@pytest.mark.gpu
+def test_two_patch_sheet_4m_against_oracle(gpu_lib):
+    """Configuration 3 at full size, 4,194,304 blobs and 14 levels: the
+    GPU's permutation and cells equal the oracle's (the reference's dense
+    tree restated) bit for bit, and 256 sampled targets meet the parity bar
+    against the oracle's traversal.  The dense tree takes about 20 GB of
+    host memory and a 1.4 GB traversal stack per thread, as the
+    reference's does."""
+    P = gpu_lib
+    W = workloads()
+    b = W.two_patch_sheet()
+    threads = max(1, min(8, os.cpu_count() or 1))
+    need = 22 + 1.5 * threads
+    if _mem_available_gb() < need:
+        pytest.skip(f"the dense oracle tree needs ~{need:.0f} GB of host memory")
+    P.set_params(b.nterms, b.num_p, b.theta)
+    P.set_mode(P.MODE_PLAIN)
+    P.make_tree(b.xy, b.cir, b.cor)
     d = P.export_tree(b.n, b.nterms)
+    idx = W.sample_targets(b.n, 256, seed=19)
+    uv = P.biot_tree_batch(b.xy[idx])
+    O = oracle()
+    o = O.Oracle(b.nterms, b.num_p, b.theta)
+    o.make_tree(b.xy, b.cir, b.cor, max_level_cap=20)
+    assert o.levels() == P.stats()["depth"]
     od = o.dump(b.n)
-    assert np.array_equal(d["perm"], od["perm"])
-    assert np.array_equal(d["begin"], od["begin"]) and np.array_equal(d["level"], od["level"])
+    assert_same_tree(d, od)
+    ref = o.biot(b.xy[idx], threads=threads)
+    del od
+    o.close()
+    assert_parity(uv, ref, b.xy[idx], ext_for(b.xy, b.cir, b.cor, b.nterms, b.num_p, b.theta),
+                  label="two_patch_sheet_4M")
 
 
 def check_tree_invariants(d, n, num_p):
@@ -85,8 +139,11 @@ def test_two_patch_sheet_4m_properties_and_accuracy(gpu_lib):
 @pytest.mark.gpu
 def test_deep_cluster_uses_full_key_depth(gpu_lib):
     """A cluster 1e-6 wide needs leaves below level 20: the build must fall
-    back from its short keys to the full 32 levels and still give a valid
-    tree and the treecode's accuracy against the FP64 direct sum."""
+    back from its short keys to the full 32 levels (the key digits below the
+    16-level centre table continue in FP64) and still give the reference's
+    tree bit for bit -- against the sparse restatement of the reference tree,
+    as the dense one cannot hold 20+ levels -- its velocities within the
+    parity bar, and the treecode's accuracy against the FP64 direct sum."""
     torch = pytest.importorskip("torch")
     P = gpu_lib
     rng = np.random.default_rng(17)
@@ -101,6 +158,12 @@ def test_deep_cluster_uses_full_key_depth(gpu_lib):
     d = P.export_tree(3000, 11)
     check_tree_invariants(d, 3000, 33)
     uv = P.biot_tree_batch(xy)
+    O = oracle()
+    s = O.SparseOracle(11, 33, 0.5)
+    s.make_tree(xy, cir, cor)
+    assert s.levels() == st["depth"]
+    assert_same_tree(d, s.dump(3000))
+    assert_parity(uv, s.biot(xy), xy, s.biot_ext, label="deep_cluster")
     dev = torch.device("cuda:0")
     t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)  # noqa: E731
     out = torch.empty((3000, 2), dtype=torch.float64, device=dev)

@@ -3,34 +3,86 @@ vectors from the reference built from its sources) and against the oracle.
 
 Bar (the drop-in contract): tree structure -- permutation, cell levels,
 ranges, leaf flags, centres and sides -- bit-exact; velocities within 1e-12
-relative per component, with an absolute floor of 1e-13 of the target's
-speed (|du| <= 1e-12 |u| + 1e-13 |(u,v)|), and within 1e-12 normwise;
+relative per component, |du| <= 1e-12 |u_ref|, and within 1e-12 normwise;
 coefficients within 1e-12 of each cell's norm.
 
-The floor exists because a component far below its target's speed is a
-cancellation residue: the reference computes every power with cpow
-(exp(k log z)), whose rounding (~1e-15 of each term) is then amplified by
-the cancellation.  Against an extended-precision evaluation of the same
-treecode the GPU's multiply/Horner form is about 3x closer than the
-reference itself, so the residue is the reference's.
+Some components cannot meet the per-component bar in FP64 at all: a
+component far below its target's speed is a cancellation residue, and the
+reference forms every power with cpow (exp(k log z)), whose rounding the
+cancellation amplifies.  Every component that misses the bar is therefore
+checked against the same treecode evaluated in extended precision
+(oracle/tree2d_sparse.c, ora_sp_biot_ext: the same accepted cells and pairs,
+long double arithmetic).  A miss is accepted only when the GPU's value is
+within the bar of that exact value (the reference's rounding caused the
+miss), or when the reference itself misses the bar against the exact value
+and the GPU is no farther from it than four times the reference is (the bar
+is out of FP64's reach there).  The counts and the worst cases are printed
+(`pytest -s`).
 """
 from __future__ import annotations
 
 import numpy as np
 import pytest
 
-from conftest import golden_names, load_golden, rel_err
+from conftest import golden_names, load_golden, oracle, rel_err
 
 TOL = 1e-12
-FLOOR = 1e-13
 
 
-def assert_parity(uv, ref):
+def assert_parity(uv, ref, txy=None, ext_of=None, label=""):
+    """Per-component parity of `uv` with the reference values `ref` at the
+    targets `txy`.  `ext_of(points)` returns the extended-precision treecode
+    value at those points (SparseOracle.biot_ext on the same blobs); without
+    it every component must meet the strict bar.  Returns the counts."""
+    uv = np.asarray(uv).reshape(-1, 2)
+    ref = np.asarray(ref).reshape(-1, 2)
     rel, nrm = rel_err(uv, ref)
-    mag = np.linalg.norm(ref, axis=1, keepdims=True)
-    ok = np.abs(uv - ref) <= TOL * np.abs(ref) + FLOOR * mag
-    assert nrm.max() <= TOL, f"normwise max {nrm.max():.3e}"
-    assert ok.all(), f"{(~ok).sum()} components beyond 1e-12|c| + 1e-13|uv| (worst rel {rel[~ok].max():.3e})"
+    assert np.isfinite(uv).all()
+    assert nrm.max() <= TOL, f"{label}: normwise max {nrm.max():.3e}"
+    miss = np.abs(uv - ref) > TOL * np.abs(ref)
+    rows = np.flatnonzero(miss.any(axis=1))
+    out = {"components": int(miss.size), "strict_misses": int(miss.sum()), "explained": 0}
+    if len(rows) == 0:
+        print(f"[parity] {label}: {miss.size} components, all within 1e-12 relative")
+        return out
+    assert ext_of is not None and txy is not None, \
+        f"{label}: {miss.sum()} components beyond 1e-12 relative (worst {rel[miss].max():.3e})"
+    ext = np.asarray(ext_of(np.asarray(txy).reshape(-1, 2)[rows])).reshape(-1, 2)
+    g, r = uv[rows], ref[rows]
+    m = miss[rows]
+    e_gpu = np.abs(g - ext)
+    e_ref = np.abs(r - ext)
+    gpu_exact = e_gpu <= TOL * np.abs(ext)
+    ref_off = e_ref > TOL * np.abs(ext)
+    ok = gpu_exact | (ref_off & (e_gpu <= 4 * e_ref))
+    bad = m & ~ok
+    out["explained"] = int((m & ok).sum())
+    mag = np.linalg.norm(ext, axis=1)
+    worst = np.argsort(-(np.abs(g - r) / np.maximum(np.abs(r), 1e-300) * m).max(axis=1))[:3]
+    lines = [f"target {rows[i]}: |u|/|uv| {np.abs(ext[i]).min() / mag[i]:.1e}, gpu-ref {rel[rows[i]].max():.1e}, "
+             f"gpu-exact {(e_gpu[i] / np.maximum(np.abs(ext[i]), 1e-300)).max():.1e}, "
+             f"ref-exact {(e_ref[i] / np.maximum(np.abs(ext[i]), 1e-300)).max():.1e}" for i in worst]
+    print(f"[parity] {label}: {miss.size} components, {int(m.sum())} beyond 1e-12 relative to the reference, "
+          f"{int((m & gpu_exact).sum())} of them within 1e-12 of the exact treecode value, "
+          f"{int((m & ~gpu_exact & ok).sum())} where the reference itself misses the exact value by more; "
+          f"worst: " + "; ".join(lines))
+    assert not bad.any(), f"{label}: {int(bad.sum())} components beyond the bar not explained by the reference's " \
+                          f"own rounding: " + "; ".join(lines)
+    return out
+
+
+def ext_for(xy, cir, cor, nterms, num_p, theta):
+    """Extended-precision treecode values on these blobs (the sparse oracle,
+    built on the first call)."""
+    state = {}
+
+    def ext(pts):
+        if "s" not in state:
+            state["s"] = oracle().SparseOracle(int(nterms), int(num_p), float(theta))
+            state["s"].make_tree(xy, cir, cor)
+        return state["s"].biot_ext(pts)
+
+    return ext
 
 
 def run_golden(P, g):
@@ -46,7 +98,8 @@ def test_velocity_matches_reference(gpu_lib, name):
     P = gpu_lib
     g = load_golden(name)
     uv = run_golden(P, g)
-    assert_parity(uv, g["uv"])
+    assert_parity(uv, g["uv"], g["txy"], ext_for(g["xy"], g["cir"], g["cor"], g["nterms"], g["num_p"], g["theta"]),
+                  label=name)
 
 
 @pytest.mark.gpu
