@@ -133,6 +133,8 @@ struct Solver {
   Tree tree;
   Arena mirror;   // blobs + images when a mirror wall is set
   bool plain_coef = false;  // FP64 coefficients present (plain upward ran)
+  bool mixed_ready = false; // the last solve was a mixed/learned one: its view, lists and
+                            // expansions are intact (off-blob points use them)
   Arena io;       // device copies of host inputs and outputs
   Arena targets;  // evaluation-order targets
   Arena lookup;   // query points and answers of a batch lookup
@@ -289,6 +291,7 @@ int solve_body(Lib &L, Solver &S, int n, const double *d_xy, const double *d_cir
   Params bp = L.params;
   if (L.mode != TREE2D_MODE_PLAIN) bp.num_p = mixed_leaf_blobs(L.mixed, n / (nsets > 0 ? nsets : 1), L.params.num_p) + 1;
   st.leaf_blobs = bp.num_p - 1;
+  S.mixed_ready = false;
   int rc = build_tree(ws, n, d_xy, d_cir, d_cor, bp, S.tree, s, d_set_off, nsets, cir_cor_ready);
   if (rc) return rc;
   T2D_CUDA_TRY(cudaEventRecord(ws.ev[1], s));
@@ -308,6 +311,7 @@ int solve_body(Lib &L, Solver &S, int n, const double *d_xy, const double *d_cir
     mp.lp_version = L.lp_version;
     rc = mixed_solve(ws, S.tree, mp, d_uv, s, st);
     if (rc) return rc;
+    S.mixed_ready = nsets <= 1;
   }
   T2D_CUDA_TRY(cudaEventRecord(ws.ev[3], s));
   T2D_CUDA_TRY(cudaMemcpyAsync(ws.h_status, ws.status, sizeof(DevStatus), cudaMemcpyDeviceToHost, s));
@@ -446,9 +450,11 @@ int eval_points(Lib &L, int m, const double *xy, double *uv) {
   int *out = S.targets.take<int>(m);
   T2D_CUDA_TRY(cudaMemcpyAsync(d_xy, xy, sizeof(double) * 2 * (size_t)m, cudaMemcpyHostToDevice, s));
   int rc;
-  if (!S.plain_coef) {
-    // Points off the blobs are answered by the plain FP64 treecode; after a
-    // mixed-mode make_tree its FP64 coefficients are formed on first need.
+  // Points off the blobs: after a plain make_tree the plain FP64 treecode
+  // (the reference's method); after a mixed or learned one a traversal of
+  // the mixed tree with its own expansions, to the mixed form's accuracy.
+  const bool mixed = S.mixed_ready;
+  if (!mixed && !S.plain_coef) {
     rc = plain_upward(S.ws, S.tree, L.params, s);
     if (rc) return rc;
     S.plain_coef = true;
@@ -462,7 +468,8 @@ int eval_points(Lib &L, int m, const double *xy, double *uv) {
   }
   if (rc) return rc;
   T2D_CUDA_TRY(cudaMemsetAsync(S.ws.status, 0, sizeof(DevStatus), s));
-  rc = plain_evaluate(S.ws, S.tree, L.params, m, tx, ty, out, d_uv, s);
+  rc = mixed ? mixed_eval_points(S.ws, m, tx, ty, out, d_uv, s)
+             : plain_evaluate(S.ws, S.tree, L.params, m, tx, ty, out, d_uv, s);
   if (rc) return rc;
   T2D_CUDA_TRY(cudaMemcpyAsync(uv, d_uv, sizeof(double) * 2 * (size_t)m, cudaMemcpyDeviceToHost, s));
   T2D_CUDA_TRY(cudaMemcpyAsync(S.ws.h_status, S.ws.status, sizeof(DevStatus), cudaMemcpyDeviceToHost, s));

@@ -1431,6 +1431,132 @@ __global__ void __launch_bounds__(32 * kWarps, 32 / kWarps) k_eval_mixed(MixedVi
   if (lane == 0) atomicAdd(&m.st->n_pairs, pairs);
 }
 
+// ------------------------------------------------------------ off-blob points
+
+// Velocity at arbitrary points (not blob positions) on a mixed tree: one
+// warp per 32 points (in key order), each lane one point, the warp walking
+// the union of its lanes' traversals (a LIFO of cells with the lanes still
+// inside each).  A lane accepts a cell's multipole when the point is at
+// least kPtMac cell sides from the cell's centre (the scaled FP32 multipole
+// of order P then truncates at (sqrt(2)/2 / kPtMac)^P = 0.283^16 = 2e-9 of
+// the cell's field) and farther than the correction radius rc from the
+// cell's box (so the point-vortex form leaves out only exp(-rc^2/s^2)
+// terms, as the near field's correction list does).  Other cells are
+// descended; leaves are summed pair by pair with the regularised kernel
+// (fmm.c:121-142, the near field's FP32 pair), each leaf in FP32 and added
+// in FP64.  Cells without a multipole (the root and the level-1 cells above
+// the upward pass) are always descended.  The FP64 point is offset from
+// each cell's FP64 centre before rounding to FP32, as the near field's
+// centre offsets are.
+constexpr int kPtWarps = 4;
+constexpr int kPtStack = 160;
+constexpr double kPtMac = 2.5;
+
+__global__ void __launch_bounds__(kPtWarps * 32) k_eval_points(MixedView m, int ntgt, const double *tx,
+                                                               const double *ty, const int *out_idx, double *uv) {
+  __shared__ int s_cell[kPtWarps][kPtStack];
+  __shared__ unsigned s_mask[kPtWarps][kPtStack];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const long i = ((long)blockIdx.x * kPtWarps + warp) * 32 + lane;
+  const bool valid = i < ntgt;
+  const unsigned vmask = __ballot_sync(0xffffffffu, valid);
+  if (vmask == 0) return;
+  const double x = valid ? tx[i] : 0.0, y = valid ? ty[i] : 0.0;
+  const double rc = (double)*m.rc_ptr, rc2 = rc * rc;
+  const double mac2 = kPtMac * kPtMac;
+  const int P = m.P;
+  double phx = 0.0, phy = 0.0, ax = 0.0, ay = 0.0;
+  unsigned long long n_m2p = 0, n_pairs = 0;
+  bool overflow = false;
+  int top = 0;
+  if (lane == 0) {
+    s_cell[warp][0] = 0;
+    s_mask[warp][0] = vmask;
+  }
+  __syncwarp();
+  while (top >= 0) {
+    const int c = s_cell[warp][top];
+    const unsigned msk = s_mask[warp][top];
+    __syncwarp();
+    top--;
+    const bool act = (msk >> lane) & 1u;
+    const bool is_leaf = m.leaf[c] != 0;
+    const bool has_mp = is_leaf || m.level[c] >= 2 + m.lev0;
+    bool far = false;
+    double dx = 0.0, dy = 0.0;
+    if (act && c != 0) {
+      dx = x - m.cx[c];
+      dy = y - m.cy[c];
+      const double side = m.region[c];
+      const double gx = fmax(fabs(dx) - 0.5 * side, 0.0), gy = fmax(fabs(dy) - 0.5 * side, 0.0);
+      far = has_mp && dx * dx + dy * dy >= mac2 * side * side && gx * gx + gy * gy > rc2;
+    }
+    if (far) {
+      // M2P: phi = (1/h) sum_k M_k w^(k+1), w = h / (z - zc)
+      const float ih = m.inv_h[c];
+      const float zx = __fmul_rn((float)dx, ih), zy = __fmul_rn((float)dy, ih);
+      const float ir2 = __fdiv_rn(1.f, fmaf(zx, zx, __fmul_rn(zy, zy)));
+      const float2 w = make_float2(__fmul_rn(zx, ir2), -__fmul_rn(zy, ir2));
+      const float *MA = m.M + (size_t)c * 2 * P;
+      float2 a = make_float2(MA[P - 1], MA[2 * P - 1]);
+      for (int k = P - 2; k >= 0; k--) {
+        a = fmul(a, w);
+        a.x = __fadd_rn(a.x, MA[k]);
+        a.y = __fadd_rn(a.y, MA[P + k]);
+      }
+      a = fmul(a, w);
+      phx += (double)__fmul_rn(a.x, ih);
+      phy += (double)__fmul_rn(a.y, ih);
+      n_m2p++;
+    }
+    if (is_leaf) {
+      if (act && !far) {
+        const float fx = (float)dx, fy = (float)dy;
+        float sx = 0.f, sy = 0.f;
+        for (int j = m.begin[c]; j < m.end[c]; j++) pair<false>(m.src4[j], fx, fy, sx, sy);
+        ax += (double)sx;
+        ay += (double)sy;
+        n_pairs += (unsigned long long)(m.end[c] - m.begin[c]);
+      }
+    } else {
+      const unsigned dmask = __ballot_sync(0xffffffffu, act && !far);
+      if (dmask) {
+        const int4 ch = reinterpret_cast<const int4 *>(m.child)[c];
+        for (int q = 3; q >= 0; q--) {
+          const int cc = (&ch.x)[q];
+          if (cc < 0) continue;
+          if (top + 1 >= kPtStack) {
+            overflow = true;
+            break;
+          }
+          top++;
+          if (lane == 0) {
+            s_cell[warp][top] = cc;
+            s_mask[warp][top] = dmask;
+          }
+        }
+      }
+      __syncwarp();
+      if (overflow) break;  // warp-uniform
+    }
+  }
+  if (overflow && lane == 0) set_err(m.st, TREE2D_ERR_TIMEOUT);
+  if (valid) {
+    const double inv2pi = 0.15915494309189533577;
+    const long o = out_idx ? out_idx[i] : i;
+    uv[2 * o] = overflow ? NAN : (phy + ax) * inv2pi;
+    uv[2 * o + 1] = overflow ? NAN : (phx + ay) * inv2pi;
+  }
+  for (int o = 16; o; o >>= 1) {
+    n_m2p += __shfl_xor_sync(0xffffffffu, n_m2p, o);
+    n_pairs += __shfl_xor_sync(0xffffffffu, n_pairs, o);
+  }
+  if (lane == 0) {
+    atomicAdd(&m.st->n_m2s, n_m2p);
+    atomicAdd(&m.st->n_pairs, n_pairs);
+  }
+}
+
 // ------------------------------------------------------------ host side
 
 double binom_d(int n, int k) {
@@ -1693,6 +1819,17 @@ int near_field(Workspace &ws, const MixedParams &mp, MixedView &m, bool learned,
   if (v < 0 || v >= kEvalVariants) v = 0;
   T2D_CUDA_TRY(run(v));
   st.eval_variant = v;
+  return TREE2D_OK;
+}
+
+int mixed_eval_points(Workspace &ws, int ntgt, const double *tx, const double *ty, const int *out_idx, double *uv,
+                      cudaStream_t s) {
+  if (ntgt <= 0) return TREE2D_OK;
+  if (!ws.mxv) return TREE2D_ERR_NO_TREE;
+  const int warps = (ntgt + 31) / 32;
+  k_eval_points<<<(warps + kPtWarps - 1) / kPtWarps, kPtWarps * 32, 0, s>>>(*ws.mxv, ntgt, tx, ty, out_idx, uv);
+  g_launches.fetch_add(1, std::memory_order_relaxed);
+  T2D_CUDA_TRY(cudaGetLastError());
   return TREE2D_OK;
 }
 

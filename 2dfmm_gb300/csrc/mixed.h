@@ -87,4 +87,13 @@ void m2l_b_images(int P, const float *h_m2l, std::vector<float> &img);
 int mixed_solve(Workspace &ws, const Tree &t, const MixedParams &mp, double *d_uv, cudaStream_t s,
                 tree2d_stats_t &st);
 
+// Velocity at ntgt arbitrary points (tx, ty, FP64, device; in key order for
+// warp coherence) against the last mixed solve of `ws` (its view, lists and
+// expansions must be intact): uv[2 * out_idx[i]] (out_idx may be null).  A
+// per-point traversal that accepts a cell's multipole only far from the
+// point (2.5 cell sides, beyond the correction radius) and sums the rest
+// pair by pair, for points that are not blob positions.
+int mixed_eval_points(Workspace &ws, int ntgt, const double *tx, const double *ty, const int *out_idx, double *uv,
+                      cudaStream_t s);
+
 }  // namespace t2d

@@ -100,7 +100,7 @@ def lib():
             L.ora_sp_levels.restype = ctypes.c_int
             L.ora_sp_num_nodes.restype = ctypes.c_long
             L.ora_sp_biot_many.argtypes = [ctypes.c_int, _dp, _dp, ctypes.c_int, _lp, _lp]
-            L.ora_sp_biot_ext.argtypes = [ctypes.c_int, _dp, _dp, ctypes.c_int]
+            L.ora_sp_biot_ext.argtypes = [ctypes.c_int, _dp, _dp, _dp, ctypes.c_int]
             L.ora_sp_dump_tree.argtypes = [_ip, ctypes.c_long, _ip, _ip, _ip, _ip, _dp, _dp, _dp, _dp]
             L.ora_sp_dump_tree.restype = ctypes.c_long
             _lib = L
@@ -205,13 +205,16 @@ class SparseOracle:
         self.L.ora_sp_biot_many(len(txy), _p(txy), _p(uv), threads, ctypes.byref(a), ctypes.byref(b))
         return (uv, a.value, b.value) if counters else uv
 
-    def biot_ext(self, txy, threads: int = 0):
+    def biot_ext(self, txy, threads: int = 0, cond: bool = False):
         """The same treecode (same accepted cells and pairs) evaluated in
-        extended precision: its value to far below FP64 rounding."""
+        extended precision: its value to far below FP64 rounding.  With
+        cond=True also the sum of its contributions' magnitudes per target
+        (the scale of any FP64 evaluation's rounding error)."""
         txy = _f64(txy).reshape(-1, 2)
         uv = np.empty_like(txy)
-        self.L.ora_sp_biot_ext(len(txy), _p(txy), _p(uv), threads)
-        return uv
+        c = np.empty(len(txy))
+        self.L.ora_sp_biot_ext(len(txy), _p(txy), _p(uv), _p(c), threads)
+        return (uv, c) if cond else uv
 
     def dump(self, n: int):
         nc = self.L.ora_sp_dump_tree(None, 0, None, None, None, None, None, None, None, None)

@@ -373,9 +373,10 @@ static void sp_make_ext(void) {
   S.have_ext = 1;
 }
 
-static void sp_biot_ext_one(double x, double y, double *u, double *v) {
+static void sp_biot_ext_one(double x, double y, double *u, double *v, double *cond) {
   ldc phi = 0.0L;
   long double axs = 0.0L, ays = 0.0L;
+  long double mag = 0.0L; /* sum of the contributions' magnitudes */
   const ldc z = (long double)x + (long double)y * I;
   long cap = 64, top = 0;
   long *stack = (long *)malloc(sizeof(long) * (size_t)cap);
@@ -398,6 +399,7 @@ static void sp_biot_ext_one(double x, double y, double *u, double *v) {
           long double rv = (long double)S.cir[b] * (1.0L - expl(-xai2));
           axs -= rv * ly / r2;
           ays += rv * lx / r2;
+          mag += fabsl(rv) / sqrtl(r2);
         }
       }
     } else {
@@ -416,6 +418,7 @@ static void sp_biot_ext_one(double x, double y, double *u, double *v) {
           ldc wk = w;
           for (int k = 0; k < S.nterms - 1; k++) {
             phi += wk * cn->ae[k];
+            mag += cabsl(wk * cn->ae[k]);
             wk *= w;
           }
         }
@@ -426,11 +429,16 @@ static void sp_biot_ext_one(double x, double y, double *u, double *v) {
   const long double pi = 3.141592653589793238462643383279502884L;
   *u = (double)((cimagl(phi) + axs) / (2.0L * pi));
   *v = (double)((creall(phi) + ays) / (2.0L * pi));
+  if (cond) *cond = (double)(mag / (2.0L * pi));
 }
 
 /* The treecode's value at n targets in extended precision (see the file
- * header); uv interleaved, rounded to FP64 at the end. */
-void ora_sp_biot_ext(int n, const double *xy, double *uv, int threads) {
+ * header); uv interleaved, rounded to FP64 at the end.  cond (may be NULL)
+ * receives per target the sum of the magnitudes of all its contributions
+ * (M2S terms and pairs, over 2 pi): the scale of the rounding error any FP64
+ * evaluation of the sum carries, which a cancelling component can be far
+ * below. */
+void ora_sp_biot_ext(int n, const double *xy, double *uv, double *cond, int threads) {
   if (!S.node) {
     for (int i = 0; i < 2 * n; i++) uv[i] = NAN;
     return;
@@ -440,7 +448,8 @@ void ora_sp_biot_ext(int n, const double *xy, double *uv, int threads) {
   if (threads <= 0) threads = omp_get_max_threads();
 #pragma omp parallel for schedule(dynamic, 4) num_threads(threads)
 #endif
-  for (int i = 0; i < n; i++) sp_biot_ext_one(xy[2 * i], xy[2 * i + 1], &uv[2 * i], &uv[2 * i + 1]);
+  for (int i = 0; i < n; i++)
+    sp_biot_ext_one(xy[2 * i], xy[2 * i + 1], &uv[2 * i], &uv[2 * i + 1], cond ? &cond[i] : NULL);
   (void)threads;
 }
 

@@ -81,7 +81,7 @@ def test_extended_precision_value_of_the_treecode(name):
     # every such component is a small fraction of its target's speed
     assert (np.abs(ext)[misses] < 0.05 * np.repeat(mag[:, None], 2, axis=1)[misses]).all()
     # the reference itself passes the checker (against itself, trivially)
-    assert_parity(ref, ref, g["txy"], s.biot_ext, label=name)
+    assert_parity(ref, ref, g["txy"], lambda pts: s.biot_ext(pts, cond=True), label=name)
 
 
 def test_checker_catches_planted_errors():
@@ -98,7 +98,7 @@ def test_checker_catches_planted_errors():
     k = int(np.argmax(np.abs(ref[:, 0])))  # a large component, far from cancellation
     bad[k, 0] *= 1 + 1e-10
     with pytest.raises(AssertionError, match="normwise"):
-        assert_parity(bad, ref, g["txy"], s.biot_ext, label="planted")
+        assert_parity(bad, ref, g["txy"], lambda pts: s.biot_ext(pts, cond=True), label="planted")
     ext = s.biot_ext(g["txy"])
     frac = np.abs(ref[:, 1]) / np.linalg.norm(ref, axis=1)
     ok = np.abs(ref[:, 1] - ext[:, 1]) <= 1e-13 * np.abs(ext[:, 1])
@@ -106,4 +106,4 @@ def test_checker_catches_planted_errors():
     bad = ref.copy()
     bad[k, 1] *= 1 + 5e-11
     with pytest.raises(AssertionError, match="not explained"):
-        assert_parity(bad, ref, g["txy"], s.biot_ext, label="planted")
+        assert_parity(bad, ref, g["txy"], lambda pts: s.biot_ext(pts, cond=True), label="planted")

@@ -163,7 +163,7 @@ def test_deep_cluster_uses_full_key_depth(gpu_lib):
     s.make_tree(xy, cir, cor)
     assert s.levels() == st["depth"]
     assert_same_tree(d, s.dump(3000))
-    assert_parity(uv, s.biot(xy), xy, s.biot_ext, label="deep_cluster")
+    assert_parity(uv, s.biot(xy), xy, lambda pts: s.biot_ext(pts, cond=True), label="deep_cluster")
     dev = torch.device("cuda:0")
     t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)  # noqa: E731
     out = torch.empty((3000, 2), dtype=torch.float64, device=dev)
