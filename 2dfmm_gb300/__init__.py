@@ -53,6 +53,7 @@ class Stats(ctypes.Structure):
         ("n_launches", ctypes.c_longlong), ("m2l_path", ctypes.c_int), ("eval_variant", ctypes.c_int),
         ("learned_active", ctypes.c_int), ("n_list_u", ctypes.c_longlong), ("n_list_k", ctypes.c_longlong),
         ("leaf_blobs", ctypes.c_int), ("n_list_k_blobs", ctypes.c_longlong),
+        ("n_pairs_k", ctypes.c_longlong), ("n_pairs_k_listed", ctypes.c_longlong),
     ]
 
     def as_dict(self):

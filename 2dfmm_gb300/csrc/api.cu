@@ -292,7 +292,10 @@ int solve_body(Lib &L, Solver &S, int n, const double *d_xy, const double *d_cir
   if (L.mode != TREE2D_MODE_PLAIN) bp.num_p = mixed_leaf_blobs(L.mixed, n / (nsets > 0 ? nsets : 1), L.params.num_p) + 1;
   st.leaf_blobs = bp.num_p - 1;
   S.mixed_ready = false;
-  int rc = build_tree(ws, n, d_xy, d_cir, d_cor, bp, S.tree, s, d_set_off, nsets, cir_cor_ready);
+  // the plain form keeps the reference's in-leaf order (parity); the mixed
+  // forms keep the key order, which their correction cull needs
+  int rc = build_tree(ws, n, d_xy, d_cir, d_cor, bp, S.tree, s, d_set_off, nsets, cir_cor_ready,
+                      L.mode == TREE2D_MODE_PLAIN);
   if (rc) return rc;
   T2D_CUDA_TRY(cudaEventRecord(ws.ev[1], s));
   S.plain_coef = false;
@@ -323,6 +326,8 @@ int solve_body(Lib &L, Solver &S, int n, const double *d_xy, const double *d_cir
   st.depth = S.tree.depth;
   st.n_m2s = (long long)ws.h_status->n_m2s;
   st.n_pairs = (long long)ws.h_status->n_pairs;
+  st.n_pairs_k = (long long)ws.h_status->n_pairs_k;
+  st.n_pairs_k_listed = (long long)ws.h_status->n_pairs_k_listed;
   st.n_m2l = (long long)ws.h_status->n_m2l;
   st.ms_build = elapsed(ws.ev[0], ws.ev[1]);
   if (L.mode == TREE2D_MODE_PLAIN) {

@@ -78,6 +78,8 @@ struct DevStatus {
   int list_overflow;       // mixed: a leaf's lists did not fit the one-walk scratch
   int list_max;            // mixed: most list entries (U + W + K) of one leaf
   unsigned long long k_blobs;  // mixed: source blobs of the K leaves of all leaves, out to the walk radius
+  unsigned long long n_pairs_k;   // mixed: correction pairs evaluated (part of n_pairs)
+  unsigned long long n_pairs_k_listed;  // mixed: correction pairs of the K entries evaluated, before the chunk cull
 };
 
 // Bump allocator over one device allocation.  Buffers are 256-byte aligned.
@@ -143,6 +145,9 @@ struct Tree {
   const int *set_off = nullptr;   // batched: device offsets of the sets (nsets + 1)
   const double *set_cor = nullptr;  // batched: core radii in input order (valid during the solve)
   int lev0 = 0;                   // batched: levels of container cells above the set roots
+  int leaf_cap = 0;               // most blobs a leaf can hold (num_p - 1 of the build)
+  bool ref_leaf_order = true;     // blobs inside a leaf in ascending original index (the
+                                  // reference's order); false: in key order (spatially compact)
 };
 
 // Per-solver working state (one per library instance).
@@ -184,9 +189,13 @@ cudaError_t workspace_init(Workspace &ws);
 // `cir_cor_ready`, when given, is an event the stream waits for before the
 // circulations and core radii are first read (the positions must be ready
 // when the call is made); the caller may still be uploading them.
+// `ref_leaf_order`: blobs inside each leaf in ascending original index, as
+// the reference buckets them (the plain form's parity needs it); false keeps
+// them in key order, so that consecutive blobs of a leaf are close together
+// (the mixed forms cull their correction pairs by 32-blob chunks).
 int build_tree(Workspace &ws, int n, const double *d_xy, const double *d_cir, const double *d_cor,
                const Params &p, Tree &t, cudaStream_t s, const int *d_set_off = nullptr, int nsets = 1,
-               cudaEvent_t cir_cor_ready = nullptr);
+               cudaEvent_t cir_cor_ready = nullptr, bool ref_leaf_order = true);
 // Bytes build_tree reserves in ws.blob_arena and ws.tmp_arena for n blobs in
 // nsets sets (what a caller with fixed arenas must provide).
 size_t build_blob_bytes(int n, int nsets);

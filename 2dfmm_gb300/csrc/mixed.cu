@@ -146,16 +146,33 @@ __global__ void k_leaf_setup(MixedView m, const double *x, const double *y, cons
   if (wid >= m.nleaf) return;
   const int c = m.leaf_cell[wid];
   const double cx = m.cx[c], cy = m.cy[c];
-  for (int i = m.begin[c] + lane; i < m.end[c]; i += 32) {
-    m.leaf_of[i] = c;
-    m.loc[i] = make_float2((float)(x[i] - cx), (float)(y[i] - cy));
-    m.gam[i] = (float)cir[i];
-    // 1/sigma^2 is only kept in FP32, so it is formed in FP32 (the FP64
-    // divide is slow on this GPU and buys nothing after the rounding)
-    const float sf = (float)cor[i];
-    const float w = 1.f / (sf * sf);
-    m.s2inv[i] = w;
-    m.src4[i] = make_float4(m.loc[i].x, m.loc[i].y, m.gam[i], -1.44269504f * w);
+  const int b = m.begin[c], e = m.end[c];
+  for (int i0 = b; i0 < e; i0 += 32) {  // warp-uniform: one 32-blob chunk per round
+    const int i = i0 + lane;
+    float2 lc = make_float2(0.f, 0.f);
+    const bool v = i < e;
+    if (v) {
+      m.leaf_of[i] = c;
+      lc = make_float2((float)(x[i] - cx), (float)(y[i] - cy));
+      m.loc[i] = lc;
+      m.gam[i] = (float)cir[i];
+      // 1/sigma^2 is only kept in FP32, so it is formed in FP32 (the FP64
+      // divide is slow on this GPU and buys nothing after the rounding)
+      const float sf = (float)cor[i];
+      const float w = 1.f / (sf * sf);
+      m.s2inv[i] = w;
+      m.src4[i] = make_float4(lc.x, lc.y, m.gam[i], -1.44269504f * w);
+    }
+    // the chunk's bounding box, for the near field's correction cull
+    float x0 = v ? lc.x : INFINITY, y0 = v ? lc.y : INFINITY, x1 = v ? lc.x : -INFINITY, y1 = v ? lc.y : -INFINITY;
+    for (int o = 16; o; o >>= 1) {
+      x0 = fminf(x0, __shfl_xor_sync(0xffffffffu, x0, o));
+      y0 = fminf(y0, __shfl_xor_sync(0xffffffffu, y0, o));
+      x1 = fmaxf(x1, __shfl_xor_sync(0xffffffffu, x1, o));
+      y1 = fmaxf(y1, __shfl_xor_sync(0xffffffffu, y1, o));
+    }
+    const int k = (i0 - b) >> 5;
+    if (lane == 0 && k < m.kchunks) m.cbox[(size_t)c * m.kchunks + k] = make_float4(x0, y0, x1, y1);
   }
 }
 
@@ -1204,6 +1221,122 @@ struct Decisions {
   int margin;
 };
 
+// Correction radius of leaf cell B: the tree's, or in a batched tree its
+// set's (the same rule as the list walk, k_lists).
+__device__ __forceinline__ float leaf_cutoff(const MixedView &m, int B) {
+  float rc = *m.rc_ptr;
+  if (m.rc_set) {
+    const int sh = m.level[B] - m.lev0;
+    const unsigned tx = m.ix[B] >> sh, ty = m.iy[B] >> sh;
+    rc = m.rc_set[(ty >> 1) * (1u << (m.lev0 - 1)) + (tx >> 1)];
+  }
+  return rc;
+}
+
+// Bounding box {xmin, ymin, xmax, ymax} of the warp's targets (offsets za,
+// zb of the valid ones from the target leaf's centre) and the squared
+// correction radius, written to the warp's 5 floats of shared memory `tb`
+// (kept out of registers: the pair loop needs them all).
+__device__ __forceinline__ void target_box(float2 za, bool va, float2 zb, bool vb, float rc, float *tb, int lane) {
+  float x0 = INFINITY, y0 = INFINITY, x1 = -INFINITY, y1 = -INFINITY;
+  if (va) x0 = fminf(x0, za.x), y0 = fminf(y0, za.y), x1 = fmaxf(x1, za.x), y1 = fmaxf(y1, za.y);
+  if (vb) x0 = fminf(x0, zb.x), y0 = fminf(y0, zb.y), x1 = fmaxf(x1, zb.x), y1 = fmaxf(y1, zb.y);
+  for (int o = 16; o; o >>= 1) {
+    x0 = fminf(x0, __shfl_xor_sync(0xffffffffu, x0, o));
+    y0 = fminf(y0, __shfl_xor_sync(0xffffffffu, y0, o));
+    x1 = fmaxf(x1, __shfl_xor_sync(0xffffffffu, x1, o));
+    y1 = fmaxf(y1, __shfl_xor_sync(0xffffffffu, y1, o));
+  }
+  if (lane == 0) {
+    tb[0] = x0;
+    tb[1] = y0;
+    tb[2] = x1;
+    tb[3] = y1;
+    tb[4] = __fmul_rn(rc, rc);
+  }
+  __syncwarp();
+}
+
+constexpr unsigned kAllChunks = 0xffffffffu;
+
+// Pair counters of one warp, kept in shared memory by lane 0 (every count
+// but the targets' is warp-uniform): evaluated pairs, correction pairs
+// evaluated, correction pairs listed, per target slot of the current chunk
+// of targets, then summed over chunks times the chunk's targets.
+struct WarpCounts {
+  unsigned chunk[3];
+  unsigned long long total[3];
+};
+
+__device__ __forceinline__ void counts_add(WarpCounts *c, int lane, unsigned done, unsigned done_k, unsigned listed) {
+  if (lane == 0) {
+    c->chunk[0] += done;
+    c->chunk[1] += done_k;
+    c->chunk[2] += listed;
+  }
+}
+
+// Closes a chunk of targets; all lanes call it.
+__device__ __forceinline__ void counts_close(WarpCounts *c, int lane, bool va, bool vb) {
+  const unsigned nt = __popc(__ballot_sync(0xffffffffu, va)) + __popc(__ballot_sync(0xffffffffu, vb));
+  if (lane == 0)
+    for (int k = 0; k < 3; k++) {
+      c->total[k] += (unsigned long long)c->chunk[k] * nt;
+      c->chunk[k] = 0;
+    }
+  __syncwarp();
+}
+
+__device__ __forceinline__ void counts_flush(WarpCounts *c, int lane, DevStatus *st) {
+  if (lane == 0) {
+    atomicAdd(&st->n_pairs, c->total[0]);
+    atomicAdd(&st->n_pairs_k, c->total[1]);
+    atomicAdd(&st->n_pairs_k_listed, c->total[2]);
+  }
+}
+
+// The next run of consecutive kept chunks of mask r: blobs [s0, s1) of a
+// leaf of cnt blobs; the run is removed from r.  kAllChunks is the whole
+// leaf.
+__device__ __forceinline__ void next_run(unsigned &r, int cnt, int &s0, int &s1) {
+  if (r == kAllChunks) {
+    s0 = 0;
+    s1 = cnt;
+    r = 0;
+    return;
+  }
+  const int a = __ffs(r) - 1;
+  const unsigned gap = ~(r >> a);
+  const int len = gap ? __ffs(gap) - 1 : 32 - a;
+  s0 = a << 5;
+  s1 = min(cnt, (a + len) << 5);
+  r = a + len >= 32 ? 0u : r & ~(((1u << len) - 1u) << a);
+}
+
+// Chunks of correction source leaf A whose pairs with the warp's targets
+// can lie within the correction radius: bit k for the 32-blob chunk k of A
+// whose bounding box comes within rc of the targets' box (offset by
+// (ox, oy), A's centre seen from the target leaf).  Pairs farther than rc
+// from every target add terms below exp(-rc^2/sigma^2) of a point vortex:
+// the ones the correction list already leaves out beyond rc.  A leaf of
+// more than 32 chunks is not culled (kAllChunks).  Warp-uniform.
+__device__ __forceinline__ unsigned chunk_mask(const MixedView &m, int A, float ox, float oy, const float *tb,
+                                               int lane) {
+  const int nch = (m.end[A] - m.begin[A] + 31) >> 5;
+  if (nch > 32 || nch > m.kchunks) return kAllChunks;
+  bool keep = false;
+  if (lane < nch) {
+    const float4 T = make_float4(tb[0], tb[1], tb[2], tb[3]);
+    const float rc2 = tb[4];
+    const float4 s = m.cbox[(size_t)A * m.kchunks + lane];
+    // the targets' box in A's frame: T + (ox, oy)
+    const float gx = fmaxf(fmaxf(__fsub_rn(s.x, __fadd_rn(T.z, ox)), __fsub_rn(__fadd_rn(T.x, ox), s.z)), 0.f);
+    const float gy = fmaxf(fmaxf(__fsub_rn(s.y, __fadd_rn(T.w, oy)), __fsub_rn(__fadd_rn(T.y, oy), s.w)), 0.f);
+    keep = fmaf(gx, gx, __fmul_rn(gy, gy)) <= rc2;
+  }
+  return __ballot_sync(0xffffffffu, keep);
+}
+
 // Near field of every leaf: one warp per target leaf, two targets per lane.
 // The warp walks its direct entries (U list, then K list; in the learned
 // form the entries the network accepted are M2P'd first and skipped here)
@@ -1221,6 +1354,8 @@ __global__ void __launch_bounds__(32 * kWarps, 32 / kWarps) k_eval_staged(MixedV
                                                                            Decisions dec, long wait_limit) {
   __shared__ __align__(128) float4 s_src[kWarps][2][kStage];
   __shared__ __align__(8) uint64_t s_bar[kWarps][2];
+  __shared__ float s_tb[kWarps][5];  // target box and rc^2 of the warp's chunk
+  __shared__ WarpCounts s_cnt[kWarps];
   const int warp = threadIdx.x >> 5;
   const int l = blockIdx.x * kWarps + warp, lane = threadIdx.x & 31;
   if (l >= m.nleaf) return;  // uniform over the warp; nothing below syncs the block
@@ -1236,18 +1371,16 @@ __global__ void __launch_bounds__(32 * kWarps, 32 / kWarps) k_eval_staged(MixedV
   bool staging = true;    // false after a wait gave up
   const int B = m.leaf_cell[l];
   const double inv2pi = 0.15915494309189533577;
-  unsigned long long pairs = 0;
   const int u0 = m.u_off[l], nu = m.u_off[l + 1] - u0;
   const int k0 = m.k_off[l], nk = m.k_off[l + 1] - k0;
+  float *tbox = s_tb[warp];
+  WarpCounts *cnts = &s_cnt[warp];
+  if (lane == 0) *cnts = WarpCounts{};
   // position q of the walk: U entries, then K entries
   auto src_leaf = [&](int q) { return q < nu ? m.u_idx[u0 + q] : m.k_idx[k0 + q - nu]; };
   auto direct = [&](int q) {
     if (!kLearned) return true;
     return (q < nu ? dec.u[u0 + q] : dec.k[k0 + q - nu]) == 0;
-  };
-  auto next_direct = [&](int q) {
-    while (q < nu + nk && !direct(q)) q++;
-    return q;
   };
   // copy source leaf of position q into buffer b (warp-uniform decision)
   auto stage = [&](int q, int b) {
@@ -1268,8 +1401,28 @@ __global__ void __launch_bounds__(32 * kWarps, 32 / kWarps) k_eval_staged(MixedV
     const bool two = __any_sync(0xffffffffu, vb);
     const float2 za = va ? m.loc[ta] : make_float2(0.f, 0.f);
     const float2 zb = vb ? m.loc[tb] : make_float2(0.f, 0.f);
+    target_box(za, va, zb, vb, leaf_cutoff(m, B), tbox, lane);
+    // the next entry with work for these targets: a direct entry, and for a
+    // correction entry at least one chunk within rc (msk: its chunks, all
+    // for a U entry); culled correction entries are counted and skipped
+    auto next_work = [&](int q, unsigned &msk) {
+      for (; q < nu + nk; q++) {
+        if (!direct(q)) continue;
+        if (q < nu) {
+          msk = kAllChunks;
+          return q;
+        }
+        const int A = m.k_idx[k0 + q - nu];
+        msk = chunk_mask(m, A, centre_offset(m.cxf, m.cxl, B, A), centre_offset(m.cyf, m.cyl, B, A), tbox, lane);
+        if (msk) return q;
+        counts_add(cnts, lane, 0u, 0u, (unsigned)(m.end[A] - m.begin[A]));
+      }
+      msk = 0;
+      return q;
+    };
     float2 pa = make_float2(0.f, 0.f), pb = make_float2(0.f, 0.f);
-    int q = next_direct(0);
+    unsigned msk = 0;
+    int q = next_work(0, msk);
     int buf = 0;
     bool staged = q < nu + nk && stage(q, buf);
     if (two)
@@ -1294,7 +1447,8 @@ __global__ void __launch_bounds__(32 * kWarps, 32 / kWarps) k_eval_staged(MixedV
     float axa = 0.f, aya = 0.f, cxa = 0.f, cya = 0.f;
     float axb = 0.f, ayb = 0.f, cxb = 0.f, cyb = 0.f;
     while (q < nu + nk) {
-      const int qn = next_direct(q + 1);
+      unsigned msk_next = 0;
+      const int qn = next_work(q + 1, msk_next);
       const bool staged_next = qn < nu + nk && stage(qn, buf ^ 1);
       const int A = src_leaf(q);
       // offset of the source leaf's centre from the two-float centres: FP32
@@ -1314,27 +1468,29 @@ __global__ void __launch_bounds__(32 * kWarps, 32 / kWarps) k_eval_staged(MixedV
       }
       float sxa = 0.f, sya = 0.f, sxb = 0.f, syb = 0.f;
       const float txa = __fadd_rn(za.x, ox), tya = __fadd_rn(za.y, oy), txb = __fadd_rn(zb.x, ox), tyb = __fadd_rn(zb.y, oy);
-      if (q < nu) {
-        if (use_smem)
-          leaf_pairs<false>(s_src[warp][buf], 0, cnt, txa, tya, txb, tyb, two, sxa, sya, sxb, syb);
+      const float4 *src = use_smem ? s_src[warp][buf] : m.src4 + j0;
+      int done = 0;
+      for (unsigned r = msk; r;) {
+        int s0, s1;
+        next_run(r, cnt, s0, s1);
+        if (q < nu)
+          leaf_pairs<false>(src, s0, s1, txa, tya, txb, tyb, two, sxa, sya, sxb, syb);
         else
-          leaf_pairs<false>(m.src4 + j0, 0, cnt, txa, tya, txb, tyb, two, sxa, sya, sxb, syb);
-      } else {
-        if (use_smem)
-          leaf_pairs<true>(s_src[warp][buf], 0, cnt, txa, tya, txb, tyb, two, sxa, sya, sxb, syb);
-        else
-          leaf_pairs<true>(m.src4 + j0, 0, cnt, txa, tya, txb, tyb, two, sxa, sya, sxb, syb);
+          leaf_pairs<true>(src, s0, s1, txa, tya, txb, tyb, two, sxa, sya, sxb, syb);
+        done += s1 - s0;
       }
       kahan(axa, cxa, sxa);
       kahan(aya, cya, sya);
       kahan(axb, cxb, sxb);
       kahan(ayb, cyb, syb);
-      pairs += (unsigned long long)cnt * (unsigned long long)((va ? 1 : 0) + (vb ? 1 : 0));
+      counts_add(cnts, lane, (unsigned)done, q >= nu ? (unsigned)done : 0u, q >= nu ? (unsigned)cnt : 0u);
       __syncwarp();  // every lane is done with this buffer before it is refilled
       q = qn;
+      msk = msk_next;
       buf ^= 1;
       staged = staged_next;
     }
+    counts_close(cnts, lane, va, vb);
     // FP64 final reduction: u = Im(phi)/2pi + ax/2pi, v = Re(phi)/2pi + ay/2pi
     if (va) {
       const int o = perm[ta];
@@ -1351,8 +1507,7 @@ __global__ void __launch_bounds__(32 * kWarps, 32 / kWarps) k_eval_staged(MixedV
   // shared memory is released
   for (int b = 0; b < 2; b++)
     if (inflight & (1u << b)) mbar_wait(&bar[b], (parity >> b) & 1u, wait_limit);
-  for (int o = 16; o; o >>= 1) pairs += __shfl_xor_sync(0xffffffffu, pairs, o);
-  if (lane == 0) atomicAdd(&m.st->n_pairs, pairs);
+  counts_flush(cnts, lane, m.st);
 }
 
 // The same near field with the source blobs read straight from global
@@ -1360,17 +1515,23 @@ __global__ void __launch_bounds__(32 * kWarps, 32 / kWarps) k_eval_staged(MixedV
 template <bool kLearned, int kWarps>
 __global__ void __launch_bounds__(32 * kWarps, 32 / kWarps) k_eval_mixed(MixedView m, double *uv, const int *perm,
                                                                           Decisions dec, long) {
+  __shared__ float s_tb[kWarps][5];  // target box and rc^2 of the warp's chunk
+  __shared__ WarpCounts s_cnt[kWarps];
   const int l = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   if (l >= m.nleaf) return;
   const int B = m.leaf_cell[l];
   const double inv2pi = 0.15915494309189533577;
-  unsigned long long pairs = 0;
+  float *tbox = s_tb[threadIdx.x >> 5];
+  WarpCounts *cnts = &s_cnt[threadIdx.x >> 5];
+  if (lane == 0) *cnts = WarpCounts{};
+  const float rc = leaf_cutoff(m, B);
   for (int t0 = m.begin[B]; t0 < m.end[B]; t0 += 64) {
     const int ta = t0 + lane, tb = t0 + 32 + lane;
     const bool va = ta < m.end[B], vb = tb < m.end[B];
     const bool two = __any_sync(0xffffffffu, vb);
     const float2 za = va ? m.loc[ta] : make_float2(0.f, 0.f);
     const float2 zb = vb ? m.loc[tb] : make_float2(0.f, 0.f);
+    target_box(za, va, zb, vb, rc, tbox, lane);
     float2 pa = make_float2(0.f, 0.f), pb = make_float2(0.f, 0.f);
     if (two)
       far_field2(m, l, B, za, zb, pa, pb);
@@ -1403,18 +1564,35 @@ __global__ void __launch_bounds__(32 * kWarps, 32 / kWarps) k_eval_mixed(MixedVi
         // centres alone would carry ~3e-8 absolute error into every close pair
         const float ox = centre_offset(m.cxf, m.cxl, B, A), oy = centre_offset(m.cyf, m.cyl, B, A);
         const int j0 = m.begin[A], j1 = m.end[A];
+        const float txa = __fadd_rn(za.x, ox), tya = __fadd_rn(za.y, oy), txb = __fadd_rn(zb.x, ox),
+                    tyb = __fadd_rn(zb.y, oy);
         float sxa = 0.f, sya = 0.f, sxb = 0.f, syb = 0.f;
-        if (pass == 0)
-          leaf_pairs<false>(m.src4, j0, j1, __fadd_rn(za.x, ox), __fadd_rn(za.y, oy), __fadd_rn(zb.x, ox), __fadd_rn(zb.y, oy), two, sxa, sya, sxb, syb);
-        else
-          leaf_pairs<true>(m.src4, j0, j1, __fadd_rn(za.x, ox), __fadd_rn(za.y, oy), __fadd_rn(zb.x, ox), __fadd_rn(zb.y, oy), two, sxa, sya, sxb, syb);
+        unsigned msk = kAllChunks;
+        if (pass == 1) {
+          msk = chunk_mask(m, A, ox, oy, tbox, lane);
+          if (!msk) {
+            counts_add(cnts, lane, 0u, 0u, (unsigned)(j1 - j0));
+            continue;
+          }
+        }
+        int done = 0;
+        for (unsigned r = msk; r;) {
+          int s0, s1;
+          next_run(r, j1 - j0, s0, s1);
+          if (pass == 0)
+            leaf_pairs<false>(m.src4 + j0, s0, s1, txa, tya, txb, tyb, two, sxa, sya, sxb, syb);
+          else
+            leaf_pairs<true>(m.src4 + j0, s0, s1, txa, tya, txb, tyb, two, sxa, sya, sxb, syb);
+          done += s1 - s0;
+        }
+        counts_add(cnts, lane, (unsigned)done, pass == 1 ? (unsigned)done : 0u, pass == 1 ? (unsigned)(j1 - j0) : 0u);
         kahan(axa, cxa, sxa);
         kahan(aya, cya, sya);
         kahan(axb, cxb, sxb);
         kahan(ayb, cyb, syb);
-        pairs += (unsigned long long)(j1 - j0) * (unsigned long long)((va ? 1 : 0) + (vb ? 1 : 0));
       }
     }
+    counts_close(cnts, lane, va, vb);
     // FP64 final reduction: u = Im(phi)/2pi + ax/2pi, v = Re(phi)/2pi + ay/2pi
     if (va) {
       const int o = perm[ta];
@@ -1427,8 +1605,7 @@ __global__ void __launch_bounds__(32 * kWarps, 32 / kWarps) k_eval_mixed(MixedVi
       uv[2 * (size_t)o + 1] = ((double)pb.x + (double)ayb - (double)cyb) * inv2pi;
     }
   }
-  for (int o = 16; o; o >>= 1) pairs += __shfl_xor_sync(0xffffffffu, pairs, o);
-  if (lane == 0) atomicAdd(&m.st->n_pairs, pairs);
+  counts_flush(cnts, lane, m.st);
 }
 
 // ------------------------------------------------------------ off-blob points
@@ -1873,6 +2050,8 @@ int mixed_solve(Workspace &ws, const Tree &t, const MixedParams &mp, double *d_u
   need += Arena::bytes_for(n, 4) * 4;             // leaf_of gam s2inv + pad
   need += Arena::bytes_for(n, 8);                 // loc
   need += Arena::bytes_for(n, 16) + Arena::bytes_for(nc, 4) * 4;  // src4, cxf, cyf, cxl, cyl
+  const int kchunks = t.leaf_cap > 0 ? (t.leaf_cap + 31) / 32 : 1;
+  need += Arena::bytes_for((size_t)nc * kchunks, 16);              // chunk boxes
   need += Arena::bytes_for((size_t)nc * 9, 4) * 2;
   need += Arena::bytes_for((size_t)nc * 27, 4) + Arena::bytes_for((size_t)nc * 8, 4);
   need += Arena::bytes_for((size_t)nl + 1, 4) * 3;
@@ -1917,6 +2096,8 @@ int mixed_solve(Workspace &ws, const Tree &t, const MixedParams &mp, double *d_u
   m.gam = ws.mx_arena.take<float>(n);
   m.s2inv = ws.mx_arena.take<float>(n);
   m.src4 = ws.mx_arena.take<float4>(n);
+  m.kchunks = kchunks;
+  m.cbox = ws.mx_arena.take<float4>((size_t)nc * kchunks);
   m.cxf = ws.mx_arena.take<float>(nc);
   m.cyf = ws.mx_arena.take<float>(nc);
   m.cxl = ws.mx_arena.take<float>(nc);

@@ -31,7 +31,10 @@ struct MixedView {
   int *leaf_of;          // per position
   float2 *loc;           // per position, offset from its leaf centre
   float *gam, *s2inv;    // per position
-  float4 *src4;          // per position {loc.x, loc.y, G, 1/sigma^2}
+  float4 *src4;          // per position {loc.x, loc.y, G, -log2(e)/sigma^2}
+  float4 *cbox;          // per leaf cell, kchunks entries: bounding box {xmin, ymin, xmax, ymax}
+                         // of each 32-blob chunk of the leaf (from its first blob), leaf-local
+  int kchunks;           // chunk boxes per cell: ceil(most blobs per leaf / 32)
   float *cxf, *cyf;      // per cell, FP32 centre (rounded)
   float *cxl, *cyl;      // per cell, the rest: centre - (double)cxf, in FP32
   int *coll, *coarse;    // 9 per cell

@@ -464,6 +464,11 @@ def run_ours(args):
             "tree": {"cells": st["n_cells"], "leaves": st["n_leaves"], "depth": st["depth"],
                      "m2s_per_target": st["n_m2s"] / n, "pairs_per_target": st["n_pairs"] / n,
                      "m2l_pairs": st["n_m2l"]},
+            "pairs_per_target": {"direct_u": (st["n_pairs"] - st["n_pairs_k"]) / n,
+                                 "correction_k": st["n_pairs_k"] / n,
+                                 "correction_k_listed": st["n_pairs_k_listed"] / n,
+                                 "note": "correction pairs of the K leaves evaluated, after and before skipping "
+                                         "32-blob chunks farther than the correction radius from the targets"},
             "clocks": clocks,
         }
         line.update(beside)

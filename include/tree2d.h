@@ -162,6 +162,11 @@ typedef struct {
   long long n_list_k_blobs; /* mixed: source blobs of the K lists, summed
                              over the leaves; learned: out to the
                              envelope's radius (the envelope statistic) */
+  long long n_pairs_k;    /* mixed: correction pairs evaluated (part of
+                             n_pairs; the rest are direct U pairs)      */
+  long long n_pairs_k_listed; /* mixed: pairs of the correction entries
+                             evaluated, before 32-blob chunks farther than
+                             the correction radius were skipped          */
 } tree2d_stats_t;
 int tree2d_get_stats(tree2d_stats_t *out);
 
