@@ -23,7 +23,7 @@ LIB_PATH = os.path.join(HERE, "libtree2d_gb300.so")
 
 OK = 0
 ERR_PARAM_FILE, ERR_BAD_PARAMS, ERR_BAD_INPUT, ERR_TOO_DEEP, ERR_CUDA, ERR_NO_TREE, ERR_NO_DEVICE, ERR_TIMEOUT, \
-    ERR_MODE, ERR_TOO_LARGE = range(1, 11)
+    ERR_MODE, ERR_TOO_LARGE, ERR_FILE = range(1, 12)
 STATIC_MAX_BLOBS = 65536
 MODE_PLAIN, MODE_MIXED, MODE_LEARNED = 0, 1, 2
 
@@ -32,7 +32,7 @@ EXPORTS = [
     "make_tree", "biot_tree", "tree2d_last_error", "tree2d_error_string", "tree2d_set_params",
     "tree2d_clear_params", "tree2d_get_params", "tree2d_set_mode", "tree2d_get_mode", "tree2d_set_mixed_params", "tree2d_set_mixed_leaf", "biot_tree_batch",
     "tree2d_solve_device", "tree2d_solve_device_static", "tree2d_solve_sets", "tree2d_set_tuning", "tree2d_get_stats", "tree2d_export_tree", "tree2d_direct_device", "tree2d_fp64_probe", "tree2d_pipe_probe", "tree2d_wait_probe", "tree2d_version",
-    "tree2d_learn_param_count", "tree2d_learn_set_weights", "tree2d_learn_set_envelope", "tree2d_learn_get_weights", "tree2d_learn_set_options",
+    "tree2d_learn_param_count", "tree2d_learn_load", "tree2d_learn_set_weights", "tree2d_learn_set_envelope", "tree2d_learn_get_weights", "tree2d_learn_set_options",
     "tree2d_learn_collect", "tree2d_learn_train", "tree2d_mlp_grad", "tree2d_mlp_forward",
     "tree2d_set_mirror", "tree2d_advect_device",
 ]
@@ -127,6 +127,8 @@ def load(path: str | None = None):
     L.tree2d_version.restype = ctypes.c_char_p
     fp = ctypes.POINTER(ctypes.c_float)
     L.tree2d_learn_param_count.restype = ctypes.c_int
+    L.tree2d_learn_load.argtypes = [ctypes.c_char_p]
+    L.tree2d_learn_load.restype = ctypes.c_int
     L.tree2d_learn_set_weights.argtypes = [fp, ctypes.c_int]
     L.tree2d_learn_get_weights.argtypes = [fp, ctypes.c_int]
     L.tree2d_learn_set_options.argtypes = [ctypes.c_float, ctypes.c_int, ctypes.c_double]
@@ -339,6 +341,12 @@ def _fp(a):
 
 def learn_param_count() -> int:
     return load().tree2d_learn_param_count()
+
+
+def learn_load(path: str) -> int:
+    """Loads a .t2dw weights file (parameters and training envelope) through
+    the C loader; returns the status."""
+    return load().tree2d_learn_load(os.fsencode(path))
 
 
 def learn_set_weights(theta):

@@ -138,6 +138,7 @@ struct Solver {
   Arena io;       // device copies of host inputs and outputs
   Arena targets;  // evaluation-order targets
   Arena lookup;   // query points and answers of a batch lookup
+  Arena keyed;    // the blobs as targets in key order (plain evaluation)
 };
 
 struct Lib {
@@ -292,10 +293,7 @@ int solve_body(Lib &L, Solver &S, int n, const double *d_xy, const double *d_cir
   if (L.mode != TREE2D_MODE_PLAIN) bp.num_p = mixed_leaf_blobs(L.mixed, n / (nsets > 0 ? nsets : 1), L.params.num_p) + 1;
   st.leaf_blobs = bp.num_p - 1;
   S.mixed_ready = false;
-  // the plain form keeps the reference's in-leaf order (parity); the mixed
-  // forms keep the key order, which their correction cull needs
-  int rc = build_tree(ws, n, d_xy, d_cir, d_cor, bp, S.tree, s, d_set_off, nsets, cir_cor_ready,
-                      L.mode == TREE2D_MODE_PLAIN);
+  int rc = build_tree(ws, n, d_xy, d_cir, d_cor, bp, S.tree, s, d_set_off, nsets, cir_cor_ready);
   if (rc) return rc;
   T2D_CUDA_TRY(cudaEventRecord(ws.ev[1], s));
   S.plain_coef = false;
@@ -304,7 +302,19 @@ int solve_body(Lib &L, Solver &S, int n, const double *d_xy, const double *d_cir
     if (rc) return rc;
     S.plain_coef = true;
     T2D_CUDA_TRY(cudaEventRecord(ws.ev[2], s));
-    rc = plain_evaluate(ws, S.tree, L.params, n, S.tree.x, S.tree.y, S.tree.perm, d_uv, s);
+    // The blobs as targets in full-key order, so that a warp's 32 targets
+    // are neighbours (inside a leaf the tree order is the reference's index
+    // order, spread over the whole leaf) and their traversals coincide.  A
+    // target's result does not depend on its warp: each lane meets its own
+    // cells in its own LIFO order.
+    T2D_CUDA_TRY(S.keyed.reserve(Arena::bytes_for(n, 8) * 2 + Arena::bytes_for(n, 4)));
+    S.keyed.reset();
+    double *ktx = S.keyed.take<double>(n);
+    double *kty = S.keyed.take<double>(n);
+    int *kout = S.keyed.take<int>(n);
+    rc = gather_targets(n, d_xy, reinterpret_cast<const int *>(S.tree.key_order), ktx, kty, kout, s);
+    if (rc) return rc;
+    rc = plain_evaluate(ws, S.tree, L.params, n, ktx, kty, kout, d_uv, s);
     if (rc) return rc;
   } else {
     T2D_CUDA_TRY(cudaEventRecord(ws.ev[2], s));
@@ -750,6 +760,7 @@ const char *tree2d_error_string(int code) {
     case TREE2D_ERR_NO_DEVICE: return "no CUDA device";
     case TREE2D_ERR_TIMEOUT: return "a bounded device loop gave up (traversal stack overflow)";
     case TREE2D_ERR_MODE: return "unknown or unavailable mode";
+    case TREE2D_ERR_FILE: return "could not read the file, or it is not a weights file of this version";
     case TREE2D_ERR_TOO_LARGE:
       return "problem too large for this path (the fixed scratch of tree2d_solve_device_static: 65536 blobs, "
              "32 MiB; or more than 2^31 - 1 interaction-list entries)";
@@ -1021,6 +1032,38 @@ int tree2d_learn_set_envelope(double k_blobs_per_leaf_max, double cutoff_sigmas)
 }
 
 int tree2d_learn_param_count(void) { return kMlpParams; }
+
+// Weights file (little-endian): "T2DW", uint32 version 1, uint32 parameter
+// count, uint32 header bytes (32), float64 envelope limit (K-list source
+// blobs per leaf; 0 = none), float64 the correction radius it is counted at
+// (units of max sigma), then the parameters as float32.
+int tree2d_learn_load(const char *path) {
+  if (!path) return fail(TREE2D_ERR_BAD_INPUT);
+  FILE *f = std::fopen(path, "rb");
+  if (!f) return fail(TREE2D_ERR_FILE);
+  unsigned char hdr[32];
+  const bool got = std::fread(hdr, 1, sizeof(hdr), f) == sizeof(hdr);
+  uint32_t version = 0, count = 0, hbytes = 0;
+  double limit = 0.0, cutoff = 0.0;
+  if (got) {
+    std::memcpy(&version, hdr + 4, 4);
+    std::memcpy(&count, hdr + 8, 4);
+    std::memcpy(&hbytes, hdr + 12, 4);
+    std::memcpy(&limit, hdr + 16, 8);
+    std::memcpy(&cutoff, hdr + 24, 8);
+  }
+  if (!got || std::memcmp(hdr, "T2DW", 4) != 0 || version != 1 || count != (uint32_t)kMlpParams || hbytes != 32) {
+    std::fclose(f);
+    return fail(TREE2D_ERR_FILE);
+  }
+  std::vector<float> theta(kMlpParams);
+  const bool body = std::fread(theta.data(), sizeof(float), theta.size(), f) == theta.size();
+  std::fclose(f);
+  if (!body) return fail(TREE2D_ERR_FILE);
+  int rc = tree2d_learn_set_envelope(limit, cutoff);
+  if (rc) return rc;
+  return tree2d_learn_set_weights(theta.data(), kMlpParams);
+}
 
 // ---------------------------------------------------------------- extensions
 

@@ -770,12 +770,10 @@ size_t build_cell_bytes(long long ncell, long long nleaf, int nterms) {
 }
 
 int build_tree(Workspace &ws, int n, const double *d_xy, const double *d_cir, const double *d_cor, const Params &p,
-               Tree &t, cudaStream_t s, const int *d_set_off, int nsets, cudaEvent_t cir_cor_ready,
-               bool ref_leaf_order) {
+               Tree &t, cudaStream_t s, const int *d_set_off, int nsets, cudaEvent_t cir_cor_ready) {
   t.n = n;
   t.nterms = p.nterms;
   t.leaf_cap = p.num_p - 1;
-  t.ref_leaf_order = ref_leaf_order;
   const bool batched = nsets > 1;
   int lev0 = 0;  // levels of container cells above the set roots
   if (batched) {
@@ -868,6 +866,7 @@ retry:
                                    vals, sort_tmp, s));
   else
     T2D_CUDA_TRY(radix_sort_pairs(t.keys, vals, keys_alt, vals_alt, n, 64 - 2 * total_levels, 64, sort_tmp, s));
+  t.key_order = vals;
   // 4-5. leaf levels
   k_cpl<<<(n + 255) / 256, 256, 0, s>>>(t.keys, n, p.num_p, cpl, w);
   ::t2d::g_launches.fetch_add(1, std::memory_order_relaxed);
@@ -929,13 +928,11 @@ retry:
   k_children<<<(t.ncell + 255) / 256, 256, 0, s>>>(t.keys, cpl, cellbase, t.ncell, t.level, t.begin, t.end, t.leaf,
                                                     t.child);
   ::t2d::g_launches.fetch_add(1, std::memory_order_relaxed);
-  // 8. in-leaf order (the reference's, or the key order the sort left), 9. gather
-  if (t.nleaf > 0 && ref_leaf_order) {
+  // 8. in-leaf order, 9. gather
+  if (t.nleaf > 0) {
     k_leaf_order<<<(int)(((long)t.nleaf * 32 + 255) / 256), 256, 0, s>>>(vals, t.nleaf, t.leaf_cell, t.begin, t.end,
                                                                           t.perm);
     ::t2d::g_launches.fetch_add(1, std::memory_order_relaxed);
-  } else {
-    T2D_CUDA_TRY(cudaMemcpyAsync(t.perm, vals, sizeof(int) * (size_t)n, cudaMemcpyDeviceToDevice, s));
   }
   if (cir_cor_ready) T2D_CUDA_TRY(cudaStreamWaitEvent(s, cir_cor_ready, 0));
   k_gather<<<(n + 255) / 256, 256, 0, s>>>(d_xy, d_cir, d_cor, t.perm, n, t.x, t.y, t.cir, t.cor, t.icor2,

@@ -146,8 +146,8 @@ struct Tree {
   const double *set_cor = nullptr;  // batched: core radii in input order (valid during the solve)
   int lev0 = 0;                   // batched: levels of container cells above the set roots
   int leaf_cap = 0;               // most blobs a leaf can hold (num_p - 1 of the build)
-  bool ref_leaf_order = true;     // blobs inside a leaf in ascending original index (the
-                                  // reference's order); false: in key order (spatially compact)
+  const uint32_t *key_order = nullptr;  // blob indices in key order (build scratch in the tmp
+                                        // arena: valid until that arena is next used)
 };
 
 // Per-solver working state (one per library instance).
@@ -189,13 +189,9 @@ cudaError_t workspace_init(Workspace &ws);
 // `cir_cor_ready`, when given, is an event the stream waits for before the
 // circulations and core radii are first read (the positions must be ready
 // when the call is made); the caller may still be uploading them.
-// `ref_leaf_order`: blobs inside each leaf in ascending original index, as
-// the reference buckets them (the plain form's parity needs it); false keeps
-// them in key order, so that consecutive blobs of a leaf are close together
-// (the mixed forms cull their correction pairs by 32-blob chunks).
 int build_tree(Workspace &ws, int n, const double *d_xy, const double *d_cir, const double *d_cor,
                const Params &p, Tree &t, cudaStream_t s, const int *d_set_off = nullptr, int nsets = 1,
-               cudaEvent_t cir_cor_ready = nullptr, bool ref_leaf_order = true);
+               cudaEvent_t cir_cor_ready = nullptr);
 // Bytes build_tree reserves in ws.blob_arena and ws.tmp_arena for n blobs in
 // nsets sets (what a caller with fixed arenas must provide).
 size_t build_blob_bytes(int n, int nsets);

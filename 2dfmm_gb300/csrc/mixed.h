@@ -32,6 +32,10 @@ struct MixedView {
   float2 *loc;           // per position, offset from its leaf centre
   float *gam, *s2inv;    // per position
   float4 *src4;          // per position {loc.x, loc.y, G, -log2(e)/sigma^2}
+  int *mperm;            // per position: original blob index.  The per-position arrays of the
+                         // mixed form hold each leaf's blobs in a spatial order (a Morton code of
+                         // the offset from the leaf centre, ties by tree position), not the tree's
+  unsigned *skey;        // per position: scratch of that ordering
   float4 *cbox;          // per leaf cell, kchunks entries: bounding box {xmin, ymin, xmax, ymax}
                          // of each 32-blob chunk of the leaf (from its first blob), leaf-local
   int kchunks;           // chunk boxes per cell: ceil(most blobs per leaf / 32)

@@ -47,6 +47,8 @@ ENVELOPE_LEAF_BLOBS = 64   # leaf size of the training solves (configuration 5, 
 
 
 def save_weights(path, theta, meta, k_blobs_per_leaf_train=None, cutoff_train=None, extra=None):
+    """Writes the .npz (weights, metadata, training envelope) and beside it
+    the raw .t2dw file that the C loader tree2d_learn_load reads."""
     os.makedirs(os.path.dirname(os.path.abspath(path)), exist_ok=True)
     extra = dict(extra or {})
     if k_blobs_per_leaf_train is not None:
@@ -54,6 +56,22 @@ def save_weights(path, theta, meta, k_blobs_per_leaf_train=None, cutoff_train=No
     if cutoff_train is not None:
         extra["cutoff_train"] = np.float64(cutoff_train)
     np.savez(path, version=WEIGHTS_VERSION, theta=np.asarray(theta, np.float32), meta=json.dumps(meta), **extra)
+    write_raw_weights(os.path.splitext(path)[0] + ".t2dw", theta, *load_envelope(path))
+
+
+def write_raw_weights(path, theta, k_blobs_limit=0.0, cutoff=0.0):
+    """The weights file of tree2d_learn_load (include/tree2d.h): "T2DW",
+    uint32 version, count, header bytes (32), float64 envelope limit and its
+    correction radius, float32 parameters; little-endian."""
+    import struct
+    theta = np.asarray(theta, dtype="<f4").ravel()
+    with open(path, "wb") as f:
+        f.write(b"T2DW" + struct.pack("<III", RAW_VERSION, theta.size, 32) + struct.pack("<dd", k_blobs_limit, cutoff))
+        f.write(theta.tobytes())
+
+
+RAW_VERSION = 1
+DEFAULT_RAW_WEIGHTS = os.path.join(HERE, "data", "learned_weights.t2dw")
 
 
 def load_weights(path=DEFAULT_WEIGHTS):

@@ -12,9 +12,11 @@ A step is one whole solve: tree build, upward pass and evaluation at all
 targets.  `value` times the device-resident call (inputs already in HBM,
 CUDA events on the launching stream, L2 flushed between steps); `e2e`
 times the reference-facing calls with host buffers (make_tree + one batch
-of biot_tree answers), copies included.  `cpu_baseline` times the CPU
-oracle (the reference's algorithm restated in C) on the host cores on a
-bounded sample.  `--impl reference` times that CPU implementation alone.
+of biot_tree answers), copies included.  `cpu_baseline` times the
+reference's own CPU code (ver-c/src built on the host from the staged
+sources; the oracle, its restatement in C, where that build is absent) on
+the host cores on a bounded sample.  `--impl reference` times that CPU
+implementation alone.
 
 Run:  python bench.py [--gpus N --steps K --warmup W] [--impl reference]
 """
@@ -57,7 +59,9 @@ def parse():
     ap.add_argument("--eval-variant", type=int, default=-1,
                     help="mixed/learned: force a near-field kernel variant 0..3 (default: the tuner's choice)")
     ap.add_argument("--workload", default="two_patch_sheet",
-                    choices=["two_patch_sheet", "lamb_oseen", "uniform", "batch_sets"])
+                    choices=["two_patch_sheet", "lamb_oseen", "uniform", "batch_sets", "advected"])
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the compact measurements of the other configurations in the default line")
     ap.add_argument("--nsets", type=int, default=512, help="batch_sets: number of independent sets")
     ap.add_argument("--set-targets", type=int, default=4096, help="batch_sets: targets per set measured against the direct sum")
     ap.add_argument("--n", type=int, default=0, help="override the blob count (exploration only)")
@@ -154,7 +158,7 @@ class Clocks:
 
 
 # --------------------------------------------------------------------------
-# CPU baseline: the oracle (the reference's algorithm, restated in C)
+# CPU baseline: the reference's own code (or the oracle, its restatement)
 
 def mem_available_gb():
     try:
@@ -167,49 +171,65 @@ def mem_available_gb():
 
 
 def cpu_reference(b, depth_hint, steps, warmup, sample, threads=0):
-    """Times the oracle on `b`: make_tree once (single-threaded, as the
-    reference), then `steps` batches of `sample` sampled targets over all
-    host threads.  Returns (targets/s projected to the whole job, detail)."""
+    """Times the reference's CPU implementation of the path on `b`: its own
+    build (ver-c/src compiled from the staged sources by oracle/Makefile,
+    `kind: reference`) where it runs here, else the oracle (the reference's
+    algorithm restated in C, `kind: port`).  make_tree runs once,
+    single-threaded as in the reference, then `warmup + steps` batches of
+    `sample` sampled targets over all host threads (biot_tree is re-entrant,
+    as the reference caller's MPI target split uses it).  Returns (targets/s
+    projected to the whole job, detail)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O  # noqa: WPS433
     W = importlib.import_module("2dfmm_gb300.workloads")
+    use_ref = O.reference_available()
     threads = threads or O.max_threads()
-    # the reference's dense complete tree: (4^(L+1)-1)/3 nodes of ~56 B, plus
-    # one num_nodes-int traversal stack per concurrent biot_tree call
+    # the reference's dense complete tree: (4^(L+1)-1)/3 nodes of 64 B (56 in
+    # the port), plus one num_nodes-int traversal stack per concurrent call
     nodes = (4 ** (depth_hint + 1) - 1) // 3
-    need_gb = nodes * 56 / 1e9 + 1.2 * b.n * 64 / 1e9
+    need_gb = nodes * (64 if use_ref else 56) / 1e9 + 1.2 * b.n * 64 / 1e9
     per_thread_gb = nodes * 4 / 1e9
     avail = mem_available_gb()
     if avail and need_gb + per_thread_gb > 0.7 * avail:
         return None, {"unavailable": f"dense reference tree needs {need_gb:.1f} GB, {avail:.1f} GB available"}
     if avail:
         threads = max(1, min(threads, int((0.7 * avail - need_gb) / max(per_thread_gb, 1e-9))))
-    o = O.Oracle(b.nterms, b.num_p, b.theta)
-    t0 = time.perf_counter()
-    o.make_tree(b.xy, b.cir, b.cor, max_level_cap=30)
-    t_make = time.perf_counter() - t0
     if not sample:
-        # aim for ~2 s per step
-        probe = W.sample_targets(b.n, threads, seed=99)
+        # about 2 s per batch: each call allocates and fills its num_nodes
+        # stack (~0.5 ns per node) before a traversal of ~0.2 ms
+        est = 0.5e-9 * nodes + 2e-4
+        sample = int(min(200_000, b.n, max(1, round(2.0 / est)) * threads))
+    idx = W.sample_targets(b.n, sample, seed=100)
+    if use_ref:
+        with tempfile.TemporaryDirectory() as d:
+            t_make, per, levels = O.time_reference(d, b.xy, b.cir, b.cor, b.xy[idx], b.nterms, b.num_p, b.theta,
+                                                   threads=threads, batches=warmup + steps)
+        times = per[warmup:] or per
+        kind = "reference"
+        what = "the reference's own ver-c/src (gcc -O2, built on this host from the staged sources)"
+    else:
+        o = O.Oracle(b.nterms, b.num_p, b.theta)
         t0 = time.perf_counter()
-        o.biot(b.xy[probe], threads=threads)
-        per = (time.perf_counter() - t0) / threads
-        sample = int(max(threads, min(200_000, 2.0 * threads / max(per, 1e-9))))
-        sample -= sample % threads
-    times = []
-    for k in range(warmup + steps):
-        idx = W.sample_targets(b.n, sample, seed=100 + k)
-        t0 = time.perf_counter()
-        o.biot(b.xy[idx], threads=threads)
-        dt = time.perf_counter() - t0
-        if k >= warmup:
-            times.append(dt)
+        o.make_tree(b.xy, b.cir, b.cor, max_level_cap=30)
+        t_make = time.perf_counter() - t0
+        times = []
+        for k in range(warmup + steps):
+            t0 = time.perf_counter()
+            o.biot(b.xy[idx], threads=threads)
+            if k >= warmup:
+                times.append(time.perf_counter() - t0)
+        levels = o.levels()
+        o.close()
+        kind = "port"
+        what = "the oracle (the reference's algorithm restated in C, oracle/tree2d_oracle.c)"
     per_target = statistics.median(times) / sample
     value = b.n / (t_make + b.n * per_target)
     detail = {"make_tree_s": round(t_make, 3), "biot_tree_s_per_target_per_job": per_target,
-              "sample": f"make_tree over all {b.n} blobs (1 thread, as the reference), then {steps} batches of "
-                        f"{sample} sampled targets over {threads} threads; value = N / (t_make + N * t_target)",
-              "cores": threads, "levels": o.levels()}
+              "batch_s_median": statistics.median(times),
+              "sample": f"{what}: make_tree over all {b.n} blobs (1 thread, as the reference), then {len(times)} "
+                        f"timed batches of {sample} sampled targets over {threads} threads (after {warmup} "
+                        f"untimed); value = N / (t_make + N * t_target)",
+              "cores": threads, "levels": levels, "kind": kind}
     return value, detail
 
 
@@ -243,8 +263,10 @@ def run_reference(args):
     if value is None:
         line.update({"value": None, "unavailable": det["unavailable"]})
     else:
-        line.update({"value": value, "ms_per_step": 1e3 * b.n / value,
-                     "cpu_baseline": {"value": value, "unit": UNIT, "cores": det["cores"], "kind": "port",
+        # a step is one timed batch of sampled targets (ms_per_step is its
+        # measured time); value is the whole job's projected rate
+        line.update({"value": value, "ms_per_step": 1e3 * det["batch_s_median"],
+                     "cpu_baseline": {"value": value, "unit": UNIT, "cores": det["cores"], "kind": det["kind"],
                                       "sample": det["sample"]},
                      "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
                      "detail": det})
@@ -419,14 +441,20 @@ def run_ours(args):
     e2e_t = max_over_ranks(statistics.mean(e2e_times), world, dev)
     e2e_match = bool(np.array_equal(out, uv.cpu().numpy()))
 
+    extras = None
+    if rank == 0 and world == 1 and not args.no_extras and args.workload == "two_patch_sheet" and not args.n:
+        t0 = time.perf_counter()
+        extras = other_configurations(P, torch, stream, flush)
+        extras["wall_s"] = round(time.perf_counter() - t0, 1)
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         depth = sts[-1]["depth"]
         v, det = cpu_reference(b, depth, 1, 0, args.cpu_sample)
         if v is None:
-            cpu = {"value": None, "unit": UNIT, "cores": 0, "kind": "port", "sample": det["unavailable"]}
+            cpu = {"value": None, "unit": UNIT, "cores": 0, "kind": "reference", "sample": det["unavailable"]}
         else:
-            cpu = {"value": v, "unit": UNIT, "cores": det["cores"], "kind": "port", "sample": det["sample"],
+            cpu = {"value": v, "unit": UNIT, "cores": det["cores"], "kind": det["kind"], "sample": det["sample"],
                    "make_tree_s": det["make_tree_s"]}
 
     if rank == 0:
@@ -472,6 +500,8 @@ def run_ours(args):
             "clocks": clocks,
         }
         line.update(beside)
+        if extras is not None:
+            line["other_configurations"] = extras
         if learned_note:
             line["config"]["learned_weights"] = learned_note
         if cpu is not None:
@@ -631,12 +661,222 @@ def run_batch(args):
         print(json.dumps(line), flush=True)
 
 
+# --------------------------------------------------------------------------
+# the other configurations, compactly (appended to the default line)
+
+def _events_ms(torch, stream, fn, steps, flush=None):
+    """Per-step CUDA-event times of fn() on `stream` (L2 flushed first)."""
+    out = []
+    for _ in range(steps):
+        if flush is not None:
+            flush.fill_(1)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        out.append(e0.elapsed_time(e1))
+    return out
+
+
+def _dev(torch, b, dev):
+    xy = torch.from_numpy(np.ascontiguousarray(b.xy)).to(dev)
+    return xy, torch.from_numpy(b.cir).to(dev), torch.from_numpy(b.cor).to(dev), torch.empty_like(xy)
+
+
+def _rel_l2_at(P, torch, xy, cir, cor, n, uvs, idx, sp):
+    t = torch.from_numpy(idx).to(xy.device)
+    txy = xy[t].contiguous()
+    ref = torch.empty_like(txy)
+    P.direct_device(txy.data_ptr(), len(idx), xy.data_ptr(), cir.data_ptr(), cor.data_ptr(), n, ref.data_ptr(), sp)
+    torch.cuda.synchronize()
+    return [float(torch.linalg.norm(u[t] - ref) / torch.linalg.norm(ref)) for u in uvs]
+
+
+def _use_learned(P, L, mode):
+    if mode == "learned":
+        P.learn_load(L.DEFAULT_RAW_WEIGHTS)
+        P.learn_set_options(1.0, 1)
+
+
+def advected(P, torch, stream, steps_total=100, train_until=20, dt=1e-3, score_every=10, score_targets=2048,
+             n=1_048_576):
+    """Configuration 5: the configuration-2 set (1M Lamb-Oseen blobs)
+    advected 100 forward-Euler steps (dt 1e-3) on the device by its own
+    velocity (the fixed mixed form's, P = 16), the tree rebuilt every step.
+    The packaged network was trained on steps 0-20; on steps 21-100 every
+    form solves the same state: learned, the fixed-order FMM at p = 12 and
+    at P = 16, and the plain FP64 treecode (every `score_every` steps).
+    relL2 against the FP64 direct sum on sampled targets every
+    `score_every` steps."""
+    W = importlib.import_module("2dfmm_gb300.workloads")
+    L = importlib.import_module("2dfmm_gb300.learn")
+    dev = torch.device("cuda", torch.cuda.current_device())
+    sp = stream.cuda_stream
+    b = W.lamb_oseen(n, seed=2)
+    P.set_params(b.nterms, b.num_p, b.theta)
+    P.set_mixed_leaf(-1)
+    _use_learned(P, L, "learned")
+    xy, cir, cor, uv = _dev(torch, b, dev)
+    uvs = {k: torch.empty_like(xy) for k in ("learned", "p12", "p16", "plain")}
+    forms = {"learned": (P.MODE_LEARNED, 16), "p12": (P.MODE_MIXED, 12), "p16": (P.MODE_MIXED, 16),
+             "plain": (P.MODE_PLAIN, 16)}
+    times = {k: [] for k in forms}
+    rels = {k: [] for k in forms}
+    pairs = {"learned": [], "p16": []}
+    learned_active = []
+
+    def solve(kind):
+        mode, pt = forms[kind]
+        P.set_mode(mode)
+        P.set_mixed_params(pt, 2.5, True)
+        out = uvs[kind]
+        return _events_ms(torch, stream, lambda: P.solve_device(xy.data_ptr(), cir.data_ptr(), cor.data_ptr(),
+                                                                out.data_ptr(), n, sp), 1)[0]
+
+    for k in ("learned", "p12", "p16"):  # warm-up: tuner and buffers of each form
+        solve(k)
+    for step in range(steps_total + 1):
+        scored = step > train_until
+        if scored:
+            for k in ("learned", "p12"):
+                times[k].append(solve(k))
+                st = P.stats()
+                if k == "learned":
+                    pairs["learned"].append(st["n_pairs"])
+                    learned_active.append(st["learned_active"])
+        times_p16 = solve("p16")
+        if scored:
+            times["p16"].append(times_p16)
+            pairs["p16"].append(P.stats()["n_pairs"])
+            if (step - train_until - 1) % score_every == 0 or step == steps_total:
+                times["plain"].append(solve("plain"))
+                idx = W.sample_targets(n, score_targets, seed=step)
+                for k, r in zip(forms, _rel_l2_at(P, torch, xy, cir, cor, n, [uvs[k] for k in forms], idx, sp)):
+                    rels[k].append(r)
+        P.advect_device(xy.data_ptr(), uvs["p16"].data_ptr(), n, dt, sp)
+    torch.cuda.synchronize()
+    P.set_mode(P.MODE_PLAIN)
+    P.set_mixed_params(16, 2.5, True)
+    nsc = steps_total - train_until
+    res = {"workload": "advected_lamb_oseen_1M", "n_blobs": n, "steps_scored": f"{train_until + 1}-{steps_total}",
+           "dt": dt, "trajectory": "forward Euler on the device by the fixed mixed form's velocity (P = 16)",
+           "score_targets": score_targets, "scored_every": score_every}
+    for k in forms:
+        ms = statistics.mean(times[k])
+        res[k] = {"ms_per_step": ms, "value": n / (ms * 1e-3), "unit": UNIT,
+                  "max_relL2_vs_fp64_direct": max(rels[k]), "steps_timed": len(times[k])}
+    res["learned"]["learned_active_steps"] = int(sum(learned_active))
+    res["learned"]["pairs_ratio_vs_p16"] = float(np.mean(np.array(pairs["learned"]) / np.array(pairs["p16"])))
+    res["learned_speedup"] = {"vs_fixed_p12": res["p12"]["ms_per_step"] / res["learned"]["ms_per_step"],
+                              "vs_fixed_p16": res["p16"]["ms_per_step"] / res["learned"]["ms_per_step"],
+                              "vs_plain": res["plain"]["ms_per_step"] / res["learned"]["ms_per_step"]}
+    assert nsc == len(times["learned"])
+    return res
+
+
+def other_configurations(P, torch, stream, flush):
+    """Compact measurements of configurations 1, 2, 4 and 5 for the default
+    line (each a few steps; the headline is configuration 3)."""
+    W = importlib.import_module("2dfmm_gb300.workloads")
+    L = importlib.import_module("2dfmm_gb300.learn")
+    dev = torch.device("cuda", torch.cuda.current_device())
+    sp = stream.cuda_stream
+    out = {}
+    # configuration 1: the plain path against the reference's own outputs
+    g = np.load(os.path.join(ROOT, "tests", "golden", "cfg1.npz"))
+    b = W.uniform()
+    assert np.array_equal(b.xy, g["xy"])
+    P.set_params(int(g["nterms"]), int(g["num_p"]), float(g["theta"]))
+    P.set_mode(P.MODE_PLAIN)
+    xy, cir, cor, uv = _dev(torch, b, dev)
+    solve = lambda: P.solve_device(xy.data_ptr(), cir.data_ptr(), cor.data_ptr(), uv.data_ptr(), b.n, sp)  # noqa
+    _events_ms(torch, stream, solve, 3)
+    ms = statistics.mean(_events_ms(torch, stream, solve, 5, flush))
+    got = uv.cpu().numpy()
+    ref = g["uv"][: b.n]
+    comp = np.abs(got - ref) / np.maximum(np.abs(ref), 1e-300)
+    nrm = np.linalg.norm(got - ref, axis=1) / np.linalg.norm(ref, axis=1)
+    out["config1_uniform_20k_plain"] = {
+        "value": b.n / (ms * 1e-3), "unit": UNIT, "ms_per_step": ms,
+        "vs_reference_outputs": {"max_normwise": float(nrm.max()), "max_per_component": float(comp.max()),
+                                 "components_beyond_1e-12": int((comp > 1e-12).sum()), "components": int(comp.size),
+                                 "note": "golden outputs of the reference built from its sources; the components "
+                                         "beyond 1e-12 are cancellation residues (tests/test_plain_parity.py)"}}
+    # configuration 2: plain and learned at 1M
+    b = W.lamb_oseen(seed=2)
+    P.set_params(b.nterms, b.num_p, b.theta)
+    xy, cir, cor, uv = _dev(torch, b, dev)
+    idx = W.sample_targets(b.n, 2048, seed=7)
+    c2 = {}
+    for mode in ("plain", "learned"):
+        P.set_mode(MODES[mode])
+        _use_learned(P, L, mode)
+        solve = lambda: P.solve_device(xy.data_ptr(), cir.data_ptr(), cor.data_ptr(), uv.data_ptr(), b.n, sp)  # noqa
+        _events_ms(torch, stream, solve, 2)
+        ms = statistics.mean(_events_ms(torch, stream, solve, 3, flush))
+        rel = _rel_l2_at(P, torch, xy, cir, cor, b.n, [uv], idx, sp)[0]
+        c2[mode] = {"value": b.n / (ms * 1e-3), "unit": UNIT, "ms_per_step": ms, "relL2_vs_fp64_direct": rel}
+    c2["learned_active"] = bool(P.stats()["learned_active"])
+    out["config2_lamb_oseen_1M"] = c2
+    # configuration 4: 512 sets in one batched solve
+    sets = W.batch_sets(nsets=512, seed=4)
+    P.set_params(sets[0].nterms, sets[0].num_p, sets[0].theta)
+    P.set_mode(P.MODE_MIXED)
+    off = np.concatenate([[0], np.cumsum([s_.n for s_ in sets])]).astype(np.int32)
+    n = int(off[-1])
+    xy = torch.from_numpy(np.concatenate([s_.xy for s_ in sets])).to(dev)
+    cir = torch.from_numpy(np.concatenate([s_.cir for s_ in sets])).to(dev)
+    cor = torch.from_numpy(np.concatenate([s_.cor for s_ in sets])).to(dev)
+    uv = torch.empty_like(xy)
+    solve = lambda: P.solve_sets(xy.data_ptr(), cir.data_ptr(), cor.data_ptr(), uv.data_ptr(), off, sp)  # noqa
+    _events_ms(torch, stream, solve, 2)
+    ms = statistics.mean(_events_ms(torch, stream, solve, 3, flush))
+    rels = []
+    for k, s_ in enumerate(sets):
+        a, e = int(off[k]), int(off[k + 1])
+        rels.append(_rel_l2_at(P, torch, xy[a:e], cir[a:e], cor[a:e], s_.n, [uv[a:e]],
+                               W.sample_targets(s_.n, 1024, seed=1000 + k), sp)[0])
+    out["config4_batch_512_sets"] = {"value": n / (ms * 1e-3), "unit": UNIT, "ms_per_step": ms, "n_blobs": n,
+                                     "relL2_max_over_sets": max(rels), "relL2_median": float(np.median(rels)),
+                                     "sets_above_1e-6": int(sum(r > 1e-6 for r in rels)),
+                                     "targets_per_set": 1024}
+    del xy, cir, cor, uv
+    # configuration 5: learned order selection on the advected set
+    out["config5_advected"] = advected(P, torch, stream)
+    P.set_mode(P.MODE_PLAIN)
+    return out
+
+
+def run_advected(args):
+    """`--workload advected`: configuration 5 alone, as its own line."""
+    import torch
+    torch.cuda.set_device(0)
+    P = importlib.import_module("2dfmm_gb300")
+    P.load()
+    stream = torch.cuda.current_stream()
+    with Clocks(0) as clk:
+        res = advected(P, torch, stream)
+    line = {"metric": "target evals/s on configuration 5 (1M Lamb-Oseen advected), steps 21-100, learned order "
+                      "selection, relL2 <= 1e-6 vs FP64 direct",
+            "value": res["learned"]["value"], "unit": UNIT, "n_gpus": 1, "steps": len(range(21, 101)),
+            "warmup": 3, "ms_per_step": res["learned"]["ms_per_step"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 (tf32x3 tensor M2L, bf16 MLP, f64 final sum)",
+            "data": "synthetic (seeded numpy PCG64)", "config": {"workload": res["workload"]},
+            "advected": res, "clocks": clk.summary(), "cpu_baseline": None}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
     elif args.workload == "batch_sets":
         run_batch(args)
+    elif args.workload == "advected":
+        run_advected(args)
     else:
         run_ours(args)
 

@@ -60,6 +60,7 @@ void biot_tree(double x, double y, double *u, double *v);
 #define TREE2D_ERR_MODE 9          /* unknown mode                                 */
 #define TREE2D_ERR_TOO_LARGE 10    /* beyond the fixed scratch of the static solve,
                                       or more than 2^31 - 1 interaction-list entries */
+#define TREE2D_ERR_FILE 11         /* a file could not be read or has the wrong format */
 
 /* Evaluation modes (tree2d_set_mode). */
 #define TREE2D_MODE_PLAIN 0        /* FP64 treecode, reference semantics             */
@@ -231,6 +232,16 @@ int tree2d_wait_probe(long long polls, int *status);
 
 /* Number of network parameters (flat FP32 vector W1 b1 W2 b2 W3 b3 W4 b4). */
 int tree2d_learn_param_count(void);
+/* Loads a weights file (2dfmm_gb300/data/learned_weights.t2dw is the
+ * packaged one): the parameters and the training envelope it records, as
+ * tree2d_learn_set_weights + tree2d_learn_set_envelope do, so that a C or
+ * Fortran caller enables TREE2D_MODE_LEARNED with one call.  Format,
+ * little-endian: the bytes "T2DW", uint32 version (1), uint32 parameter
+ * count, uint32 header size (32), float64 envelope limit (K-list source
+ * blobs per leaf, 0 = none), float64 the correction radius it is counted at,
+ * then the float32 parameters.  TREE2D_ERR_FILE for a missing or malformed
+ * file (nothing is changed then). */
+int tree2d_learn_load(const char *path);
 int tree2d_learn_set_weights(const float *theta, int n);
 int tree2d_learn_get_weights(float *theta, int n);
 /* direct_bias: added to the direct-evaluation logit; order_margin: chosen

@@ -273,7 +273,27 @@ def read_output(path):
                 coef=coef[..., 0] + 1j * coef[..., 1], max_level=int(max_level))
 
 
-def run_reference(workdir, xy, cir, cor, txy, nterms, num_p, theta, r_min=0.01, threads=1):
+def reference_available() -> bool:
+    """The reference's own build (_ref/ref_driver) exists and runs here."""
+    return os.path.exists(REF_DRIVER) and _runs(REF_DRIVER)
+
+
+def time_reference(workdir, xy, cir, cor, txy, nterms, num_p, theta, threads=1, batches=1):
+    """Times the reference's own code on this machine: make_tree over all
+    blobs once, then `batches` evaluations of the targets `txy` over
+    `threads` OpenMP threads, in a fresh process.  Returns (make_tree
+    seconds, [seconds per batch], max level)."""
+    import re
+    out = run_reference(workdir, xy, cir, cor, txy, nterms, num_p, theta, threads=threads, batches=batches)
+    log = out["log"]
+    m = re.search(r"make_tree ([0-9.]+) s", log)
+    per = [float(x) for x in re.findall(r"batch \d+ biot_tree ([0-9.]+) s", log)]
+    if not per:
+        per = [float(re.search(r"biot_tree ([0-9.]+) s", log).group(1))]
+    return float(m.group(1)), per, out["max_level"]
+
+
+def run_reference(workdir, xy, cir, cor, txy, nterms, num_p, theta, r_min=0.01, threads=1, batches=1):
     """Runs the reference (built from its sources) in a fresh process.
 
     The reference reads ../cal_cond/fmm_param.dat relative to its working
@@ -290,7 +310,7 @@ def run_reference(workdir, xy, cir, cor, txy, nterms, num_p, theta, r_min=0.01, 
     fout = os.path.join(workdir, "out.bin")
     write_input(fin, xy, cir, cor, txy)
     env = dict(os.environ)
-    p = subprocess.run(["bash", "-c", f"ulimit -s unlimited; exec {REF_DRIVER} {fin} {fout} {threads}"],
+    p = subprocess.run(["bash", "-c", f"ulimit -s unlimited; exec {REF_DRIVER} {fin} {fout} {threads} {batches}"],
                        cwd=run, env=env, capture_output=True, text=True)
     if p.returncode != 0:
         raise RuntimeError(f"reference driver failed ({p.returncode}): {p.stderr}")

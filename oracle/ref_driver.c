@@ -5,7 +5,9 @@
  * generates the golden vectors that pin the oracle, and is never part of
  * the product.
  *
- * Usage:  ref_driver <input.bin> <output.bin> [threads]
+ * Usage:  ref_driver <input.bin> <output.bin> [threads] [batches]
+ * With batches > 1 the targets are evaluated that many times over the same
+ * tree (a timed CPU baseline); every batch's time is printed.
  * The reference reads its parameters from ../cal_cond/fmm_param.dat
  * relative to the working directory (quadtree.c:12-27), so the caller runs
  * this program from a directory that has that file beside it.
@@ -78,6 +80,8 @@ int main(int argc, char **argv) {
     return 2;
   }
   int threads = argc > 3 ? atoi(argv[3]) : 1;
+  int batches = argc > 4 ? atoi(argv[4]) : 1;
+  if (batches < 1) batches = 1;
   FILE *f = fopen(argv[1], "rb");
   if (!f) return 3;
   int n, nt;
@@ -95,14 +99,18 @@ int main(int argc, char **argv) {
 
   double t0 = now();
   make_tree(n, (void *)xy, cir, cor);
-  double t1 = now();
+  double t1 = now(), t2 = t1;
+  for (int rep = 0; rep < batches; rep++) {
+    double tb = now();
 #ifdef _OPENMP
-#pragma omp parallel for schedule(dynamic, 16) num_threads(threads)
+#pragma omp parallel for schedule(dynamic, 1) num_threads(threads)
 #endif
-  for (int i = 0; i < nt; i++) biot_tree(txy[2 * i], txy[2 * i + 1], &uv[2 * i], &uv[2 * i + 1]);
-  double t2 = now();
+    for (int i = 0; i < nt; i++) biot_tree(txy[2 * i], txy[2 * i + 1], &uv[2 * i], &uv[2 * i + 1]);
+    t2 = now();
+    if (batches > 1) fprintf(stderr, "ref: batch %d biot_tree %.6f s\n", rep, t2 - tb);
+  }
   fprintf(stderr, "ref: n=%d ntgt=%d make_tree %.4f s, biot_tree %.4f s (%d threads), max_level %d\n",
-          n, nt, t1 - t0, t2 - t1, threads, qtree.max_level);
+          n, nt, t1 - t0, (t2 - t1) / batches, threads, qtree.max_level);
 
   /* count, then dump */
   g_perm = malloc(sizeof(int) * (size_t)(n > 0 ? n : 1));

@@ -32,7 +32,7 @@ def test_exports_every_declared_symbol(lib):
 def test_version_and_errors(lib):
     P = pkg()
     assert "sm_103a" in P.version()
-    for code in range(0, 11):
+    for code in range(0, 12):
         assert P.error_string(code)
 
 
