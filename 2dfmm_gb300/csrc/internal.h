@@ -157,8 +157,8 @@ struct Workspace {
   Arena tmp_arena;    // scratch (sort buffers, scans)
   Arena mx_arena;     // mixed form: per-cell and per-position arrays
   Arena mx_lists;     // mixed form: interaction lists
-  Arena mx_tables;    // mixed form: translation operators
-  int mx_tables_P = 0;
+  std::map<int, Arena> mx_tables;  // mixed form: translation operators, per expansion length P
+                                   // (made once each: switching P between solves rebuilds nothing)
   Arena lr_arena;     // learned form: weights, leaf statistics, decisions
   long lr_version = -1;
   MixedView *mxv = nullptr;  // the last mixed solve's view (kept for sampling)

@@ -2056,30 +2056,35 @@ int mixed_solve(Workspace &ws, const Tree &t, const MixedParams &mp, double *d_u
   const bool tc = mp.use_tensor_cores && (P % 4 == 0);
   const size_t n_m2l = (size_t)4 * 27 * P * P * 2, n_tr = (size_t)4 * kMaxP * kMaxP * 2;
   const size_t n_img = (size_t)4 * 27 * 2 * m2l_npad(P) * 2 * P;
-  if (ws.mx_tables_P != P) {
+  Arena &tab = ws.mx_tables[P];
+  if (tab.capacity() == 0) {
     std::vector<float> m2l(n_m2l), m2m(n_tr), l2l(n_tr), img;
     T2D_CUDA_TRY(mixed_tables(P, m2l.data(), m2m.data(), l2l.data()));
     m2l_b_images(P, m2l.data(), img);
     size_t need = Arena::bytes_for(n_m2l, 4) + 2 * Arena::bytes_for(n_tr, 4) + Arena::bytes_for(n_img, 4);
-    T2D_CUDA_TRY(ws.mx_tables.reserve(need));
-    ws.mx_tables.reset();
-    float *dm2l = ws.mx_tables.take<float>(n_m2l);
-    float *dm2m = ws.mx_tables.take<float>(n_tr);
-    float *dl2l = ws.mx_tables.take<float>(n_tr);
-    float *dimg = ws.mx_tables.take<float>(n_img);
-    T2D_CUDA_TRY(cudaMemcpy(dm2l, m2l.data(), n_m2l * 4, cudaMemcpyHostToDevice));
-    T2D_CUDA_TRY(cudaMemcpy(dm2m, m2m.data(), n_tr * 4, cudaMemcpyHostToDevice));
-    T2D_CUDA_TRY(cudaMemcpy(dl2l, l2l.data(), n_tr * 4, cudaMemcpyHostToDevice));
-    T2D_CUDA_TRY(cudaMemcpy(dimg, img.data(), n_img * 4, cudaMemcpyHostToDevice));
-    ws.mx_tables_P = P;
+    T2D_CUDA_TRY(tab.reserve(need));
+    tab.reset();
+    float *dm2l = tab.take<float>(n_m2l);
+    float *dm2m = tab.take<float>(n_tr);
+    float *dl2l = tab.take<float>(n_tr);
+    float *dimg = tab.take<float>(n_img);
+    cudaError_t e = cudaMemcpy(dm2l, m2l.data(), n_m2l * 4, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(dm2m, m2m.data(), n_tr * 4, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(dl2l, l2l.data(), n_tr * 4, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(dimg, img.data(), n_img * 4, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+      ws.mx_tables.erase(P);  // not filled: made again by the next solve at this P
+      note_cuda_error(e, "mixed operator tables");
+      return TREE2D_ERR_CUDA;
+    }
   } else {
     T2D_CUDA_TRY(mixed_tables(P, nullptr, nullptr, nullptr));
   }
-  ws.mx_tables.reset();
-  const float *dm2l = ws.mx_tables.take<float>(n_m2l);
-  const float *dm2m = ws.mx_tables.take<float>(n_tr);
-  const float *dl2l = ws.mx_tables.take<float>(n_tr);
-  const float *dimg = ws.mx_tables.take<float>(n_img);
+  tab.reset();
+  const float *dm2l = tab.take<float>(n_m2l);
+  const float *dm2m = tab.take<float>(n_tr);
+  const float *dl2l = tab.take<float>(n_tr);
+  const float *dimg = tab.take<float>(n_img);
 
   // ---- arrays
   size_t need = 0;
