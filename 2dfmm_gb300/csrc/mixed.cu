@@ -142,58 +142,84 @@ __global__ void k_cell_info(MixedView m) {
 // Per leaf: leaf_of for its positions, FP32 local coordinates, circulation,
 // 1/sigma^2.
 // Per-position arrays of the mixed form, one warp per leaf.  Inside a leaf
-// the blobs are laid out in a spatial order: the Morton code of their FP64
-// offset from the leaf centre on a 256 x 256 grid over the leaf, ties by
-// tree position.  Consecutive blobs are then neighbours, so a 32-blob chunk
-// has a small bounding box (the near field culls correction chunks by it),
-// and the order depends only on the leaf's own blobs and geometry: a set
-// gets the same layout alone or in a batch.  mperm maps each position to
-// its original blob.  Leaves of more than kSortMax blobs keep the tree's
-// order (the rank sort is quadratic).
-constexpr int kSortMax = 1024;
+// the blobs are laid out by sub-cell: the leaf is cut into 8 x 8 sub-cells,
+// taken in Morton order, and the blobs of one sub-cell keep their tree
+// order (a stable counting sort: each 32-blob round groups equal sub-cells
+// with __match_any_sync, and shared-memory counters hold the running
+// offsets).  Consecutive blobs are then neighbours, so a 32-blob chunk has a
+// small bounding box (the near field culls correction chunks by it), and
+// the layout depends only on the leaf's own blobs and geometry: a set gets
+// the same layout alone or in a batch.  mperm maps each position to its
+// original blob.
+constexpr int kSubCells = 64;
+constexpr int kSetupWarps = 8;
 
-__device__ __forceinline__ unsigned spread8(unsigned v) {  // 8 bits -> even bits of 16
-  v = (v | (v << 4)) & 0x0f0fu;
-  v = (v | (v << 2)) & 0x3333u;
-  v = (v | (v << 1)) & 0x5555u;
+__device__ __forceinline__ unsigned spread3(unsigned v) {  // 3 bits -> even bits of 6
+  v = (v | (v << 2)) & 0x13u;
+  v = (v | (v << 1)) & 0x15u;
   return v;
 }
 
-__global__ void k_leaf_setup(MixedView m, const double *x, const double *y, const double *cir, const double *cor,
-                             const int *perm) {
-  const int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-  if (wid >= m.nleaf) return;
+__global__ void __launch_bounds__(32 * kSetupWarps) k_leaf_setup(MixedView m, const double *x, const double *y,
+                                                                 const double *cir, const double *cor,
+                                                                 const int *perm) {
+  __shared__ int s_cnt[kSetupWarps][kSubCells + 1];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int wid = blockIdx.x * kSetupWarps + warp;
+  if (wid >= m.nleaf) return;  // warp-uniform; nothing below syncs the block
+  int *cnt = s_cnt[warp];
   const int c = m.leaf_cell[wid];
   const double cx = m.cx[c], cy = m.cy[c], side = m.region[c];
-  const int b = m.begin[c], e = m.end[c], cnt = e - b;
-  const bool sorted = cnt <= kSortMax;
-  if (sorted) {
-    const double x0 = cx - 0.5 * side, y0 = cy - 0.5 * side, q = 256.0 / side;
-    for (int i = b + lane; i < e; i += 32) {
-      const int qx = min(max((int)((x[i] - x0) * q), 0), 255), qy = min(max((int)((y[i] - y0) * q), 0), 255);
-      m.skey[i] = ((spread8((unsigned)qx) | (spread8((unsigned)qy) << 1)) << 16) | (unsigned)(i - b);
-    }
+  const int b = m.begin[c], e = m.end[c];
+  const double x0 = cx - 0.5 * side, y0 = cy - 0.5 * side, q = 8.0 / side;
+  const unsigned lt = (1u << lane) - 1u;
+  auto code_of = [&](int i) {
+    const int qx = min(max((int)((x[i] - x0) * q), 0), 7), qy = min(max((int)((y[i] - y0) * q), 0), 7);
+    return (int)(spread3((unsigned)qx) | (spread3((unsigned)qy) << 1));
+  };
+  // pass 1: blobs per sub-cell
+  for (int k = lane; k <= kSubCells; k += 32) cnt[k] = 0;
+  __syncwarp();
+  for (int i0 = b; i0 < e; i0 += 32) {
+    const int i = i0 + lane;
+    const int code = i < e ? code_of(i) : kSubCells;
+    const unsigned grp = __match_any_sync(0xffffffffu, code);
+    if ((grp & lt) == 0) cnt[code] += __popc(grp);  // one leader per sub-cell
     __syncwarp();
   }
-  for (int i = b + lane; i < e; i += 32) {
-    int d = i;
-    if (sorted) {
-      const unsigned k = m.skey[i];
-      int r = 0;
-      for (int j = b; j < e; j++) r += m.skey[j] < k;
-      d = b + r;
+  // exclusive prefix over the sub-cells: the first position of each
+  if (lane == 0) {
+    int run = 0;
+    for (int k = 0; k < kSubCells; k++) {
+      const int v = cnt[k];
+      cnt[k] = run;
+      run += v;
     }
-    m.leaf_of[d] = c;
-    const float2 lc = make_float2((float)(x[i] - cx), (float)(y[i] - cy));
-    m.loc[d] = lc;
-    m.gam[d] = (float)cir[i];
-    // 1/sigma^2 is only kept in FP32, so it is formed in FP32 (the FP64
-    // divide is slow on this GPU and buys nothing after the rounding)
-    const float sf = (float)cor[i];
-    const float w = 1.f / (sf * sf);
-    m.s2inv[d] = w;
-    m.src4[d] = make_float4(lc.x, lc.y, m.gam[d], -1.44269504f * w);
-    m.mperm[d] = perm[i];
+  }
+  __syncwarp();
+  // pass 2: place every blob
+  for (int i0 = b; i0 < e; i0 += 32) {
+    const int i = i0 + lane;
+    const bool v = i < e;
+    const int code = v ? code_of(i) : kSubCells;
+    const unsigned grp = __match_any_sync(0xffffffffu, code);
+    const int d = b + cnt[code] + __popc(grp & lt);
+    __syncwarp();
+    if ((grp & lt) == 0) cnt[code] += __popc(grp);
+    __syncwarp();
+    if (v) {
+      m.leaf_of[d] = c;
+      const float2 lc = make_float2((float)(x[i] - cx), (float)(y[i] - cy));
+      m.loc[d] = lc;
+      m.gam[d] = (float)cir[i];
+      // 1/sigma^2 is only kept in FP32, so it is formed in FP32 (the FP64
+      // divide is slow on this GPU and buys nothing after the rounding)
+      const float sf = (float)cor[i];
+      const float w = 1.f / (sf * sf);
+      m.s2inv[d] = w;
+      m.src4[d] = make_float4(lc.x, lc.y, m.gam[d], -1.44269504f * w);
+      m.mperm[d] = perm[i];
+    }
   }
   __syncwarp();
   // each 32-blob chunk's bounding box, for the near field's correction cull
@@ -201,15 +227,15 @@ __global__ void k_leaf_setup(MixedView m, const double *x, const double *y, cons
     const int i = i0 + lane;
     const bool v = i < e;
     const float2 lc = v ? m.loc[i] : make_float2(0.f, 0.f);
-    float x0 = v ? lc.x : INFINITY, y0 = v ? lc.y : INFINITY, x1 = v ? lc.x : -INFINITY, y1 = v ? lc.y : -INFINITY;
+    float bx0 = v ? lc.x : INFINITY, by0 = v ? lc.y : INFINITY, bx1 = v ? lc.x : -INFINITY, by1 = v ? lc.y : -INFINITY;
     for (int o = 16; o; o >>= 1) {
-      x0 = fminf(x0, __shfl_xor_sync(0xffffffffu, x0, o));
-      y0 = fminf(y0, __shfl_xor_sync(0xffffffffu, y0, o));
-      x1 = fmaxf(x1, __shfl_xor_sync(0xffffffffu, x1, o));
-      y1 = fmaxf(y1, __shfl_xor_sync(0xffffffffu, y1, o));
+      bx0 = fminf(bx0, __shfl_xor_sync(0xffffffffu, bx0, o));
+      by0 = fminf(by0, __shfl_xor_sync(0xffffffffu, by0, o));
+      bx1 = fmaxf(bx1, __shfl_xor_sync(0xffffffffu, bx1, o));
+      by1 = fmaxf(by1, __shfl_xor_sync(0xffffffffu, by1, o));
     }
     const int k = (i0 - b) >> 5;
-    if (lane == 0 && k < m.kchunks) m.cbox[(size_t)c * m.kchunks + k] = make_float4(x0, y0, x1, y1);
+    if (lane == 0 && k < m.kchunks) m.cbox[(size_t)c * m.kchunks + k] = make_float4(bx0, by0, bx1, by1);
   }
 }
 
@@ -1902,7 +1928,8 @@ int mixed_fill_lists(MixedView &m, bool from_scratch, cudaStream_t s) {
 }
 
 int mixed_leaf_setup(MixedView &m, const Tree &t, cudaStream_t s) {
-  k_leaf_setup<<<(int)(((long)m.nleaf * 32 + 255) / 256), 256, 0, s>>>(m, t.x, t.y, t.cir, t.cor, t.perm);
+  k_leaf_setup<<<(m.nleaf + kSetupWarps - 1) / kSetupWarps, 32 * kSetupWarps, 0, s>>>(m, t.x, t.y, t.cir, t.cor,
+                                                                                        t.perm);
   g_launches.fetch_add(1, std::memory_order_relaxed);
   T2D_CUDA_TRY(cudaGetLastError());
   return TREE2D_OK;
@@ -2094,7 +2121,7 @@ int mixed_solve(Workspace &ws, const Tree &t, const MixedParams &mp, double *d_u
   need += Arena::bytes_for(n, 16) + Arena::bytes_for(nc, 4) * 4;  // src4, cxf, cyf, cxl, cyl
   const int kchunks = t.leaf_cap > 0 ? (t.leaf_cap + 31) / 32 : 1;
   need += Arena::bytes_for((size_t)nc * kchunks, 16);              // chunk boxes
-  need += Arena::bytes_for(n, 4) * 2;                              // mperm, skey
+  need += Arena::bytes_for(n, 4);                                  // mperm
   need += Arena::bytes_for((size_t)nc * 9, 4) * 2;
   need += Arena::bytes_for((size_t)nc * 27, 4) + Arena::bytes_for((size_t)nc * 8, 4);
   need += Arena::bytes_for((size_t)nl + 1, 4) * 3;
@@ -2142,7 +2169,6 @@ int mixed_solve(Workspace &ws, const Tree &t, const MixedParams &mp, double *d_u
   m.kchunks = kchunks;
   m.cbox = ws.mx_arena.take<float4>((size_t)nc * kchunks);
   m.mperm = ws.mx_arena.take<int>(n);
-  m.skey = ws.mx_arena.take<unsigned>(n);
   m.cxf = ws.mx_arena.take<float>(nc);
   m.cyf = ws.mx_arena.take<float>(nc);
   m.cxl = ws.mx_arena.take<float>(nc);

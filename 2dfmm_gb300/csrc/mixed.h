@@ -33,9 +33,8 @@ struct MixedView {
   float *gam, *s2inv;    // per position
   float4 *src4;          // per position {loc.x, loc.y, G, -log2(e)/sigma^2}
   int *mperm;            // per position: original blob index.  The per-position arrays of the
-                         // mixed form hold each leaf's blobs in a spatial order (a Morton code of
-                         // the offset from the leaf centre, ties by tree position), not the tree's
-  unsigned *skey;        // per position: scratch of that ordering
+                         // mixed form hold each leaf's blobs by sub-cell (8 x 8 sub-cells in
+                         // Morton order, tree order inside one), not in the tree's order
   float4 *cbox;          // per leaf cell, kchunks entries: bounding box {xmin, ymin, xmax, ymax}
                          // of each 32-blob chunk of the leaf (from its first blob), leaf-local
   int kchunks;           // chunk boxes per cell: ceil(most blobs per leaf / 32)
