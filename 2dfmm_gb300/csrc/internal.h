@@ -80,6 +80,7 @@ struct DevStatus {
   unsigned long long k_blobs;  // mixed: source blobs of the K leaves of all leaves, out to the walk radius
   unsigned long long n_pairs_k;   // mixed: correction pairs evaluated (part of n_pairs)
   unsigned long long n_pairs_k_listed;  // mixed: correction pairs of the K entries evaluated, before the chunk cull
+  unsigned eval_next;      // mixed: next target leaf of the persistent near-field warps
 };
 
 // Bump allocator over one device allocation.  Buffers are 256-byte aligned.

@@ -219,8 +219,6 @@ __global__ void __launch_bounds__(32 * kSetupWarps) k_leaf_setup(MixedView m, co
       m.s2inv[d] = w;
       const float g = m.gam[d], tw = -1.44269504f * w;
       m.src4[d] = make_float4(lc.x, lc.y, g, tw);
-      m.src8[2 * (size_t)d] = make_float4(-lc.x, -lc.x, -lc.y, -lc.y);
-      m.src8[2 * (size_t)d + 1] = make_float4(g, g, tw, tw);
       m.mperm[d] = perm[i];
     }
   }
@@ -1259,91 +1257,23 @@ __device__ __forceinline__ void pair2(const float4 sj, float2 tx, float2 ty, flo
   sy = __ffma2_rn(f, rx, sy);
 }
 
-// pair2 from the duplicated source record (src8: a = {-x, -x, -y, -y},
-// b = {G, G, w, w} with w = -log2(e)/sigma^2): every operand is already a
-// register pair, so no per-source broadcast is needed, and the signs are
-// arranged so that no per-pair negation is either.  It accumulates
-//   direct (U):     (-sx, sy) of pair2<false>,
-//   correction (K): (sx, -sy) of pair2<true>,
-// each bit for bit (negation is exact and commutes with rounding); the
-// caller applies the signs once per source leaf.
-template <bool kCorrection>
-__device__ __forceinline__ void pair2_dup(const float4 a, const float4 b, float2 tx, float2 ty, float2 &px,
-                                          float2 &py) {
-  const float2 rx = __fadd2_rn(tx, make_float2(a.x, a.y)), ry = __fadd2_rn(ty, make_float2(a.z, a.w));
-  const float2 r2 = __ffma2_rn(rx, rx, __ffma2_rn(ry, ry, f2(1e-30f)));
-  const float2 t = __fmul2_rn(r2, make_float2(b.z, b.w));
-  const float2 e = make_float2(sfu_exp2(t.x), sfu_exp2(t.y));
-  const float2 ir2 = make_float2(sfu_rcp(r2.x), sfu_rcp(r2.y));
-  float2 f;
-  if (!kCorrection) {
-    const float2 x2 = __fmul2_rn(t, f2(-0.69314718f));
-    const float2 ser = __fmul2_rn(x2, __ffma2_rn(f2(-0.5f), x2, f2(1.f)));
-    const float2 ome = __ffma2_rn(e, f2(-1.f), f2(1.f));
-    const float2 e1f = make_float2(t.x > -1.44269504e-3f ? ser.x : ome.x, t.y > -1.44269504e-3f ? ser.y : ome.y);
-    f = __fmul2_rn(__fmul2_rn(make_float2(b.x, b.y), e1f), ir2);
-  } else {
-    f = __fmul2_rn(__fmul2_rn(make_float2(b.x, b.y), e), ir2);  // G e / r^2: minus the correction's factor
-  }
-  px = __ffma2_rn(f, ry, px);
-  py = __ffma2_rn(f, rx, py);
-}
-
-// The scalar pair from the duplicated record (one target per lane), with
-// pair<>'s roundings and signs.
-template <bool kCorrection>
-__device__ __forceinline__ void pair_dup(const float4 a, const float4 b, float tx, float ty, float &sx, float &sy) {
-  const float rx = __fadd_rn(tx, a.x), ry = __fadd_rn(ty, a.z);
-  const float r2 = fmaf(rx, rx, fmaf(ry, ry, 1e-30f));
-  const float t = __fmul_rn(r2, b.z);
-  const float e = sfu_exp2(t);
-  const float ir2 = sfu_rcp(r2);
-  float f;
-  if (!kCorrection) {
-    const float x2 = __fmul_rn(t, -0.69314718f);
-    const float ser = __fmul_rn(x2, fmaf(-0.5f, x2, 1.f)), ome = __fsub_rn(1.f, e);
-    const float e1f = t > -1.44269504e-3f ? ser : ome;
-    f = __fmul_rn(__fmul_rn(b.x, e1f), ir2);
-  } else {
-    f = -__fmul_rn(__fmul_rn(b.x, e), ir2);
-  }
-  sx = fmaf(-f, ry, sx);
-  sy = fmaf(f, rx, sy);
-}
-
 // Direct (U list) or correction (K list) contributions of one source leaf
 // to the lane's two targets.  Each leaf is summed in plain FP32 and then
 // added with compensation, so the compensated sum costs once per leaf, not
-// once per pair.  kDup: `src` holds the duplicated records (two float4 per
-// source, src8) instead of one (src4); the sums are the same bit for bit.
-template <bool kCorrection, bool kDup = false>
+// once per pair.
+template <bool kCorrection>
 __device__ __forceinline__ void leaf_pairs(const float4 *__restrict__ src, int j0, int j1, float txa, float tya,
                                            float txb, float tyb, bool two, float &sxa, float &sya, float &sxb,
                                            float &syb) {
   if (two) {
     const float2 tx = make_float2(txa, txb), ty = make_float2(tya, tyb);
-    if (kDup) {
-      // U accumulates (-sx, sy), K (sx, -sy): see pair2_dup
-      float2 px = kCorrection ? make_float2(sxa, sxb) : make_float2(-sxa, -sxb);
-      float2 py = kCorrection ? make_float2(-sya, -syb) : make_float2(sya, syb);
+    float2 sx = make_float2(sxa, sxb), sy = make_float2(sya, syb);
 #pragma unroll 2
-      for (int j = j0; j < j1; j++) pair2_dup<kCorrection>(src[2 * j], src[2 * j + 1], tx, ty, px, py);
-      sxa = kCorrection ? px.x : -px.x;
-      sxb = kCorrection ? px.y : -px.y;
-      sya = kCorrection ? -py.x : py.x;
-      syb = kCorrection ? -py.y : py.y;
-    } else {
-      float2 sx = make_float2(sxa, sxb), sy = make_float2(sya, syb);
-#pragma unroll 2
-      for (int j = j0; j < j1; j++) pair2<kCorrection>(src[j], tx, ty, sx, sy);
-      sxa = sx.x;
-      sxb = sx.y;
-      sya = sy.x;
-      syb = sy.y;
-    }
-  } else if (kDup) {
-#pragma unroll 4
-    for (int j = j0; j < j1; j++) pair_dup<kCorrection>(src[2 * j], src[2 * j + 1], txa, tya, sxa, sya);
+    for (int j = j0; j < j1; j++) pair2<kCorrection>(src[j], tx, ty, sx, sy);
+    sxa = sx.x;
+    sxb = sx.y;
+    sya = sy.x;
+    syb = sy.y;
   } else {
 #pragma unroll 4
     for (int j = j0; j < j1; j++) pair<kCorrection>(src[j], txa, tya, sxa, sya);
@@ -1354,6 +1284,17 @@ struct Decisions {
   const unsigned char *u, *k;  // class per U / K entry; null: all direct
   int margin;
 };
+
+// Persistent near-field warps: the grid holds as many warps as fit on the
+// GPU at once, and each warp takes the next target leaf from a counter
+// (DevStatus::eval_next, zeroed before each launch) until none is left.
+// Leaves differ widely in work, so a warp that finishes early takes more
+// instead of idling beside the slowest warp of a resident block.
+__device__ __forceinline__ int next_leaf(DevStatus *st, int lane) {
+  int l = 0;
+  if (lane == 0) l = (int)atomicAdd(&st->eval_next, 1u);
+  return __shfl_sync(0xffffffffu, l, 0);
+}
 
 // Correction radius of leaf cell B: the tree's, or in a batched tree its
 // set's (the same rule as the list walk, k_lists).
@@ -1483,16 +1424,15 @@ __device__ __forceinline__ unsigned chunk_mask(const MixedView &m, int A, float 
 constexpr int kStage = 128;  // blobs per stage buffer: the largest leaf of the default leaf sizes
 constexpr long kEvalWaitLimit = 1l << 22;  // polls; a healthy copy lands within microseconds
 
-template <bool kLearned, int kWarps, bool kDup = false>
+template <bool kLearned, int kWarps>
 __global__ void __launch_bounds__(32 * kWarps, 32 / kWarps) k_eval_staged(MixedView m, double *uv, const int *perm,
                                                                            Decisions dec, long wait_limit) {
-  constexpr int kRec = kDup ? 2 : 1;  // float4 records per source
-  __shared__ __align__(128) float4 s_src[kWarps][2][kStage * kRec];
+  __shared__ __align__(128) float4 s_src[kWarps][2][kStage];
   __shared__ __align__(8) uint64_t s_bar[kWarps][2];
   __shared__ float s_tb[kWarps][5];  // target box and rc^2 of the warp's chunk
   __shared__ WarpCounts s_cnt[kWarps];
-  const int warp = threadIdx.x >> 5;
-  const int l = blockIdx.x * kWarps + warp, lane = threadIdx.x & 31;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  int l = next_leaf(m.st, lane);
   if (l >= m.nleaf) return;  // uniform over the warp; nothing below syncs the block
   uint64_t *bar = s_bar[warp];
   if (lane == 0) {
@@ -1504,13 +1444,14 @@ __global__ void __launch_bounds__(32 * kWarps, 32 / kWarps) k_eval_staged(MixedV
   unsigned parity = 0;    // bit b: parity of buffer b's next completion
   unsigned inflight = 0;  // bit b: a copy into buffer b not yet waited for
   bool staging = true;    // false after a wait gave up
-  const int B = m.leaf_cell[l];
   const double inv2pi = 0.15915494309189533577;
-  const int u0 = m.u_off[l], nu = m.u_off[l + 1] - u0;
-  const int k0 = m.k_off[l], nk = m.k_off[l + 1] - k0;
   float *tbox = s_tb[warp];
   WarpCounts *cnts = &s_cnt[warp];
   if (lane == 0) *cnts = WarpCounts{};
+  for (; l < m.nleaf; l = next_leaf(m.st, lane)) {
+  const int B = m.leaf_cell[l];
+  const int u0 = m.u_off[l], nu = m.u_off[l + 1] - u0;
+  const int k0 = m.k_off[l], nk = m.k_off[l + 1] - k0;
   // position q of the walk: U entries, then K entries
   auto src_leaf = [&](int q) { return q < nu ? m.u_idx[u0 + q] : m.k_idx[k0 + q - nu]; };
   auto direct = [&](int q) {
@@ -1524,8 +1465,8 @@ __global__ void __launch_bounds__(32 * kWarps, 32 / kWarps) k_eval_staged(MixedV
     if (!staging || cnt > kStage) return false;
     if (lane == 0) {
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-      mbar_expect_tx(&bar[b], (uint32_t)cnt * 16u * kRec);
-      bulk_g2s(s_src[warp][b], kDup ? m.src8 + 2 * (size_t)j0 : m.src4 + j0, (uint32_t)cnt * 16u * kRec, &bar[b]);
+      mbar_expect_tx(&bar[b], (uint32_t)cnt * 16u);
+      bulk_g2s(s_src[warp][b], m.src4 + j0, (uint32_t)cnt * 16u, &bar[b]);
     }
     inflight |= 1u << b;
     return true;
@@ -1603,15 +1544,15 @@ __global__ void __launch_bounds__(32 * kWarps, 32 / kWarps) k_eval_staged(MixedV
       }
       float sxa = 0.f, sya = 0.f, sxb = 0.f, syb = 0.f;
       const float txa = __fadd_rn(za.x, ox), tya = __fadd_rn(za.y, oy), txb = __fadd_rn(zb.x, ox), tyb = __fadd_rn(zb.y, oy);
-      const float4 *src = use_smem ? s_src[warp][buf] : (kDup ? m.src8 + 2 * (size_t)j0 : m.src4 + j0);
+      const float4 *src = use_smem ? s_src[warp][buf] : m.src4 + j0;
       int done = 0;
       for (unsigned r = msk; r;) {
         int s0, s1;
         next_run(r, cnt, s0, s1);
         if (q < nu)
-          leaf_pairs<false, kDup>(src, s0, s1, txa, tya, txb, tyb, two, sxa, sya, sxb, syb);
+          leaf_pairs<false>(src, s0, s1, txa, tya, txb, tyb, two, sxa, sya, sxb, syb);
         else
-          leaf_pairs<true, kDup>(src, s0, s1, txa, tya, txb, tyb, two, sxa, sya, sxb, syb);
+          leaf_pairs<true>(src, s0, s1, txa, tya, txb, tyb, two, sxa, sya, sxb, syb);
         done += s1 - s0;
       }
       kahan(axa, cxa, sxa);
@@ -1638,6 +1579,7 @@ __global__ void __launch_bounds__(32 * kWarps, 32 / kWarps) k_eval_staged(MixedV
       uv[2 * (size_t)o + 1] = ((double)pb.x + (double)ayb - (double)cyb) * inv2pi;
     }
   }
+  }  // next leaf
   // copies still in flight after a wait gave up: wait (bounded) before the
   // shared memory is released
   for (int b = 0; b < 2; b++)
@@ -1647,18 +1589,20 @@ __global__ void __launch_bounds__(32 * kWarps, 32 / kWarps) k_eval_staged(MixedV
 
 // The same near field with the source blobs read straight from global
 // memory (through L1), the other variant the tuner times.
-template <bool kLearned, int kWarps, bool kDup = false>
+template <bool kLearned, int kWarps>
 __global__ void __launch_bounds__(32 * kWarps, 32 / kWarps) k_eval_mixed(MixedView m, double *uv, const int *perm,
                                                                           Decisions dec, long) {
   __shared__ float s_tb[kWarps][5];  // target box and rc^2 of the warp's chunk
   __shared__ WarpCounts s_cnt[kWarps];
-  const int l = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  const int lane = threadIdx.x & 31;
+  int l = next_leaf(m.st, lane);
   if (l >= m.nleaf) return;
-  const int B = m.leaf_cell[l];
   const double inv2pi = 0.15915494309189533577;
   float *tbox = s_tb[threadIdx.x >> 5];
   WarpCounts *cnts = &s_cnt[threadIdx.x >> 5];
   if (lane == 0) *cnts = WarpCounts{};
+  for (; l < m.nleaf; l = next_leaf(m.st, lane)) {
+  const int B = m.leaf_cell[l];
   const float rc = leaf_cutoff(m, B);
   for (int t0 = m.begin[B]; t0 < m.end[B]; t0 += 64) {
     const int ta = t0 + lane, tb = t0 + 32 + lane;
@@ -1714,11 +1658,10 @@ __global__ void __launch_bounds__(32 * kWarps, 32 / kWarps) k_eval_mixed(MixedVi
         for (unsigned r = msk; r;) {
           int s0, s1;
           next_run(r, j1 - j0, s0, s1);
-          const float4 *src = kDup ? m.src8 + 2 * (size_t)j0 : m.src4 + j0;
           if (pass == 0)
-            leaf_pairs<false, kDup>(src, s0, s1, txa, tya, txb, tyb, two, sxa, sya, sxb, syb);
+            leaf_pairs<false>(m.src4 + j0, s0, s1, txa, tya, txb, tyb, two, sxa, sya, sxb, syb);
           else
-            leaf_pairs<true, kDup>(src, s0, s1, txa, tya, txb, tyb, two, sxa, sya, sxb, syb);
+            leaf_pairs<true>(m.src4 + j0, s0, s1, txa, tya, txb, tyb, two, sxa, sya, sxb, syb);
           done += s1 - s0;
         }
         counts_add(cnts, lane, (unsigned)done, pass == 1 ? (unsigned)done : 0u, pass == 1 ? (unsigned)(j1 - j0) : 0u);
@@ -1741,6 +1684,7 @@ __global__ void __launch_bounds__(32 * kWarps, 32 / kWarps) k_eval_mixed(MixedVi
       uv[2 * (size_t)o + 1] = ((double)pb.x + (double)ayb - (double)cyb) * inv2pi;
     }
   }
+  }  // next leaf
   counts_flush(cnts, lane, m.st);
 }
 
@@ -2063,32 +2007,53 @@ int mixed_downward(MixedView &m, int depth, const int *lev_off, cudaStream_t s) 
 
 // Near-field variants (bit-identical results): 0/1 read the source blobs
 // from global memory with 4/8 warps per block, 2/3 stage them in shared
-// memory by bulk copies with 4/8 warps per block; 4/5 are 0/2 on the
-// duplicated 32-byte records (src8), which spare the per-source operand
-// broadcasts at twice the bytes per source.
-constexpr int kEvalVariants = 6;
+// memory by bulk copies with 4/8 warps per block.
+constexpr int kEvalVariants = 4;
+
+// Blocks of a persistent near-field launch: as many as are resident on the
+// device at once (the kernel's occupancy times the SM count, found once per
+// kernel and kept in *resident), fewer when the leaves are fewer.
+template <class K>
+int persistent_blocks(K kernel, int warps_per_block, int nleaf, int *resident) {
+  if (*resident == 0) {
+    int dev = 0, sms = 0, per_sm = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, 32 * warps_per_block, 0) != cudaSuccess ||
+        per_sm < 1)
+      return (nleaf + warps_per_block - 1) / warps_per_block;  // one warp per leaf
+    *resident = sms * per_sm;
+  }
+  const int need = (nleaf + warps_per_block - 1) / warps_per_block;
+  return need < *resident ? need : *resident;
+}
 
 template <bool kLearned>
 cudaError_t launch_eval(int v, const MixedView &m, double *uv, const int *perm, Decisions d, cudaStream_t s) {
+  static int resident[kEvalVariants] = {};  // per variant (the devices here are all one model)
+  cudaError_t e = cudaMemsetAsync(&m.st->eval_next, 0, sizeof(unsigned), s);
+  if (e != cudaSuccess) return e;
   switch (v) {
-    case 0:
-      k_eval_mixed<kLearned, 4><<<(m.nleaf + 3) / 4, 128, 0, s>>>(m, uv, perm, d, kEvalWaitLimit);
+    case 0: {
+      auto k = k_eval_mixed<kLearned, 4>;
+      k<<<persistent_blocks(k, 4, m.nleaf, &resident[0]), 128, 0, s>>>(m, uv, perm, d, kEvalWaitLimit);
       break;
-    case 1:
-      k_eval_mixed<kLearned, 8><<<(m.nleaf + 7) / 8, 256, 0, s>>>(m, uv, perm, d, kEvalWaitLimit);
+    }
+    case 1: {
+      auto k = k_eval_mixed<kLearned, 8>;
+      k<<<persistent_blocks(k, 8, m.nleaf, &resident[1]), 256, 0, s>>>(m, uv, perm, d, kEvalWaitLimit);
       break;
-    case 2:
-      k_eval_staged<kLearned, 4><<<(m.nleaf + 3) / 4, 128, 0, s>>>(m, uv, perm, d, kEvalWaitLimit);
+    }
+    case 2: {
+      auto k = k_eval_staged<kLearned, 4>;
+      k<<<persistent_blocks(k, 4, m.nleaf, &resident[2]), 128, 0, s>>>(m, uv, perm, d, kEvalWaitLimit);
       break;
-    case 3:
-      k_eval_staged<kLearned, 8><<<(m.nleaf + 7) / 8, 256, 0, s>>>(m, uv, perm, d, kEvalWaitLimit);
+    }
+    default: {
+      auto k = k_eval_staged<kLearned, 8>;
+      k<<<persistent_blocks(k, 8, m.nleaf, &resident[3]), 256, 0, s>>>(m, uv, perm, d, kEvalWaitLimit);
       break;
-    case 4:
-      k_eval_mixed<kLearned, 4, true><<<(m.nleaf + 3) / 4, 128, 0, s>>>(m, uv, perm, d, kEvalWaitLimit);
-      break;
-    default:
-      k_eval_staged<kLearned, 4, true><<<(m.nleaf + 3) / 4, 128, 0, s>>>(m, uv, perm, d, kEvalWaitLimit);
-      break;
+    }
   }
   g_launches.fetch_add(1, std::memory_order_relaxed);
   return cudaGetLastError();
@@ -2203,7 +2168,6 @@ int mixed_solve(Workspace &ws, const Tree &t, const MixedParams &mp, double *d_u
   const int kchunks = t.leaf_cap > 0 ? (t.leaf_cap + 31) / 32 : 1;
   need += Arena::bytes_for((size_t)nc * kchunks, 16);              // chunk boxes
   need += Arena::bytes_for(n, 4);                                  // mperm
-  need += Arena::bytes_for(2 * (size_t)n, 16);                     // src8
   need += Arena::bytes_for((size_t)nc * 9, 4) * 2;
   need += Arena::bytes_for((size_t)nc * 27, 4) + Arena::bytes_for((size_t)nc * 8, 4);
   need += Arena::bytes_for((size_t)nl + 1, 4) * 3;
@@ -2251,7 +2215,6 @@ int mixed_solve(Workspace &ws, const Tree &t, const MixedParams &mp, double *d_u
   m.kchunks = kchunks;
   m.cbox = ws.mx_arena.take<float4>((size_t)nc * kchunks);
   m.mperm = ws.mx_arena.take<int>(n);
-  m.src8 = ws.mx_arena.take<float4>(2 * (size_t)n);
   m.cxf = ws.mx_arena.take<float>(nc);
   m.cyf = ws.mx_arena.take<float>(nc);
   m.cxl = ws.mx_arena.take<float>(nc);

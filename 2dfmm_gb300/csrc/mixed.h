@@ -32,8 +32,6 @@ struct MixedView {
   float2 *loc;           // per position, offset from its leaf centre
   float *gam, *s2inv;    // per position
   float4 *src4;          // per position {loc.x, loc.y, G, -log2(e)/sigma^2}
-  float4 *src8;          // per position, two records: {-x, -x, -y, -y}, {G, G, w, w} (x, y = loc,
-                         // w = -log2(e)/sigma^2): the near field's duplicated-operand form
   int *mperm;            // per position: original blob index.  The per-position arrays of the
                          // mixed form hold each leaf's blobs by sub-cell (8 x 8 sub-cells in
                          // Morton order, tree order inside one), not in the tree's order

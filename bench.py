@@ -57,7 +57,7 @@ def parse():
     ap.add_argument("--cuda-core-m2l", action="store_true", help="mixed form: M2L on CUDA cores")
     ap.add_argument("--no-plain", action="store_true", help="skip timing the plain FP64 path beside")
     ap.add_argument("--eval-variant", type=int, default=-1,
-                    help="mixed/learned: force a near-field kernel variant 0..5 (default: the tuner's choice)")
+                    help="mixed/learned: force a near-field kernel variant 0..3 (default: the tuner's choice)")
     ap.add_argument("--workload", default="two_patch_sheet",
                     choices=["two_patch_sheet", "lamb_oseen", "uniform", "batch_sets", "advected"])
     ap.add_argument("--no-extras", action="store_true",
@@ -473,7 +473,7 @@ def run_ours(args):
                        "l2": "flushed between steps (256 MiB write); inputs 134 MB > L2"},
             "gpu_launches": int(sum(s["n_launches"] for s in sts)),
             "tuned": {"eval_variant": int(st["eval_variant"]),
-                      "variants": "0/1 global loads, 2/3 bulk-copy staging (4/8 warps per block); 4/5 the same (4 warps) on duplicated 32-byte source records"},
+                      "variants": "0/1 global loads, 2/3 bulk-copy staging; 4/8 warps per block"},
             "learned_active": bool(st["learned_active"]),
             "k_list_per_leaf": st["n_list_k"] / max(1, st["n_leaves"]),
             "k_list_blobs_per_leaf": st["n_list_k_blobs"] / max(1, st["n_leaves"]),
@@ -640,7 +640,7 @@ def run_batch(args):
                        "l2": "flushed between steps (256 MiB write)"},
             "gpu_launches": int(sum(x["n_launches"] for x in sts)),
             "tuned": {"eval_variant": int(st["eval_variant"]),
-                      "variants": "0/1 global loads, 2/3 bulk-copy staging (4/8 warps per block); 4/5 the same (4 warps) on duplicated 32-byte source records"},
+                      "variants": "0/1 global loads, 2/3 bulk-copy staging; 4/8 warps per block"},
             "e2e": {"value": world * n / e2e_t, "unit": UNIT, "h2d_bytes_per_step": n * 32,
                     "d2h_bytes_per_step": n * 16, "api": "host->device copies + tree2d_solve_sets + device->host"},
             "roofline": {"bound": "fp32", "achieved": flops / (ms_eval * 1e-3) / 1e12, "peak": peak,

@@ -152,8 +152,7 @@ typedef struct {
   int m2l_path;           /* mixed: 1 = CUDA cores, 2 = tensor cores  */
   int eval_variant;       /* mixed: near-field kernel variant that ran
                              (0/1: global loads, 4/8 warps per block;
-                              2/3: blobs staged by bulk copies, 4/8;
-                              4/5: 0/2 on duplicated 32-byte records)  */
+                              2/3: blobs staged by bulk copies, 4/8)    */
   int learned_active;     /* learned: 1 if the network's decisions were
                              applied, 0 if the solve ran the fixed mixed
                              form (no weights, a batched tree, or lists
@@ -190,12 +189,10 @@ int tree2d_direct_device(int ntgt, const double *d_txy, int nsrc, const double *
 /* Near-field kernel tuning of the mixed/learned forms.  The variants give
  * bit-identical results and differ only in speed: source blobs read from
  * global memory or staged in shared memory by bulk copies, 4 or 8 warps
- * per block, 16-byte source records or duplicated 32-byte ones (4: global
- * loads, 5: staged, both 4 warps).  autotune = 1 (default): the first solve
- * of each (device, form, P, leaf-count class) times every variant with CUDA
- * events and keeps the fastest; eval_variant >= 0 forces one (0..5);
- * eval_variant = -1 with autotune = 0 runs variant 0.  No counterpart in
- * the reference. */
+ * per block.  autotune = 1 (default): the first solve of each (device,
+ * form, P, leaf-count class) times every variant with CUDA events and keeps
+ * the fastest; eval_variant >= 0 forces one (0..3); eval_variant = -1 with
+ * autotune = 0 runs variant 0.  No counterpart in the reference. */
 int tree2d_set_tuning(int autotune, int eval_variant);
 
 /* Batched solve of nsets independent blob sets in one tree: set k is blobs
