@@ -35,6 +35,7 @@
 // centre, formed from the FP64 centres), compensated (Kahan) sums for the
 // direct and correction terms, FP64 for the final per-target reduction.
 #include <cmath>
+#include <type_traits>
 #include <vector>
 
 #include "dev_common.cuh"
@@ -139,20 +140,23 @@ __global__ void k_cell_info(MixedView m) {
   m.cyl[c] = (float)(m.cy[c] - (double)m.cyf[c]);
 }
 
-// Per leaf: leaf_of for its positions, FP32 local coordinates, circulation,
-// 1/sigma^2.
-// Per-position arrays of the mixed form, one warp per leaf.  Inside a leaf
-// the blobs are laid out by sub-cell: the leaf is cut into 8 x 8 sub-cells,
-// taken in Morton order, and the blobs of one sub-cell keep their tree
-// order (a stable counting sort: each 32-blob round groups equal sub-cells
-// with __match_any_sync, and shared-memory counters hold the running
-// offsets).  Consecutive blobs are then neighbours, so a 32-blob chunk has a
-// small bounding box (the near field culls correction chunks by it), and
-// the layout depends only on the leaf's own blobs and geometry: a set gets
-// the same layout alone or in a batch.  mperm maps each position to its
-// original blob.
+// Per-position arrays of the mixed form (leaf_of, FP32 offsets from the
+// leaf centre, circulation, 1/sigma^2, the near field's source records),
+// one warp per leaf.  Inside a leaf the blobs are laid out by sub-cell: the
+// leaf is cut into 8 x 8 sub-cells, taken in Morton order, and the blobs of
+// one sub-cell keep their tree order (a stable counting sort: each 32-blob
+// round groups equal sub-cells with __match_any_sync, shared-memory
+// counters hold the running offsets).  Consecutive blobs are then
+// neighbours, so a 32-blob chunk has a small bounding box (the near field
+// culls correction chunks by it), and the layout depends only on the
+// leaf's own blobs and geometry: a set gets the same layout alone or in a
+// batch.  mperm maps each position to its original blob.  The sub-cell of a
+// blob comes from its FP32 offset; the offsets and sub-cells of a leaf's
+// first kSetupStage blobs are kept in shared memory between the passes
+// (larger leaves form the rest again from global memory).
 constexpr int kSubCells = 64;
 constexpr int kSetupWarps = 8;
+constexpr int kSetupStage = 128;
 
 __device__ __forceinline__ unsigned spread3(unsigned v) {  // 3 bits -> even bits of 6
   v = (v | (v << 2)) & 0x13u;
@@ -163,7 +167,10 @@ __device__ __forceinline__ unsigned spread3(unsigned v) {  // 3 bits -> even bit
 __global__ void __launch_bounds__(32 * kSetupWarps) k_leaf_setup(MixedView m, const double *x, const double *y,
                                                                  const double *cir, const double *cor,
                                                                  const int *perm) {
-  __shared__ int s_cnt[kSetupWarps][kSubCells + 1];
+  __shared__ int s_cnt[kSetupWarps][kSubCells];
+  __shared__ float2 s_lc[kSetupWarps][kSetupStage];   // offsets, in tree order
+  __shared__ float2 s_out[kSetupWarps][kSetupStage];  // offsets, in the new order
+  __shared__ unsigned char s_code[kSetupWarps][kSetupStage];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int wid = blockIdx.x * kSetupWarps + warp;
   if (wid >= m.nleaf) return;  // warp-uniform; nothing below syncs the block
@@ -171,69 +178,96 @@ __global__ void __launch_bounds__(32 * kSetupWarps) k_leaf_setup(MixedView m, co
   const int c = m.leaf_cell[wid];
   const double cx = m.cx[c], cy = m.cy[c], side = m.region[c];
   const int b = m.begin[c], e = m.end[c];
-  const double x0 = cx - 0.5 * side, y0 = cy - 0.5 * side, q = 8.0 / side;
+  const float hs = (float)(0.5 * side), q = (float)(8.0 / side);
   const unsigned lt = (1u << lane) - 1u;
-  auto code_of = [&](int i) {
-    const int qx = min(max((int)((x[i] - x0) * q), 0), 7), qy = min(max((int)((y[i] - y0) * q), 0), 7);
+  auto offset_of = [&](int i) { return make_float2((float)(x[i] - cx), (float)(y[i] - cy)); };
+  auto code_of = [&](float2 lc) {
+    const int qx = min(max((int)(__fmul_rn(__fadd_rn(lc.x, hs), q)), 0), 7);
+    const int qy = min(max((int)(__fmul_rn(__fadd_rn(lc.y, hs), q)), 0), 7);
     return (int)(spread3((unsigned)qx) | (spread3((unsigned)qy) << 1));
   };
   // pass 1: blobs per sub-cell
-  for (int k = lane; k <= kSubCells; k += 32) cnt[k] = 0;
+  cnt[lane] = 0;
+  cnt[lane + 32] = 0;
   __syncwarp();
   for (int i0 = b; i0 < e; i0 += 32) {
-    const int i = i0 + lane;
-    const int code = i < e ? code_of(i) : kSubCells;
+    const int i = i0 + lane, o = i - b;
+    int code = kSubCells;
+    if (i < e) {
+      const float2 lc = offset_of(i);
+      code = code_of(lc);
+      if (o < kSetupStage) {
+        s_lc[warp][o] = lc;
+        s_code[warp][o] = (unsigned char)code;
+      }
+    }
     const unsigned grp = __match_any_sync(0xffffffffu, code);
-    if ((grp & lt) == 0) cnt[code] += __popc(grp);  // one leader per sub-cell
+    if (code < kSubCells && (grp & lt) == 0) cnt[code] += __popc(grp);  // one leader per sub-cell
     __syncwarp();
   }
-  // exclusive prefix over the sub-cells: the first position of each
-  if (lane == 0) {
-    int run = 0;
-    for (int k = 0; k < kSubCells; k++) {
-      const int v = cnt[k];
-      cnt[k] = run;
-      run += v;
+  // exclusive prefix over the sub-cells (two per lane): the first position of each
+  {
+    const int c0 = cnt[2 * lane], c1 = cnt[2 * lane + 1];
+    int incl = c0 + c1;
+    for (int d = 1; d < 32; d <<= 1) {
+      const int t = __shfl_up_sync(0xffffffffu, incl, d);
+      if (lane >= d) incl += t;
     }
+    const int excl = incl - c0 - c1;
+    __syncwarp();
+    cnt[2 * lane] = excl;
+    cnt[2 * lane + 1] = excl + c0;
   }
   __syncwarp();
   // pass 2: place every blob
   for (int i0 = b; i0 < e; i0 += 32) {
-    const int i = i0 + lane;
+    const int i = i0 + lane, o = i - b;
     const bool v = i < e;
-    const int code = v ? code_of(i) : kSubCells;
+    float2 lc = make_float2(0.f, 0.f);
+    int code = kSubCells;
+    if (v) {
+      if (o < kSetupStage) {
+        lc = s_lc[warp][o];
+        code = s_code[warp][o];
+      } else {
+        lc = offset_of(i);
+        code = code_of(lc);
+      }
+    }
     const unsigned grp = __match_any_sync(0xffffffffu, code);
-    const int d = b + cnt[code] + __popc(grp & lt);
+    const int r = v ? cnt[code] + __popc(grp & lt) : 0;  // position within the leaf
     __syncwarp();
-    if ((grp & lt) == 0) cnt[code] += __popc(grp);
+    if (v && (grp & lt) == 0) cnt[code] += __popc(grp);
     __syncwarp();
     if (v) {
+      const int d = b + r;
+      if (r < kSetupStage) s_out[warp][r] = lc;
       m.leaf_of[d] = c;
-      const float2 lc = make_float2((float)(x[i] - cx), (float)(y[i] - cy));
       m.loc[d] = lc;
-      m.gam[d] = (float)cir[i];
+      const float g = (float)cir[i];
+      m.gam[d] = g;
       // 1/sigma^2 is only kept in FP32, so it is formed in FP32 (the FP64
-      // divide is slow on this GPU and buys nothing after the rounding)
+      // divide is slow on this GPU and buys nothing after the rounding);
+      // the correctly rounded reciprocal is 1.f / (sf * sf) exactly
       const float sf = (float)cor[i];
-      const float w = 1.f / (sf * sf);
+      const float w = __frcp_rn(sf * sf);
       m.s2inv[d] = w;
-      const float g = m.gam[d], tw = -1.44269504f * w;
-      m.src4[d] = make_float4(lc.x, lc.y, g, tw);
+      m.src4[d] = make_float4(lc.x, lc.y, g, -1.44269504f * w);
       m.mperm[d] = perm[i];
     }
   }
   __syncwarp();
   // each 32-blob chunk's bounding box, for the near field's correction cull
   for (int i0 = b; i0 < e; i0 += 32) {  // warp-uniform
-    const int i = i0 + lane;
+    const int i = i0 + lane, o = i - b;
     const bool v = i < e;
-    const float2 lc = v ? m.loc[i] : make_float2(0.f, 0.f);
+    const float2 lc = !v ? make_float2(0.f, 0.f) : (o < kSetupStage ? s_out[warp][o] : m.loc[i]);
     float bx0 = v ? lc.x : INFINITY, by0 = v ? lc.y : INFINITY, bx1 = v ? lc.x : -INFINITY, by1 = v ? lc.y : -INFINITY;
-    for (int o = 16; o; o >>= 1) {
-      bx0 = fminf(bx0, __shfl_xor_sync(0xffffffffu, bx0, o));
-      by0 = fminf(by0, __shfl_xor_sync(0xffffffffu, by0, o));
-      bx1 = fmaxf(bx1, __shfl_xor_sync(0xffffffffu, bx1, o));
-      by1 = fmaxf(by1, __shfl_xor_sync(0xffffffffu, by1, o));
+    for (int sh = 16; sh; sh >>= 1) {
+      bx0 = fminf(bx0, __shfl_xor_sync(0xffffffffu, bx0, sh));
+      by0 = fminf(by0, __shfl_xor_sync(0xffffffffu, by0, sh));
+      bx1 = fmaxf(bx1, __shfl_xor_sync(0xffffffffu, bx1, sh));
+      by1 = fmaxf(by1, __shfl_xor_sync(0xffffffffu, by1, sh));
     }
     const int k = (i0 - b) >> 5;
     if (lane == 0 && k < m.kchunks) m.cbox[(size_t)c * m.kchunks + k] = make_float4(bx0, by0, bx1, by1);
@@ -1198,85 +1232,117 @@ __device__ __forceinline__ float sfu_rcp(float x) {
   return r;
 }
 
-// One pair: source (x, y, G, t) with t = -log2(e)/sigma^2, target (tx, ty).
-// r2 carries a 1e-30 floor, so a coincident pair has a finite factor and
-// contributes f * (0, 0) = 0, as the reference skips r <= 1e-10
-// (fmm.c:132); nothing else sees the floor (it is below FP32 resolution of
-// any r2 that matters).
-//   direct (U):     f = G (1 - exp(-r^2/s^2)) / r^2, with 1 - e^-x taken
-//                   from its series x (1 - x/2) below x = 1e-3, where the
+// One pair: source (x, y, G, t) with t = -log2(e)/sigma^2, target given
+// negated, (ntx, nty) = (-tx, -ty).  The offset is taken source minus
+// target, (nrx, nry) = -(tx - x, ty - y) exactly (round to nearest is
+// symmetric), and the pair adds f nry to a and f nrx to b with f >= 0 up to
+// the sign of G:
+//   direct (U):     f = G (1 - exp(-r^2/s^2)) / r^2, velocity (a, -b);
+//                   1 - e^-x is taken from its series x (1 - x/2) =
+//                   t (-ln2 - (ln2)^2/2 t) below x = 1e-3, where the
 //                   subtraction would cancel;
-//   correction (K): f = -G exp(-r^2/s^2) / r^2 for every pair of the two
-//                   leaves (the list holds the leaves within rc; pairs beyond
-//                   rc add their tiny exact terms).
-// The quotient is G (...) times the SFU reciprocal of r2.
+//   correction (K): f = G exp(-r^2/s^2) / r^2, velocity (-a, b): the
+//                   correction -G exp(-r^2/s^2) / r^2 of every pair of the
+//                   two leaves (the list holds the leaves within rc; pairs
+//                   beyond rc add their tiny exact terms).
+// The signs are applied once per source leaf, in its compensated add, so no
+// pair spends an instruction on them.  r2 carries a 1e-30 floor, so a
+// coincident pair has a finite factor and contributes f * (0, 0) = 0, as
+// the reference skips r <= 1e-10 (fmm.c:132); nothing else sees the floor
+// (it is below FP32 resolution of any r2 that matters).  The quotient is
+// G (...) times the SFU reciprocal of r2.
+constexpr float kSer1 = -0.69314718f;  // -ln 2
+constexpr float kSer2 = -0.24022651f;  // -(ln 2)^2 / 2
+constexpr float kSerT = -1.44269504e-3f;  // t at x = 1e-3
+
 template <bool kCorrection>
-__device__ __forceinline__ void pair(const float4 sj, float tx, float ty, float &sx, float &sy) {
-  const float rx = __fsub_rn(tx, sj.x), ry = __fsub_rn(ty, sj.y);
-  const float r2 = fmaf(rx, rx, fmaf(ry, ry, 1e-30f));
+__device__ __forceinline__ void pair(const float4 sj, float ntx, float nty, float &a, float &b) {
+  const float nrx = __fadd_rn(sj.x, ntx), nry = __fadd_rn(sj.y, nty);
+  const float r2 = fmaf(nrx, nrx, fmaf(nry, nry, 1e-30f));
   const float t = __fmul_rn(r2, sj.w);
   const float e = sfu_exp2(t);
   const float ir2 = sfu_rcp(r2);
   float f;
   if (!kCorrection) {
-    const float x2 = __fmul_rn(t, -0.69314718f);
-    const float ser = __fmul_rn(x2, fmaf(-0.5f, x2, 1.f)), ome = __fsub_rn(1.f, e);
-    const float e1f = t > -1.44269504e-3f ? ser : ome;
-    f = __fmul_rn(__fmul_rn(sj.z, e1f), ir2);
+    const float ser = __fmul_rn(t, fmaf(kSer2, t, kSer1)), ome = fmaf(-1.f, e, 1.f);
+    f = __fmul_rn(__fmul_rn(sj.z, t > kSerT ? ser : ome), ir2);
   } else {
-    f = -__fmul_rn(__fmul_rn(sj.z, e), ir2);
+    f = __fmul_rn(__fmul_rn(sj.z, e), ir2);
   }
-  sx = fmaf(-f, ry, sx);
-  sy = fmaf(f, rx, sy);
+  a = fmaf(f, nry, a);
+  b = fmaf(f, nrx, b);
 }
 
 // The same pair for two targets at once, on packed FP32x2 arithmetic: one
 // instruction forms both targets' value of every step, with the rounding
 // of the scalar step (each component rounds as the scalar operation does),
-// so a target's sum does not depend on whether its lane holds one target
-// or two.
-
+// so a target's sum does not depend on how many targets its lane holds.
 template <bool kCorrection>
-__device__ __forceinline__ void pair2(const float4 sj, float2 tx, float2 ty, float2 &sx, float2 &sy) {
-  const float2 rx = __fadd2_rn(tx, f2(-sj.x)), ry = __fadd2_rn(ty, f2(-sj.y));
-  const float2 r2 = __ffma2_rn(rx, rx, __ffma2_rn(ry, ry, f2(1e-30f)));
+__device__ __forceinline__ void pair2(const float4 sj, float2 ntx, float2 nty, float2 &a, float2 &b) {
+  const float2 nrx = __fadd2_rn(f2(sj.x), ntx), nry = __fadd2_rn(f2(sj.y), nty);
+  const float2 r2 = __ffma2_rn(nrx, nrx, __ffma2_rn(nry, nry, f2(1e-30f)));
   const float2 t = __fmul2_rn(r2, f2(sj.w));
   const float2 e = make_float2(sfu_exp2(t.x), sfu_exp2(t.y));
   const float2 ir2 = make_float2(sfu_rcp(r2.x), sfu_rcp(r2.y));
   float2 f;
   if (!kCorrection) {
-    const float2 x2 = __fmul2_rn(t, f2(-0.69314718f));
-    const float2 ser = __fmul2_rn(x2, __ffma2_rn(f2(-0.5f), x2, f2(1.f)));
-    const float2 ome = __fadd2_rn(f2(1.f), make_float2(-e.x, -e.y));
-    const float2 e1f = make_float2(t.x > -1.44269504e-3f ? ser.x : ome.x, t.y > -1.44269504e-3f ? ser.y : ome.y);
+    const float2 ser = __fmul2_rn(t, __ffma2_rn(f2(kSer2), t, f2(kSer1)));
+    const float2 ome = __ffma2_rn(f2(-1.f), e, f2(1.f));
+    const float2 e1f = make_float2(t.x > kSerT ? ser.x : ome.x, t.y > kSerT ? ser.y : ome.y);
     f = __fmul2_rn(__fmul2_rn(f2(sj.z), e1f), ir2);
   } else {
-    f = __fmul2_rn(__fmul2_rn(f2(-sj.z), e), ir2);
+    f = __fmul2_rn(__fmul2_rn(f2(sj.z), e), ir2);
   }
-  sx = __ffma2_rn(make_float2(-f.x, -f.y), ry, sx);
-  sy = __ffma2_rn(f, rx, sy);
+  a = __ffma2_rn(f, nry, a);
+  b = __ffma2_rn(f, nrx, b);
 }
 
-// Direct (U list) or correction (K list) contributions of one source leaf
-// to the lane's two targets.  Each leaf is summed in plain FP32 and then
-// added with compensation, so the compensated sum costs once per leaf, not
-// once per pair.
-template <bool kCorrection>
-__device__ __forceinline__ void leaf_pairs(const float4 *__restrict__ src, int j0, int j1, float txa, float tya,
-                                           float txb, float tyb, bool two, float &sxa, float &sya, float &sxb,
-                                           float &syb) {
-  if (two) {
-    const float2 tx = make_float2(txa, txb), ty = make_float2(tya, tyb);
-    float2 sx = make_float2(sxa, sxb), sy = make_float2(sya, syb);
-#pragma unroll 2
-    for (int j = j0; j < j1; j++) pair2<kCorrection>(src[j], tx, ty, sx, sy);
-    sxa = sx.x;
-    sxb = sx.y;
-    sya = sy.x;
-    syb = sy.y;
-  } else {
+// Source records {x, y, G, t} of one leaf, read from a stage buffer in
+// shared memory (ld.shared, from its shared-window address) or from global
+// memory (read-only while the kernel runs).  Two types, so that the pair
+// loop issues shared or global loads, never generic ones.
+struct SmemSrc {
+  uint32_t base;
+  __device__ __forceinline__ float4 operator[](int j) const {
+    float4 v;
+    asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];"
+                 : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+                 : "r"(base + 16u * (uint32_t)j));
+    return v;
+  }
+};
+struct GlobalSrc {
+  const float4 *__restrict__ p;
+  __device__ __forceinline__ float4 operator[](int j) const { return __ldg(p + j); }
+};
+
+// Direct (U list) or correction (K list) sums of source blobs [j0, j1) for
+// one target per lane (leaf_pairs1), one pack of two (leaf_pairs2) or two
+// packs sharing every source record (leaf_pairs4); the targets are given
+// negated (see pair).  Each source leaf is summed in plain FP32 and then
+// added with compensation (leaf_add), so the compensated sum costs once per
+// leaf, not once per pair.
+template <bool kCorrection, class S>
+__device__ __forceinline__ void leaf_pairs1(const S src, int j0, int j1, float ntx, float nty, float &a, float &b) {
 #pragma unroll 4
-    for (int j = j0; j < j1; j++) pair<kCorrection>(src[j], txa, tya, sxa, sya);
+  for (int j = j0; j < j1; j++) pair<kCorrection>(src[j], ntx, nty, a, b);
+}
+
+template <bool kCorrection, class S>
+__device__ __forceinline__ void leaf_pairs2(const S src, int j0, int j1, float2 ntx, float2 nty, float2 &a,
+                                            float2 &b) {
+#pragma unroll 2
+  for (int j = j0; j < j1; j++) pair2<kCorrection>(src[j], ntx, nty, a, b);
+}
+
+template <bool kCorrection, class S>
+__device__ __forceinline__ void leaf_pairs4(const S src, int j0, int j1, float2 ntx0, float2 nty0, float2 ntx1,
+                                            float2 nty1, float2 &a0, float2 &b0, float2 &a1, float2 &b1) {
+#pragma unroll 2
+  for (int j = j0; j < j1; j++) {
+    const float4 sj = src[j];
+    pair2<kCorrection>(sj, ntx0, nty0, a0, b0);
+    pair2<kCorrection>(sj, ntx1, nty1, a1, b1);
   }
 }
 
@@ -1308,36 +1374,12 @@ __device__ __forceinline__ float leaf_cutoff(const MixedView &m, int B) {
   return rc;
 }
 
-// Bounding box {xmin, ymin, xmax, ymax} of the warp's targets (offsets za,
-// zb of the valid ones from the target leaf's centre) and the squared
-// correction radius, written to the warp's 5 floats of shared memory `tb`
-// (kept out of registers: the pair loop needs them all).
-__device__ __forceinline__ void target_box(float2 za, bool va, float2 zb, bool vb, float rc, float *tb, int lane) {
-  float x0 = INFINITY, y0 = INFINITY, x1 = -INFINITY, y1 = -INFINITY;
-  if (va) x0 = fminf(x0, za.x), y0 = fminf(y0, za.y), x1 = fmaxf(x1, za.x), y1 = fmaxf(y1, za.y);
-  if (vb) x0 = fminf(x0, zb.x), y0 = fminf(y0, zb.y), x1 = fmaxf(x1, zb.x), y1 = fmaxf(y1, zb.y);
-  for (int o = 16; o; o >>= 1) {
-    x0 = fminf(x0, __shfl_xor_sync(0xffffffffu, x0, o));
-    y0 = fminf(y0, __shfl_xor_sync(0xffffffffu, y0, o));
-    x1 = fmaxf(x1, __shfl_xor_sync(0xffffffffu, x1, o));
-    y1 = fmaxf(y1, __shfl_xor_sync(0xffffffffu, y1, o));
-  }
-  if (lane == 0) {
-    tb[0] = x0;
-    tb[1] = y0;
-    tb[2] = x1;
-    tb[3] = y1;
-    tb[4] = __fmul_rn(rc, rc);
-  }
-  __syncwarp();
-}
-
 constexpr unsigned kAllChunks = 0xffffffffu;
 
 // Pair counters of one warp, kept in shared memory by lane 0 (every count
-// but the targets' is warp-uniform): evaluated pairs, correction pairs
-// evaluated, correction pairs listed, per target slot of the current chunk
-// of targets, then summed over chunks times the chunk's targets.
+// is warp-uniform): target-source pairs evaluated, correction pairs
+// evaluated and correction pairs listed, over the current chunk of targets
+// and then summed over chunks.
 struct WarpCounts {
   unsigned chunk[3];
   unsigned long long total[3];
@@ -1351,17 +1393,6 @@ __device__ __forceinline__ void counts_add(WarpCounts *c, int lane, unsigned don
   }
 }
 
-// Closes a chunk of targets; all lanes call it.
-__device__ __forceinline__ void counts_close(WarpCounts *c, int lane, bool va, bool vb) {
-  const unsigned nt = __popc(__ballot_sync(0xffffffffu, va)) + __popc(__ballot_sync(0xffffffffu, vb));
-  if (lane == 0)
-    for (int k = 0; k < 3; k++) {
-      c->total[k] += (unsigned long long)c->chunk[k] * nt;
-      c->chunk[k] = 0;
-    }
-  __syncwarp();
-}
-
 __device__ __forceinline__ void counts_flush(WarpCounts *c, int lane, DevStatus *st) {
   if (lane == 0) {
     atomicAdd(&st->n_pairs, c->total[0]);
@@ -1370,322 +1401,370 @@ __device__ __forceinline__ void counts_flush(WarpCounts *c, int lane, DevStatus 
   }
 }
 
-// The next run of consecutive kept chunks of mask r: blobs [s0, s1) of a
-// leaf of cnt blobs; the run is removed from r.  kAllChunks is the whole
-// leaf.
-__device__ __forceinline__ void next_run(unsigned &r, int cnt, int &s0, int &s1) {
-  if (r == kAllChunks) {
+// The next run of consecutive source chunks (32 blobs each, bit k of a mask
+// for chunk k of a leaf of cnt blobs) kept for the same target packs: r0
+// and r1 are the chunks kept for pack 0 and pack 1, kAllChunks for both the
+// whole leaf.  Returns blobs [s0, s1) and the packs (bit 0: pack 0, bit 1:
+// pack 1); the run is removed from both masks.
+__device__ __forceinline__ int next_run(unsigned &r0, unsigned &r1, int cnt, int &s0, int &s1) {
+  if (r0 == kAllChunks && r1 == kAllChunks) {
     s0 = 0;
     s1 = cnt;
-    r = 0;
-    return;
+    r0 = r1 = 0;
+    return 3;
   }
-  const int a = __ffs(r) - 1;
-  const unsigned gap = ~(r >> a);
+  const int a = __ffs(r0 | r1) - 1;
+  const int packs = (int)((r0 >> a) & 1u) | (int)(((r1 >> a) & 1u) << 1);
+  const unsigned same = ((packs & 1) ? r0 : ~r0) & ((packs & 2) ? r1 : ~r1);
+  const unsigned gap = ~(same >> a);
   const int len = gap ? __ffs(gap) - 1 : 32 - a;
   s0 = a << 5;
   s1 = min(cnt, (a + len) << 5);
-  r = a + len >= 32 ? 0u : r & ~(((1u << len) - 1u) << a);
+  const unsigned run = a + len >= 32 ? ~0u << a : ((1u << len) - 1u) << a;
+  r0 &= ~run;
+  r1 &= ~run;
+  return packs;
 }
 
-// Chunks of correction source leaf A whose pairs with the warp's targets
-// can lie within the correction radius: bit k for the 32-blob chunk k of A
-// whose bounding box comes within rc of the targets' box (offset by
-// (ox, oy), A's centre seen from the target leaf).  Pairs farther than rc
-// from every target add terms below exp(-rc^2/sigma^2) of a point vortex:
-// the ones the correction list already leaves out beyond rc.  A leaf of
-// more than 32 chunks is not culled (kAllChunks).  Warp-uniform.
-__device__ __forceinline__ unsigned chunk_mask(const MixedView &m, int A, float ox, float oy, const float *tb,
-                                               int lane) {
+// Chunks of correction source leaf A whose pairs with a pack of targets can
+// lie within the correction radius: bit k of *m0 (*m1) for the 32-blob chunk
+// k of A whose bounding box comes within rc of pack 0's (pack 1's) target
+// box, tb[0..3] (tb[4..7]), rc^2 in tb[8]; the boxes are offsets from the
+// target leaf's centre, (ox, oy) is A's centre seen from there.  Pairs
+// farther than rc from every target add terms below exp(-rc^2/sigma^2) of a
+// point vortex: the ones the correction list already leaves out beyond rc.
+// A leaf of more than 32 chunks is not culled (kAllChunks).  Warp-uniform.
+template <int kPacks>
+__device__ __forceinline__ void chunk_mask(const MixedView &m, int A, float ox, float oy, const float *tb, int lane,
+                                           unsigned &m0, unsigned &m1) {
   const int nch = (m.end[A] - m.begin[A] + 31) >> 5;
-  if (nch > 32 || nch > m.kchunks) return kAllChunks;
-  bool keep = false;
-  if (lane < nch) {
-    const float4 T = make_float4(tb[0], tb[1], tb[2], tb[3]);
-    const float rc2 = tb[4];
-    const float4 s = m.cbox[(size_t)A * m.kchunks + lane];
-    // the targets' box in A's frame: T + (ox, oy)
-    const float gx = fmaxf(fmaxf(__fsub_rn(s.x, __fadd_rn(T.z, ox)), __fsub_rn(__fadd_rn(T.x, ox), s.z)), 0.f);
-    const float gy = fmaxf(fmaxf(__fsub_rn(s.y, __fadd_rn(T.w, oy)), __fsub_rn(__fadd_rn(T.y, oy), s.w)), 0.f);
-    keep = fmaf(gx, gx, __fmul_rn(gy, gy)) <= rc2;
+  if (nch > 32 || nch > m.kchunks) {
+    m0 = m1 = kAllChunks;
+    return;
   }
-  return __ballot_sync(0xffffffffu, keep);
+  bool keep[2] = {false, false};
+  if (lane < nch) {
+    const float rc2 = tb[8];
+    const float4 s = m.cbox[(size_t)A * m.kchunks + lane];
+#pragma unroll
+    for (int p = 0; p < kPacks; p++) {
+      // pack p's box in A's frame: T + (ox, oy)
+      const float4 T = make_float4(tb[4 * p], tb[4 * p + 1], tb[4 * p + 2], tb[4 * p + 3]);
+      const float gx = fmaxf(fmaxf(__fsub_rn(s.x, __fadd_rn(T.z, ox)), __fsub_rn(__fadd_rn(T.x, ox), s.z)), 0.f);
+      const float gy = fmaxf(fmaxf(__fsub_rn(s.y, __fadd_rn(T.w, oy)), __fsub_rn(__fadd_rn(T.y, oy), s.w)), 0.f);
+      keep[p] = fmaf(gx, gx, __fmul_rn(gy, gy)) <= rc2;
+    }
+  }
+  m0 = __ballot_sync(0xffffffffu, keep[0]);
+  m1 = kPacks == 2 ? __ballot_sync(0xffffffffu, keep[1]) : m0;
 }
 
-// Near field of every leaf: one warp per target leaf, two targets per lane.
-// The warp walks its direct entries (U list, then K list; in the learned
-// form the entries the network accepted are M2P'd first and skipped here)
-// and stages each source leaf's blobs in shared memory with a bulk copy
-// (cp.async.bulk, one 16-byte record per blob, completion on a per-buffer
-// mbarrier), double-buffered: the next leaf is in flight while the lanes
-// sum the current one.  Leaves larger than a stage buffer, and every leaf
-// after a wait that gave up (recorded as TREE2D_ERR_TIMEOUT), are read from
-// global memory instead, so the result never depends on the staging.
+// Near field of every leaf: one warp per target leaf.  The leaf's targets
+// are taken in chunks of 128, 64 or 32 (4, 2 or 1 per lane, packed in
+// twos: a leaf of 97-128 blobs walks its source lists once with four
+// targets per lane instead of twice with two).  For each chunk the warp
+// walks its direct entries (U list, then K list; in the learned form the
+// entries the network accepted are M2P'd after the walk and skipped in it)
+// and sums each source leaf's blobs for every target.  kStaged: each source
+// leaf is staged in shared memory by a bulk copy (cp.async.bulk, one
+// 16-byte record per blob, completion on a per-buffer mbarrier),
+// double-buffered, so the next leaf is in flight while the lanes sum the
+// current one; leaves larger than a stage buffer, and every leaf after a
+// wait that gave up (recorded as TREE2D_ERR_TIMEOUT), are read from global
+// memory instead, so the result never depends on the staging.  Otherwise
+// the sources are read from global memory (through L1).  The compensated
+// per-target sums live in shared memory (written once per source leaf),
+// which keeps the pair loop's registers for the targets.
 constexpr int kStage = 128;  // blobs per stage buffer: the largest leaf of the default leaf sizes
 constexpr long kEvalWaitLimit = 1l << 22;  // polls; a healthy copy lands within microseconds
 
-template <bool kLearned, int kWarps>
-__global__ void __launch_bounds__(32 * kWarps, 32 / kWarps) k_eval_staged(MixedView m, double *uv, const int *perm,
-                                                                           Decisions dec, long wait_limit) {
-  __shared__ __align__(128) float4 s_src[kWarps][2][kStage];
-  __shared__ __align__(8) uint64_t s_bar[kWarps][2];
-  __shared__ float s_tb[kWarps][5];  // target box and rc^2 of the warp's chunk
-  __shared__ WarpCounts s_cnt[kWarps];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  int l = next_leaf(m.st, lane);
-  if (l >= m.nleaf) return;  // uniform over the warp; nothing below syncs the block
-  uint64_t *bar = s_bar[warp];
+struct NearWarp {
+  float4 *src;       // stage buffers [2][kStage] (kStaged)
+  uint64_t *bar;     // their mbarriers [2]
+  float *tbox;       // target boxes of the chunk's packs and rc^2
+  float4 *acc;       // compensated sums {ax, cx, ay, cy} [4][32]
+  WarpCounts *cnts;
+  unsigned parity;   // bit b: parity of buffer b's next completion
+  unsigned inflight; // bit b: a copy into buffer b not yet waited for
+  bool staging;      // false after a wait gave up
+};
+
+// Adds one source leaf's sums (sa, sb of pair) to target slot k's
+// compensated sums: velocity (a, -b) for a direct leaf, (-a, b) for a
+// correction leaf.
+__device__ __forceinline__ void leaf_add(float4 *acc, int k, int lane, bool corr, float a, float b) {
+  float4 s = acc[32 * k + lane];
+  kahan(s.x, s.y, corr ? -a : a);
+  kahan(s.z, s.w, corr ? b : -b);
+  acc[32 * k + lane] = s;
+}
+
+// One chunk of a target leaf's targets: 32 kT of them from t0 on, kT per
+// lane (target t0 + 32 k + lane in slot k), in packs of two slots (k = 0, 1
+// and k = 2, 3), each pack with its own bounding box for the correction
+// cull.  The tree's in-leaf order is spatial (k_leaf_setup), so a pack of
+// 64 consecutive targets is compact.
+template <bool kLearned, bool kStaged, int kT>
+__device__ __forceinline__ void near_chunk(const MixedView &m, const Decisions &dec, double *uv, const int *perm,
+                                           long wait_limit, int l, int B, int t0, int lane, NearWarp &w) {
+  constexpr int kPacks = kT == 4 ? 2 : 1;
+  const int tend = m.end[B];
+  float bx[kPacks][4];
+#pragma unroll
+  for (int p = 0; p < kPacks; p++) bx[p][0] = bx[p][1] = INFINITY, bx[p][2] = bx[p][3] = -INFINITY;
+#pragma unroll
+  for (int k = 0; k < kT; k++) {
+    const int t = t0 + 32 * k + lane, p = k >> 1;
+    const float2 zk = t < tend ? m.loc[t] : make_float2(0.f, 0.f);
+    if (t < tend)
+      bx[p][0] = fminf(bx[p][0], zk.x), bx[p][1] = fminf(bx[p][1], zk.y), bx[p][2] = fmaxf(bx[p][2], zk.x),
+      bx[p][3] = fmaxf(bx[p][3], zk.y);
+    w.acc[32 * k + lane] = make_float4(0.f, 0.f, 0.f, 0.f);
+  }
+  // each pack's target box (offsets from B's centre) and rc^2, in shared memory
+#pragma unroll
+  for (int p = 0; p < kPacks; p++)
+    for (int o = 16; o; o >>= 1) {
+      bx[p][0] = fminf(bx[p][0], __shfl_xor_sync(0xffffffffu, bx[p][0], o));
+      bx[p][1] = fminf(bx[p][1], __shfl_xor_sync(0xffffffffu, bx[p][1], o));
+      bx[p][2] = fmaxf(bx[p][2], __shfl_xor_sync(0xffffffffu, bx[p][2], o));
+      bx[p][3] = fmaxf(bx[p][3], __shfl_xor_sync(0xffffffffu, bx[p][3], o));
+    }
   if (lane == 0) {
-    mbar_init(&bar[0], 1);
-    mbar_init(&bar[1], 1);
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    const float rc = leaf_cutoff(m, B);
+#pragma unroll
+    for (int p = 0; p < kPacks; p++)
+      for (int i = 0; i < 4; i++) w.tbox[4 * p + i] = bx[p][i];
+    w.tbox[8] = __fmul_rn(rc, rc);
   }
   __syncwarp();
-  unsigned parity = 0;    // bit b: parity of buffer b's next completion
-  unsigned inflight = 0;  // bit b: a copy into buffer b not yet waited for
-  bool staging = true;    // false after a wait gave up
-  const double inv2pi = 0.15915494309189533577;
-  float *tbox = s_tb[warp];
-  WarpCounts *cnts = &s_cnt[warp];
-  if (lane == 0) *cnts = WarpCounts{};
-  for (; l < m.nleaf; l = next_leaf(m.st, lane)) {
-  const int B = m.leaf_cell[l];
+  // target offsets from B's centre (read again where needed: L1-resident, and
+  // registers and shared memory are kept for the pair loop and occupancy)
+  auto zof = [&](int k) {
+    const int t = t0 + 32 * k + lane;
+    return t < tend ? m.loc[t] : make_float2(0.f, 0.f);
+  };
+  // valid targets of each pack (the pair counts are per target)
+  const unsigned nt = (unsigned)min(tend - t0, 32 * kT);
+  const unsigned vp0 = kT == 4 ? min(nt, 64u) : nt, vp1 = kT == 4 ? nt - vp0 : 0u;
   const int u0 = m.u_off[l], nu = m.u_off[l + 1] - u0;
   const int k0 = m.k_off[l], nk = m.k_off[l + 1] - k0;
-  // position q of the walk: U entries, then K entries
   auto src_leaf = [&](int q) { return q < nu ? m.u_idx[u0 + q] : m.k_idx[k0 + q - nu]; };
   auto direct = [&](int q) {
     if (!kLearned) return true;
     return (q < nu ? dec.u[u0 + q] : dec.k[k0 + q - nu]) == 0;
   };
+  // the next entry with work for these targets: a direct entry, and for a
+  // correction entry at least one chunk within rc of a pack (r0, r1: its
+  // chunks per pack, all for a U entry); culled correction entries are
+  // counted and skipped
+  auto next_work = [&](int q, unsigned &r0, unsigned &r1) {
+    for (; q < nu + nk; q++) {
+      if (!direct(q)) continue;
+      if (q < nu) {
+        r0 = r1 = kAllChunks;
+        return q;
+      }
+      const int A = m.k_idx[k0 + q - nu];
+      chunk_mask<kPacks>(m, A, centre_offset(m.cxf, m.cxl, B, A), centre_offset(m.cyf, m.cyl, B, A), w.tbox, lane,
+                         r0, r1);
+      if (r0 | r1) return q;
+      counts_add(w.cnts, lane, 0u, 0u, (unsigned)(m.end[A] - m.begin[A]) * nt);
+    }
+    r0 = r1 = 0;
+    return q;
+  };
   // copy source leaf of position q into buffer b (warp-uniform decision)
   auto stage = [&](int q, int b) {
+    if (!kStaged) return false;
     const int A = src_leaf(q);
     const int j0 = m.begin[A], cnt = m.end[A] - j0;
-    if (!staging || cnt > kStage) return false;
+    if (!w.staging || cnt > kStage) return false;
     if (lane == 0) {
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-      mbar_expect_tx(&bar[b], (uint32_t)cnt * 16u);
-      bulk_g2s(s_src[warp][b], m.src4 + j0, (uint32_t)cnt * 16u, &bar[b]);
+      mbar_expect_tx(&w.bar[b], (uint32_t)cnt * 16u);
+      bulk_g2s(w.src + b * kStage, m.src4 + j0, (uint32_t)cnt * 16u, &w.bar[b]);
     }
-    inflight |= 1u << b;
+    w.inflight |= 1u << b;
     return true;
   };
-  for (int t0 = m.begin[B]; t0 < m.end[B]; t0 += 64) {
-    const int ta = t0 + lane, tb = t0 + 32 + lane;
-    const bool va = ta < m.end[B], vb = tb < m.end[B];
-    const bool two = __any_sync(0xffffffffu, vb);
-    const float2 za = va ? m.loc[ta] : make_float2(0.f, 0.f);
-    const float2 zb = vb ? m.loc[tb] : make_float2(0.f, 0.f);
-    target_box(za, va, zb, vb, leaf_cutoff(m, B), tbox, lane);
-    // the next entry with work for these targets: a direct entry, and for a
-    // correction entry at least one chunk within rc (msk: its chunks, all
-    // for a U entry); culled correction entries are counted and skipped
-    auto next_work = [&](int q, unsigned &msk) {
-      for (; q < nu + nk; q++) {
-        if (!direct(q)) continue;
-        if (q < nu) {
-          msk = kAllChunks;
-          return q;
-        }
-        const int A = m.k_idx[k0 + q - nu];
-        msk = chunk_mask(m, A, centre_offset(m.cxf, m.cxl, B, A), centre_offset(m.cyf, m.cyl, B, A), tbox, lane);
-        if (msk) return q;
-        counts_add(cnts, lane, 0u, 0u, (unsigned)(m.end[A] - m.begin[A]));
-      }
-      msk = 0;
-      return q;
-    };
-    float2 pa = make_float2(0.f, 0.f), pb = make_float2(0.f, 0.f);
-    unsigned msk = 0;
-    int q = next_work(0, msk);
-    int buf = 0;
-    bool staged = q < nu + nk && stage(q, buf);
-    if (two)
-      far_field2(m, l, B, za, zb, pa, pb);
-    else
-      far_field(m, l, B, za, pa);
-    if (kLearned) {
-      // accepted U entries: the source leaf's multipole at the chosen order
-      // (accepted K entries: the correction is left out)
-      for (int e = u0; e < u0 + nu; e++) {
-        const int d = dec.u[e];
-        if (d > 0) {
-          const int A = m.u_idx[e];
-          const int p = min(min(class_order(d) + dec.margin, 16), m.P);
-          if (two)
-            m2p_order2(m, B, A, p, za, zb, pa, pb);
-          else
-            m2p_order(m, B, A, p, za, pa);
-        }
+  unsigned r0 = 0, r1 = 0;
+  int q = next_work(0, r0, r1);
+  int buf = 0;
+  bool staged = q < nu + nk && stage(q, buf);
+  while (q < nu + nk) {
+    unsigned r0n = 0, r1n = 0;
+    const int qn = next_work(q + 1, r0n, r1n);
+    const bool staged_next = qn < nu + nk && stage(qn, buf ^ 1);
+    const int A = src_leaf(q);
+    // offset of the source leaf's centre from the two-float centres: FP32
+    // centres alone would carry ~3e-8 absolute error into every close pair
+    const float ox = centre_offset(m.cxf, m.cxl, B, A), oy = centre_offset(m.cyf, m.cyl, B, A);
+    const int j0 = m.begin[A], cnt = m.end[A] - j0;
+    bool use_smem = false;
+    if (staged) {
+      if (mbar_wait(&w.bar[buf], (w.parity >> buf) & 1u, wait_limit)) {
+        w.parity ^= 1u << buf;
+        w.inflight &= ~(1u << buf);
+        use_smem = true;
+      } else {
+        w.staging = false;  // the copy stays in flight; read global memory from now on
+        if (lane == 0) set_err(m.st, TREE2D_ERR_TIMEOUT);
       }
     }
-    float axa = 0.f, aya = 0.f, cxa = 0.f, cya = 0.f;
-    float axb = 0.f, ayb = 0.f, cxb = 0.f, cyb = 0.f;
-    while (q < nu + nk) {
-      unsigned msk_next = 0;
-      const int qn = next_work(q + 1, msk_next);
-      const bool staged_next = qn < nu + nk && stage(qn, buf ^ 1);
-      const int A = src_leaf(q);
-      // offset of the source leaf's centre from the two-float centres: FP32
-      // centres alone would carry ~3e-8 absolute error into every close pair
-      const float ox = centre_offset(m.cxf, m.cxl, B, A), oy = centre_offset(m.cyf, m.cyl, B, A);
-      const int j0 = m.begin[A], cnt = m.end[A] - j0;
-      bool use_smem = false;
-      if (staged) {
-        if (mbar_wait(&bar[buf], (parity >> buf) & 1u, wait_limit)) {
-          parity ^= 1u << buf;
-          inflight &= ~(1u << buf);
-          use_smem = true;
-        } else {
-          staging = false;  // the copy stays in flight; read global memory from now on
-          if (lane == 0) set_err(m.st, TREE2D_ERR_TIMEOUT);
-        }
-      }
-      float sxa = 0.f, sya = 0.f, sxb = 0.f, syb = 0.f;
-      const float txa = __fadd_rn(za.x, ox), tya = __fadd_rn(za.y, oy), txb = __fadd_rn(zb.x, ox), tyb = __fadd_rn(zb.y, oy);
-      const float4 *src = use_smem ? s_src[warp][buf] : m.src4 + j0;
-      int done = 0;
-      for (unsigned r = msk; r;) {
-        int s0, s1;
-        next_run(r, cnt, s0, s1);
-        if (q < nu)
-          leaf_pairs<false>(src, s0, s1, txa, tya, txb, tyb, two, sxa, sya, sxb, syb);
+    const bool corr = q >= nu;
+    // the targets' offsets from A's centre, negated (see pair)
+    float ntx[kT], nty[kT], sa[kT], sb[kT];
+#pragma unroll
+    for (int k = 0; k < kT; k++) {
+      const float2 zk = zof(k);
+      ntx[k] = -__fadd_rn(zk.x, ox);
+      nty[k] = -__fadd_rn(zk.y, oy);
+      sa[k] = 0.f;
+      sb[k] = 0.f;
+    }
+    unsigned done = 0;  // pairs evaluated for the chunk's valid targets
+    auto runs = [&](const auto src) {
+    while (r0 | r1) {
+      int s0, s1;
+      const int packs = next_run(r0, r1, cnt, s0, s1);
+      done += (unsigned)(s1 - s0) * ((packs & 1 ? vp0 : 0u) + (packs & 2 ? vp1 : 0u));
+      if (kT == 1) {
+        if (!corr)
+          leaf_pairs1<false>(src, s0, s1, ntx[0], nty[0], sa[0], sb[0]);
         else
-          leaf_pairs<true>(src, s0, s1, txa, tya, txb, tyb, two, sxa, sya, sxb, syb);
-        done += s1 - s0;
+          leaf_pairs1<true>(src, s0, s1, ntx[0], nty[0], sa[0], sb[0]);
+      } else if (kT == 2 || packs != 3) {
+        // one pack: slots 0, 1, or in a four-slot chunk 2, 3 when the run is
+        // pack 1's alone (constant indices keep the slots in registers)
+        auto one_pack = [&](auto k_) {
+          constexpr int k = decltype(k_)::value;
+          const float2 tx = make_float2(ntx[k], ntx[k + 1]), ty = make_float2(nty[k], nty[k + 1]);
+          float2 a = make_float2(sa[k], sa[k + 1]), b = make_float2(sb[k], sb[k + 1]);
+          if (!corr)
+            leaf_pairs2<false>(src, s0, s1, tx, ty, a, b);
+          else
+            leaf_pairs2<true>(src, s0, s1, tx, ty, a, b);
+          sa[k] = a.x, sa[k + 1] = a.y, sb[k] = b.x, sb[k + 1] = b.y;
+        };
+        if (kT == 4 && packs == 2)
+          one_pack(std::integral_constant<int, kT - 2>{});
+        else
+          one_pack(std::integral_constant<int, 0>{});
+      } else {
+        const float2 tx0 = make_float2(ntx[0], ntx[1]), ty0 = make_float2(nty[0], nty[1]);
+        const float2 tx1 = make_float2(ntx[kT - 2], ntx[kT - 1]), ty1 = make_float2(nty[kT - 2], nty[kT - 1]);
+        float2 a0 = make_float2(sa[0], sa[1]), b0 = make_float2(sb[0], sb[1]);
+        float2 a1 = make_float2(sa[kT - 2], sa[kT - 1]), b1 = make_float2(sb[kT - 2], sb[kT - 1]);
+        if (!corr)
+          leaf_pairs4<false>(src, s0, s1, tx0, ty0, tx1, ty1, a0, b0, a1, b1);
+        else
+          leaf_pairs4<true>(src, s0, s1, tx0, ty0, tx1, ty1, a0, b0, a1, b1);
+        sa[0] = a0.x, sa[1] = a0.y, sb[0] = b0.x, sb[1] = b0.y;
+        sa[kT - 2] = a1.x, sa[kT - 1] = a1.y, sb[kT - 2] = b1.x, sb[kT - 1] = b1.y;
       }
-      kahan(axa, cxa, sxa);
-      kahan(aya, cya, sya);
-      kahan(axb, cxb, sxb);
-      kahan(ayb, cyb, syb);
-      counts_add(cnts, lane, (unsigned)done, q >= nu ? (unsigned)done : 0u, q >= nu ? (unsigned)cnt : 0u);
-      __syncwarp();  // every lane is done with this buffer before it is refilled
-      q = qn;
-      msk = msk_next;
-      buf ^= 1;
-      staged = staged_next;
     }
-    counts_close(cnts, lane, va, vb);
-    // FP64 final reduction: u = Im(phi)/2pi + ax/2pi, v = Re(phi)/2pi + ay/2pi
-    if (va) {
-      const int o = perm[ta];
-      uv[2 * (size_t)o] = ((double)pa.y + (double)axa - (double)cxa) * inv2pi;
-      uv[2 * (size_t)o + 1] = ((double)pa.x + (double)aya - (double)cya) * inv2pi;
-    }
-    if (vb) {
-      const int o = perm[tb];
-      uv[2 * (size_t)o] = ((double)pb.y + (double)axb - (double)cxb) * inv2pi;
-      uv[2 * (size_t)o + 1] = ((double)pb.x + (double)ayb - (double)cyb) * inv2pi;
+    };
+    if (use_smem)
+      runs(SmemSrc{smem_u32(w.src + buf * kStage)});
+    else
+      runs(GlobalSrc{m.src4 + j0});
+#pragma unroll
+    for (int k = 0; k < kT; k++) leaf_add(w.acc, k, lane, corr, sa[k], sb[k]);
+    counts_add(w.cnts, lane, done, corr ? done : 0u, corr ? (unsigned)cnt * nt : 0u);
+    __syncwarp();  // every lane is done with this buffer before it is refilled
+    q = qn;
+    r0 = r0n;
+    r1 = r1n;
+    buf ^= 1;
+    staged = staged_next;
+  }
+  // far field: L2P of B's local expansion and the W list's M2P, then in the
+  // learned form the accepted U entries' multipoles at the chosen order
+  float2 phi[kT], z[kT];
+#pragma unroll
+  for (int k = 0; k < kT; k++) z[k] = zof(k);
+  if (kT == 1) {
+    far_field(m, l, B, z[0], phi[0]);
+  } else {
+#pragma unroll
+    for (int k = 0; k < kT; k += 2) far_field2(m, l, B, z[k], z[(k + 1) % kT], phi[k], phi[(k + 1) % kT]);
+  }
+  if (kLearned) {
+    for (int e = u0; e < u0 + nu; e++) {
+      const int d = dec.u[e];
+      if (d > 0) {
+        const int A = m.u_idx[e];
+        const int p = min(min(class_order(d) + dec.margin, 16), m.P);
+        if (kT == 1) {
+          m2p_order(m, B, A, p, z[0], phi[0]);
+        } else {
+#pragma unroll
+          for (int k = 0; k < kT; k += 2) m2p_order2(m, B, A, p, z[k], z[(k + 1) % kT], phi[k], phi[(k + 1) % kT]);
+        }
+      }
     }
   }
-  }  // next leaf
-  // copies still in flight after a wait gave up: wait (bounded) before the
-  // shared memory is released
-  for (int b = 0; b < 2; b++)
-    if (inflight & (1u << b)) mbar_wait(&bar[b], (parity >> b) & 1u, wait_limit);
-  counts_flush(cnts, lane, m.st);
+  if (lane == 0)
+    for (int c = 0; c < 3; c++) {
+      w.cnts->total[c] += w.cnts->chunk[c];
+      w.cnts->chunk[c] = 0;
+    }
+  // FP64 final reduction: u = Im(phi)/2pi + ax/2pi, v = Re(phi)/2pi + ay/2pi
+  const double inv2pi = 0.15915494309189533577;
+#pragma unroll
+  for (int k = 0; k < kT; k++)
+    if (t0 + 32 * k + lane < tend) {
+      const float4 sacc = w.acc[32 * k + lane];
+      const int o = perm[t0 + 32 * k + lane];
+      uv[2 * (size_t)o] = ((double)phi[k].y + (double)sacc.x - (double)sacc.y) * inv2pi;
+      uv[2 * (size_t)o + 1] = ((double)phi[k].x + (double)sacc.z - (double)sacc.w) * inv2pi;
+    }
+  __syncwarp();
 }
 
-// The same near field with the source blobs read straight from global
-// memory (through L1), the other variant the tuner times.
-template <bool kLearned, int kWarps>
-__global__ void __launch_bounds__(32 * kWarps, 32 / kWarps) k_eval_mixed(MixedView m, double *uv, const int *perm,
-                                                                          Decisions dec, long) {
-  __shared__ float s_tb[kWarps][5];  // target box and rc^2 of the warp's chunk
+template <bool kLearned, bool kStaged, int kWarps>
+__global__ void __launch_bounds__(32 * kWarps, 32 / kWarps) k_eval_near(MixedView m, double *uv, const int *perm,
+                                                                         Decisions dec, long wait_limit) {
+  extern __shared__ __align__(128) float4 s_src[];  // kStaged: [kWarps][2 * kStage]
+  __shared__ __align__(8) uint64_t s_bar[kWarps][2];
+  __shared__ float s_tb[kWarps][9];
+  __shared__ __align__(16) float4 s_acc[kWarps][4 * 32];
   __shared__ WarpCounts s_cnt[kWarps];
-  const int lane = threadIdx.x & 31;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   int l = next_leaf(m.st, lane);
-  if (l >= m.nleaf) return;
-  const double inv2pi = 0.15915494309189533577;
-  float *tbox = s_tb[threadIdx.x >> 5];
-  WarpCounts *cnts = &s_cnt[threadIdx.x >> 5];
-  if (lane == 0) *cnts = WarpCounts{};
+  if (l >= m.nleaf) return;  // uniform over the warp; nothing below syncs the block
+  NearWarp w{s_src + (kStaged ? warp * 2 * kStage : 0), s_bar[warp], s_tb[warp], s_acc[warp], &s_cnt[warp], 0u, 0u,
+             true};
+  if (kStaged && lane == 0) {
+    mbar_init(&w.bar[0], 1);
+    mbar_init(&w.bar[1], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (lane == 0) *w.cnts = WarpCounts{};
+  __syncwarp();
   for (; l < m.nleaf; l = next_leaf(m.st, lane)) {
-  const int B = m.leaf_cell[l];
-  const float rc = leaf_cutoff(m, B);
-  for (int t0 = m.begin[B]; t0 < m.end[B]; t0 += 64) {
-    const int ta = t0 + lane, tb = t0 + 32 + lane;
-    const bool va = ta < m.end[B], vb = tb < m.end[B];
-    const bool two = __any_sync(0xffffffffu, vb);
-    const float2 za = va ? m.loc[ta] : make_float2(0.f, 0.f);
-    const float2 zb = vb ? m.loc[tb] : make_float2(0.f, 0.f);
-    target_box(za, va, zb, vb, rc, tbox, lane);
-    float2 pa = make_float2(0.f, 0.f), pb = make_float2(0.f, 0.f);
-    if (two)
-      far_field2(m, l, B, za, zb, pa, pb);
-    else
-      far_field(m, l, B, za, pa);
-    float axa = 0.f, aya = 0.f, cxa = 0.f, cya = 0.f;
-    float axb = 0.f, ayb = 0.f, cxb = 0.f, cyb = 0.f;
-    for (int pass = 0; pass < 2; pass++) {
-      const int e0 = pass == 0 ? m.u_off[l] : m.k_off[l];
-      const int e1 = pass == 0 ? m.u_off[l + 1] : m.k_off[l + 1];
-      const int *idx = pass == 0 ? m.u_idx : m.k_idx;
-      for (int e = e0; e < e1; e++) {
-        const int A = idx[e];
-        if (kLearned) {
-          const int d = pass == 0 ? dec.u[e] : dec.k[e];
-          if (d > 0) {
-            // accepted: the source leaf's multipole at the chosen order (U), or
-            // the correction left out (K)
-            if (pass == 0) {
-              const int p = min(min(class_order(d) + dec.margin, 16), m.P);
-              if (two)
-                m2p_order2(m, B, A, p, za, zb, pa, pb);
-              else
-                m2p_order(m, B, A, p, za, pa);
-            }
-            continue;
-          }
-        }
-        // offset of the source leaf's centre from the two-float centres: FP32
-        // centres alone would carry ~3e-8 absolute error into every close pair
-        const float ox = centre_offset(m.cxf, m.cxl, B, A), oy = centre_offset(m.cyf, m.cyl, B, A);
-        const int j0 = m.begin[A], j1 = m.end[A];
-        const float txa = __fadd_rn(za.x, ox), tya = __fadd_rn(za.y, oy), txb = __fadd_rn(zb.x, ox),
-                    tyb = __fadd_rn(zb.y, oy);
-        float sxa = 0.f, sya = 0.f, sxb = 0.f, syb = 0.f;
-        unsigned msk = kAllChunks;
-        if (pass == 1) {
-          msk = chunk_mask(m, A, ox, oy, tbox, lane);
-          if (!msk) {
-            counts_add(cnts, lane, 0u, 0u, (unsigned)(j1 - j0));
-            continue;
-          }
-        }
-        int done = 0;
-        for (unsigned r = msk; r;) {
-          int s0, s1;
-          next_run(r, j1 - j0, s0, s1);
-          if (pass == 0)
-            leaf_pairs<false>(m.src4 + j0, s0, s1, txa, tya, txb, tyb, two, sxa, sya, sxb, syb);
-          else
-            leaf_pairs<true>(m.src4 + j0, s0, s1, txa, tya, txb, tyb, two, sxa, sya, sxb, syb);
-          done += s1 - s0;
-        }
-        counts_add(cnts, lane, (unsigned)done, pass == 1 ? (unsigned)done : 0u, pass == 1 ? (unsigned)(j1 - j0) : 0u);
-        kahan(axa, cxa, sxa);
-        kahan(aya, cya, sya);
-        kahan(axb, cxb, sxb);
-        kahan(ayb, cyb, syb);
+    const int B = m.leaf_cell[l];
+    for (int t0 = m.begin[B]; t0 < m.end[B];) {
+      const int rem = m.end[B] - t0;
+      if (rem > 96) {
+        near_chunk<kLearned, kStaged, 4>(m, dec, uv, perm, wait_limit, l, B, t0, lane, w);
+        t0 += 128;
+      } else if (rem > 32) {
+        near_chunk<kLearned, kStaged, 2>(m, dec, uv, perm, wait_limit, l, B, t0, lane, w);
+        t0 += 64;
+      } else {
+        near_chunk<kLearned, kStaged, 1>(m, dec, uv, perm, wait_limit, l, B, t0, lane, w);
+        t0 += 32;
       }
     }
-    counts_close(cnts, lane, va, vb);
-    // FP64 final reduction: u = Im(phi)/2pi + ax/2pi, v = Re(phi)/2pi + ay/2pi
-    if (va) {
-      const int o = perm[ta];
-      uv[2 * (size_t)o] = ((double)pa.y + (double)axa - (double)cxa) * inv2pi;
-      uv[2 * (size_t)o + 1] = ((double)pa.x + (double)aya - (double)cya) * inv2pi;
-    }
-    if (vb) {
-      const int o = perm[tb];
-      uv[2 * (size_t)o] = ((double)pb.y + (double)axb - (double)cxb) * inv2pi;
-      uv[2 * (size_t)o + 1] = ((double)pb.x + (double)ayb - (double)cyb) * inv2pi;
-    }
   }
-  }  // next leaf
-  counts_flush(cnts, lane, m.st);
+  // copies still in flight after a wait gave up: wait (bounded) before the
+  // shared memory is released
+  if (kStaged)
+    for (int b = 0; b < 2; b++)
+      if (w.inflight & (1u << b)) mbar_wait(&w.bar[b], (w.parity >> b) & 1u, wait_limit);
+  counts_flush(w.cnts, lane, m.st);
 }
 
 // ------------------------------------------------------------ off-blob points
@@ -1768,11 +1847,11 @@ __global__ void __launch_bounds__(kPtWarps * 32) k_eval_points(MixedView m, int 
     }
     if (is_leaf) {
       if (act && !far) {
-        const float fx = (float)dx, fy = (float)dy;
-        float sx = 0.f, sy = 0.f;
-        for (int j = m.begin[c]; j < m.end[c]; j++) pair<false>(m.src4[j], fx, fy, sx, sy);
-        ax += (double)sx;
-        ay += (double)sy;
+        const float nfx = -(float)dx, nfy = -(float)dy;
+        float sa = 0.f, sb = 0.f;  // velocity (sa, -sb), see pair
+        for (int j = m.begin[c]; j < m.end[c]; j++) pair<false>(m.src4[j], nfx, nfy, sa, sb);
+        ax += (double)sa;
+        ay -= (double)sb;
         n_pairs += (unsigned long long)(m.end[c] - m.begin[c]);
       }
     } else {
@@ -2014,12 +2093,12 @@ constexpr int kEvalVariants = 4;
 // device at once (the kernel's occupancy times the SM count, found once per
 // kernel and kept in *resident), fewer when the leaves are fewer.
 template <class K>
-int persistent_blocks(K kernel, int warps_per_block, int nleaf, int *resident) {
+int persistent_blocks(K kernel, int warps_per_block, size_t smem, int nleaf, int *resident) {
   if (*resident == 0) {
     int dev = 0, sms = 0, per_sm = 0;
     if (cudaGetDevice(&dev) != cudaSuccess ||
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, 32 * warps_per_block, 0) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, 32 * warps_per_block, smem) != cudaSuccess ||
         per_sm < 1)
       return (nleaf + warps_per_block - 1) / warps_per_block;  // one warp per leaf
     *resident = sms * per_sm;
@@ -2028,33 +2107,32 @@ int persistent_blocks(K kernel, int warps_per_block, int nleaf, int *resident) {
   return need < *resident ? need : *resident;
 }
 
+// One near-field variant: kStaged sources (stage buffers in dynamic shared
+// memory, 4 KB per warp), kWarps warps per block, persistent blocks.
+template <bool kLearned, bool kStaged, int kWarps>
+cudaError_t launch_near(const MixedView &m, double *uv, const int *perm, Decisions d, cudaStream_t s, int *resident) {
+  auto k = k_eval_near<kLearned, kStaged, kWarps>;
+  const size_t smem = kStaged ? (size_t)kWarps * 2 * kStage * sizeof(float4) : 0;
+  if (*resident == 0 && smem > 0) {
+    const cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+  }
+  k<<<persistent_blocks(k, kWarps, smem, m.nleaf, resident), 32 * kWarps, smem, s>>>(m, uv, perm, d, kEvalWaitLimit);
+  return cudaSuccess;
+}
+
 template <bool kLearned>
 cudaError_t launch_eval(int v, const MixedView &m, double *uv, const int *perm, Decisions d, cudaStream_t s) {
   static int resident[kEvalVariants] = {};  // per variant (the devices here are all one model)
   cudaError_t e = cudaMemsetAsync(&m.st->eval_next, 0, sizeof(unsigned), s);
   if (e != cudaSuccess) return e;
   switch (v) {
-    case 0: {
-      auto k = k_eval_mixed<kLearned, 4>;
-      k<<<persistent_blocks(k, 4, m.nleaf, &resident[0]), 128, 0, s>>>(m, uv, perm, d, kEvalWaitLimit);
-      break;
-    }
-    case 1: {
-      auto k = k_eval_mixed<kLearned, 8>;
-      k<<<persistent_blocks(k, 8, m.nleaf, &resident[1]), 256, 0, s>>>(m, uv, perm, d, kEvalWaitLimit);
-      break;
-    }
-    case 2: {
-      auto k = k_eval_staged<kLearned, 4>;
-      k<<<persistent_blocks(k, 4, m.nleaf, &resident[2]), 128, 0, s>>>(m, uv, perm, d, kEvalWaitLimit);
-      break;
-    }
-    default: {
-      auto k = k_eval_staged<kLearned, 8>;
-      k<<<persistent_blocks(k, 8, m.nleaf, &resident[3]), 256, 0, s>>>(m, uv, perm, d, kEvalWaitLimit);
-      break;
-    }
+    case 0: e = launch_near<kLearned, false, 4>(m, uv, perm, d, s, &resident[0]); break;
+    case 1: e = launch_near<kLearned, false, 8>(m, uv, perm, d, s, &resident[1]); break;
+    case 2: e = launch_near<kLearned, true, 4>(m, uv, perm, d, s, &resident[2]); break;
+    default: e = launch_near<kLearned, true, 8>(m, uv, perm, d, s, &resident[3]); break;
   }
+  if (e != cudaSuccess) return e;
   g_launches.fetch_add(1, std::memory_order_relaxed);
   return cudaGetLastError();
 }

@@ -26,8 +26,13 @@ def test_training_gradient_matches_oracle(gpu_lib):
     X, y, theta = random_batch(512, 3)
     loss, g = P.mlp_grad(X, y, theta)
     lref, gref = M.loss_and_grad(theta.astype(np.float64), X.astype(np.float64), y)
-    assert abs(loss - lref) <= 1e-3 * abs(lref)
-    assert np.linalg.norm(g - gref) <= 1e-2 * np.linalg.norm(gref)
+    # The oracle restates the BF16 roundings of weights and layer inputs and
+    # accumulates in float64; the GPU accumulates in FP32 in its own order.
+    # Measured on GB300 over six seeds: loss within 6.0e-6 relative,
+    # gradient within 6.0e-5 normwise (a BF16 input rounding that the two
+    # accumulation orders send to different sides moves both).
+    assert abs(loss - lref) <= 5e-5 * abs(lref)
+    assert np.linalg.norm(g - gref) <= 5e-4 * np.linalg.norm(gref)
 
 
 @pytest.mark.gpu
@@ -38,10 +43,25 @@ def test_tensor_core_inference_matches_training_forward(gpu_lib):
     tc = P.mlp_forward(X, theta, tensor_cores=True)
     ref, _ = M.forward(theta.astype(np.float64), X.astype(np.float64))
     scale = np.abs(ref[:, :14]).max()
-    assert np.abs(cc[:, :14] - ref[:, :14]).max() <= 2e-2 * scale
-    assert np.abs(tc[:, :14] - ref[:, :14]).max() <= 5e-2 * scale
+    # The CUDA-core forward rounds the layer inputs to BF16 as the oracle
+    # does and accumulates in FP32: all but a few logits agree to FP32
+    # accumulation order (measured over six seeds: 99th percentile 1.2e-7 of
+    # the scale); the rest follow an input whose BF16 rounding the two
+    # orders decide differently (largest measured 1.8e-3).
+    dc = np.abs(cc[:, :14] - ref[:, :14])
+    assert np.percentile(dc, 99) <= 1e-6 * scale
+    assert dc.max() <= 4e-3 * scale
+    # The tensor-core path forms the GELU itself in BF16 (every step rounded
+    # to BF16, tanh from the SFU's BF16 approximation), which no float64
+    # restatement reproduces step for step: its logits sit at the BF16
+    # rounding level (measured over six seeds: 99th percentile 3.0-3.7e-3,
+    # largest 7.5e-3 of the scale) and pick the same class for >= 99.2% of
+    # rows.
+    dt = np.abs(tc[:, :14] - ref[:, :14])
+    assert np.percentile(dt, 99) <= 6e-3 * scale
+    assert dt.max() <= 2e-2 * scale
     agree = (tc[:, :14].argmax(1) == ref[:, :14].argmax(1)).mean()
-    assert agree >= 0.95, agree
+    assert agree >= 0.98, agree
 
 
 def _solve(P, torch, b, mode, cutoff=3.0):
