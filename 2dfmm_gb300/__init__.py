@@ -26,12 +26,13 @@ ERR_PARAM_FILE, ERR_BAD_PARAMS, ERR_BAD_INPUT, ERR_TOO_DEEP, ERR_CUDA, ERR_NO_TR
     ERR_MODE, ERR_TOO_LARGE, ERR_FILE = range(1, 12)
 STATIC_MAX_BLOBS = 65536
 MODE_PLAIN, MODE_MIXED, MODE_LEARNED = 0, 1, 2
+EVAL_VARIANTS = 5  # TREE2D_EVAL_VARIANTS
 
 # Every symbol include/tree2d.h declares.
 EXPORTS = [
     "make_tree", "biot_tree", "tree2d_last_error", "tree2d_error_string", "tree2d_set_params",
     "tree2d_clear_params", "tree2d_get_params", "tree2d_set_mode", "tree2d_get_mode", "tree2d_set_mixed_params", "tree2d_set_mixed_leaf", "biot_tree_batch",
-    "tree2d_solve_device", "tree2d_solve_device_static", "tree2d_solve_sets", "tree2d_set_tuning", "tree2d_get_stats", "tree2d_export_tree", "tree2d_direct_device", "tree2d_fp64_probe", "tree2d_pipe_probe", "tree2d_wait_probe", "tree2d_version",
+    "tree2d_solve_device", "tree2d_solve_device_static", "tree2d_solve_sets", "tree2d_set_tuning", "tree2d_set_level_chain", "tree2d_get_stats", "tree2d_export_tree", "tree2d_direct_device", "tree2d_fp64_probe", "tree2d_pipe_probe", "tree2d_wait_probe", "tree2d_version",
     "tree2d_learn_param_count", "tree2d_learn_load", "tree2d_learn_set_weights", "tree2d_learn_set_envelope", "tree2d_learn_get_weights", "tree2d_learn_set_options",
     "tree2d_learn_collect", "tree2d_learn_train", "tree2d_mlp_grad", "tree2d_mlp_forward",
     "tree2d_set_mirror", "tree2d_advect_device",
@@ -119,6 +120,8 @@ def load(path: str | None = None):
     L.tree2d_pipe_probe.restype = ctypes.c_int
     L.tree2d_set_tuning.argtypes = [ctypes.c_int, ctypes.c_int]
     L.tree2d_set_tuning.restype = ctypes.c_int
+    L.tree2d_set_level_chain.argtypes = [ctypes.c_int]
+    L.tree2d_set_level_chain.restype = ctypes.c_int
     L.tree2d_solve_sets.argtypes = [ctypes.c_int, _ip, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                     ctypes.c_void_p, ctypes.c_void_p]
     L.tree2d_solve_sets.restype = ctypes.c_int
@@ -253,8 +256,14 @@ def solve_device(d_xy: int, d_cir: int, d_cor: int, d_uv: int, n: int, stream: i
 
 def set_tuning(autotune: bool = True, eval_variant: int = -1):
     """Near-field kernel tuning (bit-identical variants): autotune on the
-    first solve of each size class, or force a variant 0..3."""
+    first solve of each size class, or force a variant 0..EVAL_VARIANTS-1."""
     _check(load().tree2d_set_tuning(int(autotune), eval_variant), "set_tuning")
+
+
+def set_level_chain(on: bool = False):
+    """P = 16 M2M / L2L levels as one cooperative launch each, or one launch
+    per level (default); the results are the same."""
+    _check(load().tree2d_set_level_chain(int(on)), "set_level_chain")
 
 
 def solve_sets(d_xy: int, d_cir: int, d_cor: int, d_uv: int, offsets, stream: int = 0):

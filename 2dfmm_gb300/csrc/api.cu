@@ -813,9 +813,16 @@ int tree2d_get_mode(void) { return lib().mode; }
 int tree2d_set_tuning(int autotune, int eval_variant) {
   Lib &L = lib();
   std::lock_guard<std::mutex> lk(L.mu);
-  if (eval_variant < -1 || eval_variant > 3) return fail(TREE2D_ERR_BAD_PARAMS);
+  if (eval_variant < -1 || eval_variant >= kEvalVariantCount) return fail(TREE2D_ERR_BAD_PARAMS);
   L.mixed.autotune = autotune ? 1 : 0;
   L.mixed.eval_variant = eval_variant;
+  return TREE2D_OK;
+}
+
+int tree2d_set_level_chain(int on) {
+  Lib &L = lib();
+  std::lock_guard<std::mutex> lk(L.mu);
+  L.mixed.level_chain = on ? 1 : 0;
   return TREE2D_OK;
 }
 

@@ -863,7 +863,7 @@ retry:
   // 3. sort
   if (packed)
     T2D_CUDA_TRY(radix_sort_packed(words, words == t.keys ? keys_alt : t.keys, n, 64 - 2 * total_levels, t.keys,
-                                   vals, sort_tmp, s));
+                                   vals, sort_tmp, ws.status, s));
   else
     T2D_CUDA_TRY(radix_sort_pairs(t.keys, vals, keys_alt, vals_alt, n, 64 - 2 * total_levels, 64, sort_tmp, s));
   t.key_order = vals;

@@ -46,18 +46,21 @@ struct MixedParams {
   int eval_variant = -1;  // >= 0: force this near-field variant
   int leaf_blobs = -1;    // most blobs per leaf of the mixed forms' tree: -1 by set size
                           // (mixed_leaf_blobs), 0 the parameters' num_p - 1, > 0 this
+  int level_chain = 0;    // M2M / L2L level chains as one cooperative launch each (P = 16)
 };
 
 // Most blobs per leaf of the tree the mixed forms build (the plain form keeps
 // the parameters' num_p - 1, the reference's).  By set size (n_set blobs per
 // set): a leaf's near field grows with its size while the per-leaf work (lists,
 // decisions, expansions, M2L) shrinks, and in larger, denser sets more of each
-// leaf's list is correction entries, so larger leaves pay: 64 below 512K
-// blobs, 96 below 2M, 128 from 2M.
+// leaf's list is correction entries, so larger leaves pay: 96 below 2M
+// blobs, 128 from 2M (measured on GB300: the 512-set batch of 2K-200K blobs
+// per set takes 16.9 ms at 96 against 17.5 at 64 and 17.4 at 112; 1M
+// Lamb-Oseen blobs 2.13 ms at 96 and 128 against 2.39 at 64).
 inline int mixed_leaf_blobs(const MixedParams &mp, long n_set, int num_p) {
   if (mp.leaf_blobs > 0) return mp.leaf_blobs;
   if (mp.leaf_blobs == 0) return num_p - 1;
-  return n_set < (512l << 10) ? 64 : (n_set < (2l << 20) ? 96 : 128);
+  return n_set < (2l << 20) ? 96 : 128;
 }
 
 // Root box, written on the device (quadtree.c:81-99 semantics).
@@ -81,6 +84,8 @@ struct DevStatus {
   unsigned long long n_pairs_k;   // mixed: correction pairs evaluated (part of n_pairs)
   unsigned long long n_pairs_k_listed;  // mixed: correction pairs of the K entries evaluated, before the chunk cull
   unsigned eval_next;      // mixed: next target leaf of the persistent near-field warps
+  unsigned bar_count;      // mixed: arrivals at the level chain's grid barrier (zeroed before a launch)
+  unsigned bar_gen;        // mixed: generation of that barrier
 };
 
 // Bump allocator over one device allocation.  Buffers are 256-byte aligned.
@@ -222,9 +227,11 @@ size_t radix_sort_temp_bytes(int n);
 // (their contents are scratch afterwards); the last pass writes the keys
 // (low half cleared) to keys_out and the values to vals_out.  The last pass
 // reads words when the pass count ceil((64 - begin_bit) / 8) is odd and
-// words_alt when it is even: keys_out may be the other one.
+// words_alt when it is even: keys_out may be the other one.  With st, each
+// pass is a single kernel (decoupled look-back; a look-back that times out
+// records TREE2D_ERR_TIMEOUT in st); without, the reduce-then-scan form.
 cudaError_t radix_sort_packed(uint64_t *words, uint64_t *words_alt, int n, int begin_bit, uint64_t *keys_out,
-                              uint32_t *vals_out, void *temp, cudaStream_t s);
+                              uint32_t *vals_out, void *temp, DevStatus *st, cudaStream_t s);
 cudaError_t radix_sort_pairs(uint64_t *keys, uint32_t *vals, uint64_t *keys_alt, uint32_t *vals_alt,
                              int n, int begin_bit, int end_bit, void *temp, cudaStream_t s);
 

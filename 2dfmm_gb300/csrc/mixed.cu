@@ -970,16 +970,18 @@ __device__ __forceinline__ int child_of(const int4 ch, int q) {
   return q == 0 ? ch.x : q == 1 ? ch.y : q == 2 ? ch.z : ch.w;
 }
 
-template <int kP>
-__global__ void __launch_bounds__(kQuadThreads) k_m2m_quad(MixedView m, int lev) {
-  __shared__ float2 s_tab[4 * (kP * kP + 1)];  // [q][n][k], padded per q
-  stage_translation_padded<kP>(m.m2m, s_tab);
+// One level of M2M with four threads per parent cell (thread q of a quad
+// translates child q, the quad sums the four by shuffles), cells i0, i0 +
+// stride, ... of level lev.  kCg: the children's multipoles are read past
+// L1 (written by other blocks of the same launch in the level chain).
+template <int kP, bool kCg>
+__device__ __forceinline__ void m2m_quad_level(const MixedView &m, const float2 *s_tab, int lev, int i0, int stride) {
   const int lane = threadIdx.x & 31, q = lane & 3;
   const unsigned qmask = 0xfu << (lane & ~3);
   const int *cells = m.by_level + m.level_off[lev];
   const int cnt = m.level_off[lev + 1] - m.level_off[lev];
   const float2 *t = s_tab + q * (kP * kP + 1);
-  for (int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 2; i < cnt; i += (gridDim.x * blockDim.x) >> 2) {
+  for (int i = i0; i < cnt; i += stride) {
     const int p = cells[i];
     if (m.leaf[p]) continue;  // the same cell, so the same branch, for the whole quad
     const int c = child_of(reinterpret_cast<const int4 *>(m.child)[p], q);
@@ -991,7 +993,7 @@ __global__ void __launch_bounds__(kQuadThreads) k_m2m_quad(MixedView m, int lev)
       float a[2 * kP];
 #pragma unroll
       for (int j = 0; j < kP / 2; j++) {
-        const float4 v = src[j];
+        const float4 v = kCg ? __ldcg(src + j) : src[j];
         a[4 * j] = v.x;
         a[4 * j + 1] = v.y;
         a[4 * j + 2] = v.z;
@@ -1025,15 +1027,16 @@ __global__ void __launch_bounds__(kQuadThreads) k_m2m_quad(MixedView m, int lev)
   }
 }
 
-template <int kP>
-__global__ void __launch_bounds__(kQuadThreads) k_l2l_quad(MixedView m, int lev) {
-  __shared__ float2 s_tab[4 * (kP * kP + 1)];  // [q][k][l], padded per q
-  stage_translation_padded<kP>(m.l2l, s_tab);
+// One level of L2L from the internal cells of level lev-1 into their
+// children, thread q of a quad for child q.  kCg: the parents' local
+// expansions are read past L1 (the level chain).
+template <int kP, bool kCg>
+__device__ __forceinline__ void l2l_quad_level(const MixedView &m, const float2 *s_tab, int lev, int i0, int stride) {
   const int q = threadIdx.x & 3;
   const int *cells = m.by_level + m.level_off[lev - 1];
   const int cnt = m.level_off[lev] - m.level_off[lev - 1];
   const float2 *t = s_tab + q * (kP * kP + 1);
-  for (int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 2; i < cnt; i += (gridDim.x * blockDim.x) >> 2) {
+  for (int i = i0; i < cnt; i += stride) {
     const int p = cells[i];
     if (m.leaf[p]) continue;
     const int c = child_of(reinterpret_cast<const int4 *>(m.child)[p], q);
@@ -1042,7 +1045,7 @@ __global__ void __launch_bounds__(kQuadThreads) k_l2l_quad(MixedView m, int lev)
     float b[2 * kP];
 #pragma unroll
     for (int j = 0; j < kP / 2; j++) {
-      const float4 v = src[j];
+      const float4 v = kCg ? __ldcg(src + j) : src[j];
       b[4 * j] = v.x;
       b[4 * j + 1] = v.y;
       b[4 * j + 2] = v.z;
@@ -1076,6 +1079,74 @@ __global__ void __launch_bounds__(kQuadThreads) k_l2l_quad(MixedView m, int lev)
       dst[j] = re;
       dst[kP / 4 + j] = im;
     }
+  }
+}
+
+template <int kP>
+__global__ void __launch_bounds__(kQuadThreads) k_m2m_quad(MixedView m, int lev) {
+  __shared__ float2 s_tab[4 * (kP * kP + 1)];  // [q][n][k], padded per q
+  stage_translation_padded<kP>(m.m2m, s_tab);
+  m2m_quad_level<kP, false>(m, s_tab, lev, (blockIdx.x * blockDim.x + threadIdx.x) >> 2,
+                            (gridDim.x * blockDim.x) >> 2);
+}
+
+template <int kP>
+__global__ void __launch_bounds__(kQuadThreads) k_l2l_quad(MixedView m, int lev) {
+  __shared__ float2 s_tab[4 * (kP * kP + 1)];  // [q][k][l], padded per q
+  stage_translation_padded<kP>(m.l2l, s_tab);
+  l2l_quad_level<kP, false>(m, s_tab, lev, (blockIdx.x * blockDim.x + threadIdx.x) >> 2,
+                            (gridDim.x * blockDim.x) >> 2);
+}
+
+// Grid-wide barrier of a cooperative launch (every block resident): block
+// arrivals are counted in st->bar_count (zero before the launch); the last
+// block to arrive resets it and advances st->bar_gen, the others poll the
+// generation, at most `limit` times (a healthy barrier ends in
+// microseconds).  After a poll limit the kernel records TREE2D_ERR_TIMEOUT
+// and returns false in every thread of the block; later barriers of that
+// block do not wait.
+__device__ bool grid_barrier(DevStatus *st, unsigned nblocks, long limit, bool &ok) {
+  __syncthreads();
+  if (threadIdx.x == 0 && ok) {
+    volatile unsigned *gen = &st->bar_gen;
+    const unsigned g = *gen;
+    __threadfence();
+    if (atomicAdd(&st->bar_count, 1u) + 1u == nblocks) {
+      st->bar_count = 0;
+      __threadfence();
+      atomicAdd(&st->bar_gen, 1u);
+    } else {
+      long i = 0;
+      while (*gen == g && i < limit) i++;
+      if (*gen == g) {
+        ok = false;
+        set_err(st, TREE2D_ERR_TIMEOUT);
+      }
+    }
+    __threadfence();
+  }
+  ok = __syncthreads_and(threadIdx.x == 0 ? ok : 1) != 0;
+  return ok;
+}
+
+// The M2M chain (kUp: levels depth-1 down to lev_end) or the L2L chain
+// (levels lev_end up to depth) in one cooperative launch of persistent
+// blocks: each level's cells are spread over all blocks, and the blocks
+// meet at the grid barrier before the next level reads what this one wrote.
+template <int kP, bool kUp>
+__global__ void __launch_bounds__(kQuadThreads) k_chain_quad(MixedView m, int lev_first, int lev_last, long limit) {
+  __shared__ float2 s_tab[4 * (kP * kP + 1)];
+  stage_translation_padded<kP>(kUp ? m.m2m : m.l2l, s_tab);
+  const int i0 = (blockIdx.x * blockDim.x + threadIdx.x) >> 2, stride = (gridDim.x * blockDim.x) >> 2;
+  bool ok = true;
+  const int step = kUp ? -1 : 1;
+  for (int lev = lev_first;; lev += step) {
+    if (kUp)
+      m2m_quad_level<kP, true>(m, s_tab, lev, i0, stride);
+    else
+      l2l_quad_level<kP, true>(m, s_tab, lev, i0, stride);
+    if (lev == lev_last) break;
+    if (!grid_barrier(m.st, gridDim.x, limit, ok)) return;
   }
 }
 
@@ -1328,17 +1399,17 @@ __device__ __forceinline__ void leaf_pairs1(const S src, int j0, int j1, float n
   for (int j = j0; j < j1; j++) pair<kCorrection>(src[j], ntx, nty, a, b);
 }
 
-template <bool kCorrection, class S>
+template <bool kCorrection, int kUnroll, class S>
 __device__ __forceinline__ void leaf_pairs2(const S src, int j0, int j1, float2 ntx, float2 nty, float2 &a,
                                             float2 &b) {
-#pragma unroll 2
+#pragma unroll kUnroll
   for (int j = j0; j < j1; j++) pair2<kCorrection>(src[j], ntx, nty, a, b);
 }
 
-template <bool kCorrection, class S>
+template <bool kCorrection, int kUnroll, class S>
 __device__ __forceinline__ void leaf_pairs4(const S src, int j0, int j1, float2 ntx0, float2 nty0, float2 ntx1,
                                             float2 nty1, float2 &a0, float2 &b0, float2 &a1, float2 &b1) {
-#pragma unroll 2
+#pragma unroll kUnroll
   for (int j = j0; j < j1; j++) {
     const float4 sj = src[j];
     pair2<kCorrection>(sj, ntx0, nty0, a0, b0);
@@ -1504,7 +1575,7 @@ __device__ __forceinline__ void leaf_add(float4 *acc, int k, int lane, bool corr
 // and k = 2, 3), each pack with its own bounding box for the correction
 // cull.  The tree's in-leaf order is spatial (k_leaf_setup), so a pack of
 // 64 consecutive targets is compact.
-template <bool kLearned, bool kStaged, int kT>
+template <bool kLearned, bool kStaged, int kT, int kUnroll>
 __device__ __forceinline__ void near_chunk(const MixedView &m, const Decisions &dec, double *uv, const int *perm,
                                            long wait_limit, int l, int B, int t0, int lane, NearWarp &w) {
   constexpr int kPacks = kT == 4 ? 2 : 1;
@@ -1642,9 +1713,9 @@ __device__ __forceinline__ void near_chunk(const MixedView &m, const Decisions &
           const float2 tx = make_float2(ntx[k], ntx[k + 1]), ty = make_float2(nty[k], nty[k + 1]);
           float2 a = make_float2(sa[k], sa[k + 1]), b = make_float2(sb[k], sb[k + 1]);
           if (!corr)
-            leaf_pairs2<false>(src, s0, s1, tx, ty, a, b);
+            leaf_pairs2<false, kUnroll>(src, s0, s1, tx, ty, a, b);
           else
-            leaf_pairs2<true>(src, s0, s1, tx, ty, a, b);
+            leaf_pairs2<true, kUnroll>(src, s0, s1, tx, ty, a, b);
           sa[k] = a.x, sa[k + 1] = a.y, sb[k] = b.x, sb[k + 1] = b.y;
         };
         if (kT == 4 && packs == 2)
@@ -1657,9 +1728,9 @@ __device__ __forceinline__ void near_chunk(const MixedView &m, const Decisions &
         float2 a0 = make_float2(sa[0], sa[1]), b0 = make_float2(sb[0], sb[1]);
         float2 a1 = make_float2(sa[kT - 2], sa[kT - 1]), b1 = make_float2(sb[kT - 2], sb[kT - 1]);
         if (!corr)
-          leaf_pairs4<false>(src, s0, s1, tx0, ty0, tx1, ty1, a0, b0, a1, b1);
+          leaf_pairs4<false, kUnroll>(src, s0, s1, tx0, ty0, tx1, ty1, a0, b0, a1, b1);
         else
-          leaf_pairs4<true>(src, s0, s1, tx0, ty0, tx1, ty1, a0, b0, a1, b1);
+          leaf_pairs4<true, kUnroll>(src, s0, s1, tx0, ty0, tx1, ty1, a0, b0, a1, b1);
         sa[0] = a0.x, sa[1] = a0.y, sb[0] = b0.x, sb[1] = b0.y;
         sa[kT - 2] = a1.x, sa[kT - 1] = a1.y, sb[kT - 2] = b1.x, sb[kT - 1] = b1.y;
       }
@@ -1723,8 +1794,8 @@ __device__ __forceinline__ void near_chunk(const MixedView &m, const Decisions &
   __syncwarp();
 }
 
-template <bool kLearned, bool kStaged, int kWarps>
-__global__ void __launch_bounds__(32 * kWarps, 32 / kWarps) k_eval_near(MixedView m, double *uv, const int *perm,
+template <bool kLearned, bool kStaged, int kWarps, bool kWide>
+__global__ void __launch_bounds__(32 * kWarps, (kWide ? 24 : 32) / kWarps) k_eval_near(MixedView m, double *uv, const int *perm,
                                                                          Decisions dec, long wait_limit) {
   extern __shared__ __align__(128) float4 s_src[];  // kStaged: [kWarps][2 * kStage]
   __shared__ __align__(8) uint64_t s_bar[kWarps][2];
@@ -1748,13 +1819,13 @@ __global__ void __launch_bounds__(32 * kWarps, 32 / kWarps) k_eval_near(MixedVie
     for (int t0 = m.begin[B]; t0 < m.end[B];) {
       const int rem = m.end[B] - t0;
       if (rem > 96) {
-        near_chunk<kLearned, kStaged, 4>(m, dec, uv, perm, wait_limit, l, B, t0, lane, w);
+        near_chunk<kLearned, kStaged, 4, kWide ? 4 : 2>(m, dec, uv, perm, wait_limit, l, B, t0, lane, w);
         t0 += 128;
       } else if (rem > 32) {
-        near_chunk<kLearned, kStaged, 2>(m, dec, uv, perm, wait_limit, l, B, t0, lane, w);
+        near_chunk<kLearned, kStaged, 2, kWide ? 4 : 2>(m, dec, uv, perm, wait_limit, l, B, t0, lane, w);
         t0 += 64;
       } else {
-        near_chunk<kLearned, kStaged, 1>(m, dec, uv, perm, wait_limit, l, B, t0, lane, w);
+        near_chunk<kLearned, kStaged, 1, kWide ? 4 : 2>(m, dec, uv, perm, wait_limit, l, B, t0, lane, w);
         t0 += 32;
       }
     }
@@ -2050,10 +2121,49 @@ static int quad_blocks(const int *lev_off, int lev) {
   return b < 1 ? 1 : (b > full ? full : b);
 }
 
-int mixed_upward(MixedView &m, int depth, const int *lev_off, cudaStream_t s) {
+// The M2M or L2L level chain as one cooperative launch of persistent
+// blocks (k_chain_quad), for P = 16 and at least two levels: returns false
+// (nothing launched) where the device cannot co-schedule the grid, and the
+// caller launches one kernel per level instead.
+constexpr long kChainWaitLimit = 1l << 22;
+
+template <bool kUp>
+bool launch_chain(MixedView &m, int lev_first, int lev_last, cudaStream_t s) {
+  static int blocks[2] = {0, 0};  // per direction: resident blocks, found once (the devices here are one model)
+  int &nb = blocks[kUp ? 1 : 0];
+  auto k = k_chain_quad<16, kUp>;
+  if (nb == 0) {
+    int dev = 0, sms = 0, per_sm = 0, coop = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev) != cudaSuccess || !coop ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, kQuadThreads, 0) != cudaSuccess || per_sm < 1) {
+      nb = -1;
+    } else {
+      nb = sms * (per_sm < 4 ? per_sm : 4);
+    }
+  }
+  if (nb < 0) return false;
+  if (cudaMemsetAsync(&m.st->bar_count, 0, sizeof(unsigned), s) != cudaSuccess) return false;
+  long limit = kChainWaitLimit;
+  void *args[] = {&m, &lev_first, &lev_last, &limit};
+  if (cudaLaunchCooperativeKernel((const void *)k, dim3((unsigned)nb), dim3(kQuadThreads), args, 0, s) !=
+      cudaSuccess) {
+    (void)cudaGetLastError();  // not launched: clear the error, run per level
+    return false;
+  }
+  g_launches.fetch_add(1, std::memory_order_relaxed);
+  return true;
+}
+
+int mixed_upward(MixedView &m, int depth, const int *lev_off, cudaStream_t s, bool chain) {
   k_s2m_f32<<<(int)(((long)m.nleaf * 32 + 255) / 256), 256, 0, s>>>(m);
   g_launches.fetch_add(1, std::memory_order_relaxed);
   const size_t tab_bytes = 4 * sizeof(float2) * m.P * m.P;
+  if (chain && m.P == 16 && depth - 1 > 2 + m.lev0 && launch_chain<true>(m, depth - 1, 2 + m.lev0, s)) {
+    T2D_CUDA_TRY(cudaGetLastError());
+    return TREE2D_OK;
+  }
   for (int lev = depth - 1; lev >= 2 + m.lev0; lev--) {
     if (m.P == 16)
       k_m2m_quad<16><<<quad_blocks(lev_off, lev), kQuadThreads, 0, s>>>(m, lev);
@@ -2067,10 +2177,14 @@ int mixed_upward(MixedView &m, int depth, const int *lev_off, cudaStream_t s) {
   return TREE2D_OK;
 }
 
-int mixed_downward(MixedView &m, int depth, const int *lev_off, cudaStream_t s) {
+int mixed_downward(MixedView &m, int depth, const int *lev_off, cudaStream_t s, bool chain) {
   k_p2l<<<(int)(((long)m.ncell * 32 + 255) / 256), 256, 0, s>>>(m);
   g_launches.fetch_add(1, std::memory_order_relaxed);
   const size_t tab_bytes = 4 * sizeof(float2) * m.P * m.P;
+  if (chain && m.P == 16 && depth > 3 + m.lev0 && launch_chain<false>(m, 3 + m.lev0, depth, s)) {
+    T2D_CUDA_TRY(cudaGetLastError());
+    return TREE2D_OK;
+  }
   for (int lev = 3 + m.lev0; lev <= depth; lev++) {
     if (m.P == 16)
       k_l2l_quad<16><<<quad_blocks(lev_off, lev - 1), kQuadThreads, 0, s>>>(m, lev);
@@ -2086,8 +2200,11 @@ int mixed_downward(MixedView &m, int depth, const int *lev_off, cudaStream_t s) 
 
 // Near-field variants (bit-identical results): 0/1 read the source blobs
 // from global memory with 4/8 warps per block, 2/3 stage them in shared
-// memory by bulk copies with 4/8 warps per block.
-constexpr int kEvalVariants = 4;
+// memory by bulk copies with 4/8 warps per block, 4 stages them with 4
+// warps per block of up to 80 registers per thread (6 blocks per SM) and
+// the pair loops unrolled four times.  At 1M Lamb-Oseen blobs 4 is the
+// fastest, at 4M two-patch + sheet blobs 2, for the 512-set batch 0.
+constexpr int kEvalVariants = kEvalVariantCount;
 
 // Blocks of a persistent near-field launch: as many as are resident on the
 // device at once (the kernel's occupancy times the SM count, found once per
@@ -2109,9 +2226,9 @@ int persistent_blocks(K kernel, int warps_per_block, size_t smem, int nleaf, int
 
 // One near-field variant: kStaged sources (stage buffers in dynamic shared
 // memory, 4 KB per warp), kWarps warps per block, persistent blocks.
-template <bool kLearned, bool kStaged, int kWarps>
+template <bool kLearned, bool kStaged, int kWarps, bool kWide = false>
 cudaError_t launch_near(const MixedView &m, double *uv, const int *perm, Decisions d, cudaStream_t s, int *resident) {
-  auto k = k_eval_near<kLearned, kStaged, kWarps>;
+  auto k = k_eval_near<kLearned, kStaged, kWarps, kWide>;
   const size_t smem = kStaged ? (size_t)kWarps * 2 * kStage * sizeof(float4) : 0;
   if (*resident == 0 && smem > 0) {
     const cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -2130,7 +2247,8 @@ cudaError_t launch_eval(int v, const MixedView &m, double *uv, const int *perm, 
     case 0: e = launch_near<kLearned, false, 4>(m, uv, perm, d, s, &resident[0]); break;
     case 1: e = launch_near<kLearned, false, 8>(m, uv, perm, d, s, &resident[1]); break;
     case 2: e = launch_near<kLearned, true, 4>(m, uv, perm, d, s, &resident[2]); break;
-    default: e = launch_near<kLearned, true, 8>(m, uv, perm, d, s, &resident[3]); break;
+    case 3: e = launch_near<kLearned, true, 8>(m, uv, perm, d, s, &resident[3]); break;
+    default: e = launch_near<kLearned, true, 4, true>(m, uv, perm, d, s, &resident[4]); break;
   }
   if (e != cudaSuccess) return e;
   g_launches.fetch_add(1, std::memory_order_relaxed);
@@ -2465,13 +2583,13 @@ int mixed_solve(Workspace &ws, const Tree &t, const MixedParams &mp, double *d_u
     T2D_TRY_DRAIN(cudaStreamWaitEvent(ws.hi, ws.hi_fork, 0));
     su = ws.hi;
   }
-  rc = mixed_upward(m, t.depth, ws.h_levels, su);
+  rc = mixed_upward(m, t.depth, ws.h_levels, su, mp.level_chain != 0);
   if (rc) return drain(rc);
   T2D_TRY_DRAIN(cudaMemsetAsync(m.L, 0, sizeof(float) * (size_t)nc * 2 * P, su));
   rc = tc ? m2l_tensor_cores(m, dimg, cls_list, cls_count, su) : m2l_cuda_cores(m, dm2l, su);
   if (rc) return drain(rc);
   st.m2l_path = tc ? 2 : 1;
-  rc = mixed_downward(m, t.depth, ws.h_levels, su);
+  rc = mixed_downward(m, t.depth, ws.h_levels, su, mp.level_chain != 0);
   if (rc) return drain(rc);
   if (side) {
     T2D_TRY_DRAIN(cudaEventRecord(ws.hi_join, ws.hi));

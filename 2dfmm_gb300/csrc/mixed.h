@@ -75,8 +75,10 @@ int mixed_lists(MixedView &m, cudaStream_t s);
 int mixed_fill_lists(MixedView &m, bool from_scratch, cudaStream_t s);
 // lev_off: the per-level cell offsets on the host (level_off's first
 // kKeyLevels + 2 entries), to size each level's grid; null = full grids.
-int mixed_upward(MixedView &m, int depth, const int *lev_off, cudaStream_t s);
-int mixed_downward(MixedView &m, int depth, const int *lev_off, cudaStream_t s);
+// chain: run the P = 16 M2M (L2L) levels as one cooperative launch of
+// persistent blocks where the device allows it, else one launch per level.
+int mixed_upward(MixedView &m, int depth, const int *lev_off, cudaStream_t s, bool chain);
+int mixed_downward(MixedView &m, int depth, const int *lev_off, cudaStream_t s, bool chain);
 
 // M2L over the V lists (m2l.cu): L[c] += sum_s T(class(c), s) M[V[c][s]].
 // `tables` is the device copy of the [4][27][P][P] complex operators.
@@ -90,6 +92,9 @@ void m2l_b_images(int P, const float *h_m2l, std::vector<float> &img);
 // Whole mixed solve on a built tree: lists, upward, M2L, downward,
 // evaluation; uv written in original blob order.  Synchronises the stream
 // once (to size the interaction lists).
+// Near-field kernel variants the tuner times (tree2d_set_tuning forces one).
+constexpr int kEvalVariantCount = TREE2D_EVAL_VARIANTS;
+
 int mixed_solve(Workspace &ws, const Tree &t, const MixedParams &mp, double *d_uv, cudaStream_t s,
                 tree2d_stats_t &st);
 

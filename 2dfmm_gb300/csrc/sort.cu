@@ -9,6 +9,17 @@
 // Tiles are processed warp-striped: warp w owns 512 consecutive pairs, its
 // lanes take 32 consecutive pairs per step, so (warp, step, lane) is the
 // input order and the ranking is stable.
+//
+// Packed words (key in the high 32 bits, value in the low 32) take a
+// single-pass form per digit instead (radix_sort_packed): one read of the
+// words forms every pass's digit histogram up front (k_hist_all), and each
+// pass is one kernel (k_onesweep) in which a tile ranks its words as the
+// downsweep does, publishes its per-digit counts, and finds the counts of
+// all earlier tiles by looking back over their published words (decoupled
+// look-back: a tile's word carries either its own count or, once known,
+// the running total through it), then scatters.  Tiles are numbered in the
+// order blocks start (an atomic counter), so a tile only ever waits on
+// tiles that are already running.
 #include "dev_common.cuh"
 
 namespace t2d {
@@ -184,11 +195,164 @@ __global__ void __launch_bounds__(kThreads) k_downsweep(const uint64_t *__restri
   }
 }
 
+// ---------------------------------------------------------------- single pass
+
+constexpr int kMaxPasses = 4;                 // packed words: bits [32, 64)
+constexpr unsigned kFlagAgg = 1u << 30;       // the tile's own count
+constexpr unsigned kFlagPre = 2u << 30;       // the running total through the tile
+constexpr unsigned kCountMask = kFlagAgg - 1u;
+constexpr long kLookbackLimit = 1l << 22;     // polls; a healthy look-back ends in microseconds
+
+// Every pass's digit histogram in one read of the words: per block in
+// shared memory, then added to hist[pass][digit].
+__global__ void __launch_bounds__(kThreads) k_hist_all(const uint64_t *__restrict__ words, int n, int begin_bit,
+                                                       int passes, unsigned *__restrict__ hist) {
+  __shared__ unsigned h[kMaxPasses][kBins];
+  for (int i = threadIdx.x; i < kMaxPasses * kBins; i += kThreads) (&h[0][0])[i] = 0;
+  __syncthreads();
+  const unsigned ltmask = lanemask_lt();
+  const long stride = (long)gridDim.x * kThreads;
+  for (long i0 = (long)blockIdx.x * kThreads + (threadIdx.x & ~31); i0 < n; i0 += stride) {  // warp-uniform
+    const long i = i0 + (threadIdx.x & 31);
+    const bool valid = i < n;
+    const uint64_t w = valid ? words[i] : 0;
+    for (int p = 0; p < passes; p++) {
+      // one shared-memory add per distinct digit of the warp
+      const unsigned d = valid ? (unsigned)(w >> (begin_bit + 8 * p)) & 0xffu : 0x100u;
+      const unsigned peers = __match_any_sync(0xffffffffu, d);
+      if (valid && (peers & ltmask) == 0) atomicAdd(&h[p][d], (unsigned)__popc(peers));
+    }
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < passes * kBins; i += kThreads) {
+    const unsigned v = (&h[0][0])[i];
+    if (v) atomicAdd(&hist[i], v);
+  }
+}
+
+// One pass over packed words: tile ranking as in k_downsweep, the tile's
+// per-digit offset from the look-back over earlier tiles' status words
+// (status[tile][digit], zero before the pass), then the scatter through
+// shared memory.  `hist` is this pass's digit histogram, `ctr` its tile
+// counter (zero before the pass).  A look-back that polls `limit` times
+// without an answer records TREE2D_ERR_TIMEOUT and takes the missing count
+// as zero (the output is then wrong and the build reports the error).
+__global__ void __launch_bounds__(kThreads) k_onesweep(const uint64_t *__restrict__ kin, uint64_t *__restrict__ kout,
+                                                       uint32_t *__restrict__ vout, int n, int shift,
+                                                       const unsigned *__restrict__ hist, unsigned *status,
+                                                       unsigned *ctr, int ntiles, int split, long limit,
+                                                       DevStatus *st) {
+  extern __shared__ __align__(16) unsigned char stage[];
+  uint64_t *sk = reinterpret_cast<uint64_t *>(stage);  // kTile words, tile digit order
+  __shared__ unsigned wcount[kWarps][kBins];
+  __shared__ unsigned lbase[kBins];
+  __shared__ unsigned gbase[kBins];
+  __shared__ unsigned wsum[kWarps];
+  __shared__ int s_tile;
+  if (threadIdx.x == 0) s_tile = (int)atomicAdd(ctr, 1u);
+  const unsigned dbase = block_exclusive_scan(hist[threadIdx.x], wsum);  // synchronises: s_tile is set
+  const int tile = s_tile;
+  if (tile >= ntiles) return;  // uniform for the block (the grid is exactly ntiles blocks)
+  for (int i = threadIdx.x; i < kWarps * kBins; i += kThreads) (&wcount[0][0])[i] = 0;
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const long tile0 = (long)tile * kTile;
+  const long base = tile0 + warp * (kItems * 32);
+  uint64_t k[kItems];
+  unsigned r[kItems];
+  const unsigned ltmask = lanemask_lt();
+#pragma unroll
+  for (int j = 0; j < kItems; j++) {
+    const long i = base + j * 32 + lane;
+    const bool valid = i < n;
+    k[j] = valid ? kin[i] : 0;
+    const unsigned d = valid ? (unsigned)((k[j] >> shift) & 0xff) : 0x100u;
+    const unsigned peers = __match_any_sync(0xffffffffu, d);
+    const unsigned rank = __popc(peers & ltmask);
+    const unsigned c = valid ? wcount[warp][d] : 0;
+    __syncwarp();
+    if (valid && rank == 0) wcount[warp][d] = c + __popc(peers);
+    __syncwarp();
+    r[j] = c + rank;
+  }
+  __syncthreads();
+  unsigned cnt = 0;
+  {
+    const int d = threadIdx.x;
+#pragma unroll
+    for (int w = 0; w < kWarps; w++) {
+      const unsigned c = wcount[w][d];
+      wcount[w][d] = cnt;
+      cnt += c;
+    }
+  }
+  // publish this tile's count of digit d, then look back for the earlier
+  // tiles' total (thread d owns digit d)
+  {
+    const int d = threadIdx.x;
+    volatile unsigned *my = status + (size_t)tile * kBins + d;
+    unsigned excl = 0;
+    if (tile == 0) {
+      *my = kFlagPre | cnt;
+    } else {
+      *my = kFlagAgg | cnt;
+      int t = tile - 1;
+      long polls = 0;
+      while (t >= 0) {
+        const unsigned v = *(volatile const unsigned *)(status + (size_t)t * kBins + d);
+        if ((v & ~kCountMask) == 0u) {
+          if (++polls > limit) {
+            set_err(st, TREE2D_ERR_TIMEOUT);
+            break;
+          }
+          continue;
+        }
+        excl += v & kCountMask;
+        if (v & kFlagPre) break;
+        t--;
+      }
+      *my = kFlagPre | (excl + cnt);
+    }
+    gbase[d] = dbase + excl;
+  }
+  const unsigned lb = block_exclusive_scan(cnt, wsum);
+  lbase[threadIdx.x] = lb;
+  __syncthreads();
+#pragma unroll
+  for (int j = 0; j < kItems; j++) {
+    const long i = base + j * 32 + lane;
+    if (i < n) {
+      const unsigned d = (unsigned)((k[j] >> shift) & 0xff);
+      sk[lbase[d] + wcount[warp][d] + r[j]] = k[j];
+    }
+  }
+  __syncthreads();
+  const int tile_n = (int)min((long)kTile, (long)n - tile0);
+  for (int p = threadIdx.x; p < tile_n; p += kThreads) {
+    const uint64_t key = sk[p];
+    const unsigned d = (unsigned)((key >> shift) & 0xff);
+    const unsigned pos = gbase[d] + ((unsigned)p - lbase[d]);
+    if (split) {
+      kout[pos] = key & 0xffffffff00000000ull;
+      vout[pos] = (uint32_t)key;
+    } else {
+      kout[pos] = key;
+    }
+  }
+}
+
 }  // namespace
+
+static size_t onesweep_temp_bytes(int n) {
+  const size_t ntiles = (size_t)(n > 0 ? (n + kTile - 1) / kTile : 1);
+  return ((size_t)kMaxPasses * kBins + kMaxPasses + (size_t)kMaxPasses * ntiles * kBins) * sizeof(unsigned);
+}
 
 size_t radix_sort_temp_bytes(int n) {
   long ntiles = (n + kTile - 1) / kTile;
-  return (size_t)kBins * (size_t)(ntiles > 0 ? ntiles : 1) * sizeof(unsigned) + kBins * sizeof(unsigned);
+  const size_t classic = (size_t)kBins * (size_t)(ntiles > 0 ? ntiles : 1) * sizeof(unsigned) + kBins * sizeof(unsigned);
+  const size_t single = onesweep_temp_bytes(n);
+  return classic > single ? classic : single;
 }
 
 cudaError_t radix_sort_pairs(uint64_t *keys, uint32_t *vals, uint64_t *keys_alt, uint32_t *vals_alt, int n,
@@ -225,16 +389,41 @@ cudaError_t radix_sort_pairs(uint64_t *keys, uint32_t *vals, uint64_t *keys_alt,
 }
 
 cudaError_t radix_sort_packed(uint64_t *words, uint64_t *words_alt, int n, int begin_bit, uint64_t *keys_out,
-                              uint32_t *vals_out, void *temp, cudaStream_t s) {
+                              uint32_t *vals_out, void *temp, DevStatus *st, cudaStream_t s) {
   if (begin_bit < 32 || begin_bit >= 64 || n < 2) return cudaErrorInvalidValue;
   const int passes = (64 - begin_bit + 7) / 8;
   const int ntiles = (n + kTile - 1) / kTile;
+  uint64_t *ka = words, *kb = words_alt;
+  if (n < (1 << 30) && st) {
+    // single pass per digit: counts up to 2^30 - 1 fit a status word
+    unsigned *hist = static_cast<unsigned *>(temp);
+    unsigned *ctr = hist + kMaxPasses * kBins;
+    unsigned *status = ctr + kMaxPasses;
+    const size_t zero = ((size_t)kMaxPasses * kBins + kMaxPasses + (size_t)passes * ntiles * kBins) * sizeof(unsigned);
+    cudaError_t e = cudaMemsetAsync(temp, 0, zero, s);
+    if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(k_onesweep, cudaFuncAttributeMaxDynamicSharedMemorySize, kStagePackedBytes);
+    if (e != cudaSuccess) return e;
+    const int hblocks = ntiles < 152 * 4 ? ntiles : 152 * 4;
+    k_hist_all<<<hblocks, kThreads, 0, s>>>(ka, n, begin_bit, passes, hist);
+    ::t2d::g_launches.fetch_add(1, std::memory_order_relaxed);
+    for (int p = 0; p < passes; p++) {
+      const bool last = p == passes - 1;
+      k_onesweep<<<ntiles, kThreads, kStagePackedBytes, s>>>(
+          ka, last ? keys_out : kb, last ? vals_out : nullptr, n, begin_bit + 8 * p, hist + p * kBins,
+          status + (size_t)p * ntiles * kBins, ctr + p, ntiles, last ? 1 : 0, kLookbackLimit, st);
+      ::t2d::g_launches.fetch_add(1, std::memory_order_relaxed);
+      uint64_t *t = ka;
+      ka = kb;
+      kb = t;
+    }
+    return cudaGetLastError();
+  }
   unsigned *counts = static_cast<unsigned *>(temp);
   unsigned *totals = counts + (size_t)kBins * ntiles;
   cudaError_t e = cudaFuncSetAttribute(k_downsweep<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        kStagePackedBytes);
   if (e != cudaSuccess) return e;
-  uint64_t *ka = words, *kb = words_alt;
   for (int p = 0; p < passes; p++) {
     const int shift = begin_bit + 8 * p;
     const bool last = p == passes - 1;

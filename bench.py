@@ -57,7 +57,9 @@ def parse():
     ap.add_argument("--cuda-core-m2l", action="store_true", help="mixed form: M2L on CUDA cores")
     ap.add_argument("--no-plain", action="store_true", help="skip timing the plain FP64 path beside")
     ap.add_argument("--eval-variant", type=int, default=-1,
-                    help="mixed/learned: force a near-field kernel variant 0..3 (default: the tuner's choice)")
+                    help="mixed/learned: force a near-field kernel variant 0..4 (default: the tuner's choice)")
+    ap.add_argument("--level-chain", action="store_true",
+                    help="mixed/learned: one cooperative launch per M2M / L2L chain instead of one launch per level")
     ap.add_argument("--workload", default="two_patch_sheet",
                     choices=["two_patch_sheet", "lamb_oseen", "uniform", "batch_sets", "advected"])
     ap.add_argument("--no-extras", action="store_true",
@@ -365,6 +367,7 @@ def run_ours(args):
     P.set_mixed_params(args.pterms, args.cutoff, not args.cuda_core_m2l)
     P.set_mixed_leaf(args.leaf_blobs)
     P.set_tuning(args.eval_variant < 0, args.eval_variant)
+    P.set_level_chain(args.level_chain)
     learned_note = None
     if args.mode == "learned":
         L = importlib.import_module("2dfmm_gb300.learn")
@@ -473,7 +476,7 @@ def run_ours(args):
                        "l2": "flushed between steps (256 MiB write); inputs 134 MB > L2"},
             "gpu_launches": int(sum(s["n_launches"] for s in sts)),
             "tuned": {"eval_variant": int(st["eval_variant"]),
-                      "variants": "0/1 global loads, 2/3 bulk-copy staging; 4/8 warps per block"},
+                      "variants": "0/1 global loads, 2/3/4 bulk-copy staging; 4/8/4 warps per block (4: 80 registers, unroll 4)"},
             "learned_active": bool(st["learned_active"]),
             "k_list_per_leaf": st["n_list_k"] / max(1, st["n_leaves"]),
             "k_list_blobs_per_leaf": st["n_list_k_blobs"] / max(1, st["n_leaves"]),
@@ -537,6 +540,7 @@ def run_batch(args):
     P.set_mode(MODES["mixed"])
     P.set_mixed_params(args.pterms, args.cutoff, not args.cuda_core_m2l)
     P.set_tuning(args.eval_variant < 0, args.eval_variant)
+    P.set_level_chain(args.level_chain)
     off = np.concatenate([[0], np.cumsum([b.n for b in sets])]).astype(np.int32)
     n = int(off[-1])
     h_xy = np.concatenate([b.xy for b in sets])
@@ -640,7 +644,7 @@ def run_batch(args):
                        "l2": "flushed between steps (256 MiB write)"},
             "gpu_launches": int(sum(x["n_launches"] for x in sts)),
             "tuned": {"eval_variant": int(st["eval_variant"]),
-                      "variants": "0/1 global loads, 2/3 bulk-copy staging; 4/8 warps per block"},
+                      "variants": "0/1 global loads, 2/3/4 bulk-copy staging; 4/8/4 warps per block (4: 80 registers, unroll 4)"},
             "e2e": {"value": world * n / e2e_t, "unit": UNIT, "h2d_bytes_per_step": n * 32,
                     "d2h_bytes_per_step": n * 16, "api": "host->device copies + tree2d_solve_sets + device->host"},
             "roofline": {"bound": "fp32", "achieved": flops / (ms_eval * 1e-3) / 1e12, "peak": peak,

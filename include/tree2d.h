@@ -92,9 +92,9 @@ int tree2d_set_mixed_params(int pterms, double cutoff_sigmas, int use_tensor_cor
 
 /* Most blobs per leaf of the tree the mixed and learned forms build (the
  * plain form always uses the parameters' num_p - 1, as the reference does):
- * -1 (the default) chooses by the blobs per set: 64 below 524,288, 96 below
- * 2,097,152, 128 above (a batched solve uses its mean set size); 0 uses
- * num_p - 1; 1..65535 fixes it. */
+ * -1 (the default) chooses by the blobs per set: 96 below 2,097,152, 128
+ * above (a batched solve uses its mean set size); 0 uses num_p - 1;
+ * 1..65535 fixes it. */
 int tree2d_set_mixed_leaf(int max_blobs);
 
 /* Evaluates n targets (xy interleaved, host memory) into uv (interleaved,
@@ -188,11 +188,23 @@ int tree2d_direct_device(int ntgt, const double *d_txy, int nsrc, const double *
 
 /* Near-field kernel tuning of the mixed/learned forms.  The variants give
  * bit-identical results and differ only in speed: source blobs read from
- * global memory or staged in shared memory by bulk copies, 4 or 8 warps
- * per block.  autotune = 1 (default): the first solve of each (device,
- * form, P, leaf-count class) times every variant with CUDA events and keeps
- * the fastest; eval_variant >= 0 forces one (0..3); eval_variant = -1 with
- * autotune = 0 runs variant 0.  No counterpart in the reference. */
+ * global memory (0: 4 warps per block, 1: 8) or staged in shared memory by
+ * bulk copies (2: 4 warps, 3: 8, 4: 4 warps with more registers per thread,
+ * fewer resident warps and a deeper unrolled pair loop).  autotune = 1
+ * (default): the first solve of each (device, form, P, leaf-count class)
+ * times every variant with CUDA events and keeps the fastest;
+ * eval_variant >= 0 forces one (0 .. TREE2D_EVAL_VARIANTS - 1);
+ * eval_variant = -1 with autotune = 0 runs variant 0.  No counterpart in
+ * the reference. */
+#define TREE2D_EVAL_VARIANTS 5
+
+/* Mixed/learned forms with P = 16: on = 1 runs the M2M levels and the L2L
+ * levels as one cooperative launch each, persistent blocks meeting at a
+ * grid barrier between levels (bounded waits); on = 0 (default) launches
+ * one kernel per level, which measured faster on GB300 (the barriers cost
+ * more than the launches they save).  Results are the same either way.  No
+ * counterpart in the reference. */
+int tree2d_set_level_chain(int on);
 int tree2d_set_tuning(int autotune, int eval_variant);
 
 /* Batched solve of nsets independent blob sets in one tree: set k is blobs

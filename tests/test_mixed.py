@@ -107,7 +107,7 @@ def test_near_field_variants_bit_identical(gpu_lib, mode):
     cor = torch.from_numpy(b.cor).to(dev)
     outs = []
     try:
-        for v in range(4):
+        for v in range(P.EVAL_VARIANTS):
             P.set_tuning(False, v)
             uv = torch.empty_like(xy)
             P.solve_device(xy.data_ptr(), cir.data_ptr(), cor.data_ptr(), uv.data_ptr(), b.n)
@@ -122,10 +122,52 @@ def test_near_field_variants_bit_identical(gpu_lib, mode):
             P.solve_device(xy.data_ptr(), cir.data_ptr(), cor.data_ptr(), uv.data_ptr(), b.n)
             torch.cuda.synchronize()
             assert np.array_equal(uv.cpu().numpy(), outs[0][0])
-            assert 0 <= P.stats()["eval_variant"] <= 3 and P.stats()["n_pairs"] == outs[0][1]
+            assert 0 <= P.stats()["eval_variant"] < P.EVAL_VARIANTS and P.stats()["n_pairs"] == outs[0][1]
     finally:
         P.set_tuning(True, -1)
         P.set_mode(P.MODE_PLAIN)
+
+
+@pytest.mark.gpu
+def test_level_chain_equals_per_level_launches(gpu_lib):
+    """The M2M and L2L levels run as one cooperative launch each (persistent
+    blocks, a grid barrier between levels) or as one launch per level: the
+    same arithmetic in the same order, so the velocities agree bit for bit,
+    for one set and for a batch of sets (whose chains start below the set
+    roots)."""
+    torch = pytest.importorskip("torch")
+    import importlib
+    P = gpu_lib
+    W = importlib.import_module("2dfmm_gb300.workloads")
+    dev = torch.device("cuda:0")
+    b = W.lamb_oseen(262_144, seed=9)
+    P.set_params(b.nterms, b.num_p, b.theta)
+    P.set_mixed_params(16, 2.5, True)
+    P.set_mode(P.MODE_MIXED)
+    xy = torch.from_numpy(b.xy).to(dev)
+    cir = torch.from_numpy(b.cir).to(dev)
+    cor = torch.from_numpy(b.cor).to(dev)
+    sets = W.batch_sets(nsets=24, seed=5, lo=2048, hi=20_000)
+    sxy = torch.from_numpy(np.concatenate([s.xy for s in sets])).to(dev)
+    scir = torch.from_numpy(np.concatenate([s.cir for s in sets])).to(dev)
+    scor = torch.from_numpy(np.concatenate([s.cor for s in sets])).to(dev)
+    offs = np.concatenate([[0], np.cumsum([s.n for s in sets])]).astype(np.int32)
+    outs = []
+    try:
+        for chain in (True, False):
+            P.set_level_chain(chain)
+            uv = torch.empty_like(xy)
+            P.solve_device(xy.data_ptr(), cir.data_ptr(), cor.data_ptr(), uv.data_ptr(), b.n)
+            suv = torch.empty_like(sxy)
+            P.solve_sets(sxy.data_ptr(), scir.data_ptr(), scor.data_ptr(), suv.data_ptr(), offs)
+            torch.cuda.synchronize()
+            outs.append((uv.cpu().numpy(), suv.cpu().numpy()))
+    finally:
+        P.set_level_chain(False)
+        P.set_mode(P.MODE_PLAIN)
+    assert np.all(np.isfinite(outs[0][0])) and np.all(np.isfinite(outs[0][1]))
+    assert np.array_equal(outs[0][0], outs[1][0])
+    assert np.array_equal(outs[0][1], outs[1][1])
 
 
 @pytest.mark.gpu
@@ -201,15 +243,15 @@ def test_repeated_solves_bit_identical(gpu_lib, mode):
 
 @pytest.mark.gpu
 def test_mixed_leaf_size_rule_and_override(gpu_lib):
-    """The mixed forms build their own leaf size (64 blobs for sets below
-    524,288 by default, or the one set), the plain form the parameters'
+    """The mixed forms build their own leaf size (96 blobs for sets below
+    2,097,152 by default, or the one set), the plain form the parameters'
     num_p - 1; every choice keeps relL2 <= 1e-6."""
     torch = pytest.importorskip("torch")
     P = gpu_lib
     W = workloads()
     b = W.uniform(20_000, seed=3)  # num_p 33
     try:
-        for leaf, want in ((-1, 64), (0, 32), (100, 100)):
+        for leaf, want in ((-1, 96), (0, 32), (100, 100)):
             P.set_mixed_leaf(leaf)
             rel, _ = solve_and_measure(P, torch, b)
             st = P.stats()
