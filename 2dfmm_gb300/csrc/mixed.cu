@@ -1530,6 +1530,30 @@ __device__ __forceinline__ void chunk_mask(const MixedView &m, int A, float ox, 
   m1 = kPacks == 2 ? __ballot_sync(0xffffffffu, keep[1]) : m0;
 }
 
+// The persistent near-field warps take target leaves in the order of
+// m.leaf_order.  Leaves differ in work by two orders of magnitude (the
+// dense patch centres against the sheet), and a heavy leaf taken last
+// keeps one warp busy while the rest of the GPU idles, so the schedule is
+// longest first: k_leaf_cost keys each leaf by its estimated pairs
+// (targets x the blobs of its U and K entries) on a half-octave scale, and
+// one stable radix pass orders the keys (ties by leaf ordinal).  The order
+// changes only which warp evaluates a leaf, never a result.
+__global__ void k_leaf_cost(MixedView m, uint64_t *keys, uint32_t *vals) {
+  const int l = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (l >= m.nleaf) return;
+  const int B = m.leaf_cell[l];
+  float src = 0.f;
+  for (int e = m.u_off[l] + lane; e < m.u_off[l + 1]; e += 32) src += (float)(m.end[m.u_idx[e]] - m.begin[m.u_idx[e]]);
+  for (int e = m.k_off[l] + lane; e < m.k_off[l + 1]; e += 32) src += (float)(m.end[m.k_idx[e]] - m.begin[m.k_idx[e]]);
+  for (int o = 16; o; o >>= 1) src += __shfl_xor_sync(0xffffffffu, src, o);
+  if (lane == 0) {
+    const float work = src * (float)(m.end[B] - m.begin[B]) + 1.f;
+    const int b = min(max((int)(2.f * __log2f(work)), 0), 127);  // half octaves, 2^63 at most
+    keys[l] = (uint64_t)(255 - b) << 56;  // ascending key = descending work
+    vals[l] = (uint32_t)l;
+  }
+}
+
 // Near field of every leaf: one warp per target leaf.  The leaf's targets
 // are taken in chunks of 128, 64 or 32 (4, 2 or 1 per lane, packed in
 // twos: a leaf of 97-128 blobs walks its source lists once with four
@@ -1803,8 +1827,8 @@ __global__ void __launch_bounds__(32 * kWarps, (kWide ? 24 : 32) / kWarps) k_eva
   __shared__ __align__(16) float4 s_acc[kWarps][4 * 32];
   __shared__ WarpCounts s_cnt[kWarps];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  int l = next_leaf(m.st, lane);
-  if (l >= m.nleaf) return;  // uniform over the warp; nothing below syncs the block
+  int i = next_leaf(m.st, lane);
+  if (i >= m.nleaf) return;  // uniform over the warp; nothing below syncs the block
   NearWarp w{s_src + (kStaged ? warp * 2 * kStage : 0), s_bar[warp], s_tb[warp], s_acc[warp], &s_cnt[warp], 0u, 0u,
              true};
   if (kStaged && lane == 0) {
@@ -1814,7 +1838,8 @@ __global__ void __launch_bounds__(32 * kWarps, (kWide ? 24 : 32) / kWarps) k_eva
   }
   if (lane == 0) *w.cnts = WarpCounts{};
   __syncwarp();
-  for (; l < m.nleaf; l = next_leaf(m.st, lane)) {
+  for (; i < m.nleaf; i = next_leaf(m.st, lane)) {
+    const int l = m.leaf_order ? m.leaf_order[i] : i;
     const int B = m.leaf_cell[l];
     for (int t0 = m.begin[B]; t0 < m.end[B];) {
       const int rem = m.end[B] - t0;
@@ -2377,6 +2402,9 @@ int mixed_solve(Workspace &ws, const Tree &t, const MixedParams &mp, double *d_u
   if (one_walk) need += Arena::bytes_for((size_t)nl * cap, 4);
   need += Arena::bytes_for((size_t)nc * 2 * P, 4) * 2;
   need += Arena::bytes_for((size_t)nc * 4, 4) + 1024;  // class lists + counts
+  // near-field schedule: keys, values and their sort buffers
+  need += 2 * Arena::bytes_for((size_t)nl, 8) + 2 * Arena::bytes_for((size_t)nl, 4) +
+          Arena::bytes_for(radix_sort_temp_bytes(nl), 1);
   need += 256;
   T2D_CUDA_TRY(ws.mx_arena.reserve(need));
   ws.mx_arena.reset();
@@ -2429,6 +2457,10 @@ int mixed_solve(Workspace &ws, const Tree &t, const MixedParams &mp, double *d_u
   m.level_off = ws.mx_arena.take<int>(2 * kKeyLevels + 4);
   m.M = ws.mx_arena.take<float>((size_t)nc * 2 * P);
   m.L = ws.mx_arena.take<float>((size_t)nc * 2 * P);
+  uint64_t *ord_keys = ws.mx_arena.take<uint64_t>((size_t)nl), *ord_keys2 = ws.mx_arena.take<uint64_t>((size_t)nl);
+  uint32_t *ord_vals = ws.mx_arena.take<uint32_t>((size_t)nl), *ord_vals2 = ws.mx_arena.take<uint32_t>((size_t)nl);
+  void *ord_tmp = ws.mx_arena.take<char>(radix_sort_temp_bytes(nl));
+  m.leaf_order = nullptr;
   unsigned *rc_bits = ws.mx_arena.take<unsigned>(1);
   unsigned *rc_set_bits = t.nsets > 1 ? ws.mx_arena.take<unsigned>((size_t)t.nsets) : nullptr;
   int *cls_list = ws.mx_arena.take<int>((size_t)nc * 4);
@@ -2492,6 +2524,15 @@ int mixed_solve(Workspace &ws, const Tree &t, const MixedParams &mp, double *d_u
   m.k_leaf = ws.mx_lists.take<int>((size_t)tot[2] + 1);
   rc = mixed_fill_lists(m, from_scratch, s);
   if (rc) return rc;
+  // the near field's largest-first schedule, on the second stream beside
+  // the expansions (joined before the near field)
+  if (nl > 1) m.leaf_order = reinterpret_cast<const int *>(ord_vals);
+  auto schedule = [&](cudaStream_t q) -> cudaError_t {
+    if (nl <= 1) return cudaSuccess;
+    k_leaf_cost<<<(int)(((long)nl * 32 + 255) / 256), 256, 0, q>>>(m, ord_keys, ord_vals);
+    g_launches.fetch_add(1, std::memory_order_relaxed);
+    return radix_sort_pairs(ord_keys, ord_vals, ord_keys2, ord_vals2, nl, 56, 64, ord_tmp, q);
+  };
   // keep the view for sampling (training data)
   if (!ws.mxv) ws.mxv = new MixedView();
   *ws.mxv = m;
@@ -2571,7 +2612,14 @@ int mixed_solve(Workspace &ws, const Tree &t, const MixedParams &mp, double *d_u
       rc = learned_decide(m, stats, uref, wimg, bias, mp.lp->direct_bias, tot[0], tot[2], u_dec, k_dec, s2);
       if (rc) return drain(rc);
     }
+    T2D_TRY_DRAIN(schedule(s2));
     T2D_TRY_DRAIN(cudaEventRecord(ws.join_ev, s2));
+  } else {
+    T2D_CUDA_TRY(cudaEventRecord(ws.fork_ev, s));
+    T2D_CUDA_TRY(cudaStreamWaitEvent(ws.side, ws.fork_ev, 0));
+    forked = true;
+    T2D_TRY_DRAIN(schedule(ws.side));
+    T2D_TRY_DRAIN(cudaEventRecord(ws.join_ev, ws.side));
   }
   // Beside the decisions, the expansions run on the highest-priority
   // stream: their chain of short per-level kernels is the critical path,
@@ -2594,8 +2642,8 @@ int mixed_solve(Workspace &ws, const Tree &t, const MixedParams &mp, double *d_u
   if (side) {
     T2D_TRY_DRAIN(cudaEventRecord(ws.hi_join, ws.hi));
     T2D_TRY_DRAIN(cudaStreamWaitEvent(s, ws.hi_join, 0));
-    T2D_TRY_DRAIN(cudaStreamWaitEvent(s, ws.join_ev, 0));
   }
+  T2D_TRY_DRAIN(cudaStreamWaitEvent(s, ws.join_ev, 0));
   T2D_CUDA_TRY(cudaEventRecord(ws.ev[4], s));
   const Decisions dec = learned ? Decisions{u_dec, k_dec, mp.lp->order_margin} : Decisions{nullptr, nullptr, 0};
   rc = near_field(ws, mp, m, learned, dec, d_uv, m.mperm, s, st);

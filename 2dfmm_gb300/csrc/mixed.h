@@ -51,6 +51,7 @@ struct MixedView {
   int *level_off;              // [kKeyLevels + 2]: start of each level in by_level, then cursors
   int *u_idx, *w_idx, *k_idx;
   int *u_leaf, *k_leaf;  // leaf ordinal of each U / K entry
+  const int *leaf_order; // near-field schedule: leaf ordinals by estimated work, largest first
   float *M, *L;          // per cell, 2P floats (re[P], im[P])
   const float2 *m2m, *l2l;  // [4][kMaxP][kMaxP] translation operators
   DevStatus *st;
