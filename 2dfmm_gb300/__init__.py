@@ -33,7 +33,7 @@ EXPORTS = [
     "make_tree", "biot_tree", "tree2d_last_error", "tree2d_error_string", "tree2d_set_params",
     "tree2d_clear_params", "tree2d_get_params", "tree2d_set_mode", "tree2d_get_mode", "tree2d_set_mixed_params", "tree2d_set_mixed_leaf", "biot_tree_batch",
     "tree2d_solve_device", "tree2d_solve_device_static", "tree2d_solve_sets", "tree2d_set_tuning", "tree2d_set_level_chain", "tree2d_get_stats", "tree2d_export_tree", "tree2d_direct_device", "tree2d_fp64_probe", "tree2d_pipe_probe", "tree2d_wait_probe", "tree2d_version",
-    "tree2d_learn_param_count", "tree2d_learn_load", "tree2d_learn_set_weights", "tree2d_learn_set_envelope", "tree2d_learn_get_weights", "tree2d_learn_set_options",
+    "tree2d_learn_param_count", "tree2d_learn_load", "tree2d_learn_set_weights", "tree2d_learn_set_envelope", "tree2d_learn_get_weights", "tree2d_learn_set_options", "tree2d_learn_set_far_orders",
     "tree2d_learn_collect", "tree2d_learn_train", "tree2d_mlp_grad", "tree2d_mlp_forward",
     "tree2d_set_mirror", "tree2d_advect_device",
 ]
@@ -147,8 +147,9 @@ def load(path: str | None = None):
     L.tree2d_advect_device.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_double,
                                        ctypes.c_void_p]
     L.tree2d_advect_device.restype = ctypes.c_int
+    L.tree2d_learn_set_far_orders.argtypes = [ctypes.c_int]
     for f in ("tree2d_learn_set_weights", "tree2d_learn_get_weights", "tree2d_learn_set_options",
-              "tree2d_learn_collect", "tree2d_learn_train", "tree2d_mlp_grad", "tree2d_mlp_forward"):
+              "tree2d_learn_set_far_orders", "tree2d_learn_collect", "tree2d_learn_train", "tree2d_mlp_grad", "tree2d_mlp_forward"):
         getattr(L, f).restype = ctypes.c_int
     _lib = L
     return L
@@ -371,6 +372,12 @@ def learn_get_weights():
 
 def learn_set_options(direct_bias: float = 1.0, order_margin: int = 1, budget: float = 3e-7):
     _check(load().tree2d_learn_set_options(direct_bias, order_margin, budget), "learn_set_options")
+
+
+def learn_set_far_orders(on: bool = False):
+    """Learned form: the network also sets each W-list M2P's order (leaf
+    sources), or (off) they all keep the full order."""
+    _check(load().tree2d_learn_set_far_orders(int(on)), "learn_set_far_orders")
 
 
 def learn_set_envelope(k_blobs_per_leaf_max: float, cutoff_sigmas: float = 0.0):

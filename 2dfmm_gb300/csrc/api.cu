@@ -1027,6 +1027,13 @@ int tree2d_learn_set_options(float direct_bias, int order_margin, double budget)
   return TREE2D_OK;
 }
 
+int tree2d_learn_set_far_orders(int on) {
+  Lib &L = lib();
+  std::lock_guard<std::mutex> lk(L.mu);
+  L.lp->far_orders = on ? 1 : 0;
+  return TREE2D_OK;
+}
+
 int tree2d_learn_set_envelope(double k_blobs_per_leaf_max, double cutoff_sigmas) {
   Lib &L = lib();
   std::lock_guard<std::mutex> lk(L.mu);

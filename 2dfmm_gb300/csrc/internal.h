@@ -86,6 +86,7 @@ struct DevStatus {
   unsigned eval_next;      // mixed: next target leaf of the persistent near-field warps
   unsigned bar_count;      // mixed: arrivals at the level chain's grid barrier (zeroed before a launch)
   unsigned bar_gen;        // mixed: generation of that barrier
+  int nonuniform;          // mixed: some leaf's blobs have different core radii
 };
 
 // Bump allocator over one device allocation.  Buffers are 256-byte aligned.

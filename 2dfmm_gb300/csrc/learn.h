@@ -27,6 +27,7 @@ struct LearnedParams {
   double budget = 3e-7;      // label budget: per-interaction error / (sum|G| / R0)
   double k_blobs_max = 0;    // training envelope: mean source blobs of the K leaves per leaf; 0 = none
   double cutoff_train = 0;   // correction radius (units of max sigma) the envelope was counted at; 0 = the one in force
+  int far_orders = 0;        // the network also sets the order of each W-list M2P (leaf sources)
 };
 
 // Per-leaf source statistics for the features.
@@ -76,12 +77,16 @@ __device__ __forceinline__ void interaction_features(const MixedView &m, const L
 int learned_leaf_stats(MixedView &m, LeafStats *stats, cudaStream_t s);
 int learned_uref(MixedView &m, const LeafStats *stats, const RootBox *root, float *out, cudaStream_t s);
 
-// Decisions (class per list entry) for all U and K entries of every leaf,
-// by the tensor-core network (learn_tc.cu).  `wimg` holds the BF16 weights
-// in the kernel's operand layout (learn_weight_images).
+// Decisions (class per list entry) for all U, K and (w_dec non-null) W
+// entries of every leaf, by the tensor-core network (learn_tc.cu).  A W
+// entry is presented as a U entry (an M2P of its source into the target
+// leaf); its class c >= 1 sets that M2P's order as for a U entry, class 0
+// keeps the full order, and so does every W entry whose source is not a
+// leaf (the source statistics are per leaf).  `wimg` holds the BF16
+// weights in the kernel's operand layout (learn_weight_images).
 int learned_decide(MixedView &m, const LeafStats *stats, const float *u_ref_ptr, const uint16_t *wimg,
-                   const float *bias, float direct_bias, long n_u, long n_k, unsigned char *u_dec,
-                   unsigned char *k_dec, cudaStream_t s);
+                   const float *bias, float direct_bias, long n_u, long n_k, long n_w, unsigned char *u_dec,
+                   unsigned char *k_dec, unsigned char *w_dec, cudaStream_t s);
 void learn_weight_images(const float *theta, std::vector<uint16_t> &img, std::vector<float> &bias);
 size_t learn_weight_image_elems();
 

@@ -34,8 +34,8 @@ struct InferArgs {
   const uint16_t *wimg;
   const float *bias;  // b1[64] b2[64] b3[64] b4[16]
   float direct_bias;
-  long n_u, n_k;
-  unsigned char *u_dec, *k_dec;
+  long n_u, n_k, n_w;
+  unsigned char *u_dec, *k_dec, *w_dec;
   const float *X;  // checking path: explicit features [nx][16]
   long nx;
   float *logits;   // checking path output [nx][16]
@@ -96,7 +96,7 @@ __global__ void __launch_bounds__(kTile) k_mlp_infer(InferArgs a) {
   unsigned char *wsm = smem;
   unsigned char *act = smem + kWBytes;
   const int tid = threadIdx.x, warp = tid >> 5;
-  const long total = a.X ? a.nx : a.n_u + a.n_k;
+  const long total = a.X ? a.nx : a.n_u + a.n_k + a.n_w;
   const long ntiles = (total + kTile - 1) / kTile;
   if ((long)blockIdx.x >= ntiles) return;
 
@@ -147,12 +147,15 @@ __global__ void __launch_bounds__(kTile) k_mlp_infer(InferArgs a) {
     } else if (a.X) {
       for (int k = 0; k < kMlpIn; k++) v[k] = a.X[gi * kMlpIn + k];
     } else {
-      kind = gi < a.n_u ? 0 : 1;
-      e = kind == 0 ? gi : gi - a.n_u;
-      const int l = (kind == 0 ? m.u_leaf : m.k_leaf)[e];
+      // U entries, then K entries, then W entries (kind 2), whose source
+      // cell's multipole the network sees as a U entry's: an M2P at order p
+      // into the target leaf, with the same per-interaction error budget
+      kind = gi < a.n_u ? 0 : (gi < a.n_u + a.n_k ? 1 : 2);
+      e = kind == 0 ? gi : (kind == 1 ? gi - a.n_u : gi - a.n_u - a.n_k);
+      const int l = (kind == 0 ? m.u_leaf : (kind == 1 ? m.k_leaf : m.w_leaf))[e];
       const int B = m.leaf_cell[l];
-      const int A = kind == 0 ? m.u_idx[e] : m.k_idx[e];
-      interaction_features(m, a.st, B, A, kind, u_ref, v);
+      const int A = kind == 0 ? m.u_idx[e] : (kind == 1 ? m.k_idx[e] : m.w_idx[e]);
+      interaction_features(m, a.st, B, A, kind == 1 ? 1 : 0, u_ref, v);
     }
     store_row(act, tid, v, 16);
     // layer 1 .. 4
@@ -223,7 +226,8 @@ __global__ void __launch_bounds__(kTile) k_mlp_infer(InferArgs a) {
         int best = 0;
         for (int c = 1; c < kMlpClasses; c++)
           if (v[c] > v[best]) best = c;
-        (kind == 0 ? a.u_dec : a.k_dec)[e] = (unsigned char)best;
+        if (kind == 2 && !m.leaf[m.w_idx[e]]) best = 0;  // statistics exist for leaf sources only: full order
+        (kind == 0 ? a.u_dec : (kind == 1 ? a.k_dec : a.w_dec))[e] = (unsigned char)best;
       }
     }
   }
@@ -295,8 +299,8 @@ static int launch_infer(InferArgs &a, long total, cudaStream_t s) {
 }
 
 int learned_decide(MixedView &m, const LeafStats *stats, const float *u_ref_ptr, const uint16_t *wimg,
-                   const float *bias, float direct_bias, long n_u, long n_k, unsigned char *u_dec,
-                   unsigned char *k_dec, cudaStream_t s) {
+                   const float *bias, float direct_bias, long n_u, long n_k, long n_w, unsigned char *u_dec,
+                   unsigned char *k_dec, unsigned char *w_dec, cudaStream_t s) {
   InferArgs a{};
   a.m = m;
   a.st = stats;
@@ -306,9 +310,11 @@ int learned_decide(MixedView &m, const LeafStats *stats, const float *u_ref_ptr,
   a.direct_bias = direct_bias;
   a.n_u = n_u;
   a.n_k = n_k;
+  a.n_w = w_dec ? n_w : 0;
   a.u_dec = u_dec;
   a.k_dec = k_dec;
-  return launch_infer(a, n_u + n_k, s);
+  a.w_dec = w_dec;
+  return launch_infer(a, n_u + n_k + a.n_w, s);
 }
 
 int mlp_forward_tc(int n, const float *X, const uint16_t *wimg, const float *bias, float *logits, DevStatus *st,

@@ -186,14 +186,17 @@ __global__ void __launch_bounds__(32 * kSetupWarps) k_leaf_setup(MixedView m, co
     const int qy = min(max((int)(__fmul_rn(__fadd_rn(lc.y, hs), q)), 0), 7);
     return (int)(spread3((unsigned)qx) | (spread3((unsigned)qy) << 1));
   };
-  // pass 1: blobs per sub-cell
+  // pass 1: blobs per sub-cell, and whether all share the first one's core
   cnt[lane] = 0;
   cnt[lane + 32] = 0;
   __syncwarp();
+  const double cor0 = cor[b];
+  bool same = true;
   for (int i0 = b; i0 < e; i0 += 32) {
     const int i = i0 + lane, o = i - b;
     int code = kSubCells;
     if (i < e) {
+      same = same && cor[i] == cor0;
       const float2 lc = offset_of(i);
       code = code_of(lc);
       if (o < kSetupStage) {
@@ -204,6 +207,14 @@ __global__ void __launch_bounds__(32 * kSetupWarps) k_leaf_setup(MixedView m, co
     const unsigned grp = __match_any_sync(0xffffffffu, code);
     if (code < kSubCells && (grp & lt) == 0) cnt[code] += __popc(grp);  // one leader per sub-cell
     __syncwarp();
+  }
+  const bool uniform = __all_sync(0xffffffffu, same);
+  // s = sqrt(log2 e) / sigma from the FP32 1/sigma^2 the records carry
+  const float sf0 = (float)cor0;
+  const float sc = uniform ? sqrtf(1.44269504f * __frcp_rn(sf0 * sf0)) : 0.f;
+  if (lane == 0) {
+    m.lscale[c] = sc;
+    if (!uniform) m.st->nonuniform = 1;
   }
   // exclusive prefix over the sub-cells (two per lane): the first position of each
   {
@@ -253,6 +264,7 @@ __global__ void __launch_bounds__(32 * kSetupWarps) k_leaf_setup(MixedView m, co
       const float w = __frcp_rn(sf * sf);
       m.s2inv[d] = w;
       m.src4[d] = make_float4(lc.x, lc.y, g, -1.44269504f * w);
+      if (uniform) m.src4s[d] = make_float4(__fmul_rn(lc.x, sc), __fmul_rn(lc.y, sc), __fmul_rn(g, sc), 0.f);
       m.mperm[d] = perm[i];
     }
   }
@@ -554,7 +566,7 @@ __global__ void __launch_bounds__(32 * kWalkWarps) k_lists(MixedView m) {
     base[2] = m.k_off[l];
   }
   int *const dst[3] = {m.u_idx, m.w_idx, m.k_idx};
-  int *const own[3] = {m.u_leaf, nullptr, m.k_leaf};
+  int *const own[3] = {m.u_leaf, m.w_leaf, m.k_leaf};
   int *const row = kMode == 2 ? m.list_scratch + (size_t)l * m.list_cap : nullptr;
   // each lane offers (kind, id), kind -1 = nothing; outputs keep lane order
   auto emit = [&](int kind, int id) {
@@ -669,7 +681,7 @@ __global__ void __launch_bounds__(256) k_lists_compact(MixedView m) {
   const int n = (m.u_off[l + 1] - base[0]) + (m.w_off[l + 1] - base[1]) + (m.k_off[l + 1] - base[2]);
   const int *row = m.list_scratch + (size_t)l * m.list_cap;
   int *const dst[3] = {m.u_idx, m.w_idx, m.k_idx};
-  int *const own[3] = {m.u_leaf, nullptr, m.k_leaf};
+  int *const own[3] = {m.u_leaf, m.w_leaf, m.k_leaf};
   for (int c0 = 0; c0 < n; c0 += 32) {
     const int e = c0 + lane;
     const unsigned enc = e < n ? (unsigned)row[e] : 0u;
@@ -1202,6 +1214,12 @@ __device__ __forceinline__ void kahan(float &s, float &cmp, float v) {
   s = t;
 }
 
+// Order of an M2P the network chose: class c >= 1 is order c + 3 (4..16),
+// raised by the margin, capped at P; class 0 of a W entry keeps P.
+__device__ __forceinline__ int chosen_order(int d, int margin, int P) {
+  return d > 0 ? min(min(class_order(d) + margin, 16), P) : P;
+}
+
 // M2P of source leaf A at order p (terms 0..p-1) at a target offset z from
 // leaf B's centre, added to phi.
 __device__ __forceinline__ void m2p_order(const MixedView &m, int B, int A, int p, float2 z, float2 &phi) {
@@ -1253,7 +1271,8 @@ __device__ __forceinline__ void m2p_order2(const MixedView &m, int B, int A, int
 // of 64 targets), so a leaf of <= 64 blobs walks its source lists once.
 // Sources are read as one float4 {x, y, G, 1/sigma^2} (offsets from their
 // leaf centre), the same address for the whole warp.
-__device__ __forceinline__ void far_field(const MixedView &m, int l, int B, float2 zt, float2 &phi) {
+__device__ __forceinline__ void far_field(const MixedView &m, int l, int B, float2 zt, float2 &phi,
+                                          const unsigned char *wdec = nullptr, int margin = 0) {
   const int P = m.P;
   const float ihB = m.inv_h[B];
   const float *LB = m.L + (size_t)B * 2 * P;
@@ -1266,13 +1285,14 @@ __device__ __forceinline__ void far_field(const MixedView &m, int l, int B, floa
   }
   phi.x = __fmul_rn(acc.x, ihB);
   phi.y = __fmul_rn(acc.y, ihB);
-  for (int e = m.w_off[l]; e < m.w_off[l + 1]; e++) m2p_order(m, B, m.w_idx[e], P, zt, phi);
+  for (int e = m.w_off[l]; e < m.w_off[l + 1]; e++)
+    m2p_order(m, B, m.w_idx[e], wdec ? chosen_order(wdec[e], margin, P) : P, zt, phi);
 }
 
 // far_field for the lane's two targets in packed arithmetic (each target's
 // value is far_field's, bit for bit).
 __device__ __forceinline__ void far_field2(const MixedView &m, int l, int B, float2 za, float2 zb, float2 &pa,
-                                           float2 &pb) {
+                                           float2 &pb, const unsigned char *wdec = nullptr, int margin = 0) {
   const int P = m.P;
   const float ihB = m.inv_h[B];
   const float *LB = m.L + (size_t)B * 2 * P;
@@ -1286,7 +1306,8 @@ __device__ __forceinline__ void far_field2(const MixedView &m, int l, int B, flo
   const float2 px = __fmul2_rn(acc.x, f2(ihB)), py = __fmul2_rn(acc.y, f2(ihB));
   pa = make_float2(px.x, py.x);
   pb = make_float2(px.y, py.y);
-  for (int e = m.w_off[l]; e < m.w_off[l + 1]; e++) m2p_order2(m, B, m.w_idx[e], P, za, zb, pa, pb);
+  for (int e = m.w_off[l]; e < m.w_off[l + 1]; e++)
+    m2p_order2(m, B, m.w_idx[e], wdec ? chosen_order(wdec[e], margin, P) : P, za, zb, pa, pb);
 }
 
 // 2^t on the SFU (PTX ex2.approx: relative error ~2^-22, FTZ).
@@ -1326,17 +1347,27 @@ constexpr float kSer1 = -0.69314718f;  // -ln 2
 constexpr float kSer2 = -0.24022651f;  // -(ln 2)^2 / 2
 constexpr float kSerT = -1.44269504e-3f;  // t at x = 1e-3
 
-template <bool kCorrection>
+// kScaled: the records of a leaf whose blobs share one core radius, held
+// scaled by s = sqrt(log2 e) / sigma, {x s, y s, G s, -} (src4s), with the
+// targets' offsets scaled by the same s: the squared distance is then
+// q = r^2 log2(e) / sigma^2 itself, the Gaussian exp2(-q) needs no product
+// per pair, and G s / q carries the 1 / r^2 (G s / q (y s) = G / r^2 y).
+// One FP32 operation fewer per pair, the same quantities up to rounding.
+template <bool kCorrection, bool kScaled = false>
 __device__ __forceinline__ void pair(const float4 sj, float ntx, float nty, float &a, float &b) {
   const float nrx = __fadd_rn(sj.x, ntx), nry = __fadd_rn(sj.y, nty);
   const float r2 = fmaf(nrx, nrx, fmaf(nry, nry, 1e-30f));
-  const float t = __fmul_rn(r2, sj.w);
-  const float e = sfu_exp2(t);
+  // the Gaussian's exponent, base 2: t = r2 * (-log2(e)/sigma^2), or -q scaled
+  const float t = kScaled ? 0.f : __fmul_rn(r2, sj.w);
+  const float e = sfu_exp2(kScaled ? -r2 : t);
   const float ir2 = sfu_rcp(r2);
   float f;
   if (!kCorrection) {
-    const float ser = __fmul_rn(t, fmaf(kSer2, t, kSer1)), ome = fmaf(-1.f, e, 1.f);
-    f = __fmul_rn(__fmul_rn(sj.z, t > kSerT ? ser : ome), ir2);
+    // x (1 - x/2) = t (-ln2 - (ln2)^2/2 t) = q (ln2 - (ln2)^2/2 q), the same bits
+    const float ser = kScaled ? __fmul_rn(r2, fmaf(kSer2, r2, -kSer1)) : __fmul_rn(t, fmaf(kSer2, t, kSer1));
+    const float ome = fmaf(-1.f, e, 1.f);
+    const bool small = kScaled ? r2 < -kSerT : t > kSerT;
+    f = __fmul_rn(__fmul_rn(sj.z, small ? ser : ome), ir2);
   } else {
     f = __fmul_rn(__fmul_rn(sj.z, e), ir2);
   }
@@ -1348,18 +1379,20 @@ __device__ __forceinline__ void pair(const float4 sj, float ntx, float nty, floa
 // instruction forms both targets' value of every step, with the rounding
 // of the scalar step (each component rounds as the scalar operation does),
 // so a target's sum does not depend on how many targets its lane holds.
-template <bool kCorrection>
+template <bool kCorrection, bool kScaled = false>
 __device__ __forceinline__ void pair2(const float4 sj, float2 ntx, float2 nty, float2 &a, float2 &b) {
   const float2 nrx = __fadd2_rn(f2(sj.x), ntx), nry = __fadd2_rn(f2(sj.y), nty);
   const float2 r2 = __ffma2_rn(nrx, nrx, __ffma2_rn(nry, nry, f2(1e-30f)));
-  const float2 t = __fmul2_rn(r2, f2(sj.w));
-  const float2 e = make_float2(sfu_exp2(t.x), sfu_exp2(t.y));
+  const float2 t = kScaled ? f2(0.f) : __fmul2_rn(r2, f2(sj.w));
+  const float2 e = kScaled ? make_float2(sfu_exp2(-r2.x), sfu_exp2(-r2.y)) : make_float2(sfu_exp2(t.x), sfu_exp2(t.y));
   const float2 ir2 = make_float2(sfu_rcp(r2.x), sfu_rcp(r2.y));
   float2 f;
   if (!kCorrection) {
-    const float2 ser = __fmul2_rn(t, __ffma2_rn(f2(kSer2), t, f2(kSer1)));
+    const float2 ser = kScaled ? __fmul2_rn(r2, __ffma2_rn(f2(kSer2), r2, f2(-kSer1)))
+                               : __fmul2_rn(t, __ffma2_rn(f2(kSer2), t, f2(kSer1)));
     const float2 ome = __ffma2_rn(f2(-1.f), e, f2(1.f));
-    const float2 e1f = make_float2(t.x > kSerT ? ser.x : ome.x, t.y > kSerT ? ser.y : ome.y);
+    const bool sx = kScaled ? r2.x < -kSerT : t.x > kSerT, sy = kScaled ? r2.y < -kSerT : t.y > kSerT;
+    const float2 e1f = make_float2(sx ? ser.x : ome.x, sy ? ser.y : ome.y);
     f = __fmul2_rn(__fmul2_rn(f2(sj.z), e1f), ir2);
   } else {
     f = __fmul2_rn(__fmul2_rn(f2(sj.z), e), ir2);
@@ -1393,34 +1426,36 @@ struct GlobalSrc {
 // negated (see pair).  Each source leaf is summed in plain FP32 and then
 // added with compensation (leaf_add), so the compensated sum costs once per
 // leaf, not once per pair.
-template <bool kCorrection, class S>
+template <bool kCorrection, bool kScaled, class S>
 __device__ __forceinline__ void leaf_pairs1(const S src, int j0, int j1, float ntx, float nty, float &a, float &b) {
 #pragma unroll 4
-  for (int j = j0; j < j1; j++) pair<kCorrection>(src[j], ntx, nty, a, b);
+  for (int j = j0; j < j1; j++) pair<kCorrection, kScaled>(src[j], ntx, nty, a, b);
 }
 
-template <bool kCorrection, int kUnroll, class S>
+template <bool kCorrection, bool kScaled, int kUnroll, class S>
 __device__ __forceinline__ void leaf_pairs2(const S src, int j0, int j1, float2 ntx, float2 nty, float2 &a,
                                             float2 &b) {
 #pragma unroll kUnroll
-  for (int j = j0; j < j1; j++) pair2<kCorrection>(src[j], ntx, nty, a, b);
+  for (int j = j0; j < j1; j++) pair2<kCorrection, kScaled>(src[j], ntx, nty, a, b);
 }
 
-template <bool kCorrection, int kUnroll, class S>
+template <bool kCorrection, bool kScaled, int kUnroll, class S>
 __device__ __forceinline__ void leaf_pairs4(const S src, int j0, int j1, float2 ntx0, float2 nty0, float2 ntx1,
                                             float2 nty1, float2 &a0, float2 &b0, float2 &a1, float2 &b1) {
 #pragma unroll kUnroll
   for (int j = j0; j < j1; j++) {
     const float4 sj = src[j];
-    pair2<kCorrection>(sj, ntx0, nty0, a0, b0);
-    pair2<kCorrection>(sj, ntx1, nty1, a1, b1);
+    pair2<kCorrection, kScaled>(sj, ntx0, nty0, a0, b0);
+    pair2<kCorrection, kScaled>(sj, ntx1, nty1, a1, b1);
   }
 }
 
 struct Decisions {
   const unsigned char *u, *k;  // class per U / K entry; null: all direct
   int margin;
+  const unsigned char *w;      // class per W entry (order of its M2P); null: all at the full order
 };
+
 
 // Persistent near-field warps: the grid holds as many warps as fit on the
 // GPU at once, and each warp takes the next target leaf from a counter
@@ -1599,7 +1634,7 @@ __device__ __forceinline__ void leaf_add(float4 *acc, int k, int lane, bool corr
 // and k = 2, 3), each pack with its own bounding box for the correction
 // cull.  The tree's in-leaf order is spatial (k_leaf_setup), so a pack of
 // 64 consecutive targets is compact.
-template <bool kLearned, bool kStaged, int kT, int kUnroll>
+template <bool kLearned, bool kStaged, int kT, int kUnroll, bool kScaled>
 __device__ __forceinline__ void near_chunk(const MixedView &m, const Decisions &dec, double *uv, const int *perm,
                                            long wait_limit, int l, int B, int t0, int lane, NearWarp &w) {
   constexpr int kPacks = kT == 4 ? 2 : 1;
@@ -1678,7 +1713,7 @@ __device__ __forceinline__ void near_chunk(const MixedView &m, const Decisions &
     if (lane == 0) {
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       mbar_expect_tx(&w.bar[b], (uint32_t)cnt * 16u);
-      bulk_g2s(w.src + b * kStage, m.src4 + j0, (uint32_t)cnt * 16u, &w.bar[b]);
+      bulk_g2s(w.src + b * kStage, (kScaled ? m.src4s : m.src4) + j0, (uint32_t)cnt * 16u, &w.bar[b]);
     }
     w.inflight |= 1u << b;
     return true;
@@ -1708,13 +1743,15 @@ __device__ __forceinline__ void near_chunk(const MixedView &m, const Decisions &
       }
     }
     const bool corr = q >= nu;
-    // the targets' offsets from A's centre, negated (see pair)
+    // the targets' offsets from A's centre, negated (see pair), and scaled
+    // by A's s with scaled records
+    const float sA = kScaled ? m.lscale[A] : 1.f;
     float ntx[kT], nty[kT], sa[kT], sb[kT];
 #pragma unroll
     for (int k = 0; k < kT; k++) {
       const float2 zk = zof(k);
-      ntx[k] = -__fadd_rn(zk.x, ox);
-      nty[k] = -__fadd_rn(zk.y, oy);
+      ntx[k] = kScaled ? __fmul_rn(-__fadd_rn(zk.x, ox), sA) : -__fadd_rn(zk.x, ox);
+      nty[k] = kScaled ? __fmul_rn(-__fadd_rn(zk.y, oy), sA) : -__fadd_rn(zk.y, oy);
       sa[k] = 0.f;
       sb[k] = 0.f;
     }
@@ -1726,9 +1763,9 @@ __device__ __forceinline__ void near_chunk(const MixedView &m, const Decisions &
       done += (unsigned)(s1 - s0) * ((packs & 1 ? vp0 : 0u) + (packs & 2 ? vp1 : 0u));
       if (kT == 1) {
         if (!corr)
-          leaf_pairs1<false>(src, s0, s1, ntx[0], nty[0], sa[0], sb[0]);
+          leaf_pairs1<false, kScaled>(src, s0, s1, ntx[0], nty[0], sa[0], sb[0]);
         else
-          leaf_pairs1<true>(src, s0, s1, ntx[0], nty[0], sa[0], sb[0]);
+          leaf_pairs1<true, kScaled>(src, s0, s1, ntx[0], nty[0], sa[0], sb[0]);
       } else if (kT == 2 || packs != 3) {
         // one pack: slots 0, 1, or in a four-slot chunk 2, 3 when the run is
         // pack 1's alone (constant indices keep the slots in registers)
@@ -1737,9 +1774,9 @@ __device__ __forceinline__ void near_chunk(const MixedView &m, const Decisions &
           const float2 tx = make_float2(ntx[k], ntx[k + 1]), ty = make_float2(nty[k], nty[k + 1]);
           float2 a = make_float2(sa[k], sa[k + 1]), b = make_float2(sb[k], sb[k + 1]);
           if (!corr)
-            leaf_pairs2<false, kUnroll>(src, s0, s1, tx, ty, a, b);
+            leaf_pairs2<false, kScaled, kUnroll>(src, s0, s1, tx, ty, a, b);
           else
-            leaf_pairs2<true, kUnroll>(src, s0, s1, tx, ty, a, b);
+            leaf_pairs2<true, kScaled, kUnroll>(src, s0, s1, tx, ty, a, b);
           sa[k] = a.x, sa[k + 1] = a.y, sb[k] = b.x, sb[k + 1] = b.y;
         };
         if (kT == 4 && packs == 2)
@@ -1752,9 +1789,9 @@ __device__ __forceinline__ void near_chunk(const MixedView &m, const Decisions &
         float2 a0 = make_float2(sa[0], sa[1]), b0 = make_float2(sb[0], sb[1]);
         float2 a1 = make_float2(sa[kT - 2], sa[kT - 1]), b1 = make_float2(sb[kT - 2], sb[kT - 1]);
         if (!corr)
-          leaf_pairs4<false, kUnroll>(src, s0, s1, tx0, ty0, tx1, ty1, a0, b0, a1, b1);
+          leaf_pairs4<false, kScaled, kUnroll>(src, s0, s1, tx0, ty0, tx1, ty1, a0, b0, a1, b1);
         else
-          leaf_pairs4<true, kUnroll>(src, s0, s1, tx0, ty0, tx1, ty1, a0, b0, a1, b1);
+          leaf_pairs4<true, kScaled, kUnroll>(src, s0, s1, tx0, ty0, tx1, ty1, a0, b0, a1, b1);
         sa[0] = a0.x, sa[1] = a0.y, sb[0] = b0.x, sb[1] = b0.y;
         sa[kT - 2] = a1.x, sa[kT - 1] = a1.y, sb[kT - 2] = b1.x, sb[kT - 1] = b1.y;
       }
@@ -1763,7 +1800,7 @@ __device__ __forceinline__ void near_chunk(const MixedView &m, const Decisions &
     if (use_smem)
       runs(SmemSrc{smem_u32(w.src + buf * kStage)});
     else
-      runs(GlobalSrc{m.src4 + j0});
+      runs(GlobalSrc{(kScaled ? m.src4s : m.src4) + j0});
 #pragma unroll
     for (int k = 0; k < kT; k++) leaf_add(w.acc, k, lane, corr, sa[k], sb[k]);
     counts_add(w.cnts, lane, done, corr ? done : 0u, corr ? (unsigned)cnt * nt : 0u);
@@ -1779,11 +1816,13 @@ __device__ __forceinline__ void near_chunk(const MixedView &m, const Decisions &
   float2 phi[kT], z[kT];
 #pragma unroll
   for (int k = 0; k < kT; k++) z[k] = zof(k);
+  const unsigned char *wdec = kLearned ? dec.w : nullptr;
   if (kT == 1) {
-    far_field(m, l, B, z[0], phi[0]);
+    far_field(m, l, B, z[0], phi[0], wdec, dec.margin);
   } else {
 #pragma unroll
-    for (int k = 0; k < kT; k += 2) far_field2(m, l, B, z[k], z[(k + 1) % kT], phi[k], phi[(k + 1) % kT]);
+    for (int k = 0; k < kT; k += 2)
+      far_field2(m, l, B, z[k], z[(k + 1) % kT], phi[k], phi[(k + 1) % kT], wdec, dec.margin);
   }
   if (kLearned) {
     for (int e = u0; e < u0 + nu; e++) {
@@ -1818,7 +1857,7 @@ __device__ __forceinline__ void near_chunk(const MixedView &m, const Decisions &
   __syncwarp();
 }
 
-template <bool kLearned, bool kStaged, int kWarps, bool kWide>
+template <bool kLearned, bool kStaged, int kWarps, bool kWide, bool kScaled>
 __global__ void __launch_bounds__(32 * kWarps, (kWide ? 24 : 32) / kWarps) k_eval_near(MixedView m, double *uv, const int *perm,
                                                                          Decisions dec, long wait_limit) {
   extern __shared__ __align__(128) float4 s_src[];  // kStaged: [kWarps][2 * kStage]
@@ -1844,13 +1883,13 @@ __global__ void __launch_bounds__(32 * kWarps, (kWide ? 24 : 32) / kWarps) k_eva
     for (int t0 = m.begin[B]; t0 < m.end[B];) {
       const int rem = m.end[B] - t0;
       if (rem > 96) {
-        near_chunk<kLearned, kStaged, 4, kWide ? 4 : 2>(m, dec, uv, perm, wait_limit, l, B, t0, lane, w);
+        near_chunk<kLearned, kStaged, 4, kWide ? 4 : 2, kScaled>(m, dec, uv, perm, wait_limit, l, B, t0, lane, w);
         t0 += 128;
       } else if (rem > 32) {
-        near_chunk<kLearned, kStaged, 2, kWide ? 4 : 2>(m, dec, uv, perm, wait_limit, l, B, t0, lane, w);
+        near_chunk<kLearned, kStaged, 2, kWide ? 4 : 2, kScaled>(m, dec, uv, perm, wait_limit, l, B, t0, lane, w);
         t0 += 64;
       } else {
-        near_chunk<kLearned, kStaged, 1, kWide ? 4 : 2>(m, dec, uv, perm, wait_limit, l, B, t0, lane, w);
+        near_chunk<kLearned, kStaged, 1, kWide ? 4 : 2, kScaled>(m, dec, uv, perm, wait_limit, l, B, t0, lane, w);
         t0 += 32;
       }
     }
@@ -2251,9 +2290,9 @@ int persistent_blocks(K kernel, int warps_per_block, size_t smem, int nleaf, int
 
 // One near-field variant: kStaged sources (stage buffers in dynamic shared
 // memory, 4 KB per warp), kWarps warps per block, persistent blocks.
-template <bool kLearned, bool kStaged, int kWarps, bool kWide = false>
+template <bool kLearned, bool kScaled, bool kStaged, int kWarps, bool kWide = false>
 cudaError_t launch_near(const MixedView &m, double *uv, const int *perm, Decisions d, cudaStream_t s, int *resident) {
-  auto k = k_eval_near<kLearned, kStaged, kWarps, kWide>;
+  auto k = k_eval_near<kLearned, kStaged, kWarps, kWide, kScaled>;
   const size_t smem = kStaged ? (size_t)kWarps * 2 * kStage * sizeof(float4) : 0;
   if (*resident == 0 && smem > 0) {
     const cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -2263,17 +2302,17 @@ cudaError_t launch_near(const MixedView &m, double *uv, const int *perm, Decisio
   return cudaSuccess;
 }
 
-template <bool kLearned>
+template <bool kLearned, bool kScaled>
 cudaError_t launch_eval(int v, const MixedView &m, double *uv, const int *perm, Decisions d, cudaStream_t s) {
   static int resident[kEvalVariants] = {};  // per variant (the devices here are all one model)
   cudaError_t e = cudaMemsetAsync(&m.st->eval_next, 0, sizeof(unsigned), s);
   if (e != cudaSuccess) return e;
   switch (v) {
-    case 0: e = launch_near<kLearned, false, 4>(m, uv, perm, d, s, &resident[0]); break;
-    case 1: e = launch_near<kLearned, false, 8>(m, uv, perm, d, s, &resident[1]); break;
-    case 2: e = launch_near<kLearned, true, 4>(m, uv, perm, d, s, &resident[2]); break;
-    case 3: e = launch_near<kLearned, true, 8>(m, uv, perm, d, s, &resident[3]); break;
-    default: e = launch_near<kLearned, true, 4, true>(m, uv, perm, d, s, &resident[4]); break;
+    case 0: e = launch_near<kLearned, kScaled, false, 4>(m, uv, perm, d, s, &resident[0]); break;
+    case 1: e = launch_near<kLearned, kScaled, false, 8>(m, uv, perm, d, s, &resident[1]); break;
+    case 2: e = launch_near<kLearned, kScaled, true, 4>(m, uv, perm, d, s, &resident[2]); break;
+    case 3: e = launch_near<kLearned, kScaled, true, 8>(m, uv, perm, d, s, &resident[3]); break;
+    default: e = launch_near<kLearned, kScaled, true, 4, true>(m, uv, perm, d, s, &resident[4]); break;
   }
   if (e != cudaSuccess) return e;
   g_launches.fetch_add(1, std::memory_order_relaxed);
@@ -2288,8 +2327,12 @@ cudaError_t launch_eval(int v, const MixedView &m, double *uv, const int *perm, 
 // the last one stands).
 int near_field(Workspace &ws, const MixedParams &mp, MixedView &m, bool learned, Decisions d, double *uv,
                const int *perm, cudaStream_t s, tree2d_stats_t &st) {
+  // scaled source records where every leaf's blobs share one core radius
+  const bool scaled = m.src4s && !ws.h_status->nonuniform;
   auto run = [&](int v) {
-    return learned ? launch_eval<true>(v, m, uv, perm, d, s) : launch_eval<false>(v, m, uv, perm, d, s);
+    if (scaled)
+      return learned ? launch_eval<true, true>(v, m, uv, perm, d, s) : launch_eval<false, true>(v, m, uv, perm, d, s);
+    return learned ? launch_eval<true, false>(v, m, uv, perm, d, s) : launch_eval<false, false>(v, m, uv, perm, d, s);
   };
   int v = mp.eval_variant;
   if (v < 0 && mp.autotune) {
@@ -2386,6 +2429,7 @@ int mixed_solve(Workspace &ws, const Tree &t, const MixedParams &mp, double *d_u
   need += Arena::bytes_for(n, 4) * 4;             // leaf_of gam s2inv + pad
   need += Arena::bytes_for(n, 8);                 // loc
   need += Arena::bytes_for(n, 16) + Arena::bytes_for(nc, 4) * 4;  // src4, cxf, cyf, cxl, cyl
+  need += Arena::bytes_for(n, 16) + Arena::bytes_for(nc, 4);      // src4s, lscale
   const int kchunks = t.leaf_cap > 0 ? (t.leaf_cap + 31) / 32 : 1;
   need += Arena::bytes_for((size_t)nc * kchunks, 16);              // chunk boxes
   need += Arena::bytes_for(n, 4);                                  // mperm
@@ -2436,6 +2480,8 @@ int mixed_solve(Workspace &ws, const Tree &t, const MixedParams &mp, double *d_u
   m.gam = ws.mx_arena.take<float>(n);
   m.s2inv = ws.mx_arena.take<float>(n);
   m.src4 = ws.mx_arena.take<float4>(n);
+  m.src4s = ws.mx_arena.take<float4>(n);
+  m.lscale = ws.mx_arena.take<float>(nc);
   m.kchunks = kchunks;
   m.cbox = ws.mx_arena.take<float4>((size_t)nc * kchunks);
   m.mperm = ws.mx_arena.take<int>(n);
@@ -2513,7 +2559,7 @@ int mixed_solve(Workspace &ws, const Tree &t, const MixedParams &mp, double *d_u
     note_cuda_error(cudaErrorMemoryAllocation, "interaction lists beyond 2^31 entries");
     return TREE2D_ERR_TOO_LARGE;
   }
-  size_t lneed = 2 * Arena::bytes_for((size_t)tot[0] + 1, 4) + Arena::bytes_for((size_t)tot[1] + 1, 4) +
+  size_t lneed = 2 * Arena::bytes_for((size_t)tot[0] + 1, 4) + 2 * Arena::bytes_for((size_t)tot[1] + 1, 4) +
                  2 * Arena::bytes_for((size_t)tot[2] + 1, 4);
   T2D_CUDA_TRY(ws.mx_lists.reserve(lneed));
   ws.mx_lists.reset();
@@ -2521,6 +2567,7 @@ int mixed_solve(Workspace &ws, const Tree &t, const MixedParams &mp, double *d_u
   m.w_idx = ws.mx_lists.take<int>((size_t)tot[1] + 1);
   m.k_idx = ws.mx_lists.take<int>((size_t)tot[2] + 1);
   m.u_leaf = ws.mx_lists.take<int>((size_t)tot[0] + 1);
+  m.w_leaf = ws.mx_lists.take<int>((size_t)tot[1] + 1);
   m.k_leaf = ws.mx_lists.take<int>((size_t)tot[2] + 1);
   rc = mixed_fill_lists(m, from_scratch, s);
   if (rc) return rc;
@@ -2557,7 +2604,7 @@ int mixed_solve(Workspace &ws, const Tree &t, const MixedParams &mp, double *d_u
   st.n_list_u = tot[0];
   st.n_list_k = tot[2];
   st.n_list_k_blobs = (long long)ws.h_status->k_blobs;
-  unsigned char *u_dec = nullptr, *k_dec = nullptr;
+  unsigned char *u_dec = nullptr, *k_dec = nullptr, *w_dec = nullptr;
   const bool side = (learned || mp.learned) && t.lev0 == 0;
   // after the fork, an early return first waits for the second stream, so
   // that no kernel of this solve still runs when its buffers are reused
@@ -2581,7 +2628,8 @@ int mixed_solve(Workspace &ws, const Tree &t, const MixedParams &mp, double *d_u
     // leaf statistics and u_ref (also used by sampling), then decisions
     const size_t wim = learn_weight_image_elems();
     size_t need = Arena::bytes_for(wim, 2) + Arena::bytes_for(208, 4) + Arena::bytes_for((size_t)nc, sizeof(LeafStats)) +
-                  Arena::bytes_for((size_t)tot[0] + 1, 1) + Arena::bytes_for((size_t)tot[2] + 1, 1) + 512;
+                  Arena::bytes_for((size_t)tot[0] + 1, 1) + Arena::bytes_for((size_t)tot[2] + 1, 1) +
+                  Arena::bytes_for((size_t)tot[1] + 1, 1) + 512;
     const size_t cap0 = ws.lr_arena.capacity();
     T2D_CUDA_TRY(ws.lr_arena.reserve(need));
     if (ws.lr_arena.capacity() != cap0) ws.lr_version = -1;  // reallocated: weights must be uploaded again
@@ -2591,6 +2639,7 @@ int mixed_solve(Workspace &ws, const Tree &t, const MixedParams &mp, double *d_u
     LeafStats *stats = ws.lr_arena.take<LeafStats>((size_t)nc);
     u_dec = ws.lr_arena.take<unsigned char>((size_t)tot[0] + 1);
     k_dec = ws.lr_arena.take<unsigned char>((size_t)tot[2] + 1);
+    w_dec = mp.lp->far_orders ? ws.lr_arena.take<unsigned char>((size_t)tot[1] + 1) : nullptr;
     float *uref = ws.lr_arena.take<float>(1);
     if (learned && ws.lr_version != mp.lp_version) {
       std::vector<uint16_t> img;
@@ -2609,7 +2658,8 @@ int mixed_solve(Workspace &ws, const Tree &t, const MixedParams &mp, double *d_u
     rc = learned_uref(m, stats, t.root, uref, s2);
     if (rc) return drain(rc);
     if (learned) {
-      rc = learned_decide(m, stats, uref, wimg, bias, mp.lp->direct_bias, tot[0], tot[2], u_dec, k_dec, s2);
+      rc = learned_decide(m, stats, uref, wimg, bias, mp.lp->direct_bias, tot[0], tot[2], tot[1], u_dec, k_dec,
+                          w_dec, s2);
       if (rc) return drain(rc);
     }
     T2D_TRY_DRAIN(schedule(s2));
@@ -2645,7 +2695,8 @@ int mixed_solve(Workspace &ws, const Tree &t, const MixedParams &mp, double *d_u
   }
   T2D_TRY_DRAIN(cudaStreamWaitEvent(s, ws.join_ev, 0));
   T2D_CUDA_TRY(cudaEventRecord(ws.ev[4], s));
-  const Decisions dec = learned ? Decisions{u_dec, k_dec, mp.lp->order_margin} : Decisions{nullptr, nullptr, 0};
+  const Decisions dec = learned ? Decisions{u_dec, k_dec, mp.lp->order_margin, w_dec}
+                                : Decisions{nullptr, nullptr, 0, nullptr};
   rc = near_field(ws, mp, m, learned, dec, d_uv, m.mperm, s, st);
   if (rc) return rc;
   T2D_CUDA_TRY(cudaEventRecord(ws.ev[5], s));

@@ -32,6 +32,9 @@ struct MixedView {
   float2 *loc;           // per position, offset from its leaf centre
   float *gam, *s2inv;    // per position
   float4 *src4;          // per position {loc.x, loc.y, G, -log2(e)/sigma^2}
+  float4 *src4s;         // per position of a leaf with one core radius: {loc.x s, loc.y s, G s, 0},
+                         // s = sqrt(log2 e) / sigma (the near field's scaled records)
+  float *lscale;         // per leaf cell: that s, 0 where its blobs' core radii differ
   int *mperm;            // per position: original blob index.  The per-position arrays of the
                          // mixed form hold each leaf's blobs by sub-cell (8 x 8 sub-cells in
                          // Morton order, tree order inside one), not in the tree's order
@@ -50,7 +53,7 @@ struct MixedView {
   int list_cap;
   int *level_off;              // [kKeyLevels + 2]: start of each level in by_level, then cursors
   int *u_idx, *w_idx, *k_idx;
-  int *u_leaf, *k_leaf;  // leaf ordinal of each U / K entry
+  int *u_leaf, *w_leaf, *k_leaf;  // leaf ordinal of each U / W / K entry
   const int *leaf_order; // near-field schedule: leaf ordinals by estimated work, largest first
   float *M, *L;          // per cell, 2P floats (re[P], im[P])
   const float2 *m2m, *l2l;  // [4][kMaxP][kMaxP] translation operators

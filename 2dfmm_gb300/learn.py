@@ -43,7 +43,8 @@ DEFAULT_WEIGHTS = os.path.join(HERE, "data", "learned_weights.npz")
 # form stays at 4.7-5.3e-7 throughout).  The multiples are in the design
 # notes.
 ENVELOPE_FACTOR = 2.5
-ENVELOPE_LEAF_BLOBS = 64   # leaf size of the training solves (configuration 5, num_p 65)
+ENVELOPE_LEAF_BLOBS = 96   # leaf size of the training solves (the mixed forms' default below 2M blobs)
+TRAIN_CUTOFF = 2.5         # correction radius of the training solves (the default in force)
 
 
 def save_weights(path, theta, meta, k_blobs_per_leaf_train=None, cutoff_train=None, extra=None):
@@ -131,8 +132,8 @@ def _rel_l2(P, torch, arrays, n, idx, uv_list):
 
 
 def run(n=1_048_576, steps=100, dt=1e-3, train_until=20, samples=200_000, train_steps=2000, batch=4096,
-        lr=2e-3, score_every=10, score_targets=2048, pterms=16, cutoff=3.0, seed=0, out=None, quiet=False,
-        leaf_blobs=ENVELOPE_LEAF_BLOBS):
+        lr=2e-3, score_every=10, score_targets=2048, pterms=16, cutoff=TRAIN_CUTOFF, seed=0, out=None, quiet=False,
+        leaf_blobs=ENVELOPE_LEAF_BLOBS, budget=3e-7):
     import torch
     P = importlib.import_module("2dfmm_gb300")
     W = importlib.import_module("2dfmm_gb300.workloads")
@@ -141,6 +142,7 @@ def run(n=1_048_576, steps=100, dt=1e-3, train_until=20, samples=200_000, train_
     P.set_params(b.nterms, b.num_p, b.theta)
     P.set_mixed_params(pterms, cutoff, True)
     P.set_mixed_leaf(leaf_blobs)
+    P.learn_set_options(1.0, 1, budget)
     per_step = int(np.ceil(samples / (train_until + 1)))
     Xs, ys = [], []
     log = {"collect": [], "score": []}
@@ -164,7 +166,8 @@ def run(n=1_048_576, steps=100, dt=1e-3, train_until=20, samples=200_000, train_
     theta = P.learn_get_weights()
     hist = np.bincount(y, minlength=14).tolist()
     summary = {"samples": int(len(y)), "label_histogram": hist, "final_loss": loss, "collect_s": t_collect,
-               "train_s": t_train, "k_blobs_per_leaf_train": k_blobs, "leaf_blobs": leaf_blobs}
+               "train_s": t_train, "k_blobs_per_leaf_train": k_blobs, "leaf_blobs": leaf_blobs,
+               "cutoff": cutoff, "budget": budget}
     if out:
         save_weights(out, theta, summary, k_blobs_per_leaf_train=k_blobs, cutoff_train=cutoff)
     P.learn_set_envelope(k_blobs * ENVELOPE_FACTOR, cutoff)
@@ -205,10 +208,11 @@ def run(n=1_048_576, steps=100, dt=1e-3, train_until=20, samples=200_000, train_
     })
     P.set_mode(P.MODE_PLAIN)
     P.set_mixed_leaf(-1)
+    P.learn_set_options(1.0, 1, 3e-7)
     return summary, log
 
 
-def measure_envelope(path=DEFAULT_WEIGHTS, n=1_048_576, train_until=20, dt=1e-3, pterms=16, cutoff=3.0,
+def measure_envelope(path=DEFAULT_WEIGHTS, n=1_048_576, train_until=20, dt=1e-3, pterms=16, cutoff=TRAIN_CUTOFF,
                      leaf_blobs=ENVELOPE_LEAF_BLOBS):
     """Records in the weights file at `path` the training solves' largest
     mean K-list source blobs per leaf: the configuration-5 steps 0..train_until
@@ -252,6 +256,10 @@ def main():
     ap.add_argument("--leaf-blobs", type=int, default=ENVELOPE_LEAF_BLOBS, help="leaf size of the training solves")
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--log", default=None)
+    ap.add_argument("--cutoff", type=float, default=TRAIN_CUTOFF,
+                    help="correction radius (max sigma) of the training solves")
+    ap.add_argument("--budget", type=float, default=3e-7,
+                    help="label budget: per-interaction error in units of sum|G| / root side")
     ap.add_argument("--measure-envelope", action="store_true",
                     help="only record the training density in the weights file at --out")
     a = ap.parse_args()
@@ -260,7 +268,7 @@ def main():
         return
     summary, log = run(n=a.n, steps=a.steps, train_until=a.train_until, samples=a.samples,
                        train_steps=a.train_steps, score_every=a.score_every, out=a.out, seed=a.seed,
-                       leaf_blobs=a.leaf_blobs)
+                       leaf_blobs=a.leaf_blobs, cutoff=a.cutoff, budget=a.budget)
     print(json.dumps(summary), flush=True)
     if a.log:
         with open(a.log, "w") as f:

@@ -52,6 +52,8 @@ def parse():
     ap.add_argument("--weights", default=None, help="learned form: weights file (default: the packaged ones)")
     ap.add_argument("--direct-bias", type=float, default=1.0, help="learned form: logit bias towards direct evaluation")
     ap.add_argument("--order-margin", type=int, default=1, help="learned form: orders added to the network's choice")
+    ap.add_argument("--far-orders", action="store_true",
+                    help="learned form: the network also sets each W-list M2P's order")
     ap.add_argument("--pterms", type=int, default=16, help="mixed form: expansion length")
     ap.add_argument("--cutoff", type=float, default=2.5, help="mixed form: correction radius / max sigma")
     ap.add_argument("--cuda-core-m2l", action="store_true", help="mixed form: M2L on CUDA cores")
@@ -378,6 +380,7 @@ def run_ours(args):
         else:
             P.learn_set_weights(theta)
             P.learn_set_options(args.direct_bias, args.order_margin)
+            P.learn_set_far_orders(args.far_orders)
             envelope, env_cutoff = L.load_envelope(path)
             P.learn_set_envelope(envelope, env_cutoff)
             learned_note = (f"{os.path.relpath(path, ROOT)} (trained on configuration-5 steps 0-20 by "

@@ -260,6 +260,16 @@ int tree2d_learn_get_weights(float *theta, int n);
  * order raised by this much; budget: label tolerance per interaction in
  * units of sum|G| / root side.  Defaults 1.0, 1, 3e-7. */
 int tree2d_learn_set_options(float direct_bias, int order_margin, double budget);
+/* on = 1: the network also sets the expansion order of the far field's M2P
+ * terms, each W-list entry (a cell's multipole evaluated at a leaf's blobs)
+ * whose source is a leaf, presented to it as a U entry: the same order
+ * classes and per-interaction budget; W entries with an internal-cell
+ * source keep the full order.  on = 0 (default): every W entry at the full
+ * order.  Off by default: with the packaged network it saved no time at
+ * 4M two-patch + sheet blobs (7.43 against 7.41 ms per solve) and 0.4% at
+ * 1M Lamb-Oseen blobs, and a network trained only briefly let relL2 pass
+ * 1e-6 with it.  No counterpart in the reference. */
+int tree2d_learn_set_far_orders(int on);
 /* Training envelope of the loaded network: the largest mean number of
  * source blobs in a leaf's K (correction) list leaves that the training
  * solves had, counted with the correction radius cutoff_sigmas (units of the

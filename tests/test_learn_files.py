@@ -14,7 +14,7 @@ def test_packaged_weights_and_envelope(tmp_path):
     assert theta is not None and theta.dtype == np.float32 and theta.size == 10448
     k, cutoff = L.load_envelope()
     d = np.load(L.DEFAULT_WEIGHTS)
-    assert cutoff == float(d["cutoff_train"]) == 3.0
+    assert cutoff == float(d["cutoff_train"]) == L.TRAIN_CUTOFF
     assert k == float(d["k_blobs_per_leaf_train"]) * L.ENVELOPE_FACTOR and k > 0
     # a file written without the training figure: no limit
     p = tmp_path / "w.npz"
