@@ -208,10 +208,15 @@ __global__ void __launch_bounds__(32 * kSetupWarps) k_leaf_setup(MixedView m, co
     if (code < kSubCells && (grp & lt) == 0) cnt[code] += __popc(grp);  // one leader per sub-cell
     __syncwarp();
   }
-  const bool uniform = __all_sync(0xffffffffu, same);
-  // s = sqrt(log2 e) / sigma from the FP32 1/sigma^2 the records carry
+  // s = sqrt(log2 e) / sigma from the FP32 1/sigma^2 the records carry.
+  // Scaled records need a finite s whose products with the leaf's offsets
+  // stay far inside FP32 (their squares too): a core radius of 0 (the
+  // mirror images are point vortices) or one far below the leaf's size
+  // keeps the leaf, and so the solve, on the unscaled records.
   const float sf0 = (float)cor0;
-  const float sc = uniform ? sqrtf(1.44269504f * __frcp_rn(sf0 * sf0)) : 0.f;
+  const float s0 = sqrtf(1.44269504f * __frcp_rn(sf0 * sf0));
+  const bool uniform = __all_sync(0xffffffffu, same) && s0 > 0.f && __fmul_rn(s0, (float)side) < 1e15f;
+  const float sc = uniform ? s0 : 0.f;
   if (lane == 0) {
     m.lscale[c] = sc;
     if (!uniform) m.st->nonuniform = 1;
@@ -1668,12 +1673,14 @@ __device__ __forceinline__ void near_chunk(const MixedView &m, const Decisions &
     w.tbox[8] = __fmul_rn(rc, rc);
   }
   __syncwarp();
-  // target offsets from B's centre (read again where needed: L1-resident, and
-  // registers and shared memory are kept for the pair loop and occupancy)
-  auto zof = [&](int k) {
+  // target offsets from B's centre, held in registers for the chunk
+  float2 zr[kT];
+#pragma unroll
+  for (int k = 0; k < kT; k++) {
     const int t = t0 + 32 * k + lane;
-    return t < tend ? m.loc[t] : make_float2(0.f, 0.f);
-  };
+    zr[k] = t < tend ? m.loc[t] : make_float2(0.f, 0.f);
+  }
+  auto zof = [&](int k) { return zr[k]; };
   // valid targets of each pack (the pair counts are per target)
   const unsigned nt = (unsigned)min(tend - t0, 32 * kT);
   const unsigned vp0 = kT == 4 ? min(nt, 64u) : nt, vp1 = kT == 4 ? nt - vp0 : 0u;

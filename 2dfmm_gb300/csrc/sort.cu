@@ -207,9 +207,10 @@ constexpr long kLookbackLimit = 1l << 22;     // polls; a healthy look-back ends
 // shared memory, then added to hist[pass][digit].
 __global__ void __launch_bounds__(kThreads) k_hist_all(const uint64_t *__restrict__ words, int n, int begin_bit,
                                                        int passes, unsigned *__restrict__ hist) {
-  __shared__ unsigned h[kMaxPasses][kBins];
-  for (int i = threadIdx.x; i < kMaxPasses * kBins; i += kThreads) (&h[0][0])[i] = 0;
+  __shared__ unsigned hw[kWarps][kMaxPasses][kBins];  // per warp: no atomics collide across warps
+  for (int i = threadIdx.x; i < kWarps * kMaxPasses * kBins; i += kThreads) (&hw[0][0][0])[i] = 0;
   __syncthreads();
+  unsigned (*h)[kBins] = hw[threadIdx.x >> 5];
   const unsigned ltmask = lanemask_lt();
   const long stride = (long)gridDim.x * kThreads;
   for (long i0 = (long)blockIdx.x * kThreads + (threadIdx.x & ~31); i0 < n; i0 += stride) {  // warp-uniform
@@ -225,7 +226,8 @@ __global__ void __launch_bounds__(kThreads) k_hist_all(const uint64_t *__restric
   }
   __syncthreads();
   for (int i = threadIdx.x; i < passes * kBins; i += kThreads) {
-    const unsigned v = (&h[0][0])[i];
+    unsigned v = 0;
+    for (int w = 0; w < kWarps; w++) v += (&hw[w][0][0])[i];
     if (v) atomicAdd(&hist[i], v);
   }
 }
