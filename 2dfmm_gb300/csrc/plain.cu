@@ -16,7 +16,9 @@
 //              round-to-nearest FP64 operations without contraction
 //              (r = sqrt(dx*dx + dy*dy); region > theta*r), so each lane
 //              takes exactly the reference's branch.  M2S (fmm.c:60-67) is
-//              evaluated by Horner in w = 1/(z - zc); P2P is fmm.c:121-142.
+//              evaluated by Horner in w = 1/(z - zc), from a per-lane queue
+//              of accepted cells that the warp empties in rounds (all lanes
+//              busy); P2P is fmm.c:121-142.
 #include "dev_common.cuh"
 
 namespace t2d {
@@ -35,6 +37,14 @@ __device__ __forceinline__ double rcp_nr(double x) {
   y = fma(y, fma(-x, y, 1.0), y);
   y = fma(y, fma(-x, y, 1.0), y);
   return y;
+}
+
+// a b + c for complex values as FMAs only: Re = a.x b.x + (c.x - a.y b.y),
+// Im = a.x b.y + (c.y + a.y b.x), each inner term one FMA and each outer one
+// another (explicit, so the rounding does not depend on how the compiler
+// contracts the code around it).
+__device__ __forceinline__ double2 cfma(double2 a, double2 b, double2 c) {
+  return make_double2(__fma_rn(a.x, b.x, __fma_rn(-a.y, b.y, c.x)), __fma_rn(a.x, b.y, __fma_rn(a.y, b.x, c.y)));
 }
 
 __constant__ double c_binom[kMaxTerms][kMaxTerms];
@@ -97,6 +107,7 @@ __global__ void __launch_bounds__(256) k_m2m(Tree t, int nt, int lev) {
 
 constexpr int kEvalWarps = 4;
 constexpr int kStackCap = 160;
+constexpr int kQueue = 32;  // deferred M2S cells per lane
 
 struct EvalArgs {
   Tree t;
@@ -112,6 +123,7 @@ struct EvalArgs {
 __global__ void __launch_bounds__(kEvalWarps * 32) k_eval(EvalArgs a) {
   __shared__ int s_cell[kEvalWarps][kStackCap];
   __shared__ unsigned s_mask[kEvalWarps][kStackCap];
+  __shared__ int s_queue[kEvalWarps][kQueue][32];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const long i = ((long)blockIdx.x * kEvalWarps + warp) * 32 + lane;
   const bool valid = i < a.ntgt;
@@ -126,6 +138,39 @@ __global__ void __launch_bounds__(kEvalWarps * 32) k_eval(EvalArgs a) {
   double ud0 = 0.0, ud1 = 0.0;
   unsigned long long n_m2s = 0, n_pairs = 0;
   bool overflow = false;
+
+  // The lanes accept cells at different depths, so an M2S evaluated where
+  // it is accepted runs with the warp's other lanes idle.  Each lane
+  // instead queues its accepted cells (s_queue[warp][k][lane], in the order
+  // it accepts them) and the warp evaluates the queues together, one entry
+  // per lane per round, when a lane's queue could overflow and at the end.
+  // A lane's M2S terms still reach phi in its own acceptance order, each
+  // with the same operations (dx, dy, d2 formed again from the cell's
+  // centre, bit for bit), and the direct terms go to ud0/ud1 as before.
+  int nq = 0;
+  auto flush = [&]() {
+    int rounds = nq;
+    for (int o = 16; o; o >>= 1) rounds = max(rounds, __shfl_xor_sync(0xffffffffu, rounds, o));
+    for (int r = 0; r < rounds; r++) {
+      if (r < nq) {
+        // M2S, fmm.c:60-67: sum_{k<nt-1} a_k w^{k+1}, w = 1/(z - zc)
+        const int cc = s_queue[warp][r][lane];
+        const double dx = __dsub_rn(x, t.cx[cc]);
+        const double dy = __dsub_rn(y, t.cy[cc]);
+        const double d2 = __dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy));
+        const double inv = rcp_nr(d2);
+        const double2 w = make_double2(__dmul_rn(dx, inv), -__dmul_rn(dy, inv));
+        const double2 *cf = t.coef + (size_t)cc * nt;
+        // Horner, each step acc <- acc w + a_k as two FMAs per component
+        // (four per term against six for a product and a sum), and the
+        // last product added into phi the same way
+        double2 acc = cf[nt - 2];
+        for (int k = nt - 3; k >= 0; k--) acc = cfma(acc, w, cf[k]);
+        phi = cfma(acc, w, phi);
+      }
+    }
+    nq = 0;
+  };
 
   int top = 0;
   if (lane == 0) {
@@ -158,9 +203,10 @@ __global__ void __launch_bounds__(kEvalWarps * 32) k_eval(EvalArgs a) {
             // 1 - exp(-x2) rounds to exactly 1.0 once exp(-x2) < 2^-54
             // (x2 > 37.4); the shortcut keeps the result bit-identical.
             const double e1 = x2 > 40.0 ? 1.0 : 1.0 - exp(-x2);
-            const double rv = t.cir[j] * e1;
-            ax -= rv * ry * rv2;
-            ay += rv * rx * rv2;
+            // G (1 - e) / r^2 once, then one FMA per component
+            const double f = __dmul_rn(__dmul_rn(t.cir[j], e1), rv2);
+            ax = __fma_rn(-f, ry, ax);
+            ay = __fma_rn(f, rx, ay);
           }
         }
         ud0 += 0.5 * ax / kPi;
@@ -168,6 +214,8 @@ __global__ void __launch_bounds__(kEvalWarps * 32) k_eval(EvalArgs a) {
         n_pairs += (unsigned long long)(e - b);
       }
     } else {
+      // a cell's four children can add four entries to a lane's queue
+      if (__any_sync(0xffffffffu, nq > kQueue - 4)) flush();
       const int4 ch = reinterpret_cast<const int4 *>(t.child)[c];
 #pragma unroll 1
       for (int q = 0; q < 4; q++) {
@@ -196,15 +244,7 @@ __global__ void __launch_bounds__(kEvalWarps * 32) k_eval(EvalArgs a) {
           }
         }
         const unsigned dmask = __ballot_sync(0xffffffffu, desc);
-        if (act && !desc && nt >= 2) {
-          // M2S, fmm.c:60-67: sum_{k<nt-1} a_k w^{k+1}, w = 1/(z - zc)
-          const double inv = rcp_nr(d2);
-          const double2 w = make_double2(dx * inv, -dy * inv);
-          const double2 *cf = t.coef + (size_t)cc * nt;
-          double2 acc = cf[nt - 2];
-          for (int k = nt - 3; k >= 0; k--) acc = cadd(cmul(acc, w), cf[k]);
-          phi = cadd(phi, cmul(acc, w));
-        }
+        if (act && !desc && nt >= 2) s_queue[warp][nq++][lane] = cc;
         if (act && !desc) n_m2s++;
         if (dmask) {
           if (top + 1 >= kStackCap) {
@@ -222,6 +262,7 @@ __global__ void __launch_bounds__(kEvalWarps * 32) k_eval(EvalArgs a) {
       if (__any_sync(0xffffffffu, overflow)) break;
     }
   }
+  flush();
   if (__any_sync(0xffffffffu, overflow)) {
     if (lane == 0) set_err(a.st, TREE2D_ERR_TIMEOUT);
   }

@@ -45,6 +45,14 @@ DEFAULT_WEIGHTS = os.path.join(HERE, "data", "learned_weights.npz")
 ENVELOPE_FACTOR = 2.5
 ENVELOPE_LEAF_BLOBS = 96   # leaf size of the training solves (the mixed forms' default below 2M blobs)
 TRAIN_CUTOFF = 2.5         # correction radius of the training solves (the default in force)
+# Label budget of the packaged network: the per-interaction error a cheaper
+# class may add, in units of u_ref = sum|G| / root side.  Measured with
+# networks trained at 1e-6, 3e-6 and 1e-5 (relL2 against the FP64 direct
+# sum, 4M two-patch + sheet / 1M Lamb-Oseen, and the learned solve's time
+# against the fixed form's at 4M): 5.3e-7 / 4.7e-7, 1.03x; 7.0e-7 /
+# 4.9e-7, 1.08x; 3.5e-6 / 9.4e-7, 1.22x.  3e-6 keeps the 1e-6 bar with a
+# 1.4x margin.
+TRAIN_BUDGET = 3e-6
 
 
 def save_weights(path, theta, meta, k_blobs_per_leaf_train=None, cutoff_train=None, extra=None):
@@ -133,7 +141,7 @@ def _rel_l2(P, torch, arrays, n, idx, uv_list):
 
 def run(n=1_048_576, steps=100, dt=1e-3, train_until=20, samples=200_000, train_steps=2000, batch=4096,
         lr=2e-3, score_every=10, score_targets=2048, pterms=16, cutoff=TRAIN_CUTOFF, seed=0, out=None, quiet=False,
-        leaf_blobs=ENVELOPE_LEAF_BLOBS, budget=3e-7):
+        leaf_blobs=ENVELOPE_LEAF_BLOBS, budget=TRAIN_BUDGET):
     import torch
     P = importlib.import_module("2dfmm_gb300")
     W = importlib.import_module("2dfmm_gb300.workloads")
@@ -258,7 +266,7 @@ def main():
     ap.add_argument("--log", default=None)
     ap.add_argument("--cutoff", type=float, default=TRAIN_CUTOFF,
                     help="correction radius (max sigma) of the training solves")
-    ap.add_argument("--budget", type=float, default=3e-7,
+    ap.add_argument("--budget", type=float, default=TRAIN_BUDGET,
                     help="label budget: per-interaction error in units of sum|G| / root side")
     ap.add_argument("--measure-envelope", action="store_true",
                     help="only record the training density in the weights file at --out")
