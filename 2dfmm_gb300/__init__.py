@@ -32,7 +32,7 @@ EVAL_VARIANTS = 5  # TREE2D_EVAL_VARIANTS
 EXPORTS = [
     "make_tree", "biot_tree", "tree2d_last_error", "tree2d_error_string", "tree2d_set_params",
     "tree2d_clear_params", "tree2d_get_params", "tree2d_set_mode", "tree2d_get_mode", "tree2d_set_mixed_params", "tree2d_set_mixed_leaf", "biot_tree_batch",
-    "tree2d_solve_device", "tree2d_solve_device_static", "tree2d_solve_sets", "tree2d_set_tuning", "tree2d_set_level_chain", "tree2d_get_stats", "tree2d_export_tree", "tree2d_direct_device", "tree2d_fp64_probe", "tree2d_pipe_probe", "tree2d_wait_probe", "tree2d_version",
+    "tree2d_solve_device", "tree2d_solve_device_static", "tree2d_solve_sets", "tree2d_set_tuning", "tree2d_set_level_chain", "tree2d_set_m2l_rows", "tree2d_get_stats", "tree2d_export_tree", "tree2d_direct_device", "tree2d_fp64_probe", "tree2d_pipe_probe", "tree2d_wait_probe", "tree2d_version",
     "tree2d_learn_param_count", "tree2d_learn_load", "tree2d_learn_set_weights", "tree2d_learn_set_envelope", "tree2d_learn_get_weights", "tree2d_learn_set_options", "tree2d_learn_set_far_orders",
     "tree2d_learn_collect", "tree2d_learn_train", "tree2d_mlp_grad", "tree2d_mlp_forward",
     "tree2d_set_mirror", "tree2d_advect_device",
@@ -54,7 +54,7 @@ class Stats(ctypes.Structure):
         ("n_launches", ctypes.c_longlong), ("m2l_path", ctypes.c_int), ("eval_variant", ctypes.c_int),
         ("learned_active", ctypes.c_int), ("n_list_u", ctypes.c_longlong), ("n_list_k", ctypes.c_longlong),
         ("leaf_blobs", ctypes.c_int), ("n_list_k_blobs", ctypes.c_longlong),
-        ("n_pairs_k", ctypes.c_longlong), ("n_pairs_k_listed", ctypes.c_longlong),
+        ("n_pairs_k", ctypes.c_longlong), ("n_pairs_k_listed", ctypes.c_longlong), ("m2l_rows", ctypes.c_int),
     ]
 
     def as_dict(self):
@@ -122,6 +122,8 @@ def load(path: str | None = None):
     L.tree2d_set_tuning.restype = ctypes.c_int
     L.tree2d_set_level_chain.argtypes = [ctypes.c_int]
     L.tree2d_set_level_chain.restype = ctypes.c_int
+    L.tree2d_set_m2l_rows.argtypes = [ctypes.c_int]
+    L.tree2d_set_m2l_rows.restype = ctypes.c_int
     L.tree2d_solve_sets.argtypes = [ctypes.c_int, _ip, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                     ctypes.c_void_p, ctypes.c_void_p]
     L.tree2d_solve_sets.restype = ctypes.c_int
@@ -265,6 +267,12 @@ def set_level_chain(on: bool = False):
     """P = 16 M2M / L2L levels as one cooperative launch each, or one launch
     per level (default); the results are the same."""
     _check(load().tree2d_set_level_chain(int(on)), "set_level_chain")
+
+
+def set_m2l_rows(rows: int = 0):
+    """Cells per CTA of the tensor-core M2L: 128, 64 (bit-identical
+    results), or 0 for the tuner's choice."""
+    _check(load().tree2d_set_m2l_rows(int(rows)), "set_m2l_rows")
 
 
 def solve_sets(d_xy: int, d_cir: int, d_cor: int, d_uv: int, offsets, stream: int = 0):

@@ -826,6 +826,14 @@ int tree2d_set_level_chain(int on) {
   return TREE2D_OK;
 }
 
+int tree2d_set_m2l_rows(int rows) {
+  Lib &L = lib();
+  std::lock_guard<std::mutex> lk(L.mu);
+  if (rows != 0 && rows != 64 && rows != 128) return fail(TREE2D_ERR_BAD_PARAMS);
+  L.mixed.m2l_rows = rows;
+  return TREE2D_OK;
+}
+
 int tree2d_set_mixed_leaf(int max_blobs) {
   Lib &L = lib();
   std::lock_guard<std::mutex> lk(L.mu);

@@ -47,6 +47,7 @@ struct MixedParams {
   int leaf_blobs = -1;    // most blobs per leaf of the mixed forms' tree: -1 by set size
                           // (mixed_leaf_blobs), 0 the parameters' num_p - 1, > 0 this
   int level_chain = 0;    // M2M / L2L level chains as one cooperative launch each (P = 16)
+  int m2l_rows = 0;       // tensor-core M2L cells per CTA: 0 = the tuner's choice, 64 or 128 forced
 };
 
 // Most blobs per leaf of the tree the mixed forms build (the plain form keeps
@@ -171,6 +172,7 @@ struct Workspace {
   MixedView *mxv = nullptr;  // the last mixed solve's view (kept for sampling)
   long mx_tot[3] = {0, 0, 0};  // U, W, K list entries of that solve
   std::map<uint64_t, int> eval_tuned;  // size class -> fastest near-field variant
+  std::map<uint64_t, int> m2l_tuned;   // size class -> faster M2L tile rows (64 or 128)
   int last_depth = 0;  // depth of the last tree built (sizes the next keys)
   int list_cap = 256;  // entries per leaf of the one-walk list scratch (from the last solve)
   DevStatus *status = nullptr;   // device

@@ -8,7 +8,10 @@
 //     D[r, o] = sum_K A[r, K] B_q[K, o],   K = 27 slots x 2P, o < 2P,
 // rows r = target cells of the class, A[r, s*2P + j] = M[V[c_r][s]][j]
 // (gathered, zero where the slot is empty), B_q the real form of the 27
-// complex operators.  One CTA (128 threads) owns 128 rows; per slot it
+// complex operators.  One CTA (128 threads) owns 128 rows, or 64 (the
+// tile shape the tuner may pick: the MMA's other 64 rows are zero, so
+// twice the CTAs share a class's cells; a row's sums are its own either
+// way, bit for bit); per slot it
 // gathers its A chunk into shared memory, the B chunk arrives by a bulk
 // copy (cp.async.bulk, the B images are pre-laid out in global memory),
 // and one thread issues tcgen05.mma kind::tf32 (M=128, N=2P padded to 16,
@@ -70,6 +73,7 @@ struct TcArgs {
   const float *bimg;     // [4][27][2 (hi,lo)][Npad x Kc] core-matrix images
   int P, Kc, Npad, tmem_cols, ngroups;
   int nbs;               // B stages: 3 (slot i+1's images prefetched) or 2
+  int rows;              // cells per CTA: kRows, or kRows / 2 (the MMA's other rows zero)
   long wait_limit;
 };
 
@@ -93,7 +97,7 @@ __global__ void __launch_bounds__(kThreadsTC) k_m2l_tc(TcArgs a) {
 
   const int cls = blockIdx.y;
   const int count = a.cls_count[cls];
-  const int row0 = blockIdx.x * kRows;
+  const int row0 = blockIdx.x * a.rows;
   if (row0 >= count) return;  // uniform for the block
   const MixedView &m = a.m;
   const int P = a.P, Kc = a.Kc, Npad = a.Npad, nbs = a.nbs;
@@ -124,7 +128,7 @@ __global__ void __launch_bounds__(kThreadsTC) k_m2l_tc(TcArgs a) {
   const uint32_t tmem = s_tmem;
 
   const int row = row0 + tid;
-  const bool valid = row < count;
+  const bool valid = tid < a.rows && row < count;
   const int cell = valid ? a.cls_list[(size_t)cls * m.ncell + row] : -1;
   {
     unsigned mine = 0u;
@@ -398,7 +402,8 @@ void m2l_b_images(int P, const float *h_m2l, std::vector<float> &img) {
     }
 }
 
-int m2l_tensor_cores(MixedView &m, const float *bimg, int *cls_list, int *cls_count, cudaStream_t s) {
+int m2l_tensor_cores(MixedView &m, const float *bimg, int *cls_list, int *cls_count, int rows, cudaStream_t s) {
+  if (rows != kRows && rows != kRows / 2) return TREE2D_ERR_BAD_PARAMS;
   const int P = m.P, Kc = 2 * P, Npad = m2l_npad(P);
   if (Kc % 8 != 0) return TREE2D_ERR_BAD_PARAMS;  // K of one MMA is 8 TF32 elements
   T2D_CUDA_TRY(cudaMemsetAsync(cls_count, 0, 4 * sizeof(int), s));
@@ -413,13 +418,14 @@ int m2l_tensor_cores(MixedView &m, const float *bimg, int *cls_list, int *cls_co
   a.Npad = Npad;
   a.tmem_cols = 256;                            // two CTAs per SM fill the 512 columns
   a.ngroups = 256 / Npad < 8 ? 256 / Npad : 8;
+  a.rows = rows;
   a.wait_limit = 1l << 22;  // polls; a healthy wait ends within microseconds
   const size_t fixed = (size_t)27 * kRows * 4 + 2 * (2 * (size_t)kRows * Kc * 4);
   const size_t bst = 2 * (size_t)Npad * Kc * 4;
   a.nbs = fixed + 3 * bst <= 110 * 1024 ? 3 : 2;  // 3 B stages while two CTAs still fit an SM
   const size_t smem = fixed + (size_t)a.nbs * bst;
   T2D_CUDA_TRY(cudaFuncSetAttribute(k_m2l_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  dim3 grid((m.ncell + kRows - 1) / kRows, 4);
+  dim3 grid((m.ncell + rows - 1) / rows, 4);
   k_m2l_tc<<<grid, kThreadsTC, smem, s>>>(a);
   g_launches.fetch_add(2, std::memory_order_relaxed);
   T2D_CUDA_TRY(cudaGetLastError());

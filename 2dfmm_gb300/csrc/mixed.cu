@@ -2380,6 +2380,50 @@ int near_field(Workspace &ws, const MixedParams &mp, MixedView &m, bool learned,
   return TREE2D_OK;
 }
 
+// The tensor-core M2L with the tile the tuner chose for this size class
+// (cells per CTA, 128 or 64, bit-identical results): on the first solve of
+// a (device, P, cell-count octave) class both shapes run twice, in the
+// order 128 64 64 128, timed by CUDA events on the stream, and the faster
+// is kept (each run stores the same local expansions).
+int m2l_tc_tuned(Workspace &ws, const MixedParams &mp, MixedView &m, const float *dimg, int *cls_list,
+                 int *cls_count, cudaStream_t s, tree2d_stats_t &st) {
+  int rows = mp.m2l_rows;
+  if (rows == 0 && mp.autotune) {
+    int dev = 0;
+    T2D_CUDA_TRY(cudaGetDevice(&dev));
+    int octave = 0;
+    while (octave < 40 && (1ll << (octave + 1)) <= (long long)m.ncell) octave++;
+    const uint64_t key = ((uint64_t)dev << 40) | ((uint64_t)m.P << 16) | (uint64_t)octave;
+    auto it = ws.m2l_tuned.find(key);
+    if (it != ws.m2l_tuned.end()) {
+      rows = it->second;
+    } else {
+      static const int kShapes[4] = {128, 64, 64, 128};
+      float best = 0.f;
+      int br = 128;
+      for (int r = 0; r < 4; r++) {
+        T2D_CUDA_TRY(cudaEventRecord(ws.ev[6], s));
+        const int rc = m2l_tensor_cores(m, dimg, cls_list, cls_count, kShapes[r], s);
+        if (rc) return rc;
+        T2D_CUDA_TRY(cudaEventRecord(ws.ev[7], s));
+        T2D_CUDA_TRY(cudaEventSynchronize(ws.ev[7]));
+        float ms = 0.f;
+        T2D_CUDA_TRY(cudaEventElapsedTime(&ms, ws.ev[6], ws.ev[7]));
+        if (r == 0 || ms < best) {
+          best = ms;
+          br = kShapes[r];
+        }
+      }
+      ws.m2l_tuned[key] = br;
+      st.m2l_rows = br;
+      return TREE2D_OK;
+    }
+  }
+  if (rows != 64) rows = 128;
+  st.m2l_rows = rows;
+  return m2l_tensor_cores(m, dimg, cls_list, cls_count, rows, s);
+}
+
 int mixed_eval_points(Workspace &ws, int ntgt, const double *tx, const double *ty, const int *out_idx, double *uv,
                       cudaStream_t s) {
   if (ntgt <= 0) return TREE2D_OK;
@@ -2691,7 +2735,7 @@ int mixed_solve(Workspace &ws, const Tree &t, const MixedParams &mp, double *d_u
   rc = mixed_upward(m, t.depth, ws.h_levels, su, mp.level_chain != 0);
   if (rc) return drain(rc);
   T2D_TRY_DRAIN(cudaMemsetAsync(m.L, 0, sizeof(float) * (size_t)nc * 2 * P, su));
-  rc = tc ? m2l_tensor_cores(m, dimg, cls_list, cls_count, su) : m2l_cuda_cores(m, dm2l, su);
+  rc = tc ? m2l_tc_tuned(ws, mp, m, dimg, cls_list, cls_count, su, st) : m2l_cuda_cores(m, dm2l, su);
   if (rc) return drain(rc);
   st.m2l_path = tc ? 2 : 1;
   rc = mixed_downward(m, t.depth, ws.h_levels, su, mp.level_chain != 0);

@@ -89,7 +89,8 @@ int mixed_downward(MixedView &m, int depth, const int *lev_off, cudaStream_t s, 
 int m2l_cuda_cores(MixedView &m, const float *tables, cudaStream_t s);
 // Tensor-core form: needs P % 4 == 0.  `bimg` are the B operator images
 // (m2l_b_images), cls_list/cls_count scratch of 4*ncell and 4 ints.
-int m2l_tensor_cores(MixedView &m, const float *bimg, int *cls_list, int *cls_count, cudaStream_t s);
+// rows: cells per CTA, 128 or 64 (bit-identical results)
+int m2l_tensor_cores(MixedView &m, const float *bimg, int *cls_list, int *cls_count, int rows, cudaStream_t s);
 int m2l_npad(int P);
 void m2l_b_images(int P, const float *h_m2l, std::vector<float> &img);
 

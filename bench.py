@@ -478,8 +478,8 @@ def run_ours(args):
                        "parallelism": f"replicas x{world} (independent blob sets, no collective)",
                        "l2": "flushed between steps (256 MiB write); inputs 134 MB > L2"},
             "gpu_launches": int(sum(s["n_launches"] for s in sts)),
-            "tuned": {"eval_variant": int(st["eval_variant"]),
-                      "variants": "0/1 global loads, 2/3/4 bulk-copy staging; 4/8/4 warps per block (4: 80 registers, unroll 4)"},
+            "tuned": {"eval_variant": int(st["eval_variant"]), "m2l_rows": int(st["m2l_rows"]),
+                      "variants": "0/1 global loads, 2/3/4 bulk-copy staging; 4/8/4 warps per block (4: 80 registers, unroll 4); M2L 128 or 64 cells per CTA"},
             "learned_active": bool(st["learned_active"]),
             "k_list_per_leaf": st["n_list_k"] / max(1, st["n_leaves"]),
             "k_list_blobs_per_leaf": st["n_list_k_blobs"] / max(1, st["n_leaves"]),
@@ -646,8 +646,8 @@ def run_batch(args):
                        "parallelism": f"replicas x{world} (independent batches, no collective)",
                        "l2": "flushed between steps (256 MiB write)"},
             "gpu_launches": int(sum(x["n_launches"] for x in sts)),
-            "tuned": {"eval_variant": int(st["eval_variant"]),
-                      "variants": "0/1 global loads, 2/3/4 bulk-copy staging; 4/8/4 warps per block (4: 80 registers, unroll 4)"},
+            "tuned": {"eval_variant": int(st["eval_variant"]), "m2l_rows": int(st["m2l_rows"]),
+                      "variants": "0/1 global loads, 2/3/4 bulk-copy staging; 4/8/4 warps per block (4: 80 registers, unroll 4); M2L 128 or 64 cells per CTA"},
             "e2e": {"value": world * n / e2e_t, "unit": UNIT, "h2d_bytes_per_step": n * 32,
                     "d2h_bytes_per_step": n * 16, "api": "host->device copies + tree2d_solve_sets + device->host"},
             "roofline": {"bound": "fp32", "achieved": flops / (ms_eval * 1e-3) / 1e12, "peak": peak,

@@ -168,6 +168,8 @@ typedef struct {
   long long n_pairs_k_listed; /* mixed: pairs of the correction entries
                              evaluated, before 32-blob chunks farther than
                              the correction radius were skipped          */
+  int m2l_rows;           /* mixed, tensor-core M2L: cells per CTA of the
+                             solve (128 or 64)                          */
 } tree2d_stats_t;
 int tree2d_get_stats(tree2d_stats_t *out);
 
@@ -205,6 +207,16 @@ int tree2d_direct_device(int ntgt, const double *d_txy, int nsrc, const double *
  * more than the launches they save).  Results are the same either way.  No
  * counterpart in the reference. */
 int tree2d_set_level_chain(int on);
+
+/* Tile of the tensor-core M2L of the mixed/learned forms: cells per CTA.
+ * rows = 128 gives each CTA a full 128-row MMA tile; rows = 64 fills half
+ * of it (the other rows zero), so twice the CTAs share a level's cells,
+ * which can hide more of the gather latency.  Results are bit-identical.
+ * rows = 0 (default) lets the tuner pick on the first solve of each
+ * (device, P, cell-count class), timing both with CUDA events (with
+ * tree2d_set_tuning's autotune = 0: 128).  Other values:
+ * TREE2D_ERR_BAD_PARAMS.  No counterpart in the reference. */
+int tree2d_set_m2l_rows(int rows);
 int tree2d_set_tuning(int autotune, int eval_variant);
 
 /* Batched solve of nsets independent blob sets in one tree: set k is blobs

@@ -48,6 +48,8 @@ def test_param_validation(lib):
     assert lib.tree2d_set_mixed_leaf(-2) == P.ERR_BAD_PARAMS
     assert lib.tree2d_set_mixed_leaf(65536) == P.ERR_BAD_PARAMS
     assert lib.tree2d_set_mixed_leaf(100) == 0 and lib.tree2d_set_mixed_leaf(-1) == 0
+    assert lib.tree2d_set_m2l_rows(32) == P.ERR_BAD_PARAMS and lib.tree2d_set_m2l_rows(-1) == P.ERR_BAD_PARAMS
+    assert lib.tree2d_set_m2l_rows(64) == 0 and lib.tree2d_set_m2l_rows(128) == 0 and lib.tree2d_set_m2l_rows(0) == 0
     assert lib.tree2d_learn_set_envelope(-1.0, 3.0) == P.ERR_BAD_PARAMS
     assert lib.tree2d_learn_set_envelope(1.0, -3.0) == P.ERR_BAD_PARAMS
     assert lib.tree2d_learn_set_envelope(0.0, 0.0) == 0

@@ -171,6 +171,51 @@ def test_level_chain_equals_per_level_launches(gpu_lib):
 
 
 @pytest.mark.gpu
+def test_m2l_tile_rows_bit_identical(gpu_lib):
+    """The tensor-core M2L with 128 or 64 cells per CTA (the tile shapes
+    the tuner chooses between) stores the same local expansions bit for
+    bit, for one set and for a batch of sets, and the tuner picks one of
+    the two."""
+    torch = pytest.importorskip("torch")
+    import importlib
+    P = gpu_lib
+    W = importlib.import_module("2dfmm_gb300.workloads")
+    dev = torch.device("cuda:0")
+    b = W.two_patch_sheet(300_000, seed=12)
+    P.set_params(b.nterms, b.num_p, b.theta)
+    P.set_mixed_params(16, 2.5, True)
+    P.set_mode(P.MODE_MIXED)
+    xy = torch.from_numpy(b.xy).to(dev)
+    cir = torch.from_numpy(b.cir).to(dev)
+    cor = torch.from_numpy(b.cor).to(dev)
+    sets = W.batch_sets(nsets=24, seed=6, lo=2048, hi=20_000)
+    sxy = torch.from_numpy(np.concatenate([s.xy for s in sets])).to(dev)
+    scir = torch.from_numpy(np.concatenate([s.cir for s in sets])).to(dev)
+    scor = torch.from_numpy(np.concatenate([s.cor for s in sets])).to(dev)
+    offs = np.concatenate([[0], np.cumsum([s.n for s in sets])]).astype(np.int32)
+    outs = []
+    try:
+        for rows in (128, 64, 0, 0):  # forced, forced, tuned (first solve tunes), tuned
+            P.set_m2l_rows(rows)
+            uv = torch.empty_like(xy)
+            P.solve_device(xy.data_ptr(), cir.data_ptr(), cor.data_ptr(), uv.data_ptr(), b.n)
+            torch.cuda.synchronize()
+            got = P.stats()["m2l_rows"]
+            assert got == rows if rows else got in (64, 128)
+            suv = torch.empty_like(sxy)
+            P.solve_sets(sxy.data_ptr(), scir.data_ptr(), scor.data_ptr(), suv.data_ptr(), offs)
+            torch.cuda.synchronize()
+            outs.append((uv.cpu().numpy(), suv.cpu().numpy()))
+    finally:
+        P.set_m2l_rows(0)
+        P.set_mode(P.MODE_PLAIN)
+    assert np.all(np.isfinite(outs[0][0])) and np.all(np.isfinite(outs[0][1]))
+    for uv, suv in outs[1:]:
+        assert np.array_equal(uv, outs[0][0])
+        assert np.array_equal(suv, outs[0][1])
+
+
+@pytest.mark.gpu
 def test_one_walk_lists_equal_two_walk_lists(gpu_lib):
     """The interaction lists are built in one walk into per-leaf scratch rows
     sized from the previous solve, or in two walks (count, then fill) when a
