@@ -1114,6 +1114,7 @@ int tree2d_learn_collect(int max_samples, unsigned seed, float *features, int *l
   Workspace &ws = L.dev.ws;
   if (!ws.mxv || max_samples <= 0 || !features || !labels) return -fail(TREE2D_ERR_NO_TREE);
   MixedView &m = *ws.mxv;
+  if (m.lev0 > 0) return -fail(TREE2D_ERR_MODE);  // samples come from a solve of one set
   const long nu = ws.mx_tot[0], nk = ws.mx_tot[2];
   if (nu + nk <= 0) return 0;
   std::vector<int> uoff(m.nleaf + 1), koff(m.nleaf + 1);

@@ -364,6 +364,48 @@ __global__ void __launch_bounds__(1024) k_uref(MixedView m, const LeafStats *st,
   if (t == 0) *out = part[0] / (float)root->region;
 }
 
+// The leaves of each set of a batched tree: one contiguous range of the
+// leaf order (a set's cells are the subtree of its root), [lo[k], hi[k]).
+__global__ void k_set_leaf_ranges(MixedView m, int *lo, int *hi) {
+  const int l = blockIdx.x * blockDim.x + threadIdx.x;
+  if (l >= m.nleaf) return;
+  const int k = set_of_cell(m, m.leaf_cell[l]);
+  if (l == 0 || set_of_cell(m, m.leaf_cell[l - 1]) != k) lo[k] = l;
+  if (l == m.nleaf - 1 || set_of_cell(m, m.leaf_cell[l + 1]) != k) hi[k] = l + 1;
+}
+
+// k_uref for each set of a batched tree, one block per set: the set's leaves
+// in order, split over the threads as k_uref splits a single tree's, so that
+// a set's u_ref is the one it gets alone, bit for bit.
+__global__ void __launch_bounds__(1024) k_uref_sets(MixedView m, const LeafStats *st, const RootBox *root,
+                                                    const int *lo, const int *hi, float *out) {
+  __shared__ float part[1024];
+  const int k = blockIdx.x, t = threadIdx.x;
+  const int l0 = lo[k], cnt = max(hi[k] - l0, 0);
+  const int per = (cnt + 1023) / 1024;
+  float s = 0.f;
+  for (int l = t * per; l < min(cnt, (t + 1) * per); l++) s += st[m.leaf_cell[l0 + l]].g_abs;
+  part[t] = s;
+  __syncthreads();
+  for (int o = 512; o; o >>= 1) {
+    if (t < o) part[t] += part[t + o];
+    __syncthreads();
+  }
+  if (t == 0) out[k] = part[0] / (float)root[k].region;
+}
+
+int learned_uref_sets(MixedView &m, const LeafStats *stats, const RootBox *roots, int nsets, int *leaf_lo,
+                      int *leaf_hi, float *out, cudaStream_t s) {
+  if (nsets <= 0) return TREE2D_OK;
+  T2D_CUDA_TRY(cudaMemsetAsync(leaf_lo, 0, sizeof(int) * (size_t)nsets, s));
+  T2D_CUDA_TRY(cudaMemsetAsync(leaf_hi, 0, sizeof(int) * (size_t)nsets, s));
+  if (m.nleaf > 0) k_set_leaf_ranges<<<(m.nleaf + 255) / 256, 256, 0, s>>>(m, leaf_lo, leaf_hi);
+  k_uref_sets<<<nsets, 1024, 0, s>>>(m, stats, roots, leaf_lo, leaf_hi, out);
+  g_launches.fetch_add(2, std::memory_order_relaxed);
+  T2D_CUDA_TRY(cudaGetLastError());
+  return TREE2D_OK;
+}
+
 int learned_uref(MixedView &m, const LeafStats *stats, const RootBox *root, float *out, cudaStream_t s) {
   k_uref<<<1, 1024, 0, s>>>(m, stats, root, out);
   g_launches.fetch_add(1, std::memory_order_relaxed);

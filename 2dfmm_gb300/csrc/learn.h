@@ -38,6 +38,19 @@ struct LeafStats {
   float sig;     // max sigma
 };
 
+// u_ref of the set that leaf cell B belongs to: one per tree, or on a
+// batched tree (m.lev0 > 0) one per set, indexed as the sets' correction
+// radii are (set k of a batch sits in tile (2a, 2b) of the level-lev0 grid,
+// k = b 2^(lev0-1) + a).
+__device__ __forceinline__ int set_of_cell(const MixedView &m, int B) {
+  const int sh = m.level[B] - m.lev0;
+  const unsigned tx = m.ix[B] >> sh, ty = m.iy[B] >> sh;
+  return (int)((ty >> 1) * (1u << (m.lev0 - 1)) + (tx >> 1));
+}
+__device__ __forceinline__ float uref_of(const MixedView &m, const float *uref, int B) {
+  return m.lev0 > 0 ? uref[set_of_cell(m, B)] : uref[0];
+}
+
 // Feature vector of the interaction target leaf B <- source leaf A
 // (kMlpIn floats).  `type` 0 = direct (U) list, 1 = correction (K) list;
 // u_ref = sum|G| / R0.  Features: log distance over the source side, log
@@ -76,6 +89,11 @@ __device__ __forceinline__ void interaction_features(const MixedView &m, const L
 
 int learned_leaf_stats(MixedView &m, LeafStats *stats, cudaStream_t s);
 int learned_uref(MixedView &m, const LeafStats *stats, const RootBox *root, float *out, cudaStream_t s);
+// u_ref of every set of a batched tree (roots[k], out[k] for set k; leaf_lo
+// and leaf_hi are nsets-entry scratch): for each set the same sum, in the
+// same order, that learned_uref forms for the set solved alone.
+int learned_uref_sets(MixedView &m, const LeafStats *stats, const RootBox *roots, int nsets, int *leaf_lo,
+                      int *leaf_hi, float *out, cudaStream_t s);
 
 // Decisions (class per list entry) for all U, K and (w_dec non-null) W
 // entries of every leaf, by the tensor-core network (learn_tc.cu).  A W

@@ -132,7 +132,6 @@ __global__ void __launch_bounds__(kTile) k_mlp_infer(InferArgs a) {
   const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16);
   uint32_t phase = 0;
   const MixedView &m = a.m;
-  const float u_ref = a.u_ref_ptr ? *a.u_ref_ptr : 1.f;
 
   bool mma_inflight = false;
   for (long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
@@ -155,7 +154,7 @@ __global__ void __launch_bounds__(kTile) k_mlp_infer(InferArgs a) {
       const int l = (kind == 0 ? m.u_leaf : (kind == 1 ? m.k_leaf : m.w_leaf))[e];
       const int B = m.leaf_cell[l];
       const int A = kind == 0 ? m.u_idx[e] : (kind == 1 ? m.k_idx[e] : m.w_idx[e]);
-      interaction_features(m, a.st, B, A, kind == 1 ? 1 : 0, u_ref, v);
+      interaction_features(m, a.st, B, A, kind == 1 ? 1 : 0, a.u_ref_ptr ? uref_of(m, a.u_ref_ptr, B) : 1.f, v);
     }
     store_row(act, tid, v, 16);
     // layer 1 .. 4

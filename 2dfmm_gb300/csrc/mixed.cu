@@ -2641,8 +2641,8 @@ int mixed_solve(Workspace &ws, const Tree &t, const MixedParams &mp, double *d_u
   // statistics, not the expansions: they run on a second stream, forked
   // here and joined before the near field, beside the upward pass, M2L and
   // the downward pass (both chains are latency-bound and share the GPU
-  // well).  A batched tree runs the fixed mixed form: the network's
-  // reference scale u_ref is one per tree.
+  // well).  On a batched tree each set has its own reference scale u_ref,
+  // the one it has alone.
   // the network decides only inside its training envelope: denser lists
   // than it was trained on would add up more accepted errors per target
   // than its per-interaction budget allows for.  The density is the K
@@ -2650,13 +2650,13 @@ int mixed_solve(Workspace &ws, const Tree &t, const MixedParams &mp, double *d_u
   // does not depend on the leaf size, which a count of entries would.
   const double k_blobs = (double)ws.h_status->k_blobs;
   const bool in_envelope = mp.lp && (mp.lp->k_blobs_max <= 0.0 || k_blobs <= mp.lp->k_blobs_max * nl);
-  const bool learned = mp.learned && mp.lp && mp.lp->have_weights && t.lev0 == 0 && in_envelope;
+  const bool learned = mp.learned && mp.lp && mp.lp->have_weights && in_envelope;
   st.learned_active = learned ? 1 : 0;
   st.n_list_u = tot[0];
   st.n_list_k = tot[2];
   st.n_list_k_blobs = (long long)ws.h_status->k_blobs;
   unsigned char *u_dec = nullptr, *k_dec = nullptr, *w_dec = nullptr;
-  const bool side = (learned || mp.learned) && t.lev0 == 0;
+  const bool side = learned || mp.learned;
   // after the fork, an early return first waits for the second stream, so
   // that no kernel of this solve still runs when its buffers are reused
   bool forked = false;
@@ -2680,7 +2680,7 @@ int mixed_solve(Workspace &ws, const Tree &t, const MixedParams &mp, double *d_u
     const size_t wim = learn_weight_image_elems();
     size_t need = Arena::bytes_for(wim, 2) + Arena::bytes_for(208, 4) + Arena::bytes_for((size_t)nc, sizeof(LeafStats)) +
                   Arena::bytes_for((size_t)tot[0] + 1, 1) + Arena::bytes_for((size_t)tot[2] + 1, 1) +
-                  Arena::bytes_for((size_t)tot[1] + 1, 1) + 512;
+                  Arena::bytes_for((size_t)tot[1] + 1, 1) + 3 * Arena::bytes_for((size_t)t.nsets, 4) + 512;
     const size_t cap0 = ws.lr_arena.capacity();
     T2D_CUDA_TRY(ws.lr_arena.reserve(need));
     if (ws.lr_arena.capacity() != cap0) ws.lr_version = -1;  // reallocated: weights must be uploaded again
@@ -2691,7 +2691,9 @@ int mixed_solve(Workspace &ws, const Tree &t, const MixedParams &mp, double *d_u
     u_dec = ws.lr_arena.take<unsigned char>((size_t)tot[0] + 1);
     k_dec = ws.lr_arena.take<unsigned char>((size_t)tot[2] + 1);
     w_dec = mp.lp->far_orders ? ws.lr_arena.take<unsigned char>((size_t)tot[1] + 1) : nullptr;
-    float *uref = ws.lr_arena.take<float>(1);
+    float *uref = ws.lr_arena.take<float>((size_t)t.nsets);  // one per set
+    int *set_lo = t.nsets > 1 ? ws.lr_arena.take<int>((size_t)t.nsets) : nullptr;
+    int *set_hi = t.nsets > 1 ? ws.lr_arena.take<int>((size_t)t.nsets) : nullptr;
     if (learned && ws.lr_version != mp.lp_version) {
       std::vector<uint16_t> img;
       std::vector<float> b;
@@ -2706,7 +2708,8 @@ int mixed_solve(Workspace &ws, const Tree &t, const MixedParams &mp, double *d_u
     forked = true;
     rc = learned_leaf_stats(m, stats, s2);
     if (rc) return drain(rc);
-    rc = learned_uref(m, stats, t.root, uref, s2);
+    rc = t.nsets > 1 ? learned_uref_sets(m, stats, t.root, t.nsets, set_lo, set_hi, uref, s2)
+                     : learned_uref(m, stats, t.root, uref, s2);
     if (rc) return drain(rc);
     if (learned) {
       rc = learned_decide(m, stats, uref, wimg, bias, mp.lp->direct_bias, tot[0], tot[2], tot[1], u_dec, k_dec,

@@ -155,8 +155,8 @@ typedef struct {
                               2/3: blobs staged by bulk copies, 4/8)    */
   int learned_active;     /* learned: 1 if the network's decisions were
                              applied, 0 if the solve ran the fixed mixed
-                             form (no weights, a batched tree, or lists
-                             outside the network's training envelope)   */
+                             form (no weights, or lists outside the
+                             network's training envelope)               */
   long long n_list_u;     /* mixed: U (direct) list entries             */
   long long n_list_k;     /* mixed: K (correction) list entries         */
   int leaf_blobs;         /* most blobs per leaf of the tree built        */
@@ -299,7 +299,8 @@ int tree2d_learn_set_envelope(double k_blobs_per_leaf_max, double cutoff_sigmas)
  * up to max_samples interactions drawn with `seed`, their features
  * (features[max][16]) and the cheapest class whose error against the FP64
  * exact contribution stays within the budget.  Returns the sample count,
- * or minus a status code. */
+ * or minus a status code (-TREE2D_ERR_MODE after a batched solve: samples
+ * come from a solve of one set). */
 int tree2d_learn_collect(int max_samples, unsigned seed, float *features, int *labels);
 /* `steps` Adam steps on mini-batches of `batch` samples (host arrays),
  * starting from the loaded weights (or a seeded initialisation). */

@@ -63,6 +63,65 @@ def test_batched_sets_equal_single_solves(gpu_lib):
 
 
 @pytest.mark.gpu
+def test_batched_sets_learned_equal_single_solves(gpu_lib):
+    """The learned mode on a batched tree: each set's decisions use its own
+    reference scale u_ref (the one it has alone), so every set's velocities
+    equal its learned solve alone, bit for bit; the network skips work on
+    the sets with weak sources (the sheets), and the batch keeps relL2 <=
+    1e-6."""
+    torch = pytest.importorskip("torch")
+    import importlib
+    P = gpu_lib
+    W = workloads()
+    L = importlib.import_module("2dfmm_gb300.learn")
+    theta = L.load_weights()
+    if theta is None:
+        pytest.skip("no packaged weights")
+    sets = [W.two_patch_sheet(n, seed=50 + k) for k, n in enumerate((24_000, 41_000, 60_000))]
+    sets += W.batch_sets(nsets=3, seed=43, lo=4096, hi=30_000)
+    b0 = sets[0]
+    P.set_params(b0.nterms, b0.num_p, b0.theta)
+    P.set_mixed_params(16, 2.5, True)
+    P.learn_set_weights(theta)
+    P.learn_set_options(1.0, 1)
+    P.learn_set_envelope(*L.load_envelope())
+    xy, cir, cor, off = _concat(sets)
+    d_xy, d_cir, d_cor = _dev(torch, xy), _dev(torch, cir), _dev(torch, cor)
+    try:
+        pairs = {}
+        for mode in (P.MODE_MIXED, P.MODE_LEARNED):
+            P.set_mode(mode)
+            d_uv = torch.empty_like(d_xy)
+            P.solve_sets(d_xy.data_ptr(), d_cir.data_ptr(), d_cor.data_ptr(), d_uv.data_ptr(), off)
+            torch.cuda.synchronize()
+            pairs[mode] = P.stats()["n_pairs"]
+        assert P.stats()["learned_active"] == 1
+        assert pairs[P.MODE_LEARNED] < pairs[P.MODE_MIXED]
+        uv = d_uv.cpu().numpy()
+        assert np.all(np.isfinite(uv))
+        for k, b in enumerate(sets):
+            s_xy, s_cir, s_cor = _dev(torch, b.xy), _dev(torch, b.cir), _dev(torch, b.cor)
+            s_uv = torch.empty_like(s_xy)
+            P.solve_device(s_xy.data_ptr(), s_cir.data_ptr(), s_cor.data_ptr(), s_uv.data_ptr(), b.n)
+            torch.cuda.synchronize()
+            assert P.stats()["learned_active"] == 1
+            assert np.array_equal(uv[off[k]:off[k + 1]], s_uv.cpu().numpy()), f"set {k} (n={b.n})"
+            # 4,096 sampled targets per set, as configuration 4 measures
+            # (with 512 the estimate of a 24k-blob set's relL2 moved by 40%)
+            idx = W.sample_targets(b.n, 4096, seed=k)
+            txy = s_xy[torch.from_numpy(idx).to(s_xy.device)].contiguous()
+            ref = torch.empty_like(txy)
+            P.direct_device(txy.data_ptr(), len(idx), s_xy.data_ptr(), s_cir.data_ptr(), s_cor.data_ptr(), b.n,
+                            ref.data_ptr())
+            torch.cuda.synchronize()
+            ref = ref.cpu().numpy()
+            got = uv[off[k]:off[k + 1]][idx]
+            assert np.linalg.norm(got - ref) / np.linalg.norm(ref) <= 1e-6, f"set {k}"
+    finally:
+        P.set_mode(P.MODE_PLAIN)
+
+
+@pytest.mark.gpu
 def test_batched_sets_reject_plain_mode_and_bad_offsets(gpu_lib):
     torch = pytest.importorskip("torch")
     P = gpu_lib
