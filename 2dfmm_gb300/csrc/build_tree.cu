@@ -766,6 +766,7 @@ size_t build_cell_bytes(long long ncell, long long nleaf, int nterms) {
   cneed += Arena::bytes_for(ncell, 8) * 3;           // cx cy region
   cneed += Arena::bytes_for(nleaf > 0 ? nleaf : 1, 4);  // leaf_cell
   cneed += Arena::bytes_for(ncell * nterms, 16);     // coef
+  cneed += Arena::bytes_for(ncell, 16);              // mac
   return cneed;
 }
 
@@ -917,6 +918,8 @@ retry:
   t.region = ws.cell_arena.take<double>(ncell);
   t.leaf_cell = ws.cell_arena.take<int>(nleaf > 0 ? nleaf : 1);
   t.coef = ws.cell_arena.take<double2>(ncell * nt);
+  t.mac = ws.cell_arena.take<double2>(ncell);
+  ws.mac_theta = -1.0;
 
   // 7. cells
   EmitArgs ea{t.keys, cpl, leaf_level, part, t.root, n, cellbase, t.level, t.begin, t.leaf, t.cx, t.cy, t.region,

@@ -143,6 +143,8 @@ struct Tree {
   int *level_start = nullptr; // host-built cell lists per level (device copy)
   int *by_level = nullptr;    // cell ids grouped by level
   double2 *coef = nullptr;    // ncell * nterms, FP64 Laurent coefficients
+  double2 *mac = nullptr;     // plain: per cell, the squared distances below / above which
+                              // the opening test surely descends / accepts (k_mac_bounds)
   RootBox *root = nullptr;    // device
   uint64_t *keys = nullptr;   // sorted keys (tree order before in-leaf sort)
   uint8_t *cpl = nullptr;     // per position: levels shared with the next key
@@ -174,6 +176,7 @@ struct Workspace {
   std::map<uint64_t, int> eval_tuned;  // size class -> fastest near-field variant
   std::map<uint64_t, int> m2l_tuned;   // size class -> faster M2L tile rows (64 or 128)
   int last_depth = 0;  // depth of the last tree built (sizes the next keys)
+  double mac_theta = -1.0;  // theta that the tree's Tree::mac bounds were formed for (< 0: none)
   int list_cap = 256;  // entries per leaf of the one-walk list scratch (from the last solve)
   DevStatus *status = nullptr;   // device
   DevStatus *h_status = nullptr; // pinned host mirror

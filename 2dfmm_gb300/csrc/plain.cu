@@ -133,7 +133,6 @@ __global__ void __launch_bounds__(kEvalWarps * 32) k_eval(EvalArgs a) {
   const int nt = a.nt;
   const double x = valid ? a.tx[i] : 0.0, y = valid ? a.ty[i] : 0.0;
   const double theta = a.theta;
-  const double theta2 = __dmul_rn(theta, theta);
   double2 phi = make_double2(0.0, 0.0);
   double ud0 = 0.0, ud1 = 0.0;
   unsigned long long n_m2s = 0, n_pairs = 0;
@@ -221,7 +220,8 @@ __global__ void __launch_bounds__(kEvalWarps * 32) k_eval(EvalArgs a) {
       for (int q = 0; q < 4; q++) {
         const int cc = (&ch.x)[q];
         if (cc < 0) continue;
-        const double ccx = t.cx[cc], ccy = t.cy[cc], creg = t.region[cc];
+        const double ccx = t.cx[cc], ccy = t.cy[cc];
+        const double2 mb = t.mac[cc];
         bool desc = false;
         double dx = 0.0, dy = 0.0;
         double d2 = 0.0;
@@ -230,17 +230,18 @@ __global__ void __launch_bounds__(kEvalWarps * 32) k_eval(EvalArgs a) {
           dy = __dsub_rn(y, ccy);
           d2 = __dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy));
           // The reference's test is region > theta * sqrt(d2), each step
-          // rounded.  Squared, with a relative margin of 1e-13 (the rounding
-          // of either side is below 1e-15), it decides the same way without
-          // the square root; only a test within the margin takes the exact
-          // rounded path.
-          const double c2 = __dmul_rn(creg, creg), q = __dmul_rn(theta2, d2);
-          if (c2 > __dmul_rn(q, 1.0 + 1e-13)) {
+          // rounded.  Squared, region^2 > theta^2 d2, it needs no square
+          // root: below the cell's bound mb.x (region^2 / (theta^2 (1 +
+          // 2e-13))) it surely descends, above mb.y (the same with 1 -
+          // 2e-13) it surely accepts (the roundings of either side and of
+          // the bounds are below 1e-15 relative); only a d2 between the two
+          // takes the exact rounded path.
+          if (d2 < mb.x) {
             desc = true;
-          } else if (c2 < __dmul_rn(q, 1.0 - 1e-13)) {
+          } else if (d2 > mb.y) {
             desc = false;
           } else {
-            desc = creg > __dmul_rn(theta, __dsqrt_rn(d2));
+            desc = t.region[cc] > __dmul_rn(theta, __dsqrt_rn(d2));
           }
         }
         const unsigned dmask = __ballot_sync(0xffffffffu, desc);
@@ -286,6 +287,26 @@ __global__ void __launch_bounds__(kEvalWarps * 32) k_eval(EvalArgs a) {
   }
 }
 
+// The opening test's bounds per cell for a given theta: squared distances
+// d2 with d2 < lo surely have region > theta sqrt(d2) (the cell is opened),
+// d2 > hi surely not (it is accepted), with a relative margin of 2e-13 that
+// covers the roundings of the reference's test and of the bounds.
+__global__ void k_mac_bounds(Tree t, double theta) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= t.ncell) return;
+  const double r2 = t.region[c] * t.region[c], th2 = theta * theta;
+  t.mac[c] = make_double2(r2 / (th2 * (1.0 + 2e-13)), r2 / (th2 * (1.0 - 2e-13)));
+}
+
+cudaError_t mac_bounds(Workspace &ws, const Tree &t, double theta, cudaStream_t s) {
+  if (ws.mac_theta == theta || t.ncell <= 0) return cudaSuccess;
+  k_mac_bounds<<<(t.ncell + 255) / 256, 256, 0, s>>>(t, theta);
+  ::t2d::g_launches.fetch_add(1, std::memory_order_relaxed);
+  const cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) ws.mac_theta = theta;
+  return e;
+}
+
 // Binomial table, uploaded once per device (the table lives in each
 // device's copy of the module).
 bool g_binom_ready[64] = {};
@@ -328,6 +349,7 @@ int plain_upward(Workspace &ws, const Tree &t, const Params &p, cudaStream_t s) 
 int plain_evaluate(Workspace &ws, const Tree &t, const Params &p, int ntgt, const double *tx, const double *ty,
                    const int *out_idx, double *uv, cudaStream_t s) {
   if (ntgt <= 0) return TREE2D_OK;
+  T2D_CUDA_TRY(mac_bounds(ws, t, p.theta, s));
   EvalArgs a{t, p.nterms, p.theta, ntgt, tx, ty, out_idx, uv, ws.status};
   const int warps = (ntgt + 31) / 32;
   k_eval<<<(warps + kEvalWarps - 1) / kEvalWarps, kEvalWarps * 32, 0, s>>>(a);
