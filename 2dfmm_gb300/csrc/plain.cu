@@ -290,12 +290,15 @@ __global__ void __launch_bounds__(kEvalWarps * 32) k_eval(EvalArgs a) {
 // The opening test's bounds per cell for a given theta: squared distances
 // d2 with d2 < lo surely have region > theta sqrt(d2) (the cell is opened),
 // d2 > hi surely not (it is accepted), with a relative margin of 2e-13 that
-// covers the roundings of the reference's test and of the bounds.
+// covers the roundings of the reference's test and of the bounds.  With
+// theta <= 0 the reference's test opens every cell (region > 0 >= theta r):
+// both bounds are +inf.
 __global__ void k_mac_bounds(Tree t, double theta) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= t.ncell) return;
   const double r2 = t.region[c] * t.region[c], th2 = theta * theta;
-  t.mac[c] = make_double2(r2 / (th2 * (1.0 + 2e-13)), r2 / (th2 * (1.0 - 2e-13)));
+  t.mac[c] = theta > 0.0 ? make_double2(r2 / (th2 * (1.0 + 2e-13)), r2 / (th2 * (1.0 - 2e-13)))
+                         : make_double2(INFINITY, INFINITY);
 }
 
 cudaError_t mac_bounds(Workspace &ws, const Tree &t, double theta, cudaStream_t s) {

@@ -26,7 +26,7 @@ from __future__ import annotations
 import numpy as np
 import pytest
 
-from conftest import golden_names, load_golden, oracle, rel_err
+from conftest import golden_names, load_golden, oracle, rel_err, workloads
 
 TOL = 1e-12
 
@@ -139,6 +139,35 @@ def test_single_point_calls_hit_and_miss(gpu_lib):
         u, v = P.biot_tree(*g["txy"][i])
         ref = g["uv"][i]
         assert abs(u - ref[0]) <= TOL * np.linalg.norm(ref) and abs(v - ref[1]) <= TOL * np.linalg.norm(ref)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("theta", [0.0, -0.5, 0.9])
+def test_opening_angle_edge_values_match_oracle(gpu_lib, theta):
+    """The opening test decided against per-cell bounds of the squared
+    distance (k_mac_bounds) takes the reference's branch for any theta: at
+    theta <= 0 the reference opens every cell (region > theta r always), at
+    a large theta it accepts cells close by."""
+    P = gpu_lib
+    b = workloads().uniform(3000, seed=31)
+    P.set_params(b.nterms, b.num_p, theta)
+    P.set_mode(P.MODE_PLAIN)
+    try:
+        P.make_tree(b.xy, b.cir, b.cor)
+        uv = P.biot_tree_batch(b.xy)
+    finally:
+        P.clear_params()
+    O = oracle()
+    o = O.Oracle(b.nterms, b.num_p, theta)
+    o.make_tree(b.xy, b.cir, b.cor)
+    ref = o.biot(b.xy)
+    o.close()
+    sp = O.SparseOracle(b.nterms, b.num_p, theta)
+    sp.make_tree(b.xy, b.cir, b.cor)
+    try:
+        assert_parity(uv, ref, b.xy, lambda t: sp.biot_ext(t, cond=True), label=f"theta {theta}")
+    finally:
+        sp.close()
 
 
 @pytest.mark.gpu
