@@ -147,7 +147,7 @@ __global__ void k_cell_info(MixedView m) {
 // one sub-cell keep their tree order (a stable counting sort: each 32-blob
 // round groups equal sub-cells with __match_any_sync, shared-memory
 // counters hold the running offsets).  Consecutive blobs are then
-// neighbours, so a 32-blob chunk has a small bounding box (the near field
+// neighbours, so a kChunk-blob chunk has a small bounding box (the near field
 // culls correction chunks by it), and the layout depends only on the
 // leaf's own blobs and geometry: a set gets the same layout alone or in a
 // batch.  mperm maps each position to its original blob.  The sub-cell of a
@@ -274,20 +274,23 @@ __global__ void __launch_bounds__(32 * kSetupWarps) k_leaf_setup(MixedView m, co
     }
   }
   __syncwarp();
-  // each 32-blob chunk's bounding box, for the near field's correction cull
+  // each kChunk-blob chunk's bounding box, for the near field's correction
+  // cull: a warp covers 32 / kChunk chunks per round, reduced within
+  // groups of kChunk lanes
   for (int i0 = b; i0 < e; i0 += 32) {  // warp-uniform
     const int i = i0 + lane, o = i - b;
     const bool v = i < e;
     const float2 lc = !v ? make_float2(0.f, 0.f) : (o < kSetupStage ? s_out[warp][o] : m.loc[i]);
     float bx0 = v ? lc.x : INFINITY, by0 = v ? lc.y : INFINITY, bx1 = v ? lc.x : -INFINITY, by1 = v ? lc.y : -INFINITY;
-    for (int sh = 16; sh; sh >>= 1) {
+    for (int sh = kChunk / 2; sh; sh >>= 1) {
       bx0 = fminf(bx0, __shfl_xor_sync(0xffffffffu, bx0, sh));
       by0 = fminf(by0, __shfl_xor_sync(0xffffffffu, by0, sh));
       bx1 = fmaxf(bx1, __shfl_xor_sync(0xffffffffu, bx1, sh));
       by1 = fmaxf(by1, __shfl_xor_sync(0xffffffffu, by1, sh));
     }
-    const int k = (i0 - b) >> 5;
-    if (lane == 0 && k < m.kchunks) m.cbox[(size_t)c * m.kchunks + k] = make_float4(bx0, by0, bx1, by1);
+    const int k = (o >> kChunkShift);  // this lane's chunk
+    if ((lane & (kChunk - 1)) == 0 && v && k < m.kchunks)
+      m.cbox[(size_t)c * m.kchunks + k] = make_float4(bx0, by0, bx1, by1);
   }
 }
 
@@ -1512,7 +1515,7 @@ __device__ __forceinline__ void counts_flush(WarpCounts *c, int lane, DevStatus 
   }
 }
 
-// The next run of consecutive source chunks (32 blobs each, bit k of a mask
+// The next run of consecutive source chunks (kChunk blobs each, bit k of a mask
 // for chunk k of a leaf of cnt blobs) kept for the same target packs: r0
 // and r1 are the chunks kept for pack 0 and pack 1, kAllChunks for both the
 // whole leaf.  Returns blobs [s0, s1) and the packs (bit 0: pack 0, bit 1:
@@ -1529,8 +1532,8 @@ __device__ __forceinline__ int next_run(unsigned &r0, unsigned &r1, int cnt, int
   const unsigned same = ((packs & 1) ? r0 : ~r0) & ((packs & 2) ? r1 : ~r1);
   const unsigned gap = ~(same >> a);
   const int len = gap ? __ffs(gap) - 1 : 32 - a;
-  s0 = a << 5;
-  s1 = min(cnt, (a + len) << 5);
+  s0 = a << kChunkShift;
+  s1 = min(cnt, (a + len) << kChunkShift);
   const unsigned run = a + len >= 32 ? ~0u << a : ((1u << len) - 1u) << a;
   r0 &= ~run;
   r1 &= ~run;
@@ -1538,7 +1541,7 @@ __device__ __forceinline__ int next_run(unsigned &r0, unsigned &r1, int cnt, int
 }
 
 // Chunks of correction source leaf A whose pairs with a pack of targets can
-// lie within the correction radius: bit k of *m0 (*m1) for the 32-blob chunk
+// lie within the correction radius: bit k of *m0 (*m1) for the kChunk-blob chunk
 // k of A whose bounding box comes within rc of pack 0's (pack 1's) target
 // box, tb[0..3] (tb[4..7]), rc^2 in tb[8]; the boxes are offsets from the
 // target leaf's centre, (ox, oy) is A's centre seen from there.  Pairs
@@ -1548,7 +1551,7 @@ __device__ __forceinline__ int next_run(unsigned &r0, unsigned &r1, int cnt, int
 template <int kPacks>
 __device__ __forceinline__ void chunk_mask(const MixedView &m, int A, float ox, float oy, const float *tb, int lane,
                                            unsigned &m0, unsigned &m1) {
-  const int nch = (m.end[A] - m.begin[A] + 31) >> 5;
+  const int nch = (m.end[A] - m.begin[A] + kChunk - 1) >> kChunkShift;
   if (nch > 32 || nch > m.kchunks) {
     m0 = m1 = kAllChunks;
     return;
@@ -2481,7 +2484,7 @@ int mixed_solve(Workspace &ws, const Tree &t, const MixedParams &mp, double *d_u
   need += Arena::bytes_for(n, 8);                 // loc
   need += Arena::bytes_for(n, 16) + Arena::bytes_for(nc, 4) * 4;  // src4, cxf, cyf, cxl, cyl
   need += Arena::bytes_for(n, 16) + Arena::bytes_for(nc, 4);      // src4s, lscale
-  const int kchunks = t.leaf_cap > 0 ? (t.leaf_cap + 31) / 32 : 1;
+  const int kchunks = t.leaf_cap > 0 ? (t.leaf_cap + kChunk - 1) / kChunk : 1;
   need += Arena::bytes_for((size_t)nc * kchunks, 16);              // chunk boxes
   need += Arena::bytes_for(n, 4);                                  // mperm
   need += Arena::bytes_for((size_t)nc * 9, 4) * 2;

@@ -10,6 +10,12 @@ namespace t2d {
 constexpr int kMaxP = 32;  // largest expansion length of the mixed form
 
 // Everything the mixed kernels read or write, by value into each kernel.
+// Blobs per chunk of a leaf for the near field's correction cull: each
+// chunk has a bounding box, and a correction leaf's chunks farther than the
+// correction radius from a pack of targets are skipped.
+constexpr int kChunkShift = 4;
+constexpr int kChunk = 1 << kChunkShift;
+
 struct MixedView {
   int n, ncell, nleaf, P;
   const float *rc_ptr;  // device: cutoff radius of the regularisation correction
@@ -39,7 +45,7 @@ struct MixedView {
                          // mixed form hold each leaf's blobs by sub-cell (8 x 8 sub-cells in
                          // Morton order, tree order inside one), not in the tree's order
   float4 *cbox;          // per leaf cell, kchunks entries: bounding box {xmin, ymin, xmax, ymax}
-                         // of each 32-blob chunk of the leaf (from its first blob), leaf-local
+                         // of each kChunk-blob chunk of the leaf (from its first blob), leaf-local
   int kchunks;           // chunk boxes per cell: ceil(most blobs per leaf / 32)
   float *cxf, *cyf;      // per cell, FP32 centre (rounded)
   float *cxl, *cyl;      // per cell, the rest: centre - (double)cxf, in FP32

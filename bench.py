@@ -502,7 +502,7 @@ def run_ours(args):
                                  "correction_k": st["n_pairs_k"] / n,
                                  "correction_k_listed": st["n_pairs_k_listed"] / n,
                                  "note": "correction pairs of the K leaves evaluated, after and before skipping "
-                                         "32-blob chunks farther than the correction radius from the targets"},
+                                         "16-blob chunks farther than the correction radius from the targets"},
             "clocks": clocks,
         }
         line.update(beside)

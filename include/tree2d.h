@@ -166,7 +166,7 @@ typedef struct {
   long long n_pairs_k;    /* mixed: correction pairs evaluated (part of
                              n_pairs; the rest are direct U pairs)      */
   long long n_pairs_k_listed; /* mixed: pairs of the correction entries
-                             evaluated, before 32-blob chunks farther than
+                             evaluated, before 16-blob chunks farther than
                              the correction radius were skipped          */
   int m2l_rows;           /* mixed, tensor-core M2L: cells per CTA of the
                              solve (128 or 64)                          */
