@@ -219,7 +219,8 @@ __global__ void __launch_bounds__(kThreads) k_hist_all(const uint64_t *__restric
     for (int p = 0; p < passes; p++) {
       // a shared-memory add per element: lanes that hit the same digit
       // serialise on it, which measured cheaper than grouping equal digits
-      // with __match_any_sync first (0.02 against 0.096 ms at 4M words)
+      // with __match_any_sync first (the 4M-blob build took 0.68 against
+      // 0.76 ms; the grouped form's histogram alone was 0.096 ms)
       const unsigned d = (unsigned)(w >> (begin_bit + 8 * p)) & 0xffu;
       if (valid) atomicAdd(&h[p][d], 1u);
     }
