@@ -693,7 +693,52 @@ __global__ void __launch_bounds__(256) k_children(const uint64_t *__restrict__ k
   reinterpret_cast<int4 *>(child)[c] = ch;
 }
 
-// One warp per leaf: blobs of the leaf in ascending original index.
+// A warp's 32 K values (element k * 32 + lane in v[k] of that lane) sorted
+// ascending by a bitonic network: partners within a lane's column by
+// shuffles, across its registers by exchanges.  Fully unrolled, so v stays
+// in registers.
+template <int K>
+__device__ __forceinline__ void warp_bitonic_sort(uint32_t (&v)[K], int lane) {
+  constexpr int N = 32 * K;
+#pragma unroll
+  for (int size = 2; size <= N; size <<= 1) {
+#pragma unroll
+    for (int stride = size >> 1; stride > 0; stride >>= 1) {
+      uint32_t p[K];
+#pragma unroll
+      for (int k = 0; k < K; k++)
+        p[k] = stride < 32 ? __shfl_xor_sync(0xffffffffu, v[k], stride) : v[k ^ (stride >> 5)];
+#pragma unroll
+      for (int k = 0; k < K; k++) {
+        const int i = k * 32 + lane;
+        const bool up = (i & size) == 0, low = (i & stride) == 0;
+        v[k] = low == up ? min(v[k], p[k]) : max(v[k], p[k]);
+      }
+    }
+  }
+}
+
+// Blobs of leaf [b, e) in ascending original index (the values are the
+// indices, all different): a bitonic sort in registers for up to 32 K.
+template <int K>
+__device__ __forceinline__ void leaf_sort(const uint32_t *__restrict__ vals, int b, int e, int lane,
+                                          int *__restrict__ perm) {
+  uint32_t v[K];
+#pragma unroll
+  for (int k = 0; k < K; k++) {
+    const int i = b + k * 32 + lane;
+    v[k] = i < e ? vals[i] : 0xffffffffu;  // padding sorts last
+  }
+  warp_bitonic_sort<K>(v, lane);
+#pragma unroll
+  for (int k = 0; k < K; k++) {
+    const int i = b + k * 32 + lane;
+    if (i < e) perm[i] = (int)v[k];
+  }
+}
+
+// One warp per leaf: blobs of the leaf in ascending original index (leaves
+// of more than 128 blobs by counting, for each blob, the smaller ones).
 __global__ void __launch_bounds__(256) k_leaf_order(const uint32_t *__restrict__ vals, int nleaf,
                                                     const int *__restrict__ leaf_cell, const int *__restrict__ begin,
                                                     const int *__restrict__ end, int *__restrict__ perm) {
@@ -702,11 +747,20 @@ __global__ void __launch_bounds__(256) k_leaf_order(const uint32_t *__restrict__
   if (wid >= nleaf) return;
   int c = leaf_cell[wid];
   int b = begin[c], e = end[c];
-  for (int i = b + lane; i < e; i += 32) {
-    uint32_t v = vals[i];
-    int rank = 0;
-    for (int j = b; j < e; j++) rank += vals[j] < v;
-    perm[b + rank] = (int)v;
+  const int cnt = e - b;
+  if (cnt <= 32) {
+    leaf_sort<1>(vals, b, e, lane, perm);
+  } else if (cnt <= 64) {
+    leaf_sort<2>(vals, b, e, lane, perm);
+  } else if (cnt <= 128) {
+    leaf_sort<4>(vals, b, e, lane, perm);
+  } else {
+    for (int i = b + lane; i < e; i += 32) {
+      uint32_t v = vals[i];
+      int rank = 0;
+      for (int j = b; j < e; j++) rank += vals[j] < v;
+      perm[b + rank] = (int)v;
+    }
   }
 }
 

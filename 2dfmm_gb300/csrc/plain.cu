@@ -50,6 +50,7 @@ __device__ __forceinline__ double2 cfma(double2 a, double2 b, double2 c) {
 __constant__ double c_binom[kMaxTerms][kMaxTerms];
 
 constexpr double kPi = 3.14159265358979323846;
+constexpr double kInv2Pi = 0.15915494309189533577;  // 1 / (2 pi), rounded
 
 __global__ void __launch_bounds__(256) k_s2m(Tree t, int nt) {
   const int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -208,8 +209,10 @@ __global__ void __launch_bounds__(kEvalWarps * 32) k_eval(EvalArgs a) {
             ay = __fma_rn(f, rx, ay);
           }
         }
-        ud0 += 0.5 * ax / kPi;
-        ud1 += 0.5 * ay / kPi;
+        // the reference adds 0.5 ax / pi per leaf (fmm.c:140-141); a product
+        // by 1/(2 pi) instead of the FP64 division (an ulp apart)
+        ud0 = __dadd_rn(ud0, __dmul_rn(ax, kInv2Pi));
+        ud1 = __dadd_rn(ud1, __dmul_rn(ay, kInv2Pi));
         n_pairs += (unsigned long long)(e - b);
       }
     } else {
