@@ -267,7 +267,6 @@ __global__ void __launch_bounds__(32 * kSetupWarps) k_leaf_setup(MixedView m, co
       // the correctly rounded reciprocal is 1.f / (sf * sf) exactly
       const float sf = (float)cor[i];
       const float w = __frcp_rn(sf * sf);
-      m.s2inv[d] = w;
       m.src4[d] = make_float4(lc.x, lc.y, g, -1.44269504f * w);
       if (uniform) m.src4s[d] = make_float4(__fmul_rn(lc.x, sc), __fmul_rn(lc.y, sc), __fmul_rn(g, sc), 0.f);
       m.mperm[d] = perm[i];
@@ -2480,7 +2479,7 @@ int mixed_solve(Workspace &ws, const Tree &t, const MixedParams &mp, double *d_u
   // ---- arrays
   size_t need = 0;
   need += Arena::bytes_for(nc, 4) * 5;            // ix iy h inv_h parent
-  need += Arena::bytes_for(n, 4) * 4;             // leaf_of gam s2inv + pad
+  need += Arena::bytes_for(n, 4) * 3;             // leaf_of gam + pad
   need += Arena::bytes_for(n, 8);                 // loc
   need += Arena::bytes_for(n, 16) + Arena::bytes_for(nc, 4) * 4;  // src4, cxf, cyf, cxl, cyl
   need += Arena::bytes_for(n, 16) + Arena::bytes_for(nc, 4);      // src4s, lscale
@@ -2532,7 +2531,6 @@ int mixed_solve(Workspace &ws, const Tree &t, const MixedParams &mp, double *d_u
   m.leaf_of = ws.mx_arena.take<int>(n);
   m.loc = ws.mx_arena.take<float2>(n);
   m.gam = ws.mx_arena.take<float>(n);
-  m.s2inv = ws.mx_arena.take<float>(n);
   m.src4 = ws.mx_arena.take<float4>(n);
   m.src4s = ws.mx_arena.take<float4>(n);
   m.lscale = ws.mx_arena.take<float>(nc);

@@ -36,7 +36,7 @@ struct MixedView {
   int *parent;
   int *leaf_of;          // per position
   float2 *loc;           // per position, offset from its leaf centre
-  float *gam, *s2inv;    // per position
+  float *gam;            // per position: circulation
   float4 *src4;          // per position {loc.x, loc.y, G, -log2(e)/sigma^2}
   float4 *src4s;         // per position of a leaf with one core radius: {loc.x s, loc.y s, G s, 0},
                          // s = sqrt(log2 e) / sigma (the near field's scaled records)
