@@ -109,6 +109,7 @@ __global__ void __launch_bounds__(256) k_m2m(Tree t, int nt, int lev) {
 constexpr int kEvalWarps = 4;
 constexpr int kStackCap = 160;
 constexpr int kQueue = 32;  // deferred M2S cells per lane
+constexpr int kLeafQueue = 16;  // deferred direct (P2P) leaves per lane
 
 struct EvalArgs {
   Tree t;
@@ -125,6 +126,7 @@ __global__ void __launch_bounds__(kEvalWarps * 32) k_eval(EvalArgs a) {
   __shared__ int s_cell[kEvalWarps][kStackCap];
   __shared__ unsigned s_mask[kEvalWarps][kStackCap];
   __shared__ int s_queue[kEvalWarps][kQueue][32];
+  __shared__ int s_leaves[kEvalWarps][kLeafQueue][32];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const long i = ((long)blockIdx.x * kEvalWarps + warp) * 32 + lane;
   const bool valid = i < a.ntgt;
@@ -172,6 +174,70 @@ __global__ void __launch_bounds__(kEvalWarps * 32) k_eval(EvalArgs a) {
     nq = 0;
   };
 
+  // The direct sums are deferred the same way: a leaf reached by some of
+  // the warp's lanes would keep the others idle for its whole pair loop,
+  // and on this GPU an FP64 warp instruction takes the pipe for its full
+  // width whatever the lanes.  Each lane queues its leaves
+  // (s_leaves[warp][k][lane]) and the warp walks the queues together, one
+  // pair per lane per step, each lane through its own leaves in its own
+  // order.  A lane's pairs reach ax/ay and its leaf sums reach ud0/ud1 in
+  // the order and with the operations of an immediate evaluation, so the
+  // results are the same bit for bit.
+  int nl = 0;
+  auto flush_leaves = [&]() {
+    int q = 0, j = 0, e = 0;
+    double ax = 0.0, ay = 0.0;
+    if (nl > 0) {
+      const int c0 = s_leaves[warp][0][lane];
+      j = t.begin[c0];
+      e = t.end[c0];
+    }
+    // closes the leaves whose pairs are done (empty ones too) and opens the
+    // next: the reference adds 0.5 ax / pi per leaf (fmm.c:140-141); a
+    // product by 1/(2 pi) instead of the FP64 division (an ulp apart)
+    auto settle = [&]() {
+      while (q < nl && j >= e) {
+        ud0 = __dadd_rn(ud0, __dmul_rn(ax, kInv2Pi));
+        ud1 = __dadd_rn(ud1, __dmul_rn(ay, kInv2Pi));
+        ax = 0.0;
+        ay = 0.0;
+        if (++q < nl) {
+          const int cq = s_leaves[warp][q][lane];
+          j = t.begin[cq];
+          e = t.end[cq];
+        }
+      }
+    };
+    settle();
+    while (__any_sync(0xffffffffu, q < nl)) {
+      if (q < nl) {
+        // direct_evaluate, fmm.c:121-142
+        const double rx = __dsub_rn(x, t.x[j]);
+        const double ry = __dsub_rn(y, t.y[j]);
+        // The reference forms r = sqrt(r2), (r/sigma)^2 and 1/(r*r); here
+        // r2 and r2/sigma^2 (with 1/sigma^2 precomputed per blob) give the
+        // same quantities within an ulp or two and save the square root
+        // and a division per pair.  r > 1e-10 <=> r2 > 1e-20.
+        const double r2 = __dadd_rn(__dmul_rn(rx, rx), __dmul_rn(ry, ry));
+        if (r2 > 1.0e-20) {
+          const double rv2 = rcp_nr(r2);
+          const double x2 = __dmul_rn(r2, t.icor2[j]);
+          // 1 - exp(-x2) rounds to exactly 1.0 once exp(-x2) < 2^-54
+          // (x2 > 37.4); the shortcut keeps the result bit-identical.
+          const double e1 = x2 > 40.0 ? 1.0 : 1.0 - exp(-x2);
+          // G (1 - e) / r^2 once, then one FMA per component
+          const double f = __dmul_rn(__dmul_rn(t.cir[j], e1), rv2);
+          ax = __fma_rn(-f, ry, ax);
+          ay = __fma_rn(f, rx, ay);
+        }
+        n_pairs++;
+        j++;
+        settle();
+      }
+    }
+    nl = 0;
+  };
+
   int top = 0;
   if (lane == 0) {
     s_cell[warp][0] = 0;
@@ -185,36 +251,8 @@ __global__ void __launch_bounds__(kEvalWarps * 32) k_eval(EvalArgs a) {
     top--;
     const bool act = (m >> lane) & 1u;
     if (t.leaf[c]) {
-      // direct_evaluate, fmm.c:121-142
-      const int b = t.begin[c], e = t.end[c];
-      if (act) {
-        double ax = 0.0, ay = 0.0;
-        for (int j = b; j < e; j++) {
-          const double rx = __dsub_rn(x, t.x[j]);
-          const double ry = __dsub_rn(y, t.y[j]);
-          // The reference forms r = sqrt(r2), (r/sigma)^2 and 1/(r*r); here
-          // r2 and r2/sigma^2 (with 1/sigma^2 precomputed per blob) give the
-          // same quantities within an ulp or two and save the square root
-          // and a division per pair.  r > 1e-10 <=> r2 > 1e-20.
-          const double r2 = __dadd_rn(__dmul_rn(rx, rx), __dmul_rn(ry, ry));
-          if (r2 > 1.0e-20) {
-            const double rv2 = rcp_nr(r2);
-            const double x2 = __dmul_rn(r2, t.icor2[j]);
-            // 1 - exp(-x2) rounds to exactly 1.0 once exp(-x2) < 2^-54
-            // (x2 > 37.4); the shortcut keeps the result bit-identical.
-            const double e1 = x2 > 40.0 ? 1.0 : 1.0 - exp(-x2);
-            // G (1 - e) / r^2 once, then one FMA per component
-            const double f = __dmul_rn(__dmul_rn(t.cir[j], e1), rv2);
-            ax = __fma_rn(-f, ry, ax);
-            ay = __fma_rn(f, rx, ay);
-          }
-        }
-        // the reference adds 0.5 ax / pi per leaf (fmm.c:140-141); a product
-        // by 1/(2 pi) instead of the FP64 division (an ulp apart)
-        ud0 = __dadd_rn(ud0, __dmul_rn(ax, kInv2Pi));
-        ud1 = __dadd_rn(ud1, __dmul_rn(ay, kInv2Pi));
-        n_pairs += (unsigned long long)(e - b);
-      }
+      if (__any_sync(0xffffffffu, nl == kLeafQueue)) flush_leaves();
+      if (act) s_leaves[warp][nl++][lane] = c;
     } else {
       // a cell's four children can add four entries to a lane's queue
       if (__any_sync(0xffffffffu, nq > kQueue - 4)) flush();
@@ -267,6 +305,7 @@ __global__ void __launch_bounds__(kEvalWarps * 32) k_eval(EvalArgs a) {
     }
   }
   flush();
+  flush_leaves();
   if (__any_sync(0xffffffffu, overflow)) {
     if (lane == 0) set_err(a.st, TREE2D_ERR_TIMEOUT);
   }
