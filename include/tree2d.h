@@ -279,8 +279,9 @@ int tree2d_learn_set_options(float direct_bias, int order_margin, double budget)
  * source keep the full order.  on = 0 (default): every W entry at the full
  * order.  Off by default: with the packaged network it saved no time at
  * 4M two-patch + sheet blobs (7.43 against 7.41 ms per solve) and 0.4% at
- * 1M Lamb-Oseen blobs, and a network trained only briefly let relL2 pass
- * 1e-6 with it.  No counterpart in the reference. */
+ * 1M Lamb-Oseen blobs, and with it relL2 passes 1e-6 (packaged network:
+ * 1.2e-6 at 262,144 two-patch + sheet blobs).  No counterpart in the
+ * reference. */
 int tree2d_learn_set_far_orders(int on);
 /* Training envelope of the loaded network: the largest mean number of
  * source blobs in a leaf's K (correction) list leaves that the training
