@@ -109,6 +109,7 @@ __global__ void __launch_bounds__(256) k_m2m(Tree t, int nt, int lev) {
 constexpr int kEvalWarps = 4;
 constexpr int kStackCap = 160;
 constexpr int kQueue = 32;  // deferred M2S cells per lane
+static_assert((kQueue & (kQueue - 1)) == 0, "the M2S queues are rings indexed by a mask");
 constexpr int kLeafQueue = 16;  // deferred direct (P2P) leaves per lane
 
 struct EvalArgs {
@@ -149,14 +150,22 @@ __global__ void __launch_bounds__(kEvalWarps * 32) k_eval(EvalArgs a) {
   // A lane's M2S terms still reach phi in its own acceptance order, each
   // with the same operations (dx, dy, d2 formed again from the cell's
   // centre, bit for bit), and the direct terms go to ud0/ud1 as before.
-  int nq = 0;
-  auto flush = [&]() {
-    int rounds = nq;
-    for (int o = 16; o; o >>= 1) rounds = max(rounds, __shfl_xor_sync(0xffffffffu, rounds, o));
+  // The queues are rings (head qh, count nq).  A flush when some lane's
+  // queue could overflow evaluates only as many rounds as every lane can
+  // fill, or as the fullest lane needs to make room for four entries, if
+  // that is more; the end of the traversal empties them all.
+  int qh = 0, nq = 0;
+  auto flush = [&](bool all) {
+    int hi = nq, lo = nq;
+    for (int o = 16; o; o >>= 1) {
+      hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+      lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+    }
+    const int rounds = all ? hi : max(lo, hi - (kQueue - 4));
     for (int r = 0; r < rounds; r++) {
       if (r < nq) {
         // M2S, fmm.c:60-67: sum_{k<nt-1} a_k w^{k+1}, w = 1/(z - zc)
-        const int cc = s_queue[warp][r][lane];
+        const int cc = s_queue[warp][(qh + r) & (kQueue - 1)][lane];
         const double dx = __dsub_rn(x, t.cx[cc]);
         const double dy = __dsub_rn(y, t.cy[cc]);
         const double d2 = __dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy));
@@ -171,7 +180,9 @@ __global__ void __launch_bounds__(kEvalWarps * 32) k_eval(EvalArgs a) {
         phi = cfma(acc, w, phi);
       }
     }
-    nq = 0;
+    const int done = min(rounds, nq);
+    qh = (qh + done) & (kQueue - 1);
+    nq -= done;
   };
 
   // The direct sums are deferred the same way: a leaf reached by some of
@@ -255,7 +266,7 @@ __global__ void __launch_bounds__(kEvalWarps * 32) k_eval(EvalArgs a) {
       if (act) s_leaves[warp][nl++][lane] = c;
     } else {
       // a cell's four children can add four entries to a lane's queue
-      if (__any_sync(0xffffffffu, nq > kQueue - 4)) flush();
+      if (__any_sync(0xffffffffu, nq > kQueue - 4)) flush(false);
       const int4 ch = reinterpret_cast<const int4 *>(t.child)[c];
 #pragma unroll 1
       for (int q = 0; q < 4; q++) {
@@ -286,7 +297,7 @@ __global__ void __launch_bounds__(kEvalWarps * 32) k_eval(EvalArgs a) {
           }
         }
         const unsigned dmask = __ballot_sync(0xffffffffu, desc);
-        if (act && !desc && nt >= 2) s_queue[warp][nq++][lane] = cc;
+        if (act && !desc && nt >= 2) s_queue[warp][(qh + nq++) & (kQueue - 1)][lane] = cc;
         if (act && !desc) n_m2s++;
         if (dmask) {
           if (top + 1 >= kStackCap) {
@@ -304,7 +315,7 @@ __global__ void __launch_bounds__(kEvalWarps * 32) k_eval(EvalArgs a) {
       if (__any_sync(0xffffffffu, overflow)) break;
     }
   }
-  flush();
+  flush(true);
   flush_leaves();
   if (__any_sync(0xffffffffu, overflow)) {
     if (lane == 0) set_err(a.st, TREE2D_ERR_TIMEOUT);

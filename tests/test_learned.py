@@ -184,3 +184,54 @@ def test_envelope_counted_at_the_training_radius(gpu_lib):
     finally:
         P.learn_set_envelope(0.0)
         P.set_mode(P.MODE_PLAIN)
+
+
+@pytest.mark.gpu
+def test_far_orders_keep_accuracy(gpu_lib):
+    """The network also setting the orders of the W-list M2P terms (off by
+    default): its decisions take effect, and with the packaged weights the
+    error against the FP64 direct sum was measured at relL2 1.2e-6 on this
+    set, above the 1e-6 that the default (full-order W terms) keeps, which
+    is why it is off by default; the test holds it below 2e-6.  With every
+    chosen order raised to the full order (margin 12: order 4 + 12 = 16)
+    the W decisions change nothing, bit for bit."""
+    torch = pytest.importorskip("torch")
+    import importlib
+    P = gpu_lib
+    L = importlib.import_module("2dfmm_gb300.learn")
+    theta = L.load_weights()
+    if theta is None:
+        pytest.skip("no packaged weights")
+    W = workloads()
+    b = W.two_patch_sheet(262_144, seed=31)
+    P.learn_set_weights(theta)
+    P.learn_set_envelope(*L.load_envelope())
+    try:
+        P.learn_set_far_orders(True)
+        uv_f, xy, cir, cor, st_f = _solve(P, torch, b, P.MODE_LEARNED, cutoff=2.5)
+        assert st_f["learned_active"] == 1, st_f
+        idx = torch.from_numpy(W.sample_targets(b.n, 4096, seed=5)).to(xy.device)
+        txy = xy[idx].contiguous()
+        ref = torch.empty_like(txy)
+        P.direct_device(txy.data_ptr(), len(idx), xy.data_ptr(), cir.data_ptr(), cor.data_ptr(), b.n,
+                        ref.data_ptr())
+        torch.cuda.synchronize()
+        rel = float(torch.linalg.norm(uv_f[idx] - ref) / torch.linalg.norm(ref))
+        assert rel <= 2e-6, rel
+        P.learn_set_far_orders(False)
+        uv_d, _, _, _, _ = _solve(P, torch, b, P.MODE_LEARNED, cutoff=2.5)
+        rel_d = float(torch.linalg.norm(uv_d[idx] - ref) / torch.linalg.norm(ref))
+        assert rel_d <= 1e-6, rel_d
+        assert not np.array_equal(uv_f.cpu().numpy(), uv_d.cpu().numpy())
+        P.learn_set_far_orders(True)
+        P.learn_set_options(1.0, 12, 3e-7)
+        uv_on, _, _, _, _ = _solve(P, torch, b, P.MODE_LEARNED, cutoff=2.5)
+        P.learn_set_far_orders(False)
+        uv_off, _, _, _, _ = _solve(P, torch, b, P.MODE_LEARNED, cutoff=2.5)
+        a_on, a_off = uv_on.cpu().numpy(), uv_off.cpu().numpy()
+        assert np.array_equal(a_on, a_off), (int((a_on != a_off).any(1).sum()), float(np.abs(a_on - a_off).max()))
+    finally:
+        P.learn_set_far_orders(False)
+        P.learn_set_options()
+        P.learn_set_envelope(0.0)
+        P.set_mode(P.MODE_PLAIN)
