@@ -153,7 +153,9 @@ __global__ void k_cell_info(MixedView m) {
 // batch.  mperm maps each position to its original blob.  The sub-cell of a
 // blob comes from its FP32 offset; the offsets and sub-cells of a leaf's
 // first kSetupStage blobs are kept in shared memory between the passes
-// (larger leaves form the rest again from global memory).
+// (larger leaves form the rest again from global memory).  Each warp's leaf
+// is a chain of dependent loads, so the kernel is bounded to 32 registers:
+// 64 warps per SM (measured 16.36 -> 16.32 ms for the 512-set batch).
 constexpr int kSubCells = 64;
 constexpr int kSetupWarps = 8;
 constexpr int kSetupStage = 128;
@@ -164,7 +166,7 @@ __device__ __forceinline__ unsigned spread3(unsigned v) {  // 3 bits -> even bit
   return v;
 }
 
-__global__ void __launch_bounds__(32 * kSetupWarps) k_leaf_setup(MixedView m, const double *x, const double *y,
+__global__ void __launch_bounds__(32 * kSetupWarps, 8) k_leaf_setup(MixedView m, const double *x, const double *y,
                                                                  const double *cir, const double *cor,
                                                                  const int *perm) {
   __shared__ int s_cnt[kSetupWarps][kSubCells];
