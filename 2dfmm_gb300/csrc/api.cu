@@ -747,7 +747,9 @@ const char *tree2d_error_string(int code) {
   switch (code) {
     case TREE2D_OK: return "ok";
     case TREE2D_ERR_PARAM_FILE: return "could not read ../cal_cond/fmm_param.dat and no parameters were set";
-    case TREE2D_ERR_BAD_PARAMS: return "invalid parameters (need 0<=nterms<=32, 2<=num_p<=65536, finite theta)";
+    case TREE2D_ERR_BAD_PARAMS:
+      return "invalid parameters: an argument outside the range its call documents (tree2d_set_params: "
+             "0<=nterms<=32, 2<=num_p<=65536, finite theta)";
     case TREE2D_ERR_BAD_INPUT: return "invalid input (negative count, null array, or non-finite value)";
     case TREE2D_ERR_TOO_DEEP: return "tree deeper than 32 levels (>= num_p coincident blobs?)";
     case TREE2D_ERR_CUDA: {
@@ -758,8 +760,8 @@ const char *tree2d_error_string(int code) {
     }
     case TREE2D_ERR_NO_TREE: return "no valid tree (make_tree not called or failed)";
     case TREE2D_ERR_NO_DEVICE: return "no CUDA device";
-    case TREE2D_ERR_TIMEOUT: return "a bounded device loop gave up (traversal stack overflow)";
-    case TREE2D_ERR_MODE: return "unknown or unavailable mode";
+    case TREE2D_ERR_TIMEOUT: return "a bounded device loop gave up (a traversal stack overflow or a wait past its limit)";
+    case TREE2D_ERR_MODE: return "unknown mode, or a call the mode or settings in force do not support";
     case TREE2D_ERR_FILE: return "could not read the file, or it is not a weights file of this version";
     case TREE2D_ERR_TOO_LARGE:
       return "problem too large for this path (the fixed scratch of tree2d_solve_device_static: 65536 blobs, "

@@ -50,14 +50,17 @@ void biot_tree(double x, double y, double *u, double *v);
 /* Status codes (tree2d_last_error). */
 #define TREE2D_OK 0
 #define TREE2D_ERR_PARAM_FILE 1    /* parameter file missing and no override      */
-#define TREE2D_ERR_BAD_PARAMS 2    /* nterms < 2, nterms > 32, num_p < 2, theta<=0 */
+#define TREE2D_ERR_BAD_PARAMS 2    /* an argument outside its call's range; for
+                                      tree2d_set_params: nterms outside 0..32, num_p
+                                      outside 2..65536, or a non-finite theta       */
 #define TREE2D_ERR_BAD_INPUT 3     /* n < 0, or non-finite position/cir/cor        */
 #define TREE2D_ERR_TOO_DEEP 4      /* >= num_p blobs share one cell at level 32    */
 #define TREE2D_ERR_CUDA 5          /* CUDA runtime or kernel failure               */
 #define TREE2D_ERR_NO_TREE 6       /* evaluation requested before a valid tree     */
 #define TREE2D_ERR_NO_DEVICE 7     /* no CUDA device                               */
 #define TREE2D_ERR_TIMEOUT 8       /* a bounded device loop gave up                */
-#define TREE2D_ERR_MODE 9          /* unknown mode                                 */
+#define TREE2D_ERR_MODE 9          /* unknown mode, or a call that the mode or the
+                                      settings in force do not support              */
 #define TREE2D_ERR_TOO_LARGE 10    /* beyond the fixed scratch of the static solve,
                                       or more than 2^31 - 1 interaction-list entries */
 #define TREE2D_ERR_FILE 11         /* a file could not be read or has the wrong format */
