@@ -821,6 +821,8 @@ size_t build_cell_bytes(long long ncell, long long nleaf, int nterms) {
   cneed += Arena::bytes_for(nleaf > 0 ? nleaf : 1, 4);  // leaf_cell
   cneed += Arena::bytes_for(ncell * nterms, 16);     // coef
   cneed += Arena::bytes_for(ncell, 16);              // mac
+  cneed += Arena::bytes_for(ncell, 16);              // cf32
+  cneed += Arena::bytes_for(ncell, 8);               // macf
   return cneed;
 }
 
@@ -973,6 +975,8 @@ retry:
   t.leaf_cell = ws.cell_arena.take<int>(nleaf > 0 ? nleaf : 1);
   t.coef = ws.cell_arena.take<double2>(ncell * nt);
   t.mac = ws.cell_arena.take<double2>(ncell);
+  t.cf32 = ws.cell_arena.take<float4>(ncell);
+  t.macf = ws.cell_arena.take<float2>(ncell);
   ws.mac_theta = -1.0;
 
   // 7. cells

@@ -145,6 +145,8 @@ struct Tree {
   double2 *coef = nullptr;    // ncell * nterms, FP64 Laurent coefficients
   double2 *mac = nullptr;     // plain: per cell, the squared distances below / above which
                               // the opening test surely descends / accepts (k_mac_bounds)
+  float4 *cf32 = nullptr;     // plain: per cell, the centre as FP32 pairs (cx hi, cx lo, cy hi, cy lo)
+  float2 *macf = nullptr;     // plain: mac rounded outwards to FP32 (-1 / +inf where that is unsafe)
   RootBox *root = nullptr;    // device
   uint64_t *keys = nullptr;   // sorted keys (tree order before in-leaf sort)
   uint8_t *cpl = nullptr;     // per position: levels shared with the next key

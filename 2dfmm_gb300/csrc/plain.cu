@@ -137,6 +137,10 @@ __global__ void __launch_bounds__(kEvalWarps * 32) k_eval(EvalArgs a) {
   const int nt = a.nt;
   const double x = valid ? a.tx[i] : 0.0, y = valid ? a.ty[i] : 0.0;
   const double theta = a.theta;
+  // the target as FP32 pairs, for the opening pre-test (x - xh is exact)
+  const float xh = __double2float_rn(x), yh = __double2float_rn(y);
+  const float xl = __double2float_rn(x - (double)xh), yl = __double2float_rn(y - (double)yh);
+  const float sxy = __fadd_rn(fabsf(xh), fabsf(yh));
   double2 phi = make_double2(0.0, 0.0);
   double ud0 = 0.0, ud1 = 0.0;
   unsigned long long n_m2s = 0, n_pairs = 0;
@@ -272,15 +276,8 @@ __global__ void __launch_bounds__(kEvalWarps * 32) k_eval(EvalArgs a) {
       for (int q = 0; q < 4; q++) {
         const int cc = (&ch.x)[q];
         if (cc < 0) continue;
-        const double ccx = t.cx[cc], ccy = t.cy[cc];
-        const double2 mb = t.mac[cc];
         bool desc = false;
-        double dx = 0.0, dy = 0.0;
-        double d2 = 0.0;
         if (act) {
-          dx = __dsub_rn(x, ccx);
-          dy = __dsub_rn(y, ccy);
-          d2 = __dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy));
           // The reference's test is region > theta * sqrt(d2), each step
           // rounded.  Squared, region^2 > theta^2 d2, it needs no square
           // root: below the cell's bound mb.x (region^2 / (theta^2 (1 +
@@ -288,12 +285,41 @@ __global__ void __launch_bounds__(kEvalWarps * 32) k_eval(EvalArgs a) {
           // 2e-13) it surely accepts (the roundings of either side and of
           // the bounds are below 1e-15 relative); only a d2 between the two
           // takes the exact rounded path.
-          if (d2 < mb.x) {
+          //
+          // An FP64 instruction costs this GPU's SM sub-partition about 64
+          // issue cycles, an FP32 one 1, so d2 is first formed in FP32 from
+          // the hi/lo pairs: dxf = (xh - cxh) + (xl - cxl).  Its error is at
+          // most 2^-23 |dx| + 2^-46 (|x| + |cx|), and so
+          //   |d2f - d2| <= 3 2^-23 d2 + 2^-45 S (|dxf| + |dyf|) + (...)^2,
+          // S = |x| + |y| + |cx| + |cy|.  err below takes 2^-20 d2f and
+          // 2^-44 S, over twice that, so d2f + err < the FP32 lower bound
+          // (rounded down from mb.x) means d2 < mb.x, and d2f - err > the
+          // upper one (rounded up from mb.y) d2 > mb.y: the FP64 test would
+          // decide the same.  Anything else (and any infinity or NaN on the
+          // way, where a comparison fails) takes the FP64 test as before.
+          const float4 cf = t.cf32[cc];
+          const float2 mf = t.macf[cc];
+          const float dxf = __fadd_rn(__fsub_rn(xh, cf.x), __fsub_rn(xl, cf.y));
+          const float dyf = __fadd_rn(__fsub_rn(yh, cf.z), __fsub_rn(yl, cf.w));
+          const float d2f = __fmaf_rn(dxf, dxf, __fmul_rn(dyf, dyf));
+          const float ef = __fmul_rn(0x1p-44f, __fadd_rn(sxy, __fadd_rn(fabsf(cf.x), fabsf(cf.z))));
+          const float err = __fmaf_rn(0x1p-20f, d2f, __fmul_rn(ef, __fadd_rn(__fadd_rn(fabsf(dxf), fabsf(dyf)), ef)));
+          if (__fadd_ru(d2f, err) < mf.x) {
             desc = true;
-          } else if (d2 > mb.y) {
+          } else if (__fsub_rd(d2f, err) > mf.y && d2f <= 3.0e38f) {
             desc = false;
           } else {
-            desc = t.region[cc] > __dmul_rn(theta, __dsqrt_rn(d2));
+            const double2 mb = t.mac[cc];
+            const double dx = __dsub_rn(x, t.cx[cc]);
+            const double dy = __dsub_rn(y, t.cy[cc]);
+            const double d2 = __dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy));
+            if (d2 < mb.x) {
+              desc = true;
+            } else if (d2 > mb.y) {
+              desc = false;
+            } else {
+              desc = t.region[cc] > __dmul_rn(theta, __dsqrt_rn(d2));
+            }
           }
         }
         const unsigned dmask = __ballot_sync(0xffffffffu, desc);
@@ -346,12 +372,23 @@ __global__ void __launch_bounds__(kEvalWarps * 32) k_eval(EvalArgs a) {
 // covers the roundings of the reference's test and of the bounds.  With
 // theta <= 0 the reference's test opens every cell (region > 0 >= theta r):
 // both bounds are +inf.
+//
+// For the FP32 pre-test of k_eval: the centre as two FP32 pairs (hi = the
+// nearest float, lo = the rest, rounded) and the bounds rounded outwards to
+// FP32; a lower bound below 1e-30 becomes -1 and an upper one below 1e-30
+// +inf (no sure answer: the FP32 error bound does not cover subnormals).
 __global__ void k_mac_bounds(Tree t, double theta) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= t.ncell) return;
   const double r2 = t.region[c] * t.region[c], th2 = theta * theta;
-  t.mac[c] = theta > 0.0 ? make_double2(r2 / (th2 * (1.0 + 2e-13)), r2 / (th2 * (1.0 - 2e-13)))
-                         : make_double2(INFINITY, INFINITY);
+  const double2 mb = theta > 0.0 ? make_double2(r2 / (th2 * (1.0 + 2e-13)), r2 / (th2 * (1.0 - 2e-13)))
+                                 : make_double2(INFINITY, INFINITY);
+  t.mac[c] = mb;
+  const double cx = t.cx[c], cy = t.cy[c];
+  const float cxh = __double2float_rn(cx), cyh = __double2float_rn(cy);
+  t.cf32[c] = make_float4(cxh, __double2float_rn(cx - (double)cxh), cyh, __double2float_rn(cy - (double)cyh));
+  t.macf[c] = make_float2(mb.x >= 1e-30 ? __double2float_rd(mb.x) : -1.0f,
+                          mb.y >= 1e-30 ? __double2float_ru(mb.y) : INFINITY);
 }
 
 cudaError_t mac_bounds(Workspace &ws, const Tree &t, double theta, cudaStream_t s) {

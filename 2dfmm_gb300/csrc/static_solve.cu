@@ -43,7 +43,7 @@ constexpr size_t kStatusRegion = 4096;              // DevStatus
 // radii, 1/sigma^2, permutation, keys, cell bases, two level bytes: 3.8 MB
 // at 65,536 blobs), the scratch region about 17 B per blob plus the sort
 // counts and the level-12 centre table (1.3 MB); the cells get the rest
-// (about 28 MB: some 120,000 cells at 233 B per cell for nterms 11).  A
+// (about 28 MB: some 110,000 cells at 257 B per cell for nterms 11).  A
 // layout that leaves the cells less than half of the array is a build error,
 // caught on first use.
 static_assert(kStatusRegion >= sizeof(DevStatus), "status region too small");
