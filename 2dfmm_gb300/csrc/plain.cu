@@ -153,7 +153,7 @@ __global__ void __launch_bounds__(kEvalWarps * 32) k_eval(EvalArgs a) {
   // per lane per round, when a lane's queue could overflow and at the end.
   // A lane's M2S terms still reach phi in its own acceptance order, each
   // with the same operations (dx, dy, d2 formed again from the cell's
-  // centre, bit for bit), and the direct terms go to ud0/ud1 as before.
+  // centre, bit for bit); the direct terms are deferred too (below).
   // The queues are rings (head qh, count nq).  A flush when some lane's
   // queue could overflow evaluates only as many rounds as every lane can
   // fill, or as the fullest lane needs to make room for four entries, if
