@@ -90,3 +90,32 @@ def test_bad_input_rejected(lib):
     lib.make_tree(-1, None, None, None)
     assert P.last_error() == P.ERR_BAD_INPUT
     P.clear_params()
+
+
+def test_c_caller_compiles_and_links(lib, tmp_path):
+    """A C99 program (the reference's own language) includes the header with
+    strict warnings, links the library and gets the reference's behaviour for
+    biot_tree before any make_tree (NaN, with a status), without a GPU."""
+    import shutil
+    import subprocess
+
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        import pytest
+        pytest.skip("no C compiler")
+    src = tmp_path / "main.c"
+    src.write_text(
+        "#include <stdio.h>\n"
+        "#include \"tree2d.h\"\n"
+        "int main(void) {\n"
+        "  double u = 0.0, v = 0.0;\n"
+        "  biot_tree(0.5, 0.5, &u, &v);\n"
+        "  printf(\"%d %d %d\\n\", tree2d_last_error(), u != u, v != v);\n"
+        "  return 0;\n"
+        "}\n")
+    libdir = os.path.dirname(lib._name)
+    exe = tmp_path / "main"
+    subprocess.run([cc, "-std=c99", "-Wall", "-Wextra", "-pedantic", "-Werror", "-I", os.path.join(ROOT, "include"),
+                    str(src), "-L", libdir, "-ltree2d_gb300", "-Wl,-rpath," + libdir, "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split()
+    assert out == [str(pkg().ERR_NO_TREE), "1", "1"]
