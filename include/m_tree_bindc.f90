@@ -51,5 +51,12 @@ module m_tree_bindc
     integer(c_int) function tree2d_last_error() bind(c, name="tree2d_last_error")
       import :: c_int
     end function tree2d_last_error
+
+    ! Optional: load a network for the learned mode from its raw weights
+    ! file; path ends in a NUL, e.g. trim(dir)//"/learned_weights.t2dw"//c_null_char.
+    integer(c_int) function tree2d_learn_load(path) bind(c, name="tree2d_learn_load")
+      import :: c_int, c_char
+      character(kind=c_char), dimension(*), intent(in) :: path
+    end function tree2d_learn_load
   end interface
 end module m_tree_bindc
